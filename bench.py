@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""LJ atom-steps/s of the integer fixed-point MD step on GB300.
+
+Workload (one step = one MD step of the whole system): 3D LJ liquid NVE, N = 1,048,576 atoms on
+an FCC lattice at density 0.8442, Maxwell velocities at T = 0.72 (Threefry seed 1), cubic
+periodic box, cutoff 2.5, Verlet skin 0.3 with displacement-triggered rebuilds, dt = 0.005,
+integer fixed-point positions, f32 pair forces quantised to integer kicks. The state is
+generated on the device and stays resident; the timed region replays the engine's captured
+CUDA graphs (force + leapfrog every step, the list rebuild in a conditional node).
+
+`--impl reference` times md-ref's CPU engine (restated in C++, IntEngine3<f32>'s reference loop,
+all host threads) on the same workload.
+
+One JSON line on stdout (rank 0). Multi-GPU (torchrun): one independent replica per GPU, barrier
++ max over ranks (replicas only: the path has no exchange step).
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LJ atom-steps/s (plain vs batched/served, same GB300); p99 frame latency; FP64 err"
+UNIT = "atom-steps/s"
+
+N_ATOMS = 1 << 20
+RHO, T0, SEED, SKIN, RC, DT = 0.8442, 0.72, 1, 0.3, 2.5, 0.005
+
+
+def config_dict(extra=None):
+    d = {
+        "workload": "3D LJ liquid NVE, FCC N=1048576, rho 0.8442, T 0.72, rc 2.5, skin 0.3, dt 0.005 (configs[1], plain form)",
+        "n_atoms": N_ATOMS,
+        "density": RHO,
+        "temperature": T0,
+        "cutoff": RC,
+        "skin": SKIN,
+        "dt": DT,
+        "form": "plain (one system per launch sequence)",
+        "l2": "inputs larger than L2 (neighbour list ~0.33 GB read per step, state 48 MB)",
+    }
+    if extra:
+        d.update(extra)
+    return d
+
+
+def algorithmic_bytes_per_atom_step():
+    """B = 2 S + 4 n_list: state read + written (S = 24 B positions + 12 B velocities) and one
+    u32 index per listed neighbour, n_list = rho (4/3) pi (rc + skin)^3."""
+    s = 24 + 12
+    n_list = RHO * 4.0 / 3.0 * math.pi * (RC + SKIN) ** 3
+    return 2 * s + 4 * n_list, n_list
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per force launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "k_force_list_3d.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file,
+                stderr=subprocess.DEVNULL,
+            )
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        for line in open(self.file.name):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl"
+        try:
+            import torch
+
+            if not torch.cuda.is_available():
+                backend = "gloo"
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier_max(pg, value):
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def system3():
+    from micrographia_gb300 import Pair, System3, cube_for
+
+    return System3(cube_for(N_ATOMS, RHO), DT, Pair.lj(RC), [1.0])
+
+
+def cpu_baseline(seconds_budget=20.0, threads=None):
+    """md-ref's CPU engine (C++ restatement, IntEngine3<f32> reference loop, OpenMP over all host
+    threads) on the same workload; a bounded sample of steps."""
+    from oracle import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    sys3 = system3()
+    s0 = O.fcc_maxwell(sys3, N_ATOMS, T0, SEED, jitter=0.05)
+    e = O.IntEngine(sys3, s0, threads=threads)
+    e.step(1)  # warm-up
+    t0 = time.perf_counter()
+    done = 0
+    while done < 1 or (time.perf_counter() - t0 < seconds_budget and done < 20):
+        e.step(1)
+        done += 1
+    dt = time.perf_counter() - t0
+    return {
+        "value": N_ATOMS * done / dt,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{done} full steps of the 1,048,576-atom system after 1 warm-up step ({dt:.1f} s), IntEngine3<f32> reference loop",
+    }
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return 0
+    base = cpu_baseline(seconds_budget=min(60.0, 5.0 + 2.0 * args.steps))
+    line = {
+        "metric": METRIC,
+        "value": base["value"],
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": N_ATOMS / base["value"] * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+int64",
+        "data": "synthetic",
+        "impl": "reference",
+        "config": config_dict(),
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, world, rank, local, pg):
+    import numpy as np
+    import torch
+
+    from micrographia_gb300 import ForceMode, GpuEngine3, _abi
+    from micrographia_gb300.engine import make_init
+
+    torch.cuda.set_device(local)
+    sys3 = system3()
+    spec = make_init(_abi.INIT_FCC, N_ATOMS, T0, SEED, 0.05)
+    eng = GpuEngine3(sys3, None, ForceMode.verlet_with_skin(sys3, N_ATOMS, SKIN), init=spec, device=local)
+    stream = torch.cuda.ExternalStream(eng.stream())
+
+    # warm-up: captures the graphs and settles the lists
+    ke0, pe0 = eng.energy()
+    eng.step(args.warmup)
+    eng.wait()
+    e_warm = sum(eng.energy())
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = eng.launch_count()
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    eng.step(args.steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    eng.wait()
+    clk = clocks.stop()
+    launches = eng.launch_count() - l0
+    ms = barrier_max(pg, ms)
+    value = world * N_ATOMS * args.steps / (ms * 1e-3)
+    e_end = sum(eng.energy())
+    rebuilds, overflow = eng.read_list_stats()
+
+    # per-phase device times (CUDA events on the engine's stream) for the roofline
+    lib = _abi.lib()
+    import ctypes as C
+
+    f_ms, r_ms, nreb = C.c_double(), C.c_double(), C.c_uint32()
+    _abi.check(lib.gbmd_time_phases(eng._h, 200, C.byref(f_ms), C.byref(r_ms), C.byref(nreb)))
+    B, n_list = algorithmic_bytes_per_atom_step()
+    peaks, peak_kind = measured_peaks()
+    achieved = B * N_ATOMS / (f_ms.value * 1e-3) / 1e9
+    traffic = profile_traffic()
+
+    # end to end through the public API with host buffers: upload from pinned host memory,
+    # K steps, state read back to host memory
+    st = eng.read_state()
+    hp = torch.empty(st.pos.shape, dtype=torch.int64, pin_memory=True).numpy()
+    hv = torch.empty(st.vel.shape, dtype=torch.int32, pin_memory=True).numpy()
+    hs = torch.empty(st.species.shape, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    hp[:] = st.pos
+    hv[:] = st.vel
+    hs[:] = st.species
+    from micrographia_gb300 import State3
+
+    host_state = State3(hp, hv, hs)
+    if pg is not None:
+        pg.barrier()
+    t0 = time.perf_counter()
+    eng.upload(host_state)
+    eng.step(args.steps)
+    out = eng.read_state()
+    t_e2e = barrier_max(pg, time.perf_counter() - t0)
+    h2d = hp.nbytes + hv.nbytes + hs.nbytes
+    d2h = out.pos.nbytes + out.vel.nbytes + out.species.nbytes
+    e2e = {
+        "value": world * N_ATOMS * args.steps / t_e2e,
+        "unit": UNIT,
+        "h2d_bytes_per_step": h2d / args.steps,
+        "d2h_bytes_per_step": d2h / args.steps,
+        "what": "gbmd_upload (pinned host state) + gbmd_step(K) + gbmd_read_state to host, per K steps",
+    }
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+int64",
+        "data": "synthetic",
+        "config": config_dict({"parallelism": f"replicas{world}" if world > 1 else "single"}),
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "k_force_list<3> (LJ force + leapfrog + trigger)",
+            "achieved": achieved,
+            "peak": peaks.get("hbm_gbs", 6800.0),
+            "peak_kind": peak_kind,
+            "unit": "GB/s",
+            "frac": achieved / peaks.get("hbm_gbs", 6800.0),
+            "traffic": traffic,
+            "algorithmic_bytes_per_atom_step": B,
+            "n_list": n_list,
+            "force_ms": f_ms.value,
+        },
+        "phases": {"force_ms": f_ms.value, "rebuild_ms": r_ms.value, "rebuilds_in_200": nreb.value, "rebuilds_timed_run": rebuilds},
+        "energy": {"e0_per_atom": (ke0 + pe0) / N_ATOMS, "drift_per_atom_per_step": (e_end - e_warm) / N_ATOMS / args.steps},
+        "overflow": overflow,
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=64)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank, pg)
+    else:
+        from micrographia_gb300 import build
+
+        build.build()
+        rc = run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,238 @@
+/*
+ * gbmd.h — C ABI of the GB300-native integer fixed-point Lennard-Jones MD engine.
+ *
+ * This is the drop-in boundary for the engine interface that micrographia's `scenarios` crate,
+ * its pages and its tests drive: the method set shared by `md::GpuEngine`
+ * (crates/md/src/engine.rs:598-1098), `md::GpuEngine3` (crates/md/src/engine3.rs:334-648) and
+ * their CPU twins `md_ref::IntEngine<F>` (crates/md-ref/src/int_engine.rs:52-447) and
+ * `md_ref::IntEngine3<F>` (crates/md-ref/src/int_engine3.rs:28-240).
+ *
+ * Layouts are md-core's, so a Rust `extern "C"` crate passes `State` vectors without conversion:
+ *   - positions: int64 in units of 2^-32 sigma, interleaved per particle ([i64; 2] or [i64; 3]),
+ *     as `md_core::State::pos` / `State3::pos` (crates/md-core/src/system.rs:447-453);
+ *   - velocities: int32 displacement per step (v_{n-1/2} dt 2^32), interleaved as `State::vel`;
+ *   - species: uint32 per particle.
+ * All arrays handed across the ABI are in particle-id order (the order of the State given at
+ * creation); the engine's own storage order is private, as in the reference (ids buffer,
+ * crates/md/src/engine.rs:383-389).
+ *
+ * Conventions (the reference panics or returns `GpuError(String)`, crates/gpu-prims/src/context.rs:15-24):
+ *   - every call returns an int status: GBMD_OK (0) or a negative GBMD_E_* code;
+ *     gbmd_last_error() returns a thread-local message describing the last failure;
+ *   - the caller owns host arrays, the engine owns device memory;
+ *   - an engine is used from one host thread at a time; work is stream-ordered and asynchronous
+ *     (gbmd_step returns before the GPU finishes; read calls wait);
+ *   - no callbacks.
+ */
+#ifndef GBMD_H
+#define GBMD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBMD_MAX_SPECIES 4 /* md_core::system::MAX_SPECIES (crates/md-core/src/system.rs:7) */
+
+/* Status codes. */
+#define GBMD_OK 0
+#define GBMD_E_INVALID (-1)     /* invalid configuration or argument (the reference's assert!s) */
+#define GBMD_E_NOMEM (-2)       /* device allocation failed */
+#define GBMD_E_BUDGET (-3)      /* over the engine's or server's HBM budget */
+#define GBMD_E_OVERFLOW (-4)    /* a neighbour list overflowed its capacity */
+#define GBMD_E_NONFINITE (-5)   /* a non-finite energy or force was met */
+#define GBMD_E_TIMEOUT (-6)     /* a bounded device-side wait gave up */
+#define GBMD_E_CUDA (-7)        /* a CUDA runtime error */
+#define GBMD_E_UNSUPPORTED (-8) /* a System feature this engine does not implement */
+#define GBMD_E_NOTFOUND (-9)    /* unknown request or slot */
+
+/* Force modes: md::ForceMode (crates/md/src/engine.rs:102-142). */
+#define GBMD_MODE_AUTO 0   /* cell list below 24 000 particles in 2D, Verlet lists otherwise */
+#define GBMD_MODE_CELLS 1  /* scan the 3x3(x3) neighbouring cells every step */
+#define GBMD_MODE_VERLET 2 /* Verlet lists with a skin and a displacement-triggered rebuild */
+
+/* Pair arithmetic: md::Arith (crates/md/src/engine.rs:89-100). */
+#define GBMD_ARITH_F32 0 /* f32 pair forces, each pair's kick rounded to an integer */
+#define GBMD_ARITH_INT 1 /* all-integer table forces (md_core::table::IntTables) */
+
+/* md_core::Pair (crates/md-core/src/pair.rs:3-8): truncated and shifted LJ. */
+typedef struct gbmd_pair {
+    double eps;
+    double sigma;
+    double rc;
+} gbmd_pair;
+
+/*
+ * The System fields the LJ path needs: md_core::System (crates/md-core/src/system.rs:26-64) and
+ * md_core::three::System3 (crates/md-core/src/three.rs:13-31). `pairs` is row-major
+ * [a * nspecies + b] like `System::pairs`. Walls, baths, compartments, membranes, pistons and
+ * bonds are outside this engine: `periodic` must have every axis set.
+ */
+typedef struct gbmd_system {
+    uint32_t dim;      /* 2 or 3 */
+    uint32_t nspecies; /* 1..GBMD_MAX_SPECIES */
+    int64_t box_len[3];/* position units; box_len[2] unused in 2D */
+    double dt;
+    double masses[GBMD_MAX_SPECIES];
+    gbmd_pair pairs[GBMD_MAX_SPECIES * GBMD_MAX_SPECIES];
+    double gravity[3]; /* sigma/tau^2 */
+    uint64_t seed;
+    uint32_t periodic; /* bit a set if axis a is periodic */
+    uint32_t pinned;   /* bit s set if species s is pinned */
+} gbmd_system;
+
+/* Engine options: ForceMode + Arith + the engine's own tuning knobs. Zero-initialised is valid. */
+typedef struct gbmd_options {
+    int32_t mode;          /* GBMD_MODE_* */
+    int32_t arith;         /* GBMD_ARITH_* */
+    double skin;           /* Verlet skin in sigma; <= 0 selects 0.4 (ForceMode::verlet_for) */
+    uint32_t cap;          /* list capacity per particle; 0 sizes it like verlet_with_skin */
+    uint32_t block_steps;  /* steps per captured CUDA-graph block; 0 selects 64 */
+    int32_t device;        /* CUDA device ordinal */
+    uint32_t threads;      /* threads per block for the force kernel; 0 selects the tuned value */
+    uint32_t rescale_every;/* velocity-rescale thermostat period in steps (0: off) */
+    uint32_t _reserved;
+    double rescale_t;      /* thermostat target kT */
+} gbmd_options;
+
+typedef struct gbmd_engine gbmd_engine;
+
+/* Observables of one frame, FP64 reductions on the device (new in this engine: the reference
+ * has only f32 kinetic totals, crates/md/shaders/observe.wgsl:48-56). */
+typedef struct gbmd_frame {
+    uint64_t step;        /* net steps taken */
+    double kinetic;       /* on-step kinetic energy (IntEngine::energy, int_engine.rs:433-446) */
+    double potential;     /* pair potential energy */
+    double virial;        /* sum over pairs of r . F = sum fr r^2 (mc/src/gibbs.rs:58-66) */
+    double temperature;   /* 2 KE / (dim (N - 1)) */
+    double pressure;      /* rho T + virial / (dim V) */
+    double volume;
+    uint32_t n;
+    uint32_t dim;
+} gbmd_frame;
+
+/* ---- Engine lifecycle: GpuEngine::{new, with_mode, with_options} ---- */
+
+/* Create an engine from a system and a state (copied to the device). `opts` may be NULL. */
+int gbmd_create(const gbmd_system* sys, const int64_t* pos, const int32_t* vel,
+                const uint32_t* species, uint32_t n, const gbmd_options* opts, gbmd_engine** out);
+int gbmd_destroy(gbmd_engine* e);
+
+/* ---- Stepping: GpuEngine::step (engine.rs:852-873), reverse (engine.rs:881) ---- */
+
+/* Enqueue `steps` leapfrog steps; returns without waiting for the GPU. */
+int gbmd_step(gbmd_engine* e, uint64_t steps);
+/* Wait for all enqueued work; reports a deferred device error (list overflow, CUDA). */
+int gbmd_sync(gbmd_engine* e);
+/* Time reversal v <- -(v + kick(x) + g) (IntEngine::reverse, int_engine.rs:396-413). */
+int gbmd_reverse(gbmd_engine* e);
+
+/* ---- State I/O in id order: read_state (engine.rs:1080), upload (engine.rs:1067) ---- */
+
+int gbmd_read_state(gbmd_engine* e, int64_t* pos, int32_t* vel, uint32_t* species);
+int gbmd_upload(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const uint32_t* species);
+/* Integer kicks at the current positions and the pair potential energy (engine.rs:1089-1097). */
+int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential);
+/* Flip one bit of one coordinate of particle `id` (engine.rs:964, State::flip_bit). */
+int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit);
+
+/* ---- Observables: IntEngine::energy (int_engine.rs:433-446) and the new instruments ---- */
+
+int gbmd_energy(gbmd_engine* e, double* kinetic, double* potential);
+/* One frame of instruments. `rdf` (may be NULL) receives `rdf_bins` integer pair counts of
+ * unordered pairs with floor(r * rdf_bins / rdf_rmax) = k; `profile` (may be NULL) receives
+ * `profile_bins` particle counts along `profile_axis`. */
+int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint32_t rdf_bins,
+                 double rdf_rmax, uint64_t* profile, uint32_t profile_bins, uint32_t profile_axis);
+
+/* ---- Diagnostics ---- */
+
+/* Verlet-list rebuilds so far and whether any list overflowed (Buffers::read_list_stats). */
+int gbmd_list_stats(gbmd_engine* e, uint32_t* rebuilds, int32_t* overflow);
+/* FNV-1a hash of the id-ordered state (State::hash, system.rs:460-477; three.rs:280-297). */
+int gbmd_state_hash(gbmd_engine* e, uint64_t* hash);
+/* Net steps (GpuEngine::steps) and the clock (steps in either direction). */
+int gbmd_counters(gbmd_engine* e, int64_t* steps, uint32_t* clock);
+/* The CUDA stream the engine launches on (a cudaStream_t), for event timing by the caller. */
+int gbmd_stream(gbmd_engine* e, void** stream);
+/* Kernels launched by this engine so far (every launch, graph nodes included). */
+int gbmd_launch_count(gbmd_engine* e, uint64_t* launches);
+
+/* Per-phase device timing (the reference's PassTimer, crates/bench/src/main.rs:178-198): run
+ * `steps` steps as individual launches with CUDA events around each phase on the engine's
+ * stream; returns the mean milliseconds of one force launch and of one list rebuild (all its
+ * kernels), and how many rebuilds ran. The state advances by `steps` steps. */
+int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* rebuild_ms, uint32_t* rebuilds);
+
+/* ---- Introspection of the cell binning and the Verlet list (parity tests) ---- */
+
+/* Cell keys, cell starts and the stable sort permutation of the current storage order, exactly
+ * as md_ref::CellList::build (crates/md-ref/src/cells.rs:10-32) computes them for `cells` cells
+ * per axis (cell_of in f64, cells.rs:53-55; row-major keys). keys[n], start[ncell+1], items[n];
+ * `order` (n ids) receives the id of each storage slot the binning saw. */
+int gbmd_debug_bin(gbmd_engine* e, const uint32_t* cells, uint32_t* keys, uint32_t* start,
+                   uint32_t* items, uint32_t* order);
+/* The Verlet list as built now: for each id, its neighbour ids (any order), `counts[id]` of
+ * them, packed in id order into `nbr` (capacity `nbr_cap` entries). */
+int gbmd_debug_list(gbmd_engine* e, uint32_t* counts, uint32_t* nbr, uint64_t nbr_cap);
+
+/* ---- Seeded initial conditions on the device (md_core::init, crates/md-core/src/init.rs) ---- */
+
+/* Init recipes. */
+#define GBMD_INIT_FLUID 0       /* init::fluid: square-ish lattice, jitter 0.1, Maxwell (2D) */
+#define GBMD_INIT_TRIANGULAR 1  /* triangular lattice + Maxwell (2D; new, see init spec) */
+#define GBMD_INIT_FCC 2         /* three::fcc + three::maxwell (3D) */
+#define GBMD_INIT_SLAB 3        /* liquid slab (triangular) + jittered-lattice vapour (2D) */
+
+typedef struct gbmd_init {
+    uint32_t recipe;    /* GBMD_INIT_* */
+    uint32_t n;
+    double t;           /* kT of the Maxwell velocities */
+    uint64_t seed;
+    double jitter;      /* lattice jitter in sigma */
+    double rho_liquid;  /* slab: liquid density */
+    double rho_vapour;  /* slab: vapour density */
+    double slab_frac;   /* slab: fraction of the long (x) axis the liquid fills */
+} gbmd_init;
+
+/* Generate the id-ordered initial state on the device (bit-identical to md_core::init) and copy
+ * it to the host arrays (any of which may be NULL). */
+int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, int64_t* pos, int32_t* vel,
+                    uint32_t* species);
+/* Create an engine whose state is generated on the device by `spec` (no host round trip). */
+int gbmd_create_seeded(const gbmd_system* sys, const gbmd_init* spec, const gbmd_options* opts,
+                       gbmd_engine** out);
+
+/* ---- Batched replicas: many independent periodic systems in one persistent launch ---- */
+
+typedef struct gbmd_batch gbmd_batch;
+
+/* `systems[k]` with its own initial state, concatenated in `pos/vel/species` at `offsets[k]`
+ * (offsets[count] = total particles). */
+int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t* offsets,
+                      const int64_t* pos, const int32_t* vel, const uint32_t* species,
+                      const gbmd_options* opts, gbmd_batch** out);
+int gbmd_batch_step(gbmd_batch* b, uint64_t steps);
+int gbmd_batch_sync(gbmd_batch* b);
+/* The id-ordered state of system k. */
+int gbmd_batch_read_system(gbmd_batch* b, uint32_t k, int64_t* pos, int32_t* vel, uint32_t* species);
+int gbmd_batch_stream(gbmd_batch* b, void** stream);
+int gbmd_batch_destroy(gbmd_batch* b);
+
+/* FNV-1a hash of an id-ordered state held on the host: State::hash (system.rs:460-477) for
+ * dim 2, State3::hash (three.rs:281-297) for dim 3. */
+uint64_t gbmd_hash_state(uint32_t dim, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint32_t n);
+
+/* ---- Thread-local error message ---- */
+
+const char* gbmd_last_error(void);
+/* Library version string. */
+const char* gbmd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBMD_H */

@@ -1,0 +1,50 @@
+"""micrographia_gb300 — a GB300-native integer fixed-point Lennard-Jones MD engine.
+
+The Python face of the engine mirrors the interface micrographia's scenarios and tests drive:
+md-core's `Pair`, `System`, `State`, `System3`, `State3` and `init` helpers
+(crates/md-core/src/{pair,system,init,three}.rs), and the engines `GpuEngine` / `GpuEngine3`
+(crates/md/src/engine.rs:598-1098, engine3.rs:334-648) with `step`, `reverse`, `kicks`,
+`read_state`, `upload`, `energy`, `flip_bit`, `read_list_stats` and `ForceMode`.
+
+All compute runs in the CUDA library libgbmd.so through its C ABI (include/gbmd.h); importing
+works without a GPU, and every engine call fails loudly when the library or the GPU is missing.
+"""
+
+from .core import (
+    DT,
+    ONE,
+    ForceMode,
+    Pair,
+    State,
+    State3,
+    System,
+    System3,
+    box_for,
+    cube_for,
+    fcc_cells,
+    to_f64,
+    to_fixed,
+)
+from .engine import BatchEngine, GpuEngine, GpuEngine3, init_state
+from . import init
+
+__all__ = [
+    "DT",
+    "ONE",
+    "ForceMode",
+    "Pair",
+    "State",
+    "State3",
+    "System",
+    "System3",
+    "GpuEngine",
+    "GpuEngine3",
+    "BatchEngine",
+    "box_for",
+    "cube_for",
+    "fcc_cells",
+    "to_f64",
+    "to_fixed",
+    "init",
+    "init_state",
+]

@@ -1,0 +1,197 @@
+"""ctypes mirror of include/gbmd.h and the loader of the engine library.
+
+The engine is the C-ABI shared library micrographia_gb300/_build/libgbmd.so, built in-tree by
+micrographia_gb300/build.py. Loading fails loudly when it is missing: there is no CPU fallback.
+"""
+
+import ctypes as C
+import os
+
+MAX_SPECIES = 4
+
+OK = 0
+E_INVALID = -1
+E_NOMEM = -2
+E_BUDGET = -3
+E_OVERFLOW = -4
+E_NONFINITE = -5
+E_TIMEOUT = -6
+E_CUDA = -7
+E_UNSUPPORTED = -8
+E_NOTFOUND = -9
+
+MODE_AUTO = 0
+MODE_CELLS = 1
+MODE_VERLET = 2
+ARITH_F32 = 0
+ARITH_INT = 1
+
+INIT_FLUID = 0
+INIT_TRIANGULAR = 1
+INIT_FCC = 2
+INIT_SLAB = 3
+
+
+class gbmd_pair(C.Structure):
+    _fields_ = [("eps", C.c_double), ("sigma", C.c_double), ("rc", C.c_double)]
+
+
+class gbmd_system(C.Structure):
+    _fields_ = [
+        ("dim", C.c_uint32),
+        ("nspecies", C.c_uint32),
+        ("box_len", C.c_int64 * 3),
+        ("dt", C.c_double),
+        ("masses", C.c_double * MAX_SPECIES),
+        ("pairs", gbmd_pair * (MAX_SPECIES * MAX_SPECIES)),
+        ("gravity", C.c_double * 3),
+        ("seed", C.c_uint64),
+        ("periodic", C.c_uint32),
+        ("pinned", C.c_uint32),
+    ]
+
+
+class gbmd_options(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32),
+        ("arith", C.c_int32),
+        ("skin", C.c_double),
+        ("cap", C.c_uint32),
+        ("block_steps", C.c_uint32),
+        ("device", C.c_int32),
+        ("threads", C.c_uint32),
+        ("rescale_every", C.c_uint32),
+        ("_reserved", C.c_uint32),
+        ("rescale_t", C.c_double),
+    ]
+
+
+class gbmd_frame(C.Structure):
+    _fields_ = [
+        ("step", C.c_uint64),
+        ("kinetic", C.c_double),
+        ("potential", C.c_double),
+        ("virial", C.c_double),
+        ("temperature", C.c_double),
+        ("pressure", C.c_double),
+        ("volume", C.c_double),
+        ("n", C.c_uint32),
+        ("dim", C.c_uint32),
+    ]
+
+
+class gbmd_init(C.Structure):
+    _fields_ = [
+        ("recipe", C.c_uint32),
+        ("n", C.c_uint32),
+        ("t", C.c_double),
+        ("seed", C.c_uint64),
+        ("jitter", C.c_double),
+        ("rho_liquid", C.c_double),
+        ("rho_vapour", C.c_double),
+        ("slab_frac", C.c_double),
+    ]
+
+
+class gbmd_serve_request(C.Structure):
+    _fields_ = [
+        ("sys", gbmd_system),
+        ("init", gbmd_init),
+        ("steps", C.c_uint64),
+        ("frame_every", C.c_uint32),
+        ("rdf_bins", C.c_uint32),
+        ("rdf_rmax", C.c_double),
+        ("skin", C.c_double),
+    ]
+
+
+class gbmd_serve_frame(C.Structure):
+    _fields_ = [
+        ("request", C.c_uint64),
+        ("frame", gbmd_frame),
+        ("ready_ns", C.c_uint64),
+        ("index", C.c_uint32),
+        ("last", C.c_uint32),
+    ]
+
+
+P = C.POINTER
+VP = C.c_void_p
+_I64P = P(C.c_int64)
+_I32P = P(C.c_int32)
+_U32P = P(C.c_uint32)
+_U64P = P(C.c_uint64)
+_DP = P(C.c_double)
+
+# (name, restype, argtypes): every entry point declared in include/gbmd.h.
+SIGNATURES = [
+    ("gbmd_create", C.c_int, [P(gbmd_system), _I64P, _I32P, _U32P, C.c_uint32, P(gbmd_options), P(VP)]),
+    ("gbmd_destroy", C.c_int, [VP]),
+    ("gbmd_step", C.c_int, [VP, C.c_uint64]),
+    ("gbmd_sync", C.c_int, [VP]),
+    ("gbmd_reverse", C.c_int, [VP]),
+    ("gbmd_read_state", C.c_int, [VP, _I64P, _I32P, _U32P]),
+    ("gbmd_upload", C.c_int, [VP, _I64P, _I32P, _U32P]),
+    ("gbmd_kicks", C.c_int, [VP, _I32P, _DP]),
+    ("gbmd_flip_bit", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32]),
+    ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
+    ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),
+    ("gbmd_list_stats", C.c_int, [VP, _U32P, _I32P]),
+    ("gbmd_state_hash", C.c_int, [VP, _U64P]),
+    ("gbmd_counters", C.c_int, [VP, _I64P, _U32P]),
+    ("gbmd_stream", C.c_int, [VP, P(VP)]),
+    ("gbmd_launch_count", C.c_int, [VP, _U64P]),
+    ("gbmd_time_phases", C.c_int, [VP, C.c_uint32, _DP, _DP, _U32P]),
+    ("gbmd_debug_bin", C.c_int, [VP, _U32P, _U32P, _U32P, _U32P, _U32P]),
+    ("gbmd_debug_list", C.c_int, [VP, _U32P, _U32P, C.c_uint64]),
+    ("gbmd_init_state", C.c_int, [P(gbmd_system), P(gbmd_init), _I64P, _I32P, _U32P]),
+    ("gbmd_create_seeded", C.c_int, [P(gbmd_system), P(gbmd_init), P(gbmd_options), P(VP)]),
+    ("gbmd_batch_create", C.c_int, [P(gbmd_system), C.c_uint32, _U32P, _I64P, _I32P, _U32P, P(gbmd_options), P(VP)]),
+    ("gbmd_batch_step", C.c_int, [VP, C.c_uint64]),
+    ("gbmd_batch_sync", C.c_int, [VP]),
+    ("gbmd_batch_read_system", C.c_int, [VP, C.c_uint32, _I64P, _I32P, _U32P]),
+    ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
+    ("gbmd_batch_destroy", C.c_int, [VP]),
+    ("gbmd_hash_state", C.c_uint64, [C.c_uint32, _I64P, _I32P, _U32P, C.c_uint32]),
+    ("gbmd_last_error", C.c_char_p, []),
+    ("gbmd_version", C.c_char_p, []),
+]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgbmd.so")
+HEADER_PATH = os.path.join(HERE, "..", "include", "gbmd.h")
+
+_lib = None
+
+
+class GbmdError(RuntimeError):
+    """A failed engine call: the status code and the library's message."""
+
+    def __init__(self, code, message):
+        super().__init__(f"gbmd error {code}: {message}")
+        self.code = code
+
+
+def lib():
+    """Load libgbmd.so (once). Raises if the CUDA extension has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"the CUDA engine library {LIB_PATH} is missing: run micrographia_gb300.build.build() "
+                "(there is no CPU fallback)"
+            )
+        l = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(code):
+    if code != OK:
+        msg = lib().gbmd_last_error()
+        raise GbmdError(code, msg.decode() if msg else "")
+    return code

@@ -1,0 +1,344 @@
+"""Host-side mirror of md-core's data types (crates/md-core/src): fixed point, Pair, System,
+State, System3, State3, ForceMode, and the box helpers of init.rs / three.rs.
+
+These are plain data and exact integer/f64 host arithmetic; nothing here computes the dynamics.
+"""
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _abi
+
+ONE = 1 << 32  # fixed.rs:11
+UNIT = 1.0 / ONE
+DT = 0.005  # init.rs:165
+SEP_LIMIT = 8 * ONE
+
+
+def rust_round(x: float) -> float:
+    """f64::round: half away from zero."""
+    t = math.trunc(x)
+    if abs(x - t) >= 0.5:
+        t += math.copysign(1.0, x)
+    return t
+
+
+def to_fixed(x: float) -> int:
+    """fixed::to_fixed (fixed.rs:21-23)."""
+    return int(rust_round(x * 4294967296.0))
+
+
+def to_f64(x: int) -> float:
+    """fixed::to_f64 (fixed.rs:25-27)."""
+    return float(x) * UNIT
+
+
+def _powi(x: float, n: int) -> float:
+    # Rust's f64::powi for a constant exponent: binary powering (x^6 = x^2 * (x^2)^2)
+    res, have, sq = 1.0, False, x
+    while n:
+        if n & 1:
+            res = res * sq if have else sq
+            have = True
+        n >>= 1
+        if n:
+            sq = sq * sq
+    return res
+
+
+class Pair:
+    """md_core::Pair (pair.rs:3-57): truncated and shifted LJ."""
+
+    __slots__ = ("eps", "sigma", "rc")
+
+    def __init__(self, eps=1.0, sigma=1.0, rc=2.5):
+        self.eps, self.sigma, self.rc = float(eps), float(sigma), float(rc)
+
+    @staticmethod
+    def lj(rc):
+        return Pair(1.0, 1.0, rc)
+
+    @staticmethod
+    def wca():
+        return Pair(1.0, 1.0, 2.0 ** (1.0 / 6.0))
+
+    @staticmethod
+    def none():
+        return Pair(0.0, 1.0, 0.0)
+
+    def shift(self):
+        if self.eps == 0.0 or self.rc == 0.0:
+            return 0.0
+        s6 = _powi(self.sigma / self.rc, 6)
+        return 4.0 * self.eps * s6 * (s6 - 1.0)
+
+    def energy(self, r2):
+        if r2 >= self.rc * self.rc:
+            return 0.0
+        s6 = _powi(self.sigma * self.sigma / r2, 3)
+        return 4.0 * self.eps * s6 * (s6 - 1.0) - self.shift()
+
+    def f_over_r(self, r2):
+        if r2 >= self.rc * self.rc:
+            return 0.0
+        s6 = _powi(self.sigma * self.sigma / r2, 3)
+        return 24.0 * self.eps * s6 * (2.0 * s6 - 1.0) / r2
+
+    def __eq__(self, o):
+        return isinstance(o, Pair) and (self.eps, self.sigma, self.rc) == (o.eps, o.sigma, o.rc)
+
+    def __repr__(self):
+        return f"Pair(eps={self.eps}, sigma={self.sigma}, rc={self.rc})"
+
+
+class _SystemBase:
+    DIM = 2
+
+    def __init__(self, box_len, dt, pair, masses):
+        masses = [float(m) for m in masses]
+        if not (1 <= len(masses) <= _abi.MAX_SPECIES):
+            raise ValueError("1 to 4 species")
+        if pair.rc >= 7.9:
+            raise ValueError("cutoff must be below 8 σ")
+        self.box_len = [int(b) for b in box_len]
+        self.dt = float(dt)
+        self.masses = masses
+        ns = len(masses)
+        self.pairs = [Pair(pair.eps, pair.sigma, pair.rc) for _ in range(ns * ns)]
+        self.gravity = [0.0] * self.DIM
+        self.seed = 1
+        self.pinned = 0
+
+    def species(self):
+        return len(self.masses)
+
+    def with_pair(self, a, b, pair):
+        """System::with_pair (system.rs:201-207): both orders."""
+        if pair.rc >= 7.9:
+            raise ValueError("cutoff must be below 8 σ")
+        ns = self.species()
+        self.pairs[a * ns + b] = pair
+        self.pairs[b * ns + a] = pair
+        return self
+
+    def with_gravity(self, g):
+        self.gravity = [float(x) for x in g]
+        return self
+
+    def with_seed(self, seed):
+        self.seed = int(seed)
+        return self
+
+    def with_pinned(self, s):
+        self.pinned |= 1 << s
+        return self
+
+    def pair(self, a, b):
+        return self.pairs[a * self.species() + b]
+
+    def rc_max(self):
+        return max(p.rc for p in self.pairs)
+
+    def box_f64(self):
+        return [to_f64(b) for b in self.box_len]
+
+    def volume(self):
+        v = 1.0
+        for b in self.box_f64():
+            v *= b
+        return v
+
+    area = volume
+
+    def kick_coeff(self, s):
+        if (self.pinned >> s) & 1:
+            return 0.0
+        return self.dt * self.dt / self.masses[s] * 4294967296.0
+
+    def velocity(self, v):
+        return float(v) * UNIT / self.dt
+
+    def to_step_displacement(self, v):
+        return int(rust_round(v * self.dt * 4294967296.0))
+
+    def cells_for(self, r):
+        """System::cells_for (system.rs:438-444 / three.rs:151-157)."""
+        b = self.box_f64()
+        margin = 1e-3 + 1e-6 * max(b)
+        c = [int(math.floor(l / (r + margin))) for l in b]
+        if min(c) < 3:
+            raise ValueError(f"box too small for radius {r}: {c} cells")
+        return c
+
+    def to_c(self) -> _abi.gbmd_system:
+        s = _abi.gbmd_system()
+        s.dim = self.DIM
+        s.nspecies = self.species()
+        for a in range(self.DIM):
+            s.box_len[a] = self.box_len[a]
+        s.dt = self.dt
+        for k, m in enumerate(self.masses):
+            s.masses[k] = m
+        for k, p in enumerate(self.pairs):
+            s.pairs[k].eps, s.pairs[k].sigma, s.pairs[k].rc = p.eps, p.sigma, p.rc
+        for a in range(self.DIM):
+            s.gravity[a] = self.gravity[a]
+        s.seed = self.seed
+        s.periodic = (1 << self.DIM) - 1
+        s.pinned = self.pinned
+        return s
+
+
+class System(_SystemBase):
+    """md_core::System (system.rs:26-64), periodic LJ subset."""
+
+    DIM = 2
+
+
+class System3(_SystemBase):
+    """md_core::three::System3 (three.rs:13-31), periodic LJ subset."""
+
+    DIM = 3
+
+
+class _StateBase:
+    DIM = 2
+
+    def __init__(self, pos, vel, species):
+        self.pos = np.ascontiguousarray(pos, dtype=np.int64).reshape(-1, self.DIM)
+        self.vel = np.ascontiguousarray(vel, dtype=np.int32).reshape(-1, self.DIM)
+        self.species = np.ascontiguousarray(species, dtype=np.uint32).reshape(-1)
+        if not (len(self.pos) == len(self.vel) == len(self.species)):
+            raise ValueError("pos, vel and species must have the same length")
+
+    def n(self):
+        return len(self.species)
+
+    def copy(self):
+        return type(self)(self.pos.copy(), self.vel.copy(), self.species.copy())
+
+    def hash(self):
+        """FNV-1a over every bit, in storage order (system.rs:460-477 / three.rs:281-297)."""
+        P = C.POINTER
+        return int(
+            _abi.lib().gbmd_hash_state(
+                self.DIM,
+                self.pos.ctypes.data_as(P(C.c_int64)),
+                self.vel.ctypes.data_as(P(C.c_int32)),
+                self.species.ctypes.data_as(P(C.c_uint32)),
+                self.n(),
+            )
+        )
+
+    def permuted(self, perm):
+        """Particle perm[k] of self becomes particle k (system.rs:480-486)."""
+        perm = np.asarray(perm)
+        return type(self)(self.pos[perm], self.vel[perm], self.species[perm])
+
+    def unpermuted(self, perm):
+        perm = np.asarray(perm)
+        out = self.copy()
+        out.pos[perm] = self.pos
+        out.vel[perm] = self.vel
+        out.species[perm] = self.species
+        return out
+
+    def velocity_sum(self):
+        return [int(x) for x in self.vel.astype(np.int64).sum(axis=0)]
+
+    def flip_bit(self, particle, axis, bit):
+        self.pos[particle, axis] ^= np.int64(1) << np.int64(bit)
+
+    def position_difference(self, other, sys):
+        """Particles whose positions differ, and the largest difference in σ (system.rs:523-536)."""
+        differ = np.any(self.pos != other.pos, axis=1)
+        mx = 0.0
+        for a in range(self.DIM):
+            l = sys.box_len[a]
+            d = other.pos[:, a] - self.pos[:, a]
+            half = l // 2
+            d = np.where(d >= half, d - l, np.where(d < -half, d + l, d))
+            if differ.any():
+                mx = max(mx, float(np.abs(d[differ]).max()) * UNIT)
+        return int(differ.sum()), mx
+
+    def __eq__(self, o):
+        return (
+            type(self) is type(o)
+            and np.array_equal(self.pos, o.pos)
+            and np.array_equal(self.vel, o.vel)
+            and np.array_equal(self.species, o.species)
+        )
+
+
+class State(_StateBase):
+    """md_core::State (system.rs:447-537)."""
+
+    DIM = 2
+
+
+class State3(_StateBase):
+    """md_core::three::State3 (three.rs:267-309)."""
+
+    DIM = 3
+
+
+class ForceMode:
+    """md::ForceMode (engine.rs:102-142): CellList or Verlet { skin, cap }."""
+
+    VERLET_MIN_N = 24_000
+
+    def __init__(self, kind, skin=0.0, cap=0):
+        self.kind, self.skin, self.cap = kind, float(skin), int(cap)
+
+    @staticmethod
+    def cell_list():
+        return ForceMode("cells")
+
+    @staticmethod
+    def verlet_with_skin(sys, n, skin, cap=0):
+        """cap 0 sizes the list like verlet_with_skin / verlet3_with_skin, without the
+        128 MiB single-binding clamp."""
+        return ForceMode("verlet", skin, cap)
+
+    @staticmethod
+    def verlet_for(sys, n):
+        return ForceMode.verlet_with_skin(sys, n, 0.4)
+
+    @staticmethod
+    def auto(sys, n):
+        if sys.DIM == 2 and n < ForceMode.VERLET_MIN_N:
+            return ForceMode.cell_list()
+        return ForceMode.verlet_for(sys, n)
+
+    def __repr__(self):
+        return f"ForceMode({self.kind}, skin={self.skin}, cap={self.cap})"
+
+
+def box_for(n, density, aspect=1.0):
+    """init::box_for (init.rs:15-19)."""
+    area = n / density
+    ly = math.sqrt(area / aspect)
+    return [to_fixed(ly * aspect), to_fixed(ly)]
+
+
+def cube_for(n, density):
+    """three::cube_for (three.rs:312-315)."""
+    l = to_fixed(math.cbrt(n / density))
+    return [l, l, l]
+
+
+def fcc_cells(n, box_len):
+    """three::fcc_cells (three.rs:346-355)."""
+    b = [to_f64(x) for x in box_len]
+    a = math.cbrt(b[0] * b[1] * b[2] * 4.0 / n)
+    c = [max(int(rust_round(l / a)), 1) for l in b]
+    while 4 * c[0] * c[1] * c[2] < n:
+        k = 0
+        for x in (1, 2):
+            if b[x] / c[x] > b[k] / c[k]:
+                k = x
+        c[k] += 1
+    return c

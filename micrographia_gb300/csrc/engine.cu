@@ -1,0 +1,1022 @@
+// The single-system engine behind the C ABI of include/gbmd.h: the GB300 counterpart of
+// md::GpuEngine / md::GpuEngine3 (crates/md/src/engine.rs:598-1098, engine3.rs:334-648).
+//
+// One CUDA stream per engine. A step is: [if the rebuild flag is set: cell keys -> stable radix
+// sort -> cell starts -> gather into cell order -> Verlet-list build] -> fused LJ force +
+// leapfrog + displacement trigger. Steps are captured into CUDA graphs (blocks of
+// `block_steps`), and the rebuild runs inside a conditional graph node whose condition a
+// one-thread kernel reads from the device flag, so the decision never returns to the host (the
+// reference's indirect-dispatch gate, gpu-prims prims.rs:250-283 / gate.wgsl:13-24).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.cuh"
+#include "kernels.cuh"
+#include "sort.cuh"
+
+namespace gbmd {
+
+// ------------------------------------------------------------------ status + accounting
+static thread_local std::string t_error;
+void set_error(const std::string& msg) { t_error = msg; }
+int fail(int code, const std::string& msg) {
+    t_error = msg;
+    return code;
+}
+static std::atomic<uint64_t> g_launches{0};
+void note_launch(uint64_t k) { g_launches += k; }
+uint64_t launch_total() { return g_launches.load(); }
+
+static double to_f64h(int64_t x) { return (double)x * (1.0 / 4294967296.0); }
+
+int validate_system(const gbmd_system& sys, uint32_t n) {
+    if (sys.dim != 2 && sys.dim != 3) return fail(GBMD_E_INVALID, "dim must be 2 or 3");
+    if (sys.nspecies < 1 || sys.nspecies > GBMD_MAX_SPECIES) return fail(GBMD_E_INVALID, "species must number 1 to 4");
+    uint32_t all = (1u << sys.dim) - 1u;
+    if ((sys.periodic & all) != all)
+        return fail(GBMD_E_UNSUPPORTED, "walls are not part of this engine: every axis must be periodic");
+    for (uint32_t a = 0; a < sys.dim; a++)
+        if (sys.box_len[a] <= 0) return fail(GBMD_E_INVALID, "box lengths must be positive");
+    for (uint32_t k = 0; k < sys.nspecies * sys.nspecies; k++) {
+        const gbmd_pair& p = sys.pairs[k];
+        if (!(p.rc < 7.9)) return fail(GBMD_E_INVALID, "cutoff must be below 8 sigma"); // system.rs:190-194
+    }
+    for (uint32_t s = 0; s < sys.nspecies; s++)
+        if (!(sys.masses[s] > 0.0)) return fail(GBMD_E_INVALID, "masses must be positive");
+    if (!(sys.dt > 0.0)) return fail(GBMD_E_INVALID, "dt must be positive");
+    (void)n;
+    return GBMD_OK;
+}
+
+// ------------------------------------------------------------------ host-side System maths
+static double rc_max(const gbmd_system& s) {
+    double r = 0.0;
+    for (uint32_t k = 0; k < s.nspecies * s.nspecies; k++) r = std::max(r, s.pairs[k].rc);
+    return r;
+}
+// System::cells_for (system.rs:438-444 / three.rs:151-157)
+static int cells_for(const gbmd_system& s, double r, uint32_t* c) {
+    double bmax = 0.0;
+    for (uint32_t a = 0; a < s.dim; a++) bmax = std::max(bmax, to_f64h(s.box_len[a]));
+    double margin = 1e-3 + 1e-6 * bmax;
+    c[2] = 1;
+    for (uint32_t a = 0; a < s.dim; a++) {
+        double v = std::floor(to_f64h(s.box_len[a]) / (r + margin));
+        c[a] = v >= 4294967295.0 ? UINT32_MAX : (v > 0 ? (uint32_t)v : 0);
+        if (c[a] < 3) return fail(GBMD_E_INVALID, "box too small for the cell radius (fewer than 3 cells on an axis)");
+    }
+    return GBMD_OK;
+}
+// Pair::shift (pair.rs:28-34) with Rust powi(6) = x^2 * (x^2)^2.
+static double pair_shift(const gbmd_pair& p) {
+    if (p.eps == 0.0 || p.rc == 0.0) return 0.0;
+    double x = p.sigma / p.rc;
+    double x2 = x * x;
+    double s6 = x2 * (x2 * x2);
+    return 4.0 * p.eps * s6 * (s6 - 1.0);
+}
+static float scale2(float v, int e) { return std::ldexp(v, e); }
+
+static void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint32_t cap, const uint32_t* nc) {
+    std::memset(&P, 0, sizeof(P));
+    P.n = n;
+    P.dim = s.dim;
+    P.ns = s.nspecies;
+    P.cap = cap;
+    for (uint32_t a = 0; a < 3; a++) {
+        P.box[a] = a < s.dim ? s.box_len[a] : 1;
+        P.half[a] = P.box[a] / 2;
+        P.box_f[a] = to_f64h(P.box[a]);
+        P.nc[a] = a < s.dim ? nc[a] : 1;
+    }
+    P.ncell = P.nc[0] * P.nc[1] * P.nc[2];
+    for (uint32_t sp = 0; sp < GBMD_MAX_SPECIES; sp++) {
+        double kc = 0.0;
+        if (sp < s.nspecies && !((s.pinned >> sp) & 1u)) kc = s.dt * s.dt / s.masses[sp] * 4294967296.0; // kick_coeff
+        P.kick_cs[sp] = scale2((float)kc, 28);
+        P.masses[sp] = sp < s.nspecies ? s.masses[sp] : 1.0;
+    }
+    for (uint32_t a = 0; a < 3; a++) {
+        double g = a < s.dim ? s.gravity[a] : 0.0;
+        double v = std::round(g * s.dt * s.dt * 4294967296.0); // System::gravity_kick
+        P.gravity[a] = v != v ? 0 : (v >= 2147483647.0 ? INT32_MAX : (v <= -2147483648.0 ? INT32_MIN : (int32_t)v));
+    }
+    P.pinned = s.pinned;
+    double hs = 0.5 * skin * (1.0 - 1e-3);
+    P.half_skin2s = scale2((float)(hs * hs), 56);
+    P.dt = s.dt;
+    for (uint32_t a = 0; a < s.nspecies; a++)
+        for (uint32_t b = 0; b < s.nspecies; b++) {
+            const gbmd_pair& p = s.pairs[a * s.nspecies + b];
+            PairC& c = P.pc[a * s.nspecies + b];
+            float rc2 = (float)(p.rc * p.rc), eps4 = (float)(4.0 * p.eps), sigma2 = (float)(p.sigma * p.sigma);
+            c.rc2s = scale2(rc2, 56);
+            c.sigma2s = scale2(sigma2, 56);
+            c.eps4 = eps4;
+            c.c6 = 6.0f * eps4;
+            c.shift = (float)pair_shift(p);
+            double lr = (p.rc + skin) * (1.0 + 1e-4);
+            c.list2s = scale2((float)(lr * lr), 56);
+        }
+}
+static int key_bits(uint32_t ncell) {
+    int b = 0;
+    while (b < 32 && (ncell - 1) >> b) b++;
+    return std::max(b, 1);
+}
+static uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
+
+} // namespace gbmd
+
+using namespace gbmd;
+
+// ------------------------------------------------------------------ the engine
+struct gbmd_engine {
+    gbmd_system sys{};
+    gbmd_options opt{};
+    uint32_t n = 0;
+    int D = 2;
+    bool verlet = true;
+    bool multi = false;
+    double skin = 0.0;
+    Params P{};     // force/list parameters (cells of rc + skin)
+    int bits = 1;   // significant bits of the cell keys
+    cudaStream_t st = nullptr;
+    cudaStream_t st_body = nullptr; // capture stream of conditional bodies
+    size_t rec = 16; // bytes per position record
+
+    void* pos[2] = {nullptr, nullptr};
+    void* pos_scr = nullptr;
+    void* ref_pos = nullptr;
+    int32_t *vel = nullptr, *vel_scr = nullptr, *kicks = nullptr;
+    uint32_t *species = nullptr, *species_scr = nullptr, *ids = nullptr, *ids_scr = nullptr;
+    uint32_t *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr};
+    uint32_t *hist = nullptr, *scan_tmp = nullptr, *start = nullptr;
+    uint32_t *nbr = nullptr, *nbr_count = nullptr;
+    uint32_t* ctl = nullptr; // [0] rebuild, [1] overflow, [2] rebuilds
+    double* partial = nullptr;
+    void* staging = nullptr;  // id-ordered I/O staging (n * D int64)
+    int32_t* staging_v = nullptr;
+    uint32_t* staging_s = nullptr;
+    int sorted = 0; // which keys/vals buffer holds the sorted result
+
+    int cur = 0;
+    int64_t steps = 0;
+    uint32_t clock = 0;
+    uint32_t block_steps = 64;
+    cudaGraphExec_t exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [parity][single, block]
+    uint64_t exec_launches[2][2] = {{0, 0}, {0, 0}};
+    uint64_t body_launches = 0;
+    uint64_t launches = 0;
+    uint32_t last_rebuilds = 0;
+    bool failed = false;
+};
+
+namespace {
+
+template <int D> using Rec = PosRec<D>;
+
+int alloc(void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GBMD_E_NOMEM : GBMD_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return GBMD_OK;
+}
+template <typename T> int allocT(T** p, size_t count) { return alloc((void**)p, count * sizeof(T)); }
+
+void free_all(gbmd_engine* e) {
+    for (int p = 0; p < 2; p++)
+        for (int b = 0; b < 2; b++)
+            if (e->exec[p][b]) cudaGraphExecDestroy(e->exec[p][b]);
+    void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
+                    e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
+                    e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (e->st) cudaStreamDestroy(e->st);
+    if (e->st_body) cudaStreamDestroy(e->st_body);
+}
+
+// ---- enqueue helpers (stream-ordered; also used under capture)
+template <int D> void enqueue_bin(gbmd_engine* e, cudaStream_t s, const Params& P) {
+    k_keys<D><<<blocks_for(e->n, 256), 256, 0, s>>>(P, (const Rec<D>*)e->pos[e->cur], e->keys[0], e->vals[0]);
+    e->sorted = radix_sort_pairs(e->keys[0], e->vals[0], e->keys[1], e->vals[1], e->n, key_bits(P.ncell), e->hist, e->scan_tmp, s);
+    cell_starts(e->keys[e->sorted], e->n, P.ncell, e->start, s);
+    k_gather<D><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, D, e->vals[e->sorted], (const Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids,
+                                                       (Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr);
+    note_launch(3 + 3 * (uint64_t)radix_passes(key_bits(P.ncell)) + 2);
+}
+
+template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t s) {
+    enqueue_bin<D>(e, s, e->P);
+    k_build_list<D, MULTI><<<blocks_for(e->n, 128), 128, 0, s>>>(
+        e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, (Rec<D>*)e->pos[e->cur],
+        e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl);
+    note_launch();
+}
+
+__global__ void k_rebuild_done(uint32_t* ctl) {
+    ctl[0] = 0;
+    ctl[2] += 1;
+}
+__global__ void k_set_cond(cudaGraphConditionalHandle h, const uint32_t* ctl) { cudaGraphSetConditional(h, ctl[0] ? 1u : 0u); }
+
+void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
+    if (e->D == 2) {
+        if (e->multi) enqueue_rebuild_t<2, true>(e, s);
+        else enqueue_rebuild_t<2, false>(e, s);
+    } else {
+        if (e->multi) enqueue_rebuild_t<3, true>(e, s);
+        else enqueue_rebuild_t<3, false>(e, s);
+    }
+    k_rebuild_done<<<1, 1, 0, s>>>(e->ctl);
+    note_launch();
+}
+
+template <int D, bool MULTI> void enqueue_force_t(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
+    if (e->verlet) {
+        k_force_list<D, MULTI><<<blocks_for(e->n, threads), threads, 0, s>>>(e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1],
+                                                                           e->vel, e->species, e->nbr, e->nbr_count,
+                                                                           (const Rec<D>*)e->ref_pos, e->ctl);
+        note_launch();
+        e->cur ^= 1;
+    } else {
+        enqueue_bin<D>(e, s, e->P);
+        k_force_cells<D, MULTI><<<blocks_for(e->n, threads), threads, 0, s>>>(e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr,
+                                                                            e->ids_scr, e->keys[e->sorted], e->start,
+                                                                            (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids);
+        note_launch();
+    }
+}
+void enqueue_force(gbmd_engine* e, cudaStream_t s) {
+    uint32_t threads = e->opt.threads ? e->opt.threads : 128;
+    if (e->D == 2) {
+        if (e->multi) enqueue_force_t<2, true>(e, s, threads);
+        else enqueue_force_t<2, false>(e, s, threads);
+    } else {
+        if (e->multi) enqueue_force_t<3, true>(e, s, threads);
+        else enqueue_force_t<3, false>(e, s, threads);
+    }
+}
+
+// Capture `count` steps starting at parity `parity` into a graph.
+int capture_steps(gbmd_engine* e, int parity, uint32_t count, cudaGraphExec_t* out, uint64_t* launches) {
+    int saved_cur = e->cur;
+    e->cur = parity;
+    uint64_t l0 = launch_total();
+    cudaStream_t s = e->st;
+    GBMD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    uint64_t body = 0;
+    for (uint32_t k = 0; k < count; k++) {
+        if (e->verlet) {
+            cudaStreamCaptureStatus status;
+            cudaGraph_t g;
+            const cudaGraphNode_t* deps;
+            const cudaGraphEdgeData* edges;
+            size_t ndeps;
+            GBMD_CUDA_TRY(cudaStreamGetCaptureInfo(s, &status, nullptr, &g, &deps, &edges, &ndeps));
+            cudaGraphConditionalHandle h;
+            GBMD_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+            k_set_cond<<<1, 1, 0, s>>>(h, e->ctl);
+            note_launch();
+            GBMD_CUDA_TRY(cudaStreamGetCaptureInfo(s, &status, nullptr, &g, &deps, &edges, &ndeps));
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeIf;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            GBMD_CUDA_TRY(cudaGraphAddNode(&node, g, deps, edges, ndeps, &cp));
+            cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+            GBMD_CUDA_TRY(cudaStreamBeginCaptureToGraph(e->st_body, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            uint64_t b0 = launch_total();
+            enqueue_rebuild(e, e->st_body);
+            body = launch_total() - b0;
+            g_launches -= body; // counted per replay instead
+            cudaGraph_t tmp;
+            GBMD_CUDA_TRY(cudaStreamEndCapture(e->st_body, &tmp));
+            GBMD_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        }
+        enqueue_force(e, s);
+    }
+    cudaGraph_t graph;
+    cudaError_t err = cudaStreamEndCapture(s, &graph);
+    if (err != cudaSuccess) {
+        e->cur = saved_cur;
+        return fail(GBMD_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
+    }
+    err = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (err != cudaSuccess) {
+        e->cur = saved_cur;
+        return fail(GBMD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+    }
+    *launches = launch_total() - l0;
+    g_launches -= *launches; // launches are counted when the graph is replayed
+    e->body_launches = body;
+    e->cur = saved_cur;
+    return GBMD_OK;
+}
+
+int run_graph(gbmd_engine* e, int which) {
+    int parity = e->cur;
+    if (!e->exec[parity][which]) {
+        uint32_t count = which ? e->block_steps : 1;
+        GBMD_TRY(capture_steps(e, parity, count, &e->exec[parity][which], &e->exec_launches[parity][which]));
+    }
+    GBMD_CUDA_TRY(cudaGraphLaunch(e->exec[parity][which], e->st));
+    uint32_t count = which ? e->block_steps : 1;
+    note_launch(e->exec_launches[parity][which]);
+    e->launches += e->exec_launches[parity][which];
+    if (e->verlet && (count & 1)) e->cur ^= 1;
+    return GBMD_OK;
+}
+
+// Bring the pair structure up to date with the current positions (for kicks/observables):
+// a Verlet list is rebuilt, a cell list binned into the scratch state.
+int prepare_pairs(gbmd_engine* e) {
+    if (e->verlet) {
+        enqueue_rebuild(e, e->st);
+    } else {
+        if (e->D == 2) enqueue_bin<2>(e, e->st, e->P);
+        else enqueue_bin<3>(e, e->st, e->P);
+    }
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return GBMD_OK;
+}
+
+// Kicks (storage order) and the per-block observables at the current positions; optionally
+// reverse the velocities. Cell mode works on (and copies back) the sorted scratch state.
+template <int D, bool MULTI> int kicks_t(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
+    uint32_t threads = 128;
+    uint32_t nb = blocks_for(e->n, threads);
+    if (e->verlet) {
+        k_kicks<D, MULTI><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos[e->cur], e->species, e->nbr, e->nbr_count, nullptr, nullptr,
+                                                     e->vel, kicks, partial, reverse);
+    } else {
+        // positions, velocities and ids live in scratch (sorted) until copied back
+        k_kicks<D, MULTI><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos_scr, e->species_scr, nullptr, nullptr, e->keys[e->sorted],
+                                                     e->start, e->vel_scr, kicks, partial, reverse);
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->pos[e->cur], e->pos_scr, (size_t)e->n * e->rec, cudaMemcpyDeviceToDevice, e->st));
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->vel, e->vel_scr, (size_t)e->n * D * 4, cudaMemcpyDeviceToDevice, e->st));
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->species, e->species_scr, (size_t)e->n * 4, cudaMemcpyDeviceToDevice, e->st));
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->ids, e->ids_scr, (size_t)e->n * 4, cudaMemcpyDeviceToDevice, e->st));
+    }
+    note_launch();
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return GBMD_OK;
+}
+int kicks_dispatch(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
+    if (e->D == 2) return e->multi ? kicks_t<2, true>(e, kicks, partial, reverse) : kicks_t<2, false>(e, kicks, partial, reverse);
+    return e->multi ? kicks_t<3, true>(e, kicks, partial, reverse) : kicks_t<3, false>(e, kicks, partial, reverse);
+}
+
+// ---- id-ordered I/O
+template <int D>
+__global__ void k_to_ids(uint32_t n, const Rec<D>* pos, const int32_t* vel, const uint32_t* species, const uint32_t* ids, int64_t* opos,
+                         int32_t* ovel, uint32_t* ospecies) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    uint32_t id = ids[s];
+    int64_t x[3];
+    load_particle<D, false>(pos, nullptr, s, x);
+    for (int a = 0; a < D; a++) {
+        opos[(size_t)D * id + a] = x[a];
+        ovel[(size_t)D * id + a] = vel[D * s + a];
+    }
+    ospecies[id] = species[s];
+}
+template <int D>
+__global__ void k_from_ids(uint32_t n, const int64_t* ipos, const int32_t* ivel, const uint32_t* ispecies, Rec<D>* pos, int32_t* vel,
+                           uint32_t* species, uint32_t* ids) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int64_t x[3];
+    for (int a = 0; a < D; a++) {
+        x[a] = ipos[(size_t)D * s + a];
+        vel[D * s + a] = ivel[(size_t)D * s + a];
+    }
+    store_pos<D>(pos, s, x, ispecies[s]);
+    species[s] = ispecies[s];
+    ids[s] = s;
+}
+__global__ void k_scatter_i32(uint32_t n, uint32_t d, const uint32_t* ids, const int32_t* in, int32_t* out) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    for (uint32_t a = 0; a < d; a++) out[(size_t)d * ids[s] + a] = in[(size_t)d * s + a];
+}
+template <int D> __global__ void k_flip(uint32_t n, const uint32_t* ids, uint32_t id, uint32_t axis, uint32_t bit, Rec<D>* pos) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || ids[s] != id) return;
+    long long* p = reinterpret_cast<long long*>(pos + s);
+    p[axis] ^= (long long)(1ull << bit);
+}
+
+int upload_state(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const uint32_t* species) {
+    size_t n = e->n, D = e->D;
+    for (size_t i = 0; i < n; i++)
+        if (species[i] >= e->sys.nspecies) return fail(GBMD_E_INVALID, "species index out of range");
+    for (size_t i = 0; i < n; i++)
+        for (size_t a = 0; a < D; a++)
+            if (pos[D * i + a] < 0 || pos[D * i + a] >= e->sys.box_len[a])
+                return fail(GBMD_E_INVALID, "positions must lie in [0, L) on every axis");
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->staging, pos, n * D * 8, cudaMemcpyHostToDevice, e->st));
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->staging_v, vel, n * D * 4, cudaMemcpyHostToDevice, e->st));
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->staging_s, species, n * 4, cudaMemcpyHostToDevice, e->st));
+    if (D == 2)
+        k_from_ids<2><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, (const int64_t*)e->staging, e->staging_v, e->staging_s,
+                                                            (Rec<2>*)e->pos[e->cur], e->vel, e->species, e->ids);
+    else
+        k_from_ids<3><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, (const int64_t*)e->staging, e->staging_v, e->staging_s,
+                                                            (Rec<3>*)e->pos[e->cur], e->vel, e->species, e->ids);
+    note_launch();
+    uint32_t one = 1;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    return GBMD_OK;
+}
+
+int read_state_dev(gbmd_engine* e) {
+    size_t n = e->n;
+    if (e->D == 2)
+        k_to_ids<2><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, (const Rec<2>*)e->pos[e->cur], e->vel, e->species, e->ids,
+                                                          (int64_t*)e->staging, e->staging_v, e->staging_s);
+    else
+        k_to_ids<3><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, (const Rec<3>*)e->pos[e->cur], e->vel, e->species, e->ids,
+                                                          (int64_t*)e->staging, e->staging_v, e->staging_s);
+    note_launch();
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return GBMD_OK;
+}
+
+int check_ctl(gbmd_engine* e) {
+    uint32_t c[3];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, 12, cudaMemcpyDeviceToHost, e->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    e->last_rebuilds = c[2];
+    if (c[1]) {
+        e->failed = true;
+        return fail(GBMD_E_OVERFLOW, "a Verlet list overflowed its capacity (raise gbmd_options.cap)");
+    }
+    return GBMD_OK;
+}
+
+int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd_options* opts) {
+    e->sys = *sys;
+    if (opts) e->opt = *opts;
+    e->n = n;
+    e->D = (int)sys->dim;
+    e->multi = sys->nspecies > 1;
+    e->rec = e->D == 2 ? 16 : 32;
+    int mode = e->opt.mode;
+    if (mode == GBMD_MODE_AUTO) mode = (e->D == 2 && n < 24000) ? GBMD_MODE_CELLS : GBMD_MODE_VERLET; // ForceMode::auto
+    e->verlet = mode == GBMD_MODE_VERLET;
+    if (e->opt.arith != GBMD_ARITH_F32) return fail(GBMD_E_UNSUPPORTED, "all-integer table forces are not built in this engine yet");
+    e->skin = e->verlet ? (e->opt.skin > 0 ? e->opt.skin : 0.4) : 0.0;
+    uint32_t nc[3];
+    GBMD_TRY(cells_for(*sys, rc_max(*sys) + e->skin, nc));
+    uint32_t cap = 0;
+    if (e->verlet) {
+        // ForceMode::verlet_with_skin's sizing (engine.rs:130-141), without the 128 MiB clamp
+        double r = rc_max(*sys) + e->skin, vol = 1.0;
+        for (int a = 0; a < e->D; a++) vol *= to_f64h(sys->box_len[a]);
+        double density = (double)n / vol;
+        double sphere = e->D == 2 ? M_PI * r * r : 4.0 / 3.0 * M_PI * r * r * r;
+        cap = e->opt.cap ? e->opt.cap : (uint32_t)std::ceil(sphere * std::max(2.0 * density, 1.2)) + 8;
+    }
+    fill_params(e->P, *sys, n, e->skin, cap, nc);
+    e->block_steps = e->opt.block_steps ? e->opt.block_steps : 64;
+    GBMD_CUDA_TRY(cudaSetDevice(e->opt.device));
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st_body, cudaStreamNonBlocking));
+    size_t D = e->D;
+    GBMD_TRY(alloc(&e->pos[0], n * e->rec));
+    GBMD_TRY(alloc(&e->pos[1], n * e->rec));
+    GBMD_TRY(alloc(&e->pos_scr, n * e->rec));
+    GBMD_TRY(alloc(&e->ref_pos, n * e->rec));
+    GBMD_TRY(allocT(&e->vel, n * D));
+    GBMD_TRY(allocT(&e->vel_scr, n * D));
+    GBMD_TRY(allocT(&e->kicks, n * D));
+    GBMD_TRY(allocT(&e->species, n));
+    GBMD_TRY(allocT(&e->species_scr, n));
+    GBMD_TRY(allocT(&e->ids, n));
+    GBMD_TRY(allocT(&e->ids_scr, n));
+    for (int b = 0; b < 2; b++) {
+        GBMD_TRY(allocT(&e->keys[b], n));
+        GBMD_TRY(allocT(&e->vals[b], n));
+    }
+    size_t hist_n = radix_hist_elems(n);
+    GBMD_TRY(allocT(&e->hist, hist_n));
+    GBMD_TRY(allocT(&e->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(n))));
+    GBMD_TRY(allocT(&e->start, (size_t)e->P.ncell + 1));
+    if (e->verlet) {
+        GBMD_TRY(allocT(&e->nbr, (size_t)n * cap));
+        GBMD_TRY(allocT(&e->nbr_count, n));
+    }
+    GBMD_TRY(allocT(&e->ctl, 16));
+    GBMD_TRY(allocT(&e->partial, 4 * (size_t)blocks_for(n, 128) + 4));
+    GBMD_TRY(alloc(&e->staging, n * D * 8));
+    GBMD_TRY(allocT(&e->staging_v, n * D));
+    GBMD_TRY(allocT(&e->staging_s, n));
+    GBMD_CUDA_TRY(cudaMemsetAsync(e->ctl, 0, 64, e->st));
+    return GBMD_OK;
+}
+
+} // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int gbmd_create(const gbmd_system* sys, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint32_t n,
+                const gbmd_options* opts, gbmd_engine** out) {
+    if (!sys || !out || (n && (!pos || !vel || !species))) return fail(GBMD_E_INVALID, "null argument");
+    *out = nullptr;
+    GBMD_TRY(validate_system(*sys, n));
+    if (n == 0) return fail(GBMD_E_INVALID, "an engine needs at least one particle");
+    auto* e = new gbmd_engine;
+    int r = create_common(e, sys, n, opts);
+    if (r == GBMD_OK) r = upload_state(e, pos, vel, species);
+    if (r != GBMD_OK) {
+        std::string msg = t_error;
+        free_all(e);
+        delete e;
+        return fail(r, msg);
+    }
+    *out = e;
+    return GBMD_OK;
+}
+
+int gbmd_create_seeded(const gbmd_system* sys, const gbmd_init* spec, const gbmd_options* opts, gbmd_engine** out) {
+    if (!sys || !spec || !out) return fail(GBMD_E_INVALID, "null argument");
+    *out = nullptr;
+    GBMD_TRY(validate_system(*sys, spec->n));
+    if (spec->n == 0) return fail(GBMD_E_INVALID, "an engine needs at least one particle");
+    auto* e = new gbmd_engine;
+    int r = create_common(e, sys, spec->n, opts);
+    if (r == GBMD_OK) r = init_state_device(*sys, *spec, e->pos[e->cur], e->vel, e->species, e->st);
+    if (r == GBMD_OK) {
+        iota(e->ids, e->n, e->st);
+        note_launch();
+        uint32_t one = 1;
+        cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st);
+        if (cudaStreamSynchronize(e->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "seeded init failed");
+    }
+    if (r != GBMD_OK) {
+        std::string msg = t_error;
+        free_all(e);
+        delete e;
+        return fail(r, msg);
+    }
+    *out = e;
+    return GBMD_OK;
+}
+
+int gbmd_destroy(gbmd_engine* e) {
+    if (!e) return GBMD_OK;
+    cudaStreamSynchronize(e->st);
+    free_all(e);
+    delete e;
+    return GBMD_OK;
+}
+
+int gbmd_step(gbmd_engine* e, uint64_t steps) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (e->failed) return fail(GBMD_E_OVERFLOW, "the engine is in a failed state (a list overflowed)");
+    uint64_t left = steps;
+    while (left >= e->block_steps) {
+        GBMD_TRY(run_graph(e, 1));
+        left -= e->block_steps;
+    }
+    while (left > 0) {
+        GBMD_TRY(run_graph(e, 0));
+        left--;
+    }
+    e->steps += (int64_t)steps;
+    e->clock += (uint32_t)steps;
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return GBMD_OK;
+}
+
+int gbmd_sync(gbmd_engine* e) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    return check_ctl(e);
+}
+
+int gbmd_reverse(gbmd_engine* e) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_TRY(prepare_pairs(e));
+    GBMD_TRY(kicks_dispatch(e, nullptr, nullptr, 1));
+    e->steps = -e->steps;
+    return gbmd_sync(e);
+}
+
+int gbmd_read_state(gbmd_engine* e, int64_t* pos, int32_t* vel, uint32_t* species) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_TRY(read_state_dev(e));
+    size_t n = e->n, D = e->D;
+    if (pos) GBMD_CUDA_TRY(cudaMemcpyAsync(pos, e->staging, n * D * 8, cudaMemcpyDeviceToHost, e->st));
+    if (vel) GBMD_CUDA_TRY(cudaMemcpyAsync(vel, e->staging_v, n * D * 4, cudaMemcpyDeviceToHost, e->st));
+    if (species) GBMD_CUDA_TRY(cudaMemcpyAsync(species, e->staging_s, n * 4, cudaMemcpyDeviceToHost, e->st));
+    return gbmd_sync(e);
+}
+
+int gbmd_upload(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const uint32_t* species) {
+    if (!e || !pos || !vel || !species) return fail(GBMD_E_INVALID, "null argument");
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    e->failed = false;
+    uint32_t zero[2] = {0, 0};
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, zero, 8, cudaMemcpyHostToDevice, e->st));
+    return upload_state(e, pos, vel, species);
+}
+
+int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_TRY(prepare_pairs(e));
+    GBMD_TRY(kicks_dispatch(e, e->kicks, e->partial, 0));
+    size_t n = e->n;
+    if (kicks) {
+        k_scatter_i32<<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, e->D, e->ids, e->kicks, (int32_t*)e->staging_v);
+        note_launch();
+        GBMD_CUDA_TRY(cudaMemcpyAsync(kicks, e->staging_v, n * e->D * 4, cudaMemcpyDeviceToHost, e->st));
+    }
+    uint32_t nb = blocks_for(n, 128);
+    std::vector<double> part(4 * (size_t)nb);
+    GBMD_CUDA_TRY(cudaMemcpyAsync(part.data(), e->partial, part.size() * 8, cudaMemcpyDeviceToHost, e->st));
+    GBMD_TRY(gbmd_sync(e));
+    if (potential) {
+        double pe = 0.0;
+        for (uint32_t b = 0; b < nb; b++) pe += part[4 * b];
+        *potential = pe;
+    }
+    return GBMD_OK;
+}
+
+int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit) {
+    if (!e || id >= e->n || axis >= (uint32_t)e->D || bit > 62) return fail(GBMD_E_INVALID, "bad flip_bit argument");
+    if (e->D == 2) k_flip<2><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->ids, id, axis, bit, (Rec<2>*)e->pos[e->cur]);
+    else k_flip<3><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->ids, id, axis, bit, (Rec<3>*)e->pos[e->cur]);
+    note_launch();
+    uint32_t one = 1;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    return gbmd_sync(e);
+}
+
+int gbmd_energy(gbmd_engine* e, double* kinetic, double* potential) {
+    gbmd_frame f;
+    GBMD_TRY(gbmd_observe(e, &f, nullptr, 0, 0.0, nullptr, 0, 0));
+    if (kinetic) *kinetic = f.kinetic;
+    if (potential) *potential = f.potential;
+    return GBMD_OK;
+}
+
+int gbmd_list_stats(gbmd_engine* e, uint32_t* rebuilds, int32_t* overflow) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    uint32_t c[3];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, 12, cudaMemcpyDeviceToHost, e->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    if (rebuilds) *rebuilds = c[2];
+    if (overflow) *overflow = c[1] ? 1 : 0;
+    return GBMD_OK;
+}
+
+int gbmd_state_hash(gbmd_engine* e, uint64_t* hash) {
+    if (!e || !hash) return fail(GBMD_E_INVALID, "null argument");
+    size_t n = e->n, D = e->D;
+    std::vector<int64_t> pos(n * D);
+    std::vector<int32_t> vel(n * D);
+    std::vector<uint32_t> sp(n);
+    GBMD_TRY(gbmd_read_state(e, pos.data(), vel.data(), sp.data()));
+    *hash = gbmd_hash_state((uint32_t)D, pos.data(), vel.data(), sp.data(), (uint32_t)n);
+    return GBMD_OK;
+}
+
+int gbmd_counters(gbmd_engine* e, int64_t* steps, uint32_t* clock) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (steps) *steps = e->steps;
+    if (clock) *clock = e->clock;
+    return GBMD_OK;
+}
+
+int gbmd_stream(gbmd_engine* e, void** stream) {
+    if (!e || !stream) return fail(GBMD_E_INVALID, "null argument");
+    *stream = (void*)e->st;
+    return GBMD_OK;
+}
+
+int gbmd_launch_count(gbmd_engine* e, uint64_t* launches) {
+    if (!e || !launches) return fail(GBMD_E_INVALID, "null argument");
+    uint32_t rebuilds = 0;
+    int32_t ov = 0;
+    GBMD_TRY(gbmd_list_stats(e, &rebuilds, &ov));
+    *launches = e->launches + (uint64_t)rebuilds * e->body_launches;
+    return GBMD_OK;
+}
+
+int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* rebuild_ms, uint32_t* rebuilds) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_TRY(gbmd_sync(e));
+    cudaEvent_t a, b, c;
+    GBMD_CUDA_TRY(cudaEventCreate(&a));
+    GBMD_CUDA_TRY(cudaEventCreate(&b));
+    GBMD_CUDA_TRY(cudaEventCreate(&c));
+    double tf = 0.0, tr = 0.0;
+    uint32_t nr = 0;
+    for (uint32_t k = 0; k < steps; k++) {
+        uint32_t flag = 0;
+        if (e->verlet) {
+            GBMD_CUDA_TRY(cudaMemcpyAsync(&flag, e->ctl, 4, cudaMemcpyDeviceToHost, e->st));
+            GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+        }
+        GBMD_CUDA_TRY(cudaEventRecord(a, e->st));
+        if (flag) {
+            enqueue_rebuild(e, e->st);
+            nr++;
+        }
+        GBMD_CUDA_TRY(cudaEventRecord(b, e->st));
+        enqueue_force(e, e->st);
+        GBMD_CUDA_TRY(cudaEventRecord(c, e->st));
+        GBMD_CUDA_TRY(cudaEventSynchronize(c));
+        float m1 = 0.f, m2 = 0.f;
+        cudaEventElapsedTime(&m1, a, b);
+        cudaEventElapsedTime(&m2, b, c);
+        if (flag) tr += m1;
+        tf += m2;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaEventDestroy(c);
+    e->steps += steps;
+    e->clock += steps;
+    if (force_ms) *force_ms = steps ? tf / steps : 0.0;
+    if (rebuild_ms) *rebuild_ms = nr ? tr / nr : 0.0;
+    if (rebuilds) *rebuilds = nr;
+    return check_ctl(e);
+}
+
+int gbmd_debug_bin(gbmd_engine* e, const uint32_t* cells, uint32_t* keys, uint32_t* start, uint32_t* items, uint32_t* order) {
+    if (!e || !cells) return fail(GBMD_E_INVALID, "null argument");
+    Params P = e->P;
+    for (int a = 0; a < e->D; a++) {
+        if (cells[a] < 1) return fail(GBMD_E_INVALID, "cells must be positive");
+        P.nc[a] = cells[a];
+    }
+    P.ncell = P.nc[0] * P.nc[1] * (e->D == 3 ? P.nc[2] : 1);
+    uint32_t* st2 = nullptr;
+    GBMD_CUDA_TRY(cudaMalloc(&st2, ((size_t)P.ncell + 1) * 4));
+    uint32_t* saved = e->start;
+    e->start = st2;
+    uint32_t n = e->n;
+    std::vector<uint32_t> k(n);
+    // keys in storage order first (before the sort overwrites them)
+    if (e->D == 2) k_keys<2><<<blocks_for(n, 256), 256, 0, e->st>>>(P, (const Rec<2>*)e->pos[e->cur], e->keys[0], e->vals[0]);
+    else k_keys<3><<<blocks_for(n, 256), 256, 0, e->st>>>(P, (const Rec<3>*)e->pos[e->cur], e->keys[0], e->vals[0]);
+    cudaMemcpyAsync(k.data(), e->keys[0], (size_t)n * 4, cudaMemcpyDeviceToHost, e->st);
+    if (order) cudaMemcpyAsync(order, e->ids, (size_t)n * 4, cudaMemcpyDeviceToHost, e->st);
+    if (e->D == 2) enqueue_bin<2>(e, e->st, P);
+    else enqueue_bin<3>(e, e->st, P);
+    if (start) cudaMemcpyAsync(start, e->start, ((size_t)P.ncell + 1) * 4, cudaMemcpyDeviceToHost, e->st);
+    if (items) cudaMemcpyAsync(items, e->vals[e->sorted], (size_t)n * 4, cudaMemcpyDeviceToHost, e->st);
+    cudaError_t err = cudaStreamSynchronize(e->st);
+    e->start = saved;
+    cudaFree(st2);
+    if (err != cudaSuccess) return fail(GBMD_E_CUDA, cudaGetErrorString(err));
+    if (keys) std::memcpy(keys, k.data(), (size_t)n * 4);
+    // the sort state is scratch only: the pair structure must be rebuilt before the next use
+    uint32_t one = 1;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    return gbmd_sync(e);
+}
+
+int gbmd_debug_list(gbmd_engine* e, uint32_t* counts, uint32_t* nbr, uint64_t nbr_cap) {
+    if (!e || !counts || !nbr) return fail(GBMD_E_INVALID, "null argument");
+    if (!e->verlet) return fail(GBMD_E_INVALID, "the engine has no Verlet list (cell mode)");
+    GBMD_TRY(prepare_pairs(e));
+    GBMD_TRY(gbmd_sync(e));
+    size_t n = e->n, cap = e->P.cap;
+    std::vector<uint32_t> cnt(n), ids(n), lst(n * cap);
+    GBMD_CUDA_TRY(cudaMemcpy(cnt.data(), e->nbr_count, n * 4, cudaMemcpyDeviceToHost));
+    GBMD_CUDA_TRY(cudaMemcpy(ids.data(), e->ids, n * 4, cudaMemcpyDeviceToHost));
+    GBMD_CUDA_TRY(cudaMemcpy(lst.data(), e->nbr, n * cap * 4, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> slot_of(n);
+    for (size_t s = 0; s < n; s++) slot_of[ids[s]] = (uint32_t)s;
+    uint64_t off = 0;
+    for (size_t id = 0; id < n; id++) {
+        size_t s = slot_of[id];
+        counts[id] = cnt[s];
+        if (off + cnt[s] > nbr_cap) return fail(GBMD_E_INVALID, "nbr_cap too small");
+        for (size_t q = 0; q < cnt[s]; q++) nbr[off++] = ids[lst[q * n + s]];
+    }
+    return GBMD_OK;
+}
+
+const char* gbmd_last_error(void) { return t_error.c_str(); }
+const char* gbmd_version(void) { return "gbmd 0.1 (sm_103a)"; }
+
+} // extern "C"
+
+// ------------------------------------------------------------------ observables
+namespace {
+
+// RDF pair counts over unordered pairs of the cell-sorted scratch state: bin
+// floor(sqrt(r2) * scale) with r2 the f64 square of the exact minimum-image separation.
+template <int D>
+__global__ void k_rdf(Params P, const Rec<D>* pos, const uint32_t* keys, const uint32_t* start, uint32_t bins, double scale,
+                      unsigned long long* out) {
+    extern __shared__ uint32_t h[];
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.n) {
+        int64_t xi[3];
+        load_particle<D, false>(pos, nullptr, i, xi);
+        uint32_t c[3];
+        cell_coords(P, keys[i], c);
+        for_cells<D>(P, c, [&](uint32_t cell) {
+            for (uint32_t j = start[cell]; j < start[cell + 1]; j++) {
+                if (j <= i) continue;
+                int64_t xj[3];
+                load_particle<D, false>(pos, nullptr, j, xj);
+                double r2 = 0.0;
+                for (int a = 0; a < D; a++) {
+                    double d = to_f64(min_image(xj[a] - xi[a], P.box[a], P.half[a]));
+                    r2 = __dadd_rn(r2, __dmul_rn(d, d));
+                }
+                double r = __dmul_rn(__dsqrt_rn(r2), scale);
+                if (r < (double)bins) atomicAdd(&h[(uint32_t)r], 1u);
+            }
+        });
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x)
+        if (h[b]) atomicAdd(out + b, (unsigned long long)h[b]);
+}
+
+// Particle counts in slabs along one axis: min(floor(x / L * bins), bins - 1) in f64.
+template <int D>
+__global__ void k_profile(uint32_t n, const Rec<D>* pos, uint32_t axis, double l, uint32_t bins, unsigned long long* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long* p = reinterpret_cast<const long long*>(pos + i);
+    atomicAdd(out + cell_of(p[axis], l, bins), 1ull);
+}
+
+} // namespace
+
+extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint32_t rdf_bins, double rdf_rmax, uint64_t* profile,
+                            uint32_t profile_bins, uint32_t profile_axis) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (rdf && (rdf_bins == 0 || rdf_bins > 8192 || !(rdf_rmax > 0.0))) return fail(GBMD_E_INVALID, "bad RDF arguments");
+    if (profile && (profile_bins == 0 || profile_axis >= (uint32_t)e->D)) return fail(GBMD_E_INVALID, "bad profile arguments");
+    GBMD_TRY(prepare_pairs(e));
+    GBMD_TRY(kicks_dispatch(e, nullptr, e->partial, 0));
+    uint32_t n = e->n, nb = blocks_for(n, 128);
+    std::vector<double> part(4 * (size_t)nb);
+    GBMD_CUDA_TRY(cudaMemcpyAsync(part.data(), e->partial, part.size() * 8, cudaMemcpyDeviceToHost, e->st));
+    unsigned long long* dbuf = nullptr;
+    uint32_t* st2 = nullptr;
+    size_t nbins = (rdf ? rdf_bins : 0) + (profile ? profile_bins : 0);
+    if (nbins) {
+        GBMD_CUDA_TRY(cudaMalloc(&dbuf, nbins * 8));
+        GBMD_CUDA_TRY(cudaMemsetAsync(dbuf, 0, nbins * 8, e->st));
+    }
+    int rc = GBMD_OK;
+    if (rdf) {
+        Params P = e->P;
+        uint32_t nc[3];
+        rc = cells_for(e->sys, rdf_rmax, nc);
+        if (rc == GBMD_OK) {
+            for (int a = 0; a < e->D; a++) P.nc[a] = nc[a];
+            P.ncell = P.nc[0] * P.nc[1] * (e->D == 3 ? P.nc[2] : 1);
+            if (cudaMalloc(&st2, ((size_t)P.ncell + 1) * 4) != cudaSuccess) rc = fail(GBMD_E_NOMEM, "RDF cell starts");
+        }
+        if (rc == GBMD_OK) {
+            uint32_t* saved = e->start;
+            e->start = st2;
+            double scale = (double)rdf_bins / rdf_rmax;
+            size_t shm = (size_t)rdf_bins * 4;
+            if (e->D == 2) {
+                enqueue_bin<2>(e, e->st, P);
+                k_rdf<2><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<2>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, dbuf);
+            } else {
+                enqueue_bin<3>(e, e->st, P);
+                k_rdf<3><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<3>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, dbuf);
+            }
+            note_launch();
+            e->start = saved;
+        }
+    }
+    if (rc == GBMD_OK && profile) {
+        unsigned long long* pbuf = dbuf + (rdf ? rdf_bins : 0);
+        double l = to_f64h(e->sys.box_len[profile_axis]);
+        if (e->D == 2) k_profile<2><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], profile_axis, l, profile_bins, pbuf);
+        else k_profile<3><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<3>*)e->pos[e->cur], profile_axis, l, profile_bins, pbuf);
+        note_launch();
+    }
+    std::vector<uint64_t> hbuf(nbins);
+    if (rc == GBMD_OK && nbins) GBMD_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), dbuf, nbins * 8, cudaMemcpyDeviceToHost, e->st));
+    cudaError_t err = cudaStreamSynchronize(e->st);
+    if (dbuf) cudaFree(dbuf);
+    if (st2) cudaFree(st2);
+    if (rc != GBMD_OK) return rc;
+    if (err != cudaSuccess) return fail(GBMD_E_CUDA, cudaGetErrorString(err));
+    GBMD_TRY(check_ctl(e));
+    if (rdf) std::memcpy(rdf, hbuf.data(), (size_t)rdf_bins * 8);
+    if (profile) std::memcpy(profile, hbuf.data() + (rdf ? rdf_bins : 0), (size_t)profile_bins * 8);
+    if (rdf) {
+        // the RDF binning left the scratch state sorted by its own cells: rebuild before use
+        uint32_t one = 1;
+        GBMD_CUDA_TRY(cudaMemcpy(e->ctl, &one, 4, cudaMemcpyHostToDevice));
+    }
+    if (frame) {
+        double pe = 0.0, w = 0.0, ke = 0.0;
+        for (uint32_t b = 0; b < nb; b++) {
+            pe += part[4 * b];
+            w += part[4 * b + 1];
+            ke += part[4 * b + 2];
+        }
+        double vol = 1.0;
+        for (int a = 0; a < e->D; a++) vol *= to_f64h(e->sys.box_len[a]);
+        double dof = 0.5 * e->D * std::max((double)n - 1.0, 1.0);
+        frame->step = (uint64_t)e->steps;
+        frame->kinetic = ke;
+        frame->potential = pe;
+        frame->virial = w;
+        frame->temperature = ke / dof;
+        frame->pressure = (double)n / vol * frame->temperature + w / (e->D * vol);
+        frame->volume = vol;
+        frame->n = n;
+        frame->dim = (uint32_t)e->D;
+    }
+    return GBMD_OK;
+}
+
+// ------------------------------------------------------------------ seeded init + hashing
+extern "C" int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, int64_t* pos, int32_t* vel, uint32_t* species) {
+    if (!sys || !spec) return fail(GBMD_E_INVALID, "null argument");
+    GBMD_TRY(validate_system(*sys, spec->n));
+    size_t n = spec->n, D = sys->dim;
+    if (n == 0) return GBMD_OK;
+    cudaStream_t s;
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    void* dpos = nullptr;
+    int32_t* dvel = nullptr;
+    uint32_t* dsp = nullptr;
+    int rc = GBMD_OK;
+    if (cudaMalloc(&dpos, n * (D == 2 ? 16 : 32)) != cudaSuccess || cudaMalloc(&dvel, n * D * 4) != cudaSuccess ||
+        cudaMalloc(&dsp, n * 4) != cudaSuccess)
+        rc = fail(GBMD_E_NOMEM, "init buffers");
+    if (rc == GBMD_OK) rc = init_state_device(*sys, *spec, dpos, dvel, dsp, s);
+    std::vector<int64_t> rec;
+    if (rc == GBMD_OK) {
+        rec.resize(n * (D == 2 ? 2 : 4));
+        if (cudaMemcpyAsync(rec.data(), dpos, rec.size() * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "copy");
+        if (vel && cudaMemcpyAsync(vel, dvel, n * D * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "copy");
+        if (species && cudaMemcpyAsync(species, dsp, n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "copy");
+        cudaError_t err = cudaStreamSynchronize(s);
+        if (err != cudaSuccess) rc = fail(GBMD_E_CUDA, cudaGetErrorString(err));
+    }
+    if (rc == GBMD_OK && pos) {
+        size_t w = D == 2 ? 2 : 4;
+        for (size_t i = 0; i < n; i++)
+            for (size_t a = 0; a < D; a++) pos[D * i + a] = rec[w * i + a];
+    }
+    cudaFree(dpos);
+    cudaFree(dvel);
+    cudaFree(dsp);
+    cudaStreamDestroy(s);
+    return rc;
+}
+
+// FNV-1a of an id-ordered state (State::hash, system.rs:460-477; State3::hash, three.rs:281-297).
+extern "C" uint64_t gbmd_hash_state(uint32_t dim, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint32_t n) {
+    uint64_t h = 0xcbf29ce484222325ull;
+    auto eat = [&](const void* p, size_t len) {
+        const uint8_t* b = (const uint8_t*)p;
+        for (size_t k = 0; k < len; k++) {
+            h ^= b[k];
+            h *= 0x100000001b3ull;
+        }
+    };
+    for (size_t i = 0; i < n; i++) {
+        if (dim == 2) {
+            eat(&pos[2 * i], 8);
+            eat(&pos[2 * i + 1], 8);
+            eat(&vel[2 * i], 4);
+            eat(&vel[2 * i + 1], 4);
+        } else {
+            for (int a = 0; a < 3; a++) {
+                eat(&pos[3 * i + a], 8);
+                eat(&vel[3 * i + a], 4);
+            }
+        }
+        eat(&species[i], 4);
+    }
+    return h;
+}

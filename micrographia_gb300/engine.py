@@ -1,0 +1,317 @@
+"""The engines: GpuEngine (2D) and GpuEngine3 (3D) over the C ABI of include/gbmd.h.
+
+Their methods mirror md::GpuEngine (crates/md/src/engine.rs:598-1098) and md::GpuEngine3
+(engine3.rs:334-648): construction from (System, State) with a ForceMode, asynchronous `step`,
+`reverse`, `kicks`, `read_state` (id order), `upload`, `flip_bit`, `read_list_stats`, plus the
+CPU twins' `energy` (int_engine.rs:433-446) and the new FP64 instruments (`observe`).
+"""
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .core import ForceMode, State, State3, System, System3
+
+P = C.POINTER
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(P(t))
+
+
+def _options(mode: ForceMode, threads=0, block_steps=0, rescale_every=0, rescale_t=0.0, arith=_abi.ARITH_F32, device=0):
+    o = _abi.gbmd_options()
+    o.device = device
+    if mode is None:
+        o.mode = _abi.MODE_AUTO
+    elif mode.kind == "cells":
+        o.mode = _abi.MODE_CELLS
+    else:
+        o.mode = _abi.MODE_VERLET
+        o.skin = mode.skin
+        o.cap = mode.cap
+    o.arith = arith
+    o.threads = threads
+    o.block_steps = block_steps
+    o.rescale_every = rescale_every
+    o.rescale_t = rescale_t
+    return o
+
+
+class _Engine:
+    DIM = 2
+    STATE = State
+
+    def __init__(self, sys, state=None, mode=None, *, init=None, threads=0, block_steps=0, rescale_every=0, rescale_t=0.0, device=0):
+        """Create from (sys, state), or from a device-side seeded init (`init` = gbmd_init)."""
+        if sys.DIM != self.DIM:
+            raise ValueError(f"{type(self).__name__} needs a {self.DIM}D system")
+        self.sys = sys
+        self._lib = _abi.lib()
+        self._csys = sys.to_c()
+        self._opts = _options(mode, threads, block_steps, rescale_every, rescale_t, device=device)
+        h = C.c_void_p()
+        if init is not None:
+            _abi.check(self._lib.gbmd_create_seeded(C.byref(self._csys), C.byref(init), C.byref(self._opts), C.byref(h)))
+            self.n = init.n
+        else:
+            self.n = state.n()
+            _abi.check(
+                self._lib.gbmd_create(
+                    C.byref(self._csys),
+                    _ptr(state.pos, C.c_int64),
+                    _ptr(state.vel, C.c_int32),
+                    _ptr(state.species, C.c_uint32),
+                    self.n,
+                    C.byref(self._opts),
+                    C.byref(h),
+                )
+            )
+        self._h = h
+
+    # -- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gbmd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- stepping
+    def step(self, steps=1):
+        _abi.check(self._lib.gbmd_step(self._h, int(steps)))
+
+    def wait(self):
+        _abi.check(self._lib.gbmd_sync(self._h))
+
+    sync = wait
+
+    def reverse(self):
+        _abi.check(self._lib.gbmd_reverse(self._h))
+
+    # -- state
+    def read_state(self):
+        pos = np.empty((self.n, self.DIM), np.int64)
+        vel = np.empty((self.n, self.DIM), np.int32)
+        sp = np.empty(self.n, np.uint32)
+        _abi.check(self._lib.gbmd_read_state(self._h, _ptr(pos, C.c_int64), _ptr(vel, C.c_int32), _ptr(sp, C.c_uint32)))
+        return self.STATE(pos, vel, sp)
+
+    def upload(self, state):
+        if state.n() != self.n:
+            raise ValueError("upload needs the same number of particles")
+        _abi.check(
+            self._lib.gbmd_upload(self._h, _ptr(state.pos, C.c_int64), _ptr(state.vel, C.c_int32), _ptr(state.species, C.c_uint32))
+        )
+
+    def kicks(self):
+        k = np.empty((self.n, self.DIM), np.int32)
+        pe = C.c_double()
+        _abi.check(self._lib.gbmd_kicks(self._h, _ptr(k, C.c_int32), C.byref(pe)))
+        return k, pe.value
+
+    def flip_bit(self, particle, axis, bit):
+        _abi.check(self._lib.gbmd_flip_bit(self._h, particle, axis, bit))
+
+    def energy(self):
+        ke, pe = C.c_double(), C.c_double()
+        _abi.check(self._lib.gbmd_energy(self._h, C.byref(ke), C.byref(pe)))
+        return ke.value, pe.value
+
+    def observe(self, rdf_bins=0, rdf_rmax=5.0, profile_bins=0, profile_axis=0):
+        """One frame: (gbmd_frame, rdf counts or None, profile counts or None)."""
+        f = _abi.gbmd_frame()
+        rdf = np.zeros(rdf_bins, np.uint64) if rdf_bins else None
+        prof = np.zeros(profile_bins, np.uint64) if profile_bins else None
+        _abi.check(
+            self._lib.gbmd_observe(
+                self._h,
+                C.byref(f),
+                _ptr(rdf, C.c_uint64) if rdf is not None else None,
+                rdf_bins,
+                rdf_rmax,
+                _ptr(prof, C.c_uint64) if prof is not None else None,
+                profile_bins,
+                profile_axis,
+            )
+        )
+        return f, rdf, prof
+
+    def read_list_stats(self):
+        r, o = C.c_uint32(), C.c_int32()
+        _abi.check(self._lib.gbmd_list_stats(self._h, C.byref(r), C.byref(o)))
+        return r.value, bool(o.value)
+
+    def state_hash(self):
+        h = C.c_uint64()
+        _abi.check(self._lib.gbmd_state_hash(self._h, C.byref(h)))
+        return h.value
+
+    @property
+    def steps(self):
+        s, c = C.c_int64(), C.c_uint32()
+        _abi.check(self._lib.gbmd_counters(self._h, C.byref(s), C.byref(c)))
+        return s.value
+
+    def stream(self):
+        s = C.c_void_p()
+        _abi.check(self._lib.gbmd_stream(self._h, C.byref(s)))
+        return s.value
+
+    def launch_count(self):
+        c = C.c_uint64()
+        _abi.check(self._lib.gbmd_launch_count(self._h, C.byref(c)))
+        return c.value
+
+    # -- introspection for parity tests
+    def debug_bin(self, cells):
+        cells = (C.c_uint32 * 3)(*(list(cells) + [1] * (3 - len(cells))))
+        ncell = int(np.prod([cells[a] for a in range(self.DIM)]))
+        keys = np.empty(self.n, np.uint32)
+        start = np.empty(ncell + 1, np.uint32)
+        items = np.empty(self.n, np.uint32)
+        order = np.empty(self.n, np.uint32)
+        _abi.check(
+            self._lib.gbmd_debug_bin(
+                self._h, cells, _ptr(keys, C.c_uint32), _ptr(start, C.c_uint32), _ptr(items, C.c_uint32), _ptr(order, C.c_uint32)
+            )
+        )
+        return keys, start, items, order
+
+    def debug_list(self, max_total=None):
+        counts = np.empty(self.n, np.uint32)
+        cap = max_total or self.n * 256
+        nbr = np.empty(cap, np.uint32)
+        _abi.check(self._lib.gbmd_debug_list(self._h, _ptr(counts, C.c_uint32), _ptr(nbr, C.c_uint32), cap))
+        offs = np.concatenate([[0], np.cumsum(counts.astype(np.int64))])
+        return [np.sort(nbr[offs[i] : offs[i + 1]]) for i in range(self.n)]
+
+
+class GpuEngine(_Engine):
+    """md::GpuEngine: 2D. `mode` None selects ForceMode::auto (cell list below 24 000)."""
+
+    DIM = 2
+    STATE = State
+
+    @classmethod
+    def with_mode(cls, sys, state, mode, **kw):
+        return cls(sys, state, mode, **kw)
+
+
+class GpuEngine3(_Engine):
+    """md::GpuEngine3: 3D, Verlet lists by default (engine3.rs:337-340)."""
+
+    DIM = 3
+    STATE = State3
+
+    def __init__(self, sys, state=None, mode=None, **kw):
+        if mode is None:
+            mode = ForceMode.verlet_for(sys, state.n() if state is not None else kw["init"].n)
+        super().__init__(sys, state, mode, **kw)
+
+    @classmethod
+    def with_mode(cls, sys, state, mode, **kw):
+        return cls(sys, state, mode, **kw)
+
+
+def init_state(sys, recipe, n, t, seed, jitter=0.1, rho_liquid=0.7, rho_vapour=0.05, slab_frac=0.25):
+    """Generate a seeded initial state on the device (gbmd_init_state) and return it."""
+    spec = make_init(recipe, n, t, seed, jitter, rho_liquid, rho_vapour, slab_frac)
+    D = sys.DIM
+    pos = np.empty((n, D), np.int64)
+    vel = np.empty((n, D), np.int32)
+    sp = np.empty(n, np.uint32)
+    csys = sys.to_c()
+    _abi.check(
+        _abi.lib().gbmd_init_state(C.byref(csys), C.byref(spec), _ptr(pos, C.c_int64), _ptr(vel, C.c_int32), _ptr(sp, C.c_uint32))
+    )
+    return (State if D == 2 else State3)(pos, vel, sp)
+
+
+def make_init(recipe, n, t, seed, jitter=0.1, rho_liquid=0.7, rho_vapour=0.05, slab_frac=0.25):
+    spec = _abi.gbmd_init()
+    spec.recipe = recipe
+    spec.n = n
+    spec.t = t
+    spec.seed = seed
+    spec.jitter = jitter
+    spec.rho_liquid = rho_liquid
+    spec.rho_vapour = rho_vapour
+    spec.slab_frac = slab_frac
+    return spec
+
+
+class BatchEngine:
+    """Many independent periodic systems stepped together (gbmd_batch_*)."""
+
+    def __init__(self, systems, states, mode=None, threads=0, block_steps=0):
+        self._lib = _abi.lib()
+        if len(systems) != len(states) or not systems:
+            raise ValueError("one state per system")
+        D = systems[0].DIM
+        if any(s.DIM != D for s in systems):
+            raise ValueError("a batch holds systems of one dimension")
+        self.D = D
+        self.count = len(systems)
+        self.sizes = [st.n() for st in states]
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.uint32)
+        csys = (_abi.gbmd_system * self.count)(*[s.to_c() for s in systems])
+        pos = np.ascontiguousarray(np.concatenate([st.pos for st in states]))
+        vel = np.ascontiguousarray(np.concatenate([st.vel for st in states]))
+        sp = np.ascontiguousarray(np.concatenate([st.species for st in states]))
+        opts = _options(mode or ForceMode.verlet_for(systems[0], 0), threads, block_steps)
+        h = C.c_void_p()
+        _abi.check(
+            self._lib.gbmd_batch_create(
+                csys,
+                self.count,
+                _ptr(self.offsets, C.c_uint32),
+                _ptr(pos, C.c_int64),
+                _ptr(vel, C.c_int32),
+                _ptr(sp, C.c_uint32),
+                C.byref(opts),
+                C.byref(h),
+            )
+        )
+        self._h = h
+
+    def step(self, steps=1):
+        _abi.check(self._lib.gbmd_batch_step(self._h, int(steps)))
+
+    def wait(self):
+        _abi.check(self._lib.gbmd_batch_sync(self._h))
+
+    def read_system(self, k):
+        n = self.sizes[k]
+        pos = np.empty((n, self.D), np.int64)
+        vel = np.empty((n, self.D), np.int32)
+        sp = np.empty(n, np.uint32)
+        _abi.check(self._lib.gbmd_batch_read_system(self._h, k, _ptr(pos, C.c_int64), _ptr(vel, C.c_int32), _ptr(sp, C.c_uint32)))
+        return (State if self.D == 2 else State3)(pos, vel, sp)
+
+    def stream(self):
+        s = C.c_void_p()
+        _abi.check(self._lib.gbmd_batch_stream(self._h, C.byref(s)))
+        return s.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gbmd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,310 @@
+// ORACLE — test infrastructure only: a C API over oracle.hpp for the Python parity tests and the
+// CPU baseline. The engine never links or calls it.
+#include <cstring>
+#include <memory>
+
+#include "oracle.hpp"
+
+using namespace oracle;
+
+namespace {
+
+State make_state(int dim, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint64_t n) {
+    State s;
+    s.dim = dim;
+    s.pos.assign(pos, pos + dim * n);
+    s.vel.assign(vel, vel + dim * n);
+    s.species.assign(species, species + n);
+    return s;
+}
+State make_state_pos(int dim, const int64_t* pos, const uint32_t* species, uint64_t n) {
+    State s;
+    s.dim = dim;
+    s.pos.assign(pos, pos + dim * n);
+    s.vel.assign(dim * n, 0);
+    if (species) s.species.assign(species, species + n);
+    else s.species.assign(n, 0);
+    return s;
+}
+
+struct Engine {
+    std::unique_ptr<IntEngine<float>> f32;
+    std::unique_ptr<IntEngine<double>> f64;
+    State& state() { return f32 ? f32->state : f64->state; }
+};
+
+} // namespace
+
+extern "C" {
+
+// ---- fixed point, RNG, libm restatement
+int oracle_sep_f32(int64_t d, float* out) { return sep_f32(d, out) ? 1 : 0; }
+float oracle_sep_near(int64_t d) { return sep_near_f32(d); }
+void oracle_threefry(uint32_t c0, uint32_t c1, uint32_t k0, uint32_t k1, uint32_t rounds, uint32_t* out) {
+    auto r = threefry2x32_rounds({c0, c1}, {k0, k1}, rounds);
+    out[0] = r[0];
+    out[1] = r[1];
+}
+double oracle_uniform(uint64_t seed, uint32_t stream, uint32_t i) { return uniform(seed, stream, i); }
+double oracle_normal(uint64_t seed, uint32_t stream, uint32_t i) { return normal(seed, stream, i); }
+double oracle_log(double x) { return fdlibm::log(x); }
+double oracle_cos(double x) { return fdlibm::cos(x); }
+int64_t oracle_to_fixed(double x) { return to_fixed(x); }
+
+// ---- System helpers
+void oracle_box_for(uint64_t n, double density, double aspect, int64_t* out) {
+    auto b = box_for(n, density, aspect);
+    out[0] = b[0];
+    out[1] = b[1];
+}
+void oracle_cube_for(uint64_t n, double density, int64_t* out) {
+    auto b = cube_for(n, density);
+    for (int a = 0; a < 3; a++) out[a] = b[a];
+}
+void oracle_fcc_cells(uint64_t n, const int64_t* box, uint64_t* out) {
+    auto c = fcc_cells(n, {box[0], box[1], box[2]});
+    for (int a = 0; a < 3; a++) out[a] = c[a];
+}
+int oracle_cells_for(const gbmd_system* csys, double r, uint32_t* out) {
+    try {
+        auto c = System::from_c(*csys).cells_for(r);
+        for (int a = 0; a < 3; a++) out[a] = c[a];
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+double oracle_wca_rc(void) { return Pair::wca().rc; }
+double oracle_pair_shift(double eps, double sigma, double rc) { return Pair{eps, sigma, rc}.shift(); }
+
+// ---- initial conditions (md-core init.rs / three.rs and this engine's recipes)
+void oracle_lattice(uint64_t n, const int64_t* box, double jitter, uint64_t seed, int64_t* pos) {
+    auto p = lattice(n, {box[0], box[1]}, jitter, seed);
+    std::memcpy(pos, p.data(), p.size() * 8);
+}
+void oracle_fcc(uint64_t n, const int64_t* box, const uint64_t* cells, double jitter, uint64_t seed, int64_t* pos) {
+    auto p = fcc(n, {box[0], box[1], box[2]}, {cells[0], cells[1], cells[2]}, jitter, seed);
+    std::memcpy(pos, p.data(), p.size() * 8);
+}
+void oracle_maxwell(const gbmd_system* csys, const uint32_t* species, uint64_t n, double t, uint64_t seed, int32_t* vel) {
+    System sys = System::from_c(*csys);
+    std::vector<uint32_t> sp(species, species + n);
+    auto v = maxwell(sys, sp, t, seed);
+    std::memcpy(vel, v.data(), v.size() * 4);
+}
+void oracle_zero_velocity_sum(const gbmd_system* csys, const uint32_t* species, uint64_t n, int32_t* vel) {
+    System sys = System::from_c(*csys);
+    std::vector<uint32_t> sp(species, species + n);
+    std::vector<int32_t> v(vel, vel + sys.dim * n);
+    zero_velocity_sum(sys, sp, v, sys.dim == 3);
+    std::memcpy(vel, v.data(), v.size() * 4);
+}
+void oracle_set_temperature(const gbmd_system* csys, int32_t* vel, const uint32_t* species, uint64_t n, double t, int exact) {
+    System sys = System::from_c(*csys);
+    State s;
+    s.dim = sys.dim;
+    s.vel.assign(vel, vel + sys.dim * n);
+    s.species.assign(species, species + n);
+    s.pos.assign(sys.dim * n, 0);
+    if (exact) rescale_temperature(s, sys, t);
+    else set_temperature(s, sys, t);
+    std::memcpy(vel, s.vel.data(), s.vel.size() * 4);
+}
+double oracle_exact_kinetic(const gbmd_system* csys, const int32_t* vel, const uint32_t* species, uint64_t n) {
+    System sys = System::from_c(*csys);
+    State s;
+    s.dim = sys.dim;
+    s.vel.assign(vel, vel + sys.dim * n);
+    s.species.assign(species, species + n);
+    return exact_half_step_kinetic(sys, s);
+}
+double oracle_half_step_kinetic(const gbmd_system* csys, const int32_t* vel, const uint32_t* species, uint64_t n) {
+    System sys = System::from_c(*csys);
+    State s;
+    s.dim = sys.dim;
+    s.vel.assign(vel, vel + sys.dim * n);
+    s.species.assign(species, species + n);
+    return half_step_kinetic(sys, s);
+}
+// The recipes of gbmd_init_state, restated on the CPU.
+int oracle_init(const gbmd_system* csys, const gbmd_init* spec, int64_t* pos, int32_t* vel, uint32_t* species) {
+    try {
+        System sys = System::from_c(*csys);
+        size_t n = spec->n;
+        State st;
+        switch (spec->recipe) {
+            case GBMD_INIT_FLUID: {
+                st.dim = 2;
+                st.pos = lattice(n, {sys.box[0], sys.box[1]}, spec->jitter, spec->seed);
+                st.species.assign(n, 0);
+                st.vel = maxwell(sys, st.species, spec->t, spec->seed);
+                break;
+            }
+            case GBMD_INIT_TRIANGULAR: {
+                st.dim = 2;
+                st.pos = triangular(n, {sys.box[0], sys.box[1]}, {0, 0}, {sys.box[0], sys.box[1]}, spec->jitter, spec->seed, 0);
+                st.species.assign(n, 0);
+                st.vel = maxwell(sys, st.species, spec->t, spec->seed);
+                break;
+            }
+            case GBMD_INIT_FCC: {
+                st.dim = 3;
+                std::array<int64_t, 3> b{sys.box[0], sys.box[1], sys.box[2]};
+                st.pos = fcc(n, b, fcc_cells(n, b), spec->jitter, spec->seed);
+                st.species.assign(n, 0);
+                st.vel = maxwell(sys, st.species, spec->t, spec->seed);
+                break;
+            }
+            case GBMD_INIT_SLAB:
+                st = slab(sys, n, spec->rho_liquid, spec->rho_vapour, spec->slab_frac, spec->t, spec->jitter, spec->seed);
+                break;
+            default:
+                return -1;
+        }
+        if (pos) std::memcpy(pos, st.pos.data(), st.pos.size() * 8);
+        if (vel) std::memcpy(vel, st.vel.data(), st.vel.size() * 4);
+        if (species) std::memcpy(species, st.species.data(), st.species.size() * 4);
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// ---- cells and Verlet lists
+int oracle_cell_list(const gbmd_system* csys, const int64_t* pos, uint64_t n, const uint32_t* dims, uint32_t* keys, uint32_t* start,
+                     uint32_t* items) {
+    System sys = System::from_c(*csys);
+    State s = make_state_pos(sys.dim, pos, nullptr, n);
+    CellList cl = build_cells(sys, s, {dims[0], dims[1], dims[2]});
+    std::memcpy(keys, cl.keys.data(), n * 4);
+    std::memcpy(start, cl.start.data(), cl.start.size() * 4);
+    std::memcpy(items, cl.items.data(), n * 4);
+    return 0;
+}
+uint32_t oracle_verlet_cap(const gbmd_system* csys, uint64_t n, double skin) { return verlet_cap(System::from_c(*csys), n, skin); }
+// Lists packed particle by particle (sorted indices); returns the total, or -1 past `cap` entries.
+int64_t oracle_verlet_list(const gbmd_system* csys, const int64_t* pos, const uint32_t* species, uint64_t n, double skin, uint32_t* counts,
+                           uint32_t* nbr, uint64_t cap) {
+    System sys = System::from_c(*csys);
+    State s = make_state_pos(sys.dim, pos, species, n);
+    auto lists = verlet_lists(sys, s, skin);
+    uint64_t off = 0;
+    for (size_t i = 0; i < n; i++) {
+        counts[i] = (uint32_t)lists[i].size();
+        if (off + lists[i].size() > cap) return -1;
+        std::memcpy(nbr + off, lists[i].data(), lists[i].size() * 4);
+        off += lists[i].size();
+    }
+    return (int64_t)off;
+}
+
+// ---- engines
+void* oracle_engine_create(const gbmd_system* csys, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint64_t n, int use_f64,
+                           int fast, int int_tables, int threads) {
+    try {
+        System sys = System::from_c(*csys);
+        State s = make_state(sys.dim, pos, vel, species, n);
+        auto* e = new Engine;
+        if (use_f64) {
+            e->f64.reset(new IntEngine<double>(sys, s));
+            e->f64->fast = fast != 0;
+            e->f64->threads = threads > 0 ? threads : 1;
+            if (int_tables) e->f64->use_integer_tables();
+        } else {
+            e->f32.reset(new IntEngine<float>(sys, s));
+            e->f32->fast = fast != 0;
+            e->f32->threads = threads > 0 ? threads : 1;
+            if (int_tables) e->f32->use_integer_tables();
+        }
+        return e;
+    } catch (...) {
+        return nullptr;
+    }
+}
+void oracle_engine_destroy(void* h) { delete (Engine*)h; }
+void oracle_engine_step(void* h, uint64_t steps) {
+    Engine* e = (Engine*)h;
+    if (e->f32) e->f32->step(steps);
+    else e->f64->step(steps);
+}
+void oracle_engine_reverse(void* h) {
+    Engine* e = (Engine*)h;
+    if (e->f32) e->f32->reverse();
+    else e->f64->reverse();
+}
+double oracle_engine_kicks(void* h, int32_t* kicks) {
+    Engine* e = (Engine*)h;
+    std::vector<int32_t> k;
+    double pe = e->f32 ? e->f32->forces(k) : e->f64->forces(k);
+    std::memcpy(kicks, k.data(), k.size() * 4);
+    return pe;
+}
+void oracle_engine_state(void* h, int64_t* pos, int32_t* vel, uint32_t* species) {
+    State& s = ((Engine*)h)->state();
+    if (pos) std::memcpy(pos, s.pos.data(), s.pos.size() * 8);
+    if (vel) std::memcpy(vel, s.vel.data(), s.vel.size() * 4);
+    if (species) std::memcpy(species, s.species.data(), s.species.size() * 4);
+}
+void oracle_engine_set_state(void* h, const int64_t* pos, const int32_t* vel, const uint32_t* species) {
+    State& s = ((Engine*)h)->state();
+    std::memcpy(s.pos.data(), pos, s.pos.size() * 8);
+    std::memcpy(s.vel.data(), vel, s.vel.size() * 4);
+    std::memcpy(s.species.data(), species, s.species.size() * 4);
+}
+uint64_t oracle_engine_hash(void* h) { return ((Engine*)h)->state().hash(); }
+int64_t oracle_engine_steps(void* h) {
+    Engine* e = (Engine*)h;
+    return e->f32 ? e->f32->steps : e->f64->steps;
+}
+void oracle_engine_energy(void* h, double* ke, double* pe) {
+    Engine* e = (Engine*)h;
+    Energy en = e->f32 ? e->f32->energy() : e->f64->energy();
+    *ke = en.kinetic;
+    *pe = en.potential;
+}
+uint64_t oracle_state_hash(uint32_t dim, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint64_t n) {
+    return make_state((int)dim, pos, vel, species, n).hash();
+}
+
+void* oracle_float_create(const gbmd_system* csys, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint64_t n) {
+    System sys = System::from_c(*csys);
+    return new FloatEngine(sys, make_state(2, pos, vel, species, n));
+}
+void oracle_float_destroy(void* h) { delete (FloatEngine*)h; }
+void oracle_float_step(void* h, uint64_t steps) { ((FloatEngine*)h)->step(steps); }
+void oracle_float_positions(void* h, double* out) {
+    auto* e = (FloatEngine*)h;
+    std::memcpy(out, e->pos.data(), e->pos.size() * 8);
+}
+void oracle_float_energy(void* h, double* ke, double* pe) {
+    Energy en = ((FloatEngine*)h)->energy();
+    *ke = en.kinetic;
+    *pe = en.potential;
+}
+
+// ---- instruments
+void oracle_pair_sums(const gbmd_system* csys, const int64_t* pos, const uint32_t* species, uint64_t n, double* pe, double* virial) {
+    System sys = System::from_c(*csys);
+    PairSums ps = pair_sums_f32(sys, make_state_pos(sys.dim, pos, species, n));
+    *pe = ps.potential;
+    *virial = ps.virial;
+}
+void oracle_rdf(const gbmd_system* csys, const int64_t* pos, uint64_t n, uint32_t bins, double rmax, uint64_t* out) {
+    System sys = System::from_c(*csys);
+    auto h = rdf_counts(sys, make_state_pos(sys.dim, pos, nullptr, n), bins, rmax);
+    std::memcpy(out, h.data(), bins * 8);
+}
+void oracle_profile(const gbmd_system* csys, const int64_t* pos, uint64_t n, uint32_t bins, uint32_t axis, uint64_t* out) {
+    System sys = System::from_c(*csys);
+    auto h = density_profile(sys, make_state_pos(sys.dim, pos, nullptr, n), bins, (int)axis);
+    std::memcpy(out, h.data(), bins * 8);
+}
+
+// ---- all-integer tables (md-core table.rs)
+int oracle_int_kick(const gbmd_system* csys, uint32_t sa, uint32_t sb, const int64_t* d, int32_t* out) {
+    System sys = System::from_c(*csys);
+    IntTables t(sys);
+    return t.kick(sa, sb, d, sys.dim, out) ? 1 : 0;
+}
+
+} // extern "C"

@@ -1,0 +1,1322 @@
+// ORACLE — test infrastructure only. Only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline may load it, as the checker; the engine never links or calls it.
+//
+// A C++17 restatement of micrographia's CPU semantics for the integer fixed-point LJ path:
+//   gpu-prims: threefry.rs (Threefry-2x32, uniforms, Box–Muller), fixed64.rs
+//   md-core:   fixed.rs, pair.rs, system.rs (System/State subset), init.rs, three.rs, table.rs
+//   md-ref:    real.rs (f32/f64 Real semantics), cells.rs, int_engine.rs (periodic NVE subset),
+//              int_engine3.rs, fast.rs (the SIMD fast path: the timed CPU baseline),
+//              float_engine.rs
+//   md:        the Verlet-list definition of shaders/neighbors.wgsl:27-64 / md3.wgsl:443-483
+// plus f64 instruments the reference lacks (virial pressure after mc/src/gibbs.rs:58-66,
+// 381-390; RDF; density profile; exact-integer velocity rescale).
+//
+// Rust semantics restated exactly: `as` float->int casts saturate and send NaN to 0; i32 sums
+// wrap; `round_ties_even` is rint in the default rounding mode; `f64::round` is round();
+// nothing is contracted into FMAs (compile with -ffp-contract=off, no fast-math).
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+#include "../include/gbmd.h"
+#include "fdlibm.hpp"
+
+namespace oracle {
+
+// ---------------------------------------------------------------- Rust cast semantics
+inline int32_t sat_i32(double x) {
+    if (x != x) return 0;
+    if (x >= 2147483647.0) return INT32_MAX;
+    if (x <= -2147483648.0) return INT32_MIN;
+    return (int32_t)x;
+}
+inline int32_t sat_i32f(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)x;
+}
+inline uint32_t sat_u32(double x) {
+    if (!(x > 0.0)) return 0;
+    if (x >= 4294967295.0) return UINT32_MAX;
+    return (uint32_t)x;
+}
+inline int64_t sat_i64(double x) {
+    if (x != x) return 0;
+    if (x >= 9223372036854775807.0) return INT64_MAX;
+    if (x <= -9223372036854775808.0) return INT64_MIN;
+    return (int64_t)x;
+}
+inline int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+inline int32_t wneg(int32_t a) { return (int32_t)(0u - (uint32_t)a); }
+inline int64_t div_euclid(int64_t a, int64_t b) {
+    int64_t q = a / b, r = a % b;
+    if (r < 0) q = b > 0 ? q - 1 : q + 1;
+    return q;
+}
+inline int64_t rem_euclid(int64_t a, int64_t b) {
+    int64_t r = a % b;
+    if (r < 0) r += b < 0 ? -b : b;
+    return r;
+}
+// LLVM's expansion of powi(x, n) for a constant n > 0 (binary powering, as compiler-rt's
+// __powidf2): the result Rust's f64::powi gives.
+inline double powi(double x, int n) {
+    double res = 1.0;
+    bool have = false;
+    double sq = x;
+    while (n) {
+        if (n & 1) {
+            res = have ? res * sq : sq;
+            have = true;
+        }
+        n >>= 1;
+        if (n) sq = sq * sq;
+    }
+    return have ? res : 1.0;
+}
+
+// ---------------------------------------------------------------- gpu-prims/src/threefry.rs
+inline uint32_t rotl(uint32_t x, uint32_t r) { return (x << r) | (x >> (32 - r)); }
+// threefry.rs:7-22
+inline std::array<uint32_t, 2> threefry2x32_rounds(std::array<uint32_t, 2> ctr, std::array<uint32_t, 2> key, uint32_t rounds) {
+    static const uint32_t ROT[8] = {13, 15, 26, 6, 17, 29, 16, 24};
+    const uint32_t ks[3] = {key[0], key[1], 0x1BD11BDAu ^ key[0] ^ key[1]};
+    uint32_t x0 = ctr[0] + ks[0];
+    uint32_t x1 = ctr[1] + ks[1];
+    for (uint32_t r = 0; r < rounds; r++) {
+        x0 += x1;
+        x1 = rotl(x1, ROT[r % 8]);
+        x1 ^= x0;
+        if ((r & 3) == 3) {
+            uint32_t s = (r >> 2) + 1;
+            x0 += ks[s % 3];
+            x1 += ks[(s + 1) % 3] + s;
+        }
+    }
+    return {x0, x1};
+}
+inline std::array<uint32_t, 2> threefry2x32(std::array<uint32_t, 2> ctr, std::array<uint32_t, 2> key) {
+    return threefry2x32_rounds(ctr, key, 20);
+}
+// threefry.rs:29-32
+inline double to_unit_f64(std::array<uint32_t, 2> r) {
+    uint64_t b = ((uint64_t)r[0] << 21) ^ ((uint64_t)r[1] >> 11);
+    return (double)(b & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0);
+}
+// threefry.rs:35-37
+inline double uniform(uint64_t seed, uint32_t stream, uint32_t i) {
+    return to_unit_f64(threefry2x32({i, stream}, {(uint32_t)seed, (uint32_t)(seed >> 32)}));
+}
+// threefry.rs:42-46 (libm sqrt, log, cos)
+inline double normal(uint64_t seed, uint32_t stream, uint32_t i) {
+    double u1 = 1.0 - uniform(seed, stream, 2 * i);
+    double u2 = uniform(seed, stream, 2 * i + 1);
+    return std::sqrt(-2.0 * fdlibm::log(u1)) * fdlibm::cos(6.28318530717958647692 * u2);
+}
+
+// ---------------------------------------------------------------- md-core/src/fixed.rs
+constexpr int64_t ONE = (int64_t)1 << 32;
+constexpr double UNIT = 1.0 / 4294967296.0;
+constexpr int64_t SEP_LIMIT = 8 * ONE;
+constexpr float SEP_UNIT_F32 = 1.0f / 268435456.0f; /* 2^-28 */
+
+inline int64_t to_fixed(double x) { return sat_i64(std::round(x * 4294967296.0)); } // fixed.rs:21-23
+inline double to_f64(int64_t x) { return (double)x * UNIT; }                       // fixed.rs:25-27
+inline int64_t min_image(int64_t a, int64_t b, int64_t l) {                         // fixed.rs:31-40
+    int64_t d = b - a, half = l / 2;
+    if (d >= half) d -= l;
+    else if (d < -half) d += l;
+    return d;
+}
+inline int64_t wrap(int64_t x, int64_t l) { return x < 0 ? x + l : (x >= l ? x - l : x); } // 43-51
+// fixed.rs:55-61: separation as f32 through 2^-28 sigma units, or none beyond 8 sigma.
+inline bool sep_f32(int64_t d, float* out) {
+    if (!(d >= -SEP_LIMIT && d < SEP_LIMIT)) return false;
+    uint64_t m = d < 0 ? (uint64_t)0 - (uint64_t)d : (uint64_t)d;
+    float mag = (float)(uint32_t)(m >> 4) * SEP_UNIT_F32;
+    *out = d < 0 ? -mag : mag;
+    return true;
+}
+// md-ref real.rs:59-64: branch-free sep for |d| < 8 sigma, bit-identical to sep_f32.
+inline float sep_near_f32(int64_t d) {
+    int64_t q = (d + ((d >> 63) & 15)) >> 4;
+    float v = (float)(int32_t)q * SEP_UNIT_F32;
+    uint32_t vb;
+    std::memcpy(&vb, &v, 4);
+    vb |= (uint32_t)(d >> 32) & 0x80000000u;
+    std::memcpy(&v, &vb, 4);
+    return v;
+}
+
+// ---------------------------------------------------------------- md-core/src/pair.rs
+struct Pair {
+    double eps = 1.0, sigma = 1.0, rc = 2.5;
+    static Pair lj(double rc) { return {1.0, 1.0, rc}; }
+    static Pair wca() { return {1.0, 1.0, std::pow(2.0, 1.0 / 6.0)}; }
+    double shift() const { // pair.rs:28-34
+        if (eps == 0.0 || rc == 0.0) return 0.0;
+        double s6 = powi(sigma / rc, 6);
+        return 4.0 * eps * s6 * (s6 - 1.0);
+    }
+    double energy(double r2) const { // pair.rs:36-42
+        if (r2 >= rc * rc) return 0.0;
+        double s6 = powi(sigma * sigma / r2, 3);
+        return 4.0 * eps * s6 * (s6 - 1.0) - shift();
+    }
+    double f_over_r(double r2) const { // pair.rs:45-51
+        if (r2 >= rc * rc) return 0.0;
+        double s6 = powi(sigma * sigma / r2, 3);
+        return 24.0 * eps * s6 * (2.0 * s6 - 1.0) / r2;
+    }
+};
+
+// ---------------------------------------------------------------- md-core System / System3
+// The periodic LJ subset of System (system.rs:26-64) and System3 (three.rs:13-31).
+struct System {
+    int dim = 2;
+    std::array<int64_t, 3> box{0, 0, 0};
+    double dt = 0.005;
+    std::vector<double> masses{1.0};
+    std::vector<Pair> pairs{Pair::lj(2.5)};
+    std::array<double, 3> gravity{0, 0, 0};
+    uint64_t seed = 1;
+    uint32_t pinned = 0;
+
+    static System from_c(const gbmd_system& s) {
+        System o;
+        o.dim = (int)s.dim;
+        for (int a = 0; a < 3; a++) o.box[a] = s.box_len[a];
+        o.dt = s.dt;
+        o.masses.assign(s.masses, s.masses + s.nspecies);
+        o.pairs.clear();
+        for (uint32_t k = 0; k < s.nspecies * s.nspecies; k++) o.pairs.push_back({s.pairs[k].eps, s.pairs[k].sigma, s.pairs[k].rc});
+        for (int a = 0; a < 3; a++) o.gravity[a] = s.gravity[a];
+        o.seed = s.seed;
+        o.pinned = s.pinned;
+        return o;
+    }
+    int species() const { return (int)masses.size(); }
+    const Pair& pair(uint32_t a, uint32_t b) const { return pairs[a * masses.size() + b]; }
+    bool is_pinned(uint32_t s) const { return (pinned >> s) & 1u; }
+    double rc_max() const {
+        double r = 0.0;
+        for (auto& p : pairs) r = std::max(r, p.rc);
+        return r;
+    }
+    double box_f64(int a) const { return to_f64(box[a]); }
+    double volume() const {
+        double v = 1.0;
+        for (int a = 0; a < dim; a++) v *= box_f64(a);
+        return v;
+    }
+    // system.rs:415-420 / three.rs:134-139
+    double kick_coeff(uint32_t s) const {
+        if (is_pinned(s)) return 0.0;
+        return dt * dt / masses[s] * 4294967296.0;
+    }
+    double velocity(int32_t v) const { return (double)v * UNIT / dt; }                      // 423-425
+    int32_t to_step_displacement(double v) const { return sat_i32(std::round(v * dt * 4294967296.0)); } // 427-429
+    // system.rs:399-402: the same for every species.
+    std::array<int32_t, 3> gravity_kick() const {
+        std::array<int32_t, 3> g{0, 0, 0};
+        for (int a = 0; a < dim; a++) g[a] = sat_i32(std::round(gravity[a] * dt * dt * 4294967296.0));
+        return g;
+    }
+    // system.rs:438-444 / three.rs:151-157
+    std::array<uint32_t, 3> cells_for(double r) const {
+        double bmax = 0.0;
+        for (int a = 0; a < dim; a++) bmax = std::max(bmax, box_f64(a));
+        double margin = 1e-3 + 1e-6 * bmax;
+        std::array<uint32_t, 3> c{1, 1, 1};
+        for (int a = 0; a < dim; a++) {
+            c[a] = sat_u32(std::floor(box_f64(a) / (r + margin)));
+            if (c[a] < 3) throw std::invalid_argument("box too small for the cell radius");
+        }
+        return c;
+    }
+};
+
+// Positions, half-step velocities and species, interleaved like md-core's State / State3.
+struct State {
+    int dim = 2;
+    std::vector<int64_t> pos; // n * dim
+    std::vector<int32_t> vel; // n * dim
+    std::vector<uint32_t> species;
+    size_t n() const { return species.size(); }
+    // system.rs:460-477 (2D: x, y, vx, vy, s) and three.rs:281-297 (3D: (x, vx) per axis, s).
+    uint64_t hash() const {
+        uint64_t h = 0xcbf29ce484222325ull;
+        auto eat = [&](const void* p, size_t len) {
+            const uint8_t* b = (const uint8_t*)p;
+            for (size_t k = 0; k < len; k++) {
+                h ^= b[k];
+                h *= 0x100000001b3ull;
+            }
+        };
+        for (size_t i = 0; i < n(); i++) {
+            if (dim == 2) {
+                eat(&pos[2 * i], 8);
+                eat(&pos[2 * i + 1], 8);
+                eat(&vel[2 * i], 4);
+                eat(&vel[2 * i + 1], 4);
+            } else {
+                for (int a = 0; a < 3; a++) {
+                    eat(&pos[3 * i + a], 8);
+                    eat(&vel[3 * i + a], 4);
+                }
+            }
+            eat(&species[i], 4);
+        }
+        return h;
+    }
+};
+
+// ---------------------------------------------------------------- md-core/src/init.rs
+constexpr uint32_t STREAM_VELOCITY = 1, STREAM_JITTER = 2, STREAM_DIRECTION = 3;
+// New streams of this engine's own recipes (slab vapour placement).
+constexpr uint32_t STREAM_VAPOUR = 4;
+
+// init.rs:15-19
+inline std::array<int64_t, 2> box_for(size_t n, double density, double aspect) {
+    double area = (double)n / density;
+    double ly = std::sqrt(area / aspect);
+    return {to_fixed(ly * aspect), to_fixed(ly)};
+}
+// init.rs:22-38
+inline std::vector<int64_t> lattice(size_t n, std::array<int64_t, 2> box, double jitter, uint64_t seed) {
+    double b0 = to_f64(box[0]), b1 = to_f64(box[1]);
+    size_t nx = std::max<size_t>((size_t)sat_u32(std::ceil(std::sqrt((double)n * b0 / b1))), 1);
+    size_t ny = (n + nx - 1) / nx;
+    double a0 = b0 / (double)nx, a1 = b1 / (double)ny;
+    std::vector<int64_t> pos(2 * n);
+    for (size_t k = 0; k < n; k++) {
+        size_t i = k % nx, j = k / nx;
+        double jx = jitter * (uniform(seed, STREAM_JITTER, 2 * (uint32_t)k) - 0.5);
+        double jy = jitter * (uniform(seed, STREAM_JITTER, 2 * (uint32_t)k + 1) - 0.5);
+        pos[2 * k] = wrap(to_fixed(((double)i + 0.5) * a0 + jx), box[0]);
+        pos[2 * k + 1] = wrap(to_fixed(((double)j + 0.5) * a1 + jy), box[1]);
+    }
+    return pos;
+}
+// init.rs:76-89 (2D) and three.rs:376-389 (over moving particles; pinned excluded).
+inline void zero_velocity_sum(const System& sys, const std::vector<uint32_t>& species, std::vector<int32_t>& vel, bool skip_pinned) {
+    int d = sys.dim;
+    size_t n = species.size();
+    std::vector<size_t> moving;
+    for (size_t i = 0; i < n; i++)
+        if (!skip_pinned || !sys.is_pinned(species[i])) moving.push_back(i);
+    int64_t m = (int64_t)moving.size();
+    if (m == 0) return;
+    for (int a = 0; a < d; a++) {
+        int64_t sum = 0;
+        for (size_t i : moving) sum += vel[d * i + a];
+        int64_t q = div_euclid(sum, m), r = rem_euclid(sum, m);
+        for (size_t k = 0; k < moving.size(); k++) {
+            size_t i = moving[k];
+            vel[d * i + a] = wadd(vel[d * i + a], wneg((int32_t)(q + ((int64_t)k < r ? 1 : 0))));
+        }
+    }
+}
+// init.rs:42-57 (2D; counter 2i + a) and three.rs:359-373 (3D; counter 3i + a, pinned -> 0).
+inline std::vector<int32_t> maxwell(const System& sys, const std::vector<uint32_t>& species, double t, uint64_t seed) {
+    int d = sys.dim;
+    size_t n = species.size();
+    std::vector<int32_t> vel(d * n, 0);
+    for (size_t i = 0; i < n; i++) {
+        uint32_t s = species[i];
+        if (d == 3 && sys.is_pinned(s)) continue;
+        double sd = std::sqrt(t / sys.masses[s]);
+        for (int a = 0; a < d; a++)
+            vel[d * i + a] = sys.to_step_displacement(sd * normal(seed, STREAM_VELOCITY, (uint32_t)d * (uint32_t)i + (uint32_t)a));
+    }
+    zero_velocity_sum(sys, species, vel, d == 3);
+    return vel;
+}
+// init.rs:105-121, periodic axes only (no wall margin).
+inline State fluid(const System& sys, size_t n, double t, uint64_t seed) {
+    State s;
+    s.dim = 2;
+    s.pos = lattice(n, {sys.box[0], sys.box[1]}, 0.1, seed);
+    s.species.assign(n, 0);
+    s.vel = maxwell(sys, s.species, t, seed);
+    return s;
+}
+// init.rs:92-103 / three.rs:392-404: half-step kinetic temperature rescale.
+inline double half_step_kinetic(const System& sys, const State& s) {
+    double ke = 0.0;
+    int d = sys.dim;
+    for (size_t i = 0; i < s.n(); i++) {
+        if (d == 3 && sys.is_pinned(s.species[i])) continue;
+        double m = sys.masses[s.species[i]];
+        if (d == 2) {
+            double vx = sys.velocity(s.vel[2 * i]), vy = sys.velocity(s.vel[2 * i + 1]);
+            ke += 0.5 * m * (vx * vx + vy * vy);
+        } else {
+            double acc = 0.0;
+            for (int a = 0; a < 3; a++) acc += powi(sys.velocity(s.vel[3 * i + a]), 2);
+            ke += 0.5 * m * acc;
+        }
+    }
+    return ke;
+}
+inline void set_temperature(State& s, const System& sys, double t) {
+    int d = sys.dim;
+    size_t moving = 0;
+    for (size_t i = 0; i < s.n(); i++)
+        if (d == 2 || !sys.is_pinned(s.species[i])) moving++;
+    double dof = d == 2 ? std::max((double)s.n() - 1.0, 1.0) : 1.5 * std::max((double)moving - 1.0, 1.0);
+    double now = half_step_kinetic(sys, s) / dof;
+    if (now <= 0.0) return;
+    double f = std::sqrt(t / now);
+    for (auto& v : s.vel) v = sat_i32(std::round((double)v * f));
+    zero_velocity_sum(sys, s.species, s.vel, d == 3);
+}
+
+// three.rs:312-315
+inline std::array<int64_t, 3> cube_for(size_t n, double density) {
+    int64_t l = to_fixed(std::cbrt((double)n / density));
+    return {l, l, l};
+}
+// three.rs:346-355
+inline std::array<size_t, 3> fcc_cells(size_t n, std::array<int64_t, 3> box) {
+    double b[3] = {to_f64(box[0]), to_f64(box[1]), to_f64(box[2])};
+    double a = std::cbrt(b[0] * b[1] * b[2] * 4.0 / (double)n);
+    std::array<size_t, 3> c;
+    for (int k = 0; k < 3; k++) c[k] = std::max<size_t>((size_t)sat_u32(std::round(b[k] / a)), 1);
+    while (4 * c[0] * c[1] * c[2] < n) {
+        // the axis with the largest lattice constant (min_by of the reversed total order: the
+        // first maximum)
+        int k = 0;
+        for (int x = 1; x < 3; x++)
+            if (b[x] / (double)c[x] > b[k] / (double)c[k]) k = x;
+        c[k]++;
+    }
+    return c;
+}
+// three.rs:319-343
+inline std::vector<int64_t> fcc(size_t n, std::array<int64_t, 3> box, std::array<size_t, 3> cells, double jitter, uint64_t seed) {
+    static const double basis[4][3] = {{0.25, 0.25, 0.25}, {0.75, 0.75, 0.25}, {0.75, 0.25, 0.75}, {0.25, 0.75, 0.75}};
+    double a[3];
+    for (int k = 0; k < 3; k++) a[k] = to_f64(box[k]) / (double)cells[k];
+    std::vector<int64_t> out;
+    out.reserve(3 * n);
+    for (size_t k = 0; k < cells[2]; k++)
+        for (size_t j = 0; j < cells[1]; j++)
+            for (size_t i = 0; i < cells[0]; i++)
+                for (int s = 0; s < 4; s++) {
+                    if (out.size() / 3 == n) return out;
+                    uint32_t id = (uint32_t)(out.size() / 3);
+                    double cell[3] = {(double)i, (double)j, (double)k};
+                    for (int ax = 0; ax < 3; ax++) {
+                        double jit = jitter * (uniform(seed, STREAM_JITTER, 3 * id + (uint32_t)ax) - 0.5);
+                        out.push_back(wrap(to_fixed((cell[ax] + basis[s][ax]) * a[ax] + jit), box[ax]));
+                    }
+                }
+    return out;
+}
+
+// This engine's triangular-lattice start (no reference counterpart: md-core has a square-ish
+// lattice and FCC only). Rows of spacing a = Lx / nx, odd rows shifted by a / 2, nx chosen so
+// that the rows are as close to equilateral as the box allows, ny rounded up to an even number
+// so the stacking is periodic; even rows at x = (i + 1/4) a, odd rows at (i + 3/4) a (so a slab
+// of it keeps a quarter spacing clear of both its edges); the first n sites in row-major order,
+// jittered like init::lattice (stream JITTER, counters 2k and 2k + 1).
+inline void triangular_shape(size_t n, double b0, double b1, size_t* nx, size_t* ny) {
+    size_t x = std::max<size_t>((size_t)sat_u32(std::round(std::sqrt((double)n * (b0 / b1) * 0.86602540378443864676))), 1);
+    size_t y = (n + x - 1) / x;
+    if (y > 1 && (y & 1)) y++;
+    *nx = x;
+    *ny = y;
+}
+inline std::vector<int64_t> triangular(size_t n, std::array<int64_t, 2> box, std::array<int64_t, 2> origin, std::array<int64_t, 2> wrap_len,
+                                       double jitter, uint64_t seed, uint32_t first_id) {
+    double b0 = to_f64(box[0]), b1 = to_f64(box[1]);
+    size_t nx, ny;
+    triangular_shape(n, b0, b1, &nx, &ny);
+    double a0 = b0 / (double)nx, a1 = b1 / (double)ny;
+    std::vector<int64_t> pos(2 * n);
+    for (size_t k = 0; k < n; k++) {
+        size_t i = k % nx, j = k / nx;
+        uint32_t id = first_id + (uint32_t)k;
+        double jx = jitter * (uniform(seed, STREAM_JITTER, 2 * id) - 0.5);
+        double jy = jitter * (uniform(seed, STREAM_JITTER, 2 * id + 1) - 0.5);
+        double shift = (j & 1) ? 0.75 : 0.25;
+        pos[2 * k] = wrap(origin[0] + to_fixed(((double)i + shift) * a0 + jx), wrap_len[0]);
+        pos[2 * k + 1] = wrap(origin[1] + to_fixed(((double)j + 0.5) * a1 + jy), wrap_len[1]);
+    }
+    return pos;
+}
+
+// This engine's liquid-vapour slab (no reference counterpart; md/tests/coexistence.rs:10-18
+// builds its slab with init::fluid). The liquid fills x in [L (1 - f) / 2, L (1 + f) / 2) on a
+// triangular lattice at rho_l; the vapour fills the rest of the box, 1 sigma clear of the
+// liquid's edges, on a square lattice whose sites are displaced uniformly within
+// (spacing - 1 sigma) so that no two vapour particles start closer than 1 sigma (stream VAPOUR,
+// counters 2k, 2k + 1).
+struct SlabShape {
+    size_t n_liquid, n_vapour, vx, vy;
+    int64_t x0, x1; // liquid region
+};
+inline SlabShape slab_shape(const System& sys, size_t n, double rho_l, double rho_v, double frac) {
+    double lx = sys.box_f64(0), ly = sys.box_f64(1);
+    SlabShape s;
+    s.x0 = to_fixed(lx * (1.0 - frac) * 0.5);
+    s.x1 = to_fixed(lx * (1.0 + frac) * 0.5);
+    double wl = to_f64(s.x1 - s.x0);
+    s.n_liquid = std::min(n, (size_t)sat_u32(std::round(rho_l * wl * ly)));
+    s.n_vapour = n - s.n_liquid;
+    double wv = std::max(lx - wl - 2.0, 0.0);
+    // vapour lattice: vx columns over the vapour width, vy rows
+    size_t vy = std::max<size_t>((size_t)sat_u32(std::ceil(std::sqrt((double)s.n_vapour * ly / std::max(wv, 1e-9)))), 1);
+    size_t vx = s.n_vapour ? (s.n_vapour + vy - 1) / vy : 0;
+    s.vx = vx;
+    s.vy = vy;
+    return s;
+}
+inline State slab(const System& sys, size_t n, double rho_l, double rho_v, double frac, double t, double jitter, uint64_t seed) {
+    SlabShape sh = slab_shape(sys, n, rho_l, rho_v, frac);
+    State st;
+    st.dim = 2;
+    st.pos.resize(2 * n);
+    auto liq = triangular(sh.n_liquid, {sh.x1 - sh.x0, sys.box[1]}, {sh.x0, 0}, {sys.box[0], sys.box[1]}, jitter, seed, 0);
+    std::copy(liq.begin(), liq.end(), st.pos.begin());
+    double lx = sys.box_f64(0), ly = sys.box_f64(1);
+    double wv = std::max(lx - to_f64(sh.x1 - sh.x0) - 2.0, 0.0);
+    if (sh.n_vapour) {
+        double ax = wv / (double)sh.vx, ay = ly / (double)sh.vy;
+        double room_x = std::max(ax - 1.0, 0.0), room_y = std::max(ay - 1.0, 0.0);
+        for (size_t k = 0; k < sh.n_vapour; k++) {
+            size_t i = k % sh.vx, j = k / sh.vx;
+            uint32_t c = (uint32_t)k;
+            double ux = uniform(seed, STREAM_VAPOUR, 2 * c), uy = uniform(seed, STREAM_VAPOUR, 2 * c + 1);
+            double x = (double)i * ax + 0.5 * (ax - room_x) + ux * room_x; // in the vapour strip
+            double y = (double)j * ay + 0.5 * (ay - room_y) + uy * room_y;
+            // the vapour strip starts 1 sigma past x1 and wraps around to 1 sigma before x0
+            int64_t xf = wrap(sh.x1 + to_fixed(1.0 + x), sys.box[0]);
+            size_t id = sh.n_liquid + k;
+            st.pos[2 * id] = xf;
+            st.pos[2 * id + 1] = wrap(to_fixed(y), sys.box[1]);
+        }
+    }
+    st.species.assign(n, 0);
+    st.vel = maxwell(sys, st.species, t, seed);
+    return st;
+}
+
+// ---------------------------------------------------------------- md-ref/src/cells.rs
+inline uint32_t cell_of(double x, double l, uint32_t n) { // cells.rs:53-55
+    return std::min(sat_u32(x / l * (double)n), n - 1);
+}
+struct CellList { // cells.rs:1-32
+    std::array<uint32_t, 3> dims{1, 1, 1};
+    std::vector<uint32_t> keys, start, items;
+};
+// Row-major cell keys (2D: y nx + x; 3D: (z ny + y) nx + x) and a stable counting sort.
+inline CellList build_cells(const System& sys, const State& s, std::array<uint32_t, 3> dims) {
+    CellList cl;
+    cl.dims = dims;
+    int d = sys.dim;
+    size_t n = s.n();
+    uint32_t ncell = dims[0] * dims[1] * (d == 3 ? dims[2] : 1);
+    cl.keys.resize(n);
+    for (size_t i = 0; i < n; i++) {
+        uint32_t c[3] = {0, 0, 0};
+        for (int a = 0; a < d; a++) c[a] = cell_of(to_f64(s.pos[d * i + a]), sys.box_f64(a), dims[a]);
+        cl.keys[i] = d == 2 ? c[1] * dims[0] + c[0] : (c[2] * dims[1] + c[1]) * dims[0] + c[0];
+    }
+    cl.start.assign(ncell + 1, 0);
+    for (auto k : cl.keys) cl.start[k + 1]++;
+    for (uint32_t c = 0; c < ncell; c++) cl.start[c + 1] += cl.start[c];
+    std::vector<uint32_t> fill(cl.start.begin(), cl.start.end() - 1);
+    cl.items.resize(n);
+    for (size_t i = 0; i < n; i++) cl.items[fill[cl.keys[i]]++] = (uint32_t)i;
+    return cl;
+}
+
+// ---------------------------------------------------------------- md-ref/src/real.rs
+template <typename F> struct Real;
+template <> struct Real<float> {
+    static bool sep(int64_t d, float* o) { return sep_f32(d, o); }
+    static float sep_near(int64_t d) { return sep_near_f32(d); }
+    static float from_f64(double x) { return (float)x; }
+    static int32_t round_to_i32(float x) { return sat_i32f(std::rint(x)); }
+    static constexpr bool is_f32 = true;
+};
+template <> struct Real<double> {
+    static bool sep(int64_t d, double* o) {
+        if (!(d >= -SEP_LIMIT && d < SEP_LIMIT)) return false;
+        *o = to_f64(d);
+        return true;
+    }
+    static double sep_near(int64_t d) { return to_f64(d); }
+    static double from_f64(double x) { return x; }
+    static int32_t round_to_i32(double x) { return sat_i32(std::rint(x)); }
+    static constexpr bool is_f32 = false;
+};
+// real.rs:105-157
+template <typename F> struct PairConsts {
+    F rc2, eps4, sigma2, shift;
+    F six_eps4; // 6 * eps4, the first product of eval's left-to-right chain
+    static PairConsts make(const Pair& p) {
+        PairConsts c;
+        if (Real<F>::is_f32) { // pair.rs:54-56 gpu_constants, rounded once
+            c.rc2 = (F)(float)(p.rc * p.rc);
+            c.eps4 = (F)(float)(4.0 * p.eps);
+            c.sigma2 = (F)(float)(p.sigma * p.sigma);
+            c.shift = (F)(float)p.shift();
+        } else {
+            c.rc2 = (F)(p.rc * p.rc);
+            c.eps4 = (F)(4.0 * p.eps);
+            c.sigma2 = (F)(p.sigma * p.sigma);
+            c.shift = (F)p.shift();
+        }
+        c.six_eps4 = (F)6.0 * c.eps4;
+        return c;
+    }
+    // eval/eval3: r2 = fx fx + fy fy (+ fz fz); None unless r2 < rc2.
+    bool eval(const F* f, int d, F* fr, F* u) const {
+        F r2 = f[0] * f[0] + f[1] * f[1];
+        if (d == 3) r2 = r2 + f[2] * f[2];
+        if (!(r2 < rc2)) return false;
+        F s2 = sigma2 / r2;
+        F s6 = s2 * s2 * s2;
+        *fr = (F)6.0 * eps4 * s6 * ((F)2.0 * s6 - (F)1.0) / r2;
+        *u = eps4 * s6 * (s6 - (F)1.0) - shift;
+        return true;
+    }
+};
+
+// ---------------------------------------------------------------- md-core/src/table.rs
+struct IntTables {
+    static constexpr uint32_t SEP_BITS = 20, R2_BITS = 24, T_BITS = 2, KICK_SHIFT = 22, STEP_BITS = 12;
+    size_t ns = 1, len = 0;
+    std::vector<int32_t> data;
+    std::vector<uint32_t> rc2;
+    explicit IntTables(const System& sys) { // table.rs:45-71
+        ns = (size_t)sys.species();
+        double rcm = sys.rc_max();
+        double rc2_max = rcm * rcm;
+        len = (size_t)((uint64_t)(rc2_max * 16777216.0) >> STEP_BITS) + 2;
+        data.assign(ns * ns * len, 0);
+        rc2.assign(ns * ns, 0);
+        for (size_t a = 0; a < ns; a++) {
+            double c = sys.kick_coeff((uint32_t)a);
+            for (size_t b = 0; b < ns; b++) {
+                const Pair& p = sys.pair((uint32_t)a, (uint32_t)b);
+                rc2[a * ns + b] = sat_u32(p.rc * p.rc * 16777216.0);
+                Pair cont = p;
+                cont.rc = INFINITY;
+                for (size_t k = 0; k < len; k++) {
+                    double r2 = (double)((uint64_t)k * 4096ull) / 16777216.0;
+                    r2 = std::max(r2, 0.36);
+                    double t = r2 < p.rc * p.rc + 2.0 * 4096.0 / 16777216.0 ? cont.f_over_r(r2) * c * 4.0 : 0.0;
+                    double rt = std::round(t);
+                    rt = std::min(std::max(rt, -2147483648.0), 2147483647.0);
+                    data[(a * ns + b) * len + k] = sat_i32(rt);
+                }
+            }
+        }
+    }
+    // table.rs:76-105 (2D)
+    bool kick(uint32_t sa, uint32_t sb, const int64_t* d, int dim, int32_t* out) const {
+        const int64_t limit = (int64_t)8 << 32;
+        for (int a = 0; a < dim; a++)
+            if (!(d[a] >= -limit && d[a] < limit)) return false;
+        int64_t q[3] = {0, 0, 0};
+        for (int a = 0; a < dim; a++) {
+            uint64_t ax = d[a] < 0 ? (uint64_t)0 - (uint64_t)d[a] : (uint64_t)d[a];
+            int64_t m = (int64_t)((ax + (1ull << (31 - SEP_BITS))) >> (32 - SEP_BITS));
+            q[a] = d[a] < 0 ? -m : m;
+        }
+        uint64_t sq = 0;
+        for (int a = 0; a < dim; a++) sq += (uint64_t)(q[a] * q[a]);
+        uint32_t r2 = (uint32_t)((sq + (1ull << (2 * SEP_BITS - R2_BITS - 1))) >> (2 * SEP_BITS - R2_BITS));
+        size_t pair = (size_t)sa * ns + sb;
+        if (r2 >= rc2[pair]) return false;
+        size_t idx = r2 >> STEP_BITS;
+        int64_t frac = (int64_t)(r2 & ((1u << STEP_BITS) - 1));
+        size_t base = pair * len;
+        int64_t t0 = data[base + idx], t1 = data[base + idx + 1];
+        int64_t t = t0 + (((t1 - t0) * frac) >> STEP_BITS);
+        for (int a = 0; a < dim; a++) {
+            unsigned __int128 prod = (unsigned __int128)(uint64_t)(t < 0 ? -t : t) * (unsigned __int128)(uint64_t)(q[a] < 0 ? -q[a] : q[a]);
+            int64_t m = (int64_t)(uint64_t)(prod >> KICK_SHIFT);
+            bool neg = (t < 0) != (q[a] < 0);
+            out[a] = (int32_t)(neg ? m : -m);
+        }
+        return true;
+    }
+};
+
+// ---------------------------------------------------------------- md-ref/src/fast.rs (2D)
+// fast.rs:76-80
+inline bool fast_eligible(const System& sys, std::array<uint32_t, 3> cells) {
+    double side = std::max(sys.box_f64(0) / (double)cells[0], sys.box_f64(1) / (double)cells[1]);
+    return 2.0 * side < 7.9;
+}
+template <typename F> struct FastScratch {
+    std::vector<int64_t> sx, sy, nx, ny;
+    std::vector<uint32_t> ss, sid, start, fill, key, ni;
+    std::vector<int32_t> kx, ky, nkx, nky;
+    std::vector<F> rx, ry;
+};
+// fast.rs:230-251
+template <typename F>
+inline void row_uniform(const PairConsts<F>& p, F c, size_t lo, size_t hi, size_t m, const F* rx, const F* ry, int32_t* tkx, int32_t* tky,
+                        int32_t* okx, int32_t* oky, F* ope) {
+    const F zero = (F)0, one = (F)1, two = (F)2, six = (F)6;
+    int32_t kx = 0, ky = 0;
+    F pe = zero;
+    for (size_t k = 0; k < m; k++) {
+        F x = rx[k], y = ry[k];
+        F r2 = x * x + y * y;
+        F s2 = p.sigma2 / r2;
+        F s6 = s2 * s2 * s2;
+        F f = six * p.eps4 * s6 * (two * s6 - one) / r2;
+        F e = p.eps4 * s6 * (s6 - one) - p.shift;
+        bool on = r2 < p.rc2 && k >= lo && k < hi;
+        F a = -(on ? f : zero) * c;
+        kx = wadd(kx, Real<F>::round_to_i32(a * x));
+        ky = wadd(ky, Real<F>::round_to_i32(a * y));
+        tkx[k] = wadd(tkx[k], Real<F>::round_to_i32(a * -x));
+        tky[k] = wadd(tky[k], Real<F>::round_to_i32(a * -y));
+        pe += on ? e : zero;
+    }
+    *okx = kx;
+    *oky = ky;
+    *ope = pe;
+}
+// fast.rs:257-294
+template <typename F>
+inline void row_mixture(const PairConsts<F>* row, const F* kick_c, size_t si, size_t lo, size_t hi, size_t m, const F* rx, const F* ry,
+                        const uint32_t* ti, const uint32_t* species, int32_t* tkx, int32_t* tky, int32_t* okx, int32_t* oky, F* ope) {
+    const F zero = (F)0, one = (F)1, two = (F)2, six = (F)6;
+    F ci = kick_c[si];
+    int32_t kx = 0, ky = 0;
+    F pe = zero;
+    for (size_t k = 0; k < m; k++) {
+        size_t sj = species[ti[k]];
+        const PairConsts<F>& p = row[sj];
+        F x = rx[k], y = ry[k];
+        F r2 = x * x + y * y;
+        F s2 = p.sigma2 / r2;
+        F s6 = s2 * s2 * s2;
+        F f = six * p.eps4 * s6 * (two * s6 - one) / r2;
+        F e = p.eps4 * s6 * (s6 - one) - p.shift;
+        bool on = r2 < p.rc2 && k >= lo && k < hi;
+        f = on ? f : zero;
+        F ai = -f * ci, aj = -f * kick_c[sj];
+        kx = wadd(kx, Real<F>::round_to_i32(ai * x));
+        ky = wadd(ky, Real<F>::round_to_i32(ai * y));
+        tkx[k] = wadd(tkx[k], Real<F>::round_to_i32(aj * -x));
+        tky[k] = wadd(tky[k], Real<F>::round_to_i32(aj * -y));
+        pe += on ? e : zero;
+    }
+    *okx = kx;
+    *oky = ky;
+    *ope = pe;
+}
+// fast.rs:83-222: counting sort into cells, half shell, branch-free rows, one scatter per cell.
+template <typename F>
+inline double pair_kicks_fast(const System& sys, const State& st, const std::vector<PairConsts<F>>& consts, const std::vector<F>& kick_c,
+                              std::array<uint32_t, 3> cells, FastScratch<F>& sc, int32_t* kicks) {
+    const size_t LANES = 8;
+    size_t n = st.n();
+    size_t ns = (size_t)sys.species();
+    uint32_t cnx = cells[0], cny = cells[1];
+    size_t ncell = (size_t)cnx * cny;
+    double b0 = sys.box_f64(0), b1 = sys.box_f64(1);
+    int64_t l[2] = {sys.box[0], sys.box[1]};
+    sc.key.resize(n);
+    for (size_t i = 0; i < n; i++) {
+        uint32_t cx = cell_of(to_f64(st.pos[2 * i]), b0, cnx), cy = cell_of(to_f64(st.pos[2 * i + 1]), b1, cny);
+        sc.key[i] = cy * cnx + cx;
+    }
+    sc.start.assign(ncell + 1, 0);
+    for (auto k : sc.key) sc.start[k + 1]++;
+    for (size_t c = 0; c < ncell; c++) sc.start[c + 1] += sc.start[c];
+    sc.sx.assign(n, 0);
+    sc.sy.assign(n, 0);
+    sc.ss.assign(n, 0);
+    sc.sid.assign(n, 0);
+    sc.fill.assign(sc.start.begin(), sc.start.end());
+    for (size_t i = 0; i < n; i++) {
+        uint32_t k = sc.key[i];
+        uint32_t s = sc.fill[k]++;
+        sc.sx[s] = st.pos[2 * i];
+        sc.sy[s] = st.pos[2 * i + 1];
+        sc.ss[s] = st.species[i];
+        sc.sid[s] = (uint32_t)i;
+    }
+    sc.kx.assign(n, 0);
+    sc.ky.assign(n, 0);
+    static const int SHELL[4][2] = {{1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+    F pe = (F)0;
+    for (uint32_t cy = 0; cy < cny; cy++) {
+        for (uint32_t cx = 0; cx < cnx; cx++) {
+            size_t c = (size_t)cy * cnx + cx;
+            size_t a0 = sc.start[c], a1 = sc.start[c + 1];
+            if (a0 == a1) continue;
+            sc.nx.clear();
+            sc.ny.clear();
+            sc.ni.clear();
+            struct Range { size_t b0, b1; int64_t shx, shy; };
+            Range ranges[5];
+            size_t nr = 0;
+            ranges[nr++] = {a0, a1, 0, 0};
+            for (auto& o : SHELL) {
+                int tx = (int)cx + o[0], ty = (int)cy + o[1];
+                uint32_t dx, dy;
+                int64_t shx = 0, shy = 0;
+                if (tx < 0) { dx = (uint32_t)(tx + (int)cnx); shx = -l[0]; }
+                else if (tx >= (int)cnx) { dx = (uint32_t)(tx - (int)cnx); shx = l[0]; }
+                else dx = (uint32_t)tx;
+                if (ty < 0) { dy = (uint32_t)(ty + (int)cny); shy = -l[1]; }
+                else if (ty >= (int)cny) { dy = (uint32_t)(ty - (int)cny); shy = l[1]; }
+                else dy = (uint32_t)ty;
+                size_t d = (size_t)dy * cnx + dx;
+                ranges[nr++] = {sc.start[d], sc.start[d + 1], shx, shy};
+            }
+            for (size_t r = 0; r < nr; r++) {
+                for (size_t q = ranges[r].b0; q < ranges[r].b1; q++) {
+                    sc.nx.push_back(sc.sx[q] + ranges[r].shx);
+                    sc.ny.push_back(sc.sy[q] + ranges[r].shy);
+                    sc.ni.push_back((uint32_t)q);
+                }
+            }
+            size_t m = sc.nx.size();
+            size_t mp = (m + LANES - 1) / LANES * LANES;
+            int64_t lx = sc.nx[m - 1], ly = sc.ny[m - 1];
+            uint32_t li = sc.ni[m - 1];
+            sc.nx.resize(mp, lx);
+            sc.ny.resize(mp, ly);
+            sc.ni.resize(mp, li);
+            sc.nkx.assign(mp, 0);
+            sc.nky.assign(mp, 0);
+            sc.rx.resize(mp);
+            sc.ry.resize(mp);
+            for (size_t p = 0; p < a1 - a0; p++) {
+                size_t s = a0 + p;
+                int64_t xs = sc.sx[s], ys = sc.sy[s];
+                for (size_t k = 0; k < mp; k++) {
+                    sc.rx[k] = Real<F>::sep_near(sc.nx[k] - xs);
+                    sc.ry[k] = Real<F>::sep_near(sc.ny[k] - ys);
+                }
+                int32_t kx, ky;
+                F e;
+                if (ns == 1)
+                    row_uniform<F>(consts[0], kick_c[0], p + 1, m, mp, sc.rx.data(), sc.ry.data(), sc.nkx.data(), sc.nky.data(), &kx, &ky, &e);
+                else {
+                    size_t si = sc.ss[s];
+                    row_mixture<F>(&consts[si * ns], kick_c.data(), si, p + 1, m, mp, sc.rx.data(), sc.ry.data(), sc.ni.data(), sc.ss.data(),
+                                   sc.nkx.data(), sc.nky.data(), &kx, &ky, &e);
+                }
+                sc.kx[s] = wadd(sc.kx[s], kx);
+                sc.ky[s] = wadd(sc.ky[s], ky);
+                pe += e;
+            }
+            for (size_t k = 0; k < m; k++) {
+                size_t t = sc.ni[k];
+                sc.kx[t] = wadd(sc.kx[t], sc.nkx[k]);
+                sc.ky[t] = wadd(sc.ky[t], sc.nky[k]);
+            }
+        }
+    }
+    for (size_t s = 0; s < n; s++) {
+        kicks[2 * sc.sid[s]] = sc.kx[s];
+        kicks[2 * sc.sid[s] + 1] = sc.ky[s];
+    }
+    return (double)pe;
+}
+
+// ---------------------------------------------------------------- IntEngine<F> / IntEngine3<F>
+struct Energy { double kinetic = 0.0, potential = 0.0; };
+
+// md-ref int_engine.rs:23-447 and int_engine3.rs:12-240, for periodic systems (walls, baths,
+// bonds, pistons, membranes and compartments are outside this path). One template serves 2D and
+// 3D; in 2D `fast` selects fast.rs's half-shell path when it applies, as IntEngine::forces does.
+template <typename F> struct IntEngine {
+    System sys;
+    State state;
+    std::vector<PairConsts<F>> consts;
+    std::vector<F> kick_c;
+    std::array<int32_t, 3> gravity{0, 0, 0};
+    std::array<uint32_t, 3> cells{1, 1, 1};
+    int64_t steps = 0;
+    uint32_t clock = 0;
+    bool fast = true;
+    IntTables* tables = nullptr;
+    FastScratch<F> scratch;
+    int threads = 1; // OpenMP threads for the 3D/2D reference loop (the CPU baseline)
+
+    IntEngine(const System& s, const State& st) : sys(s), state(st) {
+        for (auto& p : sys.pairs) consts.push_back(PairConsts<F>::make(p));
+        for (int k = 0; k < sys.species(); k++) kick_c.push_back(Real<F>::from_f64(sys.kick_coeff((uint32_t)k)));
+        gravity = sys.gravity_kick();
+        cells = sys.cells_for(sys.rc_max());
+    }
+    ~IntEngine() { delete tables; }
+    void use_integer_tables() { // IntEngine::integer (int_engine.rs:94-98)
+        delete tables;
+        tables = new IntTables(sys);
+    }
+    // 2D: present_cells (int_engine.rs:108-116)
+    std::array<uint32_t, 3> present_cells() const {
+        if (sys.dim == 3) return cells;
+        uint32_t present = 0;
+        for (auto s : state.species) present |= 1u << s;
+        double rc = 0.0;
+        int ns = sys.species();
+        for (int a = 0; a < ns; a++)
+            for (int b = 0; b < ns; b++)
+                if ((present >> a & 1) && (present >> b & 1)) rc = std::max(rc, sys.pairs[a * ns + b].rc);
+        if (rc <= 0.0) return cells;
+        auto c = sys.cells_for(rc);
+        return {std::max(c[0], cells[0]), std::max(c[1], cells[1]), 1};
+    }
+
+    // IntEngine::forces (int_engine.rs:130-251) / IntEngine3::forces (int_engine3.rs:48-131):
+    // the reference loop over the 3^d neighbouring cells of each particle, or the fast path.
+    double forces(std::vector<int32_t>& kicks) {
+        int d = sys.dim;
+        size_t n = state.n();
+        int ns = sys.species();
+        kicks.assign(d * n, 0);
+        auto cl_dims = present_cells();
+        double pe = 0.0;
+        bool use_fast = d == 2 && fast && !tables && fast_eligible(sys, cl_dims);
+        if (use_fast) return pair_kicks_fast<F>(sys, state, consts, kick_c, cl_dims, scratch, kicks.data());
+        CellList cl = build_cells(sys, state, cl_dims);
+        uint32_t nc[3] = {cl_dims[0], cl_dims[1], d == 3 ? cl_dims[2] : 1u};
+        double b[3] = {sys.box_f64(0), sys.box_f64(1), d == 3 ? sys.box_f64(2) : 1.0};
+        std::vector<double> pe_part(n, 0.0);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads) if (threads > 1)
+        for (long long ii = 0; ii < (long long)n; ii++) {
+            size_t i = (size_t)ii;
+            const int64_t* pi = &state.pos[d * i];
+            uint32_t si = state.species[i];
+            F c = kick_c[si];
+            uint32_t cc[3] = {0, 0, 0};
+            for (int a = 0; a < d; a++) cc[a] = cell_of(to_f64(pi[a]), b[a], nc[a]);
+            int32_t k[3] = {0, 0, 0};
+            F pe_i = (F)0;
+            double pe_i64 = 0.0;
+            int oz_n = d == 3 ? 3 : 1;
+            for (int oz = 0; oz < oz_n; oz++) {
+                uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
+                for (int oy = 0; oy < 3; oy++) {
+                    uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
+                    for (int ox = 0; ox < 3; ox++) {
+                        uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
+                        uint32_t cell = (z * nc[1] + y) * nc[0] + x;
+                        for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
+                            size_t j = cl.items[q];
+                            if (j == i) continue;
+                            const int64_t* pj = &state.pos[d * j];
+                            int64_t dd[3];
+                            for (int a = 0; a < d; a++) dd[a] = min_image(pi[a], pj[a], sys.box[a]);
+                            if (tables) {
+                                int32_t kk[3];
+                                if (tables->kick(si, state.species[j], dd, d, kk)) {
+                                    for (int a = 0; a < d; a++) k[a] = wadd(k[a], kk[a]);
+                                    double r2 = 0.0;
+                                    for (int a = 0; a < d; a++) r2 += to_f64(dd[a]) * to_f64(dd[a]);
+                                    pe_i64 += sys.pair(si, state.species[j]).energy(r2);
+                                }
+                                continue;
+                            }
+                            F f[3];
+                            bool ok = true;
+                            for (int a = 0; a < d; a++) ok = ok && Real<F>::sep(dd[a], &f[a]);
+                            if (!ok) continue;
+                            F fr, u;
+                            if (consts[si * ns + state.species[j]].eval(f, d, &fr, &u)) {
+                                F aa = -fr * c;
+                                for (int a = 0; a < d; a++) k[a] = wadd(k[a], Real<F>::round_to_i32(aa * f[a]));
+                                pe_i += u;
+                            }
+                        }
+                    }
+                }
+            }
+            for (int a = 0; a < d; a++) kicks[d * i + a] = k[a];
+            pe_part[i] = tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i;
+        }
+        for (size_t i = 0; i < n; i++) pe += pe_part[i];
+        return pe;
+    }
+
+    // int_engine.rs:253-344 / int_engine3.rs:138-184 (periodic): v += kick + g; x += v; wrap.
+    void step(size_t nsteps) {
+        int d = sys.dim;
+        std::vector<int32_t> kicks;
+        for (size_t s = 0; s < nsteps; s++) {
+            forces(kicks);
+            for (size_t i = 0; i < state.n(); i++) {
+                bool pinned = sys.is_pinned(state.species[i]);
+                for (int a = 0; a < d; a++) {
+                    int32_t g = pinned ? 0 : gravity[a];
+                    int32_t v = wadd(wadd(state.vel[d * i + a], kicks[d * i + a]), g);
+                    state.vel[d * i + a] = v;
+                    state.pos[d * i + a] = wrap(state.pos[d * i + a] + (int64_t)v, sys.box[a]);
+                }
+            }
+            steps += 1;
+            clock += 1;
+        }
+    }
+    // int_engine.rs:396-413
+    void reverse() {
+        int d = sys.dim;
+        std::vector<int32_t> kicks;
+        forces(kicks);
+        for (size_t i = 0; i < state.n(); i++) {
+            bool pinned = sys.is_pinned(state.species[i]);
+            for (int a = 0; a < d; a++) {
+                int32_t g = pinned ? 0 : gravity[a];
+                state.vel[d * i + a] = wneg(wadd(wadd(state.vel[d * i + a], kicks[d * i + a]), g));
+            }
+        }
+        steps = -steps;
+    }
+    // int_engine.rs:417-446 / int_engine3.rs:222-239: on-step KE and the potential energy.
+    Energy energy() {
+        int d = sys.dim;
+        std::vector<int32_t> kicks;
+        Energy e;
+        e.potential = forces(kicks);
+        for (size_t i = 0; i < state.n(); i++) {
+            uint32_t s = state.species[i];
+            if (d == 3 && sys.is_pinned(s)) continue;
+            double m = sys.masses[s];
+            if (d == 2) {
+                double v[2];
+                for (int a = 0; a < 2; a++) {
+                    int32_t next = wadd(wadd(state.vel[2 * i + a], kicks[2 * i + a]), gravity[a]);
+                    v[a] = 0.5 * (sys.velocity(state.vel[2 * i + a]) + sys.velocity(next));
+                }
+                e.kinetic += 0.5 * m * (v[0] * v[0] + v[1] * v[1]);
+                for (int a = 0; a < 2; a++) e.potential -= m * sys.gravity[a] * to_f64(state.pos[2 * i + a]);
+            } else {
+                for (int a = 0; a < 3; a++) {
+                    int32_t next = wadd(wadd(state.vel[3 * i + a], kicks[3 * i + a]), gravity[a]);
+                    double v = 0.5 * (sys.velocity(state.vel[3 * i + a]) + sys.velocity(next));
+                    e.kinetic += 0.5 * m * v * v;
+                    e.potential -= m * sys.gravity[a] * to_f64(state.pos[3 * i + a]);
+                }
+            }
+        }
+        return e;
+    }
+};
+
+// ---------------------------------------------------------------- md-ref/src/float_engine.rs
+// FloatEngine<f64> in 2D (periodic): conventional MD in floats, the reference for observables.
+struct FloatEngine {
+    System sys;
+    std::vector<double> pos, vel;
+    std::vector<uint32_t> species;
+    std::vector<PairConsts<double>> consts;
+    double box[2];
+    std::vector<double> inv_mass;
+    std::array<uint32_t, 3> cells;
+    FloatEngine(const System& s, const State& st) : sys(s) {
+        box[0] = sys.box_f64(0);
+        box[1] = sys.box_f64(1);
+        for (size_t i = 0; i < st.n(); i++) {
+            pos.push_back(to_f64(st.pos[2 * i]));
+            pos.push_back(to_f64(st.pos[2 * i + 1]));
+            vel.push_back(sys.velocity(st.vel[2 * i]));
+            vel.push_back(sys.velocity(st.vel[2 * i + 1]));
+        }
+        species = st.species;
+        for (auto& p : sys.pairs) consts.push_back(PairConsts<double>::make(p));
+        for (double m : sys.masses) inv_mass.push_back(1.0 / m);
+        cells = sys.cells_for(sys.rc_max());
+    }
+    double min_image_f(double d, int a) const {
+        double l = box[a], half = l * 0.5;
+        if (d >= half) return d - l;
+        if (d < -half) return d + l;
+        return d;
+    }
+    double forces(std::vector<double>& f) const {
+        size_t n = species.size();
+        int ns = sys.species();
+        f.assign(2 * n, 0.0);
+        uint32_t nc[2] = {cells[0], cells[1]};
+        std::vector<uint32_t> keys(n);
+        auto cellc = [&](size_t i, int a) { return cell_of(pos[2 * i + a], box[a], nc[a]); };
+        for (size_t i = 0; i < n; i++) keys[i] = cellc(i, 1) * nc[0] + cellc(i, 0);
+        std::vector<uint32_t> start(nc[0] * nc[1] + 1, 0), items(n);
+        for (auto k : keys) start[k + 1]++;
+        for (size_t c = 0; c + 1 < start.size(); c++) start[c + 1] += start[c];
+        std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+        for (size_t i = 0; i < n; i++) items[fill[keys[i]]++] = (uint32_t)i;
+        double pe = 0.0;
+        for (size_t i = 0; i < n; i++) {
+            uint32_t cx = cellc(i, 0), cy = cellc(i, 1);
+            double fx_i = 0, fy_i = 0, pe_i = 0;
+            for (int oy = 0; oy < 3; oy++) {
+                uint32_t y = (cy + nc[1] + (uint32_t)oy - 1) % nc[1];
+                for (int ox = 0; ox < 3; ox++) {
+                    uint32_t x = (cx + nc[0] + (uint32_t)ox - 1) % nc[0];
+                    uint32_t k = y * nc[0] + x;
+                    for (uint32_t q = start[k]; q < start[k + 1]; q++) {
+                        size_t j = items[q];
+                        if (j == i) continue;
+                        double dd[2] = {min_image_f(pos[2 * j] - pos[2 * i], 0), min_image_f(pos[2 * j + 1] - pos[2 * i + 1], 1)};
+                        double fr, u;
+                        if (consts[species[i] * ns + species[j]].eval(dd, 2, &fr, &u)) {
+                            fx_i += -fr * dd[0];
+                            fy_i += -fr * dd[1];
+                            pe_i += u;
+                        }
+                    }
+                }
+            }
+            f[2 * i] = fx_i;
+            f[2 * i + 1] = fy_i;
+            pe += 0.5 * pe_i;
+        }
+        return pe;
+    }
+    double wrapf(double x, int a) const { return x - box[a] * std::floor(x / box[a]); }
+    void step(size_t nsteps) {
+        std::vector<double> f;
+        for (size_t s = 0; s < nsteps; s++) {
+            forces(f);
+            for (size_t i = 0; i < species.size(); i++) {
+                double k = inv_mass[species[i]] * sys.dt;
+                for (int a = 0; a < 2; a++) {
+                    vel[2 * i + a] += f[2 * i + a] * k;
+                    double x = pos[2 * i + a] + vel[2 * i + a] * sys.dt;
+                    pos[2 * i + a] = wrapf(x, a);
+                }
+            }
+        }
+    }
+    Energy energy() const {
+        std::vector<double> f;
+        Energy e;
+        e.potential = forces(f);
+        for (size_t i = 0; i < species.size(); i++) {
+            double m = sys.masses[species[i]];
+            double k = inv_mass[species[i]] * sys.dt;
+            for (int a = 0; a < 2; a++) {
+                double v = vel[2 * i + a] + 0.5 * f[2 * i + a] * k;
+                e.kinetic += 0.5 * m * v * v;
+            }
+        }
+        return e;
+    }
+};
+
+// ---------------------------------------------------------------- Verlet lists (md shaders)
+// neighbors.wgsl:27-64 / md3.wgsl:443-483 with an exactly specified f32 test: a pair is listed
+// when the f32 separations (fixed.rs sep_f32; beyond 8 sigma the GPU's 1e30) give
+// fx*fx + fy*fy (+ fz*fz), summed left to right without fusion, below the f32 of
+// ((rc_ab + skin)(1 + 1e-4))^2 (engine.rs:302-313). Every listed pair is within the scanned
+// 3^d cells because cells are at least rc + skin wide (engine.rs:152-153).
+inline float pair_list_r2(const System& sys, uint32_t a, uint32_t b, double skin) {
+    double r = (sys.pair(a, b).rc + skin) * (1.0 + 1e-4);
+    return (float)(r * r);
+}
+inline float sep_or_far(int64_t d) {
+    float f;
+    return sep_f32(d, &f) ? f : 1e30f;
+}
+// Returns, for each particle (storage index), the sorted indices of its listed neighbours.
+inline std::vector<std::vector<uint32_t>> verlet_lists(const System& sys, const State& s, double skin) {
+    int d = sys.dim;
+    size_t n = s.n();
+    auto dims = sys.cells_for(sys.rc_max() + skin);
+    CellList cl = build_cells(sys, s, dims);
+    uint32_t nc[3] = {dims[0], dims[1], d == 3 ? dims[2] : 1u};
+    std::vector<std::vector<uint32_t>> out(n);
+    for (size_t i = 0; i < n; i++) {
+        uint32_t key = cl.keys[i];
+        uint32_t cc[3] = {key % nc[0], (key / nc[0]) % nc[1], key / (nc[0] * nc[1])};
+        const int64_t* pi = &s.pos[d * i];
+        std::vector<uint32_t> seen;
+        int oz_n = d == 3 ? 3 : 1;
+        for (int oz = 0; oz < oz_n; oz++) {
+            uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
+            for (int oy = 0; oy < 3; oy++) {
+                uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
+                for (int ox = 0; ox < 3; ox++) {
+                    uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
+                    uint32_t cell = (z * nc[1] + y) * nc[0] + x;
+                    // a 3-cell-wide axis visits a cell once per offset; count each cell once
+                    if (std::find(seen.begin(), seen.end(), cell) != seen.end()) continue;
+                    seen.push_back(cell);
+                    for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
+                        uint32_t j = cl.items[q];
+                        if (j == i) continue;
+                        const int64_t* pj = &s.pos[d * j];
+                        float f[3] = {0.0f, 0.0f, 0.0f};
+                        for (int a = 0; a < d; a++) f[a] = sep_or_far(min_image(pi[a], pj[a], sys.box[a]));
+                        float r2 = f[0] * f[0] + f[1] * f[1];
+                        if (d == 3) r2 = r2 + f[2] * f[2];
+                        if (r2 < pair_list_r2(sys, s.species[i], s.species[j], skin)) out[i].push_back(j);
+                    }
+                }
+            }
+        }
+        std::sort(out[i].begin(), out[i].end());
+    }
+    return out;
+}
+// ForceMode::verlet_with_skin (engine.rs:130-141) / verlet3_with_skin (engine3.rs:61-68),
+// without the 128 MiB single-binding clamp (device memory has no per-binding cap here).
+inline uint32_t verlet_cap(const System& sys, size_t n, double skin) {
+    double r = sys.rc_max() + skin;
+    double density = (double)n / sys.volume();
+    double vol = sys.dim == 2 ? 3.14159265358979323846 * r * r : 4.0 / 3.0 * 3.14159265358979323846 * r * r * r;
+    return sat_u32(std::ceil(vol * std::max(2.0 * density, 1.2))) + 8;
+}
+
+// ---------------------------------------------------------------- instruments (new)
+// f32 pair terms exactly as the engine evaluates them, summed in f64: PE and the virial
+// sum over pairs of fr r^2 (= -r dU/dr, mc/src/gibbs.rs:58-66), over unordered pairs.
+struct PairSums { double potential = 0.0, virial = 0.0; };
+inline PairSums pair_sums_f32(const System& sys, const State& s) {
+    int d = sys.dim;
+    int ns = sys.species();
+    std::vector<PairConsts<float>> consts;
+    for (auto& p : sys.pairs) consts.push_back(PairConsts<float>::make(p));
+    auto dims = sys.cells_for(sys.rc_max());
+    CellList cl = build_cells(sys, s, dims);
+    uint32_t nc[3] = {dims[0], dims[1], d == 3 ? dims[2] : 1u};
+    PairSums out;
+    for (size_t i = 0; i < s.n(); i++) {
+        uint32_t key = cl.keys[i];
+        uint32_t cc[3] = {key % nc[0], (key / nc[0]) % nc[1], key / (nc[0] * nc[1])};
+        const int64_t* pi = &s.pos[d * i];
+        double pe_i = 0.0, w_i = 0.0;
+        int oz_n = d == 3 ? 3 : 1;
+        for (int oz = 0; oz < oz_n; oz++) {
+            uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
+            for (int oy = 0; oy < 3; oy++) {
+                uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
+                for (int ox = 0; ox < 3; ox++) {
+                    uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
+                    uint32_t cell = (z * nc[1] + y) * nc[0] + x;
+                    for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
+                        uint32_t j = cl.items[q];
+                        if (j == i) continue;
+                        const int64_t* pj = &s.pos[d * j];
+                        float f[3];
+                        bool ok = true;
+                        for (int a = 0; a < d; a++) ok = ok && sep_f32(min_image(pi[a], pj[a], sys.box[a]), &f[a]);
+                        if (!ok) continue;
+                        float fr, u;
+                        if (consts[s.species[i] * ns + s.species[j]].eval(f, d, &fr, &u)) {
+                            float r2 = f[0] * f[0] + f[1] * f[1];
+                            if (d == 3) r2 = r2 + f[2] * f[2];
+                            pe_i += (double)u;
+                            w_i += (double)(fr * r2);
+                        }
+                    }
+                }
+            }
+        }
+        out.potential += 0.5 * pe_i;
+        out.virial += 0.5 * w_i;
+    }
+    return out;
+}
+// RDF pair counts over unordered pairs: bin k = floor(sqrt(r2) * (bins / rmax)) with r2 the f64
+// square of the exact minimum-image separation.
+inline std::vector<uint64_t> rdf_counts(const System& sys, const State& s, uint32_t bins, double rmax) {
+    int d = sys.dim;
+    std::vector<uint64_t> h(bins, 0);
+    double scale = (double)bins / rmax;
+    auto dims = sys.cells_for(rmax);
+    CellList cl = build_cells(sys, s, dims);
+    uint32_t nc[3] = {dims[0], dims[1], d == 3 ? dims[2] : 1u};
+    for (size_t i = 0; i < s.n(); i++) {
+        uint32_t key = cl.keys[i];
+        uint32_t cc[3] = {key % nc[0], (key / nc[0]) % nc[1], key / (nc[0] * nc[1])};
+        const int64_t* pi = &s.pos[d * i];
+        std::vector<uint32_t> seen;
+        int oz_n = d == 3 ? 3 : 1;
+        for (int oz = 0; oz < oz_n; oz++) {
+            uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
+            for (int oy = 0; oy < 3; oy++) {
+                uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
+                for (int ox = 0; ox < 3; ox++) {
+                    uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
+                    uint32_t cell = (z * nc[1] + y) * nc[0] + x;
+                    if (std::find(seen.begin(), seen.end(), cell) != seen.end()) continue;
+                    seen.push_back(cell);
+                    for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
+                        uint32_t j = cl.items[q];
+                        if (j <= i) continue;
+                        double r2 = 0.0;
+                        for (int a = 0; a < d; a++) {
+                            double dd = to_f64(min_image(pi[a], s.pos[d * j + a], sys.box[a]));
+                            r2 = r2 + dd * dd;
+                        }
+                        double r = std::sqrt(r2) * scale;
+                        if (r < (double)bins) h[(uint32_t)r]++;
+                    }
+                }
+            }
+        }
+    }
+    return h;
+}
+// Particle counts in `bins` slabs along `axis`: bin = min(floor(x / L * bins), bins - 1) in f64.
+inline std::vector<uint64_t> density_profile(const System& sys, const State& s, uint32_t bins, int axis) {
+    std::vector<uint64_t> h(bins, 0);
+    for (size_t i = 0; i < s.n(); i++) h[cell_of(to_f64(s.pos[sys.dim * i + axis]), sys.box_f64(axis), bins)]++;
+    return h;
+}
+// The velocity-rescale thermostat of this engine: the half-step kinetic energy summed exactly as
+// integers per species (sum of v^2 in 128 bits), then f = sqrt(t / now) as set_temperature
+// (init.rs:92-103) with v <- round(v f) and an exact zero velocity sum.
+inline double exact_half_step_kinetic(const System& sys, const State& s) {
+    int d = sys.dim;
+    unsigned __int128 acc[GBMD_MAX_SPECIES] = {0, 0, 0, 0};
+    for (size_t i = 0; i < s.n(); i++) {
+        uint32_t sp = s.species[i];
+        if (sys.is_pinned(sp)) continue;
+        for (int a = 0; a < d; a++) {
+            int64_t v = s.vel[d * i + a];
+            acc[sp] += (unsigned __int128)(uint64_t)(v * v);
+        }
+    }
+    double ke = 0.0;
+    double u = UNIT / sys.dt;
+    for (int sp = 0; sp < sys.species(); sp++) {
+        double hi = (double)(uint64_t)(acc[sp] >> 64) * 18446744073709551616.0;
+        double sum = hi + (double)(uint64_t)acc[sp];
+        ke += 0.5 * sys.masses[sp] * sum * (u * u);
+    }
+    return ke;
+}
+inline void rescale_temperature(State& s, const System& sys, double t) {
+    int d = sys.dim;
+    size_t moving = 0;
+    for (size_t i = 0; i < s.n(); i++)
+        if (!sys.is_pinned(s.species[i])) moving++;
+    double dof = 0.5 * (double)d * std::max((double)moving - 1.0, 1.0);
+    double now = exact_half_step_kinetic(sys, s) / dof;
+    if (!(now > 0.0)) return;
+    double f = std::sqrt(t / now);
+    for (size_t i = 0; i < s.n(); i++) {
+        if (sys.is_pinned(s.species[i])) continue;
+        for (int a = 0; a < d; a++) s.vel[d * i + a] = sat_i32(std::round((double)s.vel[d * i + a] * f));
+    }
+    zero_velocity_sum(sys, s.species, s.vel, true);
+}
+
+} // namespace oracle

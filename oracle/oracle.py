@@ -1,0 +1,308 @@
+"""ORACLE — test infrastructure only (the CPU restatement of micrographia's md-ref / md-core).
+
+ctypes bindings of oracle/_build/liboracle.so for the parity tests, __graft_entry__.smoke() and
+bench.py's CPU baseline. The engine package never imports this module.
+"""
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from micrographia_gb300 import _abi  # noqa: E402  (ABI struct definitions only)
+from micrographia_gb300.core import State, State3  # noqa: E402
+
+from . import build as _build  # noqa: E402
+
+P = C.POINTER
+VP = C.c_void_p
+I64P, I32P, U32P, U64P, DP = P(C.c_int64), P(C.c_int32), P(C.c_uint32), P(C.c_uint64), P(C.c_double)
+SYS = P(_abi.gbmd_system)
+
+_SIGS = [
+    ("oracle_sep_f32", C.c_int, [C.c_int64, P(C.c_float)]),
+    ("oracle_sep_near", C.c_float, [C.c_int64]),
+    ("oracle_threefry", None, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, U32P]),
+    ("oracle_uniform", C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32]),
+    ("oracle_normal", C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32]),
+    ("oracle_log", C.c_double, [C.c_double]),
+    ("oracle_cos", C.c_double, [C.c_double]),
+    ("oracle_to_fixed", C.c_int64, [C.c_double]),
+    ("oracle_box_for", None, [C.c_uint64, C.c_double, C.c_double, I64P]),
+    ("oracle_cube_for", None, [C.c_uint64, C.c_double, I64P]),
+    ("oracle_fcc_cells", None, [C.c_uint64, I64P, U64P]),
+    ("oracle_cells_for", C.c_int, [SYS, C.c_double, U32P]),
+    ("oracle_wca_rc", C.c_double, []),
+    ("oracle_pair_shift", C.c_double, [C.c_double, C.c_double, C.c_double]),
+    ("oracle_lattice", None, [C.c_uint64, I64P, C.c_double, C.c_uint64, I64P]),
+    ("oracle_fcc", None, [C.c_uint64, I64P, U64P, C.c_double, C.c_uint64, I64P]),
+    ("oracle_maxwell", None, [SYS, U32P, C.c_uint64, C.c_double, C.c_uint64, I32P]),
+    ("oracle_zero_velocity_sum", None, [SYS, U32P, C.c_uint64, I32P]),
+    ("oracle_set_temperature", None, [SYS, I32P, U32P, C.c_uint64, C.c_double, C.c_int]),
+    ("oracle_exact_kinetic", C.c_double, [SYS, I32P, U32P, C.c_uint64]),
+    ("oracle_half_step_kinetic", C.c_double, [SYS, I32P, U32P, C.c_uint64]),
+    ("oracle_init", C.c_int, [SYS, P(_abi.gbmd_init), I64P, I32P, U32P]),
+    ("oracle_cell_list", C.c_int, [SYS, I64P, C.c_uint64, U32P, U32P, U32P, U32P]),
+    ("oracle_verlet_cap", C.c_uint32, [SYS, C.c_uint64, C.c_double]),
+    ("oracle_verlet_list", C.c_int64, [SYS, I64P, U32P, C.c_uint64, C.c_double, U32P, U32P, C.c_uint64]),
+    ("oracle_engine_create", VP, [SYS, I64P, I32P, U32P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("oracle_engine_destroy", None, [VP]),
+    ("oracle_engine_step", None, [VP, C.c_uint64]),
+    ("oracle_engine_reverse", None, [VP]),
+    ("oracle_engine_kicks", C.c_double, [VP, I32P]),
+    ("oracle_engine_state", None, [VP, I64P, I32P, U32P]),
+    ("oracle_engine_set_state", None, [VP, I64P, I32P, U32P]),
+    ("oracle_engine_hash", C.c_uint64, [VP]),
+    ("oracle_engine_steps", C.c_int64, [VP]),
+    ("oracle_engine_energy", None, [VP, DP, DP]),
+    ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
+    ("oracle_float_create", VP, [SYS, I64P, I32P, U32P, C.c_uint64]),
+    ("oracle_float_destroy", None, [VP]),
+    ("oracle_float_step", None, [VP, C.c_uint64]),
+    ("oracle_float_positions", None, [VP, DP]),
+    ("oracle_float_energy", None, [VP, DP, DP]),
+    ("oracle_pair_sums", None, [SYS, I64P, U32P, C.c_uint64, DP, DP]),
+    ("oracle_rdf", None, [SYS, I64P, C.c_uint64, C.c_uint32, C.c_double, U64P]),
+    ("oracle_profile", None, [SYS, I64P, C.c_uint64, C.c_uint32, C.c_uint32, U64P]),
+    ("oracle_int_kick", C.c_int, [SYS, C.c_uint32, C.c_uint32, I64P, I32P]),
+]
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        l = C.CDLL(_build.build())
+        for name, res, args in _SIGS:
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(P(t))
+
+
+def threefry(ctr, key, rounds=20):
+    out = (C.c_uint32 * 2)()
+    lib().oracle_threefry(ctr[0], ctr[1], key[0], key[1], rounds, out)
+    return [out[0], out[1]]
+
+
+def sep_f32(d):
+    f = C.c_float()
+    ok = lib().oracle_sep_f32(d, C.byref(f))
+    return f.value if ok else None
+
+
+def box_for(n, density, aspect=1.0):
+    out = (C.c_int64 * 2)()
+    lib().oracle_box_for(n, density, aspect, out)
+    return [out[0], out[1]]
+
+
+def cube_for(n, density):
+    out = (C.c_int64 * 3)()
+    lib().oracle_cube_for(n, density, out)
+    return [out[0], out[1], out[2]]
+
+
+def fcc_cells(n, box):
+    b = (C.c_int64 * 3)(*box)
+    out = (C.c_uint64 * 3)()
+    lib().oracle_fcc_cells(n, b, out)
+    return [out[0], out[1], out[2]]
+
+
+def init(sys, spec):
+    """The recipes of gbmd_init_state restated on the CPU."""
+    n, D = spec.n, sys.DIM
+    pos = np.empty((n, D), np.int64)
+    vel = np.empty((n, D), np.int32)
+    sp = np.empty(n, np.uint32)
+    c = sys.to_c()
+    if lib().oracle_init(C.byref(c), C.byref(spec), _p(pos, C.c_int64), _p(vel, C.c_int32), _p(sp, C.c_uint32)) != 0:
+        raise ValueError("oracle init failed")
+    return (State if D == 2 else State3)(pos, vel, sp)
+
+
+def fluid(sys, n, t, seed):
+    """init::fluid (periodic)."""
+    from micrographia_gb300.engine import make_init
+
+    return init(sys, make_init(_abi.INIT_FLUID, n, t, seed, jitter=0.1))
+
+
+def fcc_maxwell(sys, n, t, seed, jitter=0.05):
+    from micrographia_gb300.engine import make_init
+
+    return init(sys, make_init(_abi.INIT_FCC, n, t, seed, jitter=jitter))
+
+
+def maxwell(sys, species, t, seed):
+    species = np.ascontiguousarray(species, np.uint32)
+    vel = np.empty((len(species), sys.DIM), np.int32)
+    c = sys.to_c()
+    lib().oracle_maxwell(C.byref(c), _p(species, C.c_uint32), len(species), t, seed, _p(vel, C.c_int32))
+    return vel
+
+
+def set_temperature(sys, state, t, exact=False):
+    vel = np.ascontiguousarray(state.vel.copy())
+    c = sys.to_c()
+    lib().oracle_set_temperature(C.byref(c), _p(vel, C.c_int32), _p(state.species, C.c_uint32), state.n(), t, 1 if exact else 0)
+    return vel
+
+
+def cell_list(sys, state, dims):
+    n = state.n()
+    d = list(dims) + [1] * (3 - len(dims))
+    ncell = int(np.prod(d[: sys.DIM]))
+    keys = np.empty(n, np.uint32)
+    start = np.empty(ncell + 1, np.uint32)
+    items = np.empty(n, np.uint32)
+    c = sys.to_c()
+    dd = (C.c_uint32 * 3)(*d)
+    lib().oracle_cell_list(C.byref(c), _p(state.pos, C.c_int64), n, dd, _p(keys, C.c_uint32), _p(start, C.c_uint32), _p(items, C.c_uint32))
+    return keys, start, items
+
+
+def verlet_lists(sys, state, skin):
+    n = state.n()
+    counts = np.empty(n, np.uint32)
+    cap = n * 512
+    nbr = np.empty(cap, np.uint32)
+    c = sys.to_c()
+    tot = lib().oracle_verlet_list(C.byref(c), _p(state.pos, C.c_int64), _p(state.species, C.c_uint32), n, skin, _p(counts, C.c_uint32), _p(nbr, C.c_uint32), cap)
+    if tot < 0:
+        raise ValueError("list buffer too small")
+    offs = np.concatenate([[0], np.cumsum(counts.astype(np.int64))])
+    return [nbr[offs[i] : offs[i + 1]].copy() for i in range(n)]
+
+
+def pair_sums(sys, state):
+    pe, w = C.c_double(), C.c_double()
+    c = sys.to_c()
+    lib().oracle_pair_sums(C.byref(c), _p(state.pos, C.c_int64), _p(state.species, C.c_uint32), state.n(), C.byref(pe), C.byref(w))
+    return pe.value, w.value
+
+
+def rdf(sys, state, bins, rmax):
+    out = np.zeros(bins, np.uint64)
+    c = sys.to_c()
+    lib().oracle_rdf(C.byref(c), _p(state.pos, C.c_int64), state.n(), bins, rmax, _p(out, C.c_uint64))
+    return out
+
+
+def profile(sys, state, bins, axis):
+    out = np.zeros(bins, np.uint64)
+    c = sys.to_c()
+    lib().oracle_profile(C.byref(c), _p(state.pos, C.c_int64), state.n(), bins, axis, _p(out, C.c_uint64))
+    return out
+
+
+def half_step_kinetic(sys, state):
+    c = sys.to_c()
+    return lib().oracle_half_step_kinetic(C.byref(c), _p(state.vel, C.c_int32), _p(state.species, C.c_uint32), state.n())
+
+
+def exact_kinetic(sys, state):
+    c = sys.to_c()
+    return lib().oracle_exact_kinetic(C.byref(c), _p(state.vel, C.c_int32), _p(state.species, C.c_uint32), state.n())
+
+
+class IntEngine:
+    """md_ref::IntEngine<F> (2D) / IntEngine3<F> (3D) on the CPU: F = f32 unless f64=True;
+    `fast` selects fast.rs's path in 2D; `integer` the all-integer tables (IntEngine::integer)."""
+
+    def __init__(self, sys, state, f64=False, fast=True, integer=False, threads=1):
+        self.sys = sys
+        self.n = state.n()
+        self.D = sys.DIM
+        self._c = sys.to_c()
+        self._h = lib().oracle_engine_create(
+            C.byref(self._c),
+            _p(state.pos, C.c_int64),
+            _p(state.vel, C.c_int32),
+            _p(state.species, C.c_uint32),
+            self.n,
+            1 if f64 else 0,
+            1 if fast else 0,
+            1 if integer else 0,
+            threads,
+        )
+        if not self._h:
+            raise ValueError("oracle engine creation failed")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_engine_destroy(self._h)
+            self._h = None
+
+    def step(self, n=1):
+        lib().oracle_engine_step(self._h, n)
+
+    def reverse(self):
+        lib().oracle_engine_reverse(self._h)
+
+    def kicks(self):
+        k = np.empty((self.n, self.D), np.int32)
+        pe = lib().oracle_engine_kicks(self._h, _p(k, C.c_int32))
+        return k, pe
+
+    @property
+    def state(self):
+        pos = np.empty((self.n, self.D), np.int64)
+        vel = np.empty((self.n, self.D), np.int32)
+        sp = np.empty(self.n, np.uint32)
+        lib().oracle_engine_state(self._h, _p(pos, C.c_int64), _p(vel, C.c_int32), _p(sp, C.c_uint32))
+        return (State if self.D == 2 else State3)(pos, vel, sp)
+
+    def set_state(self, st):
+        lib().oracle_engine_set_state(self._h, _p(st.pos, C.c_int64), _p(st.vel, C.c_int32), _p(st.species, C.c_uint32))
+
+    def hash(self):
+        return lib().oracle_engine_hash(self._h)
+
+    @property
+    def steps(self):
+        return lib().oracle_engine_steps(self._h)
+
+    def energy(self):
+        ke, pe = C.c_double(), C.c_double()
+        lib().oracle_engine_energy(self._h, C.byref(ke), C.byref(pe))
+        return ke.value, pe.value
+
+
+class FloatEngine:
+    """md_ref::FloatEngine<f64> (2D, periodic)."""
+
+    def __init__(self, sys, state):
+        self.n = state.n()
+        self._c = sys.to_c()
+        self._h = lib().oracle_float_create(C.byref(self._c), _p(state.pos, C.c_int64), _p(state.vel, C.c_int32), _p(state.species, C.c_uint32), self.n)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_float_destroy(self._h)
+            self._h = None
+
+    def step(self, n=1):
+        lib().oracle_float_step(self._h, n)
+
+    def positions(self):
+        out = np.empty((self.n, 2), np.float64)
+        lib().oracle_float_positions(self._h, _p(out, C.c_double))
+        return out
+
+    def energy(self):
+        ke, pe = C.c_double(), C.c_double()
+        lib().oracle_float_energy(self._h, C.byref(ke), C.byref(pe))
+        return ke.value, pe.value

@@ -1,0 +1,57 @@
+"""The C-ABI library: it loads without a GPU and exports every entry point include/gbmd.h
+declares (no compute calls: those need a device)."""
+
+import ctypes as C
+import os
+import re
+
+from micrographia_gb300 import _abi
+
+
+def header_functions():
+    text = open(_abi.HEADER_PATH).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbmd_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = header_functions()
+    for must in ["gbmd_create", "gbmd_step", "gbmd_sync", "gbmd_reverse", "gbmd_read_state", "gbmd_upload", "gbmd_kicks",
+                 "gbmd_energy", "gbmd_observe", "gbmd_list_stats", "gbmd_state_hash", "gbmd_destroy", "gbmd_last_error"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    for name in header_functions():
+        assert hasattr(engine_lib, name), name
+
+
+def test_python_signatures_cover_the_header():
+    declared = set(header_functions())
+    bound = {name for name, _, _ in _abi.SIGNATURES}
+    assert declared == bound, (declared - bound, bound - declared)
+
+
+def test_struct_layouts_match_the_header():
+    # sizes follow from the header's field order on LP64 (no packing pragmas)
+    assert C.sizeof(_abi.gbmd_pair) == 24
+    assert C.sizeof(_abi.gbmd_system) == 4 + 4 + 24 + 8 + 32 + 16 * 24 + 24 + 8 + 4 + 4
+    assert C.sizeof(_abi.gbmd_options) == 48
+    assert C.sizeof(_abi.gbmd_frame) == 64
+
+
+def test_host_hash_matches_the_oracle(engine_lib, O):
+    import numpy as np
+
+    from micrographia_gb300 import Pair, System, System3, box_for, cube_for
+
+    sys_ = System(box_for(300, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    s = O.fluid(sys_, 300, 1.0, 3)
+    h = O.lib().oracle_state_hash(2, s.pos.ctypes.data_as(C.POINTER(C.c_int64)), s.vel.ctypes.data_as(C.POINTER(C.c_int32)),
+                                  s.species.ctypes.data_as(C.POINTER(C.c_uint32)), s.n())
+    assert s.hash() == h
+    sys3 = System3(cube_for(256, 0.8), 0.005, Pair.lj(2.5), [1.0])
+    s3 = O.fcc_maxwell(sys3, 256, 1.0, 3)
+    h3 = O.lib().oracle_state_hash(3, s3.pos.ctypes.data_as(C.POINTER(C.c_int64)), s3.vel.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   s3.species.ctypes.data_as(C.POINTER(C.c_uint32)), s3.n())
+    assert s3.hash() == h3

@@ -1,0 +1,371 @@
+"""The CUDA engine against the oracle (md-ref's CPU engine restated), through the C ABI.
+
+Bit-exact bars: initial conditions, cell keys / starts / the stable sort permutation, Verlet lists
+(as neighbour sets), per-particle kicks and integer trajectories against IntEngine<f32> /
+IntEngine3<f32>. Tolerance bars (written at each assert): energies against the f64 engine.
+Reference tests mirrored: crates/md/tests/gpu_engine.rs, three.rs, crates/md/src/checks.rs,
+crates/gpu-prims/src/checks.rs."""
+
+import math
+
+import numpy as np
+import pytest
+
+from micrographia_gb300 import ONE, ForceMode, GpuEngine, GpuEngine3, Pair, State, System, System3, box_for, cube_for
+from micrographia_gb300 import _abi
+from micrographia_gb300.engine import init_state, make_init
+
+pytestmark = pytest.mark.gpu
+
+
+def fluid(O, n, density, pair, seed, t=1.0):
+    sys_ = System(box_for(n, density, 1.0), 0.005, pair, [1.0])
+    return sys_, O.fluid(sys_, n, t, seed)
+
+
+def equilibrated(O, n, density, pair, seed, steps=200):
+    sys_, s = fluid(O, n, density, pair, seed)
+    e = O.IntEngine(sys_, s)
+    e.step(steps)
+    return sys_, e.state
+
+
+def liquid3(O, n, density, t, seed=3):
+    sys3 = System3(cube_for(n, density), 0.005, Pair.lj(2.5), [1.0])
+    return sys3, O.fcc_maxwell(sys3, n, t, seed, jitter=0.05)
+
+
+# ---------------------------------------------------------------- initial conditions
+@pytest.mark.parametrize(
+    "recipe,dim,n,args",
+    [
+        (_abi.INIT_FLUID, 2, 3000, dict(t=1.0, seed=2026, jitter=0.1)),
+        (_abi.INIT_FLUID, 2, 1, dict(t=1.0, seed=5, jitter=0.1)),
+        (_abi.INIT_TRIANGULAR, 2, 4096, dict(t=0.8, seed=1, jitter=0.1)),
+        (_abi.INIT_FCC, 3, 4000, dict(t=1.0, seed=3, jitter=0.05)),
+        (_abi.INIT_FCC, 3, 4 * 8**3, dict(t=0.72, seed=1, jitter=0.05)),
+        (_abi.INIT_SLAB, 2, 20000, dict(t=0.45, seed=7, jitter=0.1)),
+    ],
+)
+def test_seeded_init_is_bit_identical(O, recipe, dim, n, args):
+    if dim == 2:
+        rho = 0.2125 if recipe == _abi.INIT_SLAB else 0.7
+        sys_ = System(box_for(n, rho, 4.0 if recipe == _abi.INIT_SLAB else 1.0), 0.005, Pair.lj(2.5), [1.0])
+    else:
+        sys_ = System3(cube_for(n, 0.8442), 0.005, Pair.lj(2.5), [1.0])
+    spec = make_init(recipe, n, args["t"], args["seed"], args["jitter"], 0.7, 0.05, 0.25)
+    want = O.init(sys_, spec)
+    got = init_state(sys_, recipe, n, args["t"], args["seed"], args["jitter"], 0.7, 0.05, 0.25)
+    assert np.array_equal(got.pos, want.pos)
+    assert np.array_equal(got.vel, want.vel)
+    assert np.array_equal(got.species, want.species)
+    assert got.velocity_sum() == [0] * dim
+
+
+def test_libm_restatement_on_device_matches_over_many_draws(O):
+    """Millions of Box–Muller draws (log, cos): the device velocities equal the oracle's."""
+    n = 1 << 20
+    sys3 = System3(cube_for(n, 0.8442), 0.005, Pair.lj(2.5), [1.0])
+    got = init_state(sys3, _abi.INIT_FCC, n, 0.72, 12345, 0.05)
+    want = O.init(sys3, make_init(_abi.INIT_FCC, n, 0.72, 12345, 0.05))
+    assert np.array_equal(got.vel, want.vel)
+    assert np.array_equal(got.pos, want.pos)
+
+
+# ---------------------------------------------------------------- binning (gpu-prims checks.rs:30-149)
+SIZES = [1, 2, 255, 256, 257, 1023, 1024, 1025, 4097, 65537, (1 << 20) + 3]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_binning_matches_cell_list(O, n):
+    rng = np.random.default_rng(n)
+    sys_ = System(box_for(max(n, 200), 0.7, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    pos = np.stack([rng.integers(0, sys_.box_len[a], n) for a in range(2)], 1).astype(np.int64)
+    st = State(pos, np.zeros((n, 2), np.int32), np.zeros(n, np.uint32))
+    dims = sys_.cells_for(2.5)
+    with GpuEngine(sys_, st, ForceMode.cell_list()) as e:
+        keys, start, items, order = e.debug_bin(dims)
+    assert np.array_equal(order, np.arange(n))
+    wk, ws, wi = O.cell_list(sys_, st, dims)
+    assert np.array_equal(keys, wk)
+    assert np.array_equal(start, ws)
+    assert np.array_equal(items, wi)
+
+
+def test_binning_all_one_key(O):
+    n = 300_001
+    sys_ = System(box_for(n, 0.7, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    pos = np.full((n, 2), ONE // 3, np.int64)
+    pos[:, 0] += np.arange(n) % 1000
+    st = State(pos, np.zeros((n, 2), np.int32), np.zeros(n, np.uint32))
+    dims = sys_.cells_for(2.5)
+    with GpuEngine(sys_, st, ForceMode.cell_list()) as e:
+        keys, start, items, _ = e.debug_bin(dims)
+    wk, ws, wi = O.cell_list(sys_, st, dims)
+    assert np.array_equal(keys, wk) and np.array_equal(start, ws) and np.array_equal(items, wi)
+
+
+def test_binning_3d(O):
+    sys3, st = liquid3(O, 32000, 0.8442, 0.72)
+    dims = sys3.cells_for(2.8)
+    with GpuEngine3(sys3, st) as e:
+        keys, start, items, _ = e.debug_bin(dims)
+    wk, ws, wi = O.cell_list(sys3, st, dims)
+    assert np.array_equal(keys, wk) and np.array_equal(start, ws) and np.array_equal(items, wi)
+
+
+# ---------------------------------------------------------------- Verlet lists
+def test_verlet_lists_match_2d(O):
+    sys_, st = equilibrated(O, 3000, 0.7, Pair.lj(2.5), 1, steps=50)
+    with GpuEngine(sys_, st, ForceMode.verlet_with_skin(sys_, 3000, 0.3)) as e:
+        got = e.debug_list()
+    want = O.verlet_lists(sys_, st, 0.3)
+    for i in range(st.n()):
+        assert np.array_equal(got[i], want[i]), i
+
+
+def test_verlet_lists_match_3d(O):
+    sys3, st = liquid3(O, 4000, 0.8442, 0.72)
+    with GpuEngine3(sys3, st, ForceMode.verlet_with_skin(sys3, 4000, 0.3)) as e:
+        got = e.debug_list()
+    want = O.verlet_lists(sys3, st, 0.3)
+    for i in range(st.n()):
+        assert np.array_equal(got[i], want[i]), i
+
+
+# ---------------------------------------------------------------- kicks (gpu_engine.rs:27-60; three.rs:33-64)
+@pytest.mark.parametrize("pair", [Pair.wca(), Pair.lj(2.5)])
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_kicks_are_bit_identical_2d(O, pair, mode):
+    sys_, s = equilibrated(O, 3000, 0.7, pair, 1)
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_for(sys_, 3000)
+    with GpuEngine(sys_, s, m) as g:
+        kg, peg = g.kicks()
+    k32, pe32 = O.IntEngine(sys_, s).kicks()
+    k64, _ = O.IntEngine(sys_, s, f64=True).kicks()
+    assert np.array_equal(kg, k32), f"{(kg != k32).any(axis=1).sum()} kicks differ"
+    rel64 = math.sqrt(((kg.astype(np.float64) - k64) ** 2).sum() / (k64.astype(np.float64) ** 2).sum())
+    assert rel64 < 1e-5  # md-ref physics.rs:144
+    assert abs((peg - pe32) / pe32) < 1e-5  # f64 sum of the same f32 pair energies, other order
+
+
+def test_kicks_are_bit_identical_3d(O):
+    sys3, s = liquid3(O, 4000, 0.8, 1.0)
+    cpu = O.IntEngine(sys3, s)
+    cpu.step(100)
+    st = cpu.state
+    with GpuEngine3(sys3, st) as g:
+        kg, peg = g.kicks()
+    kc, pec = cpu.kicks()
+    k64, _ = O.IntEngine(sys3, st, f64=True).kicks()
+    assert np.array_equal(kg, kc)
+    rel64 = math.sqrt(((kg.astype(np.float64) - k64) ** 2).sum() / (k64.astype(np.float64) ** 2).sum())
+    assert rel64 < 1e-5
+    assert abs((peg - pec) / pec) < 1e-5
+
+
+def test_kicks_binary_mixture(O):
+    sys_ = System(box_for(3000, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 3.0]).with_pair(0, 1, Pair(0.6, 1.1, 2.5))
+    s = O.fluid(sys_, 3000, 1.0, 1)
+    s.species[::3] = 1
+    s.vel = O.maxwell(sys_, s.species, 1.0, 1)
+    cpu = O.IntEngine(sys_, s)
+    cpu.step(100)
+    st = cpu.state
+    for mode in (ForceMode.cell_list(), ForceMode.verlet_for(sys_, 3000)):
+        with GpuEngine(sys_, st, mode) as g:
+            kg, _ = g.kicks()
+        assert np.array_equal(kg, cpu.kicks()[0])
+
+
+# ---------------------------------------------------------------- trajectories
+def test_trajectory_is_bit_identical_2d_cells(O):
+    sys_, s0 = fluid(O, 2000, 0.6, Pair.wca(), 7)
+    with GpuEngine(sys_, s0, ForceMode.cell_list()) as g:
+        c = O.IntEngine(sys_, s0)
+        for _ in range(4):
+            g.step(50)
+            c.step(50)
+            assert g.read_state() == c.state
+
+
+def test_trajectory_is_bit_identical_2d_verlet(O):
+    sys_, s0 = fluid(O, 4096, 0.7, Pair.lj(2.5), 11, t=0.8)
+    with GpuEngine(sys_, s0, ForceMode.verlet_with_skin(sys_, 4096, 0.3)) as g:
+        c = O.IntEngine(sys_, s0)
+        g.step(333)
+        c.step(333)
+        assert g.read_state() == c.state
+        rebuilds, overflow = g.read_list_stats()
+        assert not overflow and rebuilds > 1
+
+
+def test_trajectory_is_bit_identical_3d_verlet(O):
+    sys3, s0 = liquid3(O, 4000, 0.8442, 0.72)
+    with GpuEngine3(sys3, s0, ForceMode.verlet_with_skin(sys3, 4000, 0.3)) as g:
+        c = O.IntEngine(sys3, s0)
+        g.step(120)
+        c.step(120)
+        assert g.read_state() == c.state
+
+
+def test_config1_triangular_4096_1000_steps(O):
+    """2D LJ N=4096, rho 0.70, triangular start, T=0.8, seed 1, cell list, 1000 steps: the GPU
+    state equals md-ref's IntEngine<f32> bit for bit."""
+    sys_ = System(box_for(4096, 0.7, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    s0 = O.init(sys_, make_init(_abi.INIT_TRIANGULAR, 4096, 0.8, 1, 0.1))
+    with GpuEngine(sys_, s0, ForceMode.cell_list()) as g:
+        c = O.IntEngine(sys_, s0)
+        g.step(1000)
+        c.step(1000)
+        assert g.read_state().hash() == c.hash()
+
+
+# ---------------------------------------------------------------- exactness properties (gpu_engine.rs:62-132, 256-273)
+def test_run_to_run_identical(O):
+    sys_, s = fluid(O, 5000, 0.6, Pair.wca(), 2)
+    hs = []
+    for _ in range(2):
+        with GpuEngine(sys_, s, ForceMode.verlet_for(sys_, 5000)) as g:
+            g.step(500)
+            hs.append(g.read_state().hash())
+    assert hs[0] == hs[1] and hs[0] != s.hash()
+
+
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_reversal_is_exact(O, mode):
+    sys_, s0 = fluid(O, 5000, 0.6, Pair.wca(), 3)
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_for(sys_, 5000)
+    with GpuEngine(sys_, s0, m) as g:
+        g.step(800)
+        g.reverse()
+        g.step(800)
+        g.reverse()
+        assert g.read_state().hash() == s0.hash()
+        assert g.steps == 0
+
+
+def test_one_bit_flip_breaks_reversal(O):
+    sys_, s0 = fluid(O, 5000, 0.6, Pair.wca(), 4)
+    with GpuEngine(sys_, s0, ForceMode.verlet_for(sys_, 5000)) as g:
+        g.step(2000)
+        g.flip_bit(17, 0, 0)
+        g.reverse()
+        g.step(2000)
+        g.reverse()
+        differ, _ = g.read_state().position_difference(s0, sys_)
+    assert differ > 4000
+
+
+def test_storage_order_does_not_matter(O):
+    sys_, s0 = fluid(O, 4000, 0.6, Pair.wca(), 5)
+    perm = np.random.default_rng(5).permutation(4000)
+    with GpuEngine(sys_, s0, ForceMode.verlet_for(sys_, 4000)) as a, GpuEngine(sys_, s0.permuted(perm), ForceMode.verlet_for(sys_, 4000)) as b:
+        a.step(500)
+        b.step(500)
+        assert a.read_state().hash() == b.read_state().unpermuted(perm).hash()
+
+
+def test_momentum_is_exactly_conserved(O):
+    sys_, s0 = fluid(O, 4000, 0.6, Pair.lj(2.5), 6)
+    with GpuEngine(sys_, s0, ForceMode.verlet_for(sys_, 4000)) as g:
+        g.step(1000)
+        assert g.read_state().velocity_sum() == [0, 0]
+
+
+@pytest.mark.parametrize("pair,density", [(Pair.wca(), 0.6), (Pair.lj(2.5), 0.7)])
+def test_cell_list_and_verlet_lists_give_identical_trajectories(O, pair, density):
+    sys_, s0 = fluid(O, 6000, density, pair, 10)
+    with GpuEngine(sys_, s0, ForceMode.cell_list()) as a, GpuEngine(sys_, s0, ForceMode.verlet_for(sys_, 6000)) as b:
+        a.step(1500)
+        b.step(1500)
+        rebuilds, overflow = b.read_list_stats()
+        assert not overflow and 1 < rebuilds < 1500
+        assert a.read_state().hash() == b.read_state().hash()
+
+
+def test_3d_cells_equal_verlet(O):
+    sys3, s0 = liquid3(O, 6000, 0.8, 1.0)
+    with GpuEngine3(sys3, s0, ForceMode.cell_list()) as a, GpuEngine3(sys3, s0) as b:
+        a.step(1000)
+        b.step(1000)
+        assert a.read_state().hash() == b.read_state().hash()
+        assert b.read_list_stats()[0] > 10
+
+
+def test_upload_and_counters(O):
+    sys_, s0 = fluid(O, 3000, 0.6, Pair.lj(2.5), 8)
+    with GpuEngine(sys_, s0, ForceMode.verlet_for(sys_, 3000)) as g:
+        g.step(100)
+        mid = g.read_state()
+        g.step(7)
+        g.upload(mid)
+        g.step(7)
+        c = O.IntEngine(sys_, mid)
+        c.step(7)
+        assert g.read_state() == c.state
+        assert g.steps == 114
+
+
+# ---------------------------------------------------------------- energies and instruments
+def test_energy_is_conserved_wca(O):
+    """gpu_engine.rs:166-183: drift < 2e-3 per particle (against the f64 CPU energy)."""
+    sys_, s0 = fluid(O, 4000, 0.6, Pair.wca(), 8)
+    with GpuEngine(sys_, s0, ForceMode.verlet_for(sys_, 4000)) as g:
+        g.step(500)
+        energy = lambda s: sum(O.IntEngine(sys_, s, f64=True).energy()) / s.n()
+        e0 = energy(g.read_state())
+        worst = 0.0
+        for _ in range(5):
+            g.step(1000)
+            worst = max(worst, abs(energy(g.read_state()) - e0))
+    assert worst < 2e-3
+
+
+def test_frame_matches_oracle(O):
+    sys_, s = equilibrated(O, 3000, 0.7, Pair.lj(2.5), 4)
+    ke64, pe64 = O.IntEngine(sys_, s, f64=True).energy()
+    pe32, w32 = O.pair_sums(sys_, s)
+    with GpuEngine(sys_, s, ForceMode.verlet_for(sys_, 3000)) as g:
+        f, rdf, prof = g.observe(rdf_bins=200, rdf_rmax=5.0, profile_bins=80, profile_axis=0)
+        ke, pe = g.energy()
+    assert abs(f.potential - pe32) < 1e-9 * abs(pe32)  # same f32 terms, f64 sums in another order
+    assert abs(f.virial - w32) < 1e-9 * abs(w32)
+    assert abs(f.kinetic - ke64) < 1e-9 * ke64  # on-step KE from the same integer velocities
+    assert abs(f.potential - pe64) < 1e-5 * abs(pe64)  # f32 pair terms against the f64 engine
+    n, vol = 3000, sys_.volume()
+    assert abs(f.temperature - f.kinetic / (n - 1)) < 1e-12
+    assert abs(f.pressure - (n / vol * f.temperature + f.virial / (2 * vol))) < 1e-9
+    assert np.array_equal(rdf, O.rdf(sys_, s, 200, 5.0))
+    assert np.array_equal(prof, O.profile(sys_, s, 80, 0))
+    assert (ke, pe) == (f.kinetic, f.potential)
+
+
+def test_frame_3d(O):
+    sys3, s = liquid3(O, 4000, 0.8442, 0.72)
+    pe32, w32 = O.pair_sums(sys3, s)
+    with GpuEngine3(sys3, s) as g:
+        f, rdf, _ = g.observe(rdf_bins=200, rdf_rmax=5.0)
+    assert abs(f.potential - pe32) < 1e-9 * abs(pe32)
+    assert abs(f.virial - w32) < 1e-9 * abs(w32)
+    assert np.array_equal(rdf, O.rdf(sys3, s, 200, 5.0))
+
+
+# ---------------------------------------------------------------- full size (configs 2): size-independent properties
+def test_config2_full_size_properties(O):
+    """3D FCC N=1,048,576, rho 0.8442, T 0.72, skin 0.3: momentum stays exactly zero, the run
+    reverses bit for bit, and the lists never overflow."""
+    n = 1 << 20
+    sys3 = System3(cube_for(n, 0.8442), 0.005, Pair.lj(2.5), [1.0])
+    spec = make_init(_abi.INIT_FCC, n, 0.72, 1, 0.05)
+    with GpuEngine3(sys3, None, ForceMode.verlet_with_skin(sys3, n, 0.3), init=spec) as g:
+        s0 = g.read_state()
+        g.step(100)
+        s1 = g.read_state()
+        assert s1.velocity_sum() == [0, 0, 0]
+        rebuilds, overflow = g.read_list_stats()
+        assert not overflow and rebuilds >= 2
+        g.reverse()
+        g.step(100)
+        g.reverse()
+        assert g.read_state().hash() == s0.hash()

@@ -1,0 +1,290 @@
+"""The oracle against the reference's own known answers and property tests (CPU only).
+
+Pins: Random123 Threefry KATs (crates/gpu-prims/src/threefry.rs:52-70), GOLDEN_INT_HASH
+(crates/md/src/checks.rs:155-167, crates/md/tests/integer.rs:250-264), fixed-point separation
+identities (crates/md-core/src/fixed.rs:74-99, crates/md-ref/tests/fast_path.rs:56-79), and the
+md-ref property tests (crates/md-ref/tests/physics.rs, fast_path.rs)."""
+
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from micrographia_gb300 import ONE, Pair, System, System3, box_for, cube_for, fcc_cells, to_f64
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+VEC = json.load(open(os.path.join(HERE, "golden", "reference_vectors.json")))
+
+
+def wca_fluid(O, n, density, t, seed, masses=(1.0,)):
+    sys_ = System(box_for(n, density, 1.0), 0.005, Pair.wca(), list(masses))
+    return sys_, O.fluid(sys_, n, t, seed)
+
+
+def test_threefry_known_answers(O):
+    assert len(VEC["threefry_kat"]) == 9
+    for k in VEC["threefry_kat"]:
+        assert O.threefry(k["ctr"], k["key"], k["rounds"]) == k["want"], k
+
+
+def test_golden_int_hash(O):
+    """All-integer forces, 3000-particle binary LJ mixture, 1000 steps: the reference's hash."""
+    sys_ = System(box_for(3000, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 2.0]).with_pair(0, 1, Pair(0.7, 1.05, 2.5))
+    s = O.fluid(sys_, 3000, 1.0, 2026)
+    s.species[::4] = 1
+    s.vel = O.maxwell(sys_, s.species, 1.0, 2026)
+    e = O.IntEngine(sys_, s, f64=True, integer=True)
+    e.step(1000)
+    assert e.hash() == int(VEC["golden_int_hash"], 16)
+
+
+def test_separation_identities(O):
+    # fixed.rs:90-98
+    for d in [1, 15, 16, 17, ONE, ONE + 7, 3 * ONE // 2, 8 * ONE - 1, 123_456_789]:
+        a, b = O.sep_f32(-d), O.sep_f32(d)
+        assert np.float32(a).tobytes() == np.float32(-b).tobytes()
+    assert O.sep_f32(8 * ONE) is None
+    assert O.sep_f32(-8 * ONE) is not None
+    assert abs(O.sep_f32(ONE + ONE // 4) - 1.25) < 1e-7
+
+
+def test_sep_near_matches_sep_f32(O):
+    # fast_path.rs:56-79 (xorshift over four ranges, 2M draws)
+    lim = 8 * ONE
+    x = 0x9E3779B97F4A7C15
+    m64 = (1 << 64) - 1
+    checked = 0
+    for k in range(200_000):
+        x ^= (x << 13) & m64
+        x ^= x >> 7
+        x ^= (x << 17) & m64
+        r = k % 4
+        if r == 0:
+            d = (x % (2 * lim)) - lim
+        elif r == 1:
+            d = (x % 1024) - 512
+        elif r == 2:
+            d = ((x % 64) - 32) << 32
+        else:
+            d = (x % (2 * lim)) - lim + 1
+        if d >= lim or d < -lim:
+            continue
+        a = np.float32(O.lib().oracle_sep_near(d)).tobytes()
+        b = np.float32(O.sep_f32(d)).tobytes()
+        assert a == b, d
+        checked += 1
+    assert checked > 150_000
+
+
+def test_box_helpers_match_host_mirror(O):
+    for n, rho, asp in [(4096, 0.7, 1.0), (3000, 0.6, 1.0), (16_777_216, 0.2125, 4.0), (500, 0.7, 2.0)]:
+        assert O.box_for(n, rho, asp) == box_for(n, rho, asp)
+    for n, rho in [(1_048_576, 0.8442), (4000, 0.8), (500, 1.0)]:
+        b = cube_for(n, rho)
+        assert O.cube_for(n, rho) == b
+        assert O.fcc_cells(n, b) == fcc_cells(n, b)
+    assert fcc_cells(4 * 64**3, cube_for(4 * 64**3, 0.8442)) == [64, 64, 64]
+    assert O.lib().oracle_wca_rc() == Pair.wca().rc
+    for p in [Pair.lj(2.5), Pair.wca(), Pair(0.7, 1.05, 2.5)]:
+        assert O.lib().oracle_pair_shift(p.eps, p.sigma, p.rc) == p.shift()
+
+
+def test_zero_sum_is_exact_and_temperature(O):
+    # init.rs:175-182
+    sys_, s = wca_fluid(O, 1000, 0.5, 1.3, 9)
+    assert s.velocity_sum() == [0, 0]
+    t = O.half_step_kinetic(sys_, s) / (s.n() - 1)
+    assert abs(t - 1.3) < 0.1
+
+
+def test_lattice_inside_box(O):
+    # init.rs:185-189
+    b = box_for(500, 0.7, 2.0)
+    sys_ = System(b, 0.005, Pair.wca(), [1.0])
+    s = O.fluid(sys_, 500, 1.0, 1)
+    assert (s.pos >= 0).all() and (s.pos[:, 0] < b[0]).all() and (s.pos[:, 1] < b[1]).all()
+
+
+def test_fcc_geometry_and_3d_maxwell(O):
+    # three.rs:410-446
+    n = 4 * 5 * 5 * 5
+    b = cube_for(n, 1.0)
+    assert fcc_cells(n, b) == [5, 5, 5]
+    sys3 = System3(b, 0.005, Pair.wca(), [1.0])
+    s = O.fcc_maxwell(sys3, n, 1.0, 1, jitter=0.0)
+    p = s.pos.astype(np.float64) / ONE
+    l = to_f64(b[0])
+    d = p[:50, None, :] - p[None, :, :]
+    d -= l * np.round(d / l)
+    r = np.sqrt((d**2).sum(-1))
+    r[r == 0] = 1e9
+    assert abs(r.min() - 4 ** (1 / 3) / math.sqrt(2)) < 1e-6
+    n = 4000
+    sys3 = System3(cube_for(n, 0.5), 0.005, Pair.wca(), [1.0])
+    s = O.fcc_maxwell(sys3, n, 1.3, 2, jitter=0.0)
+    assert s.velocity_sum() == [0, 0, 0]
+    v = s.vel.astype(np.float64) / ONE / 0.005
+    assert abs(0.5 * (v**2).sum() / (1.5 * n) - 1.3) < 0.05
+    vel = O.set_temperature(sys3, s, 0.7)
+    v = vel.astype(np.float64) / ONE / 0.005
+    assert abs(0.5 * (v**2).sum() / (1.5 * (n - 1)) - 0.7) < 1e-3
+    assert vel.astype(np.int64).sum(axis=0).tolist() == [0, 0, 0]
+
+
+def test_reversal_is_exact(O):
+    # physics.rs:17-37
+    for f64 in (False, True):
+        sys_, s0 = wca_fluid(O, 400, 0.6, 1.0, 1)
+        e = O.IntEngine(sys_, s0, f64=f64)
+        e.step(1500)
+        assert e.state != s0
+        e.reverse()
+        e.step(1500)
+        e.reverse()
+        assert e.state == s0
+        assert e.steps == 0
+
+
+def test_one_bit_flip_breaks_reversal(O):
+    # physics.rs:39-51
+    sys_, s0 = wca_fluid(O, 400, 0.6, 1.0, 2)
+    e = O.IntEngine(sys_, s0)
+    e.step(3000)
+    st = e.state
+    st.flip_bit(0, 0, 0)
+    e.set_state(st)
+    e.reverse()
+    e.step(3000)
+    e.reverse()
+    differ, mx = e.state.position_difference(s0, sys_)
+    assert differ > 300 and mx > 0.5
+
+
+def test_storage_order_does_not_matter(O):
+    # physics.rs:53-69
+    sys_, s0 = wca_fluid(O, 500, 0.6, 1.0, 3)
+    perm = np.random.default_rng(11).permutation(500)
+    a = O.IntEngine(sys_, s0)
+    b = O.IntEngine(sys_, s0.permuted(perm))
+    a.step(500)
+    b.step(500)
+    assert b.state.unpermuted(perm) == a.state
+
+
+def test_momentum_is_exactly_conserved(O):
+    sys_, s0 = wca_fluid(O, 500, 0.6, 1.0, 4)
+    assert s0.velocity_sum() == [0, 0]
+    e = O.IntEngine(sys_, s0)
+    for _ in range(5):
+        e.step(100)
+        assert e.state.velocity_sum() == [0, 0]
+
+
+def test_integer_and_float_engines_agree_initially(O):
+    # physics.rs:109-127
+    sys_, s0 = wca_fluid(O, 400, 0.6, 1.0, 6)
+    i = O.IntEngine(sys_, s0, f64=True)
+    f = O.FloatEngine(sys_, s0)
+    i.step(20)
+    f.step(20)
+    p = i.state.pos.astype(np.float64) / ONE
+    q = f.positions()
+    b = np.array(sys_.box_f64())
+    d = np.abs(p - q)
+    d = np.minimum(d, b - d)
+    assert d.max() < 1e-7
+
+
+def test_f32_kicks_match_f64_kicks(O):
+    # physics.rs:129-146
+    sys_, s0 = wca_fluid(O, 1000, 0.7, 1.0, 7)
+    k32, pe32 = O.IntEngine(sys_, s0).kicks()
+    k64, pe64 = O.IntEngine(sys_, s0, f64=True).kicks()
+    rel = math.sqrt(((k32.astype(np.float64) - k64) ** 2).sum() / (k64.astype(np.float64) ** 2).sum())
+    assert rel < 1e-5
+    assert abs((pe32 - pe64) / pe64) < 1e-5
+
+
+def test_fast_path_matches_the_reference(O):
+    # fast_path.rs:20-54 (the periodic cases)
+    sys_ = System(box_for(2000, 0.7, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    st = O.fluid(sys_, 2000, 0.8, 1)
+    a, b = O.IntEngine(sys_, st, fast=True), O.IntEngine(sys_, st, fast=False)
+    a.step(300)
+    b.step(300)
+    assert a.state == b.state
+    ea, eb = a.kicks()[1], b.kicks()[1]
+    assert abs(ea - eb) < 1e-4 * max(abs(eb), 1.0)
+    # a periodic WCA mixture of three masses and two sizes
+    wca = lambda s: Pair(1.0, s, s * 2 ** (1 / 6))
+    sys_ = System(box_for(1500, 0.3, 1.5), 0.005, wca(1.0), [1.0, 4.0, 30.0]).with_pair(0, 2, wca(2.0)).with_pair(1, 2, wca(2.0)).with_pair(2, 2, wca(3.0))
+    st = O.fluid(sys_, 1500, 1.0, 2)
+    for i in range(1500):
+        st.species[i] = 2 if i % 50 == 0 else i % 2
+    big = st.pos[st.species == 2].astype(np.float64) / ONE
+    keep = [i for i in range(1500) if st.species[i] == 2 or (((big - st.pos[i] / ONE) ** 2).sum(axis=1) > 4.0).all()]
+    st = type(st)(st.pos[keep], st.vel[keep], st.species[keep])
+    a, b = O.IntEngine(sys_, st, fast=True), O.IntEngine(sys_, st, fast=False)
+    a.step(300)
+    b.step(300)
+    assert a.state == b.state
+
+
+def test_integer_kicks_are_antisymmetric_and_accurate(O):
+    # table.rs:113-136
+    import ctypes as C
+
+    sys_ = System(box_for(100, 0.5, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    c = sys_.to_c()
+    worst = 0.0
+    for k in range(0, 2000, 7):
+        r = 0.8 + 1.69 * k / 2000.0
+        a = 0.3 + k * 0.001
+        d = (C.c_int64 * 2)(int(round(r * math.cos(a) * ONE)), int(round(r * math.sin(a) * ONE)))
+        dm = (C.c_int64 * 2)(-d[0], -d[1])
+        ki, kj = (C.c_int32 * 2)(), (C.c_int32 * 2)()
+        assert O.lib().oracle_int_kick(C.byref(c), 0, 0, d, ki) == 1
+        assert O.lib().oracle_int_kick(C.byref(c), 0, 0, dm, kj) == 1
+        assert [ki[0], ki[1]] == [-kj[0], -kj[1]]
+        f = sys_.pair(0, 0).f_over_r(r * r) * sys_.kick_coeff(0)
+        exact = [-f * r * math.cos(a), -f * r * math.sin(a)]
+        for ax in range(2):
+            worst = max(worst, abs(ki[ax] - exact[ax]) / (20.0 + 1e-5 * abs(exact[ax])))
+    assert worst < 1.0
+
+
+def test_cells_and_lists_are_consistent(O):
+    """The Verlet-list restatement holds every pair within rc (the list invariant)."""
+    sys_ = System(box_for(1500, 0.7, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    st = O.fluid(sys_, 1500, 1.0, 3)
+    lists = O.verlet_lists(sys_, st, 0.3)
+    p = st.pos.astype(np.float64) / ONE
+    b = np.array(sys_.box_f64())
+    for i in range(0, 1500, 37):
+        d = p - p[i]
+        d -= b * np.round(d / b)
+        r = np.sqrt((d**2).sum(1))
+        within = set(np.nonzero((r < 2.5) & (np.arange(1500) != i))[0].tolist())
+        assert within <= set(lists[i].tolist())
+        assert all(r[j] < 2.81 for j in lists[i])
+
+
+def test_cell_list_is_a_stable_counting_sort(O):
+    sys_ = System(box_for(3000, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    st = O.fluid(sys_, 3000, 1.0, 5)
+    dims = sys_.cells_for(2.5)
+    keys, start, items = O.cell_list(sys_, st, dims)
+    want = np.argsort(keys, kind="stable")
+    assert (items == want).all()
+    assert start[-1] == 3000 and (np.diff(start.astype(np.int64)) >= 0).all()
+
+
+def test_rescale_thermostat_is_exact(O):
+    sys_, s = wca_fluid(O, 2000, 0.5, 1.7, 4)
+    vel = O.set_temperature(sys_, s, 0.45, exact=True)
+    assert vel.astype(np.int64).sum(axis=0).tolist() == [0, 0]
+    s2 = type(s)(s.pos, vel, s.species)
+    t = O.exact_kinetic(sys_, s2) / (s.n() - 1)
+    assert abs(t - 0.45) < 1e-3
