@@ -38,7 +38,7 @@ RHO, T0, SEED, SKIN, RC, DT = 0.8442, 0.72, 1, 0.3, 2.5, 0.005
 
 def config_dict(extra=None):
     d = {
-        "workload": "3D LJ liquid NVE, FCC N=1048576, rho 0.8442, T 0.72, rc 2.5, skin 0.3, dt 0.005 (configs[1], plain form)",
+        "workload": f"3D LJ liquid NVE, FCC N={N_ATOMS}, rho 0.8442, T 0.72, rc 2.5, skin 0.3, dt 0.005 (configs[1], plain form)",
         "n_atoms": N_ATOMS,
         "density": RHO,
         "temperature": T0,
@@ -184,7 +184,7 @@ def cpu_baseline(seconds_budget=20.0, threads=None):
         "unit": UNIT,
         "cores": threads,
         "kind": "port",
-        "sample": f"{done} full steps of the 1,048,576-atom system after 1 warm-up step ({dt:.1f} s), IntEngine3<f32> reference loop",
+        "sample": f"{done} full steps of the {N_ATOMS}-atom system after 1 warm-up step ({dt:.1f} s), IntEngine3<f32> reference loop",
     }
 
 
@@ -344,7 +344,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--atoms", type=int, default=N_ATOMS, help="atoms (default 1,048,576; smaller only for profiling)")
     args = ap.parse_args()
+    global N_ATOMS
+    N_ATOMS = args.atoms
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     world, rank, local, pg = dist_setup()
