@@ -205,6 +205,30 @@ int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, int64_t* pos,
 int gbmd_create_seeded(const gbmd_system* sys, const gbmd_init* spec, const gbmd_options* opts,
                        gbmd_engine** out);
 
+/* ---- Cell binning without device allocation ---- */
+
+/* Largest particle count gbmd_bin_cells_static accepts. */
+#define GBMD_BIN_STATIC_MAX_N 262144u
+
+/* No counterpart in the reference. The cell binning of gbmd_debug_bin (row-major f64 cell keys,
+ * the stable sort permutation and the cell starts of md_ref::CellList::build) for callers that
+ * cannot allocate device memory: a host that gives the library a fixed arena at start-up and
+ * allows no later cudaMalloc, or a stream-ordered hot path where cudaMalloc/cudaFree would
+ * synchronise the device. All pointers except `sys` and `cells` are DEVICE pointers the caller
+ * owns: `pos` holds n id-ordered interleaved int64 positions (n * dim), and the outputs are
+ * keys[n], start[ncell + 1] and items[n]. `stream` is a cudaStream_t (NULL: the legacy default
+ * stream); the work is enqueued on it and the call returns without waiting.
+ * The scratch is one static device array of about 4.3 MB (4 * GBMD_BIN_STATIC_MAX_N words plus
+ * the sort's histograms), which every GPU that loads the library holds until the process
+ * exits; n above GBMD_BIN_STATIC_MAX_N is rejected with GBMD_E_INVALID. The first call on each
+ * device looks up that array's device address (cudaGetSymbolAddress, with that device current),
+ * so make the first call on a device before any stream capture. Every call shares the one
+ * array: calls that overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller. The array keeps the last call's contents; nothing in it needs to
+ * start at zero, since every word a call reads it has written first. */
+int gbmd_bin_cells_static(const gbmd_system* sys, const int64_t* pos, uint32_t n, const uint32_t* cells,
+                          uint32_t* keys, uint32_t* start, uint32_t* items, void* stream);
+
 /* ---- Batched replicas: many independent periodic systems in one persistent launch ---- */
 
 typedef struct gbmd_batch gbmd_batch;

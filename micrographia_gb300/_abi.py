@@ -31,6 +31,8 @@ INIT_TRIANGULAR = 1
 INIT_FCC = 2
 INIT_SLAB = 3
 
+BIN_STATIC_MAX_N = 262144  # GBMD_BIN_STATIC_MAX_N
+
 
 class gbmd_pair(C.Structure):
     _fields_ = [("eps", C.c_double), ("sigma", C.c_double), ("rc", C.c_double)]
@@ -146,6 +148,7 @@ SIGNATURES = [
     ("gbmd_debug_list", C.c_int, [VP, _U32P, _U32P, C.c_uint64]),
     ("gbmd_init_state", C.c_int, [P(gbmd_system), P(gbmd_init), _I64P, _I32P, _U32P]),
     ("gbmd_create_seeded", C.c_int, [P(gbmd_system), P(gbmd_init), P(gbmd_options), P(VP)]),
+    ("gbmd_bin_cells_static", C.c_int, [P(gbmd_system), C.c_void_p, C.c_uint32, _U32P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("gbmd_batch_create", C.c_int, [P(gbmd_system), C.c_uint32, _U32P, _I64P, _I32P, _U32P, P(gbmd_options), P(VP)]),
     ("gbmd_batch_step", C.c_int, [VP, C.c_uint64]),
     ("gbmd_batch_sync", C.c_int, [VP]),
