@@ -338,6 +338,7 @@ def run_ours(args, world, rank, local, pg):
 
 
 def main():
+    global N_ATOMS
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
@@ -346,7 +347,6 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="atoms (default 1,048,576; smaller only for profiling)")
     args = ap.parse_args()
-    global N_ATOMS
     N_ATOMS = args.atoms
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
