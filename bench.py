@@ -337,6 +337,151 @@ def run_ours(args, world, rank, local, pg):
     return 0
 
 
+def run_c4(args, world, rank, local, pg):
+    """configs[3]: 1024 uneven 2D systems; batched (one persistent launch per step, 100-step
+    graphs) against the plain form (one engine per system, each on its own stream)."""
+    import torch
+
+    from micrographia_gb300 import BatchEngine, ForceMode, GpuEngine, init_state, workloads
+
+    torch.cuda.set_device(local)
+    cfg = workloads.config4(args.systems)
+    systems = [s for s, _ in cfg]
+    states = [init_state(s, sp.recipe, sp.n, sp.t, sp.seed, sp.jitter) for s, sp in cfg]
+    total = sum(st.n() for st in states)
+    mode = ForceMode.verlet_with_skin(None, 0, SKIN)
+    K = args.steps
+
+    batch = BatchEngine(systems, states, mode, block_steps=100, device=local)
+    bstream = torch.cuda.ExternalStream(batch.stream())
+    batch.step(args.warmup)
+    batch.wait()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0, r0 = batch.stats()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(bstream)
+    batch.step(K)
+    ev1.record(bstream)
+    ev1.synchronize()
+    ms_b = ev0.elapsed_time(ev1)
+    batch.wait()
+    clk = clocks.stop()
+    l1, r1 = batch.stats()
+    value = world * total * K / (ms_b * 1e-3)
+    # bit-exactness spot check: the first and last replicas against their plain runs
+    checks = {}
+    plain = [GpuEngine(s, st, mode, device=local) for s, st in zip(systems, states)]
+    for e in plain:
+        e.step(args.warmup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e in plain:
+        e.step(K)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    value_plain = total * K / t_plain
+    for k in (0, len(systems) - 1):
+        checks[k] = plain[k].read_state() == batch.read_system(k)
+    for e in plain:
+        e.close()
+    batch.close()
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": ms_b / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+int64",
+        "data": "synthetic",
+        "config": {
+            "workload": f"{len(systems)} independent 2D LJ systems, N log-uniform [256, 65536] (sum {total}), rho U[0.3, 0.8], T U[0.5, 1.5], rc 2.5, skin 0.3, dt 0.005 (configs[3])",
+            "form": "batched: one persistent force launch per step over all systems, 100-step CUDA graphs",
+            "plain_value": value_plain,
+            "plain_form": "one engine per system, each stepped on its own stream, all issued back to back",
+            "batched_over_plain": value / value_plain,
+            "replicas_bit_identical_to_plain": checks,
+            "rebuilds": r1 - r0,
+        },
+        "gpu_launches": l1 - l0,
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_c3(args, world, rank, local, pg):
+    """configs[2]: 2D liquid-vapour slab, N = 2^24, rescale to T = 0.45 every 10 steps, RDF (200
+    bins to r = 5) and density profile (80 bins) every 100 steps inside the timed region."""
+    import torch
+
+    from micrographia_gb300 import ForceMode, GpuEngine, workloads
+
+    torch.cuda.set_device(local)
+    sys_, spec = workloads.config3(args.atoms if args.atoms != (1 << 20) else 1 << 24)
+    n = spec.n
+    eng = GpuEngine(sys_, None, ForceMode.verlet_with_skin(sys_, n, SKIN), init=spec, rescale_every=10, rescale_t=0.45, device=local)
+    stream = torch.cuda.ExternalStream(eng.stream())
+    eng.step(args.warmup)
+    eng.wait()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    done, frames = 0, []
+    while done < args.steps:
+        k = min(100, args.steps - done)
+        eng.step(k)
+        done += k
+        if done % 100 == 0:
+            f, rdf, prof = eng.observe(rdf_bins=200, rdf_rmax=5.0, profile_bins=80, profile_axis=0)
+            frames.append({"step": done, "T": f.temperature, "P": f.pressure, "pe_per_atom": f.potential / n})
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    rebuilds, overflow = eng.read_list_stats()
+    line = {
+        "metric": METRIC,
+        "value": world * n * args.steps / (wall),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": wall * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+int64",
+        "data": "synthetic",
+        "config": {
+            "workload": f"2D liquid-vapour slab N={n}, 4:1 box, liquid 0.70 / vapour 0.05, rescale T=0.45 every 10 steps, RDF + profile every 100 steps (configs[2])",
+            "timing": "wall clock including the frames (observables copied to the host every 100 steps)",
+            "device_ms_last_event_pair": ms,
+            "frames": frames[-3:],
+            "rebuilds": rebuilds,
+            "overflow": overflow,
+        },
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 def main():
     global N_ATOMS
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
@@ -346,6 +491,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="atoms (default 1,048,576; smaller only for profiling)")
+    ap.add_argument("--config", choices=["c2", "c3", "c4"], default="c2", help="c2 (default): 3D N=1M; c3: 2D slab 16.7M; c4: 1024 replicas")
+    ap.add_argument("--systems", type=int, default=1024, help="replicas for --config c4")
     args = ap.parse_args()
     N_ATOMS = args.atoms
     if args.warmup < 3:
@@ -357,7 +504,12 @@ def main():
         from micrographia_gb300 import build
 
         build.build()
-        rc = run_ours(args, world, rank, local, pg)
+        if args.config == "c4":
+            rc = run_c4(args, world, rank, local, pg)
+        elif args.config == "c3":
+            rc = run_c3(args, world, rank, local, pg)
+        else:
+            rc = run_ours(args, world, rank, local, pg)
     if pg is not None:
         pg.destroy_process_group()
     return rc

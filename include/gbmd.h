@@ -243,6 +243,8 @@ int gbmd_batch_sync(gbmd_batch* b);
 /* The id-ordered state of system k. */
 int gbmd_batch_read_system(gbmd_batch* b, uint32_t k, int64_t* pos, int32_t* vel, uint32_t* species);
 int gbmd_batch_stream(gbmd_batch* b, void** stream);
+/* Kernel launches of the batch so far (graph nodes included) and its list rebuilds. */
+int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds);
 int gbmd_batch_destroy(gbmd_batch* b);
 
 /* FNV-1a hash of an id-ordered state held on the host: State::hash (system.rs:460-477) for

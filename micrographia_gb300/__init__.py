@@ -26,7 +26,7 @@ from .core import (
     to_fixed,
 )
 from .engine import BatchEngine, GpuEngine, GpuEngine3, init_state
-from . import init
+from . import init, workloads
 
 __all__ = [
     "DT",
@@ -47,4 +47,5 @@ __all__ = [
     "to_fixed",
     "init",
     "init_state",
+    "workloads",
 ]

@@ -154,6 +154,7 @@ SIGNATURES = [
     ("gbmd_batch_sync", C.c_int, [VP]),
     ("gbmd_batch_read_system", C.c_int, [VP, C.c_uint32, _I64P, _I32P, _U32P]),
     ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
+    ("gbmd_batch_stats", C.c_int, [VP, _U64P, _U32P]),
     ("gbmd_batch_destroy", C.c_int, [VP]),
     ("gbmd_hash_state", C.c_uint64, [C.c_uint32, _I64P, _I32P, _U32P, C.c_uint32]),
     ("gbmd_last_error", C.c_char_p, []),

@@ -1,24 +1,553 @@
-// Batched replicas (placeholder until the batched engine lands in this file).
+// Batched replicas: many independent periodic systems of uneven size stepped together.
+//
+// The reference batches only equal compartments of one box separated by walls
+// (crates/md-core/src/system.rs:41-48, 219-256; init.rs:126-149). Here every system keeps its
+// own box, species table and seed, and all of them share one set of launches:
+//   - a segmented cell-key space: system k's cells are numbered from cell_base[k] (the cells of
+//     the systems before it), so one stable radix sort bins every system at once and leaves each
+//     system's particles contiguous and in cell order;
+//   - a per-particle system index selects the system's parameter block (box, pair constants,
+//     kick coefficients) from a device table;
+//   - the force kernel is persistent (a grid-stride loop over all particles of all systems on a
+//     grid sized to the GPU), and 100-step blocks are captured as CUDA graphs with the list
+//     rebuild in a conditional node, as in the single-system engine.
+// A system's trajectory does not depend on when lists are rebuilt (integer kicks are summed
+// order-independently), so each replica's state equals its plain single-system run bit for bit.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
 #include "common.cuh"
 #include "engine.cuh"
+#include "kernels.cuh"
+#include "sort.cuh"
 
 using namespace gbmd;
 
+namespace {
+
+// Geometry of one system held in registers by a thread.
+struct Geom {
+    int64_t box[3], half[3];
+    int32_t gravity[3];
+    uint32_t pinned;
+    float half_skin2s;
+};
+__device__ __forceinline__ Geom geom_of(const Params& P) {
+    Geom g;
+    for (int a = 0; a < 3; a++) {
+        g.box[a] = P.box[a];
+        g.half[a] = P.half[a];
+        g.gravity[a] = P.gravity[a];
+    }
+    g.pinned = P.pinned;
+    g.half_skin2s = P.half_skin2s;
+    return g;
+}
+
+template <int D>
+__global__ void k_bkeys(uint32_t N, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx, const PosRec<D>* pos,
+                        uint32_t* keys, uint32_t* vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const Params& P = tab[sysidx[i]];
+    int64_t x[3];
+    load_particle<D, false>(pos, nullptr, i, x);
+    uint32_t c[3];
+    keys[i] = P.cell_base + cell_key<D>(P, x, c);
+    vals[i] = i;
+}
+
+template <int D>
+__global__ void k_bgather(uint32_t N, const uint32_t* items, const PosRec<D>* pos, const int32_t* vel, const uint32_t* species,
+                          const uint32_t* ids, const uint32_t* sysidx, PosRec<D>* pos_o, int32_t* vel_o, uint32_t* species_o, uint32_t* ids_o,
+                          uint32_t* sysidx_o) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    uint32_t o = items[s];
+    pos_o[s] = pos[o];
+    for (int a = 0; a < D; a++) vel_o[D * s + a] = vel[D * o + a];
+    species_o[s] = species[o];
+    ids_o[s] = ids[o];
+    sysidx_o[s] = sysidx[o];
+}
+
+// The list build of k_build_list, each particle in its own system's cells and geometry.
+template <int D, bool MULTI>
+__global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, const Params* __restrict__ tab,
+                                                     const uint32_t* __restrict__ sysidx_s, const PosRec<D>* __restrict__ pos_s,
+                                                     const int32_t* __restrict__ vel_s, const uint32_t* __restrict__ species_s,
+                                                     const uint32_t* __restrict__ ids_s, const uint32_t* __restrict__ keys,
+                                                     const uint32_t* __restrict__ start, PosRec<D>* __restrict__ pos_o,
+                                                     int32_t* __restrict__ vel_o, uint32_t* __restrict__ species_o,
+                                                     uint32_t* __restrict__ ids_o, uint32_t* __restrict__ sysidx_o,
+                                                     PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ nbr,
+                                                     uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ ctl) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    uint32_t sys = sysidx_s[i];
+    const Params& P = tab[sys];
+    const Geom G = geom_of(P);
+    const uint32_t base = P.cell_base, ns = P.ns;
+    int64_t xi[3];
+    uint32_t si = load_particle<D, MULTI>(pos_s, species_s, i, xi);
+    uint32_t c[3];
+    cell_coords(P, keys[i] - base, c);
+    uint32_t count = 0;
+    for_cells<D>(P, c, [&](uint32_t cell) {
+        uint32_t j0 = __ldg(start + base + cell), j1 = __ldg(start + base + cell + 1);
+        for (uint32_t j = j0; j < j1; j++) {
+            if (j == i) continue;
+            int64_t xj[3];
+            uint32_t sj = load_particle<D, MULTI>(pos_s, species_s, j, xj);
+            bool ok = true;
+            float f[D];
+#pragma unroll
+            for (int a = 0; a < D; a++) f[a] = sep_s(min_image(xj[a] - xi[a], G.box[a], G.half[a]), ok);
+            if (!ok) continue;
+            float r2 = __fadd_rn(__fmul_rn(f[0], f[0]), __fmul_rn(f[1], f[1]));
+            if (D == 3) r2 = __fadd_rn(r2, __fmul_rn(f[2], f[2]));
+            if (r2 < P.pc[si * ns + sj].list2s) {
+                if (count < cap) nbr[(size_t)count * N + i] = j;
+                count++;
+            }
+        }
+    });
+    if (count > cap) {
+        ctl[1] = 1;
+        count = cap;
+    }
+    nbr_count[i] = count;
+    pos_o[i] = pos_s[i];
+    ref_pos[i] = pos_s[i];
+    for (int a = 0; a < D; a++) vel_o[D * i + a] = vel_s[D * i + a];
+    species_o[i] = species_s[i];
+    ids_o[i] = ids_s[i];
+    sysidx_o[i] = sys;
+}
+
+// Persistent fused force + leapfrog over every particle of every system.
+template <int D, bool MULTI>
+__global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx,
+                                                     const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
+                                                     int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
+                                                     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+                                                     const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const Params& P = tab[sysidx[i]];
+        const Geom G = geom_of(P);
+        int64_t xi[3];
+        uint32_t si = load_particle<D, MULTI>(pos_in, species, i, xi);
+        const float cs = P.kick_cs[si];
+        const uint32_t ns = P.ns;
+        const PairC pc0 = P.pc[0];
+        int32_t k[3] = {0, 0, 0};
+        const uint32_t m = __ldg(nbr_count + i);
+        for (uint32_t q = 0; q < m; q++) {
+            uint32_t j = __ldg(nbr + (size_t)q * N + i);
+            int64_t xj[3];
+            uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
+            float fr, s6, r2;
+            pair_kick<D>(G, MULTI ? P.pc[si * ns + sj] : pc0, cs, xi, xj, k, fr, s6, r2);
+        }
+        int32_t v[3];
+        for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
+        leapfrog<D>(G, si, k, v, xi);
+        for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
+        store_pos<D>(pos_out, i, xi, si);
+        int64_t xr[3];
+        load_particle<D, false>(ref_pos, nullptr, i, xr);
+        if (moved_half_skin<D>(G, xr, xi)) ctl[0] = 1;
+    }
+}
+
+template <int D>
+__global__ void k_bfrom_host(uint32_t N, const int64_t* ipos, const int32_t* ivel, const uint32_t* ispecies, const uint32_t* isys,
+                             PosRec<D>* pos, int32_t* vel, uint32_t* species, uint32_t* ids, uint32_t* sysidx) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    int64_t x[3];
+    for (int a = 0; a < D; a++) {
+        x[a] = ipos[(size_t)D * s + a];
+        vel[D * s + a] = ivel[(size_t)D * s + a];
+    }
+    store_pos<D>(pos, s, x, ispecies[s]);
+    species[s] = ispecies[s];
+    ids[s] = s;
+    sysidx[s] = isys[s];
+}
+
+template <int D>
+__global__ void k_bto_ids(uint32_t N, const PosRec<D>* pos, const int32_t* vel, const uint32_t* species, const uint32_t* ids,
+                          int64_t* opos, int32_t* ovel, uint32_t* ospecies) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    uint32_t id = ids[s];
+    int64_t x[3];
+    load_particle<D, false>(pos, nullptr, s, x);
+    for (int a = 0; a < D; a++) {
+        opos[(size_t)D * id + a] = x[a];
+        ovel[(size_t)D * id + a] = vel[D * s + a];
+    }
+    ospecies[id] = species[s];
+}
+
+__global__ void k_brebuild_done(uint32_t* ctl) {
+    ctl[0] = 0;
+    ctl[2] += 1;
+}
+__global__ void k_bset_cond(cudaGraphConditionalHandle h, const uint32_t* ctl) { cudaGraphSetConditional(h, ctl[0] ? 1u : 0u); }
+
+uint32_t nblocks(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
+
+} // namespace
+
 struct gbmd_batch {
-    int unused;
+    uint32_t K = 0, N = 0;
+    int D = 2;
+    bool multi = false;
+    std::vector<gbmd_system> sys;
+    std::vector<uint32_t> offsets;
+    std::vector<Params> P;
+    Params* tab = nullptr;
+    uint32_t cap = 0, ncell = 0, bits = 1, grid = 1;
+    size_t rec = 16;
+    cudaStream_t st = nullptr, st_body = nullptr;
+    void *pos[2] = {nullptr, nullptr}, *pos_scr = nullptr, *ref_pos = nullptr;
+    int32_t *vel = nullptr, *vel_scr = nullptr;
+    uint32_t *species = nullptr, *species_scr = nullptr, *ids = nullptr, *ids_scr = nullptr, *sysidx = nullptr, *sysidx_scr = nullptr;
+    uint32_t *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr}, *hist = nullptr, *scan_tmp = nullptr, *start = nullptr;
+    uint32_t *nbr = nullptr, *nbr_count = nullptr, *ctl = nullptr;
+    void* staging = nullptr;
+    int32_t* staging_v = nullptr;
+    uint32_t* staging_s = nullptr;
+    int cur = 0, sorted = 0;
+    uint32_t block_steps = 100;
+    cudaGraphExec_t exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    uint64_t exec_launches[2][2] = {{0, 0}, {0, 0}};
+    uint64_t body_launches = 0, launches = 0;
+    bool failed = false;
 };
 
+namespace {
+
+template <typename T> int balloc(T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GBMD_E_NOMEM : GBMD_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return GBMD_OK;
+}
+
+void bfree(gbmd_batch* b) {
+    for (int p = 0; p < 2; p++)
+        for (int k = 0; k < 2; k++)
+            if (b->exec[p][k]) cudaGraphExecDestroy(b->exec[p][k]);
+    void* ptrs[] = {b->tab, b->pos[0], b->pos[1], b->pos_scr, b->ref_pos, b->vel, b->vel_scr, b->species, b->species_scr, b->ids, b->ids_scr,
+                    b->sysidx, b->sysidx_scr, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->scan_tmp, b->start, b->nbr,
+                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (b->st) cudaStreamDestroy(b->st);
+    if (b->st_body) cudaStreamDestroy(b->st_body);
+}
+
+template <int D, bool MULTI> void benqueue_rebuild_t(gbmd_batch* b, cudaStream_t s) {
+    uint32_t N = b->N;
+    k_bkeys<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur], b->keys[0], b->vals[0]);
+    b->sorted = radix_sort_pairs(b->keys[0], b->vals[0], b->keys[1], b->vals[1], N, (int)b->bits, b->hist, b->scan_tmp, s);
+    cell_starts(b->keys[b->sorted], N, b->ncell, b->start, s);
+    k_bgather<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->vals[b->sorted], (const PosRec<D>*)b->pos[b->cur], b->vel, b->species, b->ids,
+                                                b->sysidx, (PosRec<D>*)b->pos_scr, b->vel_scr, b->species_scr, b->ids_scr, b->sysidx_scr);
+    k_bbuild_list<D, MULTI><<<nblocks(N, 128), 128, 0, s>>>(N, b->cap, b->tab, b->sysidx_scr, (const PosRec<D>*)b->pos_scr, b->vel_scr,
+                                                           b->species_scr, b->ids_scr, b->keys[b->sorted], b->start,
+                                                           (PosRec<D>*)b->pos[b->cur], b->vel, b->species, b->ids, b->sysidx,
+                                                           (PosRec<D>*)b->ref_pos, b->nbr, b->nbr_count, b->ctl);
+    k_brebuild_done<<<1, 1, 0, s>>>(b->ctl);
+    note_launch(6 + 3 * (uint64_t)radix_passes((int)b->bits));
+}
+void benqueue_rebuild(gbmd_batch* b, cudaStream_t s) {
+    if (b->D == 2) b->multi ? benqueue_rebuild_t<2, true>(b, s) : benqueue_rebuild_t<2, false>(b, s);
+    else b->multi ? benqueue_rebuild_t<3, true>(b, s) : benqueue_rebuild_t<3, false>(b, s);
+}
+template <int D, bool MULTI> void benqueue_force_t(gbmd_batch* b, cudaStream_t s) {
+    k_bforce_list<D, MULTI><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur], (PosRec<D>*)b->pos[b->cur ^ 1],
+                                                   b->vel, b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
+    note_launch();
+    b->cur ^= 1;
+}
+void benqueue_force(gbmd_batch* b, cudaStream_t s) {
+    if (b->D == 2) b->multi ? benqueue_force_t<2, true>(b, s) : benqueue_force_t<2, false>(b, s);
+    else b->multi ? benqueue_force_t<3, true>(b, s) : benqueue_force_t<3, false>(b, s);
+}
+
+int bcapture(gbmd_batch* b, int parity, uint32_t count, cudaGraphExec_t* out, uint64_t* launches) {
+    int saved = b->cur;
+    b->cur = parity;
+    uint64_t l0 = launch_total();
+    cudaStream_t s = b->st;
+    GBMD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (uint32_t k = 0; k < count; k++) {
+        cudaStreamCaptureStatus status;
+        cudaGraph_t g;
+        const cudaGraphNode_t* deps;
+        const cudaGraphEdgeData* edges;
+        size_t ndeps;
+        GBMD_CUDA_TRY(cudaStreamGetCaptureInfo(s, &status, nullptr, &g, &deps, &edges, &ndeps));
+        cudaGraphConditionalHandle h;
+        GBMD_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+        k_bset_cond<<<1, 1, 0, s>>>(h, b->ctl);
+        note_launch();
+        GBMD_CUDA_TRY(cudaStreamGetCaptureInfo(s, &status, nullptr, &g, &deps, &edges, &ndeps));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        GBMD_CUDA_TRY(cudaGraphAddNode(&node, g, deps, edges, ndeps, &cp));
+        GBMD_CUDA_TRY(cudaStreamBeginCaptureToGraph(b->st_body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                    cudaStreamCaptureModeThreadLocal));
+        uint64_t b0 = launch_total();
+        benqueue_rebuild(b, b->st_body);
+        b->body_launches = launch_total() - b0;
+        note_launch(0);
+        cudaGraph_t tmp;
+        GBMD_CUDA_TRY(cudaStreamEndCapture(b->st_body, &tmp));
+        GBMD_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        benqueue_force(b, s);
+    }
+    cudaGraph_t graph;
+    cudaError_t err = cudaStreamEndCapture(s, &graph);
+    b->cur = saved;
+    if (err != cudaSuccess) return fail(GBMD_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
+    err = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (err != cudaSuccess) return fail(GBMD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+    *launches = launch_total() - l0 - count * b->body_launches;
+    note_launch(0);
+    return GBMD_OK;
+}
+
+int brun(gbmd_batch* b, int which) {
+    int parity = b->cur;
+    uint32_t count = which ? b->block_steps : 1;
+    if (!b->exec[parity][which]) GBMD_TRY(bcapture(b, parity, count, &b->exec[parity][which], &b->exec_launches[parity][which]));
+    GBMD_CUDA_TRY(cudaGraphLaunch(b->exec[parity][which], b->st));
+    b->launches += b->exec_launches[parity][which];
+    if (count & 1) b->cur ^= 1;
+    return GBMD_OK;
+}
+
+int bcheck(gbmd_batch* b) {
+    uint32_t c[3];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(c, b->ctl, 12, cudaMemcpyDeviceToHost, b->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
+    if (c[1]) {
+        b->failed = true;
+        return fail(GBMD_E_OVERFLOW, "a Verlet list of the batch overflowed its capacity");
+    }
+    return GBMD_OK;
+}
+
+} // namespace
+
 extern "C" {
-int gbmd_batch_create(const gbmd_system*, uint32_t, const uint32_t*, const int64_t*, const int32_t*, const uint32_t*, const gbmd_options*,
-                      gbmd_batch** out) {
-    if (out) *out = nullptr;
-    return fail(GBMD_E_UNSUPPORTED, "batched replicas are not built yet");
+
+int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t* offsets, const int64_t* pos, const int32_t* vel,
+                      const uint32_t* species, const gbmd_options* opts, gbmd_batch** out) {
+    if (!systems || !offsets || !pos || !vel || !species || !out || count == 0) return fail(GBMD_E_INVALID, "null argument");
+    *out = nullptr;
+    gbmd_options o{};
+    if (opts) o = *opts;
+    if (o.arith != GBMD_ARITH_F32) return fail(GBMD_E_UNSUPPORTED, "batches run f32 pair forces");
+    if (o.mode == GBMD_MODE_CELLS) return fail(GBMD_E_UNSUPPORTED, "batches run Verlet lists");
+    uint32_t D = systems[0].dim;
+    for (uint32_t k = 0; k < count; k++) {
+        GBMD_TRY(validate_system(systems[k], offsets[k + 1] - offsets[k]));
+        if (systems[k].dim != D) return fail(GBMD_E_INVALID, "a batch holds systems of one dimension");
+        if (offsets[k + 1] <= offsets[k]) return fail(GBMD_E_INVALID, "every system needs at least one particle");
+    }
+    if (offsets[0] != 0) return fail(GBMD_E_INVALID, "offsets[0] must be 0");
+    auto* b = new gbmd_batch;
+    b->K = count;
+    b->N = offsets[count];
+    b->D = (int)D;
+    b->rec = D == 2 ? 16 : 32;
+    b->sys.assign(systems, systems + count);
+    b->offsets.assign(offsets, offsets + count + 1);
+    b->block_steps = o.block_steps ? o.block_steps : 100;
+    double skin = o.skin > 0 ? o.skin : 0.4;
+    b->P.resize(count);
+    uint64_t cell_base = 0;
+    for (uint32_t k = 0; k < count; k++) {
+        const gbmd_system& s = systems[k];
+        if (s.nspecies > 1) b->multi = true;
+        uint32_t nk = offsets[k + 1] - offsets[k];
+        uint32_t nc[3];
+        int r = cells_for(s, rc_max(s) + skin, nc);
+        if (r != GBMD_OK) {
+            delete b;
+            return r;
+        }
+        double vol = 1.0, rr = rc_max(s) + skin;
+        for (uint32_t a = 0; a < D; a++) vol *= (double)s.box_len[a] * (1.0 / 4294967296.0);
+        double sphere = D == 2 ? M_PI * rr * rr : 4.0 / 3.0 * M_PI * rr * rr * rr;
+        uint32_t cap = o.cap ? o.cap : (uint32_t)std::ceil(sphere * std::max(2.0 * nk / vol, 1.2)) + 8;
+        b->cap = std::max(b->cap, cap);
+        fill_params(b->P[k], s, nk, skin, cap, nc);
+        b->P[k].cell_base = (uint32_t)cell_base;
+        cell_base += b->P[k].ncell;
+        if (cell_base >= UINT32_MAX) {
+            delete b;
+            return fail(GBMD_E_INVALID, "too many cells in the batch");
+        }
+    }
+    for (uint32_t k = 0; k < count; k++) b->P[k].cap = b->cap;
+    b->ncell = (uint32_t)cell_base;
+    b->bits = (uint32_t)key_bits(b->ncell);
+    int dev_sms = 0;
+    int r = GBMD_OK;
+    auto step = [&](int rc) {
+        if (r == GBMD_OK) r = rc;
+    };
+    step(cudaSetDevice(o.device) == cudaSuccess ? GBMD_OK : fail(GBMD_E_CUDA, "cudaSetDevice"));
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, o.device);
+    int occ = 0;
+    if (D == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<2, true> : k_bforce_list<2, false>, 128, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<3, true> : k_bforce_list<3, false>, 128, 0);
+    b->grid = std::max<uint32_t>(1, std::min<uint32_t>(nblocks(b->N, 128), (uint32_t)std::max(dev_sms, 1) * (uint32_t)std::max(occ, 1)));
+    if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
+    if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st_body, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
+    size_t N = b->N;
+    step(balloc(&b->tab, count));
+    step(balloc((char**)&b->pos[0], N * b->rec));
+    step(balloc((char**)&b->pos[1], N * b->rec));
+    step(balloc((char**)&b->pos_scr, N * b->rec));
+    step(balloc((char**)&b->ref_pos, N * b->rec));
+    step(balloc(&b->vel, N * D));
+    step(balloc(&b->vel_scr, N * D));
+    step(balloc(&b->species, N));
+    step(balloc(&b->species_scr, N));
+    step(balloc(&b->ids, N));
+    step(balloc(&b->ids_scr, N));
+    step(balloc(&b->sysidx, N));
+    step(balloc(&b->sysidx_scr, N));
+    for (int k = 0; k < 2; k++) {
+        step(balloc(&b->keys[k], N));
+        step(balloc(&b->vals[k], N));
+    }
+    size_t hist_n = radix_hist_elems(N);
+    step(balloc(&b->hist, hist_n));
+    step(balloc(&b->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(N))));
+    step(balloc(&b->start, (size_t)b->ncell + 1));
+    step(balloc(&b->nbr, N * b->cap));
+    step(balloc(&b->nbr_count, N));
+    step(balloc(&b->ctl, 16));
+    step(balloc((char**)&b->staging, N * D * 8));
+    step(balloc(&b->staging_v, N * D));
+    step(balloc(&b->staging_s, N));
+    if (r == GBMD_OK) {
+        std::vector<uint32_t> sysi(N);
+        for (uint32_t k = 0; k < count; k++)
+            for (uint32_t i = offsets[k]; i < offsets[k + 1]; i++) sysi[i] = k;
+        for (size_t i = 0; i < N; i++) {
+            uint32_t k = sysi[i];
+            if (species[i] >= systems[k].nspecies) r = fail(GBMD_E_INVALID, "species index out of range");
+            for (uint32_t a = 0; a < D; a++)
+                if (pos[D * i + a] < 0 || pos[D * i + a] >= systems[k].box_len[a]) r = fail(GBMD_E_INVALID, "positions must lie in [0, L)");
+        }
+        uint32_t* dsys = nullptr;
+        if (r == GBMD_OK) step(balloc(&dsys, N));
+        if (r == GBMD_OK) {
+            cudaMemcpyAsync(b->tab, b->P.data(), count * sizeof(Params), cudaMemcpyHostToDevice, b->st);
+            cudaMemcpyAsync(b->staging, pos, N * D * 8, cudaMemcpyHostToDevice, b->st);
+            cudaMemcpyAsync(b->staging_v, vel, N * D * 4, cudaMemcpyHostToDevice, b->st);
+            cudaMemcpyAsync(b->staging_s, species, N * 4, cudaMemcpyHostToDevice, b->st);
+            cudaMemcpyAsync(dsys, sysi.data(), N * 4, cudaMemcpyHostToDevice, b->st);
+            if (D == 2)
+                k_bfrom_host<2><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, (const int64_t*)b->staging, b->staging_v, b->staging_s, dsys,
+                                                                   (PosRec<2>*)b->pos[0], b->vel, b->species, b->ids, b->sysidx);
+            else
+                k_bfrom_host<3><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, (const int64_t*)b->staging, b->staging_v, b->staging_s, dsys,
+                                                                   (PosRec<3>*)b->pos[0], b->vel, b->species, b->ids, b->sysidx);
+            note_launch();
+            cudaMemsetAsync(b->ctl, 0, 64, b->st);
+            uint32_t one = 1;
+            cudaMemcpyAsync(b->ctl, &one, 4, cudaMemcpyHostToDevice, b->st);
+            cudaError_t e = cudaStreamSynchronize(b->st);
+            if (e != cudaSuccess) r = fail(GBMD_E_CUDA, cudaGetErrorString(e));
+        }
+        if (dsys) cudaFree(dsys);
+    }
+    if (r != GBMD_OK) {
+        std::string msg = gbmd_last_error();
+        bfree(b);
+        delete b;
+        return fail(r, msg);
+    }
+    *out = b;
+    return GBMD_OK;
 }
-int gbmd_batch_step(gbmd_batch*, uint64_t) { return fail(GBMD_E_UNSUPPORTED, "batched replicas are not built yet"); }
-int gbmd_batch_sync(gbmd_batch*) { return fail(GBMD_E_UNSUPPORTED, "batched replicas are not built yet"); }
-int gbmd_batch_read_system(gbmd_batch*, uint32_t, int64_t*, int32_t*, uint32_t*) {
-    return fail(GBMD_E_UNSUPPORTED, "batched replicas are not built yet");
+
+int gbmd_batch_step(gbmd_batch* b, uint64_t steps) {
+    if (!b) return fail(GBMD_E_INVALID, "null batch");
+    if (b->failed) return fail(GBMD_E_OVERFLOW, "the batch is in a failed state (a list overflowed)");
+    uint64_t left = steps;
+    while (left >= b->block_steps) {
+        GBMD_TRY(brun(b, 1));
+        left -= b->block_steps;
+    }
+    while (left--) GBMD_TRY(brun(b, 0));
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return GBMD_OK;
 }
-int gbmd_batch_stream(gbmd_batch*, void**) { return fail(GBMD_E_UNSUPPORTED, "batched replicas are not built yet"); }
-int gbmd_batch_destroy(gbmd_batch*) { return GBMD_OK; }
+
+int gbmd_batch_sync(gbmd_batch* b) {
+    if (!b) return fail(GBMD_E_INVALID, "null batch");
+    GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
+    return bcheck(b);
 }
+
+int gbmd_batch_read_system(gbmd_batch* b, uint32_t k, int64_t* pos, int32_t* vel, uint32_t* species) {
+    if (!b || k >= b->K) return fail(GBMD_E_INVALID, "bad batch or system index");
+    size_t N = b->N, D = b->D;
+    if (D == 2)
+        k_bto_ids<2><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, (const PosRec<2>*)b->pos[b->cur], b->vel, b->species, b->ids,
+                                                        (int64_t*)b->staging, b->staging_v, b->staging_s);
+    else
+        k_bto_ids<3><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, (const PosRec<3>*)b->pos[b->cur], b->vel, b->species, b->ids,
+                                                        (int64_t*)b->staging, b->staging_v, b->staging_s);
+    note_launch();
+    size_t o = b->offsets[k], n = b->offsets[k + 1] - o;
+    if (pos) GBMD_CUDA_TRY(cudaMemcpyAsync(pos, (int64_t*)b->staging + o * D, n * D * 8, cudaMemcpyDeviceToHost, b->st));
+    if (vel) GBMD_CUDA_TRY(cudaMemcpyAsync(vel, b->staging_v + o * D, n * D * 4, cudaMemcpyDeviceToHost, b->st));
+    if (species) GBMD_CUDA_TRY(cudaMemcpyAsync(species, b->staging_s + o, n * 4, cudaMemcpyDeviceToHost, b->st));
+    return gbmd_batch_sync(b);
+}
+
+int gbmd_batch_stream(gbmd_batch* b, void** stream) {
+    if (!b || !stream) return fail(GBMD_E_INVALID, "null argument");
+    *stream = (void*)b->st;
+    return GBMD_OK;
+}
+
+int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds) {
+    if (!b) return fail(GBMD_E_INVALID, "null batch");
+    uint32_t c[3];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(c, b->ctl, 12, cudaMemcpyDeviceToHost, b->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
+    if (rebuilds) *rebuilds = c[2];
+    if (launches) *launches = b->launches + (uint64_t)c[2] * b->body_launches;
+    return GBMD_OK;
+}
+
+int gbmd_batch_destroy(gbmd_batch* b) {
+    if (!b) return GBMD_OK;
+    cudaStreamSynchronize(b->st);
+    bfree(b);
+    delete b;
+    return GBMD_OK;
+}
+
+} // extern "C"

@@ -55,13 +55,13 @@ int validate_system(const gbmd_system& sys, uint32_t n) {
 }
 
 // ------------------------------------------------------------------ host-side System maths
-static double rc_max(const gbmd_system& s) {
+double rc_max(const gbmd_system& s) {
     double r = 0.0;
     for (uint32_t k = 0; k < s.nspecies * s.nspecies; k++) r = std::max(r, s.pairs[k].rc);
     return r;
 }
 // System::cells_for (system.rs:438-444 / three.rs:151-157)
-static int cells_for(const gbmd_system& s, double r, uint32_t* c) {
+int cells_for(const gbmd_system& s, double r, uint32_t* c) {
     double bmax = 0.0;
     for (uint32_t a = 0; a < s.dim; a++) bmax = std::max(bmax, to_f64h(s.box_len[a]));
     double margin = 1e-3 + 1e-6 * bmax;
@@ -83,7 +83,7 @@ static double pair_shift(const gbmd_pair& p) {
 }
 static float scale2(float v, int e) { return std::ldexp(v, e); }
 
-static void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint32_t cap, const uint32_t* nc) {
+void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint32_t cap, const uint32_t* nc) {
     std::memset(&P, 0, sizeof(P));
     P.n = n;
     P.dim = s.dim;
@@ -123,9 +123,34 @@ static void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin
             c.shift = (float)pair_shift(p);
             double lr = (p.rc + skin) * (1.0 + 1e-4);
             c.list2s = scale2((float)(lr * lr), 56);
+            c.list2lo = (float)(lr * lr * (1.0 - 1e-4));
+            c.list2hi = (float)(lr * lr * (1.0 + 1e-4));
         }
+    // Listed pairs: within the list radius at the build; each particle has moved less than half
+    // the skin before the trigger fires and at most 0.5 sigma per axis (an i32 displacement) in
+    // the step after it, so |d| < r_list + skin + 2 sqrt(3) 0.5 sigma < r_list + skin + 2 sigma.
+    double r_list = (rc_max(s) + skin) * (1.0 + 1e-4);
+    P.reach = (int64_t)std::ceil((r_list + skin + 2.0) * 4294967296.0);
+    set_cells(P, P.nc, s.dim);
 }
-static int key_bits(uint32_t ncell) {
+
+// Cell grid of a parameter block: counts, the f32 cell-index helpers and whether candidates of
+// adjacent cells are certainly within 8 sigma per axis.
+void set_cells(Params& P, const uint32_t* nc, uint32_t dim) {
+    for (uint32_t a = 0; a < 3; a++) P.nc[a] = a < dim ? nc[a] : 1;
+    P.ncell = P.nc[0] * P.nc[1] * P.nc[2];
+    double side = 0.0;
+    for (uint32_t a = 0; a < dim; a++) side = std::max(side, P.box_f[a] / (double)P.nc[a]);
+    P.sep_unchecked = 2.0 * side < 7.99 ? 1u : 0u;
+    for (uint32_t a = 0; a < 3; a++) {
+        P.cell_w[a] = P.box[a] / (int64_t)P.nc[a];
+        double sc = (double)P.nc[a] / (P.box_f[a] * 4294967296.0);
+        P.cell_scale_f[a] = (float)sc;
+        // |f32 product - exact| <= 3 2^-24 (x n / L) < 2^-22 n (x < L); twice that as margin
+        P.cell_delta[a] = (float)std::min(0.5, std::ldexp((double)P.nc[a], -21));
+    }
+}
+int key_bits(uint32_t ncell) {
     int b = 0;
     while (b < 32 && (ncell - 1) >> b) b++;
     return std::max(b, 1);
@@ -159,6 +184,7 @@ struct gbmd_engine {
     uint32_t *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr};
     uint32_t *hist = nullptr, *scan_tmp = nullptr, *start = nullptr;
     uint32_t *nbr = nullptr, *nbr_count = nullptr;
+    float4* relf = nullptr;  // cell-relative f32 coordinates of the sorted scratch state
     uint32_t* ctl = nullptr; // [0] rebuild, [1] overflow, [2] rebuilds
     double* partial = nullptr;
     void* staging = nullptr;  // id-ordered I/O staging (n * D int64)
@@ -170,8 +196,17 @@ struct gbmd_engine {
     int64_t steps = 0;
     uint32_t clock = 0;
     uint32_t block_steps = 64;
-    cudaGraphExec_t exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}; // [parity][single, block]
-    uint64_t exec_launches[2][2] = {{0, 0}, {0, 0}};
+    // graphs per [parity][kind]: 0 one step, 1 a block of block_steps, 2 one step + thermostat
+    cudaGraphExec_t exec[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    uint64_t exec_launches[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    // velocity-rescale thermostat (every `rescale_every` steps)
+    uint32_t* mrank = nullptr;          // rank of each id among the moving particles
+    unsigned long long* tpart = nullptr; // exact KE partials
+    long long* vpart = nullptr;          // velocity-sum partials
+    double* tfac = nullptr;              // factor + skip flag
+    uint32_t thermo_nb = 1;
+    uint32_t moving = 0;
+    uint64_t tcount = 0;                 // steps since creation (thermostat phase)
     uint64_t body_launches = 0;
     uint64_t launches = 0;
     uint32_t last_rebuilds = 0;
@@ -192,11 +227,11 @@ template <typename T> int allocT(T** p, size_t count) { return alloc((void**)p, 
 
 void free_all(gbmd_engine* e) {
     for (int p = 0; p < 2; p++)
-        for (int b = 0; b < 2; b++)
+        for (int b = 0; b < 3; b++)
             if (e->exec[p][b]) cudaGraphExecDestroy(e->exec[p][b]);
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
-                    e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s};
+                    e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (e->st) cudaStreamDestroy(e->st);
@@ -208,16 +243,17 @@ template <int D> void enqueue_bin(gbmd_engine* e, cudaStream_t s, const Params& 
     k_keys<D><<<blocks_for(e->n, 256), 256, 0, s>>>(P, (const Rec<D>*)e->pos[e->cur], e->keys[0], e->vals[0]);
     e->sorted = radix_sort_pairs(e->keys[0], e->vals[0], e->keys[1], e->vals[1], e->n, key_bits(P.ncell), e->hist, e->scan_tmp, s);
     cell_starts(e->keys[e->sorted], e->n, P.ncell, e->start, s);
-    k_gather<D><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, D, e->vals[e->sorted], (const Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids,
-                                                       (Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr);
+    k_gather<D><<<blocks_for(e->n, 256), 256, 0, s>>>(P, e->vals[e->sorted], e->keys[e->sorted], (const Rec<D>*)e->pos[e->cur], e->vel,
+                                                       e->species, e->ids, (Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr,
+                                                       e->relf);
     note_launch(3 + 3 * (uint64_t)radix_passes(key_bits(P.ncell)) + 2);
 }
 
 template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t s) {
     enqueue_bin<D>(e, s, e->P);
     k_build_list<D, MULTI><<<blocks_for(e->n, 128), 128, 0, s>>>(
-        e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, (Rec<D>*)e->pos[e->cur],
-        e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl);
+        e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, e->relf,
+        (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl);
     note_launch();
 }
 
@@ -265,8 +301,46 @@ void enqueue_force(gbmd_engine* e, cudaStream_t s) {
     }
 }
 
-// Capture `count` steps starting at parity `parity` into a graph.
-int capture_steps(gbmd_engine* e, int parity, uint32_t count, cudaGraphExec_t* out, uint64_t* launches) {
+// The velocity-rescale thermostat: exact KE -> factor -> v <- round(v f) -> exact zero sum.
+void enqueue_thermo(gbmd_engine* e, cudaStream_t s) {
+    ThermoP T{};
+    T.nblocks = e->thermo_nb;
+    T.ns = e->sys.nspecies;
+    for (uint32_t k = 0; k < GBMD_MAX_SPECIES; k++) T.masses[k] = k < e->sys.nspecies ? e->sys.masses[k] : 1.0;
+    T.dt = e->sys.dt;
+    T.dof = 0.5 * e->D * std::max((double)e->moving - 1.0, 1.0);
+    T.t = e->opt.rescale_t;
+    uint32_t nb = e->thermo_nb;
+    if (e->D == 2) {
+        k_ke_exact<2><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tpart);
+        k_thermo_factor<<<1, 1, 0, s>>>(T, e->tpart, e->tfac);
+        k_rescale<2><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tfac, e->vpart);
+        k_zero_apply<2><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving, e->vpart, nb, e->tfac);
+    } else {
+        k_ke_exact<3><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tpart);
+        k_thermo_factor<<<1, 1, 0, s>>>(T, e->tpart, e->tfac);
+        k_rescale<3><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tfac, e->vpart);
+        k_zero_apply<3><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving, e->vpart, nb, e->tfac);
+    }
+    note_launch(4);
+}
+
+// Ranks of the moving particles in id order (zero_velocity_sum's order) from id-ordered species.
+int upload_ranks(gbmd_engine* e, const uint32_t* species) {
+    std::vector<uint32_t> r(e->n, 0);
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < e->n; i++)
+        if (!((e->sys.pinned >> species[i]) & 1u)) r[i] = k++;
+    e->moving = k;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->mrank, r.data(), (size_t)e->n * 4, cudaMemcpyHostToDevice, e->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    return GBMD_OK;
+}
+
+// Capture `count` steps starting at parity `parity` into a graph. kind 1 applies the thermostat
+// after every rescale_every-th step of the block (blocks start on a thermostat boundary); kind 2
+// applies it after its single step.
+int capture_steps(gbmd_engine* e, int parity, uint32_t count, int kind, cudaGraphExec_t* out, uint64_t* launches) {
     int saved_cur = e->cur;
     e->cur = parity;
     uint64_t l0 = launch_total();
@@ -304,6 +378,8 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, cudaGraphExec_t* o
             GBMD_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
         }
         enqueue_force(e, s);
+        uint32_t every = e->opt.rescale_every;
+        if ((kind == 1 && every && (k + 1) % every == 0) || kind == 2) enqueue_thermo(e, s);
     }
     cudaGraph_t graph;
     cudaError_t err = cudaStreamEndCapture(s, &graph);
@@ -326,12 +402,12 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, cudaGraphExec_t* o
 
 int run_graph(gbmd_engine* e, int which) {
     int parity = e->cur;
+    uint32_t count = which == 1 ? e->block_steps : 1;
     if (!e->exec[parity][which]) {
-        uint32_t count = which ? e->block_steps : 1;
-        GBMD_TRY(capture_steps(e, parity, count, &e->exec[parity][which], &e->exec_launches[parity][which]));
+        GBMD_TRY(capture_steps(e, parity, count, which, &e->exec[parity][which], &e->exec_launches[parity][which]));
     }
     GBMD_CUDA_TRY(cudaGraphLaunch(e->exec[parity][which], e->st));
-    uint32_t count = which ? e->block_steps : 1;
+    e->tcount += count;
     note_launch(e->exec_launches[parity][which]);
     e->launches += e->exec_launches[parity][which];
     if (e->verlet && (count & 1)) e->cur ^= 1;
@@ -439,7 +515,7 @@ int upload_state(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const u
     uint32_t one = 1;
     GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
     GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
-    return GBMD_OK;
+    return upload_ranks(e, species);
 }
 
 int read_state_dev(gbmd_engine* e) {
@@ -492,6 +568,12 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     }
     fill_params(e->P, *sys, n, e->skin, cap, nc);
     e->block_steps = e->opt.block_steps ? e->opt.block_steps : 64;
+    if (e->opt.rescale_every) {
+        if (!(e->opt.rescale_t > 0.0)) return fail(GBMD_E_INVALID, "the rescale thermostat needs a positive temperature");
+        uint32_t every = e->opt.rescale_every;
+        e->block_steps = every * std::max<uint32_t>(1, e->block_steps / every);
+    }
+    e->thermo_nb = std::min<uint32_t>(std::max<uint32_t>(blocks_for(n, 256), 1), 512);
     GBMD_CUDA_TRY(cudaSetDevice(e->opt.device));
     GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
     GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st_body, cudaStreamNonBlocking));
@@ -520,6 +602,11 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         GBMD_TRY(allocT(&e->nbr_count, n));
     }
     GBMD_TRY(allocT(&e->ctl, 16));
+    GBMD_TRY(allocT(&e->relf, n));
+    GBMD_TRY(allocT(&e->mrank, n));
+    GBMD_TRY(allocT(&e->tpart, 8 * (size_t)e->thermo_nb));
+    GBMD_TRY(allocT(&e->vpart, 3 * (size_t)e->thermo_nb));
+    GBMD_TRY(allocT(&e->tfac, 2));
     GBMD_TRY(allocT(&e->partial, 4 * (size_t)blocks_for(n, 128) + 4));
     GBMD_TRY(alloc(&e->staging, n * D * 8));
     GBMD_TRY(allocT(&e->staging_v, n * D));
@@ -566,6 +653,10 @@ int gbmd_create_seeded(const gbmd_system* sys, const gbmd_init* spec, const gbmd
         uint32_t one = 1;
         cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st);
         if (cudaStreamSynchronize(e->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "seeded init failed");
+        if (r == GBMD_OK) {
+            std::vector<uint32_t> zeros(e->n, 0); // the recipes create species 0 only
+            r = upload_ranks(e, zeros.data());
+        }
     }
     if (r != GBMD_OK) {
         std::string msg = t_error;
@@ -589,13 +680,17 @@ int gbmd_step(gbmd_engine* e, uint64_t steps) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
     if (e->failed) return fail(GBMD_E_OVERFLOW, "the engine is in a failed state (a list overflowed)");
     uint64_t left = steps;
-    while (left >= e->block_steps) {
-        GBMD_TRY(run_graph(e, 1));
-        left -= e->block_steps;
-    }
+    uint32_t every = e->opt.rescale_every;
     while (left > 0) {
-        GBMD_TRY(run_graph(e, 0));
-        left--;
+        bool aligned = every == 0 || e->tcount % every == 0;
+        if (aligned && left >= e->block_steps) {
+            GBMD_TRY(run_graph(e, 1));
+            left -= e->block_steps;
+        } else {
+            bool thermo = every && (e->tcount + 1) % every == 0;
+            GBMD_TRY(run_graph(e, thermo ? 2 : 0));
+            left--;
+        }
     }
     e->steps += (int64_t)steps;
     e->clock += (uint32_t)steps;
@@ -754,6 +849,7 @@ int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* r
     cudaEventDestroy(c);
     e->steps += steps;
     e->clock += steps;
+    e->tcount += steps;
     if (force_ms) *force_ms = steps ? tf / steps : 0.0;
     if (rebuild_ms) *rebuild_ms = nr ? tr / nr : 0.0;
     if (rebuilds) *rebuilds = nr;
@@ -763,11 +859,9 @@ int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* r
 int gbmd_debug_bin(gbmd_engine* e, const uint32_t* cells, uint32_t* keys, uint32_t* start, uint32_t* items, uint32_t* order) {
     if (!e || !cells) return fail(GBMD_E_INVALID, "null argument");
     Params P = e->P;
-    for (int a = 0; a < e->D; a++) {
+    for (int a = 0; a < e->D; a++)
         if (cells[a] < 1) return fail(GBMD_E_INVALID, "cells must be positive");
-        P.nc[a] = cells[a];
-    }
-    P.ncell = P.nc[0] * P.nc[1] * (e->D == 3 ? P.nc[2] : 1);
+    set_cells(P, cells, (uint32_t)e->D);
     uint32_t* st2 = nullptr;
     GBMD_CUDA_TRY(cudaMalloc(&st2, ((size_t)P.ncell + 1) * 4));
     uint32_t* saved = e->start;
@@ -892,8 +986,7 @@ extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, ui
         uint32_t nc[3];
         rc = cells_for(e->sys, rdf_rmax, nc);
         if (rc == GBMD_OK) {
-            for (int a = 0; a < e->D; a++) P.nc[a] = nc[a];
-            P.ncell = P.nc[0] * P.nc[1] * (e->D == 3 ? P.nc[2] : 1);
+            set_cells(P, nc, (uint32_t)e->D);
             if (cudaMalloc(&st2, ((size_t)P.ncell + 1) * 4) != cudaSuccess) rc = fail(GBMD_E_NOMEM, "RDF cell starts");
         }
         if (rc == GBMD_OK) {

@@ -22,4 +22,12 @@ int init_state_device(const gbmd_system& sys, const gbmd_init& spec, void* pos_d
 // Validate a system for this engine (periodic LJ subset); GBMD_OK or an error (message set).
 int validate_system(const gbmd_system& sys, uint32_t n);
 
+struct Params;
+// Host-side System maths shared by the engines.
+double rc_max(const gbmd_system& s);
+int cells_for(const gbmd_system& s, double r, uint32_t* c);                 // System::cells_for
+void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint32_t cap, const uint32_t* nc);
+int key_bits(uint32_t ncell);
+void set_cells(Params& P, const uint32_t* nc, uint32_t dim);
+
 } // namespace gbmd

@@ -35,13 +35,13 @@ __device__ __forceinline__ uint32_t load_particle(const PosRec<D>* pos, const ui
 
 // Row-major cell key (md-ref cells.rs:10-15; int_engine3.rs:53-57) with f64 cell_of per axis.
 template <int D> __device__ __forceinline__ uint32_t cell_key(const Params& P, const int64_t* x, uint32_t* c) {
-    c[0] = cell_of(x[0], P.box_f[0], P.nc[0]);
-    c[1] = cell_of(x[1], P.box_f[1], P.nc[1]);
+    c[0] = cell_of_fast(x[0], P.box_f[0], P.nc[0], P.cell_scale_f[0], P.cell_delta[0]);
+    c[1] = cell_of_fast(x[1], P.box_f[1], P.nc[1], P.cell_scale_f[1], P.cell_delta[1]);
     if constexpr (D == 2) {
         c[2] = 0;
         return c[1] * P.nc[0] + c[0];
     } else {
-        c[2] = cell_of(x[2], P.box_f[2], P.nc[2]);
+        c[2] = cell_of_fast(x[2], P.box_f[2], P.nc[2], P.cell_scale_f[2], P.cell_delta[2]);
         return (c[2] * P.nc[1] + c[1]) * P.nc[0] + c[0];
     }
 }
@@ -56,25 +56,43 @@ template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t
     vals[i] = i;
 }
 
+__device__ __forceinline__ void cell_coords(const Params& P, uint32_t key, uint32_t* c);
+
 // Storage permutation into cell order (one fused gather; reorder.wgsl's gathers + copy-backs).
+// Also records each particle's position relative to its cell's origin (c * cell_w, an exact
+// integer) as f32 sigma, with its species in the fourth word, for the list build's prefilter.
 template <int D>
-__global__ void k_gather(uint32_t n, uint32_t dim, const uint32_t* items, const PosRec<D>* pos, const int32_t* vel, const uint32_t* species,
-                         const uint32_t* ids, PosRec<D>* pos_o, int32_t* vel_o, uint32_t* species_o, uint32_t* ids_o) {
+__global__ void k_gather(Params P, const uint32_t* items, const uint32_t* keys, const PosRec<D>* pos, const int32_t* vel,
+                         const uint32_t* species, const uint32_t* ids, PosRec<D>* pos_o, int32_t* vel_o, uint32_t* species_o,
+                         uint32_t* ids_o, float4* relf) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
+    if (s >= P.n) return;
     uint32_t o = items[s];
-    pos_o[s] = pos[o];
+    PosRec<D> r = pos[o];
+    pos_o[s] = r;
     for (uint32_t a = 0; a < D; a++) vel_o[D * s + a] = vel[D * o + a];
-    species_o[s] = species[o];
+    uint32_t sp = species[o];
+    species_o[s] = sp;
     ids_o[s] = ids[o];
+    if (relf) {
+        uint32_t c[3];
+        cell_coords(P, keys[s], c);
+        const long long* x = reinterpret_cast<const long long*>(&r);
+        float4 f;
+        f.x = __fmul_rn(__ll2float_rn(x[0] - (int64_t)c[0] * P.cell_w[0]), 1.0f / 4294967296.0f);
+        f.y = __fmul_rn(__ll2float_rn(x[1] - (int64_t)c[1] * P.cell_w[1]), 1.0f / 4294967296.0f);
+        f.z = D == 3 ? __fmul_rn(__ll2float_rn(x[2] - (int64_t)c[2] * P.cell_w[2]), 1.0f / 4294967296.0f) : 0.0f;
+        f.w = __uint_as_float(sp);
+        relf[s] = f;
+    }
 }
 
 __device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
 
 // One directed pair (i from j): adds the integer kick rint(a * f) per axis, exactly
 // IntEngine::forces' `(a * fx).round_even().to_i32()` summed with wrapping adds.
-template <int D>
-__device__ __forceinline__ bool pair_kick(const Params& P, const PairC& pc, float cs, const int64_t* xi, const int64_t* xj, int32_t* k,
+template <int D, class G>
+__device__ __forceinline__ bool pair_kick(const G& P, const PairC& pc, float cs, const int64_t* xi, const int64_t* xj, int32_t* k,
                                           float& fr_s, float& s6, float& r2) {
     bool ok = true;
     float f[D];
@@ -90,8 +108,8 @@ __device__ __forceinline__ bool pair_kick(const Params& P, const PairC& pc, floa
 
 // Leapfrog of one particle (int_engine.rs:265-339 / int_engine3.rs:147-179, periodic):
 // v += kick + g (wrapping i32), x += v (exact i64), wrap into [0, L).
-template <int D>
-__device__ __forceinline__ void leapfrog(const Params& P, uint32_t si, const int32_t* k, int32_t* v, int64_t* x) {
+template <int D, class G>
+__device__ __forceinline__ void leapfrog(const G& P, uint32_t si, const int32_t* k, int32_t* v, int64_t* x) {
     bool pinned = (P.pinned >> si) & 1u;
 #pragma unroll
     for (int a = 0; a < D; a++) {
@@ -102,7 +120,7 @@ __device__ __forceinline__ void leapfrog(const Params& P, uint32_t si, const int
 
 // The displacement trigger of integrate_list (neighbors.wgsl:90-100): has the particle moved
 // half the skin since the list was built? (f32 separations; beyond 8 sigma counts as moved.)
-template <int D> __device__ __forceinline__ bool moved_half_skin(const Params& P, const int64_t* ref, const int64_t* x) {
+template <int D, class G> __device__ __forceinline__ bool moved_half_skin(const G& P, const int64_t* ref, const int64_t* x) {
     bool ok = true;
     float f[D];
 #pragma unroll
@@ -128,6 +146,35 @@ template <int D, typename Fn> __device__ __forceinline__ void for_cells(const Pa
     }
 }
 
+// Visit the 3^D cells around cell c with each cell's periodic image shift: a neighbour cell
+// reached by wrapping below 0 lies a box length lower, above n - 1 a box length higher. With at
+// least 3 cells per axis of at least the list radius, every pair within that radius is found at
+// xj + shift - xi exactly (its minimum image), and every other candidate is at least the list
+// radius away in that form too.
+template <int D, typename Fn> __device__ __forceinline__ void for_cells_shifted(const Params& P, const uint32_t* c, Fn&& f) {
+    const uint32_t nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
+    for (int oz = 0; oz < (D == 3 ? 3 : 1); oz++) {
+        int64_t sz = 0;
+        uint32_t z = 0;
+        if (D == 3) {
+            int t = (int)c[2] + oz - 1;
+            z = t < 0 ? nz - 1 : (t >= (int)nz ? 0 : (uint32_t)t);
+            sz = t < 0 ? -P.box[2] : (t >= (int)nz ? P.box[2] : 0);
+        }
+        for (int oy = 0; oy < 3; oy++) {
+            int t = (int)c[1] + oy - 1;
+            uint32_t y = t < 0 ? ny - 1 : (t >= (int)ny ? 0 : (uint32_t)t);
+            int64_t sy = t < 0 ? -P.box[1] : (t >= (int)ny ? P.box[1] : 0);
+            for (int ox = 0; ox < 3; ox++) {
+                int tx = (int)c[0] + ox - 1;
+                uint32_t x = tx < 0 ? nx - 1 : (tx >= (int)nx ? 0 : (uint32_t)tx);
+                int64_t sx = tx < 0 ? -P.box[0] : (tx >= (int)nx ? P.box[0] : 0);
+                f((z * ny + y) * nx + x, sx, sy, sz);
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ void cell_coords(const Params& P, uint32_t key, uint32_t* c) {
     c[0] = key % P.nc[0];
     c[1] = (key / P.nc[0]) % P.nc[1];
@@ -142,10 +189,11 @@ template <int D, bool MULTI>
 __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* __restrict__ pos_s, const int32_t* __restrict__ vel_s,
                                                     const uint32_t* __restrict__ species_s, const uint32_t* __restrict__ ids_s,
                                                     const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
-                                                    PosRec<D>* __restrict__ pos_o, int32_t* __restrict__ vel_o,
-                                                    uint32_t* __restrict__ species_o, uint32_t* __restrict__ ids_o,
-                                                    PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ nbr,
-                                                    uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ ctl) {
+                                                    const float4* __restrict__ relf, PosRec<D>* __restrict__ pos_o,
+                                                    int32_t* __restrict__ vel_o, uint32_t* __restrict__ species_o,
+                                                    uint32_t* __restrict__ ids_o, PosRec<D>* __restrict__ ref_pos,
+                                                    uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count,
+                                                    uint32_t* __restrict__ ctl) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     int64_t xi[3];
@@ -154,25 +202,64 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     cell_coords(P, keys[i], c);
     uint32_t count = 0;
     const uint32_t n = P.n, cap = P.cap;
-    for_cells<D>(P, c, [&](uint32_t cell) {
-        uint32_t j0 = __ldg(start + cell), j1 = __ldg(start + cell + 1);
-        for (uint32_t j = j0; j < j1; j++) {
-            if (j == i) continue;
-            int64_t xj[3];
-            uint32_t sj = load_particle<D, MULTI>(pos_s, species_s, j, xj);
-            bool ok = true;
-            float f[D];
+    const bool unchecked = P.sep_unchecked;
+    // Candidate j of a neighbour cell cj sits at d = relf[j] + base: base = (cj - c) cell_w + shift
+    // - (xi - c cell_w), an exact integer converted once per cell. Outside [lo, hi] the f32
+    // distance decides (its error is far below the 1e-4 margin); inside, the exact test does.
+    int64_t reli[3];
 #pragma unroll
-            for (int a = 0; a < D; a++) f[a] = sep_s(min_image(xj[a] - xi[a], P.box[a], P.half[a]), ok);
-            if (!ok) continue;
-            float r2 = __fadd_rn(__fmul_rn(f[0], f[0]), __fmul_rn(f[1], f[1]));
-            if (D == 3) r2 = __fadd_rn(r2, __fmul_rn(f[2], f[2]));
-            if (r2 < P.pc[si * P.ns + sj].list2s) {
-                if (count < cap) nbr[(size_t)count * n + i] = j;
-                count++;
+    for (int a = 0; a < 3; a++) reli[a] = a < D ? xi[a] - (int64_t)c[a] * P.cell_w[a] : 0;
+    auto exact = [&](uint32_t j, const int64_t* xs, uint32_t sj) -> bool {
+        int64_t xj[3];
+        load_particle<D, false>(pos_s, nullptr, j, xj);
+        float f[D];
+        bool ok = true;
+        if (unchecked) {
+#pragma unroll
+            for (int a = 0; a < D; a++) f[a] = sep_near(xj[a] - xs[a]);
+        } else {
+#pragma unroll
+            for (int a = 0; a < D; a++) f[a] = sep_s(xj[a] - xs[a], ok);
+        }
+        float r2 = __fadd_rn(__fmul_rn(f[0], f[0]), __fmul_rn(f[1], f[1]));
+        if (D == 3) r2 = __fadd_rn(r2, __fmul_rn(f[2], f[2]));
+        return ok && r2 < P.pc[si * P.ns + sj].list2s;
+    };
+    const float lo0 = P.pc[si * P.ns].list2lo, hi0 = P.pc[si * P.ns].list2hi;
+    const uint32_t nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
+    for (int oz = 0; oz < (D == 3 ? 3 : 1); oz++) {
+        int tz = (int)c[2] + oz - 1;
+        uint32_t z = D == 3 ? (tz < 0 ? nz - 1 : (tz >= (int)nz ? 0 : (uint32_t)tz)) : 0;
+        int64_t sz = D == 3 ? (tz < 0 ? -P.box[2] : (tz >= (int)nz ? P.box[2] : 0)) : 0;
+        for (int oy = 0; oy < 3; oy++) {
+            int ty = (int)c[1] + oy - 1;
+            uint32_t y = ty < 0 ? ny - 1 : (ty >= (int)ny ? 0 : (uint32_t)ty);
+            int64_t sy = ty < 0 ? -P.box[1] : (ty >= (int)ny ? P.box[1] : 0);
+            for (int ox = 0; ox < 3; ox++) {
+                int tx = (int)c[0] + ox - 1;
+                uint32_t x = tx < 0 ? nx - 1 : (tx >= (int)nx ? 0 : (uint32_t)tx);
+                int64_t sx = tx < 0 ? -P.box[0] : (tx >= (int)nx ? P.box[0] : 0);
+                uint32_t cell = (z * ny + y) * nx + x;
+                const int64_t xs[3] = {xi[0] - sx, xi[1] - sy, D == 3 ? xi[2] - sz : 0};
+                const float b0 = __fmul_rn(__ll2float_rn(((int64_t)x - (int64_t)c[0]) * P.cell_w[0] + sx - reli[0]), 1.0f / 4294967296.0f);
+                const float b1 = __fmul_rn(__ll2float_rn(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]), 1.0f / 4294967296.0f);
+                const float b2 = D == 3 ? __fmul_rn(__ll2float_rn(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]), 1.0f / 4294967296.0f) : 0.0f;
+                uint32_t j0 = __ldg(start + cell), j1 = __ldg(start + cell + 1);
+                for (uint32_t j = j0; j < j1; j++) {
+                    float4 r = __ldg(relf + j);
+                    float dx = r.x + b0, dy = r.y + b1, dz = r.z + b2;
+                    float r2a = dx * dx + dy * dy + dz * dz;
+                    uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                    float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
+                    bool in = r2a < lo || (r2a <= hi && exact(j, xs, sj));
+                    if (in && j != i) {
+                        if (count < cap) nbr[(size_t)count * n + i] = j;
+                        count++;
+                    }
+                }
             }
         }
-    });
+    }
     if (count > cap) {
         ctl[1] = 1;
         count = cap;
@@ -202,12 +289,61 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
     int32_t k[3] = {0, 0, 0};
     const uint32_t m = __ldg(nbr_count + i), n = P.n;
     const PairC pc0 = P.pc[0];
-    for (uint32_t q = 0; q < m; q++) {
-        uint32_t j = __ldg(nbr + (size_t)q * n + i);
-        int64_t xj[3];
-        uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
-        float fr, s6, r2;
-        pair_kick<D>(P, MULTI ? P.pc[si * P.ns + sj] : pc0, cs, xi, xj, k, fr, s6, r2);
+    // A particle farther than `reach` from every face sees each listed neighbour at xj - xi
+    // without a periodic image, and within 8 sigma: no minimum image, no range check.
+    bool interior = true;
+#pragma unroll
+    for (int a = 0; a < D; a++) interior = interior && xi[a] >= P.reach && xi[a] < P.box[a] - P.reach;
+    if (interior) {
+        // UNROLL neighbours at a time: their list entries, then their positions, are all loaded
+        // before any is used, so several gathers are in flight per thread.
+        constexpr int UNROLL = 4;
+        uint32_t q = 0;
+        for (; q + UNROLL <= m; q += UNROLL) {
+            uint32_t j[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; u++) j[u] = __ldg(nbr + (size_t)(q + u) * n + i);
+            int64_t xj[UNROLL][3];
+            uint32_t sj[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; u++) sj[u] = load_particle<D, MULTI>(pos_in, species, j[u], xj[u]);
+#pragma unroll
+            for (int u = 0; u < UNROLL; u++) {
+                float f[D];
+#pragma unroll
+                for (int a = 0; a < D; a++) f[a] = sep_near(xj[u][a] - xi[a]);
+                const PairC& pc = MULTI ? P.pc[si * P.ns + sj[u]] : pc0;
+                float fr, s6, r2;
+                if (pair_fr<D>(pc, f, fr, s6, r2)) {
+                    float am = __fmul_rn(-fr, cs);
+#pragma unroll
+                    for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[a])));
+                }
+            }
+        }
+        for (; q < m; q++) {
+            uint32_t j = __ldg(nbr + (size_t)q * n + i);
+            int64_t xj[3];
+            uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
+            float f[D];
+#pragma unroll
+            for (int a = 0; a < D; a++) f[a] = sep_near(xj[a] - xi[a]);
+            const PairC& pc = MULTI ? P.pc[si * P.ns + sj] : pc0;
+            float fr, s6, r2;
+            if (pair_fr<D>(pc, f, fr, s6, r2)) {
+                float am = __fmul_rn(-fr, cs);
+#pragma unroll
+                for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[a])));
+            }
+        }
+    } else {
+        for (uint32_t q = 0; q < m; q++) {
+            uint32_t j = __ldg(nbr + (size_t)q * n + i);
+            int64_t xj[3];
+            uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
+            float fr, s6, r2;
+            pair_kick<D>(P, MULTI ? P.pc[si * P.ns + sj] : pc0, cs, xi, xj, k, fr, s6, r2);
+        }
     }
     int32_t v[3];
 #pragma unroll
@@ -328,6 +464,119 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
         double s = 0.0;
         for (int wq = 0; wq < (int)(blockDim.x >> 5); wq++) s += sh[threadIdx.x][wq];
         partial[4 * blockIdx.x + threadIdx.x] = s;
+    }
+}
+
+// ---------------------------------------------------------------- velocity-rescale thermostat
+// The half-step kinetic energy summed exactly: per block and species, the 128-bit sum of v^2 over
+// the moving particles' velocity components (part[8 b + 2 s + {0: low, 1: high}]).
+template <int D>
+__global__ void k_ke_exact(uint32_t n, const int32_t* __restrict__ vel, const uint32_t* __restrict__ species, uint32_t pinned,
+                           unsigned long long* __restrict__ part) {
+    __shared__ unsigned long long lo[GBMD_MAX_SPECIES][256], hi[GBMD_MAX_SPECIES][256];
+    unsigned __int128 acc[GBMD_MAX_SPECIES] = {0, 0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t s = species[i];
+        if ((pinned >> s) & 1u) continue;
+        for (int a = 0; a < D; a++) {
+            long long v = vel[D * i + a];
+            acc[s & 3] += (unsigned __int128)(unsigned long long)(v * v);
+        }
+    }
+    for (int s = 0; s < GBMD_MAX_SPECIES; s++) {
+        lo[s][threadIdx.x] = (unsigned long long)acc[s];
+        hi[s][threadIdx.x] = (unsigned long long)(acc[s] >> 64);
+    }
+    __syncthreads();
+    if (threadIdx.x < GBMD_MAX_SPECIES) {
+        unsigned __int128 t = 0;
+        for (uint32_t k = 0; k < blockDim.x; k++) t += ((unsigned __int128)hi[threadIdx.x][k] << 64) | lo[threadIdx.x][k];
+        part[8 * blockIdx.x + 2 * threadIdx.x] = (unsigned long long)t;
+        part[8 * blockIdx.x + 2 * threadIdx.x + 1] = (unsigned long long)(t >> 64);
+    }
+}
+
+struct ThermoP {
+    uint32_t nblocks, ns;
+    double masses[GBMD_MAX_SPECIES];
+    double dt, dof, t;
+};
+// fac[0] = sqrt(t / now) with now = KE / dof, KE = sum_s 1/2 m_s S_s (UNIT / dt)^2 in f64 in
+// species order; fac[1] = 1 when now <= 0 (set_temperature then leaves the state alone).
+static __global__ void k_thermo_factor(ThermoP T, const unsigned long long* __restrict__ part, double* __restrict__ fac) {
+    double ke = 0.0;
+    double u = __ddiv_rn(1.0 / 4294967296.0, T.dt);
+    for (uint32_t s = 0; s < T.ns; s++) {
+        unsigned __int128 S = 0;
+        for (uint32_t b = 0; b < T.nblocks; b++) S += ((unsigned __int128)part[8 * b + 2 * s + 1] << 64) | part[8 * b + 2 * s];
+        double sum = __dadd_rn(__dmul_rn(__ull2double_rn((unsigned long long)(S >> 64)), 18446744073709551616.0),
+                               __ull2double_rn((unsigned long long)S));
+        ke = __dadd_rn(ke, __dmul_rn(__dmul_rn(__dmul_rn(0.5, T.masses[s]), sum), __dmul_rn(u, u)));
+    }
+    double now = __ddiv_rn(ke, T.dof);
+    bool skip = !(now > 0.0);
+    fac[0] = skip ? 1.0 : __dsqrt_rn(__ddiv_rn(T.t, now));
+    fac[1] = skip ? 1.0 : 0.0;
+}
+
+// v <- round(v f) as i32 for moving particles (init.rs:99-101), then per-block sums of the new
+// velocities of moving particles (vpart[3 b + a]).
+template <int D>
+__global__ void k_rescale(uint32_t n, int32_t* __restrict__ vel, const uint32_t* __restrict__ species, uint32_t pinned,
+                          const double* __restrict__ fac, long long* __restrict__ vpart) {
+    __shared__ long long sh[3][32];
+    const double f = fac[0];
+    const bool skip = fac[1] != 0.0;
+    long long acc[3] = {0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if ((pinned >> species[i]) & 1u) continue;
+        for (int a = 0; a < D; a++) {
+            int32_t v = vel[D * i + a];
+            if (!skip) {
+                v = sat_i32_f64(round(__dmul_rn((double)v, f)));
+                vel[D * i + a] = v;
+            }
+            acc[a] += v;
+        }
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int a = 0; a < 3; a++) {
+        long long v = acc[a];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[a][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[threadIdx.x][w];
+        vpart[3 * blockIdx.x + threadIdx.x] = t;
+    }
+}
+
+// zero_velocity_sum over the moving particles in id order (init.rs:76-89 / three.rs:376-389):
+// the k-th moving particle loses q + (k < r), q = div_euclid(sum, m), r = rem_euclid(sum, m);
+// mrank[id] is k.
+template <int D>
+__global__ void k_zero_apply(uint32_t n, int32_t* __restrict__ vel, const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids,
+                             const uint32_t* __restrict__ mrank, uint32_t pinned, uint32_t moving, const long long* __restrict__ vpart,
+                             uint32_t nblocks, const double* __restrict__ fac) {
+    __shared__ long long tot[3];
+    if (threadIdx.x < 3) {
+        long long t = 0;
+        for (uint32_t b = 0; b < nblocks; b++) t += vpart[3 * b + threadIdx.x];
+        tot[threadIdx.x] = t;
+    }
+    __syncthreads();
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fac[1] != 0.0 || moving == 0 || ((pinned >> species[i]) & 1u)) return;
+    long long m = moving, k = mrank[ids[i]];
+    for (int a = 0; a < D; a++) {
+        long long q = tot[a] / m, r = tot[a] % m;
+        if (r < 0) {
+            q -= 1;
+            r += m;
+        }
+        vel[D * i + a] = (int32_t)((uint32_t)vel[D * i + a] - (uint32_t)(q + (k < r ? 1 : 0)));
     }
 }
 

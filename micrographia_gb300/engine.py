@@ -255,7 +255,7 @@ def make_init(recipe, n, t, seed, jitter=0.1, rho_liquid=0.7, rho_vapour=0.05, s
 class BatchEngine:
     """Many independent periodic systems stepped together (gbmd_batch_*)."""
 
-    def __init__(self, systems, states, mode=None, threads=0, block_steps=0):
+    def __init__(self, systems, states, mode=None, threads=0, block_steps=0, device=0):
         self._lib = _abi.lib()
         if len(systems) != len(states) or not systems:
             raise ValueError("one state per system")
@@ -270,7 +270,7 @@ class BatchEngine:
         pos = np.ascontiguousarray(np.concatenate([st.pos for st in states]))
         vel = np.ascontiguousarray(np.concatenate([st.vel for st in states]))
         sp = np.ascontiguousarray(np.concatenate([st.species for st in states]))
-        opts = _options(mode or ForceMode.verlet_for(systems[0], 0), threads, block_steps)
+        opts = _options(mode or ForceMode.verlet_for(systems[0], 0), threads, block_steps, device=device)
         h = C.c_void_p()
         _abi.check(
             self._lib.gbmd_batch_create(
@@ -304,6 +304,17 @@ class BatchEngine:
         s = C.c_void_p()
         _abi.check(self._lib.gbmd_batch_stream(self._h, C.byref(s)))
         return s.value
+
+    def stats(self):
+        l, r = C.c_uint64(), C.c_uint32()
+        _abi.check(self._lib.gbmd_batch_stats(self._h, C.byref(l), C.byref(r)))
+        return l.value, r.value
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def close(self):
         if getattr(self, "_h", None):

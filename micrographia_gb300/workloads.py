@@ -1,0 +1,89 @@
+"""The benchmark workloads of the benchmark spec, as seeded synthetic systems (no dataset is
+involved): each function returns systems and device-init recipes, never particle data.
+
+- config2: 3D LJ liquid, FCC N = 1,048,576 at rho 0.8442, T 0.72 (the LAMMPS in.lj shape).
+- config3: 2D liquid-vapour slab, N = 2^24 in a 4:1 box, liquid rho 0.70 over the central
+  quarter, vapour 0.05, rescale to T = 0.45 every 10 steps.
+- config4: 1024 independent 2D LJ systems, N = floor(256 * 256^u) (log-uniform in [256, 65536]),
+  rho ~ U[0.3, 0.8], T ~ U[0.5, 1.5], seed base + k; u, rho and T drawn from Threefry streams 10,
+  11 and 12 of the base seed.
+- config5: a Poisson stream of 2D/3D requests with N log-uniform in [1024, 2^20].
+"""
+
+import math
+
+from . import _abi
+from .core import Pair, System, System3, box_for, cube_for
+from .engine import make_init
+
+MASK = 0xFFFFFFFF
+
+
+def threefry2x32(c0, c1, k0, k1):
+    """Threefry-2x32-20 (Random123), as gpu-prims/src/threefry.rs:7-22."""
+    rot = (13, 15, 26, 6, 17, 29, 16, 24)
+    ks = (k0, k1, 0x1BD11BDA ^ k0 ^ k1)
+    x0, x1 = (c0 + k0) & MASK, (c1 + k1) & MASK
+    for r in range(20):
+        x0 = (x0 + x1) & MASK
+        s = rot[r % 8]
+        x1 = ((x1 << s) | (x1 >> (32 - s))) & MASK
+        x1 ^= x0
+        if r & 3 == 3:
+            i = (r >> 2) + 1
+            x0 = (x0 + ks[i % 3]) & MASK
+            x1 = (x1 + ks[(i + 1) % 3] + i) & MASK
+    return x0, x1
+
+
+def uniform(seed, stream, i):
+    """threefry::uniform (threefry.rs:35-37): 53 random bits in [0, 1)."""
+    a, b = threefry2x32(i & MASK, stream, seed & MASK, (seed >> 32) & MASK)
+    bits = ((a << 21) ^ (b >> 11)) & ((1 << 53) - 1)
+    return bits * (1.0 / (1 << 53))
+
+
+def config2(n=1 << 20):
+    sys3 = System3(cube_for(n, 0.8442), 0.005, Pair.lj(2.5), [1.0])
+    return sys3, make_init(_abi.INIT_FCC, n, 0.72, 1, 0.05)
+
+
+def config3(n=1 << 24):
+    area = n / (0.25 * 0.70 + 0.75 * 0.05)
+    sys_ = System(box_for(n, n / area, 4.0), 0.005, Pair.lj(2.5), [1.0])
+    return sys_, make_init(_abi.INIT_SLAB, n, 0.45, 1, 0.1, 0.70, 0.05, 0.25)
+
+
+def config4(count=1024, base_seed=1, n_min=256, n_max=65536):
+    out = []
+    ratio = n_max / n_min
+    for k in range(count):
+        u = uniform(base_seed, 10, k)
+        n = int(math.floor(n_min * ratio**u))
+        rho = 0.3 + 0.5 * uniform(base_seed, 11, k)
+        t = 0.5 + uniform(base_seed, 12, k)
+        seed = base_seed + k
+        sys_ = System(box_for(n, rho, 1.0), 0.005, Pair.lj(2.5), [1.0]).with_seed(seed)
+        out.append((sys_, make_init(_abi.INIT_FLUID, n, t, seed, 0.1)))
+    return out
+
+
+def config5(count, rate, base_seed=1, n_min=1024, n_max=1 << 20):
+    """Poisson arrivals at `rate` requests per second: (arrival time s, system, init) each."""
+    out = []
+    t = 0.0
+    for k in range(count):
+        t += -math.log(1.0 - uniform(base_seed, 20, k)) / rate
+        u = uniform(base_seed, 21, k)
+        n = int(math.floor(n_min * (n_max / n_min) ** u))
+        rho = 0.3 + 0.55 * uniform(base_seed, 22, k)
+        temp = 0.5 + uniform(base_seed, 23, k)
+        seed = base_seed + 1000 + k
+        if uniform(base_seed, 24, k) < 0.5:
+            sys_ = System(box_for(n, rho, 1.0), 0.005, Pair.lj(2.5), [1.0]).with_seed(seed)
+            init = make_init(_abi.INIT_FLUID, n, temp, seed, 0.1)
+        else:
+            sys_ = System3(cube_for(n, rho), 0.005, Pair.lj(2.5), [1.0]).with_seed(seed)
+            init = make_init(_abi.INIT_FCC, n, temp, seed, 0.05)
+        out.append((t, sys_, init))
+    return out

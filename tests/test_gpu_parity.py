@@ -351,6 +351,28 @@ def test_frame_3d(O):
     assert np.array_equal(rdf, O.rdf(sys3, s, 200, 5.0))
 
 
+# ---------------------------------------------------------------- velocity-rescale thermostat (configs[2])
+def test_rescale_thermostat_matches_oracle(O):
+    """Slab start, rescale to T = 0.45 every 10 steps: the GPU trajectory equals the oracle's
+    (IntEngine<f32> stepped one step at a time, the exact-integer rescale after every 10th)."""
+    n = 20000
+    sys_ = System(box_for(n, 0.2125, 4.0), 0.005, Pair.lj(2.5), [1.0])
+    s0 = O.init(sys_, make_init(_abi.INIT_SLAB, n, 0.45, 7, 0.1, 0.7, 0.05, 0.25))
+    with GpuEngine(sys_, s0, ForceMode.verlet_with_skin(sys_, n, 0.3), rescale_every=10, rescale_t=0.45) as g:
+        c = O.IntEngine(sys_, s0)
+        g.step(7)
+        g.step(88)  # crosses a 60-step graph block and single steps either side
+        for k in range(95):
+            c.step(1)
+            if (k + 1) % 10 == 0:
+                st = c.state
+                st.vel = O.set_temperature(sys_, st, 0.45, exact=True)
+                c.set_state(st)
+        got = g.read_state()
+        assert got == c.state
+        assert got.velocity_sum() == [0, 0]
+
+
 # ---------------------------------------------------------------- full size (configs 2): size-independent properties
 def test_config2_full_size_properties(O):
     """3D FCC N=1,048,576, rho 0.8442, T 0.72, skin 0.3: momentum stays exactly zero, the run
@@ -369,3 +391,38 @@ def test_config2_full_size_properties(O):
         g.step(100)
         g.reverse()
         assert g.read_state().hash() == s0.hash()
+
+
+# ---------------------------------------------------------------- batched replicas (configs[3])
+def test_batch_replicas_match_their_plain_runs(O):
+    """Uneven 2D systems stepped in one batch: each replica's state equals md-ref's IntEngine<f32>
+    run of that system alone, bit for bit (through a 100-step graph block and single steps)."""
+    from micrographia_gb300 import BatchEngine, workloads
+
+    cfg = workloads.config4(count=10, base_seed=5, n_min=256, n_max=4096)
+    systems = [s for s, _ in cfg]
+    states = [O.init(s, spec) for s, spec in cfg]
+    with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3)) as b:
+        b.step(150)
+        launches, rebuilds = b.stats()
+        assert rebuilds >= 2
+        for k, (sys_, st) in enumerate(zip(systems, states)):
+            c = O.IntEngine(sys_, st)
+            c.step(150)
+            assert b.read_system(k) == c.state, k
+
+
+def test_batch_3d(O):
+    from micrographia_gb300 import BatchEngine
+
+    systems, states = [], []
+    for k, (n, rho) in enumerate([(500, 0.8), (2048, 0.6), (864, 0.85)]):
+        s3 = System3(cube_for(n, rho), 0.005, Pair.lj(2.5), [1.0])
+        systems.append(s3)
+        states.append(O.fcc_maxwell(s3, n, 0.9, 10 + k))
+    with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3)) as b:
+        b.step(60)
+        for k in range(3):
+            c = O.IntEngine(systems[k], states[k])
+            c.step(60)
+            assert b.read_system(k) == c.state
