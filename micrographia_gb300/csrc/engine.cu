@@ -185,6 +185,7 @@ struct gbmd_engine {
     uint32_t *hist = nullptr, *scan_tmp = nullptr, *start = nullptr;
     uint32_t *nbr = nullptr, *nbr_count = nullptr;
     float4* relf = nullptr;  // cell-relative f32 coordinates of the sorted scratch state
+    uint4* qpos[2] = {nullptr, nullptr}; // 3D quotient records of the positions (ping-pong)
     uint32_t* ctl = nullptr; // [0] rebuild, [1] overflow, [2] rebuilds
     double* partial = nullptr;
     void* staging = nullptr;  // id-ordered I/O staging (n * D int64)
@@ -231,7 +232,7 @@ void free_all(gbmd_engine* e) {
             if (e->exec[p][b]) cudaGraphExecDestroy(e->exec[p][b]);
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
-                    e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf};
+                    e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1]};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (e->st) cudaStreamDestroy(e->st);
@@ -253,7 +254,7 @@ template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t
     enqueue_bin<D>(e, s, e->P);
     k_build_list<D, MULTI><<<blocks_for(e->n, 128), 128, 0, s>>>(
         e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, e->relf,
-        (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl);
+        (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl, e->qpos[e->cur]);
     note_launch();
 }
 
@@ -278,6 +279,7 @@ void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
 template <int D, bool MULTI> void enqueue_force_t(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
     if (e->verlet) {
         k_force_list<D, MULTI><<<blocks_for(e->n, threads), threads, 0, s>>>(e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1],
+                                                                           e->qpos[e->cur], e->qpos[e->cur ^ 1],
                                                                            e->vel, e->species, e->nbr, e->nbr_count,
                                                                            (const Rec<D>*)e->ref_pos, e->ctl);
         note_launch();
@@ -598,11 +600,13 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     GBMD_TRY(allocT(&e->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(n))));
     GBMD_TRY(allocT(&e->start, (size_t)e->P.ncell + 1));
     if (e->verlet) {
-        GBMD_TRY(allocT(&e->nbr, (size_t)n * cap));
+        GBMD_TRY(allocT(&e->nbr, ((size_t)n + 31) / 32 * 32 * (((size_t)cap + 3) & ~(size_t)3)));
         GBMD_TRY(allocT(&e->nbr_count, n));
     }
     GBMD_TRY(allocT(&e->ctl, 16));
     GBMD_TRY(allocT(&e->relf, n));
+    GBMD_TRY(allocT(&e->qpos[0], n));
+    GBMD_TRY(allocT(&e->qpos[1], n));
     GBMD_TRY(allocT(&e->mrank, n));
     GBMD_TRY(allocT(&e->tpart, 8 * (size_t)e->thermo_nb));
     GBMD_TRY(allocT(&e->vpart, 3 * (size_t)e->thermo_nb));
@@ -893,11 +897,13 @@ int gbmd_debug_list(gbmd_engine* e, uint32_t* counts, uint32_t* nbr, uint64_t nb
     if (!e->verlet) return fail(GBMD_E_INVALID, "the engine has no Verlet list (cell mode)");
     GBMD_TRY(prepare_pairs(e));
     GBMD_TRY(gbmd_sync(e));
-    size_t n = e->n, cap = e->P.cap;
-    std::vector<uint32_t> cnt(n), ids(n), lst(n * cap);
+    size_t n = e->n, cap4 = ((size_t)e->P.cap + 3) & ~(size_t)3;
+    size_t total = (n + 31) / 32 * 32 * cap4;
+    std::vector<uint32_t> cnt(n), ids(n), lst(total);
     GBMD_CUDA_TRY(cudaMemcpy(cnt.data(), e->nbr_count, n * 4, cudaMemcpyDeviceToHost));
     GBMD_CUDA_TRY(cudaMemcpy(ids.data(), e->ids, n * 4, cudaMemcpyDeviceToHost));
-    GBMD_CUDA_TRY(cudaMemcpy(lst.data(), e->nbr, n * cap * 4, cudaMemcpyDeviceToHost));
+    GBMD_CUDA_TRY(cudaMemcpy(lst.data(), e->nbr, total * 4, cudaMemcpyDeviceToHost));
+    auto slot = [&](size_t i, size_t k) { return ((i >> 5) * cap4 + (k & ~(size_t)3)) * 32 + ((i & 31) << 2) + (k & 3); };
     std::vector<uint32_t> slot_of(n);
     for (size_t s = 0; s < n; s++) slot_of[ids[s]] = (uint32_t)s;
     uint64_t off = 0;
@@ -905,7 +911,7 @@ int gbmd_debug_list(gbmd_engine* e, uint32_t* counts, uint32_t* nbr, uint64_t nb
         size_t s = slot_of[id];
         counts[id] = cnt[s];
         if (off + cnt[s] > nbr_cap) return fail(GBMD_E_INVALID, "nbr_cap too small");
-        for (size_t q = 0; q < cnt[s]; q++) nbr[off++] = ids[lst[q * n + s]];
+        for (size_t q = 0; q < cnt[s]; q++) nbr[off++] = ids[lst[slot(s, q)]];
     }
     return GBMD_OK;
 }

@@ -181,8 +181,38 @@ __device__ __forceinline__ void cell_coords(const Params& P, uint32_t key, uint3
     c[2] = key / (P.nc[0] * P.nc[1]);
 }
 
+// Verlet lists are warp-tiled: the 32 particles of a warp (consecutive slots) store their
+// neighbours in groups of four, group g of lane l at ((w cap4 + 4 g) 32 + 4 l), so one 16-byte
+// load gives a thread four neighbours and a warp's load is 512 contiguous bytes. cap4 is the
+// capacity rounded up to a multiple of 4.
+__device__ __forceinline__ size_t list_slot(uint32_t i, uint32_t k, uint32_t cap4) {
+    return ((size_t)(i >> 5) * cap4 + (k & ~3u)) * 32 + ((i & 31u) << 2) + (k & 3u);
+}
+
+// The quotient record of a position: the low 32 bits of x >> 4 per axis and the remainders
+// x & 15 in bytes of the fourth word (species in its top byte). For two particles whose true
+// separation d = xj - xi needs no periodic image and is below 8 sigma, D = Xj - Xi in wrapping
+// 32-bit arithmetic is exact and d = 16 D + (Rj - Ri).
+template <int D> __device__ __forceinline__ uint4 quot_record(const int64_t* x, uint32_t species) {
+    uint4 r;
+    r.x = (uint32_t)(x[0] >> 4);
+    r.y = (uint32_t)(x[1] >> 4);
+    r.z = D == 3 ? (uint32_t)(x[2] >> 4) : 0u;
+    uint32_t w = (uint32_t)(x[0] & 15) | ((uint32_t)(x[1] & 15) << 8) | (species << 24);
+    if (D == 3) w |= (uint32_t)(x[2] & 15) << 16;
+    r.w = w;
+    return r;
+}
+// sep_near from quotient records: trunc(d / 16) with d = 16 D + (rj - ri), 0 <= r < 16:
+// floor(d / 16) = D - (rj < ri), and trunc adds one back when d < 0 and rj != ri.
+__device__ __forceinline__ float quot_sep(uint32_t Xj, uint32_t rj, uint32_t Xi, uint32_t ri) {
+    int32_t f = (int32_t)(Xj - Xi) - (rj < ri ? 1 : 0);
+    int32_t q = f + ((f < 0 && rj != ri) ? 1 : 0);
+    return __int2float_rn(q);
+}
+
 // Verlet-list build over the cell-sorted scratch state (neighbors.wgsl:27-64 with the exact f32
-// test of engine.rs:302-313 / 184-186): lists are column-major, nbr[k * n + i]; a particle with
+// test of engine.rs:302-313 / 184-186): lists are warp-tiled (list_slot); a particle with
 // more than `cap` neighbours sets ctl[1] (overflow). Also copies the sorted state back into the
 // engine's arrays and records each particle's reference position for the trigger.
 template <int D, bool MULTI>
@@ -193,7 +223,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                                                     int32_t* __restrict__ vel_o, uint32_t* __restrict__ species_o,
                                                     uint32_t* __restrict__ ids_o, PosRec<D>* __restrict__ ref_pos,
                                                     uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count,
-                                                    uint32_t* __restrict__ ctl) {
+                                                    uint32_t* __restrict__ ctl, uint4* __restrict__ qpos_o) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     int64_t xi[3];
@@ -201,7 +231,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     uint32_t c[3];
     cell_coords(P, keys[i], c);
     uint32_t count = 0;
-    const uint32_t n = P.n, cap = P.cap;
+    const uint32_t cap = P.cap, cap4 = (P.cap + 3u) & ~3u;
     const bool unchecked = P.sep_unchecked;
     // Candidate j of a neighbour cell cj sits at d = relf[j] + base: base = (cj - c) cell_w + shift
     // - (xi - c cell_w), an exact integer converted once per cell. Outside [lo, hi] the f32
@@ -253,7 +283,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                     float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
                     bool in = r2a < lo || (r2a <= hi && exact(j, xs, sj));
                     if (in && j != i) {
-                        if (count < cap) nbr[(size_t)count * n + i] = j;
+                        if (count < cap) nbr[list_slot(i, count, cap4)] = j;
                         count++;
                     }
                 }
@@ -267,6 +297,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     nbr_count[i] = count;
     pos_o[i] = pos_s[i];
     ref_pos[i] = pos_s[i];
+    if (D == 3 && qpos_o) qpos_o[i] = quot_record<D>(xi, si);
 #pragma unroll
     for (int a = 0; a < D; a++) vel_o[D * i + a] = vel_s[D * i + a];
     species_o[i] = species_s[i];
@@ -278,6 +309,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // ping-pongs the two), so every kick sees positions of the same time step.
 template <int D, bool MULTI>
 __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
+                                                    const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                     int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
                                                     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                     const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
@@ -287,62 +319,70 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
     uint32_t si = load_particle<D, MULTI>(pos_in, species, i, xi);
     const float cs = P.kick_cs[si];
     int32_t k[3] = {0, 0, 0};
-    const uint32_t m = __ldg(nbr_count + i), n = P.n;
+    const uint32_t m = __ldg(nbr_count + i), cap4 = (P.cap + 3u) & ~3u;
     const PairC pc0 = P.pc[0];
+    const uint4* groups = reinterpret_cast<const uint4*>(nbr + list_slot(i, 0, cap4)); // group g at groups[32 g]
     // A particle farther than `reach` from every face sees each listed neighbour at xj - xi
     // without a periodic image, and within 8 sigma: no minimum image, no range check.
     bool interior = true;
 #pragma unroll
     for (int a = 0; a < D; a++) interior = interior && xi[a] >= P.reach && xi[a] < P.box[a] - P.reach;
-    if (interior) {
-        // UNROLL neighbours at a time: their list entries, then their positions, are all loaded
-        // before any is used, so several gathers are in flight per thread.
-        constexpr int UNROLL = 4;
-        uint32_t q = 0;
-        for (; q + UNROLL <= m; q += UNROLL) {
-            uint32_t j[UNROLL];
+    auto add_kick = [&](const float* f, const PairC& pc) {
+        float fr, s6, r2;
+        if (pair_fr<D>(pc, f, fr, s6, r2)) {
+            float am = __fmul_rn(-fr, cs);
 #pragma unroll
-            for (int u = 0; u < UNROLL; u++) j[u] = __ldg(nbr + (size_t)(q + u) * n + i);
-            int64_t xj[UNROLL][3];
-            uint32_t sj[UNROLL];
-#pragma unroll
-            for (int u = 0; u < UNROLL; u++) sj[u] = load_particle<D, MULTI>(pos_in, species, j[u], xj[u]);
-#pragma unroll
-            for (int u = 0; u < UNROLL; u++) {
-                float f[D];
-#pragma unroll
-                for (int a = 0; a < D; a++) f[a] = sep_near(xj[u][a] - xi[a]);
-                const PairC& pc = MULTI ? P.pc[si * P.ns + sj[u]] : pc0;
-                float fr, s6, r2;
-                if (pair_fr<D>(pc, f, fr, s6, r2)) {
-                    float am = __fmul_rn(-fr, cs);
-#pragma unroll
-                    for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[a])));
-                }
-            }
+            for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[a])));
         }
-        for (; q < m; q++) {
-            uint32_t j = __ldg(nbr + (size_t)q * n + i);
-            int64_t xj[3];
-            uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
-            float f[D];
+    };
+    const uint32_t ngroups = (m + 3u) >> 2;
+    if (interior && D == 3) {
+        // 3D: neighbours come from the 16-byte quotient records (one gather each) and the
+        // separation is formed with 32-bit integers (quot_sep).
+        const uint4 qi = __ldg(qpos_in + i);
+        const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
+        for (uint32_t g = 0; g < ngroups; g++) {
+            if (g + 2 < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2)));
+            const uint4 jv = __ldg(groups + 32 * g);
+            const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
+            const uint32_t left = m - 4 * g;
+            uint4 r[4];
 #pragma unroll
-            for (int a = 0; a < D; a++) f[a] = sep_near(xj[a] - xi[a]);
-            const PairC& pc = MULTI ? P.pc[si * P.ns + sj] : pc0;
-            float fr, s6, r2;
-            if (pair_fr<D>(pc, f, fr, s6, r2)) {
-                float am = __fmul_rn(-fr, cs);
+            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? jj[u] : i));
 #pragma unroll
-                for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[a])));
+            for (int u = 0; u < 4; u++) {
+                if ((uint32_t)u >= left) break;
+                float f[D];
+                const uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
+#pragma unroll
+                for (int a = 0; a < D; a++) f[a] = quot_sep(Xj[a], (r[u].w >> (8 * a)) & 15u, Xi[a], (qi.w >> (8 * a)) & 15u);
+                add_kick(f, MULTI ? P.pc[si * P.ns + (r[u].w >> 24)] : pc0);
             }
         }
     } else {
-        for (uint32_t q = 0; q < m; q++) {
-            uint32_t j = __ldg(nbr + (size_t)q * n + i);
-            int64_t xj[3];
-            uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
-            float fr, s6, r2;
-            pair_kick<D>(P, MULTI ? P.pc[si * P.ns + sj] : pc0, cs, xi, xj, k, fr, s6, r2);
+        for (uint32_t g = 0; g < ngroups; g++) {
+            if (g + 2 < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2)));
+            const uint4 jv = __ldg(groups + 32 * g);
+            const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
+            const uint32_t left = m - 4 * g;
+            int64_t xj[4][3];
+            uint32_t sj[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) sj[u] = load_particle<D, MULTI>(pos_in, species, (uint32_t)u < left ? jj[u] : i, xj[u]);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if ((uint32_t)u >= left) break;
+                float f[D];
+                bool ok = true;
+                if (interior) {
+#pragma unroll
+                    for (int a = 0; a < D; a++) f[a] = sep_near(xj[u][a] - xi[a]);
+                } else {
+#pragma unroll
+                    for (int a = 0; a < D; a++) f[a] = sep_s(min_image(xj[u][a] - xi[a], P.box[a], P.half[a]), ok);
+                }
+                if (ok) add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
+            }
         }
     }
     int32_t v[3];
@@ -352,6 +392,7 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
 #pragma unroll
     for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
     store_pos<D>(pos_out, i, xi, si);
+    if (D == 3) qpos_out[i] = quot_record<D>(xi, si);
     int64_t xr[3];
     load_particle<D, false>(ref_pos, nullptr, i, xr);
     if (moved_half_skin<D>(P, xr, xi)) ctl[0] = 1;
@@ -425,7 +466,8 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
         };
         if (nbr) {
             uint32_t m = nbr_count[i];
-            for (uint32_t q = 0; q < m; q++) visit(nbr[(size_t)q * P.n + i]);
+            const uint32_t cap4 = (P.cap + 3u) & ~3u;
+            for (uint32_t q = 0; q < m; q++) visit(nbr[list_slot(i, q, cap4)]);
         } else {
             uint32_t c[3];
             cell_coords(P, keys[i], c);
