@@ -456,16 +456,20 @@ int kicks_dispatch(gbmd_engine* e, int32_t* kicks, double* partial, int reverse)
 }
 
 // ---- id-ordered I/O
+struct Box3 {
+    int64_t v[3];
+    __device__ int64_t operator[](int a) const { return v[a]; }
+};
 template <int D>
-__global__ void k_to_ids(uint32_t n, const Rec<D>* pos, const int32_t* vel, const uint32_t* species, const uint32_t* ids, int64_t* opos,
-                         int32_t* ovel, uint32_t* ospecies) {
+__global__ void k_to_ids(uint32_t n, Box3 box, const Rec<D>* pos, const int32_t* vel, const uint32_t* species, const uint32_t* ids,
+                         int64_t* opos, int32_t* ovel, uint32_t* ospecies) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     uint32_t id = ids[s];
     int64_t x[3];
     load_particle<D, false>(pos, nullptr, s, x);
     for (int a = 0; a < D; a++) {
-        opos[(size_t)D * id + a] = x[a];
+        opos[(size_t)D * id + a] = wrap(x[a], box[a]);
         ovel[(size_t)D * id + a] = vel[D * s + a];
     }
     ospecies[id] = species[s];
@@ -522,11 +526,12 @@ int upload_state(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const u
 
 int read_state_dev(gbmd_engine* e) {
     size_t n = e->n;
+    Box3 box{{e->P.box[0], e->P.box[1], e->P.box[2]}};
     if (e->D == 2)
-        k_to_ids<2><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, (const Rec<2>*)e->pos[e->cur], e->vel, e->species, e->ids,
+        k_to_ids<2><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, box, (const Rec<2>*)e->pos[e->cur], e->vel, e->species, e->ids,
                                                           (int64_t*)e->staging, e->staging_v, e->staging_s);
     else
-        k_to_ids<3><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, (const Rec<3>*)e->pos[e->cur], e->vel, e->species, e->ids,
+        k_to_ids<3><<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, box, (const Rec<3>*)e->pos[e->cur], e->vel, e->species, e->ids,
                                                           (int64_t*)e->staging, e->staging_v, e->staging_s);
     note_launch();
     GBMD_CUDA_TRY(cudaGetLastError());
@@ -560,6 +565,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     uint32_t nc[3];
     GBMD_TRY(cells_for(*sys, rc_max(*sys) + e->skin, nc));
     uint32_t cap = 0;
+    if (e->verlet && n >= (1u << 26)) return fail(GBMD_E_UNSUPPORTED, "Verlet lists hold at most 2^26 particles per engine");
     if (e->verlet) {
         // ForceMode::verlet_with_skin's sizing (engine.rs:130-141), without the 128 MiB clamp
         double r = rc_max(*sys) + e->skin, vol = 1.0;
@@ -759,6 +765,7 @@ int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential) {
 
 int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit) {
     if (!e || id >= e->n || axis >= (uint32_t)e->D || bit > 62) return fail(GBMD_E_INVALID, "bad flip_bit argument");
+    GBMD_TRY(prepare_pairs(e)); // wraps the positions into the box (they drift out between list builds)
     if (e->D == 2) k_flip<2><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->ids, id, axis, bit, (Rec<2>*)e->pos[e->cur]);
     else k_flip<3><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->ids, id, axis, bit, (Rec<3>*)e->pos[e->cur]);
     note_launch();
@@ -911,7 +918,7 @@ int gbmd_debug_list(gbmd_engine* e, uint32_t* counts, uint32_t* nbr, uint64_t nb
         size_t s = slot_of[id];
         counts[id] = cnt[s];
         if (off + cnt[s] > nbr_cap) return fail(GBMD_E_INVALID, "nbr_cap too small");
-        for (size_t q = 0; q < cnt[s]; q++) nbr[off++] = ids[lst[slot(s, q)]];
+        for (size_t q = 0; q < cnt[s]; q++) nbr[off++] = ids[lst[slot(s, q)] & ((1u << 26) - 1u)];
     }
     return GBMD_OK;
 }

@@ -51,6 +51,8 @@ template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t
     if (i >= P.n) return;
     int64_t x[3];
     load_particle<D, false>(pos, nullptr, i, x);
+#pragma unroll
+    for (int a = 0; a < D; a++) x[a] = wrap(x[a], P.box[a]);
     uint32_t c[3];
     keys[i] = cell_key<D>(P, x, c);
     vals[i] = i;
@@ -69,6 +71,11 @@ __global__ void k_gather(Params P, const uint32_t* items, const uint32_t* keys, 
     if (s >= P.n) return;
     uint32_t o = items[s];
     PosRec<D> r = pos[o];
+    {
+        long long* x = reinterpret_cast<long long*>(&r);
+#pragma unroll
+        for (int a = 0; a < D; a++) x[a] = wrap(x[a], P.box[a]);
+    }
     pos_o[s] = r;
     for (uint32_t a = 0; a < D; a++) vel_o[D * s + a] = vel[D * o + a];
     uint32_t sp = species[o];
@@ -108,13 +115,15 @@ __device__ __forceinline__ bool pair_kick(const G& P, const PairC& pc, float cs,
 
 // Leapfrog of one particle (int_engine.rs:265-339 / int_engine3.rs:147-179, periodic):
 // v += kick + g (wrapping i32), x += v (exact i64), wrap into [0, L).
-template <int D, class G>
+// With WRAP false the position is left unwrapped (the Verlet-list engine wraps at each list
+// build and on read-back: wrap(wrap(x) + v) = wrap(x + v) while x stays within a box length).
+template <int D, class G, bool WRAP = true>
 __device__ __forceinline__ void leapfrog(const G& P, uint32_t si, const int32_t* k, int32_t* v, int64_t* x) {
     bool pinned = (P.pinned >> si) & 1u;
 #pragma unroll
     for (int a = 0; a < D; a++) {
         v[a] = wadd(wadd(v[a], k[a]), pinned ? 0 : P.gravity[a]);
-        x[a] = wrap(x[a] + (int64_t)v[a], P.box[a]);
+        x[a] = WRAP ? wrap(x[a] + (int64_t)v[a], P.box[a]) : x[a] + (int64_t)v[a];
     }
 }
 
@@ -181,6 +190,16 @@ __device__ __forceinline__ void cell_coords(const Params& P, uint32_t key, uint3
     c[2] = key / (P.nc[0] * P.nc[1]);
 }
 
+// A list entry is the neighbour's slot in its low LIST_BITS bits and, above, the periodic
+// image the pair was found at (2 bits per axis: 1 for +L, 2 for -L), so that with positions left
+// unwrapped between list builds the separation is xj + image - xi exactly, with no minimum image.
+constexpr uint32_t LIST_BITS = 26;
+constexpr uint32_t LIST_MASK = (1u << LIST_BITS) - 1u;
+__device__ __forceinline__ uint32_t image_code(int64_t sx, int64_t sy, int64_t sz) {
+    uint32_t c = (sx > 0 ? 1u : sx < 0 ? 2u : 0u) | (sy > 0 ? 4u : sy < 0 ? 8u : 0u) | (sz > 0 ? 16u : sz < 0 ? 32u : 0u);
+    return c << LIST_BITS;
+}
+
 // Verlet lists are warp-tiled: the 32 particles of a warp (consecutive slots) store their
 // neighbours in groups of four, group g of lane l at ((w cap4 + 4 g) 32 + 4 l), so one 16-byte
 // load gives a thread four neighbours and a warp's load is 512 contiguous bytes. cap4 is the
@@ -205,6 +224,20 @@ template <int D> __device__ __forceinline__ uint4 quot_record(const int64_t* x, 
 }
 // sep_near from quotient records: trunc(d / 16) with d = 16 D + (rj - ri), 0 <= r < 16:
 // floor(d / 16) = D - (rj < ri), and trunc adds one back when d < 0 and rj != ri.
+// Shift a quotient record (X, R) by +L (c = 1) or -L (c = 2): x + L = 16 (X + (L >> 4)) + (R + (L & 15)),
+// carrying a sixteen out of R; x - L borrowing likewise.
+__device__ __forceinline__ void quot_shift(uint32_t c, int64_t L, uint32_t& X, uint32_t& R) {
+    const uint32_t XL = (uint32_t)(L >> 4), RL = (uint32_t)(L & 15);
+    if (c == 1u) {
+        uint32_t t = R + RL;
+        X += XL + (t >> 4);
+        R = t & 15u;
+    } else if (c == 2u) {
+        uint32_t t = R + 16u - RL;
+        X -= XL + (t < 16u ? 1u : 0u);
+        R = t & 15u;
+    }
+}
 __device__ __forceinline__ float quot_sep(uint32_t Xj, uint32_t rj, uint32_t Xi, uint32_t ri) {
     int32_t f = (int32_t)(Xj - Xi) - (rj < ri ? 1 : 0);
     int32_t q = f + ((f < 0 && rj != ri) ? 1 : 0);
@@ -271,6 +304,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                 int64_t sx = tx < 0 ? -P.box[0] : (tx >= (int)nx ? P.box[0] : 0);
                 uint32_t cell = (z * ny + y) * nx + x;
                 const int64_t xs[3] = {xi[0] - sx, xi[1] - sy, D == 3 ? xi[2] - sz : 0};
+                const uint32_t code = image_code(sx, sy, sz);
                 const float b0 = __fmul_rn(__ll2float_rn(((int64_t)x - (int64_t)c[0]) * P.cell_w[0] + sx - reli[0]), 1.0f / 4294967296.0f);
                 const float b1 = __fmul_rn(__ll2float_rn(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]), 1.0f / 4294967296.0f);
                 const float b2 = D == 3 ? __fmul_rn(__ll2float_rn(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]), 1.0f / 4294967296.0f) : 0.0f;
@@ -283,7 +317,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                     float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
                     bool in = r2a < lo || (r2a <= hi && exact(j, xs, sj));
                     if (in && j != i) {
-                        if (count < cap) nbr[list_slot(i, count, cap4)] = j;
+                        if (count < cap) nbr[list_slot(i, count, cap4)] = j | code;
                         count++;
                     }
                 }
@@ -322,11 +356,8 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
     const uint32_t m = __ldg(nbr_count + i), cap4 = (P.cap + 3u) & ~3u;
     const PairC pc0 = P.pc[0];
     const uint4* groups = reinterpret_cast<const uint4*>(nbr + list_slot(i, 0, cap4)); // group g at groups[32 g]
-    // A particle farther than `reach` from every face sees each listed neighbour at xj - xi
-    // without a periodic image, and within 8 sigma: no minimum image, no range check.
-    bool interior = true;
-#pragma unroll
-    for (int a = 0; a < D; a++) interior = interior && xi[a] >= P.reach && xi[a] < P.box[a] - P.reach;
+    // Every listed neighbour is within 8 sigma of xi at its recorded image (list radius + skin),
+    // so neither a minimum image nor a range check is needed.
     auto add_kick = [&](const float* f, const PairC& pc) {
         float fr, s6, r2;
         if (pair_fr<D>(pc, f, fr, s6, r2)) {
@@ -336,9 +367,10 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
         }
     };
     const uint32_t ngroups = (m + 3u) >> 2;
-    if (interior && D == 3) {
-        // 3D: neighbours come from the 16-byte quotient records (one gather each) and the
-        // separation is formed with 32-bit integers (quot_sep).
+    if constexpr (D == 3) {
+        // Neighbours come from the 16-byte quotient records (one gather each) and the separation
+        // is formed with 32-bit integers (quot_sep); a neighbour listed at a periodic image has
+        // its quotient record shifted by that image exactly (quot_shift).
         const uint4 qi = __ldg(qpos_in + i);
         const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
         for (uint32_t g = 0; g < ngroups; g++) {
@@ -348,14 +380,20 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
             const uint32_t left = m - 4 * g;
             uint4 r[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? jj[u] : i));
+            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? (jj[u] & LIST_MASK) : i));
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 if ((uint32_t)u >= left) break;
-                float f[D];
-                const uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
+                uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
+                uint32_t Rj[3] = {r[u].w & 15u, (r[u].w >> 8) & 15u, (r[u].w >> 16) & 15u};
+                const uint32_t code = jj[u] >> LIST_BITS;
+                if (code) {
 #pragma unroll
-                for (int a = 0; a < D; a++) f[a] = quot_sep(Xj[a], (r[u].w >> (8 * a)) & 15u, Xi[a], (qi.w >> (8 * a)) & 15u);
+                    for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
+                }
+                float f[D];
+#pragma unroll
+                for (int a = 0; a < D; a++) f[a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
                 add_kick(f, MULTI ? P.pc[si * P.ns + (r[u].w >> 24)] : pc0);
             }
         }
@@ -368,27 +406,26 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
             int64_t xj[4][3];
             uint32_t sj[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) sj[u] = load_particle<D, MULTI>(pos_in, species, (uint32_t)u < left ? jj[u] : i, xj[u]);
+            for (int u = 0; u < 4; u++) sj[u] = load_particle<D, MULTI>(pos_in, species, (uint32_t)u < left ? (jj[u] & LIST_MASK) : i, xj[u]);
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 if ((uint32_t)u >= left) break;
+                const uint32_t code = jj[u] >> LIST_BITS;
                 float f[D];
-                bool ok = true;
-                if (interior) {
 #pragma unroll
-                    for (int a = 0; a < D; a++) f[a] = sep_near(xj[u][a] - xi[a]);
-                } else {
-#pragma unroll
-                    for (int a = 0; a < D; a++) f[a] = sep_s(min_image(xj[u][a] - xi[a], P.box[a], P.half[a]), ok);
+                for (int a = 0; a < D; a++) {
+                    uint32_t c = (code >> (2 * a)) & 3u;
+                    int64_t img = c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0);
+                    f[a] = sep_near(xj[u][a] + img - xi[a]);
                 }
-                if (ok) add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
+                add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
             }
         }
     }
     int32_t v[3];
 #pragma unroll
     for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
-    leapfrog<D>(P, si, k, v, xi);
+    leapfrog<D, Params, false>(P, si, k, v, xi);
 #pragma unroll
     for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
     store_pos<D>(pos_out, i, xi, si);
@@ -467,7 +504,7 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
         if (nbr) {
             uint32_t m = nbr_count[i];
             const uint32_t cap4 = (P.cap + 3u) & ~3u;
-            for (uint32_t q = 0; q < m; q++) visit(nbr[list_slot(i, q, cap4)]);
+            for (uint32_t q = 0; q < m; q++) visit(nbr[list_slot(i, q, cap4)] & LIST_MASK);
         } else {
             uint32_t c[3];
             cell_coords(P, keys[i], c);
