@@ -482,6 +482,110 @@ def run_c3(args, world, rank, local, pg):
     return 0
 
 
+def _pct(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = min(len(xs) - 1, max(0, int(math.ceil(q / 100.0 * len(xs))) - 1))
+    return xs[k]
+
+
+def run_c5(args, world, rank, local, pg):
+    """configs[4]: a Poisson stream of 2D/3D requests (N log-uniform in [1024, 2^20], 2000 steps,
+    a frame of T, P and a 200-bin RDF every 100 steps) served under a 64 GB HBM budget, against
+    the same requests run one after another in plain form. Per-frame latency: the wall time a
+    client waits for each frame after the previous one of its request (after submission for the
+    first)."""
+    import torch
+
+    from micrographia_gb300 import ForceMode, GpuEngine, GpuEngine3, Server, workloads
+
+    torch.cuda.set_device(local)
+    reqs = workloads.config5(args.requests, args.rate)
+    steps = args.steps
+
+    def serve():
+        frames_lat, done, t_arr, t_prev = [], 0, {}, {}
+        sv = Server(64 << 30, max_active=64, device=local)
+        t0 = time.perf_counter()
+        pending = list(reqs)
+        total = 0
+        while done < len(reqs):
+            now = time.perf_counter() - t0
+            while pending and pending[0][0] <= now:
+                _, s, spec = pending.pop(0)
+                rid = sv.submit(s, spec, steps=steps, frame_every=100, rdf_bins=200, rdf_rmax=5.0)
+                t_arr[rid] = time.perf_counter() - t0
+                t_prev[rid] = t_arr[rid]
+                total += spec.n * steps
+            got = sv.poll()
+            tnow = time.perf_counter() - t0
+            for f in got:
+                frames_lat.append(tnow - t_prev[f.request])
+                t_prev[f.request] = tnow
+                if f.last:
+                    done += 1
+            if not got:
+                time.sleep(0.0002)
+        makespan = time.perf_counter() - t0
+        sv.close()
+        return total / makespan, makespan, frames_lat
+
+    def serial():
+        frames_lat = []
+        t0 = time.perf_counter()
+        total = 0
+        for t_a, s, spec in reqs:
+            while time.perf_counter() - t0 < t_a:
+                time.sleep(0.0005)
+            t_prev = t0 + t_a  # the first frame's wait counts from the request's arrival
+            cls = GpuEngine if s.DIM == 2 else GpuEngine3
+            e = cls(s, None, ForceMode.verlet_with_skin(s, spec.n, SKIN), init=spec, block_steps=100, device=local)
+            for _ in range(0, steps, 100):
+                e.step(100)
+                e.observe(rdf_bins=200, rdf_rmax=5.0)
+                t = time.perf_counter()
+                frames_lat.append(t - t_prev)
+                t_prev = t
+            e.close()
+            total += spec.n * steps
+        makespan = time.perf_counter() - t0
+        return total / makespan, makespan, frames_lat
+
+    v_serve, mk_serve, lat_serve = serve()
+    v_serial, mk_serial, lat_serial = serial()
+    line = {
+        "metric": METRIC,
+        "value": v_serve,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": None,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+int64",
+        "data": "synthetic",
+        "config": {
+            "workload": f"{len(reqs)} requests, Poisson arrivals at {args.rate}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget (configs[4])",
+            "form": "served: continuous batching (each admitted request on its own stream, intervals overlapped)",
+            "makespan_s": mk_serve,
+            "frame_latency_p50_ms": 1e3 * _pct(lat_serve, 50),
+            "frame_latency_p99_ms": 1e3 * _pct(lat_serve, 99),
+            "plain_value": v_serial,
+            "plain_makespan_s": mk_serial,
+            "plain_frame_latency_p50_ms": 1e3 * _pct(lat_serial, 50),
+            "plain_frame_latency_p99_ms": 1e3 * _pct(lat_serial, 99),
+            "served_over_plain": v_serve / v_serial,
+            "frames": len(lat_serve),
+        },
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     global N_ATOMS
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
@@ -491,7 +595,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="atoms (default 1,048,576; smaller only for profiling)")
-    ap.add_argument("--config", choices=["c2", "c3", "c4"], default="c2", help="c2 (default): 3D N=1M; c3: 2D slab 16.7M; c4: 1024 replicas")
+    ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2", help="c2 (default): 3D N=1M; c3: 2D slab 16.7M; c4: 1024 replicas; c5: served stream")
+    ap.add_argument("--requests", type=int, default=48, help="requests for --config c5")
+    ap.add_argument("--rate", type=float, default=8.0, help="Poisson arrival rate (1/s) for --config c5")
     ap.add_argument("--systems", type=int, default=1024, help="replicas for --config c4")
     args = ap.parse_args()
     N_ATOMS = args.atoms
@@ -506,6 +612,8 @@ def main():
         build.build()
         if args.config == "c4":
             rc = run_c4(args, world, rank, local, pg)
+        elif args.config == "c5":
+            rc = run_c5(args, world, rank, local, pg)
         elif args.config == "c3":
             rc = run_c3(args, world, rank, local, pg)
         else:

@@ -251,6 +251,61 @@ int gbmd_batch_destroy(gbmd_batch* b);
  * dim 2, State3::hash (three.rs:281-297) for dim 3. */
 uint64_t gbmd_hash_state(uint32_t dim, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint32_t n);
 
+/* ---- Serving: requests admitted against an HBM budget, stepped concurrently, frames streamed ---- */
+
+#define GBMD_SERVE_RDF_BINS 256
+
+/* One simulation request: a periodic system, its seeded initial state, how many steps, a frame
+ * of observables every `frame_every` steps (and after the last), with an RDF of `rdf_bins` bins
+ * to `rdf_rmax` (0 bins: none), Verlet skin `skin` (<= 0: 0.3). */
+typedef struct gbmd_serve_request {
+    gbmd_system sys;
+    gbmd_init init;
+    uint64_t steps;
+    uint32_t frame_every;
+    uint32_t rdf_bins;
+    double rdf_rmax;
+    double skin;
+} gbmd_serve_request;
+
+/* A frame delivered to the client. `ready_ns` is when the server had it, in ns since the server
+ * was created; on the request's last frame `last` is 1 and `state_hash` the FNV-1a hash of its
+ * final id-ordered state. */
+typedef struct gbmd_serve_frame {
+    uint64_t request;
+    gbmd_frame frame;
+    uint64_t ready_ns;
+    uint32_t index;
+    uint32_t last;
+    uint64_t state_hash;
+    uint64_t rdf[GBMD_SERVE_RDF_BINS];
+} gbmd_serve_frame;
+
+typedef struct gbmd_serve_stats_t {
+    uint32_t pending;
+    uint32_t active;
+    uint64_t admitted;
+    uint64_t completed;
+    uint64_t bytes_in_use;
+    uint64_t budget;
+    uint64_t atom_steps;
+} gbmd_serve_stats_t;
+
+typedef struct gbmd_server gbmd_server;
+
+/* A server on `device` holding at most `max_active` requests (0: 64) within `hbm_budget_bytes`
+ * of device memory. Requests are admitted first come, first served as memory and slots free up. */
+int gbmd_serve_create(uint64_t hbm_budget_bytes, uint32_t max_active, int32_t device, gbmd_server** out);
+int gbmd_serve_submit(gbmd_server* sv, const gbmd_serve_request* req, uint64_t* request_id);
+/* Drive the loop once without blocking on the GPU: collect finished frame intervals, enqueue the
+ * next ones, admit waiting requests, and copy out up to `cap` frames. */
+int gbmd_serve_poll(gbmd_server* sv, gbmd_serve_frame* frames, uint32_t cap, uint32_t* count);
+int gbmd_serve_cancel(gbmd_server* sv, uint64_t request_id);
+int gbmd_serve_stats(gbmd_server* sv, gbmd_serve_stats_t* stats);
+int gbmd_serve_destroy(gbmd_server* sv);
+/* Device bytes a request of this size is charged against the budget. */
+uint64_t gbmd_serve_estimate_bytes(const gbmd_system* sys, uint32_t n, double skin);
+
 /* ---- Thread-local error message ---- */
 
 const char* gbmd_last_error(void);

@@ -25,7 +25,7 @@ from .core import (
     to_f64,
     to_fixed,
 )
-from .engine import BatchEngine, GpuEngine, GpuEngine3, init_state
+from .engine import BatchEngine, GpuEngine, GpuEngine3, Server, init_state
 from . import init, workloads
 
 __all__ = [
@@ -40,6 +40,7 @@ __all__ = [
     "GpuEngine",
     "GpuEngine3",
     "BatchEngine",
+    "Server",
     "box_for",
     "cube_for",
     "fcc_cells",

@@ -107,6 +107,9 @@ class gbmd_serve_request(C.Structure):
     ]
 
 
+SERVE_RDF_BINS = 256
+
+
 class gbmd_serve_frame(C.Structure):
     _fields_ = [
         ("request", C.c_uint64),
@@ -114,6 +117,20 @@ class gbmd_serve_frame(C.Structure):
         ("ready_ns", C.c_uint64),
         ("index", C.c_uint32),
         ("last", C.c_uint32),
+        ("state_hash", C.c_uint64),
+        ("rdf", C.c_uint64 * SERVE_RDF_BINS),
+    ]
+
+
+class gbmd_serve_stats_t(C.Structure):
+    _fields_ = [
+        ("pending", C.c_uint32),
+        ("active", C.c_uint32),
+        ("admitted", C.c_uint64),
+        ("completed", C.c_uint64),
+        ("bytes_in_use", C.c_uint64),
+        ("budget", C.c_uint64),
+        ("atom_steps", C.c_uint64),
     ]
 
 
@@ -156,6 +173,13 @@ SIGNATURES = [
     ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
     ("gbmd_batch_stats", C.c_int, [VP, _U64P, _U32P]),
     ("gbmd_batch_destroy", C.c_int, [VP]),
+    ("gbmd_serve_create", C.c_int, [C.c_uint64, C.c_uint32, C.c_int32, P(VP)]),
+    ("gbmd_serve_submit", C.c_int, [VP, P(gbmd_serve_request), _U64P]),
+    ("gbmd_serve_poll", C.c_int, [VP, P(gbmd_serve_frame), C.c_uint32, _U32P]),
+    ("gbmd_serve_cancel", C.c_int, [VP, C.c_uint64]),
+    ("gbmd_serve_stats", C.c_int, [VP, P(gbmd_serve_stats_t)]),
+    ("gbmd_serve_destroy", C.c_int, [VP]),
+    ("gbmd_serve_estimate_bytes", C.c_uint64, [P(gbmd_system), C.c_uint32, C.c_double]),
     ("gbmd_hash_state", C.c_uint64, [C.c_uint32, _I64P, _I32P, _U32P, C.c_uint32]),
     ("gbmd_last_error", C.c_char_p, []),
     ("gbmd_version", C.c_char_p, []),

@@ -212,6 +212,11 @@ struct gbmd_engine {
     uint64_t launches = 0;
     uint32_t last_rebuilds = 0;
     bool failed = false;
+    // observation scratch, kept between frames (freeing it would synchronise the whole device)
+    unsigned long long* obs_bins = nullptr;
+    size_t obs_bins_cap = 0;
+    uint32_t* obs_start = nullptr;
+    size_t obs_start_cap = 0;
 };
 
 namespace {
@@ -232,7 +237,8 @@ void free_all(gbmd_engine* e) {
             if (e->exec[p][b]) cudaGraphExecDestroy(e->exec[p][b]);
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
-                    e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1]};
+                    e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1],
+                    e->obs_bins, e->obs_start};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (e->st) cudaStreamDestroy(e->st);
@@ -965,13 +971,44 @@ __global__ void k_rdf(Params P, const Rec<D>* pos, const uint32_t* keys, const u
         if (h[b]) atomicAdd(out + b, (unsigned long long)h[b]);
 }
 
-// Particle counts in slabs along one axis: min(floor(x / L * bins), bins - 1) in f64.
+// The same counts over every unordered pair, for boxes narrower than three cells of side rmax on
+// some axis (small systems only). Positions are wrapped first: between list builds they may lie
+// up to the skin outside [0, L).
 template <int D>
-__global__ void k_profile(uint32_t n, const Rec<D>* pos, uint32_t axis, double l, uint32_t bins, unsigned long long* out) {
+__global__ void k_rdf_all(Params P, const Rec<D>* pos, uint32_t bins, double scale, unsigned long long* out) {
+    extern __shared__ uint32_t h[];
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.n) {
+        int64_t xi[3];
+        load_particle<D, false>(pos, nullptr, i, xi);
+        for (int a = 0; a < D; a++) xi[a] = wrap(xi[a], P.box[a]);
+        for (uint32_t j = i + 1; j < P.n; j++) {
+            int64_t xj[3];
+            load_particle<D, false>(pos, nullptr, j, xj);
+            double r2 = 0.0;
+            for (int a = 0; a < D; a++) {
+                double d = to_f64(min_image(wrap(xj[a], P.box[a]) - xi[a], P.box[a], P.half[a]));
+                r2 = __dadd_rn(r2, __dmul_rn(d, d));
+            }
+            double r = __dmul_rn(__dsqrt_rn(r2), scale);
+            if (r < (double)bins) atomicAdd(&h[(uint32_t)r], 1u);
+        }
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x)
+        if (h[b]) atomicAdd(out + b, (unsigned long long)h[b]);
+}
+
+// Particle counts in slabs along one axis: min(floor(x / L * bins), bins - 1) in f64.
+// Positions are wrapped first (between list builds they may lie up to the skin outside [0, L)).
+template <int D>
+__global__ void k_profile(uint32_t n, const Rec<D>* pos, uint32_t axis, int64_t lfix, double l, uint32_t bins, unsigned long long* out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const long long* p = reinterpret_cast<const long long*>(pos + i);
-    atomicAdd(out + cell_of(p[axis], l, bins), 1ull);
+    atomicAdd(out + cell_of(wrap(p[axis], lfix), l, bins), 1ull);
 }
 
 } // namespace
@@ -986,25 +1023,50 @@ extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, ui
     uint32_t n = e->n, nb = blocks_for(n, 128);
     std::vector<double> part(4 * (size_t)nb);
     GBMD_CUDA_TRY(cudaMemcpyAsync(part.data(), e->partial, part.size() * 8, cudaMemcpyDeviceToHost, e->st));
-    unsigned long long* dbuf = nullptr;
-    uint32_t* st2 = nullptr;
     size_t nbins = (rdf ? rdf_bins : 0) + (profile ? profile_bins : 0);
-    if (nbins) {
-        GBMD_CUDA_TRY(cudaMalloc(&dbuf, nbins * 8));
-        GBMD_CUDA_TRY(cudaMemsetAsync(dbuf, 0, nbins * 8, e->st));
+    if (nbins > e->obs_bins_cap) {
+        if (e->obs_bins) GBMD_CUDA_TRY(cudaFree(e->obs_bins));
+        e->obs_bins = nullptr;
+        e->obs_bins_cap = 0;
+        if (cudaMalloc(&e->obs_bins, nbins * 8) != cudaSuccess) return fail(GBMD_E_NOMEM, "observation bins");
+        e->obs_bins_cap = nbins;
     }
+    unsigned long long* dbuf = e->obs_bins;
+    if (nbins) GBMD_CUDA_TRY(cudaMemsetAsync(dbuf, 0, nbins * 8, e->st));
     int rc = GBMD_OK;
+    bool rdf_cells = true;
     if (rdf) {
+        double bmax = 0.0;
+        for (int a = 0; a < e->D; a++) bmax = std::max(bmax, to_f64h(e->sys.box_len[a]));
+        for (int a = 0; a < e->D; a++)
+            if (std::floor(to_f64h(e->sys.box_len[a]) / (rdf_rmax + 1e-3 + 1e-6 * bmax)) < 3.0) rdf_cells = false;
+    }
+    if (rdf && !rdf_cells) {
+        double scale = (double)rdf_bins / rdf_rmax;
+        size_t shm = (size_t)rdf_bins * 4;
+        if (e->D == 2)
+            k_rdf_all<2><<<blocks_for(n, 128), 128, shm, e->st>>>(e->P, (const Rec<2>*)e->pos[e->cur], rdf_bins, scale, dbuf);
+        else
+            k_rdf_all<3><<<blocks_for(n, 128), 128, shm, e->st>>>(e->P, (const Rec<3>*)e->pos[e->cur], rdf_bins, scale, dbuf);
+        note_launch();
+    } else if (rdf) {
         Params P = e->P;
         uint32_t nc[3];
         rc = cells_for(e->sys, rdf_rmax, nc);
         if (rc == GBMD_OK) {
             set_cells(P, nc, (uint32_t)e->D);
-            if (cudaMalloc(&st2, ((size_t)P.ncell + 1) * 4) != cudaSuccess) rc = fail(GBMD_E_NOMEM, "RDF cell starts");
+            size_t need = (size_t)P.ncell + 1;
+            if (need > e->obs_start_cap) {
+                if (e->obs_start) cudaFree(e->obs_start);
+                e->obs_start = nullptr;
+                e->obs_start_cap = 0;
+                if (cudaMalloc(&e->obs_start, need * 4) != cudaSuccess) rc = fail(GBMD_E_NOMEM, "RDF cell starts");
+                else e->obs_start_cap = need;
+            }
         }
         if (rc == GBMD_OK) {
             uint32_t* saved = e->start;
-            e->start = st2;
+            e->start = e->obs_start;
             double scale = (double)rdf_bins / rdf_rmax;
             size_t shm = (size_t)rdf_bins * 4;
             if (e->D == 2) {
@@ -1021,24 +1083,23 @@ extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, ui
     if (rc == GBMD_OK && profile) {
         unsigned long long* pbuf = dbuf + (rdf ? rdf_bins : 0);
         double l = to_f64h(e->sys.box_len[profile_axis]);
-        if (e->D == 2) k_profile<2><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], profile_axis, l, profile_bins, pbuf);
-        else k_profile<3><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<3>*)e->pos[e->cur], profile_axis, l, profile_bins, pbuf);
+        int64_t lfix = e->P.box[profile_axis];
+        if (e->D == 2) k_profile<2><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
+        else k_profile<3><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<3>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
         note_launch();
     }
     std::vector<uint64_t> hbuf(nbins);
     if (rc == GBMD_OK && nbins) GBMD_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), dbuf, nbins * 8, cudaMemcpyDeviceToHost, e->st));
     cudaError_t err = cudaStreamSynchronize(e->st);
-    if (dbuf) cudaFree(dbuf);
-    if (st2) cudaFree(st2);
     if (rc != GBMD_OK) return rc;
     if (err != cudaSuccess) return fail(GBMD_E_CUDA, cudaGetErrorString(err));
     GBMD_TRY(check_ctl(e));
     if (rdf) std::memcpy(rdf, hbuf.data(), (size_t)rdf_bins * 8);
     if (profile) std::memcpy(profile, hbuf.data() + (rdf ? rdf_bins : 0), (size_t)profile_bins * 8);
-    if (rdf) {
+    if (rdf && rdf_cells) {
         // the RDF binning left the scratch state sorted by its own cells: rebuild before use
         uint32_t one = 1;
-        GBMD_CUDA_TRY(cudaMemcpy(e->ctl, &one, 4, cudaMemcpyHostToDevice));
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
     }
     if (frame) {
         double pe = 0.0, w = 0.0, ke = 0.0;

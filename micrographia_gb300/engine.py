@@ -326,3 +326,65 @@ class BatchEngine:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """The serving loop (gbmd_serve_*): submit requests, poll frames."""
+
+    def __init__(self, hbm_budget_bytes, max_active=64, device=0):
+        self._lib = _abi.lib()
+        h = C.c_void_p()
+        _abi.check(self._lib.gbmd_serve_create(int(hbm_budget_bytes), max_active, device, C.byref(h)))
+        self._h = h
+        self._buf = (_abi.gbmd_serve_frame * 64)()
+
+    def submit(self, sys, init, steps, frame_every=100, rdf_bins=200, rdf_rmax=5.0, skin=0.3):
+        r = _abi.gbmd_serve_request()
+        r.sys = sys.to_c()
+        r.init = init
+        r.steps = steps
+        r.frame_every = frame_every
+        r.rdf_bins = rdf_bins
+        r.rdf_rmax = rdf_rmax
+        r.skin = skin
+        rid = C.c_uint64()
+        _abi.check(self._lib.gbmd_serve_submit(self._h, C.byref(r), C.byref(rid)))
+        return rid.value
+
+    def poll(self):
+        """Frames delivered since the last poll (copies)."""
+        out = []
+        while True:
+            cnt = C.c_uint32()
+            _abi.check(self._lib.gbmd_serve_poll(self._h, self._buf, len(self._buf), C.byref(cnt)))
+            for k in range(cnt.value):
+                f = _abi.gbmd_serve_frame()
+                C.pointer(f)[0] = self._buf[k]
+                out.append(f)
+            if cnt.value < len(self._buf):
+                return out
+
+    def cancel(self, rid):
+        _abi.check(self._lib.gbmd_serve_cancel(self._h, rid))
+
+    def stats(self):
+        st = _abi.gbmd_serve_stats_t()
+        _abi.check(self._lib.gbmd_serve_stats(self._h, C.byref(st)))
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gbmd_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

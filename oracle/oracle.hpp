@@ -1239,6 +1239,26 @@ inline std::vector<uint64_t> rdf_counts(const System& sys, const State& s, uint3
     int d = sys.dim;
     std::vector<uint64_t> h(bins, 0);
     double scale = (double)bins / rmax;
+    bool fits = true;
+    {
+        double bmax = 0.0;
+        for (int a = 0; a < d; a++) bmax = std::max(bmax, sys.box_f64(a));
+        for (int a = 0; a < d; a++)
+            if (std::floor(sys.box_f64(a) / (rmax + 1e-3 + 1e-6 * bmax)) < 3.0) fits = false;
+    }
+    if (!fits) { // fewer than three cells of side rmax on an axis: every unordered pair once
+        for (size_t i = 0; i < s.n(); i++)
+            for (size_t j = i + 1; j < s.n(); j++) {
+                double r2 = 0.0;
+                for (int a = 0; a < d; a++) {
+                    double dd = to_f64(min_image(s.pos[d * i + a], s.pos[d * j + a], sys.box[a]));
+                    r2 = r2 + dd * dd;
+                }
+                double r = std::sqrt(r2) * scale;
+                if (r < (double)bins) h[(uint32_t)r]++;
+            }
+        return h;
+    }
     auto dims = sys.cells_for(rmax);
     CellList cl = build_cells(sys, s, dims);
     uint32_t nc[3] = {dims[0], dims[1], d == 3 ? dims[2] : 1u};

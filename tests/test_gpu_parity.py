@@ -351,6 +351,37 @@ def test_frame_3d(O):
     assert np.array_equal(rdf, O.rdf(sys3, s, 200, 5.0))
 
 
+def test_frame_between_list_builds(O):
+    """Frames taken mid-way between list builds, when positions may sit outside [0, L) by up to
+    the skin, count the same RDF and profile as the oracle on the wrapped state."""
+    sys_, s = equilibrated(O, 3000, 0.7, Pair.lj(2.5), 4)
+    with GpuEngine(sys_, s, ForceMode.verlet_with_skin(sys_, 3000, 0.5)) as g:
+        for k in range(4):
+            g.step(3)
+            _, rdf, prof = g.observe(rdf_bins=128, rdf_rmax=4.0, profile_bins=50, profile_axis=1)
+            st = g.read_state()
+            assert np.array_equal(rdf, O.rdf(sys_, st, 128, 4.0))
+            assert np.array_equal(prof, O.profile(sys_, st, 50, 1))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_rdf_small_box_all_pairs(O, dim):
+    """An RDF range wider than a third of the box counts every pair once (no cell list)."""
+    if dim == 3:
+        sys_, s = liquid3(O, 1000, 0.8, 1.0)
+        eng = GpuEngine3
+    else:
+        sys_, s = equilibrated(O, 200, 0.7, Pair.lj(2.5), 4)
+        eng = GpuEngine
+    with eng(sys_, s) as g:
+        g.step(5)
+        _, rdf, _ = g.observe(rdf_bins=100, rdf_rmax=6.0)
+        st = g.read_state()
+    ref = O.rdf(sys_, st, 100, 6.0)
+    assert np.array_equal(rdf, ref)
+    assert ref.sum() > 0
+
+
 # ---------------------------------------------------------------- velocity-rescale thermostat (configs[2])
 def test_rescale_thermostat_matches_oracle(O):
     """Slab start, rescale to T = 0.45 every 10 steps: the GPU trajectory equals the oracle's
@@ -426,3 +457,69 @@ def test_batch_3d(O):
             c = O.IntEngine(systems[k], states[k])
             c.step(60)
             assert b.read_system(k) == c.state
+
+
+# ---------------------------------------------------------------- serving (configs[4])
+def _drain(sv, want_last, limit_s=120.0):
+    import time
+
+    frames, last = [], {}
+    t0 = time.time()
+    while len(last) < want_last:
+        for f in sv.poll():
+            frames.append(f)
+            if f.last:
+                last[f.request] = f
+        if time.time() - t0 > limit_s:
+            raise AssertionError("serving loop did not finish in time")
+        time.sleep(0.001)
+    return frames, last
+
+
+def test_served_results_equal_solo_runs():
+    """Mixed 2D/3D requests, more than the server holds at once: each request's frames and final
+    state are bit-identical to the same request run alone."""
+    from micrographia_gb300 import Server, workloads
+
+    cfg = workloads.config5(count=6, rate=1e9, base_seed=3, n_min=800, n_max=6000)
+    with Server(hbm_budget_bytes=4 << 30, max_active=3) as sv:
+        ids = [sv.submit(s, spec, steps=300, frame_every=100, rdf_bins=64, rdf_rmax=4.0) for _, s, spec in cfg]
+        frames, last = _drain(sv, len(ids))
+    by_req = {}
+    for f in frames:
+        by_req.setdefault(f.request, []).append(f)
+    for rid, (_, s, spec) in zip(ids, cfg):
+        cls = GpuEngine if s.DIM == 2 else GpuEngine3
+        with cls(s, None, ForceMode.verlet_with_skin(s, spec.n, 0.3), init=spec, block_steps=100) as g:
+            solo = []
+            for _ in range(3):
+                g.step(100)
+                f, rdf, _ = g.observe(rdf_bins=64, rdf_rmax=4.0)
+                solo.append((f.kinetic, f.potential, f.virial, list(rdf)))
+            h = g.state_hash()
+        served = [(f.frame.kinetic, f.frame.potential, f.frame.virial, list(f.rdf[:64])) for f in sorted(by_req[rid], key=lambda f: f.index)]
+        assert served == solo
+        assert last[rid].state_hash == h
+
+
+def test_server_budget_and_cancel():
+    from micrographia_gb300 import Server, _abi, workloads
+
+    cfg = workloads.config5(count=3, rate=1e9, base_seed=9, n_min=1024, n_max=2048)
+    need = max(_abi.lib().gbmd_serve_estimate_bytes(__import__("ctypes").byref(s.to_c()), spec.n, 0.3) for _, s, spec in cfg)
+    # room for one request at a time: the others wait and are admitted as memory frees up
+    with Server(hbm_budget_bytes=need + need // 2, max_active=8) as sv:
+        ids = [sv.submit(s, spec, steps=200, frame_every=100, rdf_bins=0) for _, s, spec in cfg]
+        sv.poll()
+        assert sv.stats().active == 1
+        sv.cancel(ids[2])
+        frames, last = _drain(sv, 2)
+        assert set(last) == set(ids[:2])
+        assert sv.stats().completed == 2
+    # a request larger than the whole budget is refused with a budget error
+    with Server(hbm_budget_bytes=1 << 20) as sv:
+        _, s, spec = cfg[0]
+        sv.submit(s, spec, steps=10)
+        with pytest.raises(_abi.GbmdError) as ei:
+            sv.poll()
+        assert ei.value.code == _abi.E_BUDGET

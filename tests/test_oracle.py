@@ -288,3 +288,32 @@ def test_rescale_thermostat_is_exact(O):
     s2 = type(s)(s.pos, vel, s.species)
     t = O.exact_kinetic(sys_, s2) / (s.n() - 1)
     assert abs(t - 0.45) < 1e-3
+
+
+def _rdf_brute(sys_, st, bins, rmax):
+    """Every unordered pair's exact minimum-image separation, binned as floor(r * bins / rmax)."""
+    d = sys_.DIM
+    pos = st.pos.reshape(-1, d).astype(np.int64)
+    box = np.array(sys_.box_len, np.int64)
+    half = box // 2
+    r2 = np.zeros((len(pos), len(pos)))
+    for a in range(d):
+        dd = pos[None, :, a] - pos[:, None, a]
+        dd = np.where(dd >= half[a], dd - box[a], np.where(dd < -half[a], dd + box[a], dd))
+        f = dd.astype(np.float64) * (1.0 / ONE)
+        r2 = r2 + f * f
+    r = np.sqrt(r2) * (bins / rmax)
+    iu = np.triu_indices(len(pos), 1)
+    r = r[iu]
+    r = r[r < bins]
+    return np.bincount(r.astype(np.int64), minlength=bins).astype(np.uint64)
+
+
+@pytest.mark.parametrize("rmax", [4.0, 7.0])
+def test_rdf_counts_every_pair_once(O, rmax):
+    """Cell-list RDF (range under a third of the box) and the all-pairs form for a wider range
+    both equal a brute-force count."""
+    sys_ = System(box_for(200, 0.5, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    st = O.fluid(sys_, 200, 1.0, 9)
+    assert (sys_.box_f64()[0] / rmax >= 3) == (rmax == 4.0)
+    assert np.array_equal(O.rdf(sys_, st, 90, rmax), _rdf_brute(sys_, st, 90, rmax))
