@@ -294,6 +294,15 @@ def run_ours(args, world, rank, local, pg):
         "what": "gbmd_upload (pinned host state) + gbmd_step(K) + gbmd_read_state to host, per K steps",
     }
 
+    # FP64 force error at full size (outside the timed regions): the f32 path's integer kicks
+    # against the kicks of the same pair chain evaluated in f64 (IntEngine<f64>), relative RMS
+    # as md-ref's physics test defines it (bar 1e-5)
+    k32, _ = eng.kicks()
+    k64, _ = eng.kicks_f64()
+    d = k32.astype(np.float64) - k64.astype(np.float64)
+    fp64_err = float(np.sqrt((d * d).sum() / (k64.astype(np.float64) ** 2).sum()))
+    fp64_max = int(np.abs(d).max())
+
     line = {
         "metric": METRIC,
         "value": value,
@@ -325,6 +334,8 @@ def run_ours(args, world, rank, local, pg):
         },
         "phases": {"force_ms": f_ms.value, "rebuild_ms": r_ms.value, "rebuilds_in_200": nreb.value, "rebuilds_timed_run": rebuilds},
         "energy": {"e0_per_atom": (ke0 + pe0) / N_ATOMS, "drift_per_atom_per_step": (e_end - e_warm) / N_ATOMS / args.steps},
+        "fp64_force_error": {"rel_rms": fp64_err, "max_abs_kick_diff": fp64_max, "bar": 1e-5, "n_atoms": N_ATOMS,
+                             "reference": "kicks of the f64 pair chain (IntEngine<f64>) on the device, gbmd_kicks_f64"},
         "overflow": overflow,
     }
     if clk:

@@ -135,6 +135,9 @@ int gbmd_read_state(gbmd_engine* e, int64_t* pos, int32_t* vel, uint32_t* specie
 int gbmd_upload(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const uint32_t* species);
 /* Integer kicks at the current positions and the pair potential energy (engine.rs:1089-1097). */
 int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential);
+/* The same kicks with the pair chain in f64 (IntEngine<f64>::forces, int_engine.rs:130-251 with
+ * F = f64): the accuracy reference of the f32 path, computed on the device at full size. */
+int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential);
 /* Flip one bit of one coordinate of particle `id` (engine.rs:964, State::flip_bit). */
 int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit);
 
@@ -250,6 +253,14 @@ int gbmd_batch_destroy(gbmd_batch* b);
 /* FNV-1a hash of an id-ordered state held on the host: State::hash (system.rs:460-477) for
  * dim 2, State3::hash (three.rs:281-297) for dim 3. */
 uint64_t gbmd_hash_state(uint32_t dim, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint32_t n);
+
+/* Self-check of the pair arithmetic on `device`: the engine's own correctly rounded reciprocal
+ * and division, used by the pair force for separations above sigma / 8, compared bit for bit
+ * with CUDA's __frcp_rn / __fdiv_rn over every f32 of the reciprocal's range [2^50, 2^63), every
+ * f32 r2 of each pair type's fast range through the whole LJ chain (PairConsts::eval,
+ * crates/md-ref/src/real.rs:125-139), and `random_quotients` seeded random quotients. `checked`
+ * receives the number of cases, `mismatched` those that differ (0 when the arithmetic holds). */
+int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quotients, int32_t device, uint64_t* checked, uint64_t* mismatched);
 
 /* ---- Serving: requests admitted against an HBM budget, stepped concurrently, frames streamed ---- */
 

@@ -152,6 +152,7 @@ SIGNATURES = [
     ("gbmd_read_state", C.c_int, [VP, _I64P, _I32P, _U32P]),
     ("gbmd_upload", C.c_int, [VP, _I64P, _I32P, _U32P]),
     ("gbmd_kicks", C.c_int, [VP, _I32P, _DP]),
+    ("gbmd_kicks_f64", C.c_int, [VP, _I32P, _DP]),
     ("gbmd_flip_bit", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32]),
     ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
     ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),
@@ -181,6 +182,7 @@ SIGNATURES = [
     ("gbmd_serve_destroy", C.c_int, [VP]),
     ("gbmd_serve_estimate_bytes", C.c_uint64, [P(gbmd_system), C.c_uint32, C.c_double]),
     ("gbmd_hash_state", C.c_uint64, [C.c_uint32, _I64P, _I32P, _U32P, C.c_uint32]),
+    ("gbmd_check_pair_math", C.c_int, [P(gbmd_system), C.c_uint64, C.c_int32, P(C.c_uint64), P(C.c_uint64)]),
     ("gbmd_last_error", C.c_char_p, []),
     ("gbmd_version", C.c_char_p, []),
 ]

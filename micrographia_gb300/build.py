@@ -18,7 +18,7 @@ LIB = os.path.join(OUT, "libgbmd.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xcudafe", "--diag_suppress=177"]
-UNITS = ["engine.cu", "sort.cu", "init.cu", "batch.cu", "noalloc.cu", "serve.cu"]
+UNITS = ["engine.cu", "sort.cu", "init.cu", "batch.cu", "noalloc.cu", "serve.cu", "selfcheck.cu"]
 
 
 def _deps():

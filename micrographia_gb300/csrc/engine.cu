@@ -83,6 +83,21 @@ static double pair_shift(const gbmd_pair& p) {
 }
 static float scale2(float v, int e) { return std::ldexp(v, e); }
 
+// Lower end of the scaled r2 range in which the pair chain uses rcp_cr / div_cr: 2^50 (r of
+// 1/8 sigma) when, over [2^50, rc2s), t = c6 s6 (2 s6 - 1) stays below 2^100 in magnitude and its
+// non-zero values above 2^-60 (so t / r2 is a normal f32), else +inf (library division only).
+// Non-zero |2 s6 - 1| is at least 2^-24 (an f32 difference near 1), so |t| >= c6 s6min 2^-25.
+float fast_pair_lo(const PairC& c) {
+    const float lo = 0x1p50f;
+    if (!(c.eps4 > 0.0f) || !(c.sigma2s > 0.0f) || !(c.rc2s > lo) || !(c.rc2s <= 0x1p62f)) return INFINITY;
+    double s2max = (double)c.sigma2s / (double)lo, s2min = (double)c.sigma2s / (double)c.rc2s;
+    double s6max = s2max * s2max * s2max * 1.01, s6min = s2min * s2min * s2min * 0.99;
+    double tmax = (double)c.c6 * s6max * (2.0 * s6max + 1.0);
+    double tmin = (double)c.c6 * std::min(s6min, 0.5) * 0x1p-25;
+    if (!(tmax < 0x1p100) || !(tmin > 0x1p-60)) return INFINITY;
+    return lo;
+}
+
 void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint32_t cap, const uint32_t* nc) {
     std::memset(&P, 0, sizeof(P));
     P.n = n;
@@ -125,6 +140,7 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
             c.list2s = scale2((float)(lr * lr), 56);
             c.list2lo = (float)(lr * lr * (1.0 - 1e-4));
             c.list2hi = (float)(lr * lr * (1.0 + 1e-4));
+            c.fast_lo = fast_pair_lo(c);
         }
     // Listed pairs: within the list radius at the build; each particle has moved less than half
     // the skin before the trigger fires and at most 0.5 sigma per axis (an i32 displacement) in
@@ -764,6 +780,70 @@ int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential) {
     if (potential) {
         double pe = 0.0;
         for (uint32_t b = 0; b < nb; b++) pe += part[4 * b];
+        *potential = pe;
+    }
+    return GBMD_OK;
+}
+
+// The same kicks with f64 pair arithmetic (IntEngine<f64>): the accuracy reference of the f32
+// path, on the device so that it runs at full size.
+int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_TRY(prepare_pairs(e));
+    PairsF64 Q;
+    std::memset(&Q, 0, sizeof(Q));
+    const gbmd_system& s = e->sys;
+    for (uint32_t a = 0; a < s.nspecies; a++) {
+        Q.kick_c[a] = ((s.pinned >> a) & 1u) ? 0.0 : s.dt * s.dt / s.masses[a] * 4294967296.0;
+        for (uint32_t b = 0; b < s.nspecies; b++) {
+            const gbmd_pair& p = s.pairs[a * s.nspecies + b];
+            uint32_t q = a * e->P.ns + b;
+            Q.rc2[q] = p.rc * p.rc;
+            Q.eps4[q] = 4.0 * p.eps;
+            Q.sigma2[q] = p.sigma * p.sigma;
+            Q.shift[q] = pair_shift(p);
+            Q.six_eps4[q] = 6.0 * Q.eps4[q];
+        }
+    }
+    size_t n = e->n;
+    double* pe_dev = nullptr;
+    if (cudaMalloc(&pe_dev, n * 8) != cudaSuccess) return fail(GBMD_E_NOMEM, "f64 potential");
+    uint32_t nb = blocks_for(e->n, 128);
+    const bool cells = !e->verlet;
+    const void* pos = cells ? e->pos_scr : e->pos[e->cur];
+    const uint32_t* sp = cells ? e->species_scr : e->species;
+    const uint32_t* ids = cells ? e->ids_scr : e->ids;
+    const uint32_t* nbr = cells ? nullptr : e->nbr;
+    const uint32_t* cnt = cells ? nullptr : e->nbr_count;
+    const uint32_t* keys = cells ? e->keys[e->sorted] : nullptr;
+    const uint32_t* st = cells ? e->start : nullptr;
+#define GBMD_KF64(DD, MM) \
+    k_kicks_f64<DD, MM><<<nb, 128, 0, e->st>>>(e->P, Q, (const Rec<DD>*)pos, sp, nbr, cnt, keys, st, e->kicks, pe_dev)
+    if (e->D == 2) {
+        if (e->multi) GBMD_KF64(2, true);
+        else GBMD_KF64(2, false);
+    } else {
+        if (e->multi) GBMD_KF64(3, true);
+        else GBMD_KF64(3, false);
+    }
+#undef GBMD_KF64
+    note_launch();
+    int rc = GBMD_OK;
+    std::vector<double> pe_host(potential ? n : 0);
+    if (kicks) {
+        k_scatter_i32<<<blocks_for(n, 256), 256, 0, e->st>>>((uint32_t)n, e->D, ids, e->kicks, (int32_t*)e->staging_v);
+        note_launch();
+        if (cudaMemcpyAsync(kicks, e->staging_v, n * e->D * 4, cudaMemcpyDeviceToHost, e->st) != cudaSuccess) rc = fail(GBMD_E_CUDA, "kicks copy");
+    }
+    if (rc == GBMD_OK && potential && cudaMemcpyAsync(pe_host.data(), pe_dev, n * 8, cudaMemcpyDeviceToHost, e->st) != cudaSuccess)
+        rc = fail(GBMD_E_CUDA, "potential copy");
+    cudaError_t err = cudaStreamSynchronize(e->st);
+    cudaFree(pe_dev);
+    if (rc != GBMD_OK) return rc;
+    if (err != cudaSuccess) return fail(GBMD_E_CUDA, cudaGetErrorString(err));
+    if (potential) {
+        double pe = 0.0;
+        for (size_t i = 0; i < n; i++) pe += pe_host[i];
         *potential = pe;
     }
     return GBMD_OK;

@@ -546,6 +546,71 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
     }
 }
 
+// ---------------------------------------------------------------- FP64 reference kicks
+// The pair constants of IntEngine<f64> (real.rs:105-157 with F = f64): rounded from the f64
+// pair parameters, not through f32.
+struct PairsF64 {
+    double rc2[GBMD_MAX_SPECIES * GBMD_MAX_SPECIES], eps4[GBMD_MAX_SPECIES * GBMD_MAX_SPECIES];
+    double sigma2[GBMD_MAX_SPECIES * GBMD_MAX_SPECIES], shift[GBMD_MAX_SPECIES * GBMD_MAX_SPECIES];
+    double six_eps4[GBMD_MAX_SPECIES * GBMD_MAX_SPECIES];
+    double kick_c[GBMD_MAX_SPECIES]; // kick_coeff (system.rs:415-420), unscaled
+};
+// Per-particle kicks of IntEngine<f64>::forces (int_engine.rs:130-251): separations to_f64
+// (dropped beyond 8 sigma), PairConsts::eval in f64 left to right without fusion, each pair's
+// kick rint(-fr c d) saturated to i32 and summed with wrapping adds; pe += u in list order.
+// Walks the Verlet list (a superset of the f64 cutoff sphere) or the 3^D cells.
+template <int D, bool MULTI>
+__global__ void __launch_bounds__(128) k_kicks_f64(Params P, PairsF64 Q, const PosRec<D>* __restrict__ pos, const uint32_t* __restrict__ species,
+                                                   const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+                                                   const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
+                                                   int32_t* __restrict__ kicks, double* __restrict__ pe_out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    int64_t xi[3];
+    uint32_t si = load_particle<D, MULTI>(pos, species, i, xi);
+    const double c = Q.kick_c[si];
+    int32_t k[3] = {0, 0, 0};
+    double pe = 0.0;
+    auto visit = [&](uint32_t j) {
+        int64_t xj[3];
+        uint32_t sj = load_particle<D, MULTI>(pos, species, j, xj);
+        double f[3];
+#pragma unroll
+        for (int a = 0; a < D; a++) {
+            int64_t d = min_image(xj[a] - xi[a], P.box[a], P.half[a]);
+            if (!(d >= -((int64_t)8 << 32) && d < ((int64_t)8 << 32))) return;
+            f[a] = __dmul_rn((double)d, 1.0 / 4294967296.0);
+        }
+        const uint32_t q = si * P.ns + sj;
+        double r2 = __dadd_rn(__dmul_rn(f[0], f[0]), __dmul_rn(f[1], f[1]));
+        if (D == 3) r2 = __dadd_rn(r2, __dmul_rn(f[2], f[2]));
+        if (!(r2 < Q.rc2[q])) return;
+        double s2 = __ddiv_rn(Q.sigma2[q], r2);
+        double s6 = __dmul_rn(__dmul_rn(s2, s2), s2);
+        double fr = __ddiv_rn(__dmul_rn(__dmul_rn(Q.six_eps4[q], s6), __dsub_rn(__dmul_rn(2.0, s6), 1.0)), r2);
+        double u = __dsub_rn(__dmul_rn(__dmul_rn(Q.eps4[q], s6), __dsub_rn(s6, 1.0)), Q.shift[q]);
+        double am = __dmul_rn(-fr, c);
+#pragma unroll
+        for (int a = 0; a < D; a++) k[a] = wadd(k[a], sat_i32_f64(rint(__dmul_rn(am, f[a]))));
+        pe = __dadd_rn(pe, u);
+    };
+    if (nbr) {
+        uint32_t m = nbr_count[i];
+        const uint32_t cap4 = (P.cap + 3u) & ~3u;
+        for (uint32_t q = 0; q < m; q++) visit(nbr[list_slot(i, q, cap4)] & LIST_MASK);
+    } else {
+        uint32_t cc[3];
+        cell_coords(P, keys[i], cc);
+        for_cells<D>(P, cc, [&](uint32_t cell) {
+            for (uint32_t j = start[cell]; j < start[cell + 1]; j++)
+                if (j != i) visit(j);
+        });
+    }
+#pragma unroll
+    for (int a = 0; a < D; a++) kicks[D * i + a] = k[a];
+    pe_out[i] = 0.5 * pe;
+}
+
 // ---------------------------------------------------------------- velocity-rescale thermostat
 // The half-step kinetic energy summed exactly: per block and species, the 128-bit sum of v^2 over
 // the moving particles' velocity components (part[8 b + 2 s + {0: low, 1: high}]).

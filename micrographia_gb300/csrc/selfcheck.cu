@@ -1,0 +1,116 @@
+// Self-check of the pair chain's own correctly rounded reciprocal and division (rcp_cr, div_cr)
+// against the CUDA library's __frcp_rn / __fdiv_rn: every f32 of the reciprocal's range, every
+// f32 r2 of each pair type's fast range through the whole chain, and seeded random quotients.
+#include <cstring>
+
+#include "common.cuh"
+#include "engine.cuh"
+
+using namespace gbmd;
+
+namespace {
+
+__device__ unsigned long long g_bad;
+
+__device__ __forceinline__ void note_bad(bool bad) {
+    unsigned b = __ballot_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31u) == 0 && b) atomicAdd(&g_bad, (unsigned long long)__popc(b));
+}
+
+// bits in [lo, lo + count): rcp_cr(b) == __frcp_rn(b) bit for bit
+__global__ void k_check_rcp(uint32_t lo, uint32_t count) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k - (k & 31u) < count; k += gridDim.x * blockDim.x) {
+        bool bad = false;
+        if (k < count) {
+            float b = __uint_as_float(lo + k);
+            bad = __float_as_uint(rcp_cr(b)) != __float_as_uint(__frcp_rn(b));
+        }
+        note_bad(bad);
+    }
+}
+
+// bits in [lo, lo + count): pair_chain == pair_fr_library (fr and s6) bit for bit
+__global__ void k_check_chain(PairC p, uint32_t lo, uint32_t count) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k - (k & 31u) < count; k += gridDim.x * blockDim.x) {
+        bool bad = false;
+        if (k < count) {
+            float r2 = __uint_as_float(lo + k);
+            float fa, sa, fb, sb;
+            pair_chain(p, r2, fa, sa);
+            pair_fr_library(p, r2, fb, sb);
+            bad = __float_as_uint(fa) != __float_as_uint(fb) || __float_as_uint(sa) != __float_as_uint(sb);
+        }
+        note_bad(bad);
+    }
+}
+
+// Seeded random a in +-[2^-100, 2^100), b in [2^-30, 2^62) with a / b within [2^-120, 2^120]:
+// div_cr(a, b, rcp_cr(b)) == __fdiv_rn(a, b).
+__global__ void k_check_div(uint64_t count, uint32_t seed) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k - (k & 31u) < count; k += (uint64_t)gridDim.x * blockDim.x) {
+        bool bad = false;
+        if (k < count) {
+            uint32_t r0, r1, r2, r3;
+            threefry2x32((uint32_t)k, (uint32_t)(k >> 32), seed, 0x5eedu, r0, r1);
+            threefry2x32((uint32_t)k, (uint32_t)(k >> 32), seed, 0xd1cu, r2, r3);
+            float a = __uint_as_float(((27u + r2 % 200u) << 23) | (r0 & 0x7fffffu) | (r3 & 0x80000000u));
+            float b = __uint_as_float(((97u + r3 % 92u) << 23) | (r1 & 0x7fffffu));
+            float q = __fdiv_rn(a, b), aq = fabsf(q);
+            if (aq >= 0x1p-120f && aq <= 0x1p120f) bad = __float_as_uint(div_cr(a, b, rcp_cr(b))) != __float_as_uint(q);
+        }
+        note_bad(bad);
+    }
+}
+
+} // namespace
+
+extern "C" int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quotients, int32_t device, uint64_t* checked,
+                                    uint64_t* mismatched) {
+    if (!sys || !checked || !mismatched) return fail(GBMD_E_INVALID, "null argument");
+    GBMD_TRY(validate_system(*sys, 1));
+    GBMD_CUDA_TRY(cudaSetDevice(device));
+    Params P;
+    std::memset(&P, 0, sizeof(P));
+    uint32_t nc[3] = {3, 3, 3};
+    fill_params(P, *sys, 1, 0.3, 1, nc);
+    cudaStream_t s;
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    unsigned long long zero = 0;
+    int rc = GBMD_OK;
+    uint64_t total = 0;
+    if (cudaMemcpyToSymbolAsync(g_bad, &zero, 8, 0, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "self-check counter");
+    const int grid = 152 * 8, block = 256;
+    // the reciprocal over [2^50, 2^63)
+    if (rc == GBMD_OK) {
+        uint32_t lo = (127u + 50u) << 23, hi = (127u + 63u) << 23;
+        k_check_rcp<<<grid, block, 0, s>>>(lo, hi - lo);
+        note_launch();
+        total += hi - lo;
+    }
+    // the whole chain over [fast_lo, rc2s) of each pair type that uses the fast path
+    for (uint32_t k = 0; rc == GBMD_OK && k < sys->nspecies * sys->nspecies; k++) {
+        const PairC& c = P.pc[k];
+        if (!(c.fast_lo < c.rc2s)) continue;
+        uint32_t lo, hi;
+        std::memcpy(&lo, &c.fast_lo, 4);
+        std::memcpy(&hi, &c.rc2s, 4);
+        k_check_chain<<<grid, block, 0, s>>>(c, lo, hi - lo);
+        note_launch();
+        total += hi - lo;
+    }
+    if (rc == GBMD_OK && random_quotients) {
+        k_check_div<<<grid, block, 0, s>>>(random_quotients, 20260u);
+        note_launch();
+        total += random_quotients;
+    }
+    unsigned long long bad = 0;
+    if (rc == GBMD_OK && cudaMemcpyFromSymbolAsync(&bad, g_bad, 8, 0, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        rc = fail(GBMD_E_CUDA, "self-check counter");
+    cudaError_t err = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (rc != GBMD_OK) return rc;
+    if (err != cudaSuccess) return fail(GBMD_E_CUDA, cudaGetErrorString(err));
+    *checked = total;
+    *mismatched = bad;
+    return GBMD_OK;
+}

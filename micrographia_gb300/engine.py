@@ -121,6 +121,13 @@ class _Engine:
         _abi.check(self._lib.gbmd_kicks(self._h, _ptr(k, C.c_int32), C.byref(pe)))
         return k, pe.value
 
+    def kicks_f64(self):
+        """The kicks of IntEngine<f64> (f64 pair chain), the accuracy reference."""
+        k = np.empty((self.n, self.DIM), np.int32)
+        pe = C.c_double()
+        _abi.check(self._lib.gbmd_kicks_f64(self._h, _ptr(k, C.c_int32), C.byref(pe)))
+        return k, pe.value
+
     def flip_bit(self, particle, axis, bit):
         _abi.check(self._lib.gbmd_flip_bit(self._h, particle, axis, bit))
 

@@ -382,6 +382,66 @@ def test_rdf_small_box_all_pairs(O, dim):
     assert ref.sum() > 0
 
 
+# ---------------------------------------------------------------- FP64 reference kicks (IntEngine<f64>)
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_f64_kicks_match_oracle_2d(O, mode):
+    sys_ = System(box_for(3000, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 3.0]).with_pair(0, 1, Pair(0.6, 1.1, 2.5))
+    s = O.fluid(sys_, 3000, 1.0, 1)
+    s.species[::3] = 1
+    s.vel = O.maxwell(sys_, s.species, 1.0, 1)
+    cpu = O.IntEngine(sys_, s)
+    cpu.step(60)
+    st = cpu.state
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_for(sys_, 3000)
+    with GpuEngine(sys_, st, m) as g:
+        k64, pe64 = g.kicks_f64()
+        k32, _ = g.kicks()
+    want, want_pe = O.IntEngine(sys_, st, f64=True).kicks()
+    assert np.array_equal(k64, want)
+    assert abs(pe64 - want_pe) < 1e-12 * abs(want_pe)  # f64 sums in another order
+    rel = math.sqrt(((k32.astype(np.float64) - k64) ** 2).sum() / (k64.astype(np.float64) ** 2).sum())
+    assert rel < 1e-5  # md-ref physics.rs:144
+
+
+def test_f64_kicks_match_oracle_3d(O):
+    sys3, s = liquid3(O, 4000, 0.8, 1.0)
+    cpu = O.IntEngine(sys3, s)
+    cpu.step(30)
+    st = cpu.state
+    with GpuEngine3(sys3, st) as g:
+        g.step(7)  # positions unwrapped between list builds
+        st = g.read_state()
+        k64, _ = g.kicks_f64()
+    want, _ = O.IntEngine(sys3, st, f64=True).kicks()
+    assert np.array_equal(k64, want)
+
+
+# ---------------------------------------------------------------- the pair arithmetic's own reciprocal and division
+@pytest.mark.parametrize(
+    "pairs",
+    [
+        [Pair.lj(2.5)],
+        [Pair.wca()],
+        [Pair.lj(2.5), Pair(0.6, 1.1, 2.5), Pair(0.6, 1.1, 2.5), Pair(0.3, 0.8, 3.0)],
+    ],
+    ids=["lj", "wca", "mixture"],
+)
+def test_pair_math_matches_library(pairs):
+    """rcp_cr / div_cr equal __frcp_rn / __fdiv_rn bit for bit: every f32 of [2^50, 2^63), every
+    scaled r2 of each pair type's fast range through the LJ chain, and 2^28 random quotients."""
+    import ctypes as C
+
+    ns = 1 if len(pairs) == 1 else 2
+    sys_ = System(box_for(1000, 0.7, 1.0), 0.005, pairs[0], [1.0] * ns)
+    if ns == 2:
+        sys_ = sys_.with_pair(0, 1, pairs[1]).with_pair(1, 1, pairs[3])
+    checked, bad = C.c_uint64(), C.c_uint64()
+    cs = sys_.to_c()
+    _abi.check(_abi.lib().gbmd_check_pair_math(C.byref(cs), 1 << 28, 0, C.byref(checked), C.byref(bad)))
+    assert bad.value == 0
+    assert checked.value > (13 << 23) + (1 << 28)
+
+
 # ---------------------------------------------------------------- velocity-rescale thermostat (configs[2])
 def test_rescale_thermostat_matches_oracle(O):
     """Slab start, rescale to T = 0.45 every 10 steps: the GPU trajectory equals the oracle's
