@@ -380,7 +380,11 @@ def run_c4(args, world, rank, local, pg):
     batch.wait()
     clk = clocks.stop()
     l1, r1 = batch.stats()
-    value = world * total * K / (ms_b * 1e-3)
+    from micrographia_gb300 import replicas
+
+    # replicas: every rank runs the whole batch; units summed, time maxed over ranks
+    units, secs = replicas.aggregate(pg, total * K, ms_b * 1e-3)
+    value = units / secs
     # bit-exactness spot check: the first and last replicas against their plain runs
     checks = {}
     plain = [GpuEngine(s, st, mode, device=local) for s, st in zip(systems, states)]
@@ -511,8 +515,11 @@ def run_c5(args, world, rank, local, pg):
 
     from micrographia_gb300 import ForceMode, GpuEngine, GpuEngine3, Server, workloads
 
+    from micrographia_gb300 import replicas
+
     torch.cuda.set_device(local)
-    reqs = workloads.config5(args.requests, args.rate)
+    # replicas: the request stream is dealt out by rank (request k to rank k mod N)
+    reqs = replicas.shard(workloads.config5(args.requests, args.rate), rank, world)
     steps = args.steps
 
     def serve():
@@ -565,6 +572,13 @@ def run_c5(args, world, rank, local, pg):
 
     v_serve, mk_serve, lat_serve = serve()
     v_serial, mk_serial, lat_serial = serial()
+    # whole job over ranks: atom-steps summed, makespans maxed, latencies pooled
+    u, mk_serve = replicas.aggregate(pg, v_serve * mk_serve, mk_serve)
+    v_serve = u / mk_serve
+    u, mk_serial = replicas.aggregate(pg, v_serial * mk_serial, mk_serial)
+    v_serial = u / mk_serial
+    lat_serve = replicas.gather(pg, lat_serve)
+    lat_serial = replicas.gather(pg, lat_serial)
     line = {
         "metric": METRIC,
         "value": v_serve,
@@ -579,7 +593,7 @@ def run_c5(args, world, rank, local, pg):
         "dtype": "f32+int64",
         "data": "synthetic",
         "config": {
-            "workload": f"{len(reqs)} requests, Poisson arrivals at {args.rate}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget (configs[4])",
+            "workload": f"{args.requests} requests (dealt out over {world} GPU(s)), Poisson arrivals at {args.rate}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget (configs[4])",
             "form": "served: continuous batching (each admitted request on its own stream, intervals overlapped)",
             "makespan_s": mk_serve,
             "frame_latency_p50_ms": 1e3 * _pct(lat_serve, 50),
