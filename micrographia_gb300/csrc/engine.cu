@@ -83,6 +83,66 @@ static double pair_shift(const gbmd_pair& p) {
 }
 static float scale2(float v, int e) { return std::ldexp(v, e); }
 
+// Rust's f64::powi: square-and-multiply from the low bit (the order sets the rounding).
+static double powi_rs(double x, int n) {
+    double res = 1.0, sq = x;
+    bool have = false;
+    while (n) {
+        if (n & 1) {
+            res = have ? res * sq : sq;
+            have = true;
+        }
+        n >>= 1;
+        if (n) sq = sq * sq;
+    }
+    return have ? res : 1.0;
+}
+static int32_t sat_i32_host(double x) {
+    if (x != x) return 0;
+    if (x >= 2147483647.0) return INT32_MAX;
+    if (x <= -2147483648.0) return INT32_MIN;
+    return (int32_t)x;
+}
+static uint32_t sat_u32_host(double x) {
+    if (!(x > 0.0)) return 0;
+    if (x >= 4294967295.0) return UINT32_MAX;
+    return (uint32_t)x;
+}
+// IntTables::new (crates/md-core/src/table.rs:45-71): per pair type, the kick coefficient
+// 4 c f_over_r(r2) (f_over_r without its cutoff, pair.rs:45-51) rounded half away from zero at
+// r2 = k 2^12 / 2^24 sigma^2 (k = 0 .. len - 1, r2 at least 0.36), zero beyond rc^2 + 2 steps.
+static void int_tables(const gbmd_system& s, std::vector<int32_t>& data, uint32_t& len, uint32_t* irc2, std::vector<double>& pair4) {
+    const uint32_t ns = s.nspecies;
+    const double rcm = rc_max(s), rc2_max = rcm * rcm;
+    len = (uint32_t)(((uint64_t)(rc2_max * 16777216.0) >> 12) + 2);
+    data.assign((size_t)ns * ns * len, 0);
+    pair4.assign((size_t)ns * ns * 4, 0.0);
+    for (uint32_t a = 0; a < ns; a++) {
+        const double c = ((s.pinned >> a) & 1u) ? 0.0 : s.dt * s.dt / s.masses[a] * 4294967296.0;
+        for (uint32_t b = 0; b < ns; b++) {
+            const gbmd_pair& p = s.pairs[a * ns + b];
+            const uint32_t q = a * ns + b;
+            irc2[q] = sat_u32_host(p.rc * p.rc * 16777216.0);
+            pair4[4 * q] = p.eps;
+            pair4[4 * q + 1] = p.sigma;
+            pair4[4 * q + 2] = p.rc;
+            pair4[4 * q + 3] = pair_shift(p);
+            for (uint32_t k = 0; k < len; k++) {
+                double r2 = (double)((uint64_t)k * 4096ull) / 16777216.0;
+                r2 = std::max(r2, 0.36);
+                double t = 0.0;
+                if (r2 < p.rc * p.rc + 2.0 * 4096.0 / 16777216.0) {
+                    const double s6 = powi_rs(p.sigma * p.sigma / r2, 3);
+                    t = 24.0 * p.eps * s6 * (2.0 * s6 - 1.0) / r2 * c * 4.0;
+                }
+                double rt = std::round(t);
+                rt = std::min(std::max(rt, -2147483648.0), 2147483647.0);
+                data[(size_t)q * len + k] = sat_i32_host(rt);
+            }
+        }
+    }
+}
+
 // Lower end of the scaled r2 range in which the pair chain uses rcp_cr / div_cr: 2^50 (r of
 // 1/8 sigma) when, over [2^50, rc2s), t = c6 s6 (2 s6 - 1) stays below 2^100 in magnitude and its
 // non-zero values above 2^-60 (so t / r2 is a normal f32), else +inf (library division only).
@@ -228,6 +288,8 @@ struct gbmd_engine {
     uint64_t launches = 0;
     uint32_t last_rebuilds = 0;
     bool failed = false;
+    int32_t* itab = nullptr; // all-integer kick tables (GBMD_ARITH_INT)
+    double* ipair = nullptr;
     // observation scratch, kept between frames (freeing it would synchronise the whole device)
     unsigned long long* obs_bins = nullptr;
     size_t obs_bins_cap = 0;
@@ -254,7 +316,7 @@ void free_all(gbmd_engine* e) {
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
                     e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1],
-                    e->obs_bins, e->obs_start};
+                    e->obs_bins, e->obs_start, e->itab, e->ipair};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (e->st) cudaStreamDestroy(e->st);
@@ -298,21 +360,24 @@ void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
     note_launch();
 }
 
-template <int D, bool MULTI> void enqueue_force_t(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
+template <int D, bool MULTI, bool INT> void enqueue_force_a(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
     if (e->verlet) {
-        k_force_list<D, MULTI><<<blocks_for(e->n, threads), threads, 0, s>>>(e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1],
-                                                                           e->qpos[e->cur], e->qpos[e->cur ^ 1],
-                                                                           e->vel, e->species, e->nbr, e->nbr_count,
-                                                                           (const Rec<D>*)e->ref_pos, e->ctl);
+        k_force_list<D, MULTI, INT><<<blocks_for(e->n, threads), threads, 0, s>>>(
+            e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur], e->qpos[e->cur ^ 1], e->vel, e->species,
+            e->nbr, e->nbr_count, (const Rec<D>*)e->ref_pos, e->ctl);
         note_launch();
         e->cur ^= 1;
     } else {
         enqueue_bin<D>(e, s, e->P);
-        k_force_cells<D, MULTI><<<blocks_for(e->n, threads), threads, 0, s>>>(e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr,
-                                                                            e->ids_scr, e->keys[e->sorted], e->start,
-                                                                            (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids);
+        k_force_cells<D, MULTI, INT><<<blocks_for(e->n, threads), threads, 0, s>>>(e->P, (const Rec<D>*)e->pos_scr, e->vel_scr,
+                                                                                 e->species_scr, e->ids_scr, e->keys[e->sorted], e->start,
+                                                                                 (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids);
         note_launch();
     }
+}
+template <int D, bool MULTI> void enqueue_force_t(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
+    if (e->P.int_mode) enqueue_force_a<D, MULTI, true>(e, s, threads);
+    else enqueue_force_a<D, MULTI, false>(e, s, threads);
 }
 void enqueue_force(gbmd_engine* e, cudaStream_t s) {
     uint32_t threads = e->opt.threads ? e->opt.threads : 128;
@@ -453,16 +518,21 @@ int prepare_pairs(gbmd_engine* e) {
 
 // Kicks (storage order) and the per-block observables at the current positions; optionally
 // reverse the velocities. Cell mode works on (and copies back) the sorted scratch state.
-template <int D, bool MULTI> int kicks_t(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
+template <int D, bool MULTI, bool INT> void kicks_launch(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
     uint32_t threads = 128;
     uint32_t nb = blocks_for(e->n, threads);
-    if (e->verlet) {
-        k_kicks<D, MULTI><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos[e->cur], e->species, e->nbr, e->nbr_count, nullptr, nullptr,
-                                                     e->vel, kicks, partial, reverse);
-    } else {
+    if (e->verlet)
+        k_kicks<D, MULTI, INT><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos[e->cur], e->species, e->nbr, e->nbr_count, nullptr,
+                                                          nullptr, e->vel, kicks, partial, reverse);
+    else
+        k_kicks<D, MULTI, INT><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos_scr, e->species_scr, nullptr, nullptr,
+                                                          e->keys[e->sorted], e->start, e->vel_scr, kicks, partial, reverse);
+}
+template <int D, bool MULTI> int kicks_t(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
+    if (e->P.int_mode) kicks_launch<D, MULTI, true>(e, kicks, partial, reverse);
+    else kicks_launch<D, MULTI, false>(e, kicks, partial, reverse);
+    if (!e->verlet) {
         // positions, velocities and ids live in scratch (sorted) until copied back
-        k_kicks<D, MULTI><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos_scr, e->species_scr, nullptr, nullptr, e->keys[e->sorted],
-                                                     e->start, e->vel_scr, kicks, partial, reverse);
         GBMD_CUDA_TRY(cudaMemcpyAsync(e->pos[e->cur], e->pos_scr, (size_t)e->n * e->rec, cudaMemcpyDeviceToDevice, e->st));
         GBMD_CUDA_TRY(cudaMemcpyAsync(e->vel, e->vel_scr, (size_t)e->n * D * 4, cudaMemcpyDeviceToDevice, e->st));
         GBMD_CUDA_TRY(cudaMemcpyAsync(e->species, e->species_scr, (size_t)e->n * 4, cudaMemcpyDeviceToDevice, e->st));
@@ -582,7 +652,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     int mode = e->opt.mode;
     if (mode == GBMD_MODE_AUTO) mode = (e->D == 2 && n < 24000) ? GBMD_MODE_CELLS : GBMD_MODE_VERLET; // ForceMode::auto
     e->verlet = mode == GBMD_MODE_VERLET;
-    if (e->opt.arith != GBMD_ARITH_F32) return fail(GBMD_E_UNSUPPORTED, "all-integer table forces are not built in this engine yet");
+    if (e->opt.arith != GBMD_ARITH_F32 && e->opt.arith != GBMD_ARITH_INT) return fail(GBMD_E_INVALID, "unknown pair arithmetic");
     e->skin = e->verlet ? (e->opt.skin > 0 ? e->opt.skin : 0.4) : 0.0;
     uint32_t nc[3];
     GBMD_TRY(cells_for(*sys, rc_max(*sys) + e->skin, nc));
@@ -632,6 +702,20 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         GBMD_TRY(allocT(&e->nbr_count, n));
     }
     GBMD_TRY(allocT(&e->ctl, 16));
+    if (e->opt.arith == GBMD_ARITH_INT) {
+        std::vector<int32_t> tab;
+        std::vector<double> pair4;
+        uint32_t len = 0;
+        int_tables(*sys, tab, len, e->P.irc2, pair4);
+        GBMD_TRY(allocT(&e->itab, tab.size()));
+        GBMD_TRY(allocT(&e->ipair, pair4.size()));
+        GBMD_CUDA_TRY(cudaMemcpy(e->itab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+        GBMD_CUDA_TRY(cudaMemcpy(e->ipair, pair4.data(), pair4.size() * 8, cudaMemcpyHostToDevice));
+        e->P.int_mode = 1;
+        e->P.itab_len = len;
+        e->P.itab = e->itab;
+        e->P.ipair = e->ipair;
+    }
     GBMD_TRY(allocT(&e->relf, n));
     GBMD_TRY(allocT(&e->qpos[0], n));
     GBMD_TRY(allocT(&e->qpos[1], n));

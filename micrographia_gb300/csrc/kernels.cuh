@@ -96,6 +96,54 @@ __global__ void k_gather(Params P, const uint32_t* items, const uint32_t* keys, 
 
 __device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
 
+// ---------------------------------------------------------------- all-integer table forces
+// IntTables::kick (table.rs:76-105): d rounded to 2^-20 sigma per axis, r2 to 2^-24 sigma^2, the
+// table's kick coefficient interpolated linearly between entries 2^12 apart in r2, and each
+// axis's kick -t q >> 22 with the sign taken apart (the product fits 54 bits). Pure integer
+// arithmetic: bit-identical on every device. Adds to k and returns true inside the cutoff.
+template <int D>
+__device__ __forceinline__ bool int_kick(const Params& P, uint32_t pair, const int64_t* d, int32_t* k) {
+    const int64_t limit = (int64_t)8 << 32;
+    int64_t q[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; a++)
+        if (!(d[a] >= -limit && d[a] < limit)) return false;
+    uint64_t sq = 0;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const uint64_t ax = d[a] < 0 ? (uint64_t)0 - (uint64_t)d[a] : (uint64_t)d[a];
+        const int64_t m = (int64_t)((ax + (1ull << 11)) >> 12);
+        q[a] = d[a] < 0 ? -m : m;
+        sq += (uint64_t)(q[a] * q[a]);
+    }
+    const uint32_t r2 = (uint32_t)((sq + (1ull << 15)) >> 16);
+    if (r2 >= P.irc2[pair]) return false;
+    const int32_t* tab = P.itab + (size_t)pair * P.itab_len;
+    const int64_t t0 = __ldg(tab + (r2 >> 12)), t1 = __ldg(tab + (r2 >> 12) + 1);
+    const int64_t t = t0 + (((t1 - t0) * (int64_t)(r2 & 4095u)) >> 12);
+    const uint64_t at = t < 0 ? (uint64_t)0 - (uint64_t)t : (uint64_t)t;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const uint64_t aq = q[a] < 0 ? (uint64_t)0 - (uint64_t)q[a] : (uint64_t)q[a];
+        const int64_t m = (int64_t)((at * aq) >> 22);
+        const bool neg = (t < 0) != (q[a] < 0);
+        k[a] = (int32_t)((uint32_t)k[a] + (uint32_t)(neg ? m : -m));
+    }
+    return true;
+}
+// Pair::energy and f_over_r (pair.rs:36-51) in f64 at r2 in sigma^2: the instruments of the
+// integer path (IntEngine::forces sums Pair::energy of the exact separations).
+__device__ __forceinline__ void pair_f64(const double* c, double r2, double& u, double& fr) {
+    const double eps = c[0], sigma = c[1], rc = c[2], shift = c[3];
+    u = 0.0;
+    fr = 0.0;
+    if (r2 >= __dmul_rn(rc, rc)) return;
+    const double y = __ddiv_rn(__dmul_rn(sigma, sigma), r2);
+    const double s6 = __dmul_rn(y, __dmul_rn(y, y));
+    u = __dsub_rn(__dmul_rn(__dmul_rn(__dmul_rn(4.0, eps), s6), __dsub_rn(s6, 1.0)), shift);
+    fr = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(24.0, eps), s6), __dsub_rn(__dmul_rn(2.0, s6), 1.0)), r2);
+}
+
 // One directed pair (i from j): adds the integer kick rint(a * f) per axis, exactly
 // IntEngine::forces' `(a * fx).round_even().to_i32()` summed with wrapping adds.
 template <int D, class G>
@@ -341,7 +389,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // The hot kernel: LJ pair kicks over the Verlet list fused with the integer leapfrog and the
 // rebuild trigger. Reads positions from pos_in and writes the moved ones to pos_out (the engine
 // ping-pongs the two), so every kick sees positions of the same time step.
-template <int D, bool MULTI>
+template <int D, bool MULTI, bool INT = false>
 __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
                                                     const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                     int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
@@ -391,10 +439,19 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
 #pragma unroll
                     for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
                 }
-                float f[D];
+                if constexpr (INT) {
+                    // the exact separation from the records: d = 16 (Xj - Xi) + (rj - ri)
+                    int64_t d[3] = {0, 0, 0};
 #pragma unroll
-                for (int a = 0; a < D; a++) f[a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
-                add_kick(f, MULTI ? P.pc[si * P.ns + (r[u].w >> 24)] : pc0);
+                    for (int a = 0; a < D; a++)
+                        d[a] = (int64_t)(int32_t)(Xj[a] - Xi[a]) * 16 + ((int64_t)Rj[a] - (int64_t)((qi.w >> (8 * a)) & 15u));
+                    int_kick<D>(P, MULTI ? si * P.ns + (r[u].w >> 24) : 0u, d, k);
+                } else {
+                    float f[D];
+#pragma unroll
+                    for (int a = 0; a < D; a++) f[a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
+                    add_kick(f, MULTI ? P.pc[si * P.ns + (r[u].w >> 24)] : pc0);
+                }
             }
         }
     } else {
@@ -411,14 +468,24 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
             for (int u = 0; u < 4; u++) {
                 if ((uint32_t)u >= left) break;
                 const uint32_t code = jj[u] >> LIST_BITS;
-                float f[D];
+                if constexpr (INT) {
+                    int64_t d[3] = {0, 0, 0};
 #pragma unroll
-                for (int a = 0; a < D; a++) {
-                    uint32_t c = (code >> (2 * a)) & 3u;
-                    int64_t img = c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0);
-                    f[a] = sep_near(xj[u][a] + img - xi[a]);
+                    for (int a = 0; a < D; a++) {
+                        uint32_t c = (code >> (2 * a)) & 3u;
+                        d[a] = xj[u][a] + (c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0)) - xi[a];
+                    }
+                    int_kick<D>(P, MULTI ? si * P.ns + sj[u] : 0u, d, k);
+                } else {
+                    float f[D];
+#pragma unroll
+                    for (int a = 0; a < D; a++) {
+                        uint32_t c = (code >> (2 * a)) & 3u;
+                        int64_t img = c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0);
+                        f[a] = sep_near(xj[u][a] + img - xi[a]);
+                    }
+                    add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
                 }
-                add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
             }
         }
     }
@@ -437,7 +504,7 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
 
 // Cell-list force + leapfrog (ForceMode::CellList; md.wgsl:39-76): scans the 3^D cells of the
 // sorted scratch state and writes the moved state back into the engine's arrays.
-template <int D, bool MULTI>
+template <int D, bool MULTI, bool INT = false>
 __global__ void __launch_bounds__(128) k_force_cells(Params P, const PosRec<D>* __restrict__ pos_s, const int32_t* __restrict__ vel_s,
                                                      const uint32_t* __restrict__ species_s, const uint32_t* __restrict__ ids_s,
                                                      const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
@@ -457,8 +524,15 @@ __global__ void __launch_bounds__(128) k_force_cells(Params P, const PosRec<D>* 
             if (j == i) continue;
             int64_t xj[3];
             uint32_t sj = load_particle<D, MULTI>(pos_s, species_s, j, xj);
-            float fr, s6, r2;
-            pair_kick<D>(P, P.pc[si * P.ns + sj], cs, xi, xj, k, fr, s6, r2);
+            if constexpr (INT) {
+                int64_t d[3] = {0, 0, 0};
+#pragma unroll
+                for (int a = 0; a < D; a++) d[a] = min_image(xj[a] - xi[a], P.box[a], P.half[a]);
+                int_kick<D>(P, si * P.ns + sj, d, k);
+            } else {
+                float fr, s6, r2;
+                pair_kick<D>(P, P.pc[si * P.ns + sj], cs, xi, xj, k, fr, s6, r2);
+            }
         }
     });
     int32_t v[3];
@@ -477,7 +551,7 @@ __global__ void __launch_bounds__(128) k_force_cells(Params P, const PosRec<D>* 
 // f32 fr r^2), [2] on-step kinetic energy (int_engine.rs:417-446). `list` selects the Verlet
 // list (nbr != nullptr) or the 3^D cell scan over `start`/`keys`. With `reverse` set the
 // velocities become -(v + kick + g) (int_engine.rs:396-413).
-template <int D, bool MULTI>
+template <int D, bool MULTI, bool INT = false>
 __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __restrict__ pos, const uint32_t* __restrict__ species,
                                                const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
@@ -494,11 +568,29 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
         auto visit = [&](uint32_t j) {
             int64_t xj[3];
             uint32_t sj = load_particle<D, MULTI>(pos, species, j, xj);
-            const PairC& pc = P.pc[si * P.ns + sj];
-            float fr, s6, r2;
-            if (pair_kick<D>(P, pc, cs, xi, xj, k, fr, s6, r2)) {
-                pe += (double)pair_u(pc, s6);
-                w += (double)__fmul_rn(fr, r2);
+            if constexpr (INT) {
+                int64_t d[3] = {0, 0, 0};
+#pragma unroll
+                for (int a = 0; a < D; a++) d[a] = min_image(xj[a] - xi[a], P.box[a], P.half[a]);
+                if (int_kick<D>(P, si * P.ns + sj, d, k)) {
+                    double r2 = 0.0;
+#pragma unroll
+                    for (int a = 0; a < D; a++) {
+                        const double x = __dmul_rn((double)d[a], 1.0 / 4294967296.0);
+                        r2 = __dadd_rn(r2, __dmul_rn(x, x));
+                    }
+                    double u, fr;
+                    pair_f64(P.ipair + 4 * (si * P.ns + sj), r2, u, fr);
+                    pe += u;
+                    w += __dmul_rn(fr, r2);
+                }
+            } else {
+                const PairC& pc = P.pc[si * P.ns + sj];
+                float fr, s6, r2;
+                if (pair_kick<D>(P, pc, cs, xi, xj, k, fr, s6, r2)) {
+                    pe += (double)pair_u(pc, s6);
+                    w += (double)__fmul_rn(fr, r2);
+                }
             }
         };
         if (nbr) {

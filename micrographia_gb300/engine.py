@@ -43,14 +43,17 @@ class _Engine:
     DIM = 2
     STATE = State
 
-    def __init__(self, sys, state=None, mode=None, *, init=None, threads=0, block_steps=0, rescale_every=0, rescale_t=0.0, device=0):
-        """Create from (sys, state), or from a device-side seeded init (`init` = gbmd_init)."""
+    def __init__(self, sys, state=None, mode=None, *, init=None, threads=0, block_steps=0, rescale_every=0, rescale_t=0.0, device=0,
+                 arith=_abi.ARITH_F32):
+        """Create from (sys, state), or from a device-side seeded init (`init` = gbmd_init).
+        `arith`: ARITH_F32 (f32 pair chain, per-pair integer kicks) or ARITH_INT (all-integer
+        tables, IntEngine::integer, int_engine.rs:94-98)."""
         if sys.DIM != self.DIM:
             raise ValueError(f"{type(self).__name__} needs a {self.DIM}D system")
         self.sys = sys
         self._lib = _abi.lib()
         self._csys = sys.to_c()
-        self._opts = _options(mode, threads, block_steps, rescale_every, rescale_t, device=device)
+        self._opts = _options(mode, threads, block_steps, rescale_every, rescale_t, arith=arith, device=device)
         h = C.c_void_p()
         if init is not None:
             _abi.check(self._lib.gbmd_create_seeded(C.byref(self._csys), C.byref(init), C.byref(self._opts), C.byref(h)))

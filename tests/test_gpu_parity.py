@@ -382,6 +382,54 @@ def test_rdf_small_box_all_pairs(O, dim):
     assert ref.sum() > 0
 
 
+# ---------------------------------------------------------------- all-integer table forces (md-core table.rs)
+def golden_int_setup(O):
+    """md/src/checks.rs:155-167: 3000-particle binary LJ mixture, rho 0.6, seed 2026."""
+    sys_ = System(box_for(3000, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 2.0]).with_pair(0, 1, Pair(0.7, 1.05, 2.5))
+    s = O.fluid(sys_, 3000, 1.0, 2026)
+    s.species[::4] = 1
+    s.vel = O.maxwell(sys_, s.species, 1.0, 2026)
+    return sys_, s
+
+
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_golden_int_hash_on_gpu(O, mode):
+    """The reference's own golden vector, reproduced on the GPU: GOLDEN_INT_HASH after 1000
+    all-integer steps (md/tests/integer.rs:84-98)."""
+    import json
+    import os
+
+    golden = int(json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.json")))["golden_int_hash"], 16)
+    sys_, s = golden_int_setup(O)
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_for(sys_, 3000)
+    with GpuEngine(sys_, s, m, arith=_abi.ARITH_INT) as g:
+        g.step(1000)
+        assert g.read_state().hash() == golden
+
+
+def test_integer_kicks_match_oracle_2d_and_3d(O):
+    sys_, s = golden_int_setup(O)
+    cpu = O.IntEngine(sys_, s, f64=True, integer=True)
+    cpu.step(50)
+    st = cpu.state
+    for m in (ForceMode.cell_list(), ForceMode.verlet_for(sys_, 3000)):
+        with GpuEngine(sys_, st, m, arith=_abi.ARITH_INT) as g:
+            kg, pe = g.kicks()
+        kc, pec = cpu.kicks()
+        assert np.array_equal(kg, kc)
+        assert abs(pe - pec) < 1e-10 * abs(pec)  # f64 pair energies summed in another order
+    sys3, s3 = liquid3(O, 4000, 0.8, 1.0)
+    c3 = O.IntEngine(sys3, s3, f64=True, integer=True)
+    c3.step(20)
+    st3 = c3.state
+    with GpuEngine3(sys3, st3, arith=_abi.ARITH_INT) as g:
+        g.step(15)
+        c3.step(15)
+        assert g.read_state() == c3.state
+        kg, _ = g.kicks()
+    assert np.array_equal(kg, c3.kicks()[0])
+
+
 # ---------------------------------------------------------------- FP64 reference kicks (IntEngine<f64>)
 @pytest.mark.parametrize("mode", ["cells", "verlet"])
 def test_f64_kicks_match_oracle_2d(O, mode):
