@@ -389,8 +389,10 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // The hot kernel: LJ pair kicks over the Verlet list fused with the integer leapfrog and the
 // rebuild trigger. Reads positions from pos_in and writes the moved ones to pos_out (the engine
 // ping-pongs the two), so every kick sees positions of the same time step.
-template <int D, bool MULTI, bool INT = false>
-__global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
+// Ten blocks of 128 per SM (48 registers, a 16-byte spill outside the pair loop): measured 2.4%
+// faster than the unconstrained 62 registers at eight blocks.
+template <int D, bool MULTI, bool INT = false, bool SIG1 = false>
+__global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
                                                     const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                     int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
                                                     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(128) k_force_list(Params P, const PosRec<D>* _
     // so neither a minimum image nor a range check is needed.
     auto add_kick = [&](const float* f, const PairC& pc) {
         float fr, s6, r2;
-        if (pair_fr<D>(pc, f, fr, s6, r2)) {
+        if (pair_fr<D, SIG1>(pc, f, fr, s6, r2)) {
             float am = __fmul_rn(-fr, cs);
 #pragma unroll
             for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[a])));
