@@ -258,7 +258,9 @@ uint64_t gbmd_hash_state(uint32_t dim, const int64_t* pos, const int32_t* vel, c
  * and division, used by the pair force for separations above sigma / 8, compared bit for bit
  * with CUDA's __frcp_rn / __fdiv_rn over every f32 of the reciprocal's range [2^50, 2^63), every
  * f32 r2 of each pair type's fast range through the whole LJ chain (PairConsts::eval,
- * crates/md-ref/src/real.rs:125-139), and `random_quotients` seeded random quotients. `checked`
+ * crates/md-ref/src/real.rs:125-139), and `random_quotients` seeded random quotients; for a single
+ * species with sigma = 1, also `random_quotients` random pairs of separations through the 3D force
+ * kernel's packed (f32x2) two-pair kicks against two scalar kicks. `checked`
  * receives the number of cases, `mismatched` those that differ (0 when the arithmetic holds). */
 int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quotients, int32_t device, uint64_t* checked, uint64_t* mismatched);
 

@@ -5,6 +5,7 @@
 
 #include "common.cuh"
 #include "engine.cuh"
+#include "kernels.cuh"
 
 using namespace gbmd;
 
@@ -62,6 +63,37 @@ __global__ void k_check_div(uint64_t count, uint32_t seed) {
     }
 }
 
+// Seeded random separations (|f| < 3 sigma per axis, in the f32 units of 2^-28 sigma): the
+// packed two-pair kicks of the 3D force kernel (pair_kicks2_sig1) equal two scalar pair kicks.
+__global__ void k_check_kicks2(PairC p, float cs, uint64_t count, uint32_t seed) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k - (k & 31u) < count; k += (uint64_t)gridDim.x * blockDim.x) {
+        bool bad = false;
+        if (k < count) {
+            float f[6];
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                uint32_t r0, r1;
+                threefry2x32((uint32_t)k, (uint32_t)(k >> 32) * 8u + (uint32_t)q, seed, 0xf2u, r0, r1);
+                f[2 * q] = (float)((int32_t)(r0 % (6u << 28)) - (int32_t)(3u << 28));
+                f[2 * q + 1] = (float)((int32_t)(r1 % (6u << 28)) - (int32_t)(3u << 28));
+            }
+            int32_t k1[3] = {0, 0, 0}, k2[3] = {0, 0, 0};
+            pair_kicks2_sig1(p, cs, f, f + 3, true, true, k1);
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                float fr, s6, rr;
+                if (pair_fr<3, true>(p, f + 3 * q, fr, s6, rr)) {
+                    const float am = __fmul_rn(-fr, cs);
+#pragma unroll
+                    for (int a = 0; a < 3; a++) k2[a] = wadd(k2[a], rni_f32(__fmul_rn(am, f[3 * q + a])));
+                }
+            }
+            bad = k1[0] != k2[0] || k1[1] != k2[1] || k1[2] != k2[2];
+        }
+        note_bad(bad);
+    }
+}
+
 } // namespace
 
 extern "C" int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quotients, int32_t device, uint64_t* checked,
@@ -100,6 +132,12 @@ extern "C" int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quot
     }
     if (rc == GBMD_OK && random_quotients) {
         k_check_div<<<grid, block, 0, s>>>(random_quotients, 20260u);
+        note_launch();
+        total += random_quotients;
+    }
+    // the packed two-pair kicks, for a single species with sigma = 1 (where the force kernel uses them)
+    if (rc == GBMD_OK && random_quotients && sys->nspecies == 1 && P.pc[0].sigma2s == 0x1p56f) {
+        k_check_kicks2<<<grid, block, 0, s>>>(P.pc[0], P.kick_cs[0], random_quotients, 7u);
         note_launch();
         total += random_quotients;
     }
