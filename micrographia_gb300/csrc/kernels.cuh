@@ -144,16 +144,19 @@ __device__ __forceinline__ void pair_f64(const double* c, double r2, double& u, 
     fr = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(24.0, eps), s6), __dsub_rn(__dmul_rn(2.0, s6), 1.0)), r2);
 }
 
-// Two directed pairs of one particle (3D, single species, sigma = 1) in packed f32x2 arithmetic:
+// Two directed pairs of one particle (single species, sigma = 1) in packed f32x2 arithmetic:
 // the same roundings as two pair_fr + kick calls. A pair that is not valid (a slot past the list
 // end) or beyond the cutoff gets a zero coefficient, and rint(0 f) adds nothing; a pack holding
 // an in-range pair closer than sigma / 8 takes the scalar chain (pair_fr) for both.
+template <int D>
 __device__ __forceinline__ void pair_kicks2_sig1(const PairC& pc, float cs, const float* fa, const float* fb, bool va, bool vb, int32_t* k) {
-    const f32x2 fx = f2_pack(fa[0], fb[0]), fy = f2_pack(fa[1], fb[1]), fz = f2_pack(fa[2], fb[2]);
     // r2 as sums of products: scalar (a packed mul feeding a packed add would be fused)
-    const float r2a = __fadd_rn(__fadd_rn(__fmul_rn(fa[0], fa[0]), __fmul_rn(fa[1], fa[1])), __fmul_rn(fa[2], fa[2]));
-    const float r2b = __fadd_rn(__fadd_rn(__fmul_rn(fb[0], fb[0]), __fmul_rn(fb[1], fb[1])), __fmul_rn(fb[2], fb[2]));
-    const f32x2 r2 = f2_pack(r2a, r2b);
+    float r2a = __fadd_rn(__fmul_rn(fa[0], fa[0]), __fmul_rn(fa[1], fa[1]));
+    float r2b = __fadd_rn(__fmul_rn(fb[0], fb[0]), __fmul_rn(fb[1], fb[1]));
+    if (D == 3) {
+        r2a = __fadd_rn(r2a, __fmul_rn(fa[2], fa[2]));
+        r2b = __fadd_rn(r2b, __fmul_rn(fb[2], fb[2]));
+    }
     const bool ina = va && r2a < pc.rc2s, inb = vb && r2b < pc.rc2s;
     if (!(ina || inb)) return;
     if ((ina && !(r2a >= pc.fast_lo)) || (inb && !(r2b >= pc.fast_lo))) {
@@ -162,15 +165,15 @@ __device__ __forceinline__ void pair_kicks2_sig1(const PairC& pc, float cs, cons
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             float fr, s6, rr;
-            if (ins[q] && pair_fr<3, true>(pc, fs[q], fr, s6, rr)) {
+            if (ins[q] && pair_fr<D, true>(pc, fs[q], fr, s6, rr)) {
                 const float am = __fmul_rn(-fr, cs);
 #pragma unroll
-                for (int a = 0; a < 3; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, fs[q][a])));
+                for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, fs[q][a])));
             }
         }
         return;
     }
-    const f32x2 nr2 = f2_pack(-r2a, -r2b);
+    const f32x2 r2 = f2_pack(r2a, r2b), nr2 = f2_pack(-r2a, -r2b);
     const f32x2 y = rcp_cr2(r2, nr2);
     const f32x2 s2 = f2_mul(y, f2_pack(0x1p56f, 0x1p56f));
     const f32x2 s6 = f2_mul(f2_mul(s2, s2), s2);
@@ -180,13 +183,12 @@ __device__ __forceinline__ void pair_kicks2_sig1(const PairC& pc, float cs, cons
     float ama, amb;
     f2_unpack(f2_mul(fr, f2_pack(-cs, -cs)), ama, amb);
     const f32x2 am = f2_pack(ina ? ama : 0.0f, inb ? amb : 0.0f);
-    float ka, kb;
-    f2_unpack(f2_mul(am, fx), ka, kb);
-    k[0] = wadd(k[0], wadd(rni_f32(ka), rni_f32(kb)));
-    f2_unpack(f2_mul(am, fy), ka, kb);
-    k[1] = wadd(k[1], wadd(rni_f32(ka), rni_f32(kb)));
-    f2_unpack(f2_mul(am, fz), ka, kb);
-    k[2] = wadd(k[2], wadd(rni_f32(ka), rni_f32(kb)));
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        float ka, kb;
+        f2_unpack(f2_mul(am, f2_pack(fa[a], fb[a])), ka, kb);
+        k[a] = wadd(k[a], wadd(rni_f32(ka), rni_f32(kb)));
+    }
 }
 
 // One directed pair (i from j): adds the integer kick rint(a * f) per axis, exactly
@@ -495,7 +497,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                     for (int a = 0; a < 3; a++) f[u][a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
                 }
 #pragma unroll
-                for (int h = 0; h < 2; h++) pair_kicks2_sig1(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
+                for (int h = 0; h < 2; h++) pair_kicks2_sig1<3>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
                 continue;
             }
 #pragma unroll
@@ -533,6 +535,23 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
             uint32_t sj[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) sj[u] = load_particle<D, MULTI>(pos_in, species, (uint32_t)u < left ? (jj[u] & LIST_MASK) : i, xj[u]);
+            if constexpr (!INT && !MULTI && SIG1) {
+                // as in 3D: separations per neighbour, then two packed pairs
+                float f[4][3];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t code = (uint32_t)u < left ? jj[u] >> LIST_BITS : 0u;
+#pragma unroll
+                    for (int a = 0; a < D; a++) {
+                        const uint32_t c = (code >> (2 * a)) & 3u;
+                        f[u][a] = sep_near(xj[u][a] + (c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0)) - xi[a]);
+                    }
+                    f[u][2] = 0.0f;
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++) pair_kicks2_sig1<D>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
+                continue;
+            }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 if ((uint32_t)u >= left) break;

@@ -64,7 +64,8 @@ __global__ void k_check_div(uint64_t count, uint32_t seed) {
 }
 
 // Seeded random separations (|f| < 3 sigma per axis, in the f32 units of 2^-28 sigma): the
-// packed two-pair kicks of the 3D force kernel (pair_kicks2_sig1) equal two scalar pair kicks.
+// packed two-pair kicks of the force kernel (pair_kicks2_sig1) equal two scalar pair kicks.
+template <int D>
 __global__ void k_check_kicks2(PairC p, float cs, uint64_t count, uint32_t seed) {
     for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k - (k & 31u) < count; k += (uint64_t)gridDim.x * blockDim.x) {
         bool bad = false;
@@ -77,15 +78,16 @@ __global__ void k_check_kicks2(PairC p, float cs, uint64_t count, uint32_t seed)
                 f[2 * q] = (float)((int32_t)(r0 % (6u << 28)) - (int32_t)(3u << 28));
                 f[2 * q + 1] = (float)((int32_t)(r1 % (6u << 28)) - (int32_t)(3u << 28));
             }
+            if (D == 2) f[2] = f[5] = 0.0f;
             int32_t k1[3] = {0, 0, 0}, k2[3] = {0, 0, 0};
-            pair_kicks2_sig1(p, cs, f, f + 3, true, true, k1);
+            pair_kicks2_sig1<D>(p, cs, f, f + 3, true, true, k1);
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 float fr, s6, rr;
-                if (pair_fr<3, true>(p, f + 3 * q, fr, s6, rr)) {
+                if (pair_fr<D, true>(p, f + 3 * q, fr, s6, rr)) {
                     const float am = __fmul_rn(-fr, cs);
 #pragma unroll
-                    for (int a = 0; a < 3; a++) k2[a] = wadd(k2[a], rni_f32(__fmul_rn(am, f[3 * q + a])));
+                    for (int a = 0; a < D; a++) k2[a] = wadd(k2[a], rni_f32(__fmul_rn(am, f[3 * q + a])));
                 }
             }
             bad = k1[0] != k2[0] || k1[1] != k2[1] || k1[2] != k2[2];
@@ -137,9 +139,10 @@ extern "C" int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quot
     }
     // the packed two-pair kicks, for a single species with sigma = 1 (where the force kernel uses them)
     if (rc == GBMD_OK && random_quotients && sys->nspecies == 1 && P.pc[0].sigma2s == 0x1p56f) {
-        k_check_kicks2<<<grid, block, 0, s>>>(P.pc[0], P.kick_cs[0], random_quotients, 7u);
-        note_launch();
-        total += random_quotients;
+        k_check_kicks2<3><<<grid, block, 0, s>>>(P.pc[0], P.kick_cs[0], random_quotients, 7u);
+        k_check_kicks2<2><<<grid, block, 0, s>>>(P.pc[0], P.kick_cs[0], random_quotients, 8u);
+        note_launch(2);
+        total += 2 * random_quotients;
     }
     unsigned long long bad = 0;
     if (rc == GBMD_OK && cudaMemcpyFromSymbolAsync(&bad, g_bad, 8, 0, cudaMemcpyDeviceToHost, s) != cudaSuccess)
