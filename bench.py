@@ -179,12 +179,18 @@ def cpu_baseline(seconds_budget=20.0, threads=None):
         e.step(1)
         done += 1
     dt = time.perf_counter() - t0
+    # one thread, as the reference's own bench times its CPU engine (bench/src/main.rs:279-298)
+    e1 = O.IntEngine(sys3, e.state, threads=1)
+    t1 = time.perf_counter()
+    e1.step(1)
+    dt1 = time.perf_counter() - t1
     return {
         "value": N_ATOMS * done / dt,
         "unit": UNIT,
         "cores": threads,
         "kind": "port",
         "sample": f"{done} full steps of the {N_ATOMS}-atom system after 1 warm-up step ({dt:.1f} s), IntEngine3<f32> reference loop",
+        "single_thread": {"value": N_ATOMS / dt1, "unit": UNIT, "sample": f"1 full step on one thread ({dt1:.1f} s)"},
     }
 
 
