@@ -33,7 +33,7 @@ __device__ double dev_log(double x) {
     int k = 0;
     if (hx < 0x00100000u || (hx >> 31) != 0) {
         if ((ui << 1) == 0) return -1.0 / (x * x);
-        if ((hx >> 31) != 0) return (x - x) / 0.0;
+        if ((hx >> 31) != 0) return __longlong_as_double((long long)0xfff8000000000000ull); // log(x < 0): NaN (fdlibm's (x - x) / 0)
         k -= 54;
         x *= 18014398509481984.0;
         ui = (uint64_t)__double_as_longlong(x);
@@ -247,7 +247,7 @@ struct Fcc3 {
     uint64_t seed;
 };
 // three::fcc (three.rs:319-343): sites in (z, y, x, basis) order.
-__global__ void k_fcc3(Fcc3 F, longlong4* pos) {
+__global__ void k_fcc3(Fcc3 F, longlong4_32a* pos) {
     uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= F.n) return;
     const double basis[4][3] = {{0.25, 0.25, 0.25}, {0.75, 0.75, 0.25}, {0.75, 0.25, 0.75}, {0.25, 0.75, 0.75}};
@@ -520,7 +520,7 @@ int init_state_device(const gbmd_system& sys, const gbmd_init& spec, void* pos_d
             }
             F.jitter = spec.jitter;
             F.seed = spec.seed;
-            k_fcc3<<<blocks(n, 256), 256, 0, s>>>(F, (longlong4*)pos_dev);
+            k_fcc3<<<blocks(n, 256), 256, 0, s>>>(F, (longlong4_32a*)pos_dev);
             note_launch();
             break;
         }

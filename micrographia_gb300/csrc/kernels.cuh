@@ -498,30 +498,30 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                 }
 #pragma unroll
                 for (int h = 0; h < 2; h++) pair_kicks2_sig1<3>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
-                continue;
-            }
+            } else {
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                if ((uint32_t)u >= left) break;
-                uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
-                uint32_t Rj[3] = {r[u].w & 15u, (r[u].w >> 8) & 15u, (r[u].w >> 16) & 15u};
-                const uint32_t code = jj[u] >> LIST_BITS;
-                if (code) {
+                for (int u = 0; u < 4; u++) {
+                    if ((uint32_t)u >= left) break;
+                    uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
+                    uint32_t Rj[3] = {r[u].w & 15u, (r[u].w >> 8) & 15u, (r[u].w >> 16) & 15u};
+                    const uint32_t code = jj[u] >> LIST_BITS;
+                    if (code) {
 #pragma unroll
-                    for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
-                }
-                if constexpr (INT) {
-                    // the exact separation from the records: d = 16 (Xj - Xi) + (rj - ri)
-                    int64_t d[3] = {0, 0, 0};
+                        for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
+                    }
+                    if constexpr (INT) {
+                        // the exact separation from the records: d = 16 (Xj - Xi) + (rj - ri)
+                        int64_t d[3] = {0, 0, 0};
 #pragma unroll
-                    for (int a = 0; a < D; a++)
-                        d[a] = (int64_t)(int32_t)(Xj[a] - Xi[a]) * 16 + ((int64_t)Rj[a] - (int64_t)((qi.w >> (8 * a)) & 15u));
-                    int_kick<D>(P, MULTI ? si * P.ns + (r[u].w >> 24) : 0u, d, k);
-                } else {
-                    float f[D];
+                        for (int a = 0; a < D; a++)
+                            d[a] = (int64_t)(int32_t)(Xj[a] - Xi[a]) * 16 + ((int64_t)Rj[a] - (int64_t)((qi.w >> (8 * a)) & 15u));
+                        int_kick<D>(P, MULTI ? si * P.ns + (r[u].w >> 24) : 0u, d, k);
+                    } else {
+                        float f[D];
 #pragma unroll
-                    for (int a = 0; a < D; a++) f[a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
-                    add_kick(f, MULTI ? P.pc[si * P.ns + (r[u].w >> 24)] : pc0);
+                        for (int a = 0; a < D; a++) f[a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
+                        add_kick(f, MULTI ? P.pc[si * P.ns + (r[u].w >> 24)] : pc0);
+                    }
                 }
             }
         }
@@ -550,29 +550,29 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                 }
 #pragma unroll
                 for (int h = 0; h < 2; h++) pair_kicks2_sig1<D>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
-                continue;
-            }
+            } else {
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                if ((uint32_t)u >= left) break;
-                const uint32_t code = jj[u] >> LIST_BITS;
-                if constexpr (INT) {
-                    int64_t d[3] = {0, 0, 0};
+                for (int u = 0; u < 4; u++) {
+                    if ((uint32_t)u >= left) break;
+                    const uint32_t code = jj[u] >> LIST_BITS;
+                    if constexpr (INT) {
+                        int64_t d[3] = {0, 0, 0};
 #pragma unroll
-                    for (int a = 0; a < D; a++) {
-                        uint32_t c = (code >> (2 * a)) & 3u;
-                        d[a] = xj[u][a] + (c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0)) - xi[a];
+                        for (int a = 0; a < D; a++) {
+                            uint32_t c = (code >> (2 * a)) & 3u;
+                            d[a] = xj[u][a] + (c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0)) - xi[a];
+                        }
+                        int_kick<D>(P, MULTI ? si * P.ns + sj[u] : 0u, d, k);
+                    } else {
+                        float f[D];
+#pragma unroll
+                        for (int a = 0; a < D; a++) {
+                            uint32_t c = (code >> (2 * a)) & 3u;
+                            int64_t img = c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0);
+                            f[a] = sep_near(xj[u][a] + img - xi[a]);
+                        }
+                        add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
                     }
-                    int_kick<D>(P, MULTI ? si * P.ns + sj[u] : 0u, d, k);
-                } else {
-                    float f[D];
-#pragma unroll
-                    for (int a = 0; a < D; a++) {
-                        uint32_t c = (code >> (2 * a)) & 3u;
-                        int64_t img = c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0);
-                        f[a] = sep_near(xj[u][a] + img - xi[a]);
-                    }
-                    add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
                 }
             }
         }
