@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
 }
 
 // Persistent fused force + leapfrog over every particle of every system.
-template <int D, bool MULTI>
+template <int D, bool MULTI, bool SIG1>
 __global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx,
                                                      const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
                                                      int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
@@ -145,7 +145,25 @@ __global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, const Params* _
         const PairC pc0 = P.pc[0];
         int32_t k[3] = {0, 0, 0};
         const uint32_t m = __ldg(nbr_count + i);
-        for (uint32_t q = 0; q < m; q++) {
+        uint32_t q = 0;
+        if constexpr (!MULTI && SIG1) {
+            // neighbours two at a time through the packed f32x2 chain (pair_kicks2_sig1)
+            for (; q + 1 < m; q += 2) {
+                const uint32_t j0 = __ldg(nbr + (size_t)q * N + i), j1 = __ldg(nbr + (size_t)(q + 1) * N + i);
+                int64_t x0[3], x1[3];
+                load_particle<D, false>(pos_in, nullptr, j0, x0);
+                load_particle<D, false>(pos_in, nullptr, j1, x1);
+                float f0[3] = {0.0f, 0.0f, 0.0f}, f1[3] = {0.0f, 0.0f, 0.0f};
+                bool ok0 = true, ok1 = true;
+#pragma unroll
+                for (int a = 0; a < D; a++) {
+                    f0[a] = sep_s(min_image(x0[a] - xi[a], G.box[a], G.half[a]), ok0);
+                    f1[a] = sep_s(min_image(x1[a] - xi[a], G.box[a], G.half[a]), ok1);
+                }
+                pair_kicks2_sig1<D>(pc0, cs, f0, f1, ok0, ok1, k);
+            }
+        }
+        for (; q < m; q++) {
             uint32_t j = __ldg(nbr + (size_t)q * N + i);
             int64_t xj[3];
             uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
@@ -208,6 +226,7 @@ struct gbmd_batch {
     uint32_t K = 0, N = 0;
     int D = 2;
     bool multi = false;
+    bool sig1 = false; // every pair type sigma = 1 (and one species): the packed force path
     std::vector<gbmd_system> sys;
     std::vector<uint32_t> offsets;
     std::vector<Params> P;
@@ -271,8 +290,14 @@ void benqueue_rebuild(gbmd_batch* b, cudaStream_t s) {
     else b->multi ? benqueue_rebuild_t<3, true>(b, s) : benqueue_rebuild_t<3, false>(b, s);
 }
 template <int D, bool MULTI> void benqueue_force_t(gbmd_batch* b, cudaStream_t s) {
-    k_bforce_list<D, MULTI><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur], (PosRec<D>*)b->pos[b->cur ^ 1],
-                                                   b->vel, b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
+    if (b->sig1)
+        k_bforce_list<D, MULTI, true><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
+                                                              (PosRec<D>*)b->pos[b->cur ^ 1], b->vel, b->species, b->nbr, b->nbr_count,
+                                                              (const PosRec<D>*)b->ref_pos, b->ctl);
+    else
+        k_bforce_list<D, MULTI, false><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
+                                                               (PosRec<D>*)b->pos[b->cur ^ 1], b->vel, b->species, b->nbr, b->nbr_count,
+                                                               (const PosRec<D>*)b->ref_pos, b->ctl);
     note_launch();
     b->cur ^= 1;
 }
@@ -414,8 +439,19 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     step(cudaSetDevice(o.device) == cudaSuccess ? GBMD_OK : fail(GBMD_E_CUDA, "cudaSetDevice"));
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, o.device);
     int occ = 0;
-    if (D == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<2, true> : k_bforce_list<2, false>, 128, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<3, true> : k_bforce_list<3, false>, 128, 0);
+    // every pair type of every system with sigma = 1: the packed chain with sigma compiled in
+    b->sig1 = !b->multi;
+    for (uint32_t k = 0; k < count; k++)
+        for (uint32_t q = 0; q < b->P[k].ns * b->P[k].ns; q++) b->sig1 = b->sig1 && b->P[k].pc[q].sigma2s == 0x1p56f;
+    // the persistent grid: as many blocks as stay resident for the variant that will run
+    if (D == 2)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<2, true, false>
+                                                                     : (b->sig1 ? k_bforce_list<2, false, true> : k_bforce_list<2, false, false>),
+                                                      128, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<3, true, false>
+                                                                     : (b->sig1 ? k_bforce_list<3, false, true> : k_bforce_list<3, false, false>),
+                                                      128, 0);
     b->grid = std::max<uint32_t>(1, std::min<uint32_t>(nblocks(b->N, 128), (uint32_t)std::max(dev_sms, 1) * (uint32_t)std::max(occ, 1)));
     if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
     if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st_body, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
