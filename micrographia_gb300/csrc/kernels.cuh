@@ -360,6 +360,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     cell_coords(P, keys[i], c);
     uint32_t count = 0;
     const uint32_t cap = P.cap, cap4 = (P.cap + 3u) & ~3u;
+    const size_t lbase = list_slot(i, 0, cap4); // entry k at lbase + (k & ~3) 32 + (k & 3)
     const bool unchecked = P.sep_unchecked;
     // Candidate j of a neighbour cell cj sits at d = relf[j] + base: base = (cj - c) cell_w + shift
     // - (xi - c cell_w), an exact integer converted once per cell. Outside [lo, hi] the f32
@@ -404,15 +405,17 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                 const float b1 = __fmul_rn(__ll2float_rn(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]), 1.0f / 4294967296.0f);
                 const float b2 = D == 3 ? __fmul_rn(__ll2float_rn(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]), 1.0f / 4294967296.0f) : 0.0f;
                 uint32_t j0 = __ldg(start + cell), j1 = __ldg(start + cell + 1);
+#pragma unroll 2
                 for (uint32_t j = j0; j < j1; j++) {
                     float4 r = __ldg(relf + j);
                     float dx = r.x + b0, dy = r.y + b1, dz = r.z + b2;
-                    float r2a = dx * dx + dy * dy + dz * dz;
+                    // approximate (fused) distance: its error is far inside the 1e-4 band
+                    float r2a = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
                     uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
                     float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
                     bool in = r2a < lo || (r2a <= hi && exact(j, xs, sj));
                     if (in && j != i) {
-                        if (count < cap) nbr[list_slot(i, count, cap4)] = j | code;
+                        if (count < cap) nbr[lbase + ((size_t)(count & ~3u) << 5) + (count & 3u)] = j | code;
                         count++;
                     }
                 }
