@@ -68,16 +68,21 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per force launch from the committed ncu summary, if present."""
+def profile_figure(key):
+    """A figure of the committed ncu summary of the force kernel (`key: value` lines), if present."""
     path = os.path.join(ROOT, "profiles", "k_force_list_3d.md")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch_full_size:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].split()[0])
     except Exception:
         pass
     return None
+
+
+def profile_traffic():
+    """DRAM bytes per force launch from the committed ncu summary, if present."""
+    return profile_figure("dram_bytes_per_launch_full_size")
 
 
 class ClockSampler:
@@ -334,6 +339,12 @@ def run_ours(args, world, rank, local, pg):
             "unit": "GB/s",
             "frac": achieved / peaks.get("hbm_gbs", 6800.0),
             "traffic": traffic,
+            "pipes_ncu_pct": {
+                "issue_active": profile_figure("issue_active_pct"),
+                "alu": profile_figure("alu_pipe_pct"),
+                "fp32": profile_figure("fp32_pipe_pct"),
+                "note": "the kernel is bound by the integer ALU pipe and instruction issue (profiles/k_force_list_3d.md)",
+            },
             "algorithmic_bytes_per_atom_step": B,
             "n_list": n_list,
             "force_ms": f_ms.value,

@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                 const float b1 = __fmul_rn(__ll2float_rn(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]), 1.0f / 4294967296.0f);
                 const float b2 = D == 3 ? __fmul_rn(__ll2float_rn(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]), 1.0f / 4294967296.0f) : 0.0f;
                 uint32_t j0 = __ldg(start + cell), j1 = __ldg(start + cell + 1);
-#pragma unroll 2
+#pragma unroll 4
                 for (uint32_t j = j0; j < j1; j++) {
                     float4 r = __ldg(relf + j);
                     float dx = r.x + b0, dy = r.y + b1, dz = r.z + b2;
