@@ -183,6 +183,7 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
         P.gravity[a] = v != v ? 0 : (v >= 2147483647.0 ? INT32_MAX : (v <= -2147483648.0 ? INT32_MIN : (int32_t)v));
     }
     P.pinned = s.pinned;
+    P.one = 1;
     double hs = 0.5 * skin * (1.0 - 1e-3);
     P.half_skin2s = scale2((float)(hs * hs), 56);
     P.dt = s.dt;

@@ -338,6 +338,16 @@ __device__ __forceinline__ float quot_sep(uint32_t Xj, uint32_t rj, uint32_t Xi,
     int32_t q = f + ((f < 0 && rj != ri) ? 1 : 0);
     return __int2float_rn(q);
 }
+// The same with Xj - Xi formed as an integer multiply-add Xj * one + nXi (one = 1 from the
+// parameter block, nXi = -Xi), which issues on the FMA pipe instead of the integer ALU pipe that
+// bounds the force kernel.
+__device__ __forceinline__ float quot_sep_mad(uint32_t Xj, uint32_t rj, uint32_t nXi, uint32_t ri, uint32_t one) {
+    uint32_t d;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(Xj), "r"(one), "r"(nXi));
+    int32_t f = (int32_t)d - (rj < ri ? 1 : 0);
+    int32_t q = f + ((f < 0 && rj != ri) ? 1 : 0);
+    return __int2float_rn(q);
+}
 
 // Verlet-list build over the cell-sorted scratch state (neighbors.wgsl:27-64 with the exact f32
 // test of engine.rs:302-313 / 184-186): lists are warp-tiled (list_slot); a particle with
@@ -497,7 +507,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                         for (int a = 0; a < 3; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
                     }
 #pragma unroll
-                    for (int a = 0; a < 3; a++) f[u][a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
+                    for (int a = 0; a < 3; a++) f[u][a] = quot_sep_mad(Xj[a], Rj[a], 0u - Xi[a], (qi.w >> (8 * a)) & 15u, P.one);
                 }
 #pragma unroll
                 for (int h = 0; h < 2; h++) pair_kicks2_sig1<3>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
