@@ -500,7 +500,8 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
-                    uint32_t Rj[3] = {r[u].w & 15u, (r[u].w >> 8) & 15u, (r[u].w >> 16) & 15u};
+                    // the remainders are whole bytes of the fourth word: one byte select each
+                    uint32_t Rj[3] = {__byte_perm(r[u].w, 0u, 0x4440u), __byte_perm(r[u].w, 0u, 0x4441u), __byte_perm(r[u].w, 0u, 0x4442u)};
                     const uint32_t code = jj[u] >> LIST_BITS;
                     if (code && (uint32_t)u < left) {
 #pragma unroll
