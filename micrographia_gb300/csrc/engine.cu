@@ -262,7 +262,7 @@ struct gbmd_engine {
     uint32_t *hist = nullptr, *scan_tmp = nullptr, *start = nullptr;
     uint32_t *nbr = nullptr, *nbr_count = nullptr;
     float4* relf = nullptr;  // cell-relative f32 coordinates of the sorted scratch state
-    uint4* qpos[2] = {nullptr, nullptr}; // 3D quotient records of the positions (ping-pong)
+    uint4* qpos[2] = {nullptr, nullptr}; // quotient records of the positions (ping-pong)
     uint32_t* ctl = nullptr; // [0] rebuild, [1] overflow, [2] rebuilds
     double* partial = nullptr;
     void* staging = nullptr;  // id-ordered I/O staging (n * D int64)

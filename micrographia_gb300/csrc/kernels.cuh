@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     nbr_count[i] = count;
     pos_o[i] = pos_s[i];
     ref_pos[i] = pos_s[i];
-    if (D == 3 && qpos_o) qpos_o[i] = quot_record<D>(xi, si);
+    if (qpos_o) qpos_o[i] = quot_record<D>(xi, si);
 #pragma unroll
     for (int a = 0; a < D; a++) vel_o[D * i + a] = vel_s[D * i + a];
     species_o[i] = species_s[i];
@@ -477,10 +477,10 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
         }
     };
     const uint32_t ngroups = (m + 3u) >> 2;
-    if constexpr (D == 3) {
+    {
         // Neighbours come from the 16-byte quotient records (one gather each) and the separation
         // is formed with 32-bit integers (quot_sep); a neighbour listed at a periodic image has
-        // its quotient record shifted by that image exactly (quot_shift).
+        // its quotient record shifted by that image exactly (quot_shift). 2D and 3D alike.
         const uint4 qi = __ldg(qpos_in + i);
         const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
         for (uint32_t g = 0; g < ngroups; g++) {
@@ -505,13 +505,14 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                     const uint32_t code = jj[u] >> LIST_BITS;
                     if (code && (uint32_t)u < left) {
 #pragma unroll
-                        for (int a = 0; a < 3; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
+                        for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
                     }
 #pragma unroll
-                    for (int a = 0; a < 3; a++) f[u][a] = quot_sep_mad(Xj[a], Rj[a], 0u - Xi[a], (qi.w >> (8 * a)) & 15u, P.one);
+                    for (int a = 0; a < D; a++) f[u][a] = quot_sep_mad(Xj[a], Rj[a], 0u - Xi[a], (qi.w >> (8 * a)) & 15u, P.one);
+                    if (D == 2) f[u][2] = 0.0f;
                 }
 #pragma unroll
-                for (int h = 0; h < 2; h++) pair_kicks2_sig1<3>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
+                for (int h = 0; h < 2; h++) pair_kicks2_sig1<D>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
             } else {
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
@@ -539,57 +540,6 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                 }
             }
         }
-    } else {
-        for (uint32_t g = 0; g < ngroups; g++) {
-            if (g + 2 < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2)));
-            const uint4 jv = __ldg(groups + 32 * g);
-            const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
-            const uint32_t left = m - 4 * g;
-            int64_t xj[4][3];
-            uint32_t sj[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) sj[u] = load_particle<D, MULTI>(pos_in, species, (uint32_t)u < left ? (jj[u] & LIST_MASK) : i, xj[u]);
-            if constexpr (!INT && !MULTI && SIG1) {
-                // as in 3D: separations per neighbour, then two packed pairs
-                float f[4][3];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const uint32_t code = (uint32_t)u < left ? jj[u] >> LIST_BITS : 0u;
-#pragma unroll
-                    for (int a = 0; a < D; a++) {
-                        const uint32_t c = (code >> (2 * a)) & 3u;
-                        f[u][a] = sep_near(xj[u][a] + (c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0)) - xi[a]);
-                    }
-                    f[u][2] = 0.0f;
-                }
-#pragma unroll
-                for (int h = 0; h < 2; h++) pair_kicks2_sig1<D>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
-            } else {
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if ((uint32_t)u >= left) break;
-                    const uint32_t code = jj[u] >> LIST_BITS;
-                    if constexpr (INT) {
-                        int64_t d[3] = {0, 0, 0};
-#pragma unroll
-                        for (int a = 0; a < D; a++) {
-                            uint32_t c = (code >> (2 * a)) & 3u;
-                            d[a] = xj[u][a] + (c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0)) - xi[a];
-                        }
-                        int_kick<D>(P, MULTI ? si * P.ns + sj[u] : 0u, d, k);
-                    } else {
-                        float f[D];
-#pragma unroll
-                        for (int a = 0; a < D; a++) {
-                            uint32_t c = (code >> (2 * a)) & 3u;
-                            int64_t img = c == 1u ? P.box[a] : (c == 2u ? -P.box[a] : 0);
-                            f[a] = sep_near(xj[u][a] + img - xi[a]);
-                        }
-                        add_kick(f, MULTI ? P.pc[si * P.ns + sj[u]] : pc0);
-                    }
-                }
-            }
-        }
     }
     int32_t v[3];
 #pragma unroll
@@ -598,7 +548,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
 #pragma unroll
     for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
     store_pos<D>(pos_out, i, xi, si);
-    if (D == 3) qpos_out[i] = quot_record<D>(xi, si);
+    qpos_out[i] = quot_record<D>(xi, si);
     int64_t xr[3];
     load_particle<D, false>(ref_pos, nullptr, i, xr);
     if (moved_half_skin<D>(P, xr, xi)) ctl[0] = 1;
