@@ -539,25 +539,34 @@ def run_c5(args, world, rank, local, pg):
     reqs = replicas.shard(workloads.config5(args.requests, args.rate), rank, world)
     steps = args.steps
 
+    # frame times per request (by its place in the stream): served deliveries, and the solo
+    # schedule S_k = time from the start of service to frame k when the request runs alone
+    served_at = [[] for _ in reqs]
+    arrival = [t for t, _, _ in reqs]
+    solo = [[] for _ in reqs]
+    start_plain = [0.0] * len(reqs)
+
     def serve():
-        frames_lat, done, t_arr, t_prev = [], 0, {}, {}
+        frames_lat, done, t_arr, t_prev, order = [], 0, {}, {}, {}
         sv = Server(64 << 30, max_active=64, device=local)
         t0 = time.perf_counter()
-        pending = list(reqs)
+        pending = list(enumerate(reqs))
         total = 0
         while done < len(reqs):
             now = time.perf_counter() - t0
-            while pending and pending[0][0] <= now:
-                _, s, spec = pending.pop(0)
+            while pending and pending[0][1][0] <= now:
+                idx, (_, s, spec) = pending.pop(0)
                 rid = sv.submit(s, spec, steps=steps, frame_every=100, rdf_bins=200, rdf_rmax=5.0)
                 t_arr[rid] = time.perf_counter() - t0
                 t_prev[rid] = t_arr[rid]
+                order[rid] = idx
                 total += spec.n * steps
             got = sv.poll()
             tnow = time.perf_counter() - t0
             for f in got:
                 frames_lat.append(tnow - t_prev[f.request])
                 t_prev[f.request] = tnow
+                served_at[order[f.request]].append(tnow)
                 if f.last:
                     done += 1
             if not got:
@@ -570,10 +579,12 @@ def run_c5(args, world, rank, local, pg):
         frames_lat = []
         t0 = time.perf_counter()
         total = 0
-        for t_a, s, spec in reqs:
+        for idx, (t_a, s, spec) in enumerate(reqs):
             while time.perf_counter() - t0 < t_a:
                 time.sleep(0.0005)
             t_prev = t0 + t_a  # the first frame's wait counts from the request's arrival
+            t_start = time.perf_counter()
+            start_plain[idx] = t_start - t0
             cls = GpuEngine if s.DIM == 2 else GpuEngine3
             e = cls(s, None, ForceMode.verlet_with_skin(s, spec.n, SKIN), init=spec, block_steps=100, device=local)
             for _ in range(0, steps, 100):
@@ -581,6 +592,7 @@ def run_c5(args, world, rank, local, pg):
                 e.observe(rdf_bins=200, rdf_rmax=5.0)
                 t = time.perf_counter()
                 frames_lat.append(t - t_prev)
+                solo[idx].append(t - t_start)
                 t_prev = t
             e.close()
             total += spec.n * steps
@@ -589,6 +601,11 @@ def run_c5(args, world, rank, local, pg):
 
     v_serve, mk_serve, lat_serve = serve()
     v_serial, mk_serial, lat_serial = serial()
+    # lateness: delivery minus the frame's due time in the request's own schedule (arrival + S_k)
+    late_serve = [served_at[q][k] - (arrival[q] + solo[q][k]) for q in range(len(reqs)) for k in range(min(len(served_at[q]), len(solo[q])))]
+    late_serial = [start_plain[q] - arrival[q] for q in range(len(reqs)) for _ in solo[q]]
+    late_serve = replicas.gather(pg, late_serve)
+    late_serial = replicas.gather(pg, late_serial)
     # whole job over ranks: atom-steps summed, makespans maxed, latencies pooled
     u, mk_serve = replicas.aggregate(pg, v_serve * mk_serve, mk_serve)
     v_serve = u / mk_serve
@@ -615,6 +632,11 @@ def run_c5(args, world, rank, local, pg):
             "makespan_s": mk_serve,
             "frame_latency_p50_ms": 1e3 * _pct(lat_serve, 50),
             "frame_latency_p99_ms": 1e3 * _pct(lat_serve, 99),
+            "frame_lateness_p50_ms": 1e3 * _pct(late_serve, 50),
+            "frame_lateness_p99_ms": 1e3 * _pct(late_serve, 99),
+            "plain_frame_lateness_p50_ms": 1e3 * _pct(late_serial, 50),
+            "plain_frame_lateness_p99_ms": 1e3 * _pct(late_serial, 99),
+            "latency_definitions": "latency: wait for each frame after the previous one of its request (the first from arrival); lateness: delivery minus the frame's due time in the request's own schedule, arrival + the time the frame took from the start of service when the request ran alone (the plain arm's runs)",
             "plain_value": v_serial,
             "plain_makespan_s": mk_serial,
             "plain_frame_latency_p50_ms": 1e3 * _pct(lat_serial, 50),

@@ -149,6 +149,12 @@ int gbmd_energy(gbmd_engine* e, double* kinetic, double* potential);
  * `profile_bins` particle counts along `profile_axis`. */
 int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint32_t rdf_bins,
                  double rdf_rmax, uint64_t* profile, uint32_t profile_bins, uint32_t profile_axis);
+/* gbmd_observe in two halves, for callers that overlap frames with other work: _begin enqueues
+ * the frame's kernels and copies on the engine's stream and returns at once (0 bins: no RDF /
+ * no profile); _end waits for them (at once if an event recorded after _begin has completed)
+ * and fills `frame`, `rdf` (rdf_bins counts) and `profile`. One frame in flight per engine. */
+int gbmd_observe_begin(gbmd_engine* e, uint32_t rdf_bins, double rdf_rmax, uint32_t profile_bins, uint32_t profile_axis);
+int gbmd_observe_end(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint64_t* profile);
 
 /* ---- Diagnostics ---- */
 

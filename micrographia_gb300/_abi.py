@@ -156,6 +156,8 @@ SIGNATURES = [
     ("gbmd_flip_bit", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32]),
     ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
     ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),
+    ("gbmd_observe_begin", C.c_int, [VP, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32]),
+    ("gbmd_observe_end", C.c_int, [VP, P(gbmd_frame), _U64P, _U64P]),
     ("gbmd_list_stats", C.c_int, [VP, _U32P, _I32P]),
     ("gbmd_state_hash", C.c_int, [VP, _U64P]),
     ("gbmd_counters", C.c_int, [VP, _I64P, _U32P]),

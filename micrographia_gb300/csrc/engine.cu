@@ -12,6 +12,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -274,9 +276,10 @@ struct gbmd_engine {
     int64_t steps = 0;
     uint32_t clock = 0;
     uint32_t block_steps = 64;
-    // graphs per [parity][kind]: 0 one step, 1 a block of block_steps, 2 one step + thermostat
-    cudaGraphExec_t exec[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
-    uint64_t exec_launches[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    // graphs per [parity][kind]: 0 one step, 1 a block of block_steps, 2 one step + thermostat,
+    // 3 the conditional list rebuild alone (frames and kicks between steps)
+    cudaGraphExec_t exec[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
+    uint64_t exec_launches[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     // velocity-rescale thermostat (every `rescale_every` steps)
     uint32_t* mrank = nullptr;          // rank of each id among the moving particles
     unsigned long long* tpart = nullptr; // exact KE partials
@@ -296,32 +299,85 @@ struct gbmd_engine {
     size_t obs_bins_cap = 0;
     uint32_t* obs_start = nullptr;
     size_t obs_start_cap = 0;
+    // a frame in flight (gbmd_observe_begin .. gbmd_observe_end): results land in pinned memory
+    double* obs_part_h = nullptr;
+    size_t obs_part_cap = 0;
+    unsigned long long* obs_bins_h = nullptr;
+    size_t obs_bins_h_cap = 0;
+    bool obs_pending = false;
+    uint32_t obs_rdf_bins = 0, obs_profile_bins = 0, obs_nb = 0;
 };
 
 namespace {
 
 template <int D> using Rec = PosRec<D>;
 
-int alloc(void** p, size_t bytes) {
+// Engine memory comes from the stream-ordered allocator on the engine's own stream, and goes back
+// to it the same way: creating and destroying engines (a server does so per request) never
+// synchronises the device with other engines' work. The device's default pool keeps what is
+// freed for the next engine (release threshold raised once per device).
+static void keep_pool_memory(int device) {
+    static std::mutex mu;
+    static bool done[256] = {false};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= 256 || done[device]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done[device] = true;
+}
+int alloc(gbmd_engine* e, void** p, size_t bytes) {
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GBMD_E_NOMEM : GBMD_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    cudaError_t r = cudaMallocAsync(p, bytes, e->st);
+    if (r != cudaSuccess) return fail(r == cudaErrorMemoryAllocation ? GBMD_E_NOMEM : GBMD_E_CUDA, std::string("cudaMallocAsync: ") + cudaGetErrorString(r));
     return GBMD_OK;
 }
-template <typename T> int allocT(T** p, size_t count) { return alloc((void**)p, count * sizeof(T)); }
+template <typename T> int allocT(gbmd_engine* e, T** p, size_t count) { return alloc(e, (void**)p, count * sizeof(T)); }
+
+// Pinned host memory for frames, from a process-wide pool that is never freed (freeing pinned
+// memory synchronises the device): blocks of a power-of-two size, handed out and taken back.
+static std::mutex g_pin_mu;
+static std::map<size_t, std::vector<void*>> g_pin_free;
+static size_t pin_class(size_t bytes) {
+    size_t c = 4096;
+    while (c < bytes) c <<= 1;
+    return c;
+}
+static void* pinned_take(size_t cls) {
+    {
+        std::lock_guard<std::mutex> lock(g_pin_mu);
+        auto it = g_pin_free.find(cls);
+        if (it != g_pin_free.end() && !it->second.empty()) {
+            void* p = it->second.back();
+            it->second.pop_back();
+            return p;
+        }
+    }
+    void* p = nullptr;
+    return cudaHostAlloc(&p, cls, cudaHostAllocDefault) == cudaSuccess ? p : nullptr;
+}
+static void pinned_give(void* p, size_t cls) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_pin_mu);
+    g_pin_free[cls].push_back(p);
+}
 
 void free_all(gbmd_engine* e) {
     for (int p = 0; p < 2; p++)
-        for (int b = 0; b < 3; b++)
+        for (int b = 0; b < 4; b++)
             if (e->exec[p][b]) cudaGraphExecDestroy(e->exec[p][b]);
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
                     e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1],
                     e->obs_bins, e->obs_start, e->itab, e->ipair};
     for (void* p : ptrs)
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, e->st);
     if (e->st) cudaStreamDestroy(e->st);
     if (e->st_body) cudaStreamDestroy(e->st_body);
+    pinned_give(e->obs_part_h, e->obs_part_cap);
+    pinned_give(e->obs_bins_h, e->obs_bins_h_cap);
 }
 
 // ---- enqueue helpers (stream-ordered; also used under capture)
@@ -445,7 +501,7 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, int kind, cudaGrap
     cudaStream_t s = e->st;
     GBMD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     uint64_t body = 0;
-    for (uint32_t k = 0; k < count; k++) {
+    for (uint32_t k = 0; k < (kind == 3 ? 1u : count); k++) {
         if (e->verlet) {
             cudaStreamCaptureStatus status;
             cudaGraph_t g;
@@ -475,6 +531,7 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, int kind, cudaGrap
             GBMD_CUDA_TRY(cudaStreamEndCapture(e->st_body, &tmp));
             GBMD_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
         }
+        if (kind == 3) break; // the conditional rebuild alone
         enqueue_force(e, s);
         uint32_t every = e->opt.rescale_every;
         if ((kind == 1 && every && (k + 1) % every == 0) || kind == 2) enqueue_thermo(e, s);
@@ -500,7 +557,7 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, int kind, cudaGrap
 
 int run_graph(gbmd_engine* e, int which) {
     int parity = e->cur;
-    uint32_t count = which == 1 ? e->block_steps : 1;
+    uint32_t count = which == 1 ? e->block_steps : (which == 3 ? 0u : 1u);
     if (!e->exec[parity][which]) {
         GBMD_TRY(capture_steps(e, parity, count, which, &e->exec[parity][which], &e->exec_launches[parity][which]));
     }
@@ -512,8 +569,20 @@ int run_graph(gbmd_engine* e, int which) {
     return GBMD_OK;
 }
 
-// Bring the pair structure up to date with the current positions (for kicks/observables):
-// a Verlet list is rebuilt, a cell list binned into the scratch state.
+// Bring the pair structure up to date for kicks and observables between steps: a Verlet list is
+// rebuilt only if the displacement trigger has fired since the last build (the same device flag
+// and conditional graph node the steps use), a cell list binned into the scratch state.
+int prepare_pairs_cond(gbmd_engine* e) {
+    if (!e->verlet) {
+        if (e->D == 2) enqueue_bin<2>(e, e->st, e->P);
+        else enqueue_bin<3>(e, e->st, e->P);
+        GBMD_CUDA_TRY(cudaGetLastError());
+        return GBMD_OK;
+    }
+    return run_graph(e, 3);
+}
+// The same with the Verlet list always rebuilt (the positions wrapped into the box, the
+// storage re-sorted).
 int prepare_pairs(gbmd_engine* e) {
     if (e->verlet) {
         enqueue_rebuild(e, e->st);
@@ -684,40 +753,41 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     }
     e->thermo_nb = std::min<uint32_t>(std::max<uint32_t>(blocks_for(n, 256), 1), 512);
     GBMD_CUDA_TRY(cudaSetDevice(e->opt.device));
+    keep_pool_memory(e->opt.device);
     GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
     GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st_body, cudaStreamNonBlocking));
     size_t D = e->D;
-    GBMD_TRY(alloc(&e->pos[0], n * e->rec));
-    GBMD_TRY(alloc(&e->pos[1], n * e->rec));
-    GBMD_TRY(alloc(&e->pos_scr, n * e->rec));
-    GBMD_TRY(alloc(&e->ref_pos, n * e->rec));
-    GBMD_TRY(allocT(&e->vel, n * D));
-    GBMD_TRY(allocT(&e->vel_scr, n * D));
-    GBMD_TRY(allocT(&e->kicks, n * D));
-    GBMD_TRY(allocT(&e->species, n));
-    GBMD_TRY(allocT(&e->species_scr, n));
-    GBMD_TRY(allocT(&e->ids, n));
-    GBMD_TRY(allocT(&e->ids_scr, n));
+    GBMD_TRY(alloc(e, &e->pos[0], n * e->rec));
+    GBMD_TRY(alloc(e, &e->pos[1], n * e->rec));
+    GBMD_TRY(alloc(e, &e->pos_scr, n * e->rec));
+    GBMD_TRY(alloc(e, &e->ref_pos, n * e->rec));
+    GBMD_TRY(allocT(e, &e->vel, n * D));
+    GBMD_TRY(allocT(e, &e->vel_scr, n * D));
+    GBMD_TRY(allocT(e, &e->kicks, n * D));
+    GBMD_TRY(allocT(e, &e->species, n));
+    GBMD_TRY(allocT(e, &e->species_scr, n));
+    GBMD_TRY(allocT(e, &e->ids, n));
+    GBMD_TRY(allocT(e, &e->ids_scr, n));
     for (int b = 0; b < 2; b++) {
-        GBMD_TRY(allocT(&e->keys[b], n));
-        GBMD_TRY(allocT(&e->vals[b], n));
+        GBMD_TRY(allocT(e, &e->keys[b], n));
+        GBMD_TRY(allocT(e, &e->vals[b], n));
     }
     size_t hist_n = radix_hist_elems(n);
-    GBMD_TRY(allocT(&e->hist, hist_n));
-    GBMD_TRY(allocT(&e->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(n))));
-    GBMD_TRY(allocT(&e->start, (size_t)e->P.ncell + 1));
+    GBMD_TRY(allocT(e, &e->hist, hist_n));
+    GBMD_TRY(allocT(e, &e->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(n))));
+    GBMD_TRY(allocT(e, &e->start, (size_t)e->P.ncell + 1));
     if (e->verlet) {
-        GBMD_TRY(allocT(&e->nbr, ((size_t)n + 31) / 32 * 32 * (((size_t)cap + 3) & ~(size_t)3)));
-        GBMD_TRY(allocT(&e->nbr_count, n));
+        GBMD_TRY(allocT(e, &e->nbr, ((size_t)n + 31) / 32 * 32 * (((size_t)cap + 3) & ~(size_t)3)));
+        GBMD_TRY(allocT(e, &e->nbr_count, n));
     }
-    GBMD_TRY(allocT(&e->ctl, 16));
+    GBMD_TRY(allocT(e, &e->ctl, 16));
     if (e->opt.arith == GBMD_ARITH_INT) {
         std::vector<int32_t> tab;
         std::vector<double> pair4;
         uint32_t len = 0;
         int_tables(*sys, tab, len, e->P.irc2, pair4);
-        GBMD_TRY(allocT(&e->itab, tab.size()));
-        GBMD_TRY(allocT(&e->ipair, pair4.size()));
+        GBMD_TRY(allocT(e, &e->itab, tab.size()));
+        GBMD_TRY(allocT(e, &e->ipair, pair4.size()));
         GBMD_CUDA_TRY(cudaMemcpy(e->itab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
         GBMD_CUDA_TRY(cudaMemcpy(e->ipair, pair4.data(), pair4.size() * 8, cudaMemcpyHostToDevice));
         e->P.int_mode = 1;
@@ -725,17 +795,17 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         e->P.itab = e->itab;
         e->P.ipair = e->ipair;
     }
-    GBMD_TRY(allocT(&e->relf, n));
-    GBMD_TRY(allocT(&e->qpos[0], n));
-    GBMD_TRY(allocT(&e->qpos[1], n));
-    GBMD_TRY(allocT(&e->mrank, n));
-    GBMD_TRY(allocT(&e->tpart, 8 * (size_t)e->thermo_nb));
-    GBMD_TRY(allocT(&e->vpart, 3 * (size_t)e->thermo_nb));
-    GBMD_TRY(allocT(&e->tfac, 2));
-    GBMD_TRY(allocT(&e->partial, 4 * (size_t)blocks_for(n, 128) + 4));
-    GBMD_TRY(alloc(&e->staging, n * D * 8));
-    GBMD_TRY(allocT(&e->staging_v, n * D));
-    GBMD_TRY(allocT(&e->staging_s, n));
+    GBMD_TRY(allocT(e, &e->relf, n));
+    GBMD_TRY(allocT(e, &e->qpos[0], n));
+    GBMD_TRY(allocT(e, &e->qpos[1], n));
+    GBMD_TRY(allocT(e, &e->mrank, n));
+    GBMD_TRY(allocT(e, &e->tpart, 8 * (size_t)e->thermo_nb));
+    GBMD_TRY(allocT(e, &e->vpart, 3 * (size_t)e->thermo_nb));
+    GBMD_TRY(allocT(e, &e->tfac, 2));
+    GBMD_TRY(allocT(e, &e->partial, 4 * (size_t)blocks_for(n, 128) + 4));
+    GBMD_TRY(alloc(e, &e->staging, n * D * 8));
+    GBMD_TRY(allocT(e, &e->staging_v, n * D));
+    GBMD_TRY(allocT(e, &e->staging_s, n));
     GBMD_CUDA_TRY(cudaMemsetAsync(e->ctl, 0, 64, e->st));
     return GBMD_OK;
 }
@@ -831,7 +901,7 @@ int gbmd_sync(gbmd_engine* e) {
 
 int gbmd_reverse(gbmd_engine* e) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    GBMD_TRY(prepare_pairs(e));
+    GBMD_TRY(prepare_pairs_cond(e));
     GBMD_TRY(kicks_dispatch(e, nullptr, nullptr, 1));
     e->steps = -e->steps;
     return gbmd_sync(e);
@@ -858,7 +928,7 @@ int gbmd_upload(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const ui
 
 int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    GBMD_TRY(prepare_pairs(e));
+    GBMD_TRY(prepare_pairs_cond(e));
     GBMD_TRY(kicks_dispatch(e, e->kicks, e->partial, 0));
     size_t n = e->n;
     if (kicks) {
@@ -882,7 +952,7 @@ int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential) {
 // path, on the device so that it runs at full size.
 int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    GBMD_TRY(prepare_pairs(e));
+    GBMD_TRY(prepare_pairs_cond(e));
     PairsF64 Q;
     std::memset(&Q, 0, sizeof(Q));
     const gbmd_system& s = e->sys;
@@ -900,7 +970,7 @@ int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential) {
     }
     size_t n = e->n;
     double* pe_dev = nullptr;
-    if (cudaMalloc(&pe_dev, n * 8) != cudaSuccess) return fail(GBMD_E_NOMEM, "f64 potential");
+    if (cudaMallocAsync((void**)&pe_dev, n * 8, e->st) != cudaSuccess) return fail(GBMD_E_NOMEM, "f64 potential");
     uint32_t nb = blocks_for(e->n, 128);
     const bool cells = !e->verlet;
     const void* pos = cells ? e->pos_scr : e->pos[e->cur];
@@ -930,8 +1000,8 @@ int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential) {
     }
     if (rc == GBMD_OK && potential && cudaMemcpyAsync(pe_host.data(), pe_dev, n * 8, cudaMemcpyDeviceToHost, e->st) != cudaSuccess)
         rc = fail(GBMD_E_CUDA, "potential copy");
+    cudaFreeAsync(pe_dev, e->st);
     cudaError_t err = cudaStreamSynchronize(e->st);
-    cudaFree(pe_dev);
     if (rc != GBMD_OK) return rc;
     if (err != cudaSuccess) return fail(GBMD_E_CUDA, cudaGetErrorString(err));
     if (potential) {
@@ -1112,9 +1182,37 @@ namespace {
 
 // RDF pair counts over unordered pairs of the cell-sorted scratch state: bin
 // floor(sqrt(r2) * scale) with r2 the f64 square of the exact minimum-image separation.
+// The RDF bin of a pair at minimum-image separation d: k = floor(sqrt(r2) bins / rmax) with r2
+// the f64 square of the exact separation, or -1 beyond rmax. Decided in f32 when that is safe:
+// the f32 estimate of r bins / rmax is within 3.3e-7 of it relatively (separations rounded to
+// f32, a fused sum of squares, a square root, one product), so a pair farther than `margin` bins
+// from a bin edge, or clearly beyond rmax (r2 above lim2f), is binned without f64 arithmetic,
+// which runs at a small fraction of the f32 rate on this GPU; the rest takes the f64 definition.
+template <int D>
+__device__ __forceinline__ int rdf_bin(const int64_t* d, uint32_t bins, double scale, float scalef, float lim2f, float margin) {
+    float r2f = 0.0f;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const float x = __fmul_rn(__ll2float_rn(d[a]), 1.0f / 4294967296.0f);
+        r2f = __fmaf_rn(x, x, r2f);
+    }
+    if (r2f > lim2f) return -1;
+    const float rf = __fmul_rn(__fsqrt_rn(r2f), scalef);
+    const float fl = floorf(rf), fr = rf - fl;
+    if (fr > margin && fr < 1.0f - margin && rf < (float)bins - margin) return (int)fl;
+    double r2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const double x = to_f64(d[a]);
+        r2 = __dadd_rn(r2, __dmul_rn(x, x));
+    }
+    const double r = __dmul_rn(__dsqrt_rn(r2), scale);
+    return r < (double)bins ? (int)(uint32_t)r : -1;
+}
+
 template <int D>
 __global__ void k_rdf(Params P, const Rec<D>* pos, const uint32_t* keys, const uint32_t* start, uint32_t bins, double scale,
-                      unsigned long long* out) {
+                      float scalef, float lim2f, float margin, unsigned long long* out) {
     extern __shared__ uint32_t h[];
     for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
     __syncthreads();
@@ -1125,17 +1223,13 @@ __global__ void k_rdf(Params P, const Rec<D>* pos, const uint32_t* keys, const u
         uint32_t c[3];
         cell_coords(P, keys[i], c);
         for_cells<D>(P, c, [&](uint32_t cell) {
-            for (uint32_t j = start[cell]; j < start[cell + 1]; j++) {
-                if (j <= i) continue;
-                int64_t xj[3];
+            for (uint32_t j = max(start[cell], i + 1); j < start[cell + 1]; j++) {
+                int64_t xj[3], d[3];
                 load_particle<D, false>(pos, nullptr, j, xj);
-                double r2 = 0.0;
-                for (int a = 0; a < D; a++) {
-                    double d = to_f64(min_image(xj[a] - xi[a], P.box[a], P.half[a]));
-                    r2 = __dadd_rn(r2, __dmul_rn(d, d));
-                }
-                double r = __dmul_rn(__dsqrt_rn(r2), scale);
-                if (r < (double)bins) atomicAdd(&h[(uint32_t)r], 1u);
+#pragma unroll
+                for (int a = 0; a < D; a++) d[a] = min_image(xj[a] - xi[a], P.box[a], P.half[a]);
+                const int k = rdf_bin<D>(d, bins, scale, scalef, lim2f, margin);
+                if (k >= 0) atomicAdd(&h[k], 1u);
             }
         });
     }
@@ -1148,7 +1242,8 @@ __global__ void k_rdf(Params P, const Rec<D>* pos, const uint32_t* keys, const u
 // some axis (small systems only). Positions are wrapped first: between list builds they may lie
 // up to the skin outside [0, L).
 template <int D>
-__global__ void k_rdf_all(Params P, const Rec<D>* pos, uint32_t bins, double scale, unsigned long long* out) {
+__global__ void k_rdf_all(Params P, const Rec<D>* pos, uint32_t bins, double scale, float scalef, float lim2f, float margin,
+                          unsigned long long* out) {
     extern __shared__ uint32_t h[];
     for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
     __syncthreads();
@@ -1158,15 +1253,12 @@ __global__ void k_rdf_all(Params P, const Rec<D>* pos, uint32_t bins, double sca
         load_particle<D, false>(pos, nullptr, i, xi);
         for (int a = 0; a < D; a++) xi[a] = wrap(xi[a], P.box[a]);
         for (uint32_t j = i + 1; j < P.n; j++) {
-            int64_t xj[3];
+            int64_t xj[3], d[3];
             load_particle<D, false>(pos, nullptr, j, xj);
-            double r2 = 0.0;
-            for (int a = 0; a < D; a++) {
-                double d = to_f64(min_image(wrap(xj[a], P.box[a]) - xi[a], P.box[a], P.half[a]));
-                r2 = __dadd_rn(r2, __dmul_rn(d, d));
-            }
-            double r = __dmul_rn(__dsqrt_rn(r2), scale);
-            if (r < (double)bins) atomicAdd(&h[(uint32_t)r], 1u);
+#pragma unroll
+            for (int a = 0; a < D; a++) d[a] = min_image(wrap(xj[a], P.box[a]) - xi[a], P.box[a], P.half[a]);
+            const int k = rdf_bin<D>(d, bins, scale, scalef, lim2f, margin);
+            if (k >= 0) atomicAdd(&h[k], 1u);
         }
     }
     __syncthreads();
@@ -1186,95 +1278,116 @@ __global__ void k_profile(uint32_t n, const Rec<D>* pos, uint32_t axis, int64_t 
 
 } // namespace
 
-extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint32_t rdf_bins, double rdf_rmax, uint64_t* profile,
-                            uint32_t profile_bins, uint32_t profile_axis) {
+// Host memory that the device copies a frame into without the host waiting (pinned, grown on
+// demand and kept for the engine's life).
+static int pinned_grow(void** p, size_t* cap, size_t bytes) {
+    if (bytes <= *cap) return GBMD_OK;
+    pinned_give(*p, *cap);
+    *cap = pin_class(bytes);
+    *p = pinned_take(*cap);
+    if (!*p) {
+        *cap = 0;
+        return fail(GBMD_E_NOMEM, "pinned frame buffer");
+    }
+    return GBMD_OK;
+}
+
+extern "C" int gbmd_observe_begin(gbmd_engine* e, uint32_t rdf_bins, double rdf_rmax, uint32_t profile_bins, uint32_t profile_axis) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    if (rdf && (rdf_bins == 0 || rdf_bins > 8192 || !(rdf_rmax > 0.0))) return fail(GBMD_E_INVALID, "bad RDF arguments");
-    if (profile && (profile_bins == 0 || profile_axis >= (uint32_t)e->D)) return fail(GBMD_E_INVALID, "bad profile arguments");
-    GBMD_TRY(prepare_pairs(e));
+    if (e->obs_pending) return fail(GBMD_E_INVALID, "a frame is already in flight (gbmd_observe_end first)");
+    if (rdf_bins && (rdf_bins > 8192 || !(rdf_rmax > 0.0))) return fail(GBMD_E_INVALID, "bad RDF arguments");
+    if (profile_bins && profile_axis >= (uint32_t)e->D) return fail(GBMD_E_INVALID, "bad profile arguments");
+    GBMD_TRY(prepare_pairs_cond(e));
     GBMD_TRY(kicks_dispatch(e, nullptr, e->partial, 0));
     uint32_t n = e->n, nb = blocks_for(n, 128);
-    std::vector<double> part(4 * (size_t)nb);
-    GBMD_CUDA_TRY(cudaMemcpyAsync(part.data(), e->partial, part.size() * 8, cudaMemcpyDeviceToHost, e->st));
-    size_t nbins = (rdf ? rdf_bins : 0) + (profile ? profile_bins : 0);
+    GBMD_TRY(pinned_grow((void**)&e->obs_part_h, &e->obs_part_cap, 4 * (size_t)nb * 8));
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->obs_part_h, e->partial, 4 * (size_t)nb * 8, cudaMemcpyDeviceToHost, e->st));
+    size_t nbins = (size_t)rdf_bins + profile_bins;
     if (nbins > e->obs_bins_cap) {
-        if (e->obs_bins) GBMD_CUDA_TRY(cudaFree(e->obs_bins));
+        if (e->obs_bins) GBMD_CUDA_TRY(cudaFreeAsync(e->obs_bins, e->st));
         e->obs_bins = nullptr;
         e->obs_bins_cap = 0;
-        if (cudaMalloc(&e->obs_bins, nbins * 8) != cudaSuccess) return fail(GBMD_E_NOMEM, "observation bins");
+        if (cudaMallocAsync((void**)&e->obs_bins, nbins * 8, e->st) != cudaSuccess) return fail(GBMD_E_NOMEM, "observation bins");
         e->obs_bins_cap = nbins;
     }
     unsigned long long* dbuf = e->obs_bins;
     if (nbins) GBMD_CUDA_TRY(cudaMemsetAsync(dbuf, 0, nbins * 8, e->st));
-    int rc = GBMD_OK;
-    bool rdf_cells = true;
-    if (rdf) {
+    if (rdf_bins) {
+        bool rdf_cells = true;
         double bmax = 0.0;
         for (int a = 0; a < e->D; a++) bmax = std::max(bmax, to_f64h(e->sys.box_len[a]));
         for (int a = 0; a < e->D; a++)
             if (std::floor(to_f64h(e->sys.box_len[a]) / (rdf_rmax + 1e-3 + 1e-6 * bmax)) < 3.0) rdf_cells = false;
-    }
-    if (rdf && !rdf_cells) {
-        double scale = (double)rdf_bins / rdf_rmax;
-        size_t shm = (size_t)rdf_bins * 4;
-        if (e->D == 2)
-            k_rdf_all<2><<<blocks_for(n, 128), 128, shm, e->st>>>(e->P, (const Rec<2>*)e->pos[e->cur], rdf_bins, scale, dbuf);
-        else
-            k_rdf_all<3><<<blocks_for(n, 128), 128, shm, e->st>>>(e->P, (const Rec<3>*)e->pos[e->cur], rdf_bins, scale, dbuf);
-        note_launch();
-    } else if (rdf) {
-        Params P = e->P;
-        uint32_t nc[3];
-        rc = cells_for(e->sys, rdf_rmax, nc);
-        if (rc == GBMD_OK) {
+        const double scale = (double)rdf_bins / rdf_rmax;
+        const size_t shm = (size_t)rdf_bins * 4;
+        // f32 fast path: beyond rmax (1 + 1e-4) for sure, or more than 1e-6 bins + 1e-5 from an edge
+        const float scalef = (float)scale, lim2f = (float)(rdf_rmax * rdf_rmax * (1.0 + 1e-4));
+        const float margin = (float)(1e-6 * rdf_bins + 1e-5);
+        if (!rdf_cells) {
+            if (e->D == 2)
+                k_rdf_all<2><<<blocks_for(n, 128), 128, shm, e->st>>>(e->P, (const Rec<2>*)e->pos[e->cur], rdf_bins, scale, scalef, lim2f, margin, dbuf);
+            else
+                k_rdf_all<3><<<blocks_for(n, 128), 128, shm, e->st>>>(e->P, (const Rec<3>*)e->pos[e->cur], rdf_bins, scale, scalef, lim2f, margin, dbuf);
+            note_launch();
+        } else {
+            // its own cell grid (side >= rmax) over the scratch buffers; the engine's own state,
+            // lists and cell starts are untouched, so no list rebuild follows
+            Params P = e->P;
+            uint32_t nc[3];
+            GBMD_TRY(cells_for(e->sys, rdf_rmax, nc));
             set_cells(P, nc, (uint32_t)e->D);
             size_t need = (size_t)P.ncell + 1;
             if (need > e->obs_start_cap) {
-                if (e->obs_start) cudaFree(e->obs_start);
+                if (e->obs_start) cudaFreeAsync(e->obs_start, e->st);
                 e->obs_start = nullptr;
                 e->obs_start_cap = 0;
-                if (cudaMalloc(&e->obs_start, need * 4) != cudaSuccess) rc = fail(GBMD_E_NOMEM, "RDF cell starts");
-                else e->obs_start_cap = need;
+                if (cudaMallocAsync((void**)&e->obs_start, need * 4, e->st) != cudaSuccess) return fail(GBMD_E_NOMEM, "RDF cell starts");
+                e->obs_start_cap = need;
             }
-        }
-        if (rc == GBMD_OK) {
             uint32_t* saved = e->start;
             e->start = e->obs_start;
-            double scale = (double)rdf_bins / rdf_rmax;
-            size_t shm = (size_t)rdf_bins * 4;
             if (e->D == 2) {
                 enqueue_bin<2>(e, e->st, P);
-                k_rdf<2><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<2>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, dbuf);
+                k_rdf<2><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<2>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, scalef, lim2f, margin, dbuf);
             } else {
                 enqueue_bin<3>(e, e->st, P);
-                k_rdf<3><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<3>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, dbuf);
+                k_rdf<3><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<3>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, scalef, lim2f, margin, dbuf);
             }
             note_launch();
             e->start = saved;
         }
     }
-    if (rc == GBMD_OK && profile) {
-        unsigned long long* pbuf = dbuf + (rdf ? rdf_bins : 0);
+    if (profile_bins) {
+        unsigned long long* pbuf = dbuf + rdf_bins;
         double l = to_f64h(e->sys.box_len[profile_axis]);
         int64_t lfix = e->P.box[profile_axis];
         if (e->D == 2) k_profile<2><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
         else k_profile<3><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<3>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
         note_launch();
     }
-    std::vector<uint64_t> hbuf(nbins);
-    if (rc == GBMD_OK && nbins) GBMD_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), dbuf, nbins * 8, cudaMemcpyDeviceToHost, e->st));
-    cudaError_t err = cudaStreamSynchronize(e->st);
-    if (rc != GBMD_OK) return rc;
-    if (err != cudaSuccess) return fail(GBMD_E_CUDA, cudaGetErrorString(err));
-    GBMD_TRY(check_ctl(e));
-    if (rdf) std::memcpy(rdf, hbuf.data(), (size_t)rdf_bins * 8);
-    if (profile) std::memcpy(profile, hbuf.data() + (rdf ? rdf_bins : 0), (size_t)profile_bins * 8);
-    if (rdf && rdf_cells) {
-        // the RDF binning left the scratch state sorted by its own cells: rebuild before use
-        uint32_t one = 1;
-        GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    if (nbins) {
+        GBMD_TRY(pinned_grow((void**)&e->obs_bins_h, &e->obs_bins_h_cap, nbins * 8));
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->obs_bins_h, dbuf, nbins * 8, cudaMemcpyDeviceToHost, e->st));
     }
+    GBMD_CUDA_TRY(cudaGetLastError());
+    e->obs_pending = true;
+    e->obs_rdf_bins = rdf_bins;
+    e->obs_profile_bins = profile_bins;
+    e->obs_nb = nb;
+    return GBMD_OK;
+}
+
+extern "C" int gbmd_observe_end(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint64_t* profile) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (!e->obs_pending) return fail(GBMD_E_INVALID, "no frame in flight (gbmd_observe_begin first)");
+    e->obs_pending = false;
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st)); // returns at once when the frame's work is done
+    GBMD_TRY(check_ctl(e));
+    if (rdf && e->obs_rdf_bins) std::memcpy(rdf, e->obs_bins_h, (size_t)e->obs_rdf_bins * 8);
+    if (profile && e->obs_profile_bins) std::memcpy(profile, e->obs_bins_h + e->obs_rdf_bins, (size_t)e->obs_profile_bins * 8);
     if (frame) {
+        const uint32_t n = e->n, nb = e->obs_nb;
+        const double* part = e->obs_part_h;
         double pe = 0.0, w = 0.0, ke = 0.0;
         for (uint32_t b = 0; b < nb; b++) {
             pe += part[4 * b];
@@ -1295,6 +1408,15 @@ extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, ui
         frame->dim = (uint32_t)e->D;
     }
     return GBMD_OK;
+}
+
+extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint32_t rdf_bins, double rdf_rmax, uint64_t* profile,
+                            uint32_t profile_bins, uint32_t profile_axis) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (rdf && (rdf_bins == 0 || rdf_bins > 8192 || !(rdf_rmax > 0.0))) return fail(GBMD_E_INVALID, "bad RDF arguments");
+    if (profile && (profile_bins == 0 || profile_axis >= (uint32_t)e->D)) return fail(GBMD_E_INVALID, "bad profile arguments");
+    GBMD_TRY(gbmd_observe_begin(e, rdf ? rdf_bins : 0, rdf_rmax, profile ? profile_bins : 0, profile_axis));
+    return gbmd_observe_end(e, frame, rdf, profile);
 }
 
 // ------------------------------------------------------------------ seeded init + hashing

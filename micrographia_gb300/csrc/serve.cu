@@ -74,10 +74,14 @@ uint64_t estimate_bytes(const gbmd_system& s, uint32_t n, double skin) {
     return (uint64_t)(n * per + n * 4.0 * (std::ceil(cap / 4) * 4) + cells * 4 + (1 << 20));
 }
 
+// Enqueue the next frame interval: its steps, then the frame's kernels and copies into pinned
+// memory (gbmd_observe_begin), then the completion event. Nothing here waits on the device.
 int start_interval(gbmd_server* sv, Request& r) {
     uint64_t left = r.spec.steps - r.steps_done;
     uint64_t k = std::min<uint64_t>(left, r.spec.frame_every ? r.spec.frame_every : left);
     GBMD_TRY(gbmd_step(r.e, k));
+    const uint32_t bins = std::min<uint32_t>(r.spec.rdf_bins, GBMD_SERVE_RDF_BINS);
+    GBMD_TRY(gbmd_observe_begin(r.e, bins, r.spec.rdf_rmax > 0 ? r.spec.rdf_rmax : 5.0, 0, 0));
     void* st = nullptr;
     GBMD_TRY(gbmd_stream(r.e, &st));
     GBMD_CUDA_TRY(cudaEventRecord(r.done, (cudaStream_t)st));
@@ -124,8 +128,8 @@ int emit_frame(gbmd_server* sv, Request& r) {
     std::memset(&f, 0, sizeof(f));
     f.request = r.id;
     f.index = r.frames++;
-    uint32_t bins = std::min<uint32_t>(r.spec.rdf_bins, GBMD_SERVE_RDF_BINS);
-    GBMD_TRY(gbmd_observe(r.e, &f.frame, bins ? f.rdf : nullptr, bins, r.spec.rdf_rmax > 0 ? r.spec.rdf_rmax : 5.0, nullptr, 0, 0));
+    // the interval's event has completed: the frame is already in pinned memory
+    GBMD_TRY(gbmd_observe_end(r.e, &f.frame, f.rdf, nullptr));
     f.last = r.steps_done >= r.spec.steps ? 1u : 0u;
     if (f.last) GBMD_TRY(gbmd_state_hash(r.e, &f.state_hash));
     f.ready_ns = now_ns() - sv->t0;
@@ -176,7 +180,6 @@ int gbmd_serve_poll(gbmd_server* sv, gbmd_serve_frame* frames, uint32_t cap, uin
         Request& r = sv->active[k];
         if (r.running && cudaEventQuery(r.done) == cudaSuccess) {
             r.running = false;
-            GBMD_TRY(gbmd_sync(r.e));
             GBMD_TRY(emit_frame(sv, r));
             if (r.steps_done >= r.spec.steps || r.cancelled) {
                 sv->completed++;
