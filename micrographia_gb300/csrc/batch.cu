@@ -55,19 +55,28 @@ __global__ void k_bkeys(uint32_t N, const Params* __restrict__ tab, const uint32
     const Params& P = tab[sysidx[i]];
     int64_t x[3];
     load_particle<D, false>(pos, nullptr, i, x);
+#pragma unroll
+    for (int a = 0; a < D; a++) x[a] = wrap(x[a], P.box[a]); // positions drift out between list builds
     uint32_t c[3];
     keys[i] = P.cell_base + cell_key<D>(P, x, c);
     vals[i] = i;
 }
 
 template <int D>
-__global__ void k_bgather(uint32_t N, const uint32_t* items, const PosRec<D>* pos, const int32_t* vel, const uint32_t* species,
-                          const uint32_t* ids, const uint32_t* sysidx, PosRec<D>* pos_o, int32_t* vel_o, uint32_t* species_o, uint32_t* ids_o,
-                          uint32_t* sysidx_o) {
+__global__ void k_bgather(uint32_t N, const Params* __restrict__ tab, const uint32_t* items, const PosRec<D>* pos, const int32_t* vel,
+                          const uint32_t* species, const uint32_t* ids, const uint32_t* sysidx, PosRec<D>* pos_o, int32_t* vel_o,
+                          uint32_t* species_o, uint32_t* ids_o, uint32_t* sysidx_o) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     uint32_t o = items[s];
-    pos_o[s] = pos[o];
+    PosRec<D> r = pos[o];
+    {
+        const Params& P = tab[sysidx[o]];
+        long long* x = reinterpret_cast<long long*>(&r);
+#pragma unroll
+        for (int a = 0; a < D; a++) x[a] = wrap(x[a], P.box[a]);
+    }
+    pos_o[s] = r;
     for (int a = 0; a < D; a++) vel_o[D * s + a] = vel[D * o + a];
     species_o[s] = species[o];
     ids_o[s] = ids[o];
@@ -84,19 +93,22 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
                                                      int32_t* __restrict__ vel_o, uint32_t* __restrict__ species_o,
                                                      uint32_t* __restrict__ ids_o, uint32_t* __restrict__ sysidx_o,
                                                      PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ nbr,
-                                                     uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ ctl) {
+                                                     uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ ctl, uint4* __restrict__ qpos_o) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     uint32_t sys = sysidx_s[i];
     const Params& P = tab[sys];
-    const Geom G = geom_of(P);
-    const uint32_t base = P.cell_base, ns = P.ns;
+    const uint32_t base = P.cell_base, ns = P.ns, cap4 = (cap + 3u) & ~3u;
     int64_t xi[3];
     uint32_t si = load_particle<D, MULTI>(pos_s, species_s, i, xi);
     uint32_t c[3];
     cell_coords(P, keys[i] - base, c);
     uint32_t count = 0;
-    for_cells<D>(P, c, [&](uint32_t cell) {
+    // each neighbour cell at the periodic image that places it next to this one: the list entry
+    // carries that image, so the force kernel needs no minimum image (as k_build_list)
+    for_cells_shifted<D>(P, c, [&](uint32_t cell, int64_t sx, int64_t sy, int64_t sz) {
+        const int64_t sh[3] = {sx, sy, sz};
+        const uint32_t code = image_code(sx, sy, sz);
         uint32_t j0 = __ldg(start + base + cell), j1 = __ldg(start + base + cell + 1);
         for (uint32_t j = j0; j < j1; j++) {
             if (j == i) continue;
@@ -105,12 +117,12 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
             bool ok = true;
             float f[D];
 #pragma unroll
-            for (int a = 0; a < D; a++) f[a] = sep_s(min_image(xj[a] - xi[a], G.box[a], G.half[a]), ok);
+            for (int a = 0; a < D; a++) f[a] = sep_s(xj[a] + sh[a] - xi[a], ok);
             if (!ok) continue;
             float r2 = __fadd_rn(__fmul_rn(f[0], f[0]), __fmul_rn(f[1], f[1]));
             if (D == 3) r2 = __fadd_rn(r2, __fmul_rn(f[2], f[2]));
             if (r2 < P.pc[si * ns + sj].list2s) {
-                if (count < cap) nbr[(size_t)count * N + i] = j;
+                if (count < cap) nbr[list_slot(i, count, cap4)] = j | code;
                 count++;
             }
         }
@@ -122,59 +134,88 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
     nbr_count[i] = count;
     pos_o[i] = pos_s[i];
     ref_pos[i] = pos_s[i];
+    qpos_o[i] = quot_record<D>(xi, si);
     for (int a = 0; a < D; a++) vel_o[D * i + a] = vel_s[D * i + a];
     species_o[i] = species_s[i];
     ids_o[i] = ids_s[i];
     sysidx_o[i] = sys;
 }
 
-// Persistent fused force + leapfrog over every particle of every system.
+// Persistent fused force + leapfrog over every particle of every system, on the layout of the
+// single-system engine: warp-tiled lists with periodic-image codes, 16-byte quotient records and
+// positions left unwrapped between list builds. Warps step through the particles 32 at a time
+// (a warp is a list tile); each lane reads its own system's parameters.
 template <int D, bool MULTI, bool SIG1>
-__global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx,
+__global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, uint32_t cap, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx,
                                                      const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
+                                                     const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                      int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
                                                      const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                      const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const uint32_t lane = threadIdx.x & 31u, nwarps = (gridDim.x * blockDim.x) >> 5, cap4 = (cap + 3u) & ~3u;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32u < N; w += nwarps) {
+        const uint32_t i = w * 32u + lane;
+        if (i >= N) continue;
         const Params& P = tab[sysidx[i]];
         const Geom G = geom_of(P);
         int64_t xi[3];
-        uint32_t si = load_particle<D, MULTI>(pos_in, species, i, xi);
+        const uint32_t si = load_particle<D, MULTI>(pos_in, species, i, xi);
         const float cs = P.kick_cs[si];
-        const uint32_t ns = P.ns;
         const PairC pc0 = P.pc[0];
+        const uint32_t ns = P.ns;
         int32_t k[3] = {0, 0, 0};
         const uint32_t m = __ldg(nbr_count + i);
-        uint32_t q = 0;
-        if constexpr (!MULTI && SIG1) {
-            // neighbours two at a time through the packed f32x2 chain (pair_kicks2_sig1)
-            for (; q + 1 < m; q += 2) {
-                const uint32_t j0 = __ldg(nbr + (size_t)q * N + i), j1 = __ldg(nbr + (size_t)(q + 1) * N + i);
-                int64_t x0[3], x1[3];
-                load_particle<D, false>(pos_in, nullptr, j0, x0);
-                load_particle<D, false>(pos_in, nullptr, j1, x1);
-                float f0[3] = {0.0f, 0.0f, 0.0f}, f1[3] = {0.0f, 0.0f, 0.0f};
-                bool ok0 = true, ok1 = true;
+        const uint4* groups = reinterpret_cast<const uint4*>(nbr + list_slot(i, 0, cap4));
+        const uint4 qi = __ldg(qpos_in + i);
+        const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
+        const uint32_t ngroups = (m + 3u) >> 2;
+        for (uint32_t g = 0; g < ngroups; g++) {
+            if (g + 2 < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2)));
+            const uint4 jv = __ldg(groups + 32 * g);
+            const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
+            const uint32_t left = m - 4 * g;
+            uint4 r[4];
 #pragma unroll
-                for (int a = 0; a < D; a++) {
-                    f0[a] = sep_s(min_image(x0[a] - xi[a], G.box[a], G.half[a]), ok0);
-                    f1[a] = sep_s(min_image(x1[a] - xi[a], G.box[a], G.half[a]), ok1);
+            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? (jj[u] & LIST_MASK) : i));
+            float f[4][3];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
+                uint32_t Rj[3] = {__byte_perm(r[u].w, 0u, 0x4440u), __byte_perm(r[u].w, 0u, 0x4441u), __byte_perm(r[u].w, 0u, 0x4442u)};
+                const uint32_t code = jj[u] >> LIST_BITS;
+                if (code && (uint32_t)u < left) {
+#pragma unroll
+                    for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
                 }
-                pair_kicks2_sig1<D>(pc0, cs, f0, f1, ok0, ok1, k);
+#pragma unroll
+                for (int a = 0; a < D; a++) f[u][a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
+                if (D == 2) f[u][2] = 0.0f;
+            }
+            if constexpr (!MULTI && SIG1) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) pair_kicks2_sig1<D>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if ((uint32_t)u >= left) break;
+                    const PairC& pc = MULTI ? P.pc[si * ns + (r[u].w >> 24)] : pc0;
+                    float fr, s6, r2;
+                    if (pair_fr<D>(pc, f[u], fr, s6, r2)) {
+                        const float am = __fmul_rn(-fr, cs);
+#pragma unroll
+                        for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[u][a])));
+                    }
+                }
             }
         }
-        for (; q < m; q++) {
-            uint32_t j = __ldg(nbr + (size_t)q * N + i);
-            int64_t xj[3];
-            uint32_t sj = load_particle<D, MULTI>(pos_in, species, j, xj);
-            float fr, s6, r2;
-            pair_kick<D>(G, MULTI ? P.pc[si * ns + sj] : pc0, cs, xi, xj, k, fr, s6, r2);
-        }
         int32_t v[3];
+#pragma unroll
         for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
-        leapfrog<D>(G, si, k, v, xi);
+        leapfrog<D, Geom, false>(G, si, k, v, xi);
+#pragma unroll
         for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
         store_pos<D>(pos_out, i, xi, si);
+        qpos_out[i] = quot_record<D>(xi, si);
         int64_t xr[3];
         load_particle<D, false>(ref_pos, nullptr, i, xr);
         if (moved_half_skin<D>(G, xr, xi)) ctl[0] = 1;
@@ -198,15 +239,16 @@ __global__ void k_bfrom_host(uint32_t N, const int64_t* ipos, const int32_t* ive
 }
 
 template <int D>
-__global__ void k_bto_ids(uint32_t N, const PosRec<D>* pos, const int32_t* vel, const uint32_t* species, const uint32_t* ids,
-                          int64_t* opos, int32_t* ovel, uint32_t* ospecies) {
+__global__ void k_bto_ids(uint32_t N, const Params* __restrict__ tab, const uint32_t* sysidx, const PosRec<D>* pos, const int32_t* vel,
+                          const uint32_t* species, const uint32_t* ids, int64_t* opos, int32_t* ovel, uint32_t* ospecies) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     uint32_t id = ids[s];
     int64_t x[3];
     load_particle<D, false>(pos, nullptr, s, x);
+    const Params& P = tab[sysidx[s]];
     for (int a = 0; a < D; a++) {
-        opos[(size_t)D * id + a] = x[a];
+        opos[(size_t)D * id + a] = wrap(x[a], P.box[a]); // positions drift out between list builds
         ovel[(size_t)D * id + a] = vel[D * s + a];
     }
     ospecies[id] = species[s];
@@ -239,6 +281,7 @@ struct gbmd_batch {
     uint32_t *species = nullptr, *species_scr = nullptr, *ids = nullptr, *ids_scr = nullptr, *sysidx = nullptr, *sysidx_scr = nullptr;
     uint32_t *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr}, *hist = nullptr, *scan_tmp = nullptr, *start = nullptr;
     uint32_t *nbr = nullptr, *nbr_count = nullptr, *ctl = nullptr;
+    uint4* qpos[2] = {nullptr, nullptr}; // quotient records of the positions (ping-pong)
     void* staging = nullptr;
     int32_t* staging_v = nullptr;
     uint32_t* staging_s = nullptr;
@@ -264,7 +307,7 @@ void bfree(gbmd_batch* b) {
             if (b->exec[p][k]) cudaGraphExecDestroy(b->exec[p][k]);
     void* ptrs[] = {b->tab, b->pos[0], b->pos[1], b->pos_scr, b->ref_pos, b->vel, b->vel_scr, b->species, b->species_scr, b->ids, b->ids_scr,
                     b->sysidx, b->sysidx_scr, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->scan_tmp, b->start, b->nbr,
-                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s};
+                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1]};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->st) cudaStreamDestroy(b->st);
@@ -276,12 +319,13 @@ template <int D, bool MULTI> void benqueue_rebuild_t(gbmd_batch* b, cudaStream_t
     k_bkeys<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur], b->keys[0], b->vals[0]);
     b->sorted = radix_sort_pairs(b->keys[0], b->vals[0], b->keys[1], b->vals[1], N, (int)b->bits, b->hist, b->scan_tmp, s);
     cell_starts(b->keys[b->sorted], N, b->ncell, b->start, s);
-    k_bgather<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->vals[b->sorted], (const PosRec<D>*)b->pos[b->cur], b->vel, b->species, b->ids,
-                                                b->sysidx, (PosRec<D>*)b->pos_scr, b->vel_scr, b->species_scr, b->ids_scr, b->sysidx_scr);
+    k_bgather<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->tab, b->vals[b->sorted], (const PosRec<D>*)b->pos[b->cur], b->vel, b->species,
+                                                b->ids, b->sysidx, (PosRec<D>*)b->pos_scr, b->vel_scr, b->species_scr, b->ids_scr,
+                                                b->sysidx_scr);
     k_bbuild_list<D, MULTI><<<nblocks(N, 128), 128, 0, s>>>(N, b->cap, b->tab, b->sysidx_scr, (const PosRec<D>*)b->pos_scr, b->vel_scr,
                                                            b->species_scr, b->ids_scr, b->keys[b->sorted], b->start,
                                                            (PosRec<D>*)b->pos[b->cur], b->vel, b->species, b->ids, b->sysidx,
-                                                           (PosRec<D>*)b->ref_pos, b->nbr, b->nbr_count, b->ctl);
+                                                           (PosRec<D>*)b->ref_pos, b->nbr, b->nbr_count, b->ctl, b->qpos[b->cur]);
     k_brebuild_done<<<1, 1, 0, s>>>(b->ctl);
     note_launch(6 + 3 * (uint64_t)radix_passes((int)b->bits));
 }
@@ -291,13 +335,13 @@ void benqueue_rebuild(gbmd_batch* b, cudaStream_t s) {
 }
 template <int D, bool MULTI> void benqueue_force_t(gbmd_batch* b, cudaStream_t s) {
     if (b->sig1)
-        k_bforce_list<D, MULTI, true><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
-                                                              (PosRec<D>*)b->pos[b->cur ^ 1], b->vel, b->species, b->nbr, b->nbr_count,
-                                                              (const PosRec<D>*)b->ref_pos, b->ctl);
+        k_bforce_list<D, MULTI, true><<<b->grid, 128, 0, s>>>(b->N, b->cap, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
+                                                              (PosRec<D>*)b->pos[b->cur ^ 1], b->qpos[b->cur], b->qpos[b->cur ^ 1], b->vel,
+                                                              b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
     else
-        k_bforce_list<D, MULTI, false><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
-                                                               (PosRec<D>*)b->pos[b->cur ^ 1], b->vel, b->species, b->nbr, b->nbr_count,
-                                                               (const PosRec<D>*)b->ref_pos, b->ctl);
+        k_bforce_list<D, MULTI, false><<<b->grid, 128, 0, s>>>(b->N, b->cap, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
+                                                               (PosRec<D>*)b->pos[b->cur ^ 1], b->qpos[b->cur], b->qpos[b->cur ^ 1], b->vel,
+                                                               b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
     note_launch();
     b->cur ^= 1;
 }
@@ -477,7 +521,9 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     step(balloc(&b->hist, hist_n));
     step(balloc(&b->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(N))));
     step(balloc(&b->start, (size_t)b->ncell + 1));
-    step(balloc(&b->nbr, N * b->cap));
+    step(balloc(&b->nbr, (N + 31) / 32 * 32 * (((size_t)b->cap + 3) & ~(size_t)3))); // warp-tiled (list_slot)
+    step(balloc(&b->qpos[0], N));
+    step(balloc(&b->qpos[1], N));
     step(balloc(&b->nbr_count, N));
     step(balloc(&b->ctl, 16));
     step(balloc((char**)&b->staging, N * D * 8));
@@ -549,11 +595,11 @@ int gbmd_batch_read_system(gbmd_batch* b, uint32_t k, int64_t* pos, int32_t* vel
     if (!b || k >= b->K) return fail(GBMD_E_INVALID, "bad batch or system index");
     size_t N = b->N, D = b->D;
     if (D == 2)
-        k_bto_ids<2><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, (const PosRec<2>*)b->pos[b->cur], b->vel, b->species, b->ids,
-                                                        (int64_t*)b->staging, b->staging_v, b->staging_s);
+        k_bto_ids<2><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, b->tab, b->sysidx, (const PosRec<2>*)b->pos[b->cur], b->vel,
+                                                        b->species, b->ids, (int64_t*)b->staging, b->staging_v, b->staging_s);
     else
-        k_bto_ids<3><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, (const PosRec<3>*)b->pos[b->cur], b->vel, b->species, b->ids,
-                                                        (int64_t*)b->staging, b->staging_v, b->staging_s);
+        k_bto_ids<3><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, b->tab, b->sysidx, (const PosRec<3>*)b->pos[b->cur], b->vel,
+                                                        b->species, b->ids, (int64_t*)b->staging, b->staging_v, b->staging_s);
     note_launch();
     size_t o = b->offsets[k], n = b->offsets[k + 1] - o;
     if (pos) GBMD_CUDA_TRY(cudaMemcpyAsync(pos, (int64_t*)b->staging + o * D, n * D * 8, cudaMemcpyDeviceToHost, b->st));
