@@ -60,6 +60,11 @@ template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t
 
 __device__ __forceinline__ void cell_coords(const Params& P, uint32_t key, uint32_t* c);
 
+// A small fixed-point offset (a few cells, |v| < 2^37) as f32 sigma for the list build's
+// prefilter, through a 32-bit conversion of v >> 8 (2^-24 sigma units): the 64-bit conversion
+// runs on the slow FP64 pipe. The error, ~1e-6 sigma, is far inside the prefilter's 1e-4 band.
+__device__ __forceinline__ float off_f32(int64_t v) { return __fmul_rn(__int2float_rn((int32_t)(v >> 8)), 1.0f / 16777216.0f); }
+
 // Storage permutation into cell order (one fused gather; reorder.wgsl's gathers + copy-backs).
 // Also records each particle's position relative to its cell's origin (c * cell_w, an exact
 // integer) as f32 sigma, with its species in the fourth word, for the list build's prefilter.
@@ -86,15 +91,30 @@ __global__ void k_gather(Params P, const uint32_t* items, const uint32_t* keys, 
         cell_coords(P, keys[s], c);
         const long long* x = reinterpret_cast<const long long*>(&r);
         float4 f;
-        f.x = __fmul_rn(__ll2float_rn(x[0] - (int64_t)c[0] * P.cell_w[0]), 1.0f / 4294967296.0f);
-        f.y = __fmul_rn(__ll2float_rn(x[1] - (int64_t)c[1] * P.cell_w[1]), 1.0f / 4294967296.0f);
-        f.z = D == 3 ? __fmul_rn(__ll2float_rn(x[2] - (int64_t)c[2] * P.cell_w[2]), 1.0f / 4294967296.0f) : 0.0f;
+        f.x = off_f32(x[0] - (int64_t)c[0] * P.cell_w[0]);
+        f.y = off_f32(x[1] - (int64_t)c[1] * P.cell_w[1]);
+        f.z = D == 3 ? off_f32(x[2] - (int64_t)c[2] * P.cell_w[2]) : 0.0f;
         f.w = __uint_as_float(sp);
         relf[s] = f;
     }
 }
 
 __device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+
+// ---------------------------------------------------------------- f32 sums with f64 accuracy
+// An unevaluated sum hi + lo of two f32 (Knuth's TwoSum adds each term exactly): sums of f32 pair
+// energies to about 2^-48 relative without f64 arithmetic, which runs at a small fraction of the
+// f32 rate on this GPU. Every operation is an explicit round-to-nearest add (no fusion).
+struct F32Sum {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x), bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+        hi = s;
+        lo = __fadd_rn(lo, err);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 // ---------------------------------------------------------------- all-integer table forces
 // IntTables::kick (table.rs:76-105): d rounded to 2^-20 sigma per axis, r2 to 2^-24 sigma^2, the
@@ -411,9 +431,9 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                 uint32_t cell = (z * ny + y) * nx + x;
                 const int64_t xs[3] = {xi[0] - sx, xi[1] - sy, D == 3 ? xi[2] - sz : 0};
                 const uint32_t code = image_code(sx, sy, sz);
-                const float b0 = __fmul_rn(__ll2float_rn(((int64_t)x - (int64_t)c[0]) * P.cell_w[0] + sx - reli[0]), 1.0f / 4294967296.0f);
-                const float b1 = __fmul_rn(__ll2float_rn(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]), 1.0f / 4294967296.0f);
-                const float b2 = D == 3 ? __fmul_rn(__ll2float_rn(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]), 1.0f / 4294967296.0f) : 0.0f;
+                const float b0 = off_f32(((int64_t)x - (int64_t)c[0]) * P.cell_w[0] + sx - reli[0]);
+                const float b1 = off_f32(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]);
+                const float b2 = D == 3 ? off_f32(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]) : 0.0f;
                 uint32_t j0 = __ldg(start + cell), j1 = __ldg(start + cell + 1);
 #pragma unroll 4
                 for (uint32_t j = j0; j < j1; j++) {
@@ -612,6 +632,7 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
     __shared__ double sh[3][4];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double pe = 0.0, w = 0.0, ke = 0.0;
+    F32Sum pe32, w32; // the f32 chain's pair terms, summed without f64 arithmetic
     if (i < P.n) {
         int64_t xi[3];
         uint32_t si = load_particle<D, MULTI>(pos, species, i, xi);
@@ -640,8 +661,8 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
                 const PairC& pc = P.pc[si * P.ns + sj];
                 float fr, s6, r2;
                 if (pair_kick<D>(P, pc, cs, xi, xj, k, fr, s6, r2)) {
-                    pe += (double)pair_u(pc, s6);
-                    w += (double)__fmul_rn(fr, r2);
+                    pe32.add(pair_u(pc, s6));
+                    w32.add(__fmul_rn(fr, r2));
                 }
             }
         };
@@ -656,6 +677,10 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
                 for (uint32_t j = start[cell]; j < start[cell + 1]; j++)
                     if (j != i) visit(j);
             });
+        }
+        if constexpr (!INT) {
+            pe = pe32.value();
+            w = w32.value();
         }
         pe *= 0.5;
         w *= 0.5;
