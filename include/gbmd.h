@@ -138,6 +138,15 @@ int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential);
 /* The same kicks with the pair chain in f64 (IntEngine<f64>::forces, int_engine.rs:130-251 with
  * F = f64): the accuracy reference of the f32 path, computed on the device at full size. */
 int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential);
+/* Checkpoint / resume: a binary snapshot of the dynamical state (id order) and the step counter,
+ * clock and thermostat phase, with the state's FNV-1a hash. Layout (little-endian): "GBMDSNP1",
+ * u32 version 1, dim, n, 0; i64 steps; u32 clock, 0; u64 thermostat phase; u64 hash; then
+ * positions i64[dim n], velocities i32[dim n], species u32[n]. gbmd_restore requires the same
+ * dimension and particle count and rejects a snapshot whose arrays do not match its hash; a run
+ * of 2N steps equals N steps, snapshot, restore (in any engine of the same system), N steps. */
+size_t gbmd_snapshot_bytes(uint32_t dim, uint32_t n);
+int gbmd_snapshot(gbmd_engine* e, void* buf, size_t cap, size_t* written);
+int gbmd_restore(gbmd_engine* e, const void* buf, size_t size);
 /* Flip one bit of one coordinate of particle `id` (engine.rs:964, State::flip_bit). */
 int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit);
 

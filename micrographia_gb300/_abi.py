@@ -153,6 +153,9 @@ SIGNATURES = [
     ("gbmd_upload", C.c_int, [VP, _I64P, _I32P, _U32P]),
     ("gbmd_kicks", C.c_int, [VP, _I32P, _DP]),
     ("gbmd_kicks_f64", C.c_int, [VP, _I32P, _DP]),
+    ("gbmd_snapshot_bytes", C.c_size_t, [C.c_uint32, C.c_uint32]),
+    ("gbmd_snapshot", C.c_int, [VP, VP, C.c_size_t, P(C.c_size_t)]),
+    ("gbmd_restore", C.c_int, [VP, VP, C.c_size_t]),
     ("gbmd_flip_bit", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32]),
     ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
     ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),

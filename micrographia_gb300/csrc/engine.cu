@@ -1406,8 +1406,71 @@ extern "C" int gbmd_observe_end(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf
         frame->volume = vol;
         frame->n = n;
         frame->dim = (uint32_t)e->D;
+        if (!std::isfinite(ke) || !std::isfinite(pe) || !std::isfinite(w))
+            return fail(GBMD_E_NONFINITE, "a non-finite energy or virial (the frame is filled in)");
     }
     return GBMD_OK;
+}
+
+// ------------------------------------------------------------------ checkpoint / resume
+// Snapshot layout (little-endian): 8-byte magic "GBMDSNP1"; u32 version (1), dim, n, reserved;
+// i64 steps; u32 clock, reserved; u64 thermostat phase; u64 State::hash of the arrays; then the
+// id-ordered positions (i64 x dim x n), velocities (i32 x dim x n) and species (u32 x n).
+namespace {
+constexpr char SNAP_MAGIC[8] = {'G', 'B', 'M', 'D', 'S', 'N', 'P', '1'};
+constexpr size_t SNAP_HEADER = 8 + 4 * 4 + 8 + 4 * 2 + 8 + 8;
+} // namespace
+
+extern "C" size_t gbmd_snapshot_bytes(uint32_t dim, uint32_t n) { return SNAP_HEADER + (size_t)n * (dim * 8 + dim * 4 + 4); }
+
+extern "C" int gbmd_snapshot(gbmd_engine* e, void* buf, size_t cap, size_t* written) {
+    if (!e || !buf) return fail(GBMD_E_INVALID, "null argument");
+    const size_t need = gbmd_snapshot_bytes((uint32_t)e->D, e->n), D = (size_t)e->D, n = e->n;
+    if (cap < need) return fail(GBMD_E_INVALID, "snapshot buffer too small (gbmd_snapshot_bytes)");
+    char* p = (char*)buf;
+    int64_t* pos = (int64_t*)(p + SNAP_HEADER);
+    int32_t* vel = (int32_t*)(p + SNAP_HEADER + n * D * 8);
+    uint32_t* sp = (uint32_t*)(p + SNAP_HEADER + n * D * 12);
+    GBMD_TRY(gbmd_read_state(e, pos, vel, sp));
+    const uint64_t h = gbmd_hash_state((uint32_t)D, pos, vel, sp, e->n);
+    const uint32_t head[4] = {1u, (uint32_t)D, e->n, 0u}, clk[2] = {e->clock, 0u};
+    const int64_t steps = e->steps;
+    const uint64_t tc = e->tcount;
+    std::memcpy(p, SNAP_MAGIC, 8);
+    std::memcpy(p + 8, head, 16);
+    std::memcpy(p + 24, &steps, 8);
+    std::memcpy(p + 32, clk, 8);
+    std::memcpy(p + 40, &tc, 8);
+    std::memcpy(p + 48, &h, 8);
+    if (written) *written = need;
+    return GBMD_OK;
+}
+
+extern "C" int gbmd_restore(gbmd_engine* e, const void* buf, size_t size) {
+    if (!e || !buf) return fail(GBMD_E_INVALID, "null argument");
+    const char* p = (const char*)buf;
+    if (size < SNAP_HEADER || std::memcmp(p, SNAP_MAGIC, 8) != 0) return fail(GBMD_E_INVALID, "not a snapshot (magic)");
+    uint32_t head[4], clk[2];
+    int64_t steps;
+    uint64_t tc, h;
+    std::memcpy(head, p + 8, 16);
+    std::memcpy(&steps, p + 24, 8);
+    std::memcpy(clk, p + 32, 8);
+    std::memcpy(&tc, p + 40, 8);
+    std::memcpy(&h, p + 48, 8);
+    if (head[0] != 1u) return fail(GBMD_E_INVALID, "unknown snapshot version");
+    if (head[1] != (uint32_t)e->D || head[2] != e->n) return fail(GBMD_E_INVALID, "snapshot of another dimension or particle count");
+    if (size != gbmd_snapshot_bytes(head[1], head[2])) return fail(GBMD_E_INVALID, "snapshot size does not match its header");
+    const size_t D = head[1], n = head[2];
+    const int64_t* pos = (const int64_t*)(p + SNAP_HEADER);
+    const int32_t* vel = (const int32_t*)(p + SNAP_HEADER + n * D * 8);
+    const uint32_t* sp = (const uint32_t*)(p + SNAP_HEADER + n * D * 12);
+    if (gbmd_hash_state((uint32_t)D, pos, vel, sp, (uint32_t)n) != h) return fail(GBMD_E_INVALID, "snapshot corrupted (state hash mismatch)");
+    GBMD_TRY(gbmd_upload(e, pos, vel, sp));
+    e->steps = steps;
+    e->clock = clk[0];
+    e->tcount = tc;
+    return gbmd_sync(e);
 }
 
 extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint32_t rdf_bins, double rdf_rmax, uint64_t* profile,

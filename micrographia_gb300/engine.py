@@ -124,6 +124,19 @@ class _Engine:
         _abi.check(self._lib.gbmd_kicks(self._h, _ptr(k, C.c_int32), C.byref(pe)))
         return k, pe.value
 
+    def snapshot(self):
+        """The engine's state and counters as snapshot bytes (micrographia_gb300.snapshot)."""
+        size = self._lib.gbmd_snapshot_bytes(self.DIM, self.n)
+        buf = (C.c_char * size)()
+        written = C.c_size_t()
+        _abi.check(self._lib.gbmd_snapshot(self._h, buf, size, C.byref(written)))
+        return bytes(buf)
+
+    def restore(self, snap):
+        """Resume from snapshot bytes of the same system (GbmdError if corrupted or mismatched)."""
+        buf = C.create_string_buffer(bytes(snap), len(snap))
+        _abi.check(self._lib.gbmd_restore(self._h, buf, len(snap)))
+
     def kicks_f64(self):
         """The kicks of IntEngine<f64> (f64 pair chain), the accuracy reference."""
         k = np.empty((self.n, self.DIM), np.int32)

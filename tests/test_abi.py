@@ -5,6 +5,9 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
+import pytest
+
 from micrographia_gb300 import _abi
 
 
@@ -55,3 +58,27 @@ def test_host_hash_matches_the_oracle(engine_lib, O):
     h3 = O.lib().oracle_state_hash(3, s3.pos.ctypes.data_as(C.POINTER(C.c_int64)), s3.vel.ctypes.data_as(C.POINTER(C.c_int32)),
                                    s3.species.ctypes.data_as(C.POINTER(C.c_uint32)), s3.n())
     assert s3.hash() == h3
+
+
+def test_snapshot_format_round_trip_and_corruption():
+    """The snapshot format on the host: pack / unpack round trip, the size rule, and a flipped
+    bit anywhere in the arrays rejected through the stored state hash."""
+    from micrographia_gb300 import snapshot
+
+    rng = np.random.default_rng(4)
+    for dim, n in ((2, 37), (3, 64)):
+        pos = rng.integers(-(1 << 40), 1 << 40, (n, dim))
+        vel = rng.integers(-(1 << 30), 1 << 30, (n, dim)).astype(np.int32)
+        sp = rng.integers(0, 4, n).astype(np.uint32)
+        buf = snapshot.pack(dim, pos, vel, sp, steps=1234, clock=77, phase=9)
+        assert len(buf) == snapshot.size(dim, n)
+        d2, p2, v2, s2, steps, clock, phase = snapshot.unpack(buf)
+        assert (d2, steps, clock, phase) == (dim, 1234, 77, 9)
+        assert np.array_equal(p2, pos) and np.array_equal(v2, vel) and np.array_equal(s2, sp)
+        for off in (snapshot.HEADER.size + 3, len(buf) - 1):
+            bad = bytearray(buf)
+            bad[off] ^= 0x10
+            with pytest.raises(ValueError):
+                snapshot.unpack(bytes(bad))
+        with pytest.raises(ValueError):
+            snapshot.unpack(b"XXXXXXXX" + buf[8:])

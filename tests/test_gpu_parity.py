@@ -382,6 +382,44 @@ def test_rdf_small_box_all_pairs(O, dim):
     assert ref.sum() > 0
 
 
+# ---------------------------------------------------------------- checkpoint / resume
+@pytest.mark.parametrize("dim", [2, 3])
+def test_snapshot_resume_is_bit_identical(O, dim):
+    """2N steps against N steps, snapshot, restore into another engine, N steps: the same state
+    bit for bit (2D with the rescale thermostat, whose phase the snapshot carries); a snapshot
+    with one flipped bit is refused."""
+    from micrographia_gb300 import snapshot
+
+    if dim == 2:
+        n = 4000
+        sys_ = System(box_for(n, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0])
+        s0 = O.fluid(sys_, n, 1.0, 5)
+        kw, eng = dict(rescale_every=10, rescale_t=0.8), GpuEngine
+    else:
+        sys_, s0 = liquid3(O, 4000, 0.8, 1.0)
+        kw, eng = {}, GpuEngine3
+    with eng(sys_, s0, **kw) as a:
+        a.step(137)
+        a.step(140)
+        want = a.read_state()
+    with eng(sys_, s0, **kw) as b:
+        b.step(137)
+        snap = b.snapshot()
+        st = b.read_state()
+    d, pos, vel, sp, steps, clock, phase = snapshot.unpack(snap)
+    assert (d, steps, phase) == (dim, 137, 137)
+    assert np.array_equal(pos, st.pos.reshape(-1, dim)) and np.array_equal(vel, st.vel.reshape(-1, dim))
+    with eng(sys_, s0, **kw) as c:
+        c.step(11)
+        c.restore(snap)
+        c.step(140)
+        assert c.read_state() == want
+        bad = bytearray(snap)
+        bad[-5] ^= 1
+        with pytest.raises(_abi.GbmdError):
+            c.restore(bytes(bad))
+
+
 # ---------------------------------------------------------------- all-integer table forces (md-core table.rs)
 def golden_int_setup(O):
     """md/src/checks.rs:155-167: 3000-particle binary LJ mixture, rho 0.6, seed 2026."""
