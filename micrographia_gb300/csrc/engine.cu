@@ -417,12 +417,30 @@ void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
     note_launch();
 }
 
+// Below these particle counts the force kernel runs 4 (2) lanes per particle.
+constexpr uint32_t FORCE_SPLIT4_BELOW = 65536, FORCE_SPLIT2_BELOW = 262144;
 template <int D, bool MULTI, bool INT> void enqueue_force_a(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
     if (e->verlet) {
         // sigma = 1 for every pair type (the common LJ case): compiled into the f32 chain
         bool sig1 = !INT;
         for (uint32_t k = 0; k < e->P.ns * e->P.ns; k++) sig1 = sig1 && e->P.pc[k].sigma2s == 0x1p56f;
-        if (sig1)
+        // small single-species systems: several lanes per particle (FORCE_SPLIT4_BELOW, FORCE_SPLIT2_BELOW)
+        const uint32_t split = (!INT && !MULTI) ? (e->n < FORCE_SPLIT4_BELOW ? 4u : (e->n < FORCE_SPLIT2_BELOW ? 2u : 1u)) : 1u;
+        if (split > 1) {
+            const uint32_t lanes = (uint32_t)(((uint64_t)e->n * split + 31) / 32 * 32);
+#define GBMD_SPLIT(SS, SG)                                                                                                          \
+    k_force_list<D, false, false, SG, SS><<<blocks_for(lanes, threads), threads, 0, s>>>(                                            \
+        e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur], e->qpos[e->cur ^ 1], e->vel, e->species, \
+        e->nbr, e->nbr_count, (const Rec<D>*)e->ref_pos, e->ctl)
+            if (split == 4) {
+                if (sig1) GBMD_SPLIT(4, true);
+                else GBMD_SPLIT(4, false);
+            } else {
+                if (sig1) GBMD_SPLIT(2, true);
+                else GBMD_SPLIT(2, false);
+            }
+#undef GBMD_SPLIT
+        } else if (sig1)
             k_force_list<D, MULTI, INT, true><<<blocks_for(e->n, threads), threads, 0, s>>>(
                 e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur], e->qpos[e->cur ^ 1], e->vel,
                 e->species, e->nbr, e->nbr_count, (const Rec<D>*)e->ref_pos, e->ctl);

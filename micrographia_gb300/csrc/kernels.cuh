@@ -471,21 +471,28 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // ping-pongs the two), so every kick sees positions of the same time step.
 // Ten blocks of 128 per SM (48 registers, a 16-byte spill outside the pair loop): measured 2.4%
 // faster than the unconstrained 62 registers at eight blocks.
-template <int D, bool MULTI, bool INT = false, bool SIG1 = false>
+// S lanes per particle (1; 2 or 4 for small systems, which would otherwise leave the GPU with too
+// few threads to hide the latency of ~20 groups walked one after another): lane s of a particle
+// takes its groups s, s + S, ... and the integer kicks are summed across the S lanes (wrapping
+// integer sums: the result does not depend on the split).
+template <int D, bool MULTI, bool INT = false, bool SIG1 = false, int S = 1>
 __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
                                                     const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                     int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
                                                     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                     const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = S == 1 ? t : (t >> 5) * (32u / S) + (t & 31u) / S, seg = S == 1 ? 0u : (t & 31u) % S;
+    if (S == 1 && i >= P.n) return;
+    const bool valid = i < P.n; // (S > 1: every lane takes part in the kick sum)
+    const uint32_t iv = valid ? i : P.n - 1;
     int64_t xi[3];
-    uint32_t si = load_particle<D, MULTI>(pos_in, species, i, xi);
+    uint32_t si = load_particle<D, MULTI>(pos_in, species, iv, xi);
     const float cs = P.kick_cs[si];
     int32_t k[3] = {0, 0, 0};
-    const uint32_t m = __ldg(nbr_count + i), cap4 = (P.cap + 3u) & ~3u;
+    const uint32_t m = valid ? __ldg(nbr_count + i) : 0u, cap4 = (P.cap + 3u) & ~3u;
     const PairC pc0 = P.pc[0];
-    const uint4* groups = reinterpret_cast<const uint4*>(nbr + list_slot(i, 0, cap4)); // group g at groups[32 g]
+    const uint4* groups = reinterpret_cast<const uint4*>(nbr + list_slot(iv, 0, cap4)); // group g at groups[32 g]
     // Every listed neighbour is within 8 sigma of xi at its recorded image (list radius + skin),
     // so neither a minimum image nor a range check is needed.
     auto add_kick = [&](const float* f, const PairC& pc) {
@@ -501,16 +508,16 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
         // Neighbours come from the 16-byte quotient records (one gather each) and the separation
         // is formed with 32-bit integers (quot_sep); a neighbour listed at a periodic image has
         // its quotient record shifted by that image exactly (quot_shift). 2D and 3D alike.
-        const uint4 qi = __ldg(qpos_in + i);
+        const uint4 qi = __ldg(qpos_in + iv);
         const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
-        for (uint32_t g = 0; g < ngroups; g++) {
-            if (g + 2 < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2)));
+        for (uint32_t g = seg; g < ngroups; g += S) {
+            if (g + 2 * S < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2 * S)));
             const uint4 jv = __ldg(groups + 32 * g);
             const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
             const uint32_t left = m - 4 * g;
             uint4 r[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? (jj[u] & LIST_MASK) : i));
+            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? (jj[u] & LIST_MASK) : iv));
             if constexpr (!INT && !MULTI && SIG1) {
                 // Four neighbours as two packed pairs: integer separations per neighbour, then the
                 // f32 chain of both pairs of a pack in f32x2 instructions. Slots past the list end
@@ -560,6 +567,13 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                 }
             }
         }
+    }
+    if constexpr (S > 1) {
+#pragma unroll
+        for (int o = 1; o < S; o <<= 1)
+#pragma unroll
+            for (int a = 0; a < D; a++) k[a] = wadd(k[a], __shfl_xor_sync(0xffffffffu, k[a], o));
+        if (!valid || seg != 0) return;
     }
     int32_t v[3];
 #pragma unroll
