@@ -7,6 +7,7 @@ Reference tests mirrored: crates/md/tests/gpu_engine.rs, three.rs, crates/md/src
 crates/gpu-prims/src/checks.rs."""
 
 import math
+import os
 
 import numpy as np
 import pytest
@@ -207,6 +208,27 @@ def test_trajectory_is_bit_identical_3d_verlet(O):
         g.step(120)
         c.step(120)
         assert g.read_state() == c.state
+
+
+@pytest.mark.parametrize(
+    "dim,n,lanes",
+    [(3, 65536, 2), (3, 200_000, 2), (3, 262144, 1), (2, 300_000, 1), (2, 65535, 4)],
+)
+def test_trajectory_across_lane_splits(O, dim, n, lanes):
+    """The force kernel gives each particle 4, 2 or 1 lanes by system size (below 65536, 262144,
+    else); every variant, through list rebuilds, follows IntEngine's trajectory bit for bit."""
+    if dim == 3:
+        sys_, s0 = liquid3(O, n, 0.8442, 1.2, seed=n)
+    else:
+        sys_, s0 = fluid(O, n, 0.7, Pair.lj(2.5), n % 1000, t=1.2)
+    eng = GpuEngine3 if dim == 3 else GpuEngine
+    with eng(sys_, s0, ForceMode.verlet_with_skin(sys_, n, 0.3)) as g:
+        c = O.IntEngine(sys_, s0, threads=min(16, os.cpu_count() or 1))
+        g.step(40)
+        c.step(40)
+        assert g.read_state() == c.state
+        rebuilds, overflow = g.read_list_stats()
+        assert not overflow and rebuilds > 1
 
 
 def test_config1_triangular_4096_1000_steps(O):
