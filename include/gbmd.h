@@ -84,6 +84,11 @@ typedef struct gbmd_system {
 } gbmd_system;
 
 /* Engine options: ForceMode + Arith + the engine's own tuning knobs. Zero-initialised is valid. */
+/* gbmd_options.flags */
+#define GBMD_FLAG_WHOLE_CELLS 1u /* list builds scan whole neighbour cells (no slab sub-buckets): timing comparisons */
+/* bits 4-7 of flags: lanes per particle of the list build (1, 2, 4 or 8; 0 chooses by size) */
+#define GBMD_FLAG_BUILD_LANES(s) ((uint32_t)(s) << 4)
+
 typedef struct gbmd_options {
     int32_t mode;          /* GBMD_MODE_* */
     int32_t arith;         /* GBMD_ARITH_* */
@@ -93,7 +98,7 @@ typedef struct gbmd_options {
     int32_t device;        /* CUDA device ordinal */
     uint32_t threads;      /* threads per block for the force kernel; 0 selects the tuned value */
     uint32_t rescale_every;/* velocity-rescale thermostat period in steps (0: off) */
-    uint32_t _reserved;
+    uint32_t flags;        /* GBMD_FLAG_* */
     double rescale_t;      /* thermostat target kT */
 } gbmd_options;
 

@@ -53,6 +53,16 @@ class gbmd_system(C.Structure):
     ]
 
 
+FLAG_WHOLE_CELLS = 1  # list builds scan whole neighbour cells (no slab sub-buckets)
+
+
+def build_lanes_flag(lanes):
+    """gbmd_options.flags bits 4-7: lanes per particle of the list build (0 chooses by size)."""
+    if lanes not in (0, 1, 2, 4, 8):
+        raise ValueError("build lanes must be 0, 1, 2, 4 or 8")
+    return lanes << 4
+
+
 class gbmd_options(C.Structure):
     _fields_ = [
         ("mode", C.c_int32),
@@ -63,7 +73,7 @@ class gbmd_options(C.Structure):
         ("device", C.c_int32),
         ("threads", C.c_uint32),
         ("rescale_every", C.c_uint32),
-        ("_reserved", C.c_uint32),
+        ("flags", C.c_uint32),
         ("rescale_t", C.c_double),
     ]
 

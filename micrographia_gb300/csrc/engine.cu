@@ -218,6 +218,9 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
 void set_cells(Params& P, const uint32_t* nc, uint32_t dim) {
     for (uint32_t a = 0; a < 3; a++) P.nc[a] = a < dim ? nc[a] : 1;
     P.ncell = P.nc[0] * P.nc[1] * P.nc[2];
+    P.key_shift = 0;
+    P.sub_scale = 0.0f;
+    P.sub_delta = 0;
     double side = 0.0;
     for (uint32_t a = 0; a < dim; a++) side = std::max(side, P.box_f[a] / (double)P.nc[a]);
     P.sep_unchecked = 2.0 * side < 7.99 ? 1u : 0u;
@@ -233,6 +236,28 @@ int key_bits(uint32_t ncell) {
     int b = 0;
     while (b < 32 && (ncell - 1) >> b) b++;
     return std::max(b, 1);
+}
+
+// List builds: each cell's particles sorted by 2^shift slabs of their last coordinate, so that a
+// particle scans only the slabs of the cells one layer up (down) that can hold a neighbour: those
+// at or below (above) its own slab, 3D: 9 (2 + 2^-shift) cells instead of 27 per lane. The lanes
+// of one warp cover every slab of a cell, so the warp's walk shrinks only when a particle has
+// several lanes (small systems); the shift is the largest that adds no radix pass to the sort.
+static void set_sub_buckets(Params& P, uint32_t dim, double r_list) {
+    const uint32_t a = dim - 1;
+    const int64_t w = P.cell_w[a];
+    if (w <= 256 || w >= ((int64_t)1 << 38)) return; // sub_bucket converts (z_rel >> 8) to i32
+    const int bits = key_bits(P.ncell);
+    int shift = 3;
+    while (shift > 0 && (bits + shift > 31 || radix_passes(bits + shift) > radix_passes(bits))) shift--;
+    if (shift == 0) return;
+    P.key_shift = (uint32_t)shift;
+    P.sub_scale = (float)((double)(1u << shift) / (double)(w >> 8));
+    // A pair the exact list test accepts has |d| < r_list (1 + 2^-21) + 16 on every axis (the f32
+    // roundings of list2s, r2 and the separation); with the cell side w, a neighbour in the next
+    // layer up then sits at most reach - w above the particle's own offset in its cell.
+    const double reach = r_list * (1.0 + 0x1p-20) * 4294967296.0 + 64.0;
+    P.sub_delta = reach > (double)w ? (int64_t)std::ceil(reach - (double)w) : 0;
 }
 static uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
 
@@ -383,19 +408,32 @@ void free_all(gbmd_engine* e) {
 // ---- enqueue helpers (stream-ordered; also used under capture)
 template <int D> void enqueue_bin(gbmd_engine* e, cudaStream_t s, const Params& P) {
     k_keys<D><<<blocks_for(e->n, 256), 256, 0, s>>>(P, (const Rec<D>*)e->pos[e->cur], e->keys[0], e->vals[0]);
-    e->sorted = radix_sort_pairs(e->keys[0], e->vals[0], e->keys[1], e->vals[1], e->n, key_bits(P.ncell), e->hist, e->scan_tmp, s);
-    cell_starts(e->keys[e->sorted], e->n, P.ncell, e->start, s);
+    const uint32_t nkeys = P.ncell << P.key_shift; // cells x slabs (list builds) or cells
+    e->sorted = radix_sort_pairs(e->keys[0], e->vals[0], e->keys[1], e->vals[1], e->n, key_bits(nkeys), e->hist, e->scan_tmp, s);
+    cell_starts(e->keys[e->sorted], e->n, nkeys, e->start, s);
     k_gather<D><<<blocks_for(e->n, 256), 256, 0, s>>>(P, e->vals[e->sorted], e->keys[e->sorted], (const Rec<D>*)e->pos[e->cur], e->vel,
                                                        e->species, e->ids, (Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr,
                                                        e->relf);
-    note_launch(3 + 3 * (uint64_t)radix_passes(key_bits(P.ncell)) + 2);
+    note_launch(3 + 3 * (uint64_t)radix_passes(key_bits(nkeys)) + 2);
 }
+
+// Lanes per particle of the list build: one for large systems, more below these counts, where a
+// lane per particle would leave most of the GPU idle during its ~500-candidate walk.
+static uint32_t build_lanes(uint32_t n) { return n < 24576 ? 8u : (n < 49152 ? 4u : (n < 98304 ? 2u : 1u)); }
 
 template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t s) {
     enqueue_bin<D>(e, s, e->P);
-    k_build_list<D, MULTI><<<blocks_for(e->n, 128), 128, 0, s>>>(
-        e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, e->relf,
-        (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl, e->qpos[e->cur]);
+#define GBMD_BUILD(SS)                                                                                                              \
+    k_build_list<D, MULTI, SS><<<blocks_for((uint64_t)e->n * SS, 128), 128, 0, s>>>(                                               \
+        e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, e->relf,            \
+        (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl, e->qpos[e->cur])
+    switch (((e->opt.flags >> 4) & 15u) ? ((e->opt.flags >> 4) & 15u) : build_lanes(e->n)) {
+    case 8: GBMD_BUILD(8); break;
+    case 4: GBMD_BUILD(4); break;
+    case 2: GBMD_BUILD(2); break;
+    default: GBMD_BUILD(1); break;
+    }
+#undef GBMD_BUILD
     note_launch();
 }
 
@@ -763,6 +801,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         cap = e->opt.cap ? e->opt.cap : (uint32_t)std::ceil(sphere * std::max(2.0 * density, 1.2)) + 8;
     }
     fill_params(e->P, *sys, n, e->skin, cap, nc);
+    if (e->verlet && !(e->opt.flags & GBMD_FLAG_WHOLE_CELLS)) set_sub_buckets(e->P, sys->dim, (rc_max(*sys) + e->skin) * (1.0 + 1e-4));
     e->block_steps = e->opt.block_steps ? e->opt.block_steps : 64;
     if (e->opt.rescale_every) {
         if (!(e->opt.rescale_t > 0.0)) return fail(GBMD_E_INVALID, "the rescale thermostat needs a positive temperature");
@@ -793,7 +832,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     size_t hist_n = radix_hist_elems(n);
     GBMD_TRY(allocT(e, &e->hist, hist_n));
     GBMD_TRY(allocT(e, &e->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(n))));
-    GBMD_TRY(allocT(e, &e->start, (size_t)e->P.ncell + 1));
+    GBMD_TRY(allocT(e, &e->start, ((size_t)e->P.ncell << e->P.key_shift) + 1));
     if (e->verlet) {
         GBMD_TRY(allocT(e, &e->nbr, ((size_t)n + 31) / 32 * 32 * (((size_t)cap + 3) & ~(size_t)3)));
         GBMD_TRY(allocT(e, &e->nbr_count, n));

@@ -46,6 +46,16 @@ template <int D> __device__ __forceinline__ uint32_t cell_key(const Params& P, c
     }
 }
 
+// Slab of a particle's last coordinate inside its cell: floor(2^key_shift z_rel / cell_w) in f32,
+// z_rel the offset from the cell's origin, clamped to [0, 2^key_shift). The list build relies on
+// one property only: the slab does not decrease as z_rel grows.
+__device__ __forceinline__ uint32_t sub_bucket(const Params& P, int64_t zrel) {
+    const int b = __float2int_rd(__fmul_rn(__int2float_rn((int32_t)(zrel >> 8)), P.sub_scale));
+    const int top = (1 << P.key_shift) - 1;
+    return (uint32_t)(b < 0 ? 0 : (b > top ? top : b));
+}
+
+// Cell key per particle; with key_shift > 0 (list builds) the key is cell << key_shift | slab.
 template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t* keys, uint32_t* vals) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
@@ -54,7 +64,9 @@ template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t
 #pragma unroll
     for (int a = 0; a < D; a++) x[a] = wrap(x[a], P.box[a]);
     uint32_t c[3];
-    keys[i] = cell_key<D>(P, x, c);
+    uint32_t key = cell_key<D>(P, x, c);
+    if (P.key_shift) key = (key << P.key_shift) | sub_bucket(P, x[D - 1] - (int64_t)c[D - 1] * P.cell_w[D - 1]);
+    keys[i] = key;
     vals[i] = i;
 }
 
@@ -88,7 +100,7 @@ __global__ void k_gather(Params P, const uint32_t* items, const uint32_t* keys, 
     ids_o[s] = ids[o];
     if (relf) {
         uint32_t c[3];
-        cell_coords(P, keys[s], c);
+        cell_coords(P, keys[s] >> P.key_shift, c);
         const long long* x = reinterpret_cast<const long long*>(&r);
         float4 f;
         f.x = off_f32(x[0] - (int64_t)c[0] * P.cell_w[0]);
@@ -373,7 +385,14 @@ __device__ __forceinline__ float quot_sep_mad(uint32_t Xj, uint32_t rj, uint32_t
 // test of engine.rs:302-313 / 184-186): lists are warp-tiled (list_slot); a particle with
 // more than `cap` neighbours sets ctl[1] (overflow). Also copies the sorted state back into the
 // engine's arrays and records each particle's reference position for the trigger.
-template <int D, bool MULTI>
+// With slab keys (key_shift > 0) a cell one layer up along the last axis is scanned only over its
+// slabs up to the particle's own (of its offset + sub_delta), a cell one layer down only from the
+// particle's own slab (of its offset - sub_delta): a pair the exact test accepts lies within the
+// list radius on that axis, and a cell is at least that wide, so no neighbour is skipped.
+// S lanes per particle (small systems, whose one-lane build is a single long dependent walk):
+// lane s takes candidates s, s + S, ... of each cell and the segment's ballot orders the appends,
+// so the list is the one-lane list entry for entry.
+template <int D, bool MULTI, int S = 1>
 __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* __restrict__ pos_s, const int32_t* __restrict__ vel_s,
                                                     const uint32_t* __restrict__ species_s, const uint32_t* __restrict__ ids_s,
                                                     const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
@@ -382,15 +401,19 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                                                     uint32_t* __restrict__ ids_o, PosRec<D>* __restrict__ ref_pos,
                                                     uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count,
                                                     uint32_t* __restrict__ ctl, uint4* __restrict__ qpos_o) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = t / S, seg = t % S;
+    if (S == 1 && i >= P.n) return;
+    const bool valid = i < P.n; // (S > 1: every lane of the warp takes part in its ballots)
+    const uint32_t iv = valid ? i : P.n - 1;
     int64_t xi[3];
-    uint32_t si = load_particle<D, MULTI>(pos_s, species_s, i, xi);
+    uint32_t si = load_particle<D, MULTI>(pos_s, species_s, iv, xi);
     uint32_t c[3];
-    cell_coords(P, keys[i], c);
+    const uint32_t sh = P.key_shift;
+    cell_coords(P, keys[iv] >> sh, c);
     uint32_t count = 0;
     const uint32_t cap = P.cap, cap4 = (P.cap + 3u) & ~3u;
-    const size_t lbase = list_slot(i, 0, cap4); // entry k at lbase + (k & ~3) 32 + (k & 3)
+    const size_t lbase = list_slot(iv, 0, cap4); // entry k at lbase + (k & ~3) 32 + (k & 3)
     const bool unchecked = P.sep_unchecked;
     // Candidate j of a neighbour cell cj sits at d = relf[j] + base: base = (cj - c) cell_w + shift
     // - (xi - c cell_w), an exact integer converted once per cell. Outside [lo, hi] the f32
@@ -398,6 +421,8 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     int64_t reli[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) reli[a] = a < D ? xi[a] - (int64_t)c[a] * P.cell_w[a] : 0;
+    // slabs [0, up] of the cells a layer up, [dn, top] of those a layer down (all: no slab keys)
+    const uint32_t up = sh ? sub_bucket(P, reli[D - 1] + P.sub_delta) : 0u, dn = sh ? sub_bucket(P, reli[D - 1] - P.sub_delta) : 0u;
     auto exact = [&](uint32_t j, const int64_t* xs, uint32_t sj) -> bool {
         int64_t xj[3];
         load_particle<D, false>(pos_s, nullptr, j, xj);
@@ -424,6 +449,8 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
             int ty = (int)c[1] + oy - 1;
             uint32_t y = ty < 0 ? ny - 1 : (ty >= (int)ny ? 0 : (uint32_t)ty);
             int64_t sy = ty < 0 ? -P.box[1] : (ty >= (int)ny ? P.box[1] : 0);
+            const int layer = D == 3 ? oz : oy; // along the last axis: 0 down, 1 same, 2 up
+            const uint32_t slab0 = layer == 0 ? dn : 0u, slab1 = layer == 2 ? up + 1u : (1u << sh);
             for (int ox = 0; ox < 3; ox++) {
                 int tx = (int)c[0] + ox - 1;
                 uint32_t x = tx < 0 ? nx - 1 : (tx >= (int)nx ? 0 : (uint32_t)tx);
@@ -434,24 +461,52 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                 const float b0 = off_f32(((int64_t)x - (int64_t)c[0]) * P.cell_w[0] + sx - reli[0]);
                 const float b1 = off_f32(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]);
                 const float b2 = D == 3 ? off_f32(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]) : 0.0f;
-                uint32_t j0 = __ldg(start + cell), j1 = __ldg(start + cell + 1);
-#pragma unroll 4
-                for (uint32_t j = j0; j < j1; j++) {
+                const uint32_t j0 = __ldg(start + ((cell << sh) | slab0)), j1 = __ldg(start + (cell << sh) + slab1);
+                auto test = [&](uint32_t j) -> bool {
                     float4 r = __ldg(relf + j);
                     float dx = r.x + b0, dy = r.y + b1, dz = r.z + b2;
                     // approximate (fused) distance: its error is far inside the 1e-4 band
                     float r2a = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
                     uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
                     float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
-                    bool in = r2a < lo || (r2a <= hi && exact(j, xs, sj));
-                    if (in && j != i) {
-                        if (count < cap) nbr[lbase + ((size_t)(count & ~3u) << 5) + (count & 3u)] = j | code;
-                        count++;
+                    return (r2a < lo || (r2a <= hi && exact(j, xs, sj))) && j != i;
+                };
+                if constexpr (S == 1) {
+#pragma unroll 4
+                    for (uint32_t j = j0; j < j1; j++) {
+                        if (test(j)) {
+                            if (count < cap) nbr[lbase + ((size_t)(count & ~3u) << 5) + (count & 3u)] = j | code;
+                            count++;
+                        }
+                    }
+                } else {
+                    // the warp walks the longest of its particles' ranges, so every ballot is whole
+                    const uint32_t lane = threadIdx.x & 31u;
+                    const uint32_t segmask = ((1u << S) - 1u) << (lane & ~(uint32_t)(S - 1));
+                    const uint32_t below = ((1u << lane) - 1u) & segmask;
+                    const uint32_t je = valid ? j1 : j0;
+                    const uint32_t trips = __reduce_max_sync(0xffffffffu, (je - j0 + 4 * S - 1) / (4 * S));
+                    for (uint32_t r = 0; r < trips; r++) {
+                        const uint32_t jb = j0 + r * 4 * S;
+                        bool in[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const uint32_t j = jb + u * S + seg;
+                            in[u] = j < je && test(j);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const uint32_t m = __ballot_sync(0xffffffffu, in[u]) & segmask;
+                            const uint32_t k = count + __popc(m & below);
+                            if (in[u] && k < cap) nbr[lbase + ((size_t)(k & ~3u) << 5) + (k & 3u)] = (jb + u * S + seg) | code;
+                            count += __popc(m);
+                        }
                     }
                 }
             }
         }
     }
+    if (!valid || (S > 1 && seg != 0)) return;
     if (count > cap) {
         ctl[1] = 1;
         count = cap;

@@ -20,9 +20,10 @@ def _ptr(a, t):
     return a.ctypes.data_as(P(t))
 
 
-def _options(mode: ForceMode, threads=0, block_steps=0, rescale_every=0, rescale_t=0.0, arith=_abi.ARITH_F32, device=0):
+def _options(mode: ForceMode, threads=0, block_steps=0, rescale_every=0, rescale_t=0.0, arith=_abi.ARITH_F32, device=0, flags=0):
     o = _abi.gbmd_options()
     o.device = device
+    o.flags = flags
     if mode is None:
         o.mode = _abi.MODE_AUTO
     elif mode.kind == "cells":
@@ -44,16 +45,17 @@ class _Engine:
     STATE = State
 
     def __init__(self, sys, state=None, mode=None, *, init=None, threads=0, block_steps=0, rescale_every=0, rescale_t=0.0, device=0,
-                 arith=_abi.ARITH_F32):
+                 arith=_abi.ARITH_F32, flags=0):
         """Create from (sys, state), or from a device-side seeded init (`init` = gbmd_init).
         `arith`: ARITH_F32 (f32 pair chain, per-pair integer kicks) or ARITH_INT (all-integer
-        tables, IntEngine::integer, int_engine.rs:94-98)."""
+        tables, IntEngine::integer, int_engine.rs:94-98). `flags`: gbmd_options.flags
+        (FLAG_WHOLE_CELLS, build_lanes_flag(s)), list-build variants for comparisons."""
         if sys.DIM != self.DIM:
             raise ValueError(f"{type(self).__name__} needs a {self.DIM}D system")
         self.sys = sys
         self._lib = _abi.lib()
         self._csys = sys.to_c()
-        self._opts = _options(mode, threads, block_steps, rescale_every, rescale_t, arith=arith, device=device)
+        self._opts = _options(mode, threads, block_steps, rescale_every, rescale_t, arith=arith, device=device, flags=flags)
         h = C.c_void_p()
         if init is not None:
             _abi.check(self._lib.gbmd_create_seeded(C.byref(self._csys), C.byref(init), C.byref(self._opts), C.byref(h)))

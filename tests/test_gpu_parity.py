@@ -134,6 +134,35 @@ def test_verlet_lists_match_3d(O):
         assert np.array_equal(got[i], want[i]), i
 
 
+@pytest.mark.parametrize(
+    "dim,n,flags",
+    [
+        (3, 4000, 0),
+        (3, 4000, _abi.FLAG_WHOLE_CELLS),
+        (3, 50000, _abi.build_lanes_flag(1)),
+        (3, 50000, _abi.build_lanes_flag(4)),
+        (3, 50000, _abi.build_lanes_flag(8) | _abi.FLAG_WHOLE_CELLS),
+        (3, 250000, 0),
+        (2, 20000, _abi.build_lanes_flag(8)),
+        (2, 120000, 0),
+    ],
+)
+def test_verlet_lists_across_build_variants(O, dim, n, flags):
+    """Every list build (cells stored by slabs of the last axis or whole; 1, 2, 4 or 8 lanes per
+    particle) gives the oracle's neighbour sets."""
+    if dim == 3:
+        sys_, st = liquid3(O, n, 0.8442, 1.0, seed=n)
+        eng = GpuEngine3
+    else:
+        sys_, st = fluid(O, n, 0.7, Pair.lj(2.5), n % 997)
+        eng = GpuEngine
+    with eng(sys_, st, ForceMode.verlet_with_skin(sys_, n, 0.3), flags=flags) as e:
+        got = e.debug_list()
+    want = O.verlet_lists(sys_, st, 0.3)
+    assert [len(g) for g in got] == [len(w) for w in want]
+    assert np.array_equal(np.concatenate(got), np.concatenate(want))
+
+
 # ---------------------------------------------------------------- kicks (gpu_engine.rs:27-60; three.rs:33-64)
 @pytest.mark.parametrize("pair", [Pair.wca(), Pair.lj(2.5)])
 @pytest.mark.parametrize("mode", ["cells", "verlet"])
