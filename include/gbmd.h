@@ -86,8 +86,11 @@ typedef struct gbmd_system {
 /* Engine options: ForceMode + Arith + the engine's own tuning knobs. Zero-initialised is valid. */
 /* gbmd_options.flags */
 #define GBMD_FLAG_WHOLE_CELLS 1u /* list builds scan whole neighbour cells (no slab sub-buckets): timing comparisons */
+#define GBMD_FLAG_NO_STEP_LOOP 2u /* small systems step through per-step graph nodes, not the persistent step loop: comparisons */
 /* bits 4-7 of flags: lanes per particle of the list build (1, 2, 4 or 8; 0 chooses by size) */
 #define GBMD_FLAG_BUILD_LANES(s) ((uint32_t)(s) << 4)
+/* bits 8-12 of flags: lanes per particle of the force step (1, 2, 4, 8 or 16; 0 chooses by size) */
+#define GBMD_FLAG_FORCE_LANES(s) ((uint32_t)(s) << 8)
 
 typedef struct gbmd_options {
     int32_t mode;          /* GBMD_MODE_* */

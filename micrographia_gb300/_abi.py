@@ -54,6 +54,7 @@ class gbmd_system(C.Structure):
 
 
 FLAG_WHOLE_CELLS = 1  # list builds scan whole neighbour cells (no slab sub-buckets)
+FLAG_NO_STEP_LOOP = 2  # small systems step through per-step graph nodes, not the persistent loop
 
 
 def build_lanes_flag(lanes):
@@ -61,6 +62,13 @@ def build_lanes_flag(lanes):
     if lanes not in (0, 1, 2, 4, 8):
         raise ValueError("build lanes must be 0, 1, 2, 4 or 8")
     return lanes << 4
+
+
+def force_lanes_flag(lanes):
+    """gbmd_options.flags bits 8-12: lanes per particle of the force step (0 chooses by size)."""
+    if lanes not in (0, 1, 2, 4, 8, 16):
+        raise ValueError("force lanes must be 0, 1, 2, 4, 8 or 16")
+    return lanes << 8
 
 
 class gbmd_options(C.Structure):

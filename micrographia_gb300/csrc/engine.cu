@@ -34,6 +34,11 @@ int fail(int code, const std::string& msg) {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch(uint64_t k) { g_launches += k; }
 uint64_t launch_total() { return g_launches.load(); }
+// Engines alive in this process. The persistent step loop holds the whole grid of a cooperative
+// launch for many steps; with several engines sharing the GPU their per-step graphs interleave
+// better (1024 concurrent 2D engines: 3.20 x 10^9 atom-steps/s with per-step graphs, 2.16 with
+// loops), so the loop runs only while its engine is the only one.
+static std::atomic<int> g_live_engines{0};
 
 static double to_f64h(int64_t x) { return (double)x * (1.0 / 4294967296.0); }
 
@@ -278,6 +283,7 @@ struct gbmd_engine {
     int bits = 1;   // significant bits of the cell keys
     cudaStream_t st = nullptr;
     cudaStream_t st_body = nullptr; // capture stream of conditional bodies
+    cudaStream_t st_body2 = nullptr; // and of conditional bodies nested in them
     size_t rec = 16; // bytes per position record
 
     void* pos[2] = {nullptr, nullptr};
@@ -303,8 +309,13 @@ struct gbmd_engine {
     uint32_t block_steps = 64;
     // graphs per [parity][kind]: 0 one step, 1 a block of block_steps, 2 one step + thermostat,
     // 3 the conditional list rebuild alone (frames and kicks between steps)
-    cudaGraphExec_t exec[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
-    uint64_t exec_launches[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    // 4 a block of block_steps through the persistent step loop (small systems)
+    cudaGraphExec_t exec[2][5] = {{nullptr, nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr, nullptr}};
+    uint64_t exec_launches[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
+    uint32_t loop_lanes = 0;  // lanes per particle of the persistent step loop (0: not used)
+    uint32_t loop_blocks = 0; // its grid
+    uint32_t loop_iters = 0;  // its launches so far
+    bool live = false;        // counted in g_live_engines
     // velocity-rescale thermostat (every `rescale_every` steps)
     uint32_t* mrank = nullptr;          // rank of each id among the moving particles
     unsigned long long* tpart = nullptr; // exact KE partials
@@ -390,8 +401,12 @@ static void pinned_give(void* p, size_t cls) {
 }
 
 void free_all(gbmd_engine* e) {
+    if (e->live) {
+        e->live = false;
+        g_live_engines--;
+    }
     for (int p = 0; p < 2; p++)
-        for (int b = 0; b < 4; b++)
+        for (int b = 0; b < 5; b++)
             if (e->exec[p][b]) cudaGraphExecDestroy(e->exec[p][b]);
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
@@ -401,6 +416,7 @@ void free_all(gbmd_engine* e) {
         if (p) cudaFreeAsync(p, e->st);
     if (e->st) cudaStreamDestroy(e->st);
     if (e->st_body) cudaStreamDestroy(e->st_body);
+    if (e->st_body2) cudaStreamDestroy(e->st_body2);
     pinned_give(e->obs_part_h, e->obs_part_cap);
     pinned_give(e->obs_bins_h, e->obs_bins_h_cap);
 }
@@ -455,22 +471,35 @@ void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
     note_launch();
 }
 
-// Below these particle counts the force kernel runs 4 (2) lanes per particle.
-constexpr uint32_t FORCE_SPLIT4_BELOW = 65536, FORCE_SPLIT2_BELOW = 262144;
+// Below these particle counts the force kernel runs 8 (4, 2) lanes per particle.
+constexpr uint32_t FORCE_SPLIT8_BELOW = 20000, FORCE_SPLIT4_BELOW = 65536, FORCE_SPLIT2_BELOW = 262144;
+// Lanes per particle of the force step (single species, f32 chain): gbmd_options.flags bits 8-12
+// when set (1, 2, 4, 8 or 16), else by size.
+static uint32_t force_lanes(const gbmd_engine* e) {
+    const uint32_t o = (e->opt.flags >> 8) & 31u;
+    if (o == 1 || o == 2 || o == 4 || o == 8 || o == 16) return o;
+    return e->n < FORCE_SPLIT8_BELOW ? 8u : (e->n < FORCE_SPLIT4_BELOW ? 4u : (e->n < FORCE_SPLIT2_BELOW ? 2u : 1u));
+}
 template <int D, bool MULTI, bool INT> void enqueue_force_a(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
     if (e->verlet) {
         // sigma = 1 for every pair type (the common LJ case): compiled into the f32 chain
         bool sig1 = !INT;
         for (uint32_t k = 0; k < e->P.ns * e->P.ns; k++) sig1 = sig1 && e->P.pc[k].sigma2s == 0x1p56f;
-        // small single-species systems: several lanes per particle (FORCE_SPLIT4_BELOW, FORCE_SPLIT2_BELOW)
-        const uint32_t split = (!INT && !MULTI) ? (e->n < FORCE_SPLIT4_BELOW ? 4u : (e->n < FORCE_SPLIT2_BELOW ? 2u : 1u)) : 1u;
+        // small single-species systems: several lanes per particle (force_lanes)
+        const uint32_t split = (!INT && !MULTI) ? force_lanes(e) : 1u;
         if (split > 1) {
             const uint32_t lanes = (uint32_t)(((uint64_t)e->n * split + 31) / 32 * 32);
 #define GBMD_SPLIT(SS, SG)                                                                                                          \
     k_force_list<D, false, false, SG, SS><<<blocks_for(lanes, threads), threads, 0, s>>>(                                            \
         e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur], e->qpos[e->cur ^ 1], e->vel, e->species, \
         e->nbr, e->nbr_count, (const Rec<D>*)e->ref_pos, e->ctl)
-            if (split == 4) {
+            if (split == 16) {
+                if (sig1) GBMD_SPLIT(16, true);
+                else GBMD_SPLIT(16, false);
+            } else if (split == 8) {
+                if (sig1) GBMD_SPLIT(8, true);
+                else GBMD_SPLIT(8, false);
+            } else if (split == 4) {
                 if (sig1) GBMD_SPLIT(4, true);
                 else GBMD_SPLIT(4, false);
             } else {
@@ -547,6 +576,136 @@ int upload_ranks(gbmd_engine* e, const uint32_t* species) {
     return GBMD_OK;
 }
 
+// ---- the persistent step loop (graph kind 4)
+constexpr uint32_t CTL_WHILE_ITERS = 10; // WHILE iterations in the current block
+__global__ void k_loop_begin(uint32_t* ctl) {
+    ctl[CTL_LOOP_DONE] = 0;
+    ctl[CTL_WHILE_ITERS] = 0;
+}
+// Repeat the block's body while steps remain. Every iteration takes at least one step (the
+// rebuild before it clears the trigger), so more than target + 1 iterations means something is
+// wrong: stop then too, as after a barrier that ran out.
+__global__ void k_set_while(cudaGraphConditionalHandle h, uint32_t* ctl, uint32_t target) {
+    const uint32_t it = ctl[CTL_WHILE_ITERS] + 1u;
+    ctl[CTL_WHILE_ITERS] = it;
+    const bool more = ctl[CTL_LOOP_DONE] < target && ctl[CTL_LOOP_ERR] == 0u && it <= target + 1u;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+template <int D, int S> cudaError_t launch_loop_t(gbmd_engine* e, cudaStream_t s) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(e->loop_blocks);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative; // every block resident at once: the grid barrier needs it
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_force_loop<D, S>, e->P, (Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur],
+                              e->qpos[e->cur ^ 1], e->vel, (const uint32_t*)e->nbr, (const uint32_t*)e->nbr_count,
+                              (const Rec<D>*)e->ref_pos, e->ctl, e->block_steps);
+}
+template <int D> const void* loop_kernel(uint32_t S) {
+    switch (S) {
+    case 16: return (const void*)k_force_loop<D, 16>;
+    case 8: return (const void*)k_force_loop<D, 8>;
+    case 4: return (const void*)k_force_loop<D, 4>;
+    case 2: return (const void*)k_force_loop<D, 2>;
+    default: return (const void*)k_force_loop<D, 1>;
+    }
+}
+template <int D> cudaError_t enqueue_loop_d(gbmd_engine* e, cudaStream_t s) {
+    switch (e->loop_lanes) {
+    case 16: return launch_loop_t<D, 16>(e, s);
+    case 8: return launch_loop_t<D, 8>(e, s);
+    case 4: return launch_loop_t<D, 4>(e, s);
+    case 2: return launch_loop_t<D, 2>(e, s);
+    default: return launch_loop_t<D, 1>(e, s);
+    }
+}
+cudaError_t enqueue_loop(gbmd_engine* e, cudaStream_t s) {
+    note_launch();
+    return e->D == 2 ? enqueue_loop_d<2>(e, s) : enqueue_loop_d<3>(e, s);
+}
+
+// The persistent loop replaces per-step graph nodes for systems whose force grid fits on the GPU
+// at once (one species, sigma = 1, f32 chain, no thermostat): the per-step conditional rebuild
+// node alone costs more than the whole step of a small system. Lanes per particle as the step
+// kernel's; fewer if the grid would not be resident.
+int setup_step_loop(gbmd_engine* e) {
+    e->loop_lanes = 0;
+    if (!e->verlet || e->multi || e->P.int_mode || e->opt.rescale_every || (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP)) return GBMD_OK;
+    if (!(e->P.pc[0].sigma2s == 0x1p56f)) return GBMD_OK;
+    int coop = 0, sms = 0;
+    GBMD_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->opt.device));
+    GBMD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->opt.device));
+    if (!coop) return GBMD_OK;
+    const uint32_t first = force_lanes(e);
+    for (uint32_t S = first; S >= 1; S >>= 1) {
+        int per = 0;
+        GBMD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, e->D == 2 ? loop_kernel<2>(S) : loop_kernel<3>(S), 128, 0));
+        const uint64_t blocks = ((uint64_t)e->n * S + 127) / 128;
+        if (blocks >= 1 && blocks <= (uint64_t)per * (uint64_t)sms) {
+            e->loop_lanes = S;
+            e->loop_blocks = (uint32_t)blocks;
+            return GBMD_OK;
+        }
+    }
+    return GBMD_OK;
+}
+
+// kind 4: [k_loop_begin] -> WHILE (steps left) { [set IF] -> IF (trigger) { rebuild } -> the loop
+// launch -> [set WHILE] }.
+int capture_loop_block(gbmd_engine* e, cudaStream_t s, uint32_t target, uint64_t* body) {
+    k_loop_begin<<<1, 1, 0, s>>>(e->ctl);
+    note_launch();
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g;
+    const cudaGraphNode_t* deps;
+    const cudaGraphEdgeData* edges;
+    size_t ndeps;
+    GBMD_CUDA_TRY(cudaStreamGetCaptureInfo(s, &status, nullptr, &g, &deps, &edges, &ndeps));
+    cudaGraphConditionalHandle hw;
+    GBMD_CUDA_TRY(cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams wp{};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hw;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    GBMD_CUDA_TRY(cudaGraphAddNode(&wnode, g, deps, edges, ndeps, &wp));
+    GBMD_CUDA_TRY(cudaStreamBeginCaptureToGraph(e->st_body, wp.conditional.phGraph_out[0], nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t gb;
+    GBMD_CUDA_TRY(cudaStreamGetCaptureInfo(e->st_body, &status, nullptr, &gb, &deps, &edges, &ndeps));
+    cudaGraphConditionalHandle hi;
+    GBMD_CUDA_TRY(cudaGraphConditionalHandleCreate(&hi, gb, 0, 0));
+    k_set_cond<<<1, 1, 0, e->st_body>>>(hi, e->ctl);
+    note_launch();
+    GBMD_CUDA_TRY(cudaStreamGetCaptureInfo(e->st_body, &status, nullptr, &gb, &deps, &edges, &ndeps));
+    cudaGraphNodeParams ip{};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = hi;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    cudaGraphNode_t inode;
+    GBMD_CUDA_TRY(cudaGraphAddNode(&inode, gb, deps, edges, ndeps, &ip));
+    GBMD_CUDA_TRY(cudaStreamBeginCaptureToGraph(e->st_body2, ip.conditional.phGraph_out[0], nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const uint64_t b0 = launch_total();
+    enqueue_rebuild(e, e->st_body2);
+    *body = launch_total() - b0;
+    cudaGraph_t tmp;
+    GBMD_CUDA_TRY(cudaStreamEndCapture(e->st_body2, &tmp));
+    GBMD_CUDA_TRY(cudaStreamUpdateCaptureDependencies(e->st_body, &inode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    GBMD_CUDA_TRY(enqueue_loop(e, e->st_body));
+    k_set_while<<<1, 1, 0, e->st_body>>>(hw, e->ctl, target);
+    note_launch();
+    GBMD_CUDA_TRY(cudaStreamEndCapture(e->st_body, &tmp));
+    GBMD_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return GBMD_OK;
+}
+
 // Capture `count` steps starting at parity `parity` into a graph. kind 1 applies the thermostat
 // after every rescale_every-th step of the block (blocks start on a thermostat boundary); kind 2
 // applies it after its single step.
@@ -557,7 +716,11 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, int kind, cudaGrap
     cudaStream_t s = e->st;
     GBMD_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     uint64_t body = 0;
-    for (uint32_t k = 0; k < (kind == 3 ? 1u : count); k++) {
+    if (kind == 4) {
+        GBMD_TRY(capture_loop_block(e, s, count, &body));
+        g_launches -= body; // counted per rebuild instead
+    }
+    for (uint32_t k = 0; k < (kind == 3 ? 1u : (kind == 4 ? 0u : count)); k++) {
         if (e->verlet) {
             cudaStreamCaptureStatus status;
             cudaGraph_t g;
@@ -606,6 +769,7 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, int kind, cudaGrap
     }
     *launches = launch_total() - l0;
     g_launches -= *launches; // launches are counted when the graph is replayed
+    if (kind == 4) *launches = 1; // k_loop_begin; three per WHILE iteration are counted from the device
     e->body_launches = body;
     e->cur = saved_cur;
     return GBMD_OK;
@@ -613,7 +777,7 @@ int capture_steps(gbmd_engine* e, int parity, uint32_t count, int kind, cudaGrap
 
 int run_graph(gbmd_engine* e, int which) {
     int parity = e->cur;
-    uint32_t count = which == 1 ? e->block_steps : (which == 3 ? 0u : 1u);
+    uint32_t count = (which == 1 || which == 4) ? e->block_steps : (which == 3 ? 0u : 1u);
     if (!e->exec[parity][which]) {
         GBMD_TRY(capture_steps(e, parity, count, which, &e->exec[parity][which], &e->exec_launches[parity][which]));
     }
@@ -621,7 +785,7 @@ int run_graph(gbmd_engine* e, int which) {
     e->tcount += count;
     note_launch(e->exec_launches[parity][which]);
     e->launches += e->exec_launches[parity][which];
-    if (e->verlet && (count & 1)) e->cur ^= 1;
+    if (e->verlet && (count & 1) && which != 4) e->cur ^= 1; // (the loop ends in its home buffer)
     return GBMD_OK;
 }
 
@@ -765,10 +929,15 @@ int read_state_dev(gbmd_engine* e) {
 }
 
 int check_ctl(gbmd_engine* e) {
-    uint32_t c[3];
-    GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, 12, cudaMemcpyDeviceToHost, e->st));
+    uint32_t c[11];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, sizeof(c), cudaMemcpyDeviceToHost, e->st));
     GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
     e->last_rebuilds = c[2];
+    e->loop_iters = c[CTL_LOOP_ITERS];
+    if (c[CTL_LOOP_ERR]) {
+        e->failed = true;
+        return fail(GBMD_E_CUDA, "a grid barrier of the persistent step loop ran out of time");
+    }
     if (c[1]) {
         e->failed = true;
         return fail(GBMD_E_OVERFLOW, "a Verlet list overflowed its capacity (raise gbmd_options.cap)");
@@ -777,6 +946,8 @@ int check_ctl(gbmd_engine* e) {
 }
 
 int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd_options* opts) {
+    e->live = true;
+    g_live_engines++;
     e->sys = *sys;
     if (opts) e->opt = *opts;
     e->n = n;
@@ -813,6 +984,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     keep_pool_memory(e->opt.device);
     GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
     GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st_body, cudaStreamNonBlocking));
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&e->st_body2, cudaStreamNonBlocking));
     size_t D = e->D;
     GBMD_TRY(alloc(e, &e->pos[0], n * e->rec));
     GBMD_TRY(alloc(e, &e->pos[1], n * e->rec));
@@ -838,6 +1010,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         GBMD_TRY(allocT(e, &e->nbr_count, n));
     }
     GBMD_TRY(allocT(e, &e->ctl, 16));
+    GBMD_TRY(setup_step_loop(e));
     if (e->opt.arith == GBMD_ARITH_INT) {
         std::vector<int32_t> tab;
         std::vector<double> pair4;
@@ -936,7 +1109,7 @@ int gbmd_step(gbmd_engine* e, uint64_t steps) {
     while (left > 0) {
         bool aligned = every == 0 || e->tcount % every == 0;
         if (aligned && left >= e->block_steps) {
-            GBMD_TRY(run_graph(e, 1));
+            GBMD_TRY(run_graph(e, e->loop_lanes && g_live_engines.load() == 1 ? 4 : 1));
             left -= e->block_steps;
         } else {
             bool thermo = every && (e->tcount + 1) % every == 0;
@@ -1090,9 +1263,10 @@ int gbmd_energy(gbmd_engine* e, double* kinetic, double* potential) {
 
 int gbmd_list_stats(gbmd_engine* e, uint32_t* rebuilds, int32_t* overflow) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    uint32_t c[3];
-    GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, 12, cudaMemcpyDeviceToHost, e->st));
+    uint32_t c[11];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, sizeof(c), cudaMemcpyDeviceToHost, e->st));
     GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    e->loop_iters = c[CTL_LOOP_ITERS];
     if (rebuilds) *rebuilds = c[2];
     if (overflow) *overflow = c[1] ? 1 : 0;
     return GBMD_OK;
@@ -1127,7 +1301,7 @@ int gbmd_launch_count(gbmd_engine* e, uint64_t* launches) {
     uint32_t rebuilds = 0;
     int32_t ov = 0;
     GBMD_TRY(gbmd_list_stats(e, &rebuilds, &ov));
-    *launches = e->launches + (uint64_t)rebuilds * e->body_launches;
+    *launches = e->launches + (uint64_t)rebuilds * e->body_launches + 3ull * e->loop_iters;
     return GBMD_OK;
 }
 

@@ -16,16 +16,22 @@ template <int D> using PosRec = typename PosT<D>::T;
 
 // Position and species of slot i. In 3D the species rides in the record's fourth word; in 2D it
 // is read from `species` when the system has more than one.
-template <int D, bool MULTI>
+// CG: load through L2 only (ld.global.cg), for arrays that other blocks write during the same
+// launch (the persistent step loop); otherwise through the read-only path.
+template <bool CG, class T> __device__ __forceinline__ T ld_in(const T* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return __ldg(p);
+}
+template <int D, bool MULTI, bool CG = false>
 __device__ __forceinline__ uint32_t load_particle(const PosRec<D>* pos, const uint32_t* species, uint32_t i, int64_t* x) {
     if constexpr (D == 2) {
-        longlong2 v = __ldg(pos + i);
+        longlong2 v = ld_in<CG>(pos + i);
         x[0] = v.x;
         x[1] = v.y;
         return MULTI ? __ldg(species + i) : 0u;
     } else {
         const longlong2* q = reinterpret_cast<const longlong2*>(pos + i);
-        longlong2 a = __ldg(q), b = __ldg(q + 1);
+        longlong2 a = ld_in<CG>(q), b = ld_in<CG>(q + 1);
         x[0] = a.x;
         x[1] = a.y;
         x[2] = b.x;
@@ -530,19 +536,17 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // few threads to hide the latency of ~20 groups walked one after another): lane s of a particle
 // takes its groups s, s + S, ... and the integer kicks are summed across the S lanes (wrapping
 // integer sums: the result does not depend on the split).
-template <int D, bool MULTI, bool INT = false, bool SIG1 = false, int S = 1>
-__global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
-                                                    const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
-                                                    int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
-                                                    const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-                                                    const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+template <int D, bool MULTI, bool INT, bool SIG1, int S, bool CG>
+__device__ __forceinline__ bool force_list_one(const Params& P, uint32_t t, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
+                                               const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out, int32_t* __restrict__ vel,
+                                               const uint32_t* __restrict__ species, const uint32_t* __restrict__ nbr,
+                                               const uint32_t* __restrict__ nbr_count, const PosRec<D>* __restrict__ ref_pos) {
     const uint32_t i = S == 1 ? t : (t >> 5) * (32u / S) + (t & 31u) / S, seg = S == 1 ? 0u : (t & 31u) % S;
-    if (S == 1 && i >= P.n) return;
+    if (S == 1 && i >= P.n) return false;
     const bool valid = i < P.n; // (S > 1: every lane takes part in the kick sum)
     const uint32_t iv = valid ? i : P.n - 1;
     int64_t xi[3];
-    uint32_t si = load_particle<D, MULTI>(pos_in, species, iv, xi);
+    uint32_t si = load_particle<D, MULTI, CG>(pos_in, species, iv, xi);
     const float cs = P.kick_cs[si];
     int32_t k[3] = {0, 0, 0};
     const uint32_t m = valid ? __ldg(nbr_count + i) : 0u, cap4 = (P.cap + 3u) & ~3u;
@@ -563,7 +567,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
         // Neighbours come from the 16-byte quotient records (one gather each) and the separation
         // is formed with 32-bit integers (quot_sep); a neighbour listed at a periodic image has
         // its quotient record shifted by that image exactly (quot_shift). 2D and 3D alike.
-        const uint4 qi = __ldg(qpos_in + iv);
+        const uint4 qi = ld_in<CG>(qpos_in + iv);
         const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
         for (uint32_t g = seg; g < ngroups; g += S) {
             if (g + 2 * S < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2 * S)));
@@ -572,7 +576,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
             const uint32_t left = m - 4 * g;
             uint4 r[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? (jj[u] & LIST_MASK) : iv));
+            for (int u = 0; u < 4; u++) r[u] = ld_in<CG>(qpos_in + ((uint32_t)u < left ? (jj[u] & LIST_MASK) : iv));
             if constexpr (!INT && !MULTI && SIG1) {
                 // Four neighbours as two packed pairs: integer separations per neighbour, then the
                 // f32 chain of both pairs of a pack in f32x2 instructions. Slots past the list end
@@ -628,7 +632,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
         for (int o = 1; o < S; o <<= 1)
 #pragma unroll
             for (int a = 0; a < D; a++) k[a] = wadd(k[a], __shfl_xor_sync(0xffffffffu, k[a], o));
-        if (!valid || seg != 0) return;
+        if (!valid || seg != 0) return false;
     }
     int32_t v[3];
 #pragma unroll
@@ -640,7 +644,109 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
     qpos_out[i] = quot_record<D>(xi, si);
     int64_t xr[3];
     load_particle<D, false>(ref_pos, nullptr, i, xr);
-    if (moved_half_skin<D>(P, xr, xi)) ctl[0] = 1;
+    return moved_half_skin<D>(P, xr, xi);
+}
+
+template <int D, bool MULTI, bool INT = false, bool SIG1 = false, int S = 1>
+__global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
+                                                    const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
+                                                    int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
+                                                    const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+                                                    const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (force_list_one<D, MULTI, INT, SIG1, S, false>(P, t, pos_in, pos_out, qpos_in, qpos_out, vel, species, nbr, nbr_count, ref_pos))
+        ctl[0] = 1;
+}
+
+// ---------------------------------------------------------------- the persistent step loop
+// Words of the engine's control block used by the loop (0: trigger, 1: overflow, 2: rebuilds).
+constexpr uint32_t CTL_LOOP_DONE = 4;  // steps the loop has taken in the current graph block
+constexpr uint32_t CTL_BAR_COUNT = 5;  // grid barrier: blocks arrived
+constexpr uint32_t CTL_BAR_GEN = 6;    // grid barrier: generation (low 31 bits) | stop (bit 31)
+constexpr uint32_t CTL_BAR_TRIG = 7;   // grid barrier: a block saw the trigger in this step
+constexpr uint32_t CTL_LOOP_ERR = 8;   // a barrier wait ran out (the loop stopped; an error status)
+constexpr uint32_t CTL_LOOP_ITERS = 9; // loop launches so far (launch accounting)
+constexpr uint32_t BARRIER_SPINS = 1u << 22; // polls of ~100 ns: about half a second
+
+// Grid-wide barrier of a cooperative launch, carrying one bit: whether any block's particles
+// moved half the skin in this step. Thread 0 of each block arrives on a counter; the last to
+// arrive resets it and publishes the next generation with the bit, for which the others poll.
+// A poll is bounded: after BARRIER_SPINS the block records CTL_LOOP_ERR and returns "stop",
+// so a grid that is somehow not co-resident ends with an error status instead of a hang.
+__device__ __forceinline__ bool grid_barrier_stop(uint32_t* ctl, bool moved) {
+    __shared__ uint32_t s_res;
+    const int any = __syncthreads_or(moved ? 1 : 0);
+    if (threadIdx.x == 0) {
+        volatile uint32_t* gen = ctl + CTL_BAR_GEN;
+        const uint32_t g0 = *gen & 0x7fffffffu;
+        if (any) atomicOr(ctl + CTL_BAR_TRIG, 1u);
+        __threadfence();
+        uint32_t res;
+        if (atomicAdd(ctl + CTL_BAR_COUNT, 1u) == gridDim.x - 1) {
+            *(volatile uint32_t*)(ctl + CTL_BAR_COUNT) = 0u;
+            const uint32_t tr = atomicExch(ctl + CTL_BAR_TRIG, 0u);
+            res = ((g0 + 1u) & 0x7fffffffu) | (tr ? 0x80000000u : 0u);
+            __threadfence();
+            atomicExch(ctl + CTL_BAR_GEN, res);
+        } else {
+            uint32_t spins = 0;
+            while (((res = *gen) & 0x7fffffffu) == g0) {
+                if (++spins > BARRIER_SPINS) {
+                    atomicExch(ctl + CTL_LOOP_ERR, 1u);
+                    res = 0x80000000u;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_res = res;
+    }
+    __syncthreads();
+    return (s_res & 0x80000000u) != 0u;
+}
+
+// Steps of the Verlet-list engine in one cooperative launch (small systems, one species, sigma
+// = 1, f32 chain): force + leapfrog + trigger per step as k_force_list, a grid barrier between
+// steps, and out as soon as a particle has moved half the skin (the list must be rebuilt before
+// the next step) or the block of `target` steps is done. Positions ping-pong between pos0 and
+// pos1 inside the launch and end in pos0 (copied back after an odd number of steps), so the
+// graph around it sees one fixed buffer. Positions and records written during the launch are
+// read through L2 only (ld_in<true>).
+template <int D, int S>
+__global__ void __launch_bounds__(128, 10) k_force_loop(Params P, PosRec<D>* __restrict__ pos0, PosRec<D>* __restrict__ pos1,
+                                                    uint4* __restrict__ q0, uint4* __restrict__ q1, int32_t* __restrict__ vel,
+                                                    const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+                                                    const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl, uint32_t target) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    // Words no block writes before every block has read them: the steps done (written at the
+    // end, after the last barrier) and the error word (written only by a barrier that ran out).
+    // (The trigger is not read here: a block that started late could see this launch's own.)
+    const uint32_t done = *(volatile uint32_t*)(ctl + CTL_LOOP_DONE);
+    bool stop = done >= target || *(volatile uint32_t*)(ctl + CTL_LOOP_ERR) != 0u;
+    uint32_t k = 0;
+    while (!stop) {
+        const bool odd = k & 1u;
+        const bool moved = force_list_one<D, false, false, true, S, true>(P, t, odd ? pos1 : pos0, odd ? pos0 : pos1, odd ? q1 : q0,
+                                                                          odd ? q0 : q1, vel, nullptr, nbr, nbr_count, ref_pos);
+        if (moved) ctl[0] = 1;
+        k++;
+        stop = grid_barrier_stop(ctl, moved) || done + k >= target;
+    }
+    const uint32_t i = t / S;
+    if ((k & 1u) && t % S == 0 && i < P.n) {
+        // the record as 16-byte halves (a 3D record is two of them)
+        constexpr int H = sizeof(PosRec<D>) / sizeof(longlong2);
+        const longlong2* src = reinterpret_cast<const longlong2*>(pos1 + i);
+        longlong2* dst = reinterpret_cast<longlong2*>(pos0 + i);
+#pragma unroll
+        for (int h = 0; h < H; h++) dst[h] = __ldcg(src + h);
+        q0[i] = __ldcg(q1 + i);
+    }
+    if (t == 0) {
+        ctl[CTL_LOOP_DONE] = done + k;
+        ctl[CTL_LOOP_ITERS] += 1u;
+    }
 }
 
 // Cell-list force + leapfrog (ForceMode::CellList; md.wgsl:39-76): scans the 3^D cells of the

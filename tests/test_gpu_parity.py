@@ -260,6 +260,55 @@ def test_trajectory_across_lane_splits(O, dim, n, lanes):
         assert not overflow and rebuilds > 1
 
 
+@pytest.mark.parametrize(
+    "dim,n,lanes", [(3, 4000, 0), (3, 4000, 16), (2, 20000, 0), (2, 9000, 16), (3, 100_000, 0), (3, 150_000, 0)]
+)
+def test_step_loop_follows_the_oracle(O, dim, n, lanes):
+    """Small systems step in a persistent loop (a cooperative launch per run of steps between
+    list rebuilds), with 1 to 16 lanes per particle: 200 steps (three 64-step blocks and single
+    steps) equal IntEngine's."""
+    if dim == 3:
+        sys_, s0 = liquid3(O, n, 0.8442, 1.2, seed=n + 1)
+        eng = GpuEngine3
+    else:
+        sys_, s0 = fluid(O, n, 0.7, Pair.lj(2.5), 5, t=1.2)
+        eng = GpuEngine
+    with eng(sys_, s0, ForceMode.verlet_with_skin(sys_, n, 0.3), flags=_abi.force_lanes_flag(lanes)) as g:
+        c = O.IntEngine(sys_, s0, threads=min(16, os.cpu_count() or 1))
+        g.step(200)
+        c.step(200)
+        assert g.read_state() == c.state
+        rebuilds, overflow = g.read_list_stats()
+        assert not overflow and rebuilds > 3
+
+
+@pytest.mark.parametrize("dim,n,t", [(3, 8000, 1.0), (2, 30000, 1.0), (3, 6000, 6.0)])
+def test_step_loop_equals_per_step_graphs(O, dim, n, t):
+    """The loop and the per-step graph nodes give the same state and the same rebuilds over 1000
+    steps, also when a hot fluid rebuilds every few steps; two engines alive at once both step
+    through per-step graphs."""
+    if dim == 3:
+        sys_, s0 = liquid3(O, n, 0.8442, t, seed=7)
+        eng = GpuEngine3
+    else:
+        sys_, s0 = fluid(O, n, 0.7, Pair.lj(2.5), 9, t=t)
+        eng = GpuEngine
+    mode = ForceMode.verlet_with_skin(sys_, n, 0.3)
+    runs = []
+    for flags in (0, _abi.FLAG_NO_STEP_LOOP):  # one engine at a time: the loop runs for a lone engine
+        with eng(sys_, s0, mode, flags=flags) as g:
+            g.step(1000)
+            runs.append((g.read_state().hash(), g.read_list_stats(), g.launch_count()))
+    (ha, ra, la), (hb, rb, lb) = runs
+    assert ha == hb
+    assert ra == rb and ra[0] > 10
+    assert la < lb
+    with eng(sys_, s0, mode) as a, eng(sys_, s0, mode) as b:
+        a.step(1000)
+        b.step(1000)
+        assert a.read_state().hash() == ha and a.launch_count() == lb
+
+
 def test_config1_triangular_4096_1000_steps(O):
     """2D LJ N=4096, rho 0.70, triangular start, T=0.8, seed 1, cell list, 1000 steps: the GPU
     state equals md-ref's IntEngine<f32> bit for bit."""
