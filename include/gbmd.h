@@ -203,6 +203,11 @@ int gbmd_debug_bin(gbmd_engine* e, const uint32_t* cells, uint32_t* keys, uint32
 /* The Verlet list as built now: for each id, its neighbour ids (any order), `counts[id]` of
  * them, packed in id order into `nbr` (capacity `nbr_cap` entries). */
 int gbmd_debug_list(gbmd_engine* e, uint32_t* counts, uint32_t* nbr, uint64_t nbr_cap);
+/* No counterpart in the reference. The failure path of the persistent step loop's grid barrier,
+ * exercised without a GPU fault: a cooperative launch of `blocks` blocks of which block 0 never
+ * arrives, so the others' bounded waits run out (a fraction of a second). Returns what the
+ * engine then reports: GBMD_E_TIMEOUT with the barrier's message, the engine in its failed state. */
+int gbmd_debug_barrier_timeout(gbmd_engine* e, uint32_t blocks);
 
 /* ---- Seeded initial conditions on the device (md_core::init, crates/md-core/src/init.rs) ---- */
 

@@ -187,6 +187,7 @@ SIGNATURES = [
     ("gbmd_time_phases", C.c_int, [VP, C.c_uint32, _DP, _DP, _U32P]),
     ("gbmd_debug_bin", C.c_int, [VP, _U32P, _U32P, _U32P, _U32P, _U32P]),
     ("gbmd_debug_list", C.c_int, [VP, _U32P, _U32P, C.c_uint64]),
+    ("gbmd_debug_barrier_timeout", C.c_int, [VP, C.c_uint32]),
     ("gbmd_init_state", C.c_int, [P(gbmd_system), P(gbmd_init), _I64P, _I32P, _U32P]),
     ("gbmd_create_seeded", C.c_int, [P(gbmd_system), P(gbmd_init), P(gbmd_options), P(VP)]),
     ("gbmd_bin_cells_static", C.c_int, [P(gbmd_system), C.c_void_p, C.c_uint32, _U32P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

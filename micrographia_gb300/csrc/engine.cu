@@ -637,6 +637,7 @@ cudaError_t enqueue_loop(gbmd_engine* e, cudaStream_t s) {
 int setup_step_loop(gbmd_engine* e) {
     e->loop_lanes = 0;
     if (!e->verlet || e->multi || e->P.int_mode || e->opt.rescale_every || (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP)) return GBMD_OK;
+    if (e->block_steps > (1u << 20)) return GBMD_OK; // (the barrier counts k x blocks arrivals in 32 bits)
     if (!(e->P.pc[0].sigma2s == 0x1p56f)) return GBMD_OK;
     int coop = 0, sms = 0;
     GBMD_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->opt.device));
@@ -936,7 +937,7 @@ int check_ctl(gbmd_engine* e) {
     e->loop_iters = c[CTL_LOOP_ITERS];
     if (c[CTL_LOOP_ERR]) {
         e->failed = true;
-        return fail(GBMD_E_CUDA, "a grid barrier of the persistent step loop ran out of time");
+        return fail(GBMD_E_TIMEOUT, "a grid barrier of the persistent step loop ran out of time");
     }
     if (c[1]) {
         e->failed = true;
@@ -1103,7 +1104,7 @@ int gbmd_destroy(gbmd_engine* e) {
 
 int gbmd_step(gbmd_engine* e, uint64_t steps) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    if (e->failed) return fail(GBMD_E_OVERFLOW, "the engine is in a failed state (a list overflowed)");
+    if (e->failed) return fail(GBMD_E_OVERFLOW, "the engine is in a failed state (a list overflowed, or a step-loop barrier ran out); gbmd_upload a state to continue");
     uint64_t left = steps;
     uint32_t every = e->opt.rescale_every;
     while (left > 0) {
@@ -1153,6 +1154,8 @@ int gbmd_upload(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const ui
     e->failed = false;
     uint32_t zero[2] = {0, 0};
     GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, zero, 8, cudaMemcpyHostToDevice, e->st));
+    // the step loop's words (steps done, barrier, error, WHILE count), as at creation
+    GBMD_CUDA_TRY(cudaMemsetAsync(e->ctl + CTL_LOOP_DONE, 0, (CTL_BAR_ARRIVE + 2 - CTL_LOOP_DONE) * 4, e->st));
     return upload_state(e, pos, vel, species);
 }
 
@@ -1376,6 +1379,24 @@ int gbmd_debug_bin(gbmd_engine* e, const uint32_t* cells, uint32_t* keys, uint32
     // the sort state is scratch only: the pair structure must be rebuilt before the next use
     uint32_t one = 1;
     GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    return gbmd_sync(e);
+}
+
+int gbmd_debug_barrier_timeout(gbmd_engine* e, uint32_t blocks) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (blocks < 2 || blocks > 64) return fail(GBMD_E_INVALID, "blocks must be 2 .. 64");
+    GBMD_TRY(gbmd_sync(e));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(128);
+    cfg.stream = e->st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GBMD_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_barrier_absent, e->ctl, 0u));
+    note_launch();
     return gbmd_sync(e);
 }
 

@@ -660,50 +660,83 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
 
 // ---------------------------------------------------------------- the persistent step loop
 // Words of the engine's control block used by the loop (0: trigger, 1: overflow, 2: rebuilds).
-constexpr uint32_t CTL_LOOP_DONE = 4;  // steps the loop has taken in the current graph block
-constexpr uint32_t CTL_BAR_COUNT = 5;  // grid barrier: blocks arrived
-constexpr uint32_t CTL_BAR_GEN = 6;    // grid barrier: generation (low 31 bits) | stop (bit 31)
-constexpr uint32_t CTL_BAR_TRIG = 7;   // grid barrier: a block saw the trigger in this step
-constexpr uint32_t CTL_LOOP_ERR = 8;   // a barrier wait ran out (the loop stopped; an error status)
-constexpr uint32_t CTL_LOOP_ITERS = 9; // loop launches so far (launch accounting)
-constexpr uint32_t BARRIER_SPINS = 1u << 22; // polls of ~100 ns: about half a second
+constexpr uint32_t CTL_LOOP_DONE = 4;   // steps the loop has taken in the current graph block
+constexpr uint32_t CTL_BAR_GEN = 6;     // grid barrier: barriers released (low 31 bits) | stop (bit 31)
+constexpr uint32_t CTL_LOOP_ERR = 8;    // a barrier wait ran out (the loop stopped; an error status)
+constexpr uint32_t CTL_LOOP_ITERS = 9;  // loop launches so far (launch accounting)
+constexpr uint32_t CTL_BAR_ARRIVE = 12; // grid barrier, words 12-13 as one 64-bit counter: arrivals in
+                                        // this launch | blocks that saw the trigger << 32
+constexpr uint32_t BARRIER_SPINS = 1u << 20; // polls of 0.1-0.5 us: well under a second
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 // Grid-wide barrier of a cooperative launch, carrying one bit: whether any block's particles
-// moved half the skin in this step. Thread 0 of each block arrives on a counter; the last to
-// arrive resets it and publishes the next generation with the bit, for which the others poll.
-// A poll is bounded: after BARRIER_SPINS the block records CTL_LOOP_ERR and returns "stop",
-// so a grid that is somehow not co-resident ends with an error status instead of a hang.
-__device__ __forceinline__ bool grid_barrier_stop(uint32_t* ctl, bool moved) {
-    __shared__ uint32_t s_res;
-    const int any = __syncthreads_or(moved ? 1 : 0);
-    if (threadIdx.x == 0) {
-        volatile uint32_t* gen = ctl + CTL_BAR_GEN;
-        const uint32_t g0 = *gen & 0x7fffffffu;
-        if (any) atomicOr(ctl + CTL_BAR_TRIG, 1u);
-        __threadfence();
-        uint32_t res;
-        if (atomicAdd(ctl + CTL_BAR_COUNT, 1u) == gridDim.x - 1) {
-            *(volatile uint32_t*)(ctl + CTL_BAR_COUNT) = 0u;
-            const uint32_t tr = atomicExch(ctl + CTL_BAR_TRIG, 0u);
-            res = ((g0 + 1u) & 0x7fffffffu) | (tr ? 0x80000000u : 0u);
-            __threadfence();
-            atomicExch(ctl + CTL_BAR_GEN, res);
-        } else {
-            uint32_t spins = 0;
-            while (((res = *gen) & 0x7fffffffu) == g0) {
-                if (++spins > BARRIER_SPINS) {
-                    atomicExch(ctl + CTL_LOOP_ERR, 1u);
-                    res = 0x80000000u;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        s_res = res;
+// moved half the skin in this step. Thread 0 of each block arrives with one 64-bit atomic add
+// (one arrival, plus one in the high word if the block saw the trigger). The block whose add
+// completes the k-th barrier of the launch (k x blocks arrivals) publishes generation base + k
+// with the stop bit by a release store; the others poll for it with acquire loads. No word is
+// reset between barriers, so an arrival costs one atomic round trip and a release one store.
+// A poll is bounded: after BARRIER_SPINS the block records CTL_LOOP_ERR and returns "stop", so a
+// grid that is somehow not co-resident ends with an error status instead of a hang. The arrival
+// counter is cleared by block 0 after the launch's last barrier (every block has arrived then).
+struct GridBarrier {
+    uint32_t* ctl;
+    uint32_t base;  // generation when the launch began (read by every block before any release)
+    uint32_t k = 0; // barriers of this launch so far
+    __device__ static uint32_t begin(uint32_t* ctl) {
+        __shared__ uint32_t s_base;
+        if (threadIdx.x == 0) s_base = ld_acquire_gpu(ctl + CTL_BAR_GEN) & 0x7fffffffu;
+        __syncthreads();
+        return s_base;
     }
-    __syncthreads();
-    return (s_res & 0x80000000u) != 0u;
+    __device__ bool wait(bool moved) {
+        __shared__ uint32_t s_res;
+        const int any = __syncthreads_or(moved ? 1 : 0);
+        k++;
+        if (threadIdx.x == 0) {
+            const uint32_t want = (base + k) & 0x7fffffffu;
+            __threadfence(); // the block's stores (seen through the CTA barrier) before its arrival
+            const unsigned long long old = atomicAdd(reinterpret_cast<unsigned long long*>(ctl + CTL_BAR_ARRIVE), any ? 0x100000001ull : 1ull);
+            const uint32_t arrived = (uint32_t)old + 1u, saw = (uint32_t)(old >> 32) + (any ? 1u : 0u);
+            uint32_t res;
+            if (arrived == k * gridDim.x) {
+                res = want | (saw ? 0x80000000u : 0u);
+                st_release_gpu(ctl + CTL_BAR_GEN, res);
+            } else {
+                uint32_t spins = 0;
+                while (((res = ld_acquire_gpu(ctl + CTL_BAR_GEN)) & 0x7fffffffu) != want) {
+                    if (++spins > BARRIER_SPINS) {
+                        atomicExch(ctl + CTL_LOOP_ERR, 1u);
+                        res = 0x80000000u;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            __threadfence();
+            s_res = res;
+        }
+        __syncthreads();
+        return (s_res & 0x80000000u) != 0u;
+    }
+    // after the launch's last barrier: block 0 clears the arrival counter for the next launch
+    __device__ void end() const {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<unsigned long long*>(ctl + CTL_BAR_ARRIVE) = 0ull;
+    }
+};
+
+// The barrier with block `absent` never arriving: the others' waits run out (CTL_LOOP_ERR).
+static __global__ void k_barrier_absent(uint32_t* ctl, uint32_t absent) {
+    GridBarrier bar{ctl, GridBarrier::begin(ctl)};
+    if (blockIdx.x == absent) return;
+    bar.wait(false);
 }
 
 // Steps of the Verlet-list engine in one cooperative launch (small systems, one species, sigma
@@ -724,6 +757,7 @@ __global__ void __launch_bounds__(128, 10) k_force_loop(Params P, PosRec<D>* __r
     // (The trigger is not read here: a block that started late could see this launch's own.)
     const uint32_t done = *(volatile uint32_t*)(ctl + CTL_LOOP_DONE);
     bool stop = done >= target || *(volatile uint32_t*)(ctl + CTL_LOOP_ERR) != 0u;
+    GridBarrier bar{ctl, GridBarrier::begin(ctl)};
     uint32_t k = 0;
     while (!stop) {
         const bool odd = k & 1u;
@@ -731,8 +765,9 @@ __global__ void __launch_bounds__(128, 10) k_force_loop(Params P, PosRec<D>* __r
                                                                           odd ? q0 : q1, vel, nullptr, nbr, nbr_count, ref_pos);
         if (moved) ctl[0] = 1;
         k++;
-        stop = grid_barrier_stop(ctl, moved) || done + k >= target;
+        stop = bar.wait(moved) || done + k >= target;
     }
+    bar.end();
     const uint32_t i = t / S;
     if ((k & 1u) && t % S == 0 && i < P.n) {
         // the record as 16-byte halves (a 3D record is two of them)

@@ -214,6 +214,10 @@ class _Engine:
         )
         return keys, start, items, order
 
+    def debug_barrier_timeout(self, blocks=4):
+        """Raw status of gbmd_debug_barrier_timeout (the step loop's barrier running out)."""
+        return self._lib.gbmd_debug_barrier_timeout(self._h, int(blocks))
+
     def debug_list(self, max_total=None):
         counts = np.empty(self.n, np.uint32)
         cap = max_total or self.n * 256

@@ -769,3 +769,20 @@ def test_server_budget_and_cancel():
         with pytest.raises(_abi.GbmdError) as ei:
             sv.poll()
         assert ei.value.code == _abi.E_BUDGET
+
+
+def test_step_loop_barrier_runs_out_with_a_status(O):
+    """The grid barrier's bounded wait: a cooperative launch whose block 0 never arrives makes the
+    other blocks give up; the engine reports GBMD_E_TIMEOUT and refuses further steps, and the
+    GPU stays usable (a new engine steps normally afterwards)."""
+    sys3, s0 = liquid3(O, 4000, 0.8442, 0.72)
+    with GpuEngine3(sys3, s0) as g:
+        assert g.debug_barrier_timeout(4) == _abi.E_TIMEOUT
+        assert b"ran out of time" in _abi.lib().gbmd_last_error()
+        with pytest.raises(RuntimeError):
+            g.step(1)
+    with GpuEngine3(sys3, s0) as g:
+        c = O.IntEngine(sys3, s0)
+        g.step(70)
+        c.step(70)
+        assert g.read_state() == c.state
