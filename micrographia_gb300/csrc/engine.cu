@@ -422,15 +422,18 @@ void free_all(gbmd_engine* e) {
 }
 
 // ---- enqueue helpers (stream-ordered; also used under capture)
+// keys + first histogram -> radix passes -> gather with the cell starts (n >= 1).
 template <int D> void enqueue_bin(gbmd_engine* e, cudaStream_t s, const Params& P) {
-    k_keys<D><<<blocks_for(e->n, 256), 256, 0, s>>>(P, (const Rec<D>*)e->pos[e->cur], e->keys[0], e->vals[0]);
     const uint32_t nkeys = P.ncell << P.key_shift; // cells x slabs (list builds) or cells
-    e->sorted = radix_sort_pairs(e->keys[0], e->vals[0], e->keys[1], e->vals[1], e->n, key_bits(nkeys), e->hist, e->scan_tmp, s);
-    cell_starts(e->keys[e->sorted], e->n, nkeys, e->start, s);
+    const uint32_t tiles = blocks_for(e->n, RADIX_TILE);
+    k_keys_hist<D><<<tiles, 256, 0, s>>>(P, (const Rec<D>*)e->pos[e->cur], e->keys[0], e->vals[0], e->hist, tiles);
+    uint32_t sort_launches = 0;
+    e->sorted = radix_sort_pairs(e->keys[0], e->vals[0], e->keys[1], e->vals[1], e->n, key_bits(nkeys), e->hist, e->scan_tmp, s, true,
+                                 &sort_launches);
     k_gather<D><<<blocks_for(e->n, 256), 256, 0, s>>>(P, e->vals[e->sorted], e->keys[e->sorted], (const Rec<D>*)e->pos[e->cur], e->vel,
                                                        e->species, e->ids, (Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr,
-                                                       e->relf);
-    note_launch(3 + 3 * (uint64_t)radix_passes(key_bits(nkeys)) + 2);
+                                                       e->relf, e->start, nkeys);
+    note_launch(2 + sort_launches);
 }
 
 // Lanes per particle of the list build: one for large systems, more below these counts, where a
@@ -453,10 +456,6 @@ template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t
     note_launch();
 }
 
-__global__ void k_rebuild_done(uint32_t* ctl) {
-    ctl[0] = 0;
-    ctl[2] += 1;
-}
 __global__ void k_set_cond(cudaGraphConditionalHandle h, const uint32_t* ctl) { cudaGraphSetConditional(h, ctl[0] ? 1u : 0u); }
 
 void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
@@ -467,8 +466,6 @@ void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
         if (e->multi) enqueue_rebuild_t<3, true>(e, s);
         else enqueue_rebuild_t<3, false>(e, s);
     }
-    k_rebuild_done<<<1, 1, 0, s>>>(e->ctl);
-    note_launch();
 }
 
 // Below these particle counts the force kernel runs 8 (4, 2) lanes per particle.
@@ -578,6 +575,7 @@ int upload_ranks(gbmd_engine* e, const uint32_t* species) {
 
 // ---- the persistent step loop (graph kind 4)
 constexpr uint32_t CTL_WHILE_ITERS = 10; // WHILE iterations in the current block
+constexpr uint32_t STEP_LOOP_BELOW = 98304; // particles: the loop is used below this
 __global__ void k_loop_begin(uint32_t* ctl) {
     ctl[CTL_LOOP_DONE] = 0;
     ctl[CTL_WHILE_ITERS] = 0;
@@ -638,6 +636,9 @@ int setup_step_loop(gbmd_engine* e) {
     e->loop_lanes = 0;
     if (!e->verlet || e->multi || e->P.int_mode || e->opt.rescale_every || (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP)) return GBMD_OK;
     if (e->block_steps > (1u << 20)) return GBMD_OK; // (the barrier counts k x blocks arrivals in 32 bits)
+    // Larger systems' steps are long enough that the graph's per-step nodes cost less than the
+    // loop's barrier (3D N = 131,072: 71 us per step in graphs, 76 in the loop; 65,536: 53 vs 49).
+    if (e->n >= STEP_LOOP_BELOW) return GBMD_OK;
     if (!(e->P.pc[0].sigma2s == 0x1p56f)) return GBMD_OK;
     int coop = 0, sms = 0;
     GBMD_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->opt.device));

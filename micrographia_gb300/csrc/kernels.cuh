@@ -9,6 +9,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "sort.cuh"
 
 namespace gbmd {
 
@@ -61,10 +62,8 @@ __device__ __forceinline__ uint32_t sub_bucket(const Params& P, int64_t zrel) {
     return (uint32_t)(b < 0 ? 0 : (b > top ? top : b));
 }
 
-// Cell key per particle; with key_shift > 0 (list builds) the key is cell << key_shift | slab.
-template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t* keys, uint32_t* vals) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+// Cell key of particle i; with key_shift > 0 (list builds) the key is cell << key_shift | slab.
+template <int D> __device__ __forceinline__ uint32_t particle_key(const Params& P, const PosRec<D>* pos, uint32_t i) {
     int64_t x[3];
     load_particle<D, false>(pos, nullptr, i, x);
 #pragma unroll
@@ -72,8 +71,34 @@ template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t
     uint32_t c[3];
     uint32_t key = cell_key<D>(P, x, c);
     if (P.key_shift) key = (key << P.key_shift) | sub_bucket(P, x[D - 1] - (int64_t)c[D - 1] * P.cell_w[D - 1]);
-    keys[i] = key;
+    return key;
+}
+template <int D> __global__ void k_keys(Params P, const PosRec<D>* pos, uint32_t* keys, uint32_t* vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    keys[i] = particle_key<D>(P, pos, i);
     vals[i] = i;
+}
+// The keys fused with the first radix pass's histogram: block b keys the RADIX_TILE particles of
+// tile b (rounds of 256) and counts their low 8 bits into hist[d tiles + b], the layout of the
+// sort's own histogram kernel, which the sort then skips for that pass.
+template <int D>
+__global__ void __launch_bounds__(256) k_keys_hist(Params P, const PosRec<D>* pos, uint32_t* keys, uint32_t* vals, uint32_t* hist, uint32_t tiles) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * RADIX_TILE;
+    for (uint32_t r = 0; r < RADIX_TILE / 256; r++) {
+        const uint32_t i = base + r * 256 + threadIdx.x;
+        if (i < P.n) {
+            const uint32_t key = particle_key<D>(P, pos, i);
+            keys[i] = key;
+            vals[i] = i;
+            atomicAdd(&cnt[key & 255u], 1u);
+        }
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * tiles + blockIdx.x] = cnt[threadIdx.x];
 }
 
 __device__ __forceinline__ void cell_coords(const Params& P, uint32_t key, uint32_t* c);
@@ -86,12 +111,20 @@ __device__ __forceinline__ float off_f32(int64_t v) { return __fmul_rn(__int2flo
 // Storage permutation into cell order (one fused gather; reorder.wgsl's gathers + copy-backs).
 // Also records each particle's position relative to its cell's origin (c * cell_w, an exact
 // integer) as f32 sigma, with its species in the fourth word, for the list build's prefilter.
+// With `start` given, also the cell starts of the sorted keys (as cell_starts: start[c] = first
+// slot with key >= c, c in [0, nkeys]).
 template <int D>
 __global__ void k_gather(Params P, const uint32_t* items, const uint32_t* keys, const PosRec<D>* pos, const int32_t* vel,
                          const uint32_t* species, const uint32_t* ids, PosRec<D>* pos_o, int32_t* vel_o, uint32_t* species_o,
-                         uint32_t* ids_o, float4* relf) {
+                         uint32_t* ids_o, float4* relf, uint32_t* start = nullptr, uint32_t nkeys = 0) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= P.n) return;
+    if (start) {
+        const uint32_t cur = keys[s];
+        for (int64_t c = s == 0 ? 0 : (int64_t)keys[s - 1] + 1; c <= (int64_t)cur; c++) start[c] = s;
+        if (s == P.n - 1)
+            for (uint64_t c = (uint64_t)cur + 1; c <= nkeys; c++) start[c] = P.n;
+    }
     uint32_t o = items[s];
     PosRec<D> r = pos[o];
     {
@@ -409,6 +442,10 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                                                     uint32_t* __restrict__ ctl, uint4* __restrict__ qpos_o) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = t / S, seg = t % S;
+    if (t == 0) {
+        ctl[0] = 0; // the rebuild is done: clear the trigger, count it
+        ctl[2] += 1;
+    }
     if (S == 1 && i >= P.n) return;
     const bool valid = i < P.n; // (S > 1: every lane of the warp takes part in its ballots)
     const uint32_t iv = valid ? i : P.n - 1;

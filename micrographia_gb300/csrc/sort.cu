@@ -86,13 +86,27 @@ __global__ void k_radix_hist(const uint32_t* keys, uint32_t n, int shift, uint32
 }
 
 // Stable scatter of one tile: items are ranked in index order, warp by warp within a round of
-// 256, round by round; offs[d * tiles + tile] is the tile's first slot for digit d.
+// 256, round by round; offs[d * tiles + tile] is the tile's first slot for digit d. LOCAL: offs
+// is the histogram itself (few tiles), and each block forms its own offsets from it (the digits
+// before d over all tiles, plus digit d over the tiles before this one), with no scan launches.
+template <bool LOCAL>
 __global__ void k_radix_scatter(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n, int shift,
                                 const uint32_t* offs, uint32_t tiles) {
     __shared__ uint32_t base[256];
     __shared__ uint32_t wcnt[RADIX_WARPS][257];
     int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    base[t] = offs[(size_t)t * tiles + blockIdx.x];
+    if constexpr (LOCAL) {
+        uint32_t own = 0, tot = 0;
+        for (uint32_t j = 0; j < tiles; j++) {
+            const uint32_t c = offs[(size_t)t * tiles + j];
+            tot += c;
+            own += j < blockIdx.x ? c : 0u;
+        }
+        uint32_t all;
+        base[t] = block_exclusive_scan(tot, &all) + own;
+    } else {
+        base[t] = offs[(size_t)t * tiles + blockIdx.x];
+    }
 #pragma unroll
     for (int w = 0; w < RADIX_WARPS; w++) wcnt[w][t] = 0;
     __syncthreads();
@@ -169,20 +183,39 @@ void scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp, 
 
 int radix_passes(int bits) { return bits <= 0 ? 1 : (bits + 7) / 8; }
 
+// Kernels scan_exclusive launches for n elements.
+static uint32_t scan_launches(size_t n) {
+    if (n == 0) return 0;
+    size_t nb = blocks_of(n, SCAN_ITEMS);
+    return nb == 1 ? 1u : 2u + scan_launches(nb);
+}
+
 int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits, uint32_t* hist, uint32_t* tmp,
-                     cudaStream_t s) {
+                     cudaStream_t s, bool first_hist_done, uint32_t* launches) {
     if (n == 0) return 0;
     uint32_t tiles = (uint32_t)blocks_of(n, RADIX_TILE);
     int passes = radix_passes(bits);
+    const bool local = tiles <= RADIX_LOCAL_TILES;
     uint32_t *ki = k0, *vi = v0, *ko = k1, *vo = v1;
+    uint32_t count = 0;
     for (int p = 0; p < passes; p++) {
         int shift = 8 * p;
-        k_radix_hist<<<tiles, RADIX_THREADS, 0, s>>>(ki, n, shift, hist, tiles);
-        scan_exclusive(hist, hist, (size_t)256 * tiles, tmp, s);
-        k_radix_scatter<<<tiles, RADIX_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles);
+        if (p > 0 || !first_hist_done) {
+            k_radix_hist<<<tiles, RADIX_THREADS, 0, s>>>(ki, n, shift, hist, tiles);
+            count++;
+        }
+        if (local) {
+            k_radix_scatter<true><<<tiles, RADIX_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles);
+        } else {
+            count += scan_launches((size_t)256 * tiles);
+            scan_exclusive(hist, hist, (size_t)256 * tiles, tmp, s);
+            k_radix_scatter<false><<<tiles, RADIX_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles);
+        }
+        count++;
         std::swap(ki, ko);
         std::swap(vi, vo);
     }
+    if (launches) *launches = count;
     return passes & 1;
 }
 

@@ -12,6 +12,8 @@ namespace gbmd {
 
 constexpr uint32_t SCAN_ITEMS = 2048;  // elements per block of the scan (256 threads x 8)
 constexpr uint32_t RADIX_TILE = 2048;  // keys per block of a radix pass (8 rounds of 256)
+constexpr uint32_t RADIX_THREADS_PER_TILE = 256;
+constexpr uint32_t RADIX_LOCAL_TILES = 64; // up to this many tiles, scatter blocks form their own offsets
 
 // Scratch sizes (in uint32 elements).
 size_t scan_tmp_elems(size_t n);
@@ -23,8 +25,12 @@ void scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp, 
 // Stable sort of n (key, value) pairs by the low `bits` bits of the key, 8 bits per pass,
 // ping-ponging between (k0, v0) and (k1, v1). Returns 0 if the result is in (k0, v0), 1 if in
 // (k1, v1). `hist` holds radix_hist_elems(n) elements, `tmp` scan_tmp_elems(radix_hist_elems(n)).
+// With few tiles (RADIX_LOCAL_TILES or fewer) each scatter block forms its offsets from the
+// histogram itself: two launches per pass. `first_hist_done`: the caller's key kernel has already
+// written the first pass's histogram (k_keys_hist). `launches`, if given, receives the count of
+// kernels launched.
 int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits, uint32_t* hist, uint32_t* tmp,
-                     cudaStream_t s);
+                     cudaStream_t s, bool first_hist_done = false, uint32_t* launches = nullptr);
 int radix_passes(int bits);
 
 // start[c] = first index of sorted `keys` with key >= c, for c in [0, ncell]; start[ncell] = n.

@@ -261,7 +261,7 @@ def test_trajectory_across_lane_splits(O, dim, n, lanes):
 
 
 @pytest.mark.parametrize(
-    "dim,n,lanes", [(3, 4000, 0), (3, 4000, 16), (2, 20000, 0), (2, 9000, 16), (3, 100_000, 0), (3, 150_000, 0)]
+    "dim,n,lanes", [(3, 4000, 0), (3, 4000, 16), (2, 20000, 0), (2, 9000, 16), (3, 60_000, 0), (3, 90_000, 1)]
 )
 def test_step_loop_follows_the_oracle(O, dim, n, lanes):
     """Small systems step in a persistent loop (a cooperative launch per run of steps between
