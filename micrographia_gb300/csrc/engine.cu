@@ -247,7 +247,9 @@ int key_bits(uint32_t ncell) {
 // particle scans only the slabs of the cells one layer up (down) that can hold a neighbour: those
 // at or below (above) its own slab, 3D: 9 (2 + 2^-shift) cells instead of 27 per lane. The lanes
 // of one warp cover every slab of a cell, so the warp's walk shrinks only when a particle has
-// several lanes (small systems); the shift is the largest that adds no radix pass to the sort.
+// several lanes: used for multi-lane builds (small systems) only, where with one lane per
+// particle the lanes' different slab ranges only add divergence. The shift is the largest that
+// adds no radix pass to the sort.
 static void set_sub_buckets(Params& P, uint32_t dim, double r_list) {
     const uint32_t a = dim - 1;
     const int64_t w = P.cell_w[a];
@@ -439,6 +441,10 @@ template <int D> void enqueue_bin(gbmd_engine* e, cudaStream_t s, const Params& 
 // Lanes per particle of the list build: one for large systems, more below these counts, where a
 // lane per particle would leave most of the GPU idle during its ~500-candidate walk.
 static uint32_t build_lanes(uint32_t n) { return n < 24576 ? 8u : (n < 49152 ? 4u : (n < 98304 ? 2u : 1u)); }
+static uint32_t list_build_lanes(const gbmd_engine* e) {
+    const uint32_t o = (e->opt.flags >> 4) & 15u;
+    return o ? o : build_lanes(e->n);
+}
 
 template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t s) {
     enqueue_bin<D>(e, s, e->P);
@@ -446,7 +452,7 @@ template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t
     k_build_list<D, MULTI, SS><<<blocks_for((uint64_t)e->n * SS, 128), 128, 0, s>>>(                                               \
         e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, e->relf,            \
         (Rec<D>*)e->pos[e->cur], e->vel, e->species, e->ids, (Rec<D>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl, e->qpos[e->cur])
-    switch (((e->opt.flags >> 4) & 15u) ? ((e->opt.flags >> 4) & 15u) : build_lanes(e->n)) {
+    switch (list_build_lanes(e)) {
     case 8: GBMD_BUILD(8); break;
     case 4: GBMD_BUILD(4); break;
     case 2: GBMD_BUILD(2); break;
@@ -974,7 +980,8 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         cap = e->opt.cap ? e->opt.cap : (uint32_t)std::ceil(sphere * std::max(2.0 * density, 1.2)) + 8;
     }
     fill_params(e->P, *sys, n, e->skin, cap, nc);
-    if (e->verlet && !(e->opt.flags & GBMD_FLAG_WHOLE_CELLS)) set_sub_buckets(e->P, sys->dim, (rc_max(*sys) + e->skin) * (1.0 + 1e-4));
+    if (e->verlet && !(e->opt.flags & GBMD_FLAG_WHOLE_CELLS) && list_build_lanes(e) > 1)
+        set_sub_buckets(e->P, sys->dim, (rc_max(*sys) + e->skin) * (1.0 + 1e-4));
     e->block_steps = e->opt.block_steps ? e->opt.block_steps : 64;
     if (e->opt.rescale_every) {
         if (!(e->opt.rescale_t > 0.0)) return fail(GBMD_E_INVALID, "the rescale thermostat needs a positive temperature");

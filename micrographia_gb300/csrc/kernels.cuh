@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     int64_t xi[3];
     uint32_t si = load_particle<D, MULTI>(pos_s, species_s, iv, xi);
     uint32_t c[3];
-    const uint32_t sh = P.key_shift;
+    const uint32_t sh = S > 1 ? P.key_shift : 0u; // (slab keys come only with several lanes)
     cell_coords(P, keys[iv] >> sh, c);
     uint32_t count = 0;
     const uint32_t cap = P.cap, cap4 = (P.cap + 3u) & ~3u;
@@ -465,7 +465,8 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 #pragma unroll
     for (int a = 0; a < 3; a++) reli[a] = a < D ? xi[a] - (int64_t)c[a] * P.cell_w[a] : 0;
     // slabs [0, up] of the cells a layer up, [dn, top] of those a layer down (all: no slab keys)
-    const uint32_t up = sh ? sub_bucket(P, reli[D - 1] + P.sub_delta) : 0u, dn = sh ? sub_bucket(P, reli[D - 1] - P.sub_delta) : 0u;
+    const uint32_t up = (S > 1 && sh) ? sub_bucket(P, reli[D - 1] + P.sub_delta) : 0u;
+    const uint32_t dn = (S > 1 && sh) ? sub_bucket(P, reli[D - 1] - P.sub_delta) : 0u;
     auto exact = [&](uint32_t j, const int64_t* xs, uint32_t sj) -> bool {
         int64_t xj[3];
         load_particle<D, false>(pos_s, nullptr, j, xj);

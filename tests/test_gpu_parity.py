@@ -786,3 +786,22 @@ def test_step_loop_barrier_runs_out_with_a_status(O):
         g.step(70)
         c.step(70)
         assert g.read_state() == c.state
+
+
+@pytest.mark.parametrize("n,loop", [(4000, True), (4000, False), (120_000, False)])
+def test_list_overflow_is_reported(O, n, loop):
+    """A list capacity below the neighbour count: the build clamps the lists and sets the
+    overflow word; the engine reports GBMD_E_OVERFLOW and refuses further steps, in the step loop
+    and in per-step graphs alike; an upload clears the failed state."""
+    sys3, s0 = liquid3(O, n, 0.8442, 0.72)
+    flags = 0 if loop else _abi.FLAG_NO_STEP_LOOP
+    with GpuEngine3(sys3, s0, ForceMode.verlet_with_skin(sys3, n, 0.3, cap=16), flags=flags) as g:
+        g.step(70)
+        with pytest.raises(_abi.GbmdError) as err:
+            g.wait()
+        assert err.value.code == _abi.E_OVERFLOW
+        assert g.read_list_stats()[1]
+        with pytest.raises(_abi.GbmdError):
+            g.step(1)
+        g.upload(s0)
+        assert g.read_state() == s0
