@@ -2,11 +2,14 @@
 // md::GpuEngine / md::GpuEngine3 (crates/md/src/engine.rs:598-1098, engine3.rs:334-648).
 //
 // One CUDA stream per engine. A step is: [if the rebuild flag is set: cell keys -> stable radix
-// sort -> cell starts -> gather into cell order -> Verlet-list build] -> fused LJ force +
+// sort -> gather into cell order with the cell starts -> Verlet-list build] -> fused LJ force +
 // leapfrog + displacement trigger. Steps are captured into CUDA graphs (blocks of
 // `block_steps`), and the rebuild runs inside a conditional graph node whose condition a
 // one-thread kernel reads from the device flag, so the decision never returns to the host (the
-// reference's indirect-dispatch gate, gpu-prims prims.rs:250-283 / gate.wgsl:13-24).
+// reference's indirect-dispatch gate, gpu-prims prims.rs:250-283 / gate.wgsl:13-24). Small
+// systems run a block as a persistent step loop instead (setup_step_loop, capture_loop_block):
+// cooperative launches that step until the trigger fires, in a WHILE node with the rebuild in a
+// nested IF.
 #include <algorithm>
 #include <atomic>
 #include <cmath>

@@ -570,10 +570,11 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // ping-pongs the two), so every kick sees positions of the same time step.
 // Ten blocks of 128 per SM (48 registers, a 16-byte spill outside the pair loop): measured 2.4%
 // faster than the unconstrained 62 registers at eight blocks.
-// S lanes per particle (1; 2 or 4 for small systems, which would otherwise leave the GPU with too
-// few threads to hide the latency of ~20 groups walked one after another): lane s of a particle
-// takes its groups s, s + S, ... and the integer kicks are summed across the S lanes (wrapping
-// integer sums: the result does not depend on the split).
+// S lanes per particle (1; up to 16 for small systems, which would otherwise leave the GPU with
+// too few threads to hide the latency of ~20 groups walked one after another): lane s of a
+// particle takes its groups s, s + S, ... and the integer kicks are summed across the S lanes
+// (wrapping integer sums: the result does not depend on the split). CG: positions and records
+// are read through L2 only (the persistent step loop, where other blocks rewrite them).
 template <int D, bool MULTI, bool INT, bool SIG1, int S, bool CG>
 __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t t, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
                                                const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out, int32_t* __restrict__ vel,
