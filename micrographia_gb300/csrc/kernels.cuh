@@ -144,7 +144,8 @@ __global__ void k_gather(Params P, const uint32_t* items, const uint32_t* keys, 
         float4 f;
         f.x = off_f32(x[0] - (int64_t)c[0] * P.cell_w[0]);
         f.y = off_f32(x[1] - (int64_t)c[1] * P.cell_w[1]);
-        f.z = D == 3 ? off_f32(x[2] - (int64_t)c[2] * P.cell_w[2]) : 0.0f;
+        // (2D: the cell's x index, exact in f32, for the list build's row walk)
+        f.z = D == 3 ? off_f32(x[2] - (int64_t)c[2] * P.cell_w[2]) : (float)c[0];
         f.w = __uint_as_float(sp);
         relf[s] = f;
     }
@@ -495,6 +496,32 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
             int64_t sy = ty < 0 ? -P.box[1] : (ty >= (int)ny ? P.box[1] : 0);
             const int layer = D == 3 ? oz : oy; // along the last axis: 0 down, 1 same, 2 up
             const uint32_t slab0 = layer == 0 ? dn : 0u, slab1 = layer == 2 ? up + 1u : (1u << sh);
+            if constexpr (D == 2 && S == 1) {
+                // 2D, away from the x edges: the row's three cells are consecutive keys, one range
+                // with no x image; a candidate's offset from this particle's cell is its cell's x
+                // index (the record's third word) minus this one's, in cell widths.
+                if (c[0] >= 1u && c[0] + 1u < nx) {
+                    const uint32_t row0 = y * nx + c[0] - 1u;
+                    const uint32_t j0 = __ldg(start + row0), j1 = __ldg(start + row0 + 3u);
+                    const int64_t xs[3] = {xi[0], xi[1] - sy, 0};
+                    const uint32_t code = image_code(0, sy, 0);
+                    const float b0 = off_f32(-reli[0]), wf = off_f32(P.cell_w[0]), cxf = (float)c[0];
+                    const float b1 = off_f32(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]);
+#pragma unroll 4
+                    for (uint32_t j = j0; j < j1; j++) {
+                        float4 r = __ldg(relf + j);
+                        float dx = __fmaf_rn(__fsub_rn(r.z, cxf), wf, __fadd_rn(r.x, b0)), dy = r.y + b1;
+                        float r2a = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                        uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                        float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
+                        if ((r2a < lo || (r2a <= hi && exact(j, xs, sj))) && j != i) {
+                            if (count < cap) nbr[lbase + ((size_t)(count & ~3u) << 5) + (count & 3u)] = j | code;
+                            count++;
+                        }
+                    }
+                    continue;
+                }
+            }
             for (int ox = 0; ox < 3; ox++) {
                 int tx = (int)c[0] + ox - 1;
                 uint32_t x = tx < 0 ? nx - 1 : (tx >= (int)nx ? 0 : (uint32_t)tx);
@@ -508,7 +535,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                 const uint32_t j0 = __ldg(start + ((cell << sh) | slab0)), j1 = __ldg(start + (cell << sh) + slab1);
                 auto test = [&](uint32_t j) -> bool {
                     float4 r = __ldg(relf + j);
-                    float dx = r.x + b0, dy = r.y + b1, dz = r.z + b2;
+                    float dx = r.x + b0, dy = r.y + b1, dz = D == 3 ? r.z + b2 : 0.0f;
                     // approximate (fused) distance: its error is far inside the 1e-4 band
                     float r2a = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
                     uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
