@@ -158,6 +158,29 @@ int gbmd_restore(gbmd_engine* e, const void* buf, size_t size);
 /* Flip one bit of one coordinate of particle `id` (engine.rs:964, State::flip_bit). */
 int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit);
 
+/* ---- Page commands and run-time changes: md::GpuEngine (crates/md/src/engine.rs:895-1063) ---- */
+
+/* engine.rs:1026-1036 (md.wgsl:216-229, md3.wgsl:541-553): for every unpinned particle whose f32
+ * position, f32(x >> 32) + f32(x & 0xffffffff) 2^-32 per axis, lies in [lo, hi) (bounds rounded
+ * to f32): v <- rint(f32(v) * f32(scale)) + add on each axis, `add` a velocity in sigma/tau turned
+ * into position units per step by System::to_step_displacement. lo, hi, add: `dim` entries. */
+int gbmd_kick_region(gbmd_engine* e, const double* lo, const double* hi, double scale, const double* add);
+/* engine.rs:1042-1053 (reorder.wgsl:80-99): the particles with these ids (any order, repeats
+ * allowed) take `species`; masses and forces follow from the next step (the lists are rebuilt). */
+int gbmd_set_species(gbmd_engine* e, const uint32_t* ids, uint32_t count, uint32_t species);
+/* engine.rs:1056-1063 (md.wgsl:151-156): every particle of `species` gets the velocity v
+ * (sigma/tau, `dim` entries, as position units per step). */
+int gbmd_set_species_velocity(gbmd_engine* e, uint32_t species, const double* v);
+/* engine.rs:943-947: re-sort the storage into cell order and rebuild the lists now (the
+ * reference sorts into Morton order; the storage order is invisible to results either way). */
+int gbmd_sort_now(gbmd_engine* e);
+/* engine.rs:895-934: replace the interactions, masses, gravity, pinned species or dt at run time.
+ * The dimension, box and species count stay; no cutoff may exceed the largest the engine was
+ * built with (its cells and list capacity are sized by it); an all-integer engine keeps its
+ * tables (pairs, masses, dt, pinned). Velocities are kept as they are (position units per step).
+ * The lists are rebuilt before the next step. GBMD_E_INVALID otherwise, the engine unchanged. */
+int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys);
+
 /* ---- Observables: IntEngine::energy (int_engine.rs:433-446) and the new instruments ---- */
 
 int gbmd_energy(gbmd_engine* e, double* kinetic, double* potential);

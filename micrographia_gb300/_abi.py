@@ -175,6 +175,11 @@ SIGNATURES = [
     ("gbmd_snapshot", C.c_int, [VP, VP, C.c_size_t, P(C.c_size_t)]),
     ("gbmd_restore", C.c_int, [VP, VP, C.c_size_t]),
     ("gbmd_flip_bit", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32]),
+    ("gbmd_kick_region", C.c_int, [VP, _DP, _DP, C.c_double, _DP]),
+    ("gbmd_set_species", C.c_int, [VP, _U32P, C.c_uint32, C.c_uint32]),
+    ("gbmd_set_species_velocity", C.c_int, [VP, C.c_uint32, _DP]),
+    ("gbmd_sort_now", C.c_int, [VP]),
+    ("gbmd_update_system", C.c_int, [VP, P(gbmd_system)]),
     ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
     ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),
     ("gbmd_observe_begin", C.c_int, [VP, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32]),

@@ -643,7 +643,9 @@ cudaError_t enqueue_loop(gbmd_engine* e, cudaStream_t s) {
 // kernel's; fewer if the grid would not be resident.
 int setup_step_loop(gbmd_engine* e) {
     e->loop_lanes = 0;
-    if (!e->verlet || e->multi || e->P.int_mode || e->opt.rescale_every || (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP)) return GBMD_OK;
+    if (!e->verlet || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every ||
+        (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP))
+        return GBMD_OK;
     if (e->block_steps > (1u << 20)) return GBMD_OK; // (the barrier counts k x blocks arrivals in 32 bits)
     // Larger systems' steps are long enough that the graph's per-step nodes cost less than the
     // loop's barrier (3D N = 131,072: 71 us per step in graphs, 76 in the loop; 65,536: 53 vs 49).
@@ -901,6 +903,59 @@ template <int D> __global__ void k_flip(uint32_t n, const uint32_t* ids, uint32_
     p[axis] ^= (long long)(1ull << bit);
 }
 
+// ---- page commands (md::GpuEngine, crates/md/src/engine.rs:1026-1063)
+struct RegionCmd {
+    float lo[3], hi[3];
+    float scale;
+    int32_t add[3];
+};
+// md.wgsl:216-229 / md3.wgsl:541-553: for every unpinned particle whose coord_f32 position
+// (f32(x >> 32) + f32(x & 0xffffffff) 2^-32, of the wrapped position) is inside [lo, hi):
+// v <- rint(f32(v) scale) + add per axis, the sum wrapping.
+template <int D> __global__ void k_kick_region(Params P, const Rec<D>* pos, const uint32_t* species, int32_t* vel, RegionCmd C) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.n || ((P.pinned >> species[s]) & 1u)) return;
+    int64_t x[3];
+    load_particle<D, false>(pos, nullptr, s, x);
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const uint64_t w = (uint64_t)wrap(x[a], P.box[a]);
+        const float c = __fadd_rn(__uint2float_rn((uint32_t)(w >> 32)), __fmul_rn(__uint2float_rn((uint32_t)w), 0x1p-32f));
+        if (c < C.lo[a] || c >= C.hi[a]) return;
+    }
+#pragma unroll
+    for (int a = 0; a < D; a++) vel[D * s + a] = wadd(__float2int_rn(__fmul_rn(__int2float_rn(vel[D * s + a]), C.scale)), C.add[a]);
+}
+// reorder.wgsl:80-99 / md3.wgsl:556-574: the particles whose ids are in the sorted `list` take
+// species `to` (in the species array, the 3D record's fourth word and the quotient record's top byte).
+template <int D>
+__global__ void k_set_species(uint32_t n, const uint32_t* ids, const uint32_t* list, uint32_t count, uint32_t to, uint32_t* species, Rec<D>* pos,
+                              uint4* qpos) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t id = ids[s];
+    uint32_t lo = 0, hi = count;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (list[mid] < id) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo >= count || list[lo] != id) return;
+    species[s] = to;
+    if constexpr (D == 3) reinterpret_cast<long long*>(pos + s)[3] = (long long)to;
+    if (qpos) qpos[s].w = (qpos[s].w & 0x00ffffffu) | (to << 24);
+}
+// md.wgsl:151-156 / md3.wgsl:655-660: every particle of species `sp` gets velocity v.
+__global__ void k_set_species_velocity(uint32_t n, uint32_t dim, const uint32_t* species, uint32_t sp, int3 v, int32_t* vel) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || species[s] != sp) return;
+    vel[dim * s] = v.x;
+    vel[dim * s + 1] = v.y;
+    if (dim == 3) vel[dim * s + 2] = v.z;
+}
+// System::to_step_displacement (system.rs:427-429): (v dt 2^32).round() as i32.
+int32_t to_step_displacement(const gbmd_system& s, double v) { return sat_i32_host(std::round(v * s.dt * 4294967296.0)); }
+
 int upload_state(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const uint32_t* species) {
     size_t n = e->n, D = e->D;
     for (size_t i = 0; i < n; i++)
@@ -1022,7 +1077,6 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         GBMD_TRY(allocT(e, &e->nbr_count, n));
     }
     GBMD_TRY(allocT(e, &e->ctl, 16));
-    GBMD_TRY(setup_step_loop(e));
     if (e->opt.arith == GBMD_ARITH_INT) {
         std::vector<int32_t> tab;
         std::vector<double> pair4;
@@ -1037,6 +1091,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         e->P.itab = e->itab;
         e->P.ipair = e->ipair;
     }
+    GBMD_TRY(setup_step_loop(e)); // (after the pair arithmetic is settled: f32 engines only)
     GBMD_TRY(allocT(e, &e->relf, n));
     GBMD_TRY(allocT(e, &e->qpos[0], n));
     GBMD_TRY(allocT(e, &e->qpos[1], n));
@@ -1264,6 +1319,116 @@ int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit) {
     note_launch();
     uint32_t one = 1;
     GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    return gbmd_sync(e);
+}
+
+int gbmd_kick_region(gbmd_engine* e, const double* lo, const double* hi, double scale, const double* add) {
+    if (!e || !lo || !hi || !add) return fail(GBMD_E_INVALID, "null argument");
+    RegionCmd C{};
+    for (int a = 0; a < 3; a++) {
+        C.lo[a] = a < e->D ? (float)lo[a] : 0.0f;
+        C.hi[a] = a < e->D ? (float)hi[a] : 0.0f;
+        C.add[a] = a < e->D ? to_step_displacement(e->sys, add[a]) : 0;
+    }
+    C.scale = (float)scale;
+    if (e->D == 2) k_kick_region<2><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->P, (const Rec<2>*)e->pos[e->cur], e->species, e->vel, C);
+    else k_kick_region<3><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->P, (const Rec<3>*)e->pos[e->cur], e->species, e->vel, C);
+    note_launch();
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return GBMD_OK;
+}
+
+int gbmd_set_species(gbmd_engine* e, const uint32_t* ids, uint32_t count, uint32_t species) {
+    if (!e || (count && !ids)) return fail(GBMD_E_INVALID, "null argument");
+    if (species >= e->sys.nspecies) return fail(GBMD_E_INVALID, "species index out of range");
+    if (count == 0) return GBMD_OK;
+    std::vector<uint32_t> list(ids, ids + count);
+    std::sort(list.begin(), list.end());
+    list.erase(std::unique(list.begin(), list.end()), list.end());
+    if (list.back() >= e->n) return fail(GBMD_E_INVALID, "particle id out of range");
+    uint32_t* d_list = nullptr;
+    if (cudaMallocAsync((void**)&d_list, list.size() * 4, e->st) != cudaSuccess) return fail(GBMD_E_NOMEM, "set_species list");
+    GBMD_CUDA_TRY(cudaMemcpyAsync(d_list, list.data(), list.size() * 4, cudaMemcpyHostToDevice, e->st));
+    const uint32_t m = (uint32_t)list.size();
+    if (e->D == 2)
+        k_set_species<2><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->ids, d_list, m, species, e->species, (Rec<2>*)e->pos[e->cur],
+                                                                    e->verlet ? e->qpos[e->cur] : nullptr);
+    else
+        k_set_species<3><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->ids, d_list, m, species, e->species, (Rec<3>*)e->pos[e->cur],
+                                                                    e->verlet ? e->qpos[e->cur] : nullptr);
+    note_launch();
+    GBMD_CUDA_TRY(cudaFreeAsync(d_list, e->st));
+    // lists are built with per-pair radii: rebuild before the next step
+    uint32_t one = 1;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    if (e->sys.pinned) { // the moving set (the thermostat's zero-momentum ranks) may have changed
+        std::vector<uint32_t> sp(e->n);
+        GBMD_TRY(gbmd_read_state(e, nullptr, nullptr, sp.data()));
+        GBMD_TRY(upload_ranks(e, sp.data()));
+    }
+    return gbmd_sync(e);
+}
+
+int gbmd_set_species_velocity(gbmd_engine* e, uint32_t species, const double* v) {
+    if (!e || !v) return fail(GBMD_E_INVALID, "null argument");
+    if (species >= e->sys.nspecies) return fail(GBMD_E_INVALID, "species index out of range");
+    int3 d = make_int3(to_step_displacement(e->sys, v[0]), to_step_displacement(e->sys, v[1]), e->D == 3 ? to_step_displacement(e->sys, v[2]) : 0);
+    k_set_species_velocity<<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, (uint32_t)e->D, e->species, species, d, e->vel);
+    note_launch();
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return GBMD_OK;
+}
+
+int gbmd_sort_now(gbmd_engine* e) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_TRY(prepare_pairs(e));
+    return gbmd_sync(e);
+}
+
+int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
+    if (!e || !sys) return fail(GBMD_E_INVALID, "null argument");
+    GBMD_TRY(validate_system(*sys, e->n));
+    const gbmd_system& o = e->sys;
+    if (sys->dim != o.dim || sys->nspecies != o.nspecies) return fail(GBMD_E_INVALID, "update_system keeps the dimension and the species count");
+    for (uint32_t a = 0; a < o.dim; a++)
+        if (sys->box_len[a] != o.box_len[a]) return fail(GBMD_E_INVALID, "update_system keeps the box");
+    if (rc_max(*sys) > rc_max(o) + 1e-12) return fail(GBMD_E_INVALID, "cutoffs cannot grow at run time");
+    if (e->P.int_mode) {
+        bool same = sys->dt == o.dt && sys->pinned == o.pinned;
+        for (uint32_t k = 0; k < o.nspecies; k++) same = same && sys->masses[k] == o.masses[k];
+        for (uint32_t k = 0; k < o.nspecies * o.nspecies; k++)
+            same = same && std::memcmp(&sys->pairs[k], &o.pairs[k], sizeof(gbmd_pair)) == 0;
+        if (!same) return fail(GBMD_E_INVALID, "integer tables are fixed at creation: pairs, masses, dt and pinned species cannot change");
+    }
+    GBMD_TRY(gbmd_sync(e));
+    const bool pinned_changed = sys->pinned != o.pinned;
+    Params old = e->P;
+    e->sys = *sys;
+    fill_params(e->P, e->sys, e->n, e->skin, old.cap, old.nc);
+    // the geometry and list sizing of creation, the integer tables, the slabs
+    e->P.key_shift = old.key_shift;
+    e->P.sub_scale = old.sub_scale;
+    e->P.sub_delta = old.sub_delta;
+    e->P.int_mode = old.int_mode;
+    e->P.itab_len = old.itab_len;
+    e->P.itab = old.itab;
+    e->P.ipair = old.ipair;
+    std::memcpy(e->P.irc2, old.irc2, sizeof(old.irc2));
+    // graphs hold the old parameter block by value: capture again on the next step
+    for (int p = 0; p < 2; p++)
+        for (int b = 0; b < 5; b++)
+            if (e->exec[p][b]) {
+                GBMD_CUDA_TRY(cudaGraphExecDestroy(e->exec[p][b]));
+                e->exec[p][b] = nullptr;
+            }
+    GBMD_TRY(setup_step_loop(e));
+    uint32_t one = 1;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    if (pinned_changed) {
+        std::vector<uint32_t> sp(e->n);
+        GBMD_TRY(gbmd_read_state(e, nullptr, nullptr, sp.data()));
+        GBMD_TRY(upload_ranks(e, sp.data()));
+    }
     return gbmd_sync(e);
 }
 

@@ -149,6 +149,32 @@ class _Engine:
     def flip_bit(self, particle, axis, bit):
         _abi.check(self._lib.gbmd_flip_bit(self._h, particle, axis, bit))
 
+    # page commands and run-time changes (md::GpuEngine, crates/md/src/engine.rs:895-1063)
+    def kick_region(self, lo, hi, scale, add):
+        """Unpinned particles inside [lo, hi) (sigma): v <- rint(v * scale) + add (sigma/tau)."""
+        arr = lambda v: (C.c_double * self.DIM)(*[float(x) for x in v])
+        _abi.check(self._lib.gbmd_kick_region(self._h, arr(lo), arr(hi), float(scale), arr(add)))
+
+    def set_species(self, ids, species):
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        _abi.check(self._lib.gbmd_set_species(self._h, _ptr(ids, C.c_uint32), int(ids.size), int(species)))
+
+    def set_species_velocity(self, species, v):
+        _abi.check(self._lib.gbmd_set_species_velocity(self._h, int(species), (C.c_double * self.DIM)(*[float(x) for x in v])))
+
+    def sort_now(self):
+        _abi.check(self._lib.gbmd_sort_now(self._h))
+
+    def update_system(self, sys):
+        """Replace interactions, masses, gravity, pinned species or dt (same box and species
+        count; no cutoff above the engine's largest)."""
+        if sys.DIM != self.DIM:
+            raise ValueError("update_system keeps the dimension")
+        csys = sys.to_c()
+        _abi.check(self._lib.gbmd_update_system(self._h, C.byref(csys)))
+        self.sys = sys
+        self._csys = csys
+
     def energy(self):
         ke, pe = C.c_double(), C.c_double()
         _abi.check(self._lib.gbmd_energy(self._h, C.byref(ke), C.byref(pe)))

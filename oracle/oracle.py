@@ -5,6 +5,7 @@ bench.py's CPU baseline. The engine package never imports this module.
 """
 
 import ctypes as C
+import math
 import os
 import sys
 
@@ -216,6 +217,62 @@ def half_step_kinetic(sys, state):
 def exact_kinetic(sys, state):
     c = sys.to_c()
     return lib().oracle_exact_kinetic(C.byref(c), _p(state.vel, C.c_int32), _p(state.species, C.c_uint32), state.n())
+
+
+# ---------------------------------------------------------------- page commands
+def to_step_displacement(sys, v):
+    """System::to_step_displacement (md-core system.rs:427-429): (v dt 2^32).round() as i32,
+    Rust's round (half away from zero, exact) and saturating cast (NaN -> 0)."""
+    x = float(v) * sys.dt * 4294967296.0
+    if x != x:
+        return 0
+    r = math.trunc(x)
+    if abs(x - r) >= 0.5:
+        r += 1 if x > 0 else -1
+    return int(min(max(r, -(1 << 31)), (1 << 31) - 1))
+
+
+def _coord_f32(x):
+    """coord_f32 (md/shaders/params.wgsl:117-119) of positions in [0, L): f32(hi) + ldexp(f32(lo), -32)."""
+    u = x.astype(np.int64).view(np.uint64)
+    hi = (u >> np.uint64(32)).astype(np.uint32).astype(np.float32)
+    lo = (u & np.uint64(0xFFFFFFFF)).astype(np.uint32).astype(np.float32)
+    return (hi + np.ldexp(lo, -32).astype(np.float32)).astype(np.float32)
+
+
+def kick_region(sys, state, lo, hi, scale, add):
+    """GpuEngine::kick_region (md/src/engine.rs:1026-1036) as md.wgsl:216-229 / md3.wgsl:541-553
+    compute it: unpinned particles with lo <= coord_f32(x) < hi on every axis (f32 bounds) get
+    v <- i32(round(f32(v) * f32(scale))) + add, round half to even, the sum wrapping."""
+    d = sys.DIM
+    out = state.copy()
+    sel = ((sys.pinned >> state.species.astype(np.int64)) & 1) == 0
+    for a in range(d):
+        c = _coord_f32(state.pos[:, a])
+        sel &= ~((c < np.float32(lo[a])) | (c >= np.float32(hi[a])))
+    sc = np.float32(scale)
+    for a in range(d):
+        v = state.vel[sel, a].astype(np.float32) * sc
+        r = np.clip(np.rint(v.astype(np.float64)), -(2.0**31), 2.0**31 - 1).astype(np.int64)
+        w = (r + to_step_displacement(sys, add[a])) & 0xFFFFFFFF
+        out.vel[sel, a] = np.where(w >= 1 << 31, w - (1 << 32), w).astype(np.int32)
+    return out
+
+
+def set_species(state, ids, species):
+    """GpuEngine::set_species (md/src/engine.rs:1042-1053, reorder.wgsl:80-99)."""
+    out = state.copy()
+    out.species[np.asarray(ids, dtype=np.int64)] = species
+    return out
+
+
+def set_species_velocity(sys, state, species, v):
+    """GpuEngine::set_species_velocity (md/src/engine.rs:1056-1063, md.wgsl:151-156)."""
+    out = state.copy()
+    sel = state.species == species
+    for a in range(sys.DIM):
+        out.vel[sel, a] = to_step_displacement(sys, v[a])
+    return out
 
 
 class IntEngine:

@@ -565,7 +565,11 @@ def test_integer_kicks_match_oracle_2d_and_3d(O):
         c3.step(15)
         assert g.read_state() == c3.state
         kg, _ = g.kicks()
-    assert np.array_equal(kg, c3.kicks()[0])
+        assert np.array_equal(kg, c3.kicks()[0])
+        # whole 64-step graph blocks (a small single-species engine): still the integer tables
+        g.step(130)
+        c3.step(130)
+        assert g.read_state() == c3.state
 
 
 # ---------------------------------------------------------------- FP64 reference kicks (IntEngine<f64>)
@@ -805,3 +809,96 @@ def test_list_overflow_is_reported(O, n, loop):
             g.step(1)
         g.upload(s0)
         assert g.read_state() == s0
+
+
+# ---------------------------------------------------------------- page commands (engine.rs:895-1063)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_kick_region_and_species_velocity_match_oracle(O, dim):
+    """kick_region (md.wgsl:216-229, md3.wgsl:541-553) and set_species_velocity against their
+    restatements, then the trajectory after them against IntEngine (through 64-step blocks)."""
+    if dim == 3:
+        sys_, s0 = liquid3(O, 4000, 0.8442, 0.9)
+        eng = GpuEngine3
+    else:
+        sys_, s0 = fluid(O, 6000, 0.7, Pair.lj(2.5), 4)
+        eng = GpuEngine
+    L = [b / 2**32 for b in sys_.box_len]
+    lo, hi = [0.2 * x for x in L], [0.65 * x for x in L]
+    with eng(sys_, s0, ForceMode.verlet_with_skin(sys_, s0.n(), 0.3)) as g:
+        g.step(70)
+        st = g.read_state()
+        g.kick_region(lo, hi, 1.37, [0.25, -0.5, 0.125][:dim])
+        want = O.kick_region(sys_, st, lo, hi, 1.37, [0.25, -0.5, 0.125][:dim])
+        got = g.read_state()
+        assert got == want
+        assert (got.vel != st.vel).any(axis=1).sum() > s0.n() // 20
+        g.kick_region([0.0] * dim, [1.01 * x for x in L], 0.0, [0.0] * dim)  # freeze everything
+        frozen = g.read_state()
+        assert not frozen.vel.any()
+        g.set_species_velocity(0, [0.5, 0.25, -0.125][:dim])
+        got = g.read_state()
+        assert got == O.set_species_velocity(sys_, frozen, 0, [0.5, 0.25, -0.125][:dim])
+        assert np.array_equal(got.vel[0], [O.to_step_displacement(sys_, v) for v in [0.5, 0.25, -0.125][:dim]])
+        c = O.IntEngine(sys_, got)
+        g.step(140)
+        c.step(140)
+        assert g.read_state() == c.state
+
+
+def test_set_species_and_sort_now_match_oracle(O):
+    """set_species on a binary mixture (masses and pair constants follow the new species), a
+    forced re-sort, and the trajectory after both against IntEngine."""
+    sys_ = System(box_for(4000, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 3.0]).with_pair(0, 1, Pair(0.6, 1.1, 2.5))
+    s = O.fluid(sys_, 4000, 1.0, 3)
+    s.species[::4] = 1
+    s.vel = O.maxwell(sys_, s.species, 1.0, 3)
+    with GpuEngine(sys_, s, ForceMode.verlet_with_skin(sys_, 4000, 0.3)) as g:
+        g.step(50)
+        st = g.read_state()
+        ids = np.arange(0, 4000, 7, dtype=np.uint32)
+        g.set_species(np.concatenate([ids, ids[:10]]), 1)
+        want = O.set_species(st, ids, 1)
+        assert g.read_state() == want
+        g.sort_now()
+        assert g.read_state() == want
+        c = O.IntEngine(sys_, want)
+        g.step(100)
+        c.step(100)
+        assert g.read_state() == c.state
+        with pytest.raises(_abi.GbmdError):
+            g.set_species([1], 2)  # no species 2
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_update_system_matches_oracle(O, dim):
+    """update_system (engine.rs:895-934): new pair constants (a smaller cutoff), masses, gravity and
+    dt from the next step; the trajectory equals IntEngine run on the new system from that state.
+    A cutoff above the engine's largest, or another box, is refused with the engine unchanged."""
+    import copy
+
+    if dim == 3:
+        sys_, s0 = liquid3(O, 4000, 0.8442, 0.9)
+        eng = GpuEngine3
+    else:
+        sys_, s0 = fluid(O, 6000, 0.7, Pair.lj(2.5), 6)
+        eng = GpuEngine
+    with eng(sys_, s0, ForceMode.verlet_with_skin(sys_, s0.n(), 0.3)) as g:
+        g.step(70)
+        st = g.read_state()
+        new = copy.deepcopy(sys_)
+        new.pairs = [Pair(1.3, 1.0, 2.2) for _ in new.pairs]
+        new.masses = [1.7]
+        new.dt = 0.004
+        new.gravity = [0.0, -0.3, 0.0][:dim]
+        g.update_system(new)
+        c = O.IntEngine(new, st)
+        g.step(150)
+        c.step(150)
+        assert g.read_state() == c.state
+        bad = copy.deepcopy(new)
+        bad.pairs = [Pair(1.0, 1.0, 2.9) for _ in bad.pairs]
+        with pytest.raises(_abi.GbmdError):
+            g.update_system(bad)
+        g.step(10)
+        c.step(10)
+        assert g.read_state() == c.state

@@ -317,3 +317,11 @@ def test_rdf_counts_every_pair_once(O, rmax):
     st = O.fluid(sys_, 200, 1.0, 9)
     assert (sys_.box_f64()[0] / rmax >= 3) == (rmax == 4.0)
     assert np.array_equal(O.rdf(sys_, st, 90, rmax), _rdf_brute(sys_, st, 90, rmax))
+
+
+def test_to_step_displacement_rounds_like_rust(O):
+    """System::to_step_displacement: f64 round half away from zero, saturating, NaN -> 0."""
+    s = System(box_for(100, 0.7, 1.0), 2.0**-32, Pair.lj(2.5), [1.0])  # v dt 2^32 = v
+    assert [O.to_step_displacement(s, v) for v in (0.5, -0.5, 1.5, -2.5, 0.49999999999999994)] == [1, -1, 2, -3, 0]
+    assert O.to_step_displacement(s, 3e9) == 2**31 - 1 and O.to_step_displacement(s, -3e9) == -(2**31)
+    assert O.to_step_displacement(s, float("nan")) == 0
