@@ -508,18 +508,34 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                     const uint32_t code = image_code(0, sy, 0);
                     const float b0 = off_f32(-reli[0]), wf = off_f32(P.cell_w[0]), cxf = (float)c[0];
                     const float b1 = off_f32(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]);
+                    auto r2_of = [&](const float4& r) {
+                        const float dx = __fmaf_rn(__fsub_rn(r.z, cxf), wf, __fadd_rn(r.x, b0)), dy = r.y + b1;
+                        return __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                    };
+                    bool band = false; // (the band as in the cell walk below)
 #pragma unroll 4
                     for (uint32_t j = j0; j < j1; j++) {
-                        float4 r = __ldg(relf + j);
-                        float dx = __fmaf_rn(__fsub_rn(r.z, cxf), wf, __fadd_rn(r.x, b0)), dy = r.y + b1;
-                        float r2a = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
-                        uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
-                        float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
-                        const bool in = (r2a < lo || (r2a <= hi && exact(j, xs, sj))) && j != i;
+                        const float4 r = __ldg(relf + j);
+                        const float r2a = r2_of(r);
+                        const uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                        const float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
+                        const bool in = r2a < lo && j != i;
+                        band |= r2a >= lo && r2a <= hi;
                         const size_t at = lbase + ((size_t)(count & ~3u) << 5) + (count & 3u);
                         if (in && count < cap) nbr[at] = j | code;
                         count += in ? 1u : 0u;
                     }
+                    if (band)
+                        for (uint32_t j = j0; j < j1; j++) {
+                            const float4 r = __ldg(relf + j);
+                            const float r2a = r2_of(r);
+                            const uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                            const float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
+                            if (r2a >= lo && r2a <= hi && j != i && exact(j, xs, sj)) {
+                                if (count < cap) nbr[lbase + ((size_t)(count & ~3u) << 5) + (count & 3u)] = j | code;
+                                count++;
+                            }
+                        }
                     continue;
                 }
             }
@@ -544,15 +560,37 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
                     return (r2a < lo || (r2a <= hi && exact(j, xs, sj))) && j != i;
                 };
                 if constexpr (S == 1) {
-                    // branch-free append: a predicated store and count += accepted (6% faster
-                    // than branching around the append, which most warps take for a few lanes)
+                    // Branch-free walk: candidates inside the band's lower edge are appended by a
+                    // predicated store and count += accepted; a candidate inside the band only
+                    // marks the cell, which a second walk then settles with the exact test (rare:
+                    // ~0.02 band candidates per particle). 6% and 7% faster than branching around
+                    // the append and around the exact test (most warps took them for a few lanes).
+                    bool band = false;
 #pragma unroll 4
                     for (uint32_t j = j0; j < j1; j++) {
-                        const bool in = test(j);
+                        const float4 r = __ldg(relf + j);
+                        const float dx = r.x + b0, dy = r.y + b1, dz = D == 3 ? r.z + b2 : 0.0f;
+                        const float r2a = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                        const uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                        const float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
+                        const bool in = r2a < lo && j != i;
+                        band |= r2a >= lo && r2a <= hi;
                         const size_t at = lbase + ((size_t)(count & ~3u) << 5) + (count & 3u);
                         if (in && count < cap) nbr[at] = j | code;
                         count += in ? 1u : 0u;
                     }
+                    if (band)
+                        for (uint32_t j = j0; j < j1; j++) {
+                            const float4 r = __ldg(relf + j);
+                            const float dx = r.x + b0, dy = r.y + b1, dz = D == 3 ? r.z + b2 : 0.0f;
+                            const float r2a = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                            const uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                            const float lo = MULTI ? P.pc[si * P.ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * P.ns + sj].list2hi : hi0;
+                            if (r2a >= lo && r2a <= hi && j != i && exact(j, xs, sj)) {
+                                if (count < cap) nbr[lbase + ((size_t)(count & ~3u) << 5) + (count & 3u)] = j | code;
+                                count++;
+                            }
+                        }
                 } else {
                     // the warp walks the longest of its particles' ranges, so every ballot is whole
                     const uint32_t lane = threadIdx.x & 31u;
