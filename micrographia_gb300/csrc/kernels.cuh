@@ -677,7 +677,8 @@ __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t t, cons
         const uint4 qi = ld_in<CG>(qpos_in + iv);
         const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
         for (uint32_t g = seg; g < ngroups; g += S) {
-            if (g + 2 * S < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2 * S)));
+            // (the prefetch index clamped to the last group rather than guarded: no branch)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * min(g + 2 * S, ngroups - 1u)));
             const uint4 jv = __ldg(groups + 32 * g);
             const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
             const uint32_t left = m - 4 * g;
@@ -696,7 +697,9 @@ __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t t, cons
                     // the remainders are whole bytes of the fourth word: one byte select each
                     uint32_t Rj[3] = {__byte_perm(r[u].w, 0u, 0x4440u), __byte_perm(r[u].w, 0u, 0x4441u), __byte_perm(r[u].w, 0u, 0x4442u)};
                     const uint32_t code = jj[u] >> LIST_BITS;
-                    if (code && (uint32_t)u < left) {
+                    // (a slot past the list's end holds a stale word; shifting this particle's own
+                    // record for it is harmless, its pair gets a zero coefficient)
+                    if (code) {
 #pragma unroll
                         for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
                     }
