@@ -63,37 +63,47 @@ __global__ void k_bkeys(uint32_t N, const Params* __restrict__ tab, const uint32
 }
 
 template <int D>
-__global__ void k_bgather(uint32_t N, const Params* __restrict__ tab, const uint32_t* items, const PosRec<D>* pos, const int32_t* vel,
-                          const uint32_t* species, const uint32_t* ids, const uint32_t* sysidx, PosRec<D>* pos_o, int32_t* vel_o,
-                          uint32_t* species_o, uint32_t* ids_o, uint32_t* sysidx_o) {
+__global__ void k_bgather(uint32_t N, const Params* __restrict__ tab, const uint32_t* items, const uint32_t* keys, const PosRec<D>* pos,
+                          const int32_t* vel, const uint32_t* species, const uint32_t* ids, const uint32_t* sysidx, PosRec<D>* pos_o,
+                          int32_t* vel_o, uint32_t* species_o, uint32_t* ids_o, uint32_t* sysidx_o, float4* relf) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     uint32_t o = items[s];
     PosRec<D> r = pos[o];
-    {
-        const Params& P = tab[sysidx[o]];
-        long long* x = reinterpret_cast<long long*>(&r);
+    const Params& P = tab[sysidx[o]];
+    long long* x = reinterpret_cast<long long*>(&r);
 #pragma unroll
-        for (int a = 0; a < D; a++) x[a] = wrap(x[a], P.box[a]);
-    }
+    for (int a = 0; a < D; a++) x[a] = wrap(x[a], P.box[a]);
     pos_o[s] = r;
+    // the position relative to its cell's origin in its own system, f32 sigma (as k_gather)
+    uint32_t c[3];
+    cell_coords(P, keys[s] - P.cell_base, c);
+    float4 f;
+    f.x = off_f32(x[0] - (int64_t)c[0] * P.cell_w[0]);
+    f.y = off_f32(x[1] - (int64_t)c[1] * P.cell_w[1]);
+    f.z = D == 3 ? off_f32(x[2] - (int64_t)c[2] * P.cell_w[2]) : 0.0f;
+    f.w = __uint_as_float(species[o]);
+    relf[s] = f;
     for (int a = 0; a < D; a++) vel_o[D * s + a] = vel[D * o + a];
     species_o[s] = species[o];
     ids_o[s] = ids[o];
     sysidx_o[s] = sysidx[o];
 }
 
-// The list build of k_build_list, each particle in its own system's cells and geometry.
+// The list build of k_build_list, each particle in its own system's cells and geometry: the f32
+// prefilter over cell-relative records (relf), branch-free appends, and the exact test only for
+// the candidates in the prefilter's band, in a second walk of the cells that have one.
 template <int D, bool MULTI>
 __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, const Params* __restrict__ tab,
                                                      const uint32_t* __restrict__ sysidx_s, const PosRec<D>* __restrict__ pos_s,
                                                      const int32_t* __restrict__ vel_s, const uint32_t* __restrict__ species_s,
                                                      const uint32_t* __restrict__ ids_s, const uint32_t* __restrict__ keys,
-                                                     const uint32_t* __restrict__ start, PosRec<D>* __restrict__ pos_o,
-                                                     int32_t* __restrict__ vel_o, uint32_t* __restrict__ species_o,
-                                                     uint32_t* __restrict__ ids_o, uint32_t* __restrict__ sysidx_o,
-                                                     PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ nbr,
-                                                     uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ ctl, uint4* __restrict__ qpos_o) {
+                                                     const uint32_t* __restrict__ start, const float4* __restrict__ relf,
+                                                     PosRec<D>* __restrict__ pos_o, int32_t* __restrict__ vel_o,
+                                                     uint32_t* __restrict__ species_o, uint32_t* __restrict__ ids_o,
+                                                     uint32_t* __restrict__ sysidx_o, PosRec<D>* __restrict__ ref_pos,
+                                                     uint32_t* __restrict__ nbr, uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ ctl,
+                                                     uint4* __restrict__ qpos_o) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     uint32_t sys = sysidx_s[i];
@@ -104,29 +114,81 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
     uint32_t c[3];
     cell_coords(P, keys[i] - base, c);
     uint32_t count = 0;
+    const size_t lbase = list_slot(i, 0, cap4);
+    const bool unchecked = P.sep_unchecked;
+    int64_t reli[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) reli[a] = a < D ? xi[a] - (int64_t)c[a] * P.cell_w[a] : 0;
+    auto exact = [&](uint32_t j, const int64_t* xs, uint32_t sj) -> bool {
+        int64_t xj[3];
+        load_particle<D, false>(pos_s, nullptr, j, xj);
+        float f[D];
+        bool ok = true;
+        if (unchecked) {
+#pragma unroll
+            for (int a = 0; a < D; a++) f[a] = sep_near(xj[a] - xs[a]);
+        } else {
+#pragma unroll
+            for (int a = 0; a < D; a++) f[a] = sep_s(xj[a] - xs[a], ok);
+        }
+        float r2 = __fadd_rn(__fmul_rn(f[0], f[0]), __fmul_rn(f[1], f[1]));
+        if (D == 3) r2 = __fadd_rn(r2, __fmul_rn(f[2], f[2]));
+        return ok && r2 < P.pc[si * ns + sj].list2s;
+    };
+    const float lo0 = P.pc[si * ns].list2lo, hi0 = P.pc[si * ns].list2hi;
+    const uint32_t nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
     // each neighbour cell at the periodic image that places it next to this one: the list entry
     // carries that image, so the force kernel needs no minimum image (as k_build_list)
-    for_cells_shifted<D>(P, c, [&](uint32_t cell, int64_t sx, int64_t sy, int64_t sz) {
-        const int64_t sh[3] = {sx, sy, sz};
-        const uint32_t code = image_code(sx, sy, sz);
-        uint32_t j0 = __ldg(start + base + cell), j1 = __ldg(start + base + cell + 1);
-        for (uint32_t j = j0; j < j1; j++) {
-            if (j == i) continue;
-            int64_t xj[3];
-            uint32_t sj = load_particle<D, MULTI>(pos_s, species_s, j, xj);
-            bool ok = true;
-            float f[D];
-#pragma unroll
-            for (int a = 0; a < D; a++) f[a] = sep_s(xj[a] + sh[a] - xi[a], ok);
-            if (!ok) continue;
-            float r2 = __fadd_rn(__fmul_rn(f[0], f[0]), __fmul_rn(f[1], f[1]));
-            if (D == 3) r2 = __fadd_rn(r2, __fmul_rn(f[2], f[2]));
-            if (r2 < P.pc[si * ns + sj].list2s) {
-                if (count < cap) nbr[list_slot(i, count, cap4)] = j | code;
-                count++;
+    for (int oz = 0; oz < (D == 3 ? 3 : 1); oz++) {
+        const int tz = (int)c[2] + oz - 1;
+        const uint32_t z = D == 3 ? (tz < 0 ? nz - 1 : (tz >= (int)nz ? 0 : (uint32_t)tz)) : 0;
+        const int64_t sz = D == 3 ? (tz < 0 ? -P.box[2] : (tz >= (int)nz ? P.box[2] : 0)) : 0;
+        for (int oy = 0; oy < 3; oy++) {
+            const int ty = (int)c[1] + oy - 1;
+            const uint32_t y = ty < 0 ? ny - 1 : (ty >= (int)ny ? 0 : (uint32_t)ty);
+            const int64_t sy = ty < 0 ? -P.box[1] : (ty >= (int)ny ? P.box[1] : 0);
+            for (int ox = 0; ox < 3; ox++) {
+                const int tx = (int)c[0] + ox - 1;
+                const uint32_t x = tx < 0 ? nx - 1 : (tx >= (int)nx ? 0 : (uint32_t)tx);
+                const int64_t sx = tx < 0 ? -P.box[0] : (tx >= (int)nx ? P.box[0] : 0);
+                const uint32_t cell = (z * ny + y) * nx + x;
+                const int64_t xs[3] = {xi[0] - sx, xi[1] - sy, D == 3 ? xi[2] - sz : 0};
+                const uint32_t code = image_code(sx, sy, sz);
+                const float b0 = off_f32(((int64_t)x - (int64_t)c[0]) * P.cell_w[0] + sx - reli[0]);
+                const float b1 = off_f32(((int64_t)y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]);
+                const float b2 = D == 3 ? off_f32(((int64_t)z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]) : 0.0f;
+                const uint32_t j0 = __ldg(start + base + cell), j1 = __ldg(start + base + cell + 1);
+                auto r2_of = [&](const float4& r) {
+                    const float dx = r.x + b0, dy = r.y + b1, dz = D == 3 ? r.z + b2 : 0.0f;
+                    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                };
+                bool band = false;
+#pragma unroll 4
+                for (uint32_t j = j0; j < j1; j++) {
+                    const float4 r = __ldg(relf + j);
+                    const float r2a = r2_of(r);
+                    const uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                    const float lo = MULTI ? P.pc[si * ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * ns + sj].list2hi : hi0;
+                    const bool in = r2a < lo && j != i;
+                    band |= r2a >= lo && r2a <= hi;
+                    const size_t at = lbase + ((size_t)(count & ~3u) << 5) + (count & 3u);
+                    if (in && count < cap) nbr[at] = j | code;
+                    count += in ? 1u : 0u;
+                }
+                if (band)
+                    for (uint32_t j = j0; j < j1; j++) {
+                        const float4 r = __ldg(relf + j);
+                        const float r2a = r2_of(r);
+                        const uint32_t sj = MULTI ? __float_as_uint(r.w) : 0u;
+                        const float lo = MULTI ? P.pc[si * ns + sj].list2lo : lo0, hi = MULTI ? P.pc[si * ns + sj].list2hi : hi0;
+                        if (r2a >= lo && r2a <= hi && j != i && exact(j, xs, sj)) {
+                            if (count < cap) nbr[lbase + ((size_t)(count & ~3u) << 5) + (count & 3u)] = j | code;
+                            count++;
+                        }
+                    }
             }
         }
-    });
+    }
     if (count > cap) {
         ctl[1] = 1;
         count = cap;
@@ -282,6 +344,7 @@ struct gbmd_batch {
     uint32_t *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr}, *hist = nullptr, *scan_tmp = nullptr, *start = nullptr;
     uint32_t *nbr = nullptr, *nbr_count = nullptr, *ctl = nullptr;
     uint4* qpos[2] = {nullptr, nullptr}; // quotient records of the positions (ping-pong)
+    float4* relf = nullptr;              // cell-relative f32 coordinates of the sorted scratch state
     void* staging = nullptr;
     int32_t* staging_v = nullptr;
     uint32_t* staging_s = nullptr;
@@ -307,7 +370,7 @@ void bfree(gbmd_batch* b) {
             if (b->exec[p][k]) cudaGraphExecDestroy(b->exec[p][k]);
     void* ptrs[] = {b->tab, b->pos[0], b->pos[1], b->pos_scr, b->ref_pos, b->vel, b->vel_scr, b->species, b->species_scr, b->ids, b->ids_scr,
                     b->sysidx, b->sysidx_scr, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->scan_tmp, b->start, b->nbr,
-                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1]};
+                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1], b->relf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->st) cudaStreamDestroy(b->st);
@@ -319,11 +382,11 @@ template <int D, bool MULTI> void benqueue_rebuild_t(gbmd_batch* b, cudaStream_t
     k_bkeys<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur], b->keys[0], b->vals[0]);
     b->sorted = radix_sort_pairs(b->keys[0], b->vals[0], b->keys[1], b->vals[1], N, (int)b->bits, b->hist, b->scan_tmp, s);
     cell_starts(b->keys[b->sorted], N, b->ncell, b->start, s);
-    k_bgather<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->tab, b->vals[b->sorted], (const PosRec<D>*)b->pos[b->cur], b->vel, b->species,
-                                                b->ids, b->sysidx, (PosRec<D>*)b->pos_scr, b->vel_scr, b->species_scr, b->ids_scr,
-                                                b->sysidx_scr);
+    k_bgather<D><<<nblocks(N, 256), 256, 0, s>>>(N, b->tab, b->vals[b->sorted], b->keys[b->sorted], (const PosRec<D>*)b->pos[b->cur],
+                                                b->vel, b->species, b->ids, b->sysidx, (PosRec<D>*)b->pos_scr, b->vel_scr, b->species_scr,
+                                                b->ids_scr, b->sysidx_scr, b->relf);
     k_bbuild_list<D, MULTI><<<nblocks(N, 128), 128, 0, s>>>(N, b->cap, b->tab, b->sysidx_scr, (const PosRec<D>*)b->pos_scr, b->vel_scr,
-                                                           b->species_scr, b->ids_scr, b->keys[b->sorted], b->start,
+                                                           b->species_scr, b->ids_scr, b->keys[b->sorted], b->start, b->relf,
                                                            (PosRec<D>*)b->pos[b->cur], b->vel, b->species, b->ids, b->sysidx,
                                                            (PosRec<D>*)b->ref_pos, b->nbr, b->nbr_count, b->ctl, b->qpos[b->cur]);
     k_brebuild_done<<<1, 1, 0, s>>>(b->ctl);
@@ -523,6 +586,7 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     step(balloc(&b->start, (size_t)b->ncell + 1));
     step(balloc(&b->nbr, (N + 31) / 32 * 32 * (((size_t)b->cap + 3) & ~(size_t)3))); // warp-tiled (list_slot)
     step(balloc(&b->qpos[0], N));
+    step(balloc(&b->relf, N));
     step(balloc(&b->qpos[1], N));
     step(balloc(&b->nbr_count, N));
     step(balloc(&b->ctl, 16));

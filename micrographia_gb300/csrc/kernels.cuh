@@ -323,35 +323,6 @@ template <int D, typename Fn> __device__ __forceinline__ void for_cells(const Pa
     }
 }
 
-// Visit the 3^D cells around cell c with each cell's periodic image shift: a neighbour cell
-// reached by wrapping below 0 lies a box length lower, above n - 1 a box length higher. With at
-// least 3 cells per axis of at least the list radius, every pair within that radius is found at
-// xj + shift - xi exactly (its minimum image), and every other candidate is at least the list
-// radius away in that form too.
-template <int D, typename Fn> __device__ __forceinline__ void for_cells_shifted(const Params& P, const uint32_t* c, Fn&& f) {
-    const uint32_t nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
-    for (int oz = 0; oz < (D == 3 ? 3 : 1); oz++) {
-        int64_t sz = 0;
-        uint32_t z = 0;
-        if (D == 3) {
-            int t = (int)c[2] + oz - 1;
-            z = t < 0 ? nz - 1 : (t >= (int)nz ? 0 : (uint32_t)t);
-            sz = t < 0 ? -P.box[2] : (t >= (int)nz ? P.box[2] : 0);
-        }
-        for (int oy = 0; oy < 3; oy++) {
-            int t = (int)c[1] + oy - 1;
-            uint32_t y = t < 0 ? ny - 1 : (t >= (int)ny ? 0 : (uint32_t)t);
-            int64_t sy = t < 0 ? -P.box[1] : (t >= (int)ny ? P.box[1] : 0);
-            for (int ox = 0; ox < 3; ox++) {
-                int tx = (int)c[0] + ox - 1;
-                uint32_t x = tx < 0 ? nx - 1 : (tx >= (int)nx ? 0 : (uint32_t)tx);
-                int64_t sx = tx < 0 ? -P.box[0] : (tx >= (int)nx ? P.box[0] : 0);
-                f((z * ny + y) * nx + x, sx, sy, sz);
-            }
-        }
-    }
-}
-
 __device__ __forceinline__ void cell_coords(const Params& P, uint32_t key, uint32_t* c) {
     c[0] = key % P.nc[0];
     c[1] = (key / P.nc[0]) % P.nc[1];
