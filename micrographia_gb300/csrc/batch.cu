@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, uint32_t cap, c
         const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
         const uint32_t ngroups = (m + 3u) >> 2;
         for (uint32_t g = 0; g < ngroups; g++) {
-            if (g + 2 < ngroups) asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * (g + 2)));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * min(g + 2, ngroups - 1u)));
             const uint4 jv = __ldg(groups + 32 * g);
             const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
             const uint32_t left = m - 4 * g;
@@ -245,12 +245,12 @@ __global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, uint32_t cap, c
                 uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
                 uint32_t Rj[3] = {__byte_perm(r[u].w, 0u, 0x4440u), __byte_perm(r[u].w, 0u, 0x4441u), __byte_perm(r[u].w, 0u, 0x4442u)};
                 const uint32_t code = jj[u] >> LIST_BITS;
-                if (code && (uint32_t)u < left) {
+                if (code) { // (a stale word past the list's end only shifts this particle's own record)
 #pragma unroll
                     for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
                 }
 #pragma unroll
-                for (int a = 0; a < D; a++) f[u][a] = quot_sep(Xj[a], Rj[a], Xi[a], (qi.w >> (8 * a)) & 15u);
+                for (int a = 0; a < D; a++) f[u][a] = quot_sep_mad(Xj[a], Rj[a], 0u - Xi[a], (qi.w >> (8 * a)) & 15u, P.one);
                 if (D == 2) f[u][2] = 0.0f;
             }
             if constexpr (!MULTI && SIG1) {
