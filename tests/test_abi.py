@@ -82,3 +82,20 @@ def test_snapshot_format_round_trip_and_corruption():
                 snapshot.unpack(bytes(bad))
         with pytest.raises(ValueError):
             snapshot.unpack(b"XXXXXXXX" + buf[8:])
+
+
+def test_header_constants_match_the_python_mirror():
+    """Every plain #define GBMD_<NAME> <integer> of the header has the same value in _abi as <NAME>,
+    and the two flag-field helpers place their values where the header's macros do."""
+    text = open(_abi.HEADER_PATH).read()
+    found = 0
+    for name, value in re.findall(r"#define GBMD_([A-Z0-9_]+) \(?(-?\d+)u?\)?", text):
+        if not hasattr(_abi, name):
+            continue
+        assert getattr(_abi, name) == int(value), name
+        found += 1
+    assert found >= 20
+    assert "#define GBMD_FLAG_BUILD_LANES(s) ((uint32_t)(s) << 4)" in text and _abi.build_lanes_flag(8) == 8 << 4
+    assert "#define GBMD_FLAG_FORCE_LANES(s) ((uint32_t)(s) << 8)" in text and _abi.force_lanes_flag(16) == 16 << 8
+    with pytest.raises(ValueError):
+        _abi.force_lanes_flag(3)
