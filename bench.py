@@ -38,7 +38,7 @@ RHO, T0, SEED, SKIN, RC, DT = 0.8442, 0.72, 1, 0.3, 2.5, 0.005
 
 def config_dict(extra=None):
     d = {
-        "workload": f"3D LJ liquid NVE, FCC N={N_ATOMS}, rho 0.8442, T 0.72, rc 2.5, skin 0.3, dt 0.005 (configs[1], plain form)",
+        "workload": f"3D LJ liquid NVE, FCC N={N_ATOMS}, rho 0.8442, T 0.72, rc 2.5, skin 0.3, dt 0.005 (plain form)",
         "n_atoms": N_ATOMS,
         "density": RHO,
         "temperature": T0,
@@ -366,7 +366,7 @@ def run_ours(args, world, rank, local, pg):
 
 
 def run_c4(args, world, rank, local, pg):
-    """configs[3]: 1024 uneven 2D systems; batched (one persistent launch per step, 100-step
+    """1024 uneven 2D systems; batched (one persistent launch per step, 100-step
     graphs) against the plain form (one engine per system, each on its own stream)."""
     import torch
 
@@ -433,7 +433,7 @@ def run_c4(args, world, rank, local, pg):
         "dtype": "f32+int64",
         "data": "synthetic",
         "config": {
-            "workload": f"{len(systems)} independent 2D LJ systems, N log-uniform [256, 65536] (sum {total}), rho U[0.3, 0.8], T U[0.5, 1.5], rc 2.5, skin 0.3, dt 0.005 (configs[3])",
+            "workload": f"{len(systems)} independent 2D LJ systems, N log-uniform [256, 65536] (sum {total}), rho U[0.3, 0.8], T U[0.5, 1.5], rc 2.5, skin 0.3, dt 0.005",
             "form": "batched: one persistent force launch per step over all systems, 100-step CUDA graphs",
             "plain_value": value_plain,
             "plain_form": "one engine per system, each stepped on its own stream, all issued back to back",
@@ -451,7 +451,7 @@ def run_c4(args, world, rank, local, pg):
 
 
 def run_c3(args, world, rank, local, pg):
-    """configs[2]: 2D liquid-vapour slab, N = 2^24, rescale to T = 0.45 every 10 steps, RDF (200
+    """2D liquid-vapour slab, N = 2^24, rescale to T = 0.45 every 10 steps, RDF (200
     bins to r = 5) and density profile (80 bins) every 100 steps inside the timed region."""
     import torch
 
@@ -498,7 +498,7 @@ def run_c3(args, world, rank, local, pg):
         "dtype": "f32+int64",
         "data": "synthetic",
         "config": {
-            "workload": f"2D liquid-vapour slab N={n}, 4:1 box, liquid 0.70 / vapour 0.05, rescale T=0.45 every 10 steps, RDF + profile every 100 steps (configs[2])",
+            "workload": f"2D liquid-vapour slab N={n}, 4:1 box, liquid 0.70 / vapour 0.05, rescale T=0.45 every 10 steps, RDF + profile every 100 steps",
             "timing": "wall clock including the frames (observables copied to the host every 100 steps)",
             "device_ms_last_event_pair": ms,
             "frames": frames[-3:],
@@ -523,7 +523,7 @@ def _pct(xs, q):
 
 
 def run_c5(args, world, rank, local, pg):
-    """configs[4]: a Poisson stream of 2D/3D requests (N log-uniform in [1024, 2^20], 2000 steps,
+    """A Poisson stream of 2D/3D requests (N log-uniform in [1024, 2^20], 2000 steps,
     a frame of T, P and a 200-bin RDF every 100 steps) served under a 64 GB HBM budget, against
     the same requests run one after another in plain form. Per-frame latency: the wall time a
     client waits for each frame after the previous one of its request (after submission for the
@@ -627,7 +627,7 @@ def run_c5(args, world, rank, local, pg):
         "dtype": "f32+int64",
         "data": "synthetic",
         "config": {
-            "workload": f"{args.requests} requests (dealt out over {world} GPU(s)), Poisson arrivals at {args.rate}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget (configs[4])",
+            "workload": f"{args.requests} requests (dealt out over {world} GPU(s)), Poisson arrivals at {args.rate}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget",
             "form": "served: continuous batching (each admitted request on its own stream, intervals overlapped)",
             "makespan_s": mk_serve,
             "frame_latency_p50_ms": 1e3 * _pct(lat_serve, 50),

@@ -10,7 +10,7 @@
 // same alone and in any mix.
 //
 // The reference has no serving layer (its engines run one scenario per page,
-// crates/wasm/src/sims.rs:29-516); this is the benchmark spec's served form of the same engine.
+// crates/wasm/src/sims.rs:29-516); this is the served form of the same engine.
 #include <chrono>
 #include <cmath>
 #include <cstring>

@@ -1,4 +1,4 @@
-"""The benchmark workloads of the benchmark spec, as seeded synthetic systems (no dataset is
+"""The benchmark workloads, as seeded synthetic systems (no dataset is
 involved): each function returns systems and device-init recipes, never particle data.
 
 - config2: 3D LJ liquid, FCC N = 1,048,576 at rho 0.8442, T 0.72 (the LAMMPS in.lj shape).

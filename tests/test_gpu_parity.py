@@ -632,7 +632,7 @@ def test_pair_math_matches_library(pairs):
     assert checked.value > (13 << 23) + (1 << 28)
 
 
-# ---------------------------------------------------------------- velocity-rescale thermostat (configs[2])
+# ---------------------------------------------------------------- velocity-rescale thermostat (the 2D slab workload)
 def test_rescale_thermostat_matches_oracle(O):
     """Slab start, rescale to T = 0.45 every 10 steps: the GPU trajectory equals the oracle's
     (IntEngine<f32> stepped one step at a time, the exact-integer rescale after every 10th)."""
@@ -674,7 +674,7 @@ def test_config2_full_size_properties(O):
         assert g.read_state().hash() == s0.hash()
 
 
-# ---------------------------------------------------------------- batched replicas (configs[3])
+# ---------------------------------------------------------------- batched replicas
 def test_batch_replicas_match_their_plain_runs(O):
     """Uneven 2D systems stepped in one batch: each replica's state equals md-ref's IntEngine<f32>
     run of that system alone, bit for bit (through a 100-step graph block and single steps)."""
@@ -709,7 +709,7 @@ def test_batch_3d(O):
             assert b.read_system(k) == c.state
 
 
-# ---------------------------------------------------------------- serving (configs[4])
+# ---------------------------------------------------------------- serving
 def _drain(sv, want_last, limit_s=120.0):
     import time
 
