@@ -87,6 +87,10 @@ typedef struct gbmd_system {
 /* gbmd_options.flags */
 #define GBMD_FLAG_WHOLE_CELLS 1u /* list builds scan whole neighbour cells (no slab sub-buckets): timing comparisons */
 #define GBMD_FLAG_NO_STEP_LOOP 2u /* small systems step through per-step graph nodes, not the persistent step loop: comparisons */
+/* batches only: gbmd_batch_create times two blocks of (at most 100) steps from the given state at
+ * each skin of 0.3, 0.4, 0.5, 0.6 and 0.7 sigma and keeps the fastest; `skin` is ignored. The
+ * trajectory does not depend on the skin (the lists hold exactly the pairs within the cutoff). */
+#define GBMD_FLAG_TUNE_SKIN 4u
 /* bits 4-7 of flags: lanes per particle of the list build (1, 2, 4 or 8; 0 chooses by size) */
 #define GBMD_FLAG_BUILD_LANES(s) ((uint32_t)(s) << 4)
 /* bits 8-12 of flags: lanes per particle of the force step (1, 2, 4, 8 or 16; 0 chooses by size) */
@@ -299,6 +303,8 @@ int gbmd_batch_read_system(gbmd_batch* b, uint32_t k, int64_t* pos, int32_t* vel
 int gbmd_batch_stream(gbmd_batch* b, void** stream);
 /* Kernel launches of the batch so far (graph nodes included) and its list rebuilds. */
 int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds);
+/* The batch's Verlet skin in sigma (the one GBMD_FLAG_TUNE_SKIN chose, or the one asked for). */
+int gbmd_batch_skin(gbmd_batch* b, double* skin);
 int gbmd_batch_destroy(gbmd_batch* b);
 
 /* FNV-1a hash of an id-ordered state held on the host: State::hash (system.rs:460-477) for

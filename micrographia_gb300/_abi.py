@@ -55,6 +55,7 @@ class gbmd_system(C.Structure):
 
 FLAG_WHOLE_CELLS = 1  # list builds scan whole neighbour cells (no slab sub-buckets)
 FLAG_NO_STEP_LOOP = 2  # small systems step through per-step graph nodes, not the persistent loop
+FLAG_TUNE_SKIN = 4  # batches: time each skin of 0.3..0.7 sigma on the given state, keep the fastest
 
 
 def build_lanes_flag(lanes):
@@ -202,6 +203,7 @@ SIGNATURES = [
     ("gbmd_batch_read_system", C.c_int, [VP, C.c_uint32, _I64P, _I32P, _U32P]),
     ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
     ("gbmd_batch_stats", C.c_int, [VP, _U64P, _U32P]),
+    ("gbmd_batch_skin", C.c_int, [VP, C.POINTER(C.c_double)]),
     ("gbmd_batch_destroy", C.c_int, [VP]),
     ("gbmd_serve_create", C.c_int, [C.c_uint64, C.c_uint32, C.c_int32, P(VP)]),
     ("gbmd_serve_submit", C.c_int, [VP, P(gbmd_serve_request), _U64P]),

@@ -350,6 +350,7 @@ struct gbmd_batch {
     uint32_t* staging_s = nullptr;
     int cur = 0, sorted = 0;
     uint32_t block_steps = 100;
+    double skin = 0.4;
     cudaGraphExec_t exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     uint64_t exec_launches[2][2] = {{0, 0}, {0, 0}};
     uint64_t body_launches = 0, launches = 0;
@@ -484,6 +485,56 @@ int bcheck(gbmd_batch* b) {
 
 } // namespace
 
+extern "C" int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t* offsets, const int64_t* pos,
+                                 const int32_t* vel, const uint32_t* species, const gbmd_options* opts, gbmd_batch** out);
+
+namespace {
+
+// The skin autotuner: a trial batch per candidate skin, from the caller's state, timed with
+// CUDA events over its second block of steps (the first captures the graphs and warms up).
+// A candidate whose lists overflow a fixed capacity, or that does not fit in memory, drops out.
+// Sets o.skin to the fastest and clears the flag.
+int tune_skin(const gbmd_system* systems, uint32_t count, const uint32_t* offsets, const int64_t* pos, const int32_t* vel,
+              const uint32_t* species, gbmd_options& o) {
+    static const double cand[] = {0.3, 0.4, 0.5, 0.6, 0.7};
+    o.flags &= ~GBMD_FLAG_TUNE_SKIN;
+    gbmd_options t = o;
+    t.block_steps = std::min<uint32_t>(o.block_steps ? o.block_steps : 100, 100);
+    double best = 0.0;
+    float best_ms = 0.0f;
+    int last = GBMD_OK;
+    std::string last_msg;
+    for (double sk : cand) {
+        t.skin = sk;
+        gbmd_batch* tb = nullptr;
+        int r = gbmd_batch_create(systems, count, offsets, pos, vel, species, &t, &tb);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float ms = 0.0f;
+        if (r == GBMD_OK) r = gbmd_batch_step(tb, t.block_steps);
+        if (r == GBMD_OK) r = gbmd_batch_sync(tb);
+        if (r == GBMD_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) r = fail(GBMD_E_CUDA, "cudaEventCreate");
+        if (r == GBMD_OK && cudaEventRecord(e0, tb->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventRecord");
+        if (r == GBMD_OK) r = gbmd_batch_step(tb, t.block_steps);
+        if (r == GBMD_OK && cudaEventRecord(e1, tb->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventRecord");
+        if (r == GBMD_OK) r = gbmd_batch_sync(tb);
+        if (r == GBMD_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventElapsedTime");
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (tb) gbmd_batch_destroy(tb);
+        if (r == GBMD_OK && (best == 0.0 || ms < best_ms)) best = sk, best_ms = ms;
+        if (r != GBMD_OK) {
+            if (r != GBMD_E_OVERFLOW && r != GBMD_E_NOMEM) return r;
+            last = r;
+            last_msg = gbmd_last_error();
+        }
+    }
+    if (best == 0.0) return fail(last, "skin tuning: no candidate ran (" + last_msg + ")");
+    o.skin = best;
+    return GBMD_OK;
+}
+
+} // namespace
+
 extern "C" {
 
 int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t* offsets, const int64_t* pos, const int32_t* vel,
@@ -501,6 +552,7 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
         if (offsets[k + 1] <= offsets[k]) return fail(GBMD_E_INVALID, "every system needs at least one particle");
     }
     if (offsets[0] != 0) return fail(GBMD_E_INVALID, "offsets[0] must be 0");
+    if (o.flags & GBMD_FLAG_TUNE_SKIN) GBMD_TRY(tune_skin(systems, count, offsets, pos, vel, species, o));
     auto* b = new gbmd_batch;
     b->K = count;
     b->N = offsets[count];
@@ -510,6 +562,7 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     b->offsets.assign(offsets, offsets + count + 1);
     b->block_steps = o.block_steps ? o.block_steps : 100;
     double skin = o.skin > 0 ? o.skin : 0.4;
+    b->skin = skin;
     b->P.resize(count);
     uint64_t cell_base = 0;
     for (uint32_t k = 0; k < count; k++) {
@@ -685,6 +738,12 @@ int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds) {
     GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
     if (rebuilds) *rebuilds = c[2];
     if (launches) *launches = b->launches + (uint64_t)c[2] * b->body_launches;
+    return GBMD_OK;
+}
+
+int gbmd_batch_skin(gbmd_batch* b, double* skin) {
+    if (!b || !skin) return fail(GBMD_E_INVALID, "null argument");
+    *skin = b->skin;
     return GBMD_OK;
 }
 

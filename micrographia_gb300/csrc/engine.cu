@@ -1608,6 +1608,18 @@ const char* gbmd_version(void) { return "gbmd 0.1 (sm_103a)"; }
 // ------------------------------------------------------------------ observables
 namespace {
 
+// The exact bin of a pair whose f32 estimate was too close to a bin edge or to rmax.
+template <int D> __device__ __forceinline__ int rdf_bin_exact(const int64_t* d, uint32_t bins, double scale) {
+    double r2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const double x = to_f64(d[a]);
+        r2 = __dadd_rn(r2, __dmul_rn(x, x));
+    }
+    const double r = __dmul_rn(__dsqrt_rn(r2), scale);
+    return r < (double)bins ? (int)(uint32_t)r : -1;
+}
+
 // RDF pair counts over unordered pairs of the cell-sorted scratch state: bin
 // floor(sqrt(r2) * scale) with r2 the f64 square of the exact minimum-image separation.
 // The RDF bin of a pair at minimum-image separation d: k = floor(sqrt(r2) bins / rmax) with r2
@@ -1628,18 +1640,87 @@ __device__ __forceinline__ int rdf_bin(const int64_t* d, uint32_t bins, double s
     const float rf = __fmul_rn(__fsqrt_rn(r2f), scalef);
     const float fl = floorf(rf), fr = rf - fl;
     if (fr > margin && fr < 1.0f - margin && rf < (float)bins - margin) return (int)fl;
-    double r2 = 0.0;
-#pragma unroll
-    for (int a = 0; a < D; a++) {
-        const double x = to_f64(d[a]);
-        r2 = __dadd_rn(r2, __dmul_rn(x, x));
-    }
-    const double r = __dmul_rn(__dsqrt_rn(r2), scale);
-    return r < (double)bins ? (int)(uint32_t)r : -1;
+    return rdf_bin_exact<D>(d, bins, scale);
 }
 
+// RDF pair counts over unordered pairs of the cell-sorted scratch state (cells of side >= rmax,
+// at least three per axis). A candidate j of neighbour cell cj sits at d = relf[j] + base with
+// base = (cj - c) cell_w + image - (xi - c cell_w), an exact integer converted once per cell, so
+// the candidate costs one 16-byte load and a few f32 operations. The f32 estimate of
+// r bins / rmax is within `margin` bins of the exact value (the host bounds the conversions'
+// and the sum's rounding); a pair clear of every bin edge by that much, or beyond `lim2f`, is
+// decided by it, the rest (a fraction ~2 margin of the pairs) by the f64 definition on the exact
+// integer separation.
 template <int D>
-__global__ void k_rdf(Params P, const Rec<D>* pos, const uint32_t* keys, const uint32_t* start, uint32_t bins, double scale,
+__global__ void __launch_bounds__(128) k_rdf(Params P, const Rec<D>* pos, const float4* relf, const uint32_t* keys, const uint32_t* start,
+                                             uint32_t bins, double scale, float scalef, float lim2f, float margin, unsigned long long* out) {
+    extern __shared__ uint32_t h[];
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.n) {
+        int64_t xi[3], reli[3];
+        load_particle<D, false>(pos, nullptr, i, xi);
+        uint32_t c[3];
+        cell_coords(P, keys[i], c);
+#pragma unroll
+        for (int a = 0; a < 3; a++) reli[a] = a < D ? xi[a] - (int64_t)c[a] * P.cell_w[a] : 0;
+        const float top = (float)bins - margin, hi = 1.0f - margin;
+        for (int oz = 0; oz < (D == 3 ? 3 : 1); oz++) {
+            int64_t z = D == 3 ? (int64_t)c[2] + oz - 1 : 0, sz = 0;
+            if (D == 3 && z < 0) z += P.nc[2], sz = -P.box[2];
+            if (D == 3 && z >= (int64_t)P.nc[2]) z -= P.nc[2], sz = P.box[2];
+            for (int oy = 0; oy < 3; oy++) {
+                int64_t y = (int64_t)c[1] + oy - 1, sy = 0;
+                if (y < 0) y += P.nc[1], sy = -P.box[1];
+                if (y >= (int64_t)P.nc[1]) y -= P.nc[1], sy = P.box[1];
+                for (int ox = 0; ox < 3; ox++) {
+                    int64_t x = (int64_t)c[0] + ox - 1, sx = 0;
+                    if (x < 0) x += P.nc[0], sx = -P.box[0];
+                    if (x >= (int64_t)P.nc[0]) x -= P.nc[0], sx = P.box[0];
+                    const uint32_t cell = (uint32_t)((z * P.nc[1] + y) * P.nc[0] + x);
+                    const uint32_t j0 = max(start[cell], i + 1), j1 = start[cell + 1];
+                    if (j0 >= j1) continue;
+                    const float b0 = off_f32((x - (int64_t)c[0]) * P.cell_w[0] + sx - reli[0]);
+                    const float b1 = off_f32((y - (int64_t)c[1]) * P.cell_w[1] + sy - reli[1]);
+                    const float b2 = D == 3 ? off_f32((z - (int64_t)c[2]) * P.cell_w[2] + sz - reli[2]) : 0.0f;
+#pragma unroll 2
+                    for (uint32_t j = j0; j < j1; j++) {
+                        const float4 r = relf[j];
+                        const float d0 = __fadd_rn(r.x, b0), d1 = __fadd_rn(r.y, b1);
+                        float r2f = __fmaf_rn(d1, d1, __fmul_rn(d0, d0));
+                        if (D == 3) {
+                            const float d2 = __fadd_rn(r.z, b2);
+                            r2f = __fmaf_rn(d2, d2, r2f);
+                        }
+                        if (r2f > lim2f) continue;
+                        const float rf = __fmul_rn(__fsqrt_rn(r2f), scalef);
+                        const float fl = floorf(rf), fr = __fsub_rn(rf, fl);
+                        int k;
+                        if (fr > margin && fr < hi && rf < top) {
+                            k = (int)fl;
+                        } else {
+                            int64_t xj[3], d[3];
+                            load_particle<D, false>(pos, nullptr, j, xj);
+#pragma unroll
+                            for (int a = 0; a < D; a++) d[a] = min_image(xj[a] - xi[a], P.box[a], P.half[a]);
+                            k = rdf_bin_exact<D>(d, bins, scale);
+                        }
+                        if (k >= 0) atomicAdd(&h[k], 1u);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x)
+        if (h[b]) atomicAdd(out + b, (unsigned long long)h[b]);
+}
+
+// The same counts for cells wider than the f32 offsets of the scratch state cover (rmax beyond
+// about 40 sigma): every candidate from the exact integer separation.
+template <int D>
+__global__ void k_rdf_wide(Params P, const Rec<D>* pos, const uint32_t* keys, const uint32_t* start, uint32_t bins, double scale,
                       float scalef, float lim2f, float margin, unsigned long long* out) {
     extern __shared__ uint32_t h[];
     for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
@@ -1696,8 +1777,38 @@ __global__ void k_rdf_all(Params P, const Rec<D>* pos, uint32_t bins, double sca
 
 // Particle counts in slabs along one axis: min(floor(x / L * bins), bins - 1) in f64.
 // Positions are wrapped first (between list builds they may lie up to the skin outside [0, L)).
+// The f32 estimate x_f32 * (bins / L)_f32 is within 3 2^-24 bins (+ 2^-24 bins / L) of the
+// exact quotient: a particle farther than `margin` from a slab edge takes its floor, the rest
+// the f64 definition. Each block counts into shared memory and adds its counts once.
+__device__ __forceinline__ uint32_t profile_bin(int64_t x, double l, uint32_t bins, float sf, float margin) {
+    // x in [0, L): integer part (< 2^24 sigma) and the fraction's top 24 bits, each exact in f32
+    const float xf = __fadd_rn(__int2float_rn((int32_t)(x >> 32)), __fmul_rn(__uint2float_rn((uint32_t)x >> 8), 0x1p-24f));
+    const float t = __fmul_rn(xf, sf), fl = floorf(t), fr = __fsub_rn(t, fl);
+    if (fr > margin && fr < 1.0f - margin) {
+        const uint32_t k = (uint32_t)fl;
+        return k < bins - 1 ? k : bins - 1;
+    }
+    return cell_of(x, l, bins);
+}
+
 template <int D>
-__global__ void k_profile(uint32_t n, const Rec<D>* pos, uint32_t axis, int64_t lfix, double l, uint32_t bins, unsigned long long* out) {
+__global__ void k_profile(uint32_t n, const Rec<D>* pos, uint32_t axis, int64_t lfix, double l, uint32_t bins, float sf, float margin,
+                          unsigned long long* out) {
+    extern __shared__ uint32_t h[];
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long* p = reinterpret_cast<const long long*>(pos + i);
+        atomicAdd(&h[profile_bin(wrap(p[axis], lfix), l, bins, sf, margin)], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x)
+        if (h[b]) atomicAdd(out + b, (unsigned long long)h[b]);
+}
+
+// The same with one global atomic per particle, for more bins than fit in shared memory.
+template <int D>
+__global__ void k_profile_wide(uint32_t n, const Rec<D>* pos, uint32_t axis, int64_t lfix, double l, uint32_t bins, unsigned long long* out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const long long* p = reinterpret_cast<const long long*>(pos + i);
@@ -1774,12 +1885,36 @@ extern "C" int gbmd_observe_begin(gbmd_engine* e, uint32_t rdf_bins, double rdf_
             }
             uint32_t* saved = e->start;
             e->start = e->obs_start;
+            double wmax = 0.0;
+            for (int a = 0; a < e->D; a++) wmax = std::max(wmax, (double)P.cell_w[a] * 0x1p-32);
+            // The f32 offsets (relf, and each cell's base) lie within [-M, M), M the power of two
+            // at or above 2 cell sides + 1; each carries a truncation below 2^-24 and a rounding of
+            // at most M 2^-25, and so does their sum: per axis |d_f32 - d| <= delta. The sum of
+            // squares, the square root and the product with the f32 scale add (D + 3) 2^-24
+            // relatively. Twice the resulting bound, in bins, is the margin.
+            double M = 1.0;
+            while (M < 2.0 * wmax + 1.0) M *= 2.0;
+            const bool narrow = M <= 64.0; // offsets >> 8 fit an int32
+            const double delta = 2.0 * 0x1p-24 + 3.0 * M * 0x1p-25;
+            const double err = std::sqrt((double)e->D) * delta + (rdf_rmax + 1.0) * (e->D + 3) * 0x1p-24;
+            const float margin_c = (float)(2.0 * scale * err + 1e-5);
+            const float lim2f_c = (float)((rdf_rmax + 2.0 * err) * (rdf_rmax + 2.0 * err) * (1.0 + 0x1p-20));
             if (e->D == 2) {
                 enqueue_bin<2>(e, e->st, P);
-                k_rdf<2><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<2>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, scalef, lim2f, margin, dbuf);
+                if (narrow)
+                    k_rdf<2><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<2>*)e->pos_scr, e->relf, e->keys[e->sorted], e->start, rdf_bins,
+                                                                     scale, scalef, lim2f_c, margin_c, dbuf);
+                else
+                    k_rdf_wide<2><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<2>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins,
+                                                                          scale, scalef, lim2f, margin, dbuf);
             } else {
                 enqueue_bin<3>(e, e->st, P);
-                k_rdf<3><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<3>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins, scale, scalef, lim2f, margin, dbuf);
+                if (narrow)
+                    k_rdf<3><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<3>*)e->pos_scr, e->relf, e->keys[e->sorted], e->start, rdf_bins,
+                                                                     scale, scalef, lim2f_c, margin_c, dbuf);
+                else
+                    k_rdf_wide<3><<<blocks_for(n, 128), 128, shm, e->st>>>(P, (const Rec<3>*)e->pos_scr, e->keys[e->sorted], e->start, rdf_bins,
+                                                                          scale, scalef, lim2f, margin, dbuf);
             }
             note_launch();
             e->start = saved;
@@ -1789,8 +1924,20 @@ extern "C" int gbmd_observe_begin(gbmd_engine* e, uint32_t rdf_bins, double rdf_
         unsigned long long* pbuf = dbuf + rdf_bins;
         double l = to_f64h(e->sys.box_len[profile_axis]);
         int64_t lfix = e->P.box[profile_axis];
-        if (e->D == 2) k_profile<2><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
-        else k_profile<3><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<3>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
+        if (profile_bins <= 8192 && l < 0x1p23) {
+            const float sf = (float)((double)profile_bins / l);
+            const float margin = (float)(4.0 * 0x1p-24 * profile_bins * (1.0 + 1.0 / l) + 1e-6);
+            const uint32_t grid = std::min(blocks_for(n, 256), 1024u);
+            const size_t shm = (size_t)profile_bins * 4;
+            if (e->D == 2)
+                k_profile<2><<<grid, 256, shm, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, sf, margin, pbuf);
+            else
+                k_profile<3><<<grid, 256, shm, e->st>>>(n, (const Rec<3>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, sf, margin, pbuf);
+        } else if (e->D == 2) {
+            k_profile_wide<2><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
+        } else {
+            k_profile_wide<3><<<blocks_for(n, 256), 256, 0, e->st>>>(n, (const Rec<3>*)e->pos[e->cur], profile_axis, lfix, l, profile_bins, pbuf);
+        }
         note_launch();
     }
     if (nbins) {

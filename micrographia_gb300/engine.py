@@ -310,7 +310,9 @@ def make_init(recipe, n, t, seed, jitter=0.1, rho_liquid=0.7, rho_vapour=0.05, s
 class BatchEngine:
     """Many independent periodic systems stepped together (gbmd_batch_*)."""
 
-    def __init__(self, systems, states, mode=None, threads=0, block_steps=0, device=0):
+    def __init__(self, systems, states, mode=None, threads=0, block_steps=0, device=0, tune_skin=False):
+        """With `tune_skin`, the Verlet skin is the fastest of 0.3..0.7 sigma on a short timed
+        run from these states (mode's skin ignored); the trajectory is the same for any skin."""
         self._lib = _abi.lib()
         if len(systems) != len(states) or not systems:
             raise ValueError("one state per system")
@@ -325,7 +327,8 @@ class BatchEngine:
         pos = np.ascontiguousarray(np.concatenate([st.pos for st in states]))
         vel = np.ascontiguousarray(np.concatenate([st.vel for st in states]))
         sp = np.ascontiguousarray(np.concatenate([st.species for st in states]))
-        opts = _options(mode or ForceMode.verlet_for(systems[0], 0), threads, block_steps, device=device)
+        opts = _options(mode or ForceMode.verlet_for(systems[0], 0), threads, block_steps, device=device,
+                        flags=_abi.FLAG_TUNE_SKIN if tune_skin else 0)
         h = C.c_void_p()
         _abi.check(
             self._lib.gbmd_batch_create(
@@ -343,6 +346,12 @@ class BatchEngine:
 
     def step(self, steps=1):
         _abi.check(self._lib.gbmd_batch_step(self._h, int(steps)))
+
+    @property
+    def skin(self):
+        v = C.c_double()
+        _abi.check(self._lib.gbmd_batch_skin(self._h, C.byref(v)))
+        return v.value
 
     def wait(self):
         _abi.check(self._lib.gbmd_batch_sync(self._h))

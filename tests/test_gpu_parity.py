@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from micrographia_gb300 import ONE, ForceMode, GpuEngine, GpuEngine3, Pair, State, System, System3, box_for, cube_for
+from micrographia_gb300 import ONE, ForceMode, GpuEngine, GpuEngine3, Pair, State, State3, System, System3, box_for, cube_for
 from micrographia_gb300 import _abi
 from micrographia_gb300.engine import init_state, make_init
 
@@ -482,6 +482,42 @@ def test_rdf_small_box_all_pairs(O, dim):
     assert ref.sum() > 0
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_rdf_and_profile_on_exact_bin_edges(O, dim):
+    """A unit lattice in a box of whole sigmas: pair distances 1, 2, 3, 4 and 5 (= rmax) fall
+    exactly on RDF bin edges and every particle exactly on a profile slab edge, so the f32
+    estimates hand these to the f64 definition; the counts equal the oracle's."""
+    side = 64 if dim == 2 else 16
+    n = side**dim
+    grid = np.stack(np.meshgrid(*[np.arange(side)] * dim, indexing="ij"), -1).reshape(n, dim)
+    pos = (grid.astype(np.int64) * ONE).astype(np.int64)
+    box = [side * ONE] * dim
+    st = (State if dim == 2 else State3)(pos, np.zeros((n, dim), np.int32), np.zeros(n, np.uint32))
+    if dim == 2:
+        sys_, eng = System(box, 0.005, Pair.lj(2.5), [1.0]), GpuEngine
+    else:
+        sys_, eng = System3(box, 0.005, Pair.lj(2.5), [1.0]), GpuEngine3
+    with eng(sys_, st, ForceMode.verlet_with_skin(sys_, n, 0.3)) as g:
+        _, rdf, prof = g.observe(rdf_bins=200, rdf_rmax=5.0, profile_bins=side, profile_axis=dim - 1)
+    want = O.rdf(sys_, st, 200, 5.0)
+    assert np.array_equal(rdf, want)
+    assert want[40] > 0 and want[80] > 0  # r = 1 and r = 2 exactly at the edges of bins 40, 80
+    assert np.array_equal(prof, O.profile(sys_, st, side, dim - 1))
+    assert np.all(prof == n // side)
+
+
+def test_rdf_with_cells_wider_than_the_f32_offsets(O):
+    """rmax = 45 sigma: RDF cells of ~47 sigma, beyond what the f32 cell offsets cover; the
+    integer-separation kernel counts the same pairs as the oracle."""
+    sys_, s = fluid(O, 1000, 0.05, Pair.lj(2.5), 8)
+    with GpuEngine(sys_, s) as g:
+        g.step(20)
+        _, rdf, prof = g.observe(rdf_bins=100, rdf_rmax=45.0, profile_bins=10000, profile_axis=0)
+        st = g.read_state()
+    assert np.array_equal(rdf, O.rdf(sys_, st, 100, 45.0))
+    assert np.array_equal(prof, O.profile(sys_, st, 10000, 0))  # more bins than shared memory holds
+
+
 # ---------------------------------------------------------------- checkpoint / resume
 @pytest.mark.parametrize("dim", [2, 3])
 def test_snapshot_resume_is_bit_identical(O, dim):
@@ -691,6 +727,25 @@ def test_batch_replicas_match_their_plain_runs(O):
             c = O.IntEngine(sys_, st)
             c.step(150)
             assert b.read_system(k) == c.state, k
+
+
+def test_batch_skin_tuner_keeps_the_trajectory(O):
+    """The skin autotuner picks one of its candidates from timed trial runs on the given states;
+    the replicas still equal their plain oracle runs bit for bit at that skin."""
+    from micrographia_gb300 import BatchEngine, workloads
+
+    cfg = workloads.config4(count=6, base_seed=9, n_min=512, n_max=4096)
+    systems = [s for s, _ in cfg]
+    states = [O.init(s, spec) for s, spec in cfg]
+    with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3), tune_skin=True) as b:
+        assert b.skin in (0.3, 0.4, 0.5, 0.6, 0.7)
+        b.step(120)
+        for k, (sys_, st) in enumerate(zip(systems, states)):
+            c = O.IntEngine(sys_, st)
+            c.step(120)
+            assert b.read_system(k) == c.state, k
+    with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.45)) as b:
+        assert b.skin == 0.45
 
 
 def test_batch_3d(O):
