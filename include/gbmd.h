@@ -67,8 +67,17 @@ typedef struct gbmd_pair {
 /*
  * The System fields the LJ path needs: md_core::System (crates/md-core/src/system.rs:26-64) and
  * md_core::three::System3 (crates/md-core/src/three.rs:13-31). `pairs` is row-major
- * [a * nspecies + b] like `System::pairs`. Walls, baths, compartments, membranes, pistons and
- * bonds are outside this engine: `periodic` must have every axis set.
+ * [a * nspecies + b] like `System::pairs`. Walls, compartments, membranes, pistons and bonds are
+ * outside this engine: `periodic` must have every axis set.
+ *
+ * The Andersen heat bath (`bath` = 1): md_core::Thermostat (system.rs:156-175, built by
+ * with_thermostat / with_fan / with_bath_layer, system.rs:326-353) in 2D and three::Bath
+ * (three.rs:79-81) in 3D. After its kick, a particle of a species in `bath_species`, not pinned,
+ * and (2D) with its position along `bath_axis` in [bath_region[0], bath_region[1]) is given a new
+ * Maxwell velocity at bath_t with probability bath_rate * dt per step, drawn from Threefry on
+ * (its id, the engine's step clock): walls::andersen (walls.rs:113-133) and three::andersen
+ * (three.rs:247-265). 2D adds the fan's drift to the new x velocity. The energy the bath gives
+ * is booked in ledger slot GBMD_LEDGER_BATH.
  */
 typedef struct gbmd_system {
     uint32_t dim;      /* 2 or 3 */
@@ -81,6 +90,14 @@ typedef struct gbmd_system {
     uint64_t seed;
     uint32_t periodic; /* bit a set if axis a is periodic */
     uint32_t pinned;   /* bit s set if species s is pinned */
+    uint32_t bath;          /* 1: an Andersen heat bath (Some(Thermostat)); 0: none */
+    uint32_t bath_species;  /* bit s set if it acts on species s (with_thermostat: all) */
+    uint32_t bath_axis;     /* 2D: the axis of its region (0 x: a fan; 1 y: a bath layer) */
+    uint32_t _bath_pad;
+    double bath_t;          /* kT */
+    double bath_rate;       /* redraws per particle per tau */
+    double bath_drift;      /* 2D: mean x velocity of redrawn particles, sigma/tau */
+    int64_t bath_region[2]; /* 2D: [lo, hi) along bath_axis in position units (all: INT64_MIN, INT64_MAX) */
 } gbmd_system;
 
 /* Engine options: ForceMode + Arith + the engine's own tuning knobs. Zero-initialised is valid. */
@@ -208,6 +225,14 @@ int gbmd_list_stats(gbmd_engine* e, uint32_t* rebuilds, int32_t* overflow);
 int gbmd_state_hash(gbmd_engine* e, uint64_t* hash);
 /* Net steps (GpuEngine::steps) and the clock (steps in either direction). */
 int gbmd_counters(gbmd_engine* e, int64_t* steps, uint32_t* clock);
+/* The energy/impulse ledger (md_core::walls::Ledger, walls.rs:40-50; GpuEngine::read_ledger):
+ * GBMD_LEDGER_SLOTS entries each, slot 2 axis + side for walls, GBMD_LEDGER_BATH for the heat
+ * bath. This engine has no walls or membranes, so only the bath slot fills: the energy it gave
+ * (each event's f64 energy change rounded half away from zero to 2^-24 epsilon and summed as an
+ * integer, so the total does not depend on the order of events) and its redraw count. */
+#define GBMD_LEDGER_SLOTS 7
+#define GBMD_LEDGER_BATH 6
+int gbmd_read_ledger(gbmd_engine* e, double* energy, double* impulse, uint64_t* hits);
 /* The CUDA stream the engine launches on (a cudaStream_t), for event timing by the caller. */
 int gbmd_stream(gbmd_engine* e, void** stream);
 /* Kernels launched by this engine so far (every launch, graph nodes included). */

@@ -19,6 +19,7 @@ from .core import (
     State3,
     System,
     System3,
+    Thermostat,
     box_for,
     cube_for,
     fcc_cells,
@@ -37,6 +38,7 @@ __all__ = [
     "State3",
     "System",
     "System3",
+    "Thermostat",
     "GpuEngine",
     "GpuEngine3",
     "BatchEngine",

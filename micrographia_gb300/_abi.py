@@ -50,7 +50,19 @@ class gbmd_system(C.Structure):
         ("seed", C.c_uint64),
         ("periodic", C.c_uint32),
         ("pinned", C.c_uint32),
+        ("bath", C.c_uint32),
+        ("bath_species", C.c_uint32),
+        ("bath_axis", C.c_uint32),
+        ("_bath_pad", C.c_uint32),
+        ("bath_t", C.c_double),
+        ("bath_rate", C.c_double),
+        ("bath_drift", C.c_double),
+        ("bath_region", C.c_int64 * 2),
     ]
+
+
+LEDGER_SLOTS = 7  # md_core::walls::WALLS: 2 axis + side, membrane faces 4 and 5, the bath
+LEDGER_BATH = 6
 
 
 FLAG_WHOLE_CELLS = 1  # list builds scan whole neighbour cells (no slab sub-buckets)
@@ -204,6 +216,7 @@ SIGNATURES = [
     ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
     ("gbmd_batch_stats", C.c_int, [VP, _U64P, _U32P]),
     ("gbmd_batch_skin", C.c_int, [VP, C.POINTER(C.c_double)]),
+    ("gbmd_read_ledger", C.c_int, [VP, C.POINTER(C.c_double), C.POINTER(C.c_double), _U64P]),
     ("gbmd_batch_destroy", C.c_int, [VP]),
     ("gbmd_serve_create", C.c_int, [C.c_uint64, C.c_uint32, C.c_int32, P(VP)]),
     ("gbmd_serve_submit", C.c_int, [VP, P(gbmd_serve_request), _U64P]),

@@ -110,6 +110,7 @@ class _SystemBase:
         self.gravity = [0.0] * self.DIM
         self.seed = 1
         self.pinned = 0
+        self.thermostat = None
 
     def species(self):
         return len(self.masses)
@@ -133,6 +134,14 @@ class _SystemBase:
 
     def with_pinned(self, s):
         self.pinned |= 1 << s
+        return self
+
+    def with_thermostat(self, t, rate):
+        """System::with_thermostat (system.rs:326-333) / System3::with_thermostat (three.rs:79-83):
+        an Andersen bath at kT `t`, `rate` redraws per particle per tau, keeping the species,
+        region and drift of a bath already present."""
+        old = self.thermostat
+        self.thermostat = Thermostat(float(t), float(rate)) if old is None else Thermostat(float(t), float(rate), old.species, old.region, old.axis, old.drift)
         return self
 
     def pair(self, a, b):
@@ -188,13 +197,49 @@ class _SystemBase:
         s.seed = self.seed
         s.periodic = (1 << self.DIM) - 1
         s.pinned = self.pinned
+        th = self.thermostat
+        if th is not None:
+            s.bath = 1
+            s.bath_species = th.species & 0xFFFFFFFF
+            s.bath_axis = th.axis
+            s.bath_t, s.bath_rate, s.bath_drift = th.t, th.rate, th.drift
+            s.bath_region[0], s.bath_region[1] = th.region
         return s
+
+
+class Thermostat:
+    """md_core::Thermostat (system.rs:156-175); in 3D three::Bath (species only)."""
+
+    def __init__(self, t, rate, species=0xFFFFFFFF, region=(-(1 << 63), (1 << 63) - 1), axis=0, drift=0.0):
+        self.t, self.rate, self.species = float(t), float(rate), int(species)
+        self.region, self.axis, self.drift = (int(region[0]), int(region[1])), int(axis), float(drift)
+
+    def acts_on(self, s, p):
+        """Thermostat::acts_on (system.rs:172-174)."""
+        return bool(self.species & (1 << s)) and self.region[0] <= p[self.axis] < self.region[1]
 
 
 class System(_SystemBase):
     """md_core::System (system.rs:26-64), periodic LJ subset."""
 
     DIM = 2
+
+    def with_fan(self, species, x0, x1, drift):
+        """System::with_fan (system.rs:335-344): the bath acts on `species` (a bitmask) with
+        x0 <= x < x1 (sigma), around a mean x velocity `drift`."""
+        if self.thermostat is None:
+            raise ValueError("a fan is a thermostat with a region: add the thermostat first")
+        th = self.thermostat
+        self.thermostat = Thermostat(th.t, th.rate, species, (to_fixed(x0), to_fixed(x1)), 0, drift)
+        return self
+
+    def with_bath_layer(self, y0, y1):
+        """System::with_bath_layer (system.rs:346-353): the bath acts on y0 <= y < y1 (sigma)."""
+        if self.thermostat is None:
+            raise ValueError("a bath layer is a thermostat with a region: add the thermostat first")
+        th = self.thermostat
+        self.thermostat = Thermostat(th.t, th.rate, th.species, (to_fixed(y0), to_fixed(y1)), 1, th.drift)
+        return self
 
 
 class System3(_SystemBase):

@@ -550,6 +550,7 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
         GBMD_TRY(validate_system(systems[k], offsets[k + 1] - offsets[k]));
         if (systems[k].dim != D) return fail(GBMD_E_INVALID, "a batch holds systems of one dimension");
         if (offsets[k + 1] <= offsets[k]) return fail(GBMD_E_INVALID, "every system needs at least one particle");
+        if (systems[k].bath) return fail(GBMD_E_UNSUPPORTED, "batches run systems without a heat bath (one engine per system runs it)");
     }
     if (offsets[0] != 0) return fail(GBMD_E_INVALID, "offsets[0] must be 0");
     if (o.flags & GBMD_FLAG_TUNE_SKIN) GBMD_TRY(tune_skin(systems, count, offsets, pos, vel, species, o));

@@ -60,6 +60,11 @@ int validate_system(const gbmd_system& sys, uint32_t n) {
     for (uint32_t s = 0; s < sys.nspecies; s++)
         if (!(sys.masses[s] > 0.0)) return fail(GBMD_E_INVALID, "masses must be positive");
     if (!(sys.dt > 0.0)) return fail(GBMD_E_INVALID, "dt must be positive");
+    if (sys.bath) {
+        if (!(sys.bath_t >= 0.0 && sys.bath_t < INFINITY) || !(sys.bath_rate >= 0.0 && sys.bath_rate < INFINITY))
+            return fail(GBMD_E_INVALID, "the heat bath needs a finite temperature and rate, both >= 0");
+        if (sys.bath_axis >= sys.dim || !(std::fabs(sys.bath_drift) < INFINITY)) return fail(GBMD_E_INVALID, "bad heat bath axis or drift");
+    }
     (void)n;
     return GBMD_OK;
 }
@@ -168,6 +173,8 @@ float fast_pair_lo(const PairC& c) {
     return lo;
 }
 
+// System::to_step_displacement (system.rs:427-429): (v dt 2^32).round() as i32.
+int32_t to_step_displacement(const gbmd_system& s, double v) { return sat_i32_host(std::round(v * s.dt * 4294967296.0)); }
 void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint32_t cap, const uint32_t* nc) {
     std::memset(&P, 0, sizeof(P));
     P.n = n;
@@ -219,6 +226,20 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
     double r_list = (rc_max(s) + skin) * (1.0 + 1e-4);
     P.reach = (int64_t)std::ceil((r_list + skin + 2.0) * 4294967296.0);
     set_cells(P, P.nc, s.dim);
+    if (s.bath) {
+        // walls::andersen / three::andersen: the threshold rate dt, sqrt(t / m) per species, the
+        // thermostat key (walls.rs:110, STREAM_THERMO) and the fan's drift in integer units
+        P.bath = 1;
+        P.bath_species = s.bath_species;
+        P.bath_axis = s.dim == 2 ? s.bath_axis : 0;
+        P.bath_drift = s.dim == 2 ? to_step_displacement(s, s.bath_drift) : 0;
+        P.bath_region[0] = s.dim == 2 ? s.bath_region[0] : INT64_MIN;
+        P.bath_region[1] = s.dim == 2 ? s.bath_region[1] : INT64_MAX;
+        P.bath_rate_dt = s.bath_rate * s.dt;
+        for (uint32_t sp = 0; sp < s.nspecies; sp++) P.bath_sd[sp] = std::sqrt(s.bath_t / s.masses[sp]);
+        P.bath_key[0] = (uint32_t)s.seed;
+        P.bath_key[1] = (uint32_t)(s.seed >> 32) ^ 0x5448524du;
+    }
 }
 
 // Cell grid of a parameter block: counts, the f32 cell-index helpers and whether candidates of
@@ -301,7 +322,8 @@ struct gbmd_engine {
     uint32_t *nbr = nullptr, *nbr_count = nullptr;
     float4* relf = nullptr;  // cell-relative f32 coordinates of the sorted scratch state
     uint4* qpos[2] = {nullptr, nullptr}; // quotient records of the positions (ping-pong)
-    uint32_t* ctl = nullptr; // [0] rebuild, [1] overflow, [2] rebuilds
+    uint32_t* ctl = nullptr; // [0] rebuild, [1] overflow, [2] rebuilds; [CTL_CLOCK] the bath's step clock
+    unsigned long long* ledger = nullptr; // the bath's ledger slot: energy (2^-24 epsilon), redraws
     double* partial = nullptr;
     void* staging = nullptr;  // id-ordered I/O staging (n * D int64)
     int32_t* staging_v = nullptr;
@@ -416,7 +438,7 @@ void free_all(gbmd_engine* e) {
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
                     e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1],
-                    e->obs_bins, e->obs_start, e->itab, e->ipair};
+                    e->obs_bins, e->obs_start, e->itab, e->ipair, e->ledger};
     for (void* p : ptrs)
         if (p) cudaFreeAsync(p, e->st);
     if (e->st) cudaStreamDestroy(e->st);
@@ -535,6 +557,9 @@ template <int D, bool MULTI> void enqueue_force_t(gbmd_engine* e, cudaStream_t s
     if (e->P.int_mode) enqueue_force_a<D, MULTI, true>(e, s, threads);
     else enqueue_force_a<D, MULTI, false>(e, s, threads);
 }
+__global__ void k_clock_tick(uint32_t* ctl) { ctl[CTL_CLOCK] += 1u; }
+__global__ void k_clock_set(uint32_t* ctl, uint32_t clock) { ctl[CTL_CLOCK] = clock; }
+
 void enqueue_force(gbmd_engine* e, cudaStream_t s) {
     uint32_t threads = e->opt.threads ? e->opt.threads : 128;
     if (e->D == 2) {
@@ -543,6 +568,18 @@ void enqueue_force(gbmd_engine* e, cudaStream_t s) {
     } else {
         if (e->multi) enqueue_force_t<3, true>(e, s, threads);
         else enqueue_force_t<3, false>(e, s, threads);
+    }
+    if (e->P.bath) { // the Andersen bath on the moved state, then the step clock advances
+        const uint32_t nb = blocks_for(e->n, 256);
+        if (e->D == 2) {
+            if (e->verlet) k_bath<2, true><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<2>*)e->ref_pos, e->ctl, e->ledger);
+            else k_bath<2, false><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger);
+        } else {
+            if (e->verlet) k_bath<3, true><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<3>*)e->ref_pos, e->ctl, e->ledger);
+            else k_bath<3, false><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger);
+        }
+        k_clock_tick<<<1, 1, 0, s>>>(e->ctl);
+        note_launch(2);
     }
 }
 
@@ -643,7 +680,7 @@ cudaError_t enqueue_loop(gbmd_engine* e, cudaStream_t s) {
 // kernel's; fewer if the grid would not be resident.
 int setup_step_loop(gbmd_engine* e) {
     e->loop_lanes = 0;
-    if (!e->verlet || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every ||
+    if (!e->verlet || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath ||
         (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP))
         return GBMD_OK;
     if (e->block_steps > (1u << 20)) return GBMD_OK; // (the barrier counts k x blocks arrivals in 32 bits)
@@ -953,9 +990,6 @@ __global__ void k_set_species_velocity(uint32_t n, uint32_t dim, const uint32_t*
     vel[dim * s + 1] = v.y;
     if (dim == 3) vel[dim * s + 2] = v.z;
 }
-// System::to_step_displacement (system.rs:427-429): (v dt 2^32).round() as i32.
-int32_t to_step_displacement(const gbmd_system& s, double v) { return sat_i32_host(std::round(v * s.dt * 4294967296.0)); }
-
 int upload_state(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const uint32_t* species) {
     size_t n = e->n, D = e->D;
     for (size_t i = 0; i < n; i++)
@@ -1077,6 +1111,8 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         GBMD_TRY(allocT(e, &e->nbr_count, n));
     }
     GBMD_TRY(allocT(e, &e->ctl, 16));
+    GBMD_TRY(allocT(e, &e->ledger, 2));
+    GBMD_CUDA_TRY(cudaMemsetAsync(e->ledger, 0, 16, e->st));
     if (e->opt.arith == GBMD_ARITH_INT) {
         std::vector<int32_t> tab;
         std::vector<double> pair4;
@@ -1173,6 +1209,10 @@ int gbmd_step(gbmd_engine* e, uint64_t steps) {
     if (e->failed) return fail(GBMD_E_OVERFLOW, "the engine is in a failed state (a list overflowed, or a step-loop barrier ran out); gbmd_upload a state to continue");
     uint64_t left = steps;
     uint32_t every = e->opt.rescale_every;
+    if (e->P.bath && steps) { // the device clock follows the host's (uploads, snapshots, reversals)
+        k_clock_set<<<1, 1, 0, e->st>>>(e->ctl, e->clock);
+        note_launch();
+    }
     while (left > 0) {
         bool aligned = every == 0 || e->tcount % every == 0;
         if (aligned && left >= e->block_steps) {
@@ -1459,6 +1499,19 @@ int gbmd_state_hash(gbmd_engine* e, uint64_t* hash) {
     std::vector<uint32_t> sp(n);
     GBMD_TRY(gbmd_read_state(e, pos.data(), vel.data(), sp.data()));
     *hash = gbmd_hash_state((uint32_t)D, pos.data(), vel.data(), sp.data(), (uint32_t)n);
+    return GBMD_OK;
+}
+
+int gbmd_read_ledger(gbmd_engine* e, double* energy, double* impulse, uint64_t* hits) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    unsigned long long l[2];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(l, e->ledger, 16, cudaMemcpyDeviceToHost, e->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    for (int w = 0; w < GBMD_LEDGER_SLOTS; w++) {
+        if (energy) energy[w] = w == GBMD_LEDGER_BATH ? (double)(long long)l[0] * (1.0 / 16777216.0) : 0.0;
+        if (impulse) impulse[w] = 0.0;
+        if (hits) hits[w] = w == GBMD_LEDGER_BATH ? (uint64_t)l[1] : 0;
+    }
     return GBMD_OK;
 }
 

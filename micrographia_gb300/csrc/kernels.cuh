@@ -9,6 +9,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "fdlibm.cuh"
 #include "sort.cuh"
 
 namespace gbmd {
@@ -293,6 +294,75 @@ __device__ __forceinline__ void leapfrog(const G& P, uint32_t si, const int32_t*
         v[a] = wadd(wadd(v[a], k[a]), pinned ? 0 : P.gravity[a]);
         x[a] = WRAP ? wrap(x[a] + (int64_t)v[a], P.box[a]) : x[a] + (int64_t)v[a];
     }
+}
+
+// ---------------------------------------------------------------- the Andersen bath
+// walls::andersen (walls.rs:113-133) with IntEngine's use of it (int_engine.rs:275-293) in 2D,
+// three::andersen (three.rs:247-265) with int_engine3.rs:155-160 in 3D: Threefry on (id, clock)
+// under the thermostat key decides, with probability rate dt, to replace the kicked velocity by a
+// Maxwell draw at the bath's temperature (fdlibm ln, cos, sin in IEEE double, the reference's
+// operation order), each component rounded by to_step_displacement; 2D adds the fan's drift to
+// x. The energy change 0.5 m (|v'|^2 - |v|^2), in the reference's f64 order, is booked on the
+// ledger rounded half away from zero to 2^-24 epsilon, so the total does not depend on the order
+// in which the GPU books events.
+struct BathDraw {
+    int32_t v[3];
+    int hit;
+};
+template <int D>
+__device__ __forceinline__ BathDraw bath_draw(uint32_t id, uint32_t clock, uint32_t k0, uint32_t k1, double rate_dt, double sd, double m,
+                                           double dt, int32_t drift, int32_t v0, int32_t v1, int32_t v2, unsigned long long* ledger) {
+    BathDraw o{{v0, v1, v2}, 0};
+    uint32_t r0, r1;
+    threefry2x32(id, clock, k0, k1, r0, r1);
+    if (!(to_unit_f64(r0, 0u) < rate_dt)) return o;
+    uint32_t q0, q1;
+    threefry2x32(id, clock, k0, k1 ^ 1u, q0, q1);
+    const double tau = 6.28318530717958647692;
+    double u[3];
+    {
+        const double rad = __dsqrt_rn(__dmul_rn(-2.0, dev_log(__dsub_rn(1.0, to_unit_f64(r1, 0u)))));
+        const double a = __dmul_rn(tau, to_unit_f64(q0, 0u));
+        const double sr = __dmul_rn(sd, rad);
+        u[0] = __dmul_rn(sr, dev_cos(a));
+        u[1] = __dmul_rn(sr, dev_sin(a));
+        u[2] = 0.0;
+    }
+    if (D == 3) {
+        uint32_t w0, w1;
+        threefry2x32(id, clock, k0, k1 ^ 2u, w0, w1);
+        const double rad3 = __dsqrt_rn(__dmul_rn(-2.0, dev_log(__dsub_rn(1.0, to_unit_f64(w0, 0u)))));
+        const double a3 = __dmul_rn(tau, to_unit_f64(w1, 0u));
+        u[2] = __dmul_rn(__dmul_rn(sd, rad3), dev_cos(a3));
+    }
+    auto vel = [&](int32_t x) { return __ddiv_rn(__dmul_rn((double)x, 1.0 / 4294967296.0), dt); };
+    auto step = [&](double x) { return sat_i32_f64(round_away(__dmul_rn(__dmul_rn(x, dt), 4294967296.0))); };
+    const int32_t vin[3] = {v0, v1, v2};
+    double de;
+    if (D == 2) {
+        const double b0 = vel(v0), b1 = vel(v1);
+        o.v[0] = wadd(step(u[0]), drift);
+        o.v[1] = step(u[1]);
+        const double a0 = vel(o.v[0]), a1 = vel(o.v[1]);
+        // 0.5 m (a0 a0 + a1 a1 - b0 b0 - b1 b1), left to right
+        const double s = __dsub_rn(__dsub_rn(__dadd_rn(__dmul_rn(a0, a0), __dmul_rn(a1, a1)), __dmul_rn(b0, b0)), __dmul_rn(b1, b1));
+        de = __dmul_rn(__dmul_rn(0.5, m), s);
+    } else {
+        double before = 0.0, after = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double b = vel(vin[a]);
+            before = __dadd_rn(before, __dmul_rn(b, b));
+            o.v[a] = step(u[a]);
+            const double c = vel(o.v[a]);
+            after = __dadd_rn(after, __dmul_rn(c, c));
+        }
+        de = __dmul_rn(__dmul_rn(0.5, m), __dsub_rn(after, before));
+    }
+    atomicAdd(ledger, (unsigned long long)sat_i64_f64(round_away(__dmul_rn(de, 16777216.0))));
+    atomicAdd(ledger + 1, 1ull);
+    o.hit = 1;
+    return o;
 }
 
 // The displacement trigger of integrate_list (neighbors.wgsl:90-100): has the particle moved
@@ -741,6 +811,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
 
 // ---------------------------------------------------------------- the persistent step loop
 // Words of the engine's control block used by the loop (0: trigger, 1: overflow, 2: rebuilds).
+constexpr uint32_t CTL_CLOCK = 14;      // the Andersen bath's step clock (IntEngine::clock)
 constexpr uint32_t CTL_LOOP_DONE = 4;   // steps the loop has taken in the current graph block
 constexpr uint32_t CTL_BAR_GEN = 6;     // grid barrier: barriers released (low 31 bits) | stop (bit 31)
 constexpr uint32_t CTL_LOOP_ERR = 8;    // a barrier wait ran out (the loop stopped; an error status)
@@ -862,6 +933,49 @@ __global__ void __launch_bounds__(128, 10) k_force_loop(Params P, PosRec<D>* __r
     if (t == 0) {
         ctl[CTL_LOOP_DONE] = done + k;
         ctl[CTL_LOOP_ITERS] += 1u;
+    }
+}
+
+// The bath as a pass after the force step, so that the force kernels carry none of it: the step
+// left x' = x + v with v the kicked velocity; a redrawn particle gets v' and x' + (v' - v) =
+// x + v', exact in integers (wrapped again in cell mode, where positions stay in the box). The
+// region test uses the position before the drift, x' - v, as the reference does. With Verlet
+// lists the quotient record is rewritten and the displacement trigger re-tested at the new
+// position (a trigger the force step already set stays set: an extra rebuild changes nothing).
+// The draw is keyed on the clock word, which the next launch in the stream advances.
+template <int D, bool LIST>
+__global__ void k_bath(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict__ qpos, int32_t* __restrict__ vel,
+                       const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids, const PosRec<D>* __restrict__ ref_pos,
+                       uint32_t* __restrict__ ctl, unsigned long long* __restrict__ ledger) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const uint32_t si = species[i];
+    if (((P.pinned >> si) & 1u) || !((P.bath_species >> si) & 1u)) return;
+    int64_t x[3];
+    load_particle<D, false>(pos, nullptr, i, x);
+    int32_t v[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
+    if (D == 2) {
+        const uint32_t ax = P.bath_axis;
+        const int64_t p = wrap(x[ax] - (int64_t)v[ax], P.box[ax]);
+        if (!(p >= P.bath_region[0] && p < P.bath_region[1])) return;
+    }
+    const BathDraw o = bath_draw<D>(ids[i], ctl[CTL_CLOCK], P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si], P.masses[si], P.dt,
+                                    P.bath_drift, v[0], v[1], v[2], ledger);
+    if (!o.hit) return;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const int64_t y = x[a] + ((int64_t)o.v[a] - (int64_t)v[a]);
+        x[a] = LIST ? y : wrap(y, P.box[a]);
+        vel[D * i + a] = o.v[a];
+    }
+    store_pos<D>(pos, i, x, si);
+    if (LIST) {
+        qpos[i] = quot_record<D>(x, si);
+        int64_t xr[3];
+        load_particle<D, false>(ref_pos, nullptr, i, xr);
+        if (moved_half_skin<D>(P, xr, x)) ctl[0] = 1;
     }
 }
 

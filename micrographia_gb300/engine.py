@@ -199,6 +199,15 @@ class _Engine:
         )
         return f, rdf, prof
 
+    def read_ledger(self):
+        """GpuEngine::read_ledger: (energy, impulse, hits), one entry per ledger slot; this engine
+        fills the heat bath's slot (_abi.LEDGER_BATH): the energy it gave and its redraws."""
+        e = (C.c_double * _abi.LEDGER_SLOTS)()
+        p = (C.c_double * _abi.LEDGER_SLOTS)()
+        h = (C.c_uint64 * _abi.LEDGER_SLOTS)()
+        _abi.check(self._lib.gbmd_read_ledger(self._h, e, p, h))
+        return list(e), list(p), list(h)
+
     def read_list_stats(self):
         r, o = C.c_uint32(), C.c_int32()
         _abi.check(self._lib.gbmd_list_stats(self._h, C.byref(r), C.byref(o)))

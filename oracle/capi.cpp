@@ -252,6 +252,20 @@ void oracle_engine_set_state(void* h, const int64_t* pos, const int32_t* vel, co
     std::memcpy(s.species.data(), species, s.species.size() * 4);
 }
 uint64_t oracle_engine_hash(void* h) { return ((Engine*)h)->state().hash(); }
+void oracle_engine_ledger(void* h, double* energy, int64_t* energy_fixed, uint64_t* hits, uint32_t* clock) {
+    Engine* e = (Engine*)h;
+    const BathLedger& l = e->f32 ? e->f32->ledger : e->f64->ledger;
+    *energy = l.energy;
+    *energy_fixed = l.energy_fixed;
+    *hits = l.hits;
+    *clock = e->f32 ? e->f32->clock : e->f64->clock;
+}
+void oracle_engine_set_system(void* h, const gbmd_system* csys) {
+    Engine* e = (Engine*)h;
+    System sys = System::from_c(*csys);
+    if (e->f32) e->f32->set_system(sys);
+    else e->f64->set_system(sys);
+}
 int64_t oracle_engine_steps(void* h) {
     Engine* e = (Engine*)h;
     return e->f32 ? e->f32->steps : e->f64->steps;

@@ -178,7 +178,17 @@ struct Pair {
 };
 
 // ---------------------------------------------------------------- md-core System / System3
-// The periodic LJ subset of System (system.rs:26-64) and System3 (three.rs:13-31).
+// The Andersen heat bath: md_core::Thermostat (system.rs:156-175) in 2D, three::Bath
+// (three.rs:79-83) in 3D, which has only t, rate and species.
+struct Bath {
+    bool on = false;
+    double t = 0.0, rate = 0.0, drift = 0.0;
+    uint32_t species = 0xffffffffu;
+    int axis = 0;
+    int64_t region[2] = {INT64_MIN, INT64_MAX};
+};
+
+// The periodic LJ subset of System (system.rs:26-64) and System3 (three.rs:13-31), with the bath.
 struct System {
     int dim = 2;
     std::array<int64_t, 3> box{0, 0, 0};
@@ -188,6 +198,7 @@ struct System {
     std::array<double, 3> gravity{0, 0, 0};
     uint64_t seed = 1;
     uint32_t pinned = 0;
+    Bath bath;
 
     static System from_c(const gbmd_system& s) {
         System o;
@@ -200,6 +211,16 @@ struct System {
         for (int a = 0; a < 3; a++) o.gravity[a] = s.gravity[a];
         o.seed = s.seed;
         o.pinned = s.pinned;
+        if (s.bath) {
+            o.bath.on = true;
+            o.bath.t = s.bath_t;
+            o.bath.rate = s.bath_rate;
+            o.bath.drift = s.bath_drift;
+            o.bath.species = s.bath_species;
+            o.bath.axis = (int)s.bath_axis;
+            o.bath.region[0] = s.bath_region[0];
+            o.bath.region[1] = s.bath_region[1];
+        }
         return o;
     }
     int species() const { return (int)masses.size(); }
@@ -839,8 +860,58 @@ inline double pair_kicks_fast(const System& sys, const State& st, const std::vec
 // ---------------------------------------------------------------- IntEngine<F> / IntEngine3<F>
 struct Energy { double kinetic = 0.0, potential = 0.0; };
 
-// md-ref int_engine.rs:23-447 and int_engine3.rs:12-240, for periodic systems (walls, baths,
-// bonds, pistons, membranes and compartments are outside this path). One template serves 2D and
+// ---------------------------------------------------------------- the Andersen bath
+constexpr uint32_t STREAM_THERMO = 0x5448524du; // walls.rs:110
+constexpr double TAU = 6.28318530717958647692;  // std::f64::consts::TAU
+
+// walls::andersen (walls.rs:113-133) for 2D: acts_on (species, and the region along the bath's
+// axis of the position before the drift) and then, with probability rate dt, the new velocity
+// (sigma/tau, before the fan's drift); three::andersen (three.rs:247-265) for 3D: species and
+// pinning, three components. Threefry on (id, clock) under the seed's thermostat key; ln, cos
+// and sin are Rust's f64 methods, i.e. the platform libm (glibc), as here.
+inline bool andersen(const System& sys, uint32_t id, uint32_t clock, uint32_t s, const int64_t* p, double* out) {
+    const Bath& th = sys.bath;
+    if (!th.on) return false;
+    if (!((th.species >> s) & 1u)) return false;
+    if (sys.dim == 2 && !(th.region[0] <= p[th.axis] && p[th.axis] < th.region[1])) return false;
+    if (sys.dim == 3 && sys.is_pinned(s)) return false;
+    const std::array<uint32_t, 2> key{(uint32_t)sys.seed, (uint32_t)(sys.seed >> 32) ^ STREAM_THERMO};
+    const auto r = threefry2x32({id, clock}, key);
+    if (to_unit_f64({r[0], 0}) >= th.rate * sys.dt) return false;
+    const auto r2 = threefry2x32({id, clock}, {key[0], key[1] ^ 1u});
+    const double sd = std::sqrt(th.t / sys.masses[s]);
+    if (sys.dim == 2) {
+        const double u1 = 1.0 - to_unit_f64({r[1], 0});
+        const double u2 = to_unit_f64({r2[0], 0});
+        const double rad = std::sqrt(-2.0 * std::log(u1));
+        const double a = TAU * u2;
+        out[0] = sd * rad * std::cos(a);
+        out[1] = sd * rad * std::sin(a);
+    } else {
+        const auto r3 = threefry2x32({id, clock}, {key[0], key[1] ^ 2u});
+        const double rad = std::sqrt(-2.0 * std::log(1.0 - to_unit_f64({r[1], 0})));
+        const double a = TAU * to_unit_f64({r2[0], 0});
+        const double rad3 = std::sqrt(-2.0 * std::log(1.0 - to_unit_f64({r3[0], 0})));
+        const double a3 = TAU * to_unit_f64({r3[1], 0});
+        out[0] = sd * rad * std::cos(a);
+        out[1] = sd * rad * std::sin(a);
+        out[2] = sd * rad3 * std::cos(a3);
+    }
+    return true;
+}
+
+// The bath's ledger entry (walls::Ledger slot BATH, walls.rs:40-50): energy summed in f64 in
+// particle order as IntEngine does, the same events rounded to 2^-24 and summed as integers (the
+// order-free total the GPU engine keeps), and the redraw count.
+struct BathLedger {
+    double energy = 0.0;
+    int64_t energy_fixed = 0;
+    uint64_t hits = 0;
+};
+inline int64_t ledger_fixed(double de) { return (int64_t)std::round(de * 16777216.0); }
+
+// md-ref int_engine.rs:23-447 and int_engine3.rs:12-240, for periodic systems with an optional
+// Andersen bath (walls, bonds, pistons, membranes and compartments are outside this path). One template serves 2D and
 // 3D; in 2D `fast` selects fast.rs's half-shell path when it applies, as IntEngine::forces does.
 template <typename F> struct IntEngine {
     System sys;
@@ -851,16 +922,24 @@ template <typename F> struct IntEngine {
     std::array<uint32_t, 3> cells{1, 1, 1};
     int64_t steps = 0;
     uint32_t clock = 0;
+    BathLedger ledger;
     bool fast = true;
     IntTables* tables = nullptr;
     FastScratch<F> scratch;
     int threads = 1; // OpenMP threads for the 3D/2D reference loop (the CPU baseline)
 
-    IntEngine(const System& s, const State& st) : sys(s), state(st) {
+    IntEngine(const System& s, const State& st) : state(st) { set_system(s); }
+    // The constructor's derived constants; alone, a run-time change of system (GpuEngine::
+    // update_system, engine.rs:895-934) that keeps the state, counters, clock and ledger.
+    void set_system(const System& s) {
+        sys = s;
+        consts.clear();
+        kick_c.clear();
         for (auto& p : sys.pairs) consts.push_back(PairConsts<F>::make(p));
         for (int k = 0; k < sys.species(); k++) kick_c.push_back(Real<F>::from_f64(sys.kick_coeff((uint32_t)k)));
         gravity = sys.gravity_kick();
         cells = sys.cells_for(sys.rc_max());
+        if (tables) use_integer_tables();
     }
     ~IntEngine() { delete tables; }
     void use_integer_tables() { // IntEngine::integer (int_engine.rs:94-98)
@@ -953,20 +1032,48 @@ template <typename F> struct IntEngine {
         return pe;
     }
 
-    // int_engine.rs:253-344 / int_engine3.rs:138-184 (periodic): v += kick + g; x += v; wrap.
+    // int_engine.rs:253-344 / int_engine3.rs:138-184 (periodic): v += kick + g; the Andersen
+    // bath (int_engine.rs:275-293, int_engine3.rs:155-160); x += v; wrap.
     void step(size_t nsteps) {
         int d = sys.dim;
         std::vector<int32_t> kicks;
+        const int32_t drift = sys.to_step_displacement(sys.bath.drift);
         for (size_t s = 0; s < nsteps; s++) {
             forces(kicks);
             for (size_t i = 0; i < state.n(); i++) {
-                bool pinned = sys.is_pinned(state.species[i]);
-                for (int a = 0; a < d; a++) {
-                    int32_t g = pinned ? 0 : gravity[a];
-                    int32_t v = wadd(wadd(state.vel[d * i + a], kicks[d * i + a]), g);
-                    state.vel[d * i + a] = v;
-                    state.pos[d * i + a] = wrap(state.pos[d * i + a] + (int64_t)v, sys.box[a]);
+                const uint32_t sp = state.species[i];
+                bool pinned = sys.is_pinned(sp);
+                int32_t* v = &state.vel[d * i];
+                int64_t* x = &state.pos[d * i];
+                for (int a = 0; a < d; a++) v[a] = wadd(wadd(v[a], kicks[d * i + a]), pinned ? 0 : gravity[a]);
+                double u[3];
+                if (!pinned && andersen(sys, (uint32_t)i, clock, sp, x, u)) {
+                    const double m = sys.masses[sp];
+                    double de;
+                    if (d == 2) {
+                        const double b0 = sys.velocity(v[0]), b1 = sys.velocity(v[1]);
+                        v[0] = wadd(sys.to_step_displacement(u[0]), drift);
+                        v[1] = sys.to_step_displacement(u[1]);
+                        const double a0 = sys.velocity(v[0]), a1 = sys.velocity(v[1]);
+                        de = 0.5 * m * (a0 * a0 + a1 * a1 - b0 * b0 - b1 * b1);
+                    } else {
+                        double before = 0.0, after = 0.0;
+                        for (int a = 0; a < 3; a++) {
+                            const double b = sys.velocity(v[a]);
+                            before += b * b;
+                        }
+                        for (int a = 0; a < 3; a++) v[a] = sys.to_step_displacement(u[a]);
+                        for (int a = 0; a < 3; a++) {
+                            const double b = sys.velocity(v[a]);
+                            after += b * b;
+                        }
+                        de = 0.5 * m * (after - before);
+                    }
+                    ledger.energy += de;
+                    ledger.energy_fixed += ledger_fixed(de);
+                    ledger.hits += 1;
                 }
+                for (int a = 0; a < d; a++) x[a] = wrap(x[a] + (int64_t)v[a], sys.box[a]);
             }
             steps += 1;
             clock += 1;

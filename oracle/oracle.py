@@ -58,6 +58,8 @@ _SIGS = [
     ("oracle_engine_state", None, [VP, I64P, I32P, U32P]),
     ("oracle_engine_set_state", None, [VP, I64P, I32P, U32P]),
     ("oracle_engine_hash", C.c_uint64, [VP]),
+    ("oracle_engine_ledger", None, [VP, DP, I64P, U64P, U32P]),
+    ("oracle_engine_set_system", None, [VP, SYS]),
     ("oracle_engine_steps", C.c_int64, [VP]),
     ("oracle_engine_energy", None, [VP, DP, DP]),
     ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
@@ -327,6 +329,20 @@ class IntEngine:
 
     def hash(self):
         return lib().oracle_engine_hash(self._h)
+
+    def update_system(self, sys):
+        """A run-time change of system (GpuEngine::update_system): the state, step counter,
+        clock and ledger carry on."""
+        self.sys = sys
+        self._c = sys.to_c()
+        lib().oracle_engine_set_system(self._h, C.byref(self._c))
+
+    def ledger(self):
+        """The bath's ledger slot and the clock: (energy summed in f64 in particle order, the
+        same events rounded to 2^-24 and summed as integers (in 2^-24 units), hits, clock)."""
+        e, ef, h, c = C.c_double(), C.c_int64(), C.c_uint64(), C.c_uint32()
+        lib().oracle_engine_ledger(self._h, C.byref(e), C.byref(ef), C.byref(h), C.byref(c))
+        return e.value, ef.value, h.value, c.value
 
     @property
     def steps(self):

@@ -38,7 +38,8 @@ def test_python_signatures_cover_the_header():
 def test_struct_layouts_match_the_header():
     # sizes follow from the header's field order on LP64 (no packing pragmas)
     assert C.sizeof(_abi.gbmd_pair) == 24
-    assert C.sizeof(_abi.gbmd_system) == 4 + 4 + 24 + 8 + 32 + 16 * 24 + 24 + 8 + 4 + 4
+    # ... + the heat bath: four u32 (bath, species, axis, pad), t, rate, drift, region[2]
+    assert C.sizeof(_abi.gbmd_system) == 4 + 4 + 24 + 8 + 32 + 16 * 24 + 24 + 8 + 4 + 4 + 16 + 24 + 16
     assert C.sizeof(_abi.gbmd_options) == 48
     assert C.sizeof(_abi.gbmd_frame) == 64
 

@@ -518,6 +518,129 @@ def test_rdf_with_cells_wider_than_the_f32_offsets(O):
     assert np.array_equal(prof, O.profile(sys_, st, 10000, 0))  # more bins than shared memory holds
 
 
+# ---------------------------------------------------------------- the Andersen heat bath
+def _same_ledger(g, c):
+    """The bath's ledger slot against the oracle's: redraws exactly, the energy exactly as the
+    sum of the events rounded to 2^-24, and close to IntEngine's own f64 sum in particle order."""
+    e, imp, h = g.read_ledger()
+    oe, oef, oh, oclock = c.ledger()
+    B = _abi.LEDGER_BATH
+    assert h[B] == oh and oh > 0
+    assert e[B] == oef / 2**24
+    assert abs(e[B] - oe) <= oh * 2.0**-24 + 1e-12 * abs(oe) + 1e-9
+    assert all(x == 0 for k, x in enumerate(h) if k != B) and not any(imp)
+    return oclock
+
+
+@pytest.mark.parametrize("mode,arith", [("verlet", _abi.ARITH_F32), ("cells", _abi.ARITH_F32), ("verlet", _abi.ARITH_INT)])
+def test_bath_matches_oracle(O, mode, arith):
+    """walls::andersen after the kick (int_engine.rs:275-293): the redraws, keyed on (id, clock),
+    give the oracle's trajectory bit for bit across graph blocks, single steps and list rebuilds."""
+    sys_, s0 = fluid(O, 3000, 0.6, Pair.lj(2.5), 21, t=2.0)
+    sys_.with_thermostat(0.8, 4.0)
+    m = ForceMode.verlet_with_skin(sys_, 3000, 0.3) if mode == "verlet" else ForceMode.cell_list()
+    c = O.IntEngine(sys_, s0, integer=arith == _abi.ARITH_INT)
+    with GpuEngine(sys_, s0, m, arith=arith) as g:
+        for k in (37, 100, 1, 63):
+            g.step(k)
+            c.step(k)
+            assert g.read_state() == c.state, k
+        clock = _same_ledger(g, c)
+        assert clock == 201
+
+
+def test_bath_fan_and_layer_match_oracle(O):
+    """with_fan (species mask, an x range, a drift) and with_bath_layer (a y range), with two
+    species of different mass and a third pinned species the bath must skip."""
+    n = 4000
+    sys_ = System(box_for(n, 0.55, 1.0), 0.005, Pair.lj(2.5), [1.0, 2.0, 1.0]).with_pinned(2)
+    L = sys_.box_f64()
+    st = O.fluid(sys_, n, 1.2, 22)
+    rng = np.random.default_rng(22)
+    st.species[:] = rng.integers(0, 3, n).astype(np.uint32)
+    st.vel[st.species == 2] = 0
+    for build in (lambda s: s.with_thermostat(1.5, 6.0).with_fan(0b011, 0.2 * L[0], 0.6 * L[0], 0.7),
+                  lambda s: s.with_thermostat(0.5, 6.0).with_bath_layer(0.1 * L[1], 0.5 * L[1])):
+        import copy
+
+        sb = build(copy.deepcopy(sys_))
+        c = O.IntEngine(sb, st)
+        with GpuEngine(sb, st, ForceMode.verlet_with_skin(sb, n, 0.3)) as g:
+            for k in (50, 120):
+                g.step(k)
+                c.step(k)
+                assert g.read_state() == c.state
+            _same_ledger(g, c)
+            assert np.array_equal(g.read_state().pos[st.species == 2], st.pos[st.species == 2])
+
+
+def test_bath_3d_matches_oracle(O):
+    """three::andersen (three.rs:247-265): three components, the species mask."""
+    sys3, s0 = liquid3(O, 4000, 0.8442, 0.5)
+    sys3.masses = [1.0, 3.0]
+    sys3.pairs = sys3.pairs * 4
+    s0.species[::3] = 1
+    sys3.with_thermostat(1.2, 5.0)
+    sys3.thermostat.species = 0b10
+    c = O.IntEngine(sys3, s0)
+    with GpuEngine3(sys3, s0, ForceMode.verlet_with_skin(sys3, 4000, 0.3)) as g:
+        for k in (64, 27):
+            g.step(k)
+            c.step(k)
+            assert g.read_state() == c.state
+        _same_ledger(g, c)
+
+
+def test_bath_added_at_run_time_and_resumed_from_a_snapshot(O):
+    """update_system adds the bath mid-run (the clock counts every step since creation); a
+    snapshot taken later resumes in a fresh engine with the same clock and the same draws."""
+    import copy
+
+    sys_, s0 = fluid(O, 3000, 0.6, Pair.lj(2.5), 23, t=1.5)
+    c = O.IntEngine(sys_, s0)
+    hot = copy.deepcopy(sys_).with_thermostat(0.6, 5.0)
+    with GpuEngine(sys_, s0, ForceMode.verlet_with_skin(sys_, 3000, 0.3)) as g:
+        g.step(40)
+        c.step(40)
+        g.update_system(hot)
+        c.update_system(hot)
+        g.step(70)
+        c.step(70)
+        assert g.read_state() == c.state
+        snap = g.snapshot()
+    with GpuEngine(hot, s0, ForceMode.verlet_with_skin(hot, 3000, 0.3)) as h:
+        h.restore(snap)
+        h.step(90)
+        c.step(90)
+        assert h.read_state() == c.state
+
+
+def test_bath_thermalises():
+    """md/tests/boundaries.rs:189-202: from T = 2, a bath at T = 0.8 (rate 1) holds the
+    half-step temperature within 0.04 of 0.8 over steps 3000-5000."""
+    n = 5000
+    sys_ = System(box_for(n, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0]).with_thermostat(0.8, 1.0)
+    s0 = init_state(sys_, _abi.INIT_FLUID, n, 2.0, 12, 0.1)
+    with GpuEngine(sys_, s0) as g:
+        g.step(3000)
+        t = 0.0
+        for _ in range(20):
+            g.step(100)
+            st = g.read_state()
+            v = st.vel.astype(np.float64) / 2**32 / sys_.dt
+            t += 0.5 * (v * v).sum() / n / 20
+    assert abs(t - 0.8) < 0.04, t
+
+
+def test_batch_refuses_a_bath(O):
+    from micrographia_gb300 import BatchEngine
+
+    sys_, s0 = fluid(O, 500, 0.6, Pair.lj(2.5), 24)
+    sys_.with_thermostat(1.0, 1.0)
+    with pytest.raises(_abi.GbmdError):
+        BatchEngine([sys_], [s0], ForceMode.verlet_with_skin(None, 0, 0.3))
+
+
 # ---------------------------------------------------------------- checkpoint / resume
 @pytest.mark.parametrize("dim", [2, 3])
 def test_snapshot_resume_is_bit_identical(O, dim):

@@ -325,3 +325,68 @@ def test_to_step_displacement_rounds_like_rust(O):
     assert [O.to_step_displacement(s, v) for v in (0.5, -0.5, 1.5, -2.5, 0.49999999999999994)] == [1, -1, 2, -3, 0]
     assert O.to_step_displacement(s, 3e9) == 2**31 - 1 and O.to_step_displacement(s, -3e9) == -(2**31)
     assert O.to_step_displacement(s, float("nan")) == 0
+
+
+def _andersen_py(sys_, i, clock, s, p, dim):
+    """walls::andersen (walls.rs:113-133) / three::andersen (three.rs:247-265) restated in Python
+    (math.log/cos/sin are the platform libm, as Rust's f64 methods are): the new velocity in
+    sigma/tau, or None."""
+    from micrographia_gb300.workloads import threefry2x32
+
+    th = sys_.thermostat
+    if not (th.species >> s) & 1 or (dim == 2 and not th.region[0] <= p[th.axis] < th.region[1]):
+        return None
+    if dim == 3 and (sys_.pinned >> s) & 1:
+        return None
+    k0, k1 = sys_.seed & 0xFFFFFFFF, ((sys_.seed >> 32) ^ 0x5448524D) & 0xFFFFFFFF
+    unit = lambda w: ((w << 21) & ((1 << 53) - 1)) * (1.0 / (1 << 53))
+    r = threefry2x32(i, clock, k0, k1)
+    if unit(r[0]) >= th.rate * sys_.dt:
+        return None
+    r2 = threefry2x32(i, clock, k0, k1 ^ 1)
+    sd = math.sqrt(th.t / sys_.masses[s])
+    rad = math.sqrt(-2.0 * math.log(1.0 - unit(r[1])))
+    a = 2.0 * math.pi * unit(r2[0])
+    out = [sd * rad * math.cos(a), sd * rad * math.sin(a)]
+    if dim == 3:
+        r3 = threefry2x32(i, clock, k0, k1 ^ 2)
+        out.append(sd * math.sqrt(-2.0 * math.log(1.0 - unit(r3[0]))) * math.cos(2.0 * math.pi * unit(r3[1])))
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_bath_draws_match_a_python_restatement(O, dim):
+    """Particles too far apart to interact: after each step a particle's velocity is its bath
+    draw for (id, clock) (plus the fan's drift in 2D) or unchanged; the oracle's C++ bath equals
+    an independent Python restatement of the reference's, draw for draw."""
+    from micrographia_gb300 import State, State3, System3 as S3
+
+    n, L = 6, 60.0
+    box = [int(L * ONE)] * dim
+    if dim == 2:
+        sys_ = System(box, 0.005, Pair.lj(2.5), [1.0, 2.5]).with_thermostat(0.9, 120.0).with_fan(0b11, 0.0, 45.0, 0.25)
+    else:
+        sys_ = S3(box, 0.005, Pair.lj(2.5), [1.0, 2.5]).with_thermostat(0.9, 120.0)
+    sys_.seed = 0x1234_5678_9ABC
+    pos = np.array([[(10 * k + 3) * ONE] * dim for k in range(n)], np.int64)
+    sp = np.array([k % 2 for k in range(n)], np.uint32)
+    st = (State if dim == 2 else State3)(pos, np.zeros((n, dim), np.int32), sp)
+    c = O.IntEngine(sys_, st)
+    drift = sys_.to_step_displacement(0.25) if dim == 2 else 0
+    hits = 0
+    for clock in range(40):
+        before = c.state
+        c.step(1)
+        after = c.state
+        for i in range(n):
+            u = _andersen_py(sys_, i, clock, int(sp[i]), before.pos[i], dim)
+            if u is None:
+                assert list(after.vel[i]) == list(before.vel[i])
+            else:
+                want = [sys_.to_step_displacement(x) for x in u]
+                if dim == 2:
+                    want[0] = (want[0] + drift + 2**31) % 2**32 - 2**31
+                assert list(after.vel[i]) == want, (clock, i)
+                hits += 1
+    assert hits > 40 * n // 4  # rate dt = 0.6; in 2D the fan's x range holds 5 of the 6
+    assert c.ledger()[2] == hits and c.ledger()[3] == 40
