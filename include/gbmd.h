@@ -328,6 +328,8 @@ int gbmd_batch_read_system(gbmd_batch* b, uint32_t k, int64_t* pos, int32_t* vel
 int gbmd_batch_stream(gbmd_batch* b, void** stream);
 /* Kernel launches of the batch so far (graph nodes included) and its list rebuilds. */
 int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds);
+/* System k's ledger, as gbmd_read_ledger: its heat bath's slot (each system keeps its own). */
+int gbmd_batch_read_ledger(gbmd_batch* b, uint32_t k, double* energy, double* impulse, uint64_t* hits);
 /* The batch's Verlet skin in sigma (the one GBMD_FLAG_TUNE_SKIN chose, or the one asked for). */
 int gbmd_batch_skin(gbmd_batch* b, double* skin);
 int gbmd_batch_destroy(gbmd_batch* b);

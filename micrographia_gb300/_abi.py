@@ -216,6 +216,7 @@ SIGNATURES = [
     ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
     ("gbmd_batch_stats", C.c_int, [VP, _U64P, _U32P]),
     ("gbmd_batch_skin", C.c_int, [VP, C.POINTER(C.c_double)]),
+    ("gbmd_batch_read_ledger", C.c_int, [VP, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double), _U64P]),
     ("gbmd_read_ledger", C.c_int, [VP, C.POINTER(C.c_double), C.POINTER(C.c_double), _U64P]),
     ("gbmd_batch_destroy", C.c_int, [VP]),
     ("gbmd_serve_create", C.c_int, [C.c_uint64, C.c_uint32, C.c_int32, P(VP)]),

@@ -284,6 +284,48 @@ __global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, uint32_t cap, c
     }
 }
 
+// The Andersen bath of each system that has one, after the batch's force step: the single-system
+// pass (k_bath) with the system's own parameters, its particles' ids counted from the system's
+// first, the batch's step clock (every system of a batch has taken the same steps), and the
+// system's own ledger slot.
+template <int D>
+__global__ void k_bbath(uint32_t N, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx, PosRec<D>* __restrict__ pos,
+                        uint4* __restrict__ qpos, int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
+                        const uint32_t* __restrict__ ids, const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl,
+                        unsigned long long* __restrict__ ledger) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t k = sysidx[i];
+    const Params& P = tab[k];
+    if (!P.bath) return;
+    const uint32_t si = species[i];
+    if (((P.pinned >> si) & 1u) || !((P.bath_species >> si) & 1u)) return;
+    int64_t x[3];
+    load_particle<D, false>(pos, nullptr, i, x);
+    int32_t v[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
+    if (D == 2) {
+        const uint32_t ax = P.bath_axis;
+        const int64_t p = wrap(x[ax] - (int64_t)v[ax], P.box[ax]);
+        if (!(p >= P.bath_region[0] && p < P.bath_region[1])) return;
+    }
+    const BathDraw o = bath_draw<D>(ids[i] - P.id_base, ctl[CTL_CLOCK], P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si],
+                                    P.masses[si], P.dt, P.bath_drift, v[0], v[1], v[2], ledger + 2 * k);
+    if (!o.hit) return;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        x[a] += (int64_t)o.v[a] - (int64_t)v[a];
+        vel[D * i + a] = o.v[a];
+    }
+    store_pos<D>(pos, i, x, si);
+    qpos[i] = quot_record<D>(x, si);
+    int64_t xr[3];
+    load_particle<D, false>(ref_pos, nullptr, i, xr);
+    if (moved_half_skin<D>(geom_of(P), xr, x)) ctl[0] = 1;
+}
+__global__ void k_bclock_tick(uint32_t* ctl) { ctl[CTL_CLOCK] += 1u; }
+
 template <int D>
 __global__ void k_bfrom_host(uint32_t N, const int64_t* ipos, const int32_t* ivel, const uint32_t* ispecies, const uint32_t* isys,
                              PosRec<D>* pos, int32_t* vel, uint32_t* species, uint32_t* ids, uint32_t* sysidx) {
@@ -351,6 +393,8 @@ struct gbmd_batch {
     int cur = 0, sorted = 0;
     uint32_t block_steps = 100;
     double skin = 0.4;
+    bool bath = false;                   // some system has an Andersen bath
+    unsigned long long* ledger = nullptr; // per system: [2k] bath energy (2^-24 epsilon), [2k + 1] redraws
     cudaGraphExec_t exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     uint64_t exec_launches[2][2] = {{0, 0}, {0, 0}};
     uint64_t body_launches = 0, launches = 0;
@@ -371,7 +415,7 @@ void bfree(gbmd_batch* b) {
             if (b->exec[p][k]) cudaGraphExecDestroy(b->exec[p][k]);
     void* ptrs[] = {b->tab, b->pos[0], b->pos[1], b->pos_scr, b->ref_pos, b->vel, b->vel_scr, b->species, b->species_scr, b->ids, b->ids_scr,
                     b->sysidx, b->sysidx_scr, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->scan_tmp, b->start, b->nbr,
-                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1], b->relf};
+                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1], b->relf, b->ledger};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->st) cudaStreamDestroy(b->st);
@@ -408,6 +452,12 @@ template <int D, bool MULTI> void benqueue_force_t(gbmd_batch* b, cudaStream_t s
                                                                b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
     note_launch();
     b->cur ^= 1;
+    if (b->bath) {
+        k_bbath<D><<<nblocks(b->N, 256), 256, 0, s>>>(b->N, b->tab, b->sysidx, (PosRec<D>*)b->pos[b->cur], b->qpos[b->cur], b->vel, b->species,
+                                                      b->ids, (const PosRec<D>*)b->ref_pos, b->ctl, b->ledger);
+        k_bclock_tick<<<1, 1, 0, s>>>(b->ctl);
+        note_launch(2);
+    }
 }
 void benqueue_force(gbmd_batch* b, cudaStream_t s) {
     if (b->D == 2) b->multi ? benqueue_force_t<2, true>(b, s) : benqueue_force_t<2, false>(b, s);
@@ -550,7 +600,6 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
         GBMD_TRY(validate_system(systems[k], offsets[k + 1] - offsets[k]));
         if (systems[k].dim != D) return fail(GBMD_E_INVALID, "a batch holds systems of one dimension");
         if (offsets[k + 1] <= offsets[k]) return fail(GBMD_E_INVALID, "every system needs at least one particle");
-        if (systems[k].bath) return fail(GBMD_E_UNSUPPORTED, "batches run systems without a heat bath (one engine per system runs it)");
     }
     if (offsets[0] != 0) return fail(GBMD_E_INVALID, "offsets[0] must be 0");
     if (o.flags & GBMD_FLAG_TUNE_SKIN) GBMD_TRY(tune_skin(systems, count, offsets, pos, vel, species, o));
@@ -583,6 +632,8 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
         b->cap = std::max(b->cap, cap);
         fill_params(b->P[k], s, nk, skin, cap, nc);
         b->P[k].cell_base = (uint32_t)cell_base;
+        b->P[k].id_base = offsets[k];
+        if (s.bath) b->bath = true;
         cell_base += b->P[k].ncell;
         if (cell_base >= UINT32_MAX) {
             delete b;
@@ -644,6 +695,8 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     step(balloc(&b->qpos[1], N));
     step(balloc(&b->nbr_count, N));
     step(balloc(&b->ctl, 16));
+    step(balloc(&b->ledger, 2 * (size_t)count));
+    if (r == GBMD_OK) cudaMemsetAsync(b->ledger, 0, 16 * (size_t)count, b->st);
     step(balloc((char**)&b->staging, N * D * 8));
     step(balloc(&b->staging_v, N * D));
     step(balloc(&b->staging_s, N));
@@ -739,6 +792,19 @@ int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds) {
     GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
     if (rebuilds) *rebuilds = c[2];
     if (launches) *launches = b->launches + (uint64_t)c[2] * b->body_launches;
+    return GBMD_OK;
+}
+
+int gbmd_batch_read_ledger(gbmd_batch* b, uint32_t k, double* energy, double* impulse, uint64_t* hits) {
+    if (!b || k >= b->K) return fail(GBMD_E_INVALID, "bad batch or system index");
+    unsigned long long l[2];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(l, b->ledger + 2 * (size_t)k, 16, cudaMemcpyDeviceToHost, b->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
+    for (int w = 0; w < GBMD_LEDGER_SLOTS; w++) {
+        if (energy) energy[w] = w == GBMD_LEDGER_BATH ? (double)(long long)l[0] * (1.0 / 16777216.0) : 0.0;
+        if (impulse) impulse[w] = 0.0;
+        if (hits) hits[w] = w == GBMD_LEDGER_BATH ? (uint64_t)l[1] : 0;
+    }
     return GBMD_OK;
 }
 

@@ -362,6 +362,14 @@ class BatchEngine:
         _abi.check(self._lib.gbmd_batch_skin(self._h, C.byref(v)))
         return v.value
 
+    def read_ledger(self, k):
+        """System k's ledger (energy, impulse, hits per slot), as GpuEngine.read_ledger."""
+        e = (C.c_double * _abi.LEDGER_SLOTS)()
+        p = (C.c_double * _abi.LEDGER_SLOTS)()
+        h = (C.c_uint64 * _abi.LEDGER_SLOTS)()
+        _abi.check(self._lib.gbmd_batch_read_ledger(self._h, k, e, p, h))
+        return list(e), list(p), list(h)
+
     def wait(self):
         _abi.check(self._lib.gbmd_batch_sync(self._h))
 

@@ -1046,7 +1046,7 @@ template <typename F> struct IntEngine {
                 int32_t* v = &state.vel[d * i];
                 int64_t* x = &state.pos[d * i];
                 for (int a = 0; a < d; a++) v[a] = wadd(wadd(v[a], kicks[d * i + a]), pinned ? 0 : gravity[a]);
-                double u[3];
+                double u[3] = {0.0, 0.0, 0.0};
                 if (!pinned && andersen(sys, (uint32_t)i, clock, sp, x, u)) {
                     const double m = sys.masses[sp];
                     double de;

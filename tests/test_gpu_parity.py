@@ -632,13 +632,30 @@ def test_bath_thermalises():
     assert abs(t - 0.8) < 0.04, t
 
 
-def test_batch_refuses_a_bath(O):
-    from micrographia_gb300 import BatchEngine
+def test_batch_bath_matches_each_plain_run(O):
+    """Baths in a batch: systems with and without one, each equal to its own IntEngine run
+    (ids counted from the system's first particle, the batch's clock), each with its own ledger."""
+    from micrographia_gb300 import BatchEngine, workloads
 
-    sys_, s0 = fluid(O, 500, 0.6, Pair.lj(2.5), 24)
-    sys_.with_thermostat(1.0, 1.0)
-    with pytest.raises(_abi.GbmdError):
-        BatchEngine([sys_], [s0], ForceMode.verlet_with_skin(None, 0, 0.3))
+    cfg = workloads.config4(count=6, base_seed=31, n_min=600, n_max=3000)
+    systems = [s for s, _ in cfg]
+    for k, sys_ in enumerate(systems):
+        if k % 3 != 1:
+            sys_.with_thermostat(0.6 + 0.2 * k, 3.0 + k)
+        if k == 2:
+            L = sys_.box_f64()
+            sys_.with_fan(0b1, 0.1 * L[0], 0.7 * L[0], 0.4)
+    states = [O.init(s, spec) for s, spec in cfg]
+    with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3)) as b:
+        b.step(130)
+        for k, (sys_, st) in enumerate(zip(systems, states)):
+            c = O.IntEngine(sys_, st)
+            c.step(130)
+            assert b.read_system(k) == c.state, k
+            e, _, h = b.read_ledger(k)
+            oe, oef, oh, _ = c.ledger()
+            assert h[_abi.LEDGER_BATH] == oh and e[_abi.LEDGER_BATH] == oef / 2**24, k
+            assert (oh > 0) == (sys_.thermostat is not None)
 
 
 # ---------------------------------------------------------------- checkpoint / resume
