@@ -947,6 +947,24 @@ def test_served_results_equal_solo_runs():
         assert last[rid].state_hash == h
 
 
+def test_served_bath_requests_equal_the_oracle(O):
+    """Requests whose systems carry a heat bath: the served final state equals IntEngine's run
+    of the same system (the bath keyed on each request's own ids and step clock)."""
+    from micrographia_gb300 import Server, workloads
+
+    cfg = workloads.config5(count=4, rate=1e9, base_seed=17, n_min=800, n_max=3000)
+    for k, (_, s, _) in enumerate(cfg):
+        s.with_thermostat(0.7 + 0.3 * k, 2.0 + k)
+    with Server(hbm_budget_bytes=4 << 30, max_active=2) as sv:
+        ids = [sv.submit(s, spec, steps=200, frame_every=100, rdf_bins=0) for _, s, spec in cfg]
+        _, last = _drain(sv, len(ids))
+    for rid, (_, s, spec) in zip(ids, cfg):
+        c = O.IntEngine(s, O.init(s, spec))
+        c.step(200)
+        assert last[rid].state_hash == c.hash()
+        assert c.ledger()[2] > 0
+
+
 def test_server_budget_and_cancel():
     from micrographia_gb300 import Server, _abi, workloads
 
