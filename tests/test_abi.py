@@ -100,3 +100,40 @@ def test_header_constants_match_the_python_mirror():
     assert "#define GBMD_FLAG_FORCE_LANES(s) ((uint32_t)(s) << 8)" in text and _abi.force_lanes_flag(16) == 16 << 8
     with pytest.raises(ValueError):
         _abi.force_lanes_flag(3)
+
+
+def test_heat_bath_builders_and_validation(engine_lib):
+    """The Andersen bath's host side: md-core's builders (with_thermostat keeps a fan's species,
+    region and drift; with_fan / with_bath_layer need a thermostat first), the C struct fields,
+    and gbmd_create refusing a bad bath before any device work (runs without a GPU)."""
+    from micrographia_gb300 import ONE, Pair, System, System3, box_for, cube_for
+
+    s = System(box_for(200, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 2.0])
+    with pytest.raises(ValueError):
+        s.with_fan(0b1, 1.0, 2.0, 0.1)
+    s.with_thermostat(0.8, 1.0).with_fan(0b10, 1.5, 4.5, 0.3).with_thermostat(1.1, 2.0)
+    th = s.thermostat
+    assert (th.t, th.rate, th.species, th.axis, th.drift) == (1.1, 2.0, 0b10, 0, 0.3)
+    assert th.region == (int(1.5 * ONE), int(4.5 * ONE))
+    c = s.to_c()
+    assert (c.bath, c.bath_species, c.bath_axis, c.bath_t, c.bath_rate, c.bath_drift) == (1, 0b10, 0, 1.1, 2.0, 0.3)
+    assert list(c.bath_region) == [int(1.5 * ONE), int(4.5 * ONE)]
+    s.with_bath_layer(0.0, 3.0)
+    assert s.thermostat.axis == 1 and s.thermostat.acts_on(1, [0, 2 * ONE]) and not s.thermostat.acts_on(0, [0, 2 * ONE])
+    s3 = System3(cube_for(300, 0.8), 0.005, Pair.lj(2.5), [1.0]).with_thermostat(1.0, 1.0)
+    c3 = s3.to_c()
+    assert c3.bath == 1 and c3.bath_species == 0xFFFFFFFF and list(c3.bath_region) == [-(1 << 63), (1 << 63) - 1]
+    assert System(box_for(200, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0]).to_c().bath == 0
+
+    n = 4
+    pos = np.zeros((n, 2), np.int64)
+    vel = np.zeros((n, 2), np.int32)
+    sp = np.zeros(n, np.uint32)
+    P = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+    for field, value in (("bath_rate", -1.0), ("bath_t", float("nan")), ("bath_axis", 2), ("bath_drift", float("inf"))):
+        bad = System(box_for(200, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0]).with_thermostat(1.0, 1.0).to_c()
+        setattr(bad, field, value)
+        h = C.c_void_p()
+        rc = engine_lib.gbmd_create(C.byref(bad), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
+        assert rc == _abi.E_INVALID, field
+        assert b"bath" in engine_lib.gbmd_last_error(), field
