@@ -2,8 +2,10 @@
 
 Their methods mirror md::GpuEngine (crates/md/src/engine.rs:598-1098) and md::GpuEngine3
 (engine3.rs:334-648): construction from (System, State) with a ForceMode, asynchronous `step`,
-`reverse`, `kicks`, `read_state` (id order), `upload`, `flip_bit`, `read_list_stats`, plus the
-CPU twins' `energy` (int_engine.rs:433-446) and the new FP64 instruments (`observe`).
+`reverse`, `kicks`, `read_state` (id order), `upload`, `flip_bit`, `read_list_stats`,
+`read_ledger`, the page commands (`kick_region`, `set_species`, `set_species_velocity`,
+`sort_now`) and `update_system`, plus the CPU twins' `energy` (int_engine.rs:433-446) and the new
+FP64 instruments (`observe`).
 """
 
 import ctypes as C
