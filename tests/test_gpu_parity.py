@@ -850,6 +850,26 @@ def test_config2_full_size_properties(O):
         assert g.read_state().hash() == s0.hash()
 
 
+def test_slab_full_size_properties():
+    """2D liquid-vapour slab, N = 2^24 (4:1 box, liquid 0.70, vapour 0.05), skin 0.3, NVE: the
+    velocity sum stays exactly zero, the lists never overflow, and 60 steps reverse bit for bit
+    (the state hash of the initial state is recovered)."""
+    from micrographia_gb300 import workloads
+
+    sys_, spec = workloads.config3(1 << 24)
+    n = spec.n
+    with GpuEngine(sys_, None, ForceMode.verlet_with_skin(sys_, n, 0.3), init=spec) as g:
+        h0 = g.state_hash()
+        g.step(60)
+        assert g.read_state().velocity_sum() == [0, 0]
+        rebuilds, overflow = g.read_list_stats()
+        assert not overflow and rebuilds >= 1
+        g.reverse()
+        g.step(60)
+        g.reverse()
+        assert g.state_hash() == h0
+
+
 # ---------------------------------------------------------------- batched replicas
 def test_batch_replicas_match_their_plain_runs(O):
     """Uneven 2D systems stepped in one batch: each replica's state equals md-ref's IntEngine<f32>
