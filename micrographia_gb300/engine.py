@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from .core import ForceMode, State, State3, System, System3
+from .core import ForceMode, State, State3
 
 P = C.POINTER
 

@@ -2,7 +2,6 @@
 declares (no compute calls: those need a device)."""
 
 import ctypes as C
-import os
 import re
 
 import numpy as np
