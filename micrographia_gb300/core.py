@@ -147,6 +147,15 @@ class _SystemBase:
     def pair(self, a, b):
         return self.pairs[a * self.species() + b]
 
+    def periodic(self, axis):
+        """System::periodic (system.rs:384-386): every axis of this engine's systems is."""
+        return 0 <= axis < self.DIM
+
+    def deterministic(self):
+        """System::deterministic (system.rs:388-391): nothing stochastic happens (no heat bath),
+        so the dynamics is exactly reversible."""
+        return self.thermostat is None
+
     def rc_max(self):
         return max(p.rc for p in self.pairs)
 

@@ -122,7 +122,9 @@ def test_heat_bath_builders_and_validation(engine_lib):
     s3 = System3(cube_for(300, 0.8), 0.005, Pair.lj(2.5), [1.0]).with_thermostat(1.0, 1.0)
     c3 = s3.to_c()
     assert c3.bath == 1 and c3.bath_species == 0xFFFFFFFF and list(c3.bath_region) == [-(1 << 63), (1 << 63) - 1]
-    assert System(box_for(200, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0]).to_c().bath == 0
+    plain = System(box_for(200, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    assert plain.to_c().bath == 0 and plain.deterministic() and not s.deterministic() and not s3.deterministic()
+    assert plain.periodic(0) and plain.periodic(1) and not plain.periodic(2) and s3.periodic(2)
 
     n = 4
     pos = np.zeros((n, 2), np.int64)
