@@ -98,7 +98,18 @@ typedef struct gbmd_system {
     double bath_rate;       /* redraws per particle per tau */
     double bath_drift;      /* 2D: mean x velocity of redrawn particles, sigma/tau */
     int64_t bath_region[2]; /* 2D: [lo, hi) along bath_axis in position units (all: INT64_MIN, INT64_MAX) */
+    /* Walls on the axes whose `periodic` bit is clear (md_core::Wall, walls.rs; with_walls,
+     * system.rs:209-212): wall_kind[axis][side] (side 0 at 0, 1 at L) is a GBMD_WALL_* kind,
+     * wall_t[axis][side] a thermal wall's kT. The GPU engine runs periodic systems only
+     * (GBMD_E_UNSUPPORTED otherwise); the fields carry the reference's System whole. */
+    uint32_t wall_kind[3][2];
+    double wall_t[3][2];
 } gbmd_system;
+
+/* gbmd_system.wall_kind: md_core::Wall (walls.rs). */
+#define GBMD_WALL_HARD 1    /* exact mirror, v -> -v */
+#define GBMD_WALL_SOFT 2    /* WCA repulsion in the distance to the wall (walls.rs:103-111) */
+#define GBMD_WALL_THERMAL 3 /* a hit draws a Maxwell-flux velocity at wall_t (walls.rs:89-101) */
 
 /* Engine options: ForceMode + Arith + the engine's own tuning knobs. Zero-initialised is valid. */
 /* gbmd_options.flags */

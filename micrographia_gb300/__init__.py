@@ -22,6 +22,7 @@ from .core import (
     System,
     System3,
     Thermostat,
+    Wall,
     box_for,
     cube_for,
     fcc_cells,
@@ -41,6 +42,7 @@ __all__ = [
     "System",
     "System3",
     "Thermostat",
+    "Wall",
     "GpuEngine",
     "GpuEngine3",
     "BatchEngine",

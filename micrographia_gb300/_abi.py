@@ -58,7 +58,14 @@ class gbmd_system(C.Structure):
         ("bath_rate", C.c_double),
         ("bath_drift", C.c_double),
         ("bath_region", C.c_int64 * 2),
+        ("wall_kind", (C.c_uint32 * 2) * 3),
+        ("wall_t", (C.c_double * 2) * 3),
     ]
+
+
+WALL_HARD = 1  # md_core::Wall::Hard: exact mirror
+WALL_SOFT = 2  # Wall::Soft: WCA repulsion from the wall
+WALL_THERMAL = 3  # Wall::Thermal(t): a hit draws a Maxwell-flux velocity at kT = t
 
 
 LEDGER_SLOTS = 7  # md_core::walls::WALLS: 2 axis + side, membrane faces 4 and 5, the bath

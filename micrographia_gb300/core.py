@@ -111,6 +111,7 @@ class _SystemBase:
         self.seed = 1
         self.pinned = 0
         self.thermostat = None
+        self.walls = [None] * self.DIM
 
     def species(self):
         return len(self.masses)
@@ -147,14 +148,23 @@ class _SystemBase:
     def pair(self, a, b):
         return self.pairs[a * self.species() + b]
 
+    def with_walls(self, axis, lo, hi):
+        """System::with_walls (system.rs:209-212): walls at 0 and L on `axis` (Wall values)."""
+        self.walls[axis] = (lo, hi)
+        return self
+
     def periodic(self, axis):
-        """System::periodic (system.rs:384-386): every axis of this engine's systems is."""
-        return 0 <= axis < self.DIM
+        """System::periodic (system.rs:384-386): no walls on the axis."""
+        return 0 <= axis < self.DIM and self.walls[axis] is None
 
     def deterministic(self):
-        """System::deterministic (system.rs:388-391): nothing stochastic happens (no heat bath),
-        so the dynamics is exactly reversible."""
-        return self.thermostat is None
+        """System::deterministic (system.rs:388-391): no heat bath and no thermal wall, so the
+        dynamics is exactly reversible."""
+        return self.thermostat is None and not any(w.kind == _abi.WALL_THERMAL for ws in self.walls if ws for w in ws)
+
+    def has_soft_walls(self):
+        """System::has_soft_walls (system.rs:393-395)."""
+        return any(w.kind == _abi.WALL_SOFT for ws in self.walls if ws for w in ws)
 
     def rc_max(self):
         return max(p.rc for p in self.pairs)
@@ -204,7 +214,11 @@ class _SystemBase:
         for a in range(self.DIM):
             s.gravity[a] = self.gravity[a]
         s.seed = self.seed
-        s.periodic = (1 << self.DIM) - 1
+        s.periodic = sum(1 << a for a in range(self.DIM) if self.walls[a] is None)
+        for a, ws in enumerate(self.walls):
+            for side, w in enumerate(ws or ()):
+                s.wall_kind[a][side] = w.kind
+                s.wall_t[a][side] = w.t
         s.pinned = self.pinned
         th = self.thermostat
         if th is not None:
@@ -214,6 +228,31 @@ class _SystemBase:
             s.bath_t, s.bath_rate, s.bath_drift = th.t, th.rate, th.drift
             s.bath_region[0], s.bath_region[1] = th.region
         return s
+
+
+class Wall:
+    """md_core::Wall (walls.rs): Wall.hard(), Wall.soft(), Wall.thermal(t)."""
+
+    def __init__(self, kind, t=0.0):
+        self.kind, self.t = int(kind), float(t)
+
+    @classmethod
+    def hard(cls):
+        return cls(_abi.WALL_HARD)
+
+    @classmethod
+    def soft(cls):
+        return cls(_abi.WALL_SOFT)
+
+    @classmethod
+    def thermal(cls, t):
+        return cls(_abi.WALL_THERMAL, t)
+
+    def __eq__(self, o):
+        return isinstance(o, Wall) and (self.kind, self.t) == (o.kind, o.t)
+
+    def __repr__(self):
+        return {1: "Wall.hard()", 2: "Wall.soft()"}.get(self.kind, f"Wall.thermal({self.t})")
 
 
 class Thermostat:

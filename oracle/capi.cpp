@@ -254,11 +254,16 @@ void oracle_engine_set_state(void* h, const int64_t* pos, const int32_t* vel, co
 uint64_t oracle_engine_hash(void* h) { return ((Engine*)h)->state().hash(); }
 void oracle_engine_ledger(void* h, double* energy, int64_t* energy_fixed, uint64_t* hits, uint32_t* clock) {
     Engine* e = (Engine*)h;
-    const BathLedger& l = e->f32 ? e->f32->ledger : e->f64->ledger;
-    *energy = l.energy;
-    *energy_fixed = l.energy_fixed;
-    *hits = l.hits;
+    const Ledger& l = e->f32 ? e->f32->ledger : e->f64->ledger;
+    *energy = l.energy[LEDGER_BATH];
+    *energy_fixed = l.bath_energy_fixed;
+    *hits = l.hits[LEDGER_BATH];
     *clock = e->f32 ? e->f32->clock : e->f64->clock;
+}
+void oracle_engine_wall_ledger(void* h, double* energy, double* impulse, uint64_t* hits) {
+    Engine* e = (Engine*)h;
+    const Ledger& l = e->f32 ? e->f32->ledger : e->f64->ledger;
+    for (int w = 0; w < LEDGER_SLOTS; w++) energy[w] = l.energy[w], impulse[w] = l.impulse[w], hits[w] = l.hits[w];
 }
 void oracle_engine_set_system(void* h, const gbmd_system* csys) {
     Engine* e = (Engine*)h;

@@ -199,6 +199,12 @@ struct System {
     uint64_t seed = 1;
     uint32_t pinned = 0;
     Bath bath;
+    // Walls (md_core::Wall, walls.rs) on the axes whose periodic bit is clear: GBMD_WALL_* per side.
+    uint32_t periodic_bits = 7;
+    std::array<std::array<uint32_t, 2>, 3> wall_kind{};
+    std::array<std::array<double, 2>, 3> wall_t{};
+    bool periodic(int a) const { return (periodic_bits >> a) & 1u; } // system.rs:384-386
+    bool all_periodic() const { return (periodic_bits & ((1u << dim) - 1u)) == ((1u << dim) - 1u); }
 
     static System from_c(const gbmd_system& s) {
         System o;
@@ -211,6 +217,12 @@ struct System {
         for (int a = 0; a < 3; a++) o.gravity[a] = s.gravity[a];
         o.seed = s.seed;
         o.pinned = s.pinned;
+        o.periodic_bits = s.periodic | (s.dim == 2 ? 4u : 0u);
+        for (int a = 0; a < 3; a++)
+            for (int side = 0; side < 2; side++) {
+                o.wall_kind[a][side] = s.wall_kind[a][side];
+                o.wall_t[a][side] = s.wall_t[a][side];
+            }
         if (s.bath) {
             o.bath.on = true;
             o.bath.t = s.bath_t;
@@ -360,11 +372,17 @@ inline std::vector<int32_t> maxwell(const System& sys, const std::vector<uint32_
     zero_velocity_sum(sys, species, vel, d == 3);
     return vel;
 }
-// init.rs:105-121, periodic axes only (no wall margin).
+// init.rs:105-121: on an axis with walls the lattice keeps 1 sigma clear of them.
 inline State fluid(const System& sys, size_t n, double t, uint64_t seed) {
     State s;
     s.dim = 2;
-    s.pos = lattice(n, {sys.box[0], sys.box[1]}, 0.1, seed);
+    const int64_t margin = to_fixed(1.0);
+    int64_t inner[2];
+    for (int a = 0; a < 2; a++) inner[a] = sys.periodic(a) ? sys.box[a] : sys.box[a] - to_fixed(2.0);
+    s.pos = lattice(n, {inner[0], inner[1]}, 0.1, seed);
+    for (size_t i = 0; i < n; i++)
+        for (int a = 0; a < 2; a++)
+            if (!sys.periodic(a)) s.pos[2 * i + a] += margin;
     s.species.assign(n, 0);
     s.vel = maxwell(sys, s.species, t, seed);
     return s;
@@ -900,14 +918,55 @@ inline bool andersen(const System& sys, uint32_t id, uint32_t clock, uint32_t s,
     return true;
 }
 
-// The bath's ledger entry (walls::Ledger slot BATH, walls.rs:40-50): energy summed in f64 in
-// particle order as IntEngine does, the same events rounded to 2^-24 and summed as integers (the
-// order-free total the GPU engine keeps), and the redraw count.
-struct BathLedger {
-    double energy = 0.0;
-    int64_t energy_fixed = 0;
-    uint64_t hits = 0;
+// walls::Ledger (walls.rs:40-50): per slot (2 axis + side for walls, 6 the bath) the energy given
+// to the system and the normal momentum it gave the wall, summed in f64 in particle order as
+// IntEngine does, and the hits; for the bath also the events rounded to 2^-24 and summed as
+// integers (the order-free total the GPU engine keeps).
+constexpr int LEDGER_SLOTS = 7, LEDGER_BATH = 6;
+struct Ledger {
+    double energy[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
+    double impulse[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
+    uint64_t hits[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
+    int64_t bath_energy_fixed = 0;
 };
+
+constexpr uint32_t STREAM_WALL = 0x57414c4cu; // walls.rs:86
+constexpr double SOFT_RC = 1.122462048309373;  // walls.rs:104, 2^(1/6)
+
+// walls::mirror (walls.rs:28-38): a coordinate that left [0, l) mirrored back about -1/2 or
+// l - 1/2 (an exact involution on integers); side 0 or 1, or -1 when inside.
+inline int mirror(int64_t& x, int64_t l) {
+    if (x < 0) {
+        x = -1 - x;
+        return 0;
+    }
+    if (x >= l) {
+        x = 2 * l - 1 - x;
+        return 1;
+    }
+    return -1;
+}
+
+// A thermal wall's new velocity: walls::thermal_velocity (walls.rs:89-101) in 2D, the normal
+// component and one tangential; three::thermal_velocity (three.rs:222-243) in 3D, two tangential.
+inline void thermal_velocity(const System& sys, uint32_t id, uint32_t clock, double t, double m, double inward, double* normal,
+                             double* tang) {
+    const std::array<uint32_t, 2> key{(uint32_t)sys.seed, (uint32_t)(sys.seed >> 32) ^ STREAM_WALL};
+    const auto r = threefry2x32({id, clock}, key);
+    const auto r2 = threefry2x32({id, clock}, {key[0], key[1] ^ 1u});
+    const double u1 = 1.0 - to_unit_f64(r);
+    const double u2 = 1.0 - to_unit_f64({r2[0], 0}), u3 = to_unit_f64({r2[1], 0});
+    const double sd = std::sqrt(t / m);
+    *normal = inward * sd * std::sqrt(-2.0 * std::log(u1));
+    if (sys.dim == 2) {
+        tang[0] = sd * std::sqrt(-2.0 * std::log(u2)) * std::cos(TAU * u3);
+    } else {
+        const double rad = sd * std::sqrt(-2.0 * std::log(u2));
+        const double a = TAU * u3;
+        tang[0] = rad * std::cos(a);
+        tang[1] = rad * std::sin(a);
+    }
+}
 inline int64_t ledger_fixed(double de) { return (int64_t)std::round(de * 16777216.0); }
 
 // md-ref int_engine.rs:23-447 and int_engine3.rs:12-240, for periodic systems with an optional
@@ -922,7 +981,8 @@ template <typename F> struct IntEngine {
     std::array<uint32_t, 3> cells{1, 1, 1};
     int64_t steps = 0;
     uint32_t clock = 0;
-    BathLedger ledger;
+    Ledger ledger;
+    std::vector<std::array<double, 6>> wall_force; // per particle, the soft walls' forces (last forces())
     bool fast = true;
     IntTables* tables = nullptr;
     FastScratch<F> scratch;
@@ -970,7 +1030,9 @@ template <typename F> struct IntEngine {
         kicks.assign(d * n, 0);
         auto cl_dims = present_cells();
         double pe = 0.0;
-        bool use_fast = d == 2 && fast && !tables && fast_eligible(sys, cl_dims);
+        wall_force.assign(n, {0, 0, 0, 0, 0, 0});
+        // (with walls the reference loop: fast.rs gives the same kicks, fast_path.rs:20-54)
+        bool use_fast = d == 2 && fast && !tables && sys.all_periodic() && fast_eligible(sys, cl_dims);
         if (use_fast) return pair_kicks_fast<F>(sys, state, consts, kick_c, cl_dims, scratch, kicks.data());
         CellList cl = build_cells(sys, state, cl_dims);
         uint32_t nc[3] = {cl_dims[0], cl_dims[1], d == 3 ? cl_dims[2] : 1u};
@@ -1000,7 +1062,7 @@ template <typename F> struct IntEngine {
                             if (j == i) continue;
                             const int64_t* pj = &state.pos[d * j];
                             int64_t dd[3];
-                            for (int a = 0; a < d; a++) dd[a] = min_image(pi[a], pj[a], sys.box[a]);
+                            for (int a = 0; a < d; a++) dd[a] = sys.periodic(a) ? min_image(pi[a], pj[a], sys.box[a]) : pj[a] - pi[a]; // int_engine.rs:118-120
                             if (tables) {
                                 int32_t kk[3];
                                 if (tables->kick(si, state.species[j], dd, d, kk)) {
@@ -1025,8 +1087,30 @@ template <typename F> struct IntEngine {
                     }
                 }
             }
+            // soft walls (int_engine.rs:203-227, int_engine3.rs:107-126): WCA in the distance to
+            // the wall, in F, its kick rounded like a pair's
+            double wall_pe = 0.0;
+            for (int a = 0; a < d; a++) {
+                if (sys.periodic(a)) continue;
+                for (int side = 0; side < 2; side++) {
+                    if (sys.wall_kind[a][side] != GBMD_WALL_SOFT) continue;
+                    const int64_t dw = side == 0 ? pi[a] : sys.box[a] - pi[a];
+                    F df;
+                    if (!Real<F>::sep(dw, &df)) continue;
+                    if (df < Real<F>::from_f64(SOFT_RC)) {
+                        const F one = Real<F>::from_f64(1.0);
+                        const F s2 = one / (df * df);
+                        const F s6 = s2 * s2 * s2;
+                        const F f = Real<F>::from_f64(24.0) * s6 * (Real<F>::from_f64(2.0) * s6 - one) / df;
+                        const int32_t kw = Real<F>::round_to_i32(f * c);
+                        k[a] = wadd(k[a], side == 0 ? kw : wneg(kw));
+                        wall_force[i][2 * a + side] += (double)f;
+                        wall_pe += (double)(Real<F>::from_f64(4.0) * s6 * (s6 - one) + one);
+                    }
+                }
+            }
             for (int a = 0; a < d; a++) kicks[d * i + a] = k[a];
-            pe_part[i] = tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i;
+            pe_part[i] = (tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i) + wall_pe;
         }
         for (size_t i = 0; i < n; i++) pe += pe_part[i];
         return pe;
@@ -1040,6 +1124,10 @@ template <typename F> struct IntEngine {
         const int32_t drift = sys.to_step_displacement(sys.bath.drift);
         for (size_t s = 0; s < nsteps; s++) {
             forces(kicks);
+            // the soft walls' impulses (int_engine.rs:256-263, int_engine3.rs:140-145)
+            for (size_t i = 0; i < state.n(); i++)
+                for (int w = 0; w < 6; w++)
+                    if (wall_force[i][w] != 0.0) ledger.impulse[w] += wall_force[i][w] * sys.dt;
             for (size_t i = 0; i < state.n(); i++) {
                 const uint32_t sp = state.species[i];
                 bool pinned = sys.is_pinned(sp);
@@ -1069,15 +1157,51 @@ template <typename F> struct IntEngine {
                         }
                         de = 0.5 * m * (after - before);
                     }
-                    ledger.energy += de;
-                    ledger.energy_fixed += ledger_fixed(de);
-                    ledger.hits += 1;
+                    ledger.energy[LEDGER_BATH] += de;
+                    ledger.bath_energy_fixed += ledger_fixed(de);
+                    ledger.hits[LEDGER_BATH] += 1;
                 }
-                for (int a = 0; a < d; a++) x[a] = wrap(x[a] + (int64_t)v[a], sys.box[a]);
+                for (int a = 0; a < d; a++) x[a] += (int64_t)v[a];
+                for (int a = 0; a < d; a++) {
+                    if (sys.periodic(a)) {
+                        x[a] = wrap(x[a], sys.box[a]);
+                        continue;
+                    }
+                    const int side = mirror(x[a], sys.box[a]);
+                    if (side >= 0) collide(i, a, side, v);
+                }
             }
             steps += 1;
             clock += 1;
         }
+    }
+    // IntEngine::collide (int_engine.rs:363-390) / IntEngine3::collide (int_engine3.rs:186-205):
+    // hard and soft walls reflect the normal component; a thermal wall draws a new velocity; the
+    // ledger books the energy change and the normal momentum given to the wall.
+    void collide(size_t i, int axis, int side, int32_t* v) {
+        const int d = sys.dim;
+        const double m = sys.masses[state.species[i]];
+        const int w = 2 * axis + side;
+        double before[3] = {0, 0, 0}, after[3] = {0, 0, 0};
+        for (int a = 0; a < d; a++) before[a] = sys.velocity(v[a]);
+        if (sys.wall_kind[axis][side] == GBMD_WALL_THERMAL) {
+            double vn = 0.0, vt[2] = {0.0, 0.0};
+            thermal_velocity(sys, (uint32_t)i, clock, sys.wall_t[axis][side], m, side == 0 ? 1.0 : -1.0, &vn, vt);
+            v[axis] = sys.to_step_displacement(vn);
+            if (d == 2) {
+                v[1 - axis] = sys.to_step_displacement(vt[0]);
+            } else {
+                v[(axis + 1) % 3] = sys.to_step_displacement(vt[0]);
+                v[(axis + 2) % 3] = sys.to_step_displacement(vt[1]);
+            }
+        } else {
+            v[axis] = wneg(v[axis]);
+        }
+        for (int a = 0; a < d; a++) after[a] = sys.velocity(v[a]);
+        auto ke = [&](const double* u) { return d == 2 ? 0.5 * m * (u[0] * u[0] + u[1] * u[1]) : 0.5 * m * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]); };
+        ledger.energy[w] += ke(after) - ke(before);
+        ledger.impulse[w] += std::fabs(m * (before[axis] - after[axis]));
+        ledger.hits[w] += 1;
     }
     // int_engine.rs:396-413
     void reverse() {

@@ -60,6 +60,7 @@ _SIGS = [
     ("oracle_engine_hash", C.c_uint64, [VP]),
     ("oracle_engine_ledger", None, [VP, DP, I64P, U64P, U32P]),
     ("oracle_engine_set_system", None, [VP, SYS]),
+    ("oracle_engine_wall_ledger", None, [VP, DP, DP, U64P]),
     ("oracle_engine_steps", C.c_int64, [VP]),
     ("oracle_engine_energy", None, [VP, DP, DP]),
     ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
@@ -336,6 +337,12 @@ class IntEngine:
         self.sys = sys
         self._c = sys.to_c()
         lib().oracle_engine_set_system(self._h, C.byref(self._c))
+
+    def wall_ledger(self):
+        """walls::Ledger: (energy, impulse, hits), 7 slots each (2 axis + side, 6 the bath)."""
+        e, p, h = (C.c_double * 7)(), (C.c_double * 7)(), (C.c_uint64 * 7)()
+        lib().oracle_engine_wall_ledger(self._h, e, p, h)
+        return list(e), list(p), list(h)
 
     def ledger(self):
         """The bath's ledger slot and the clock: (energy summed in f64 in particle order, the

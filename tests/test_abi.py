@@ -37,8 +37,9 @@ def test_python_signatures_cover_the_header():
 def test_struct_layouts_match_the_header():
     # sizes follow from the header's field order on LP64 (no packing pragmas)
     assert C.sizeof(_abi.gbmd_pair) == 24
-    # ... + the heat bath: four u32 (bath, species, axis, pad), t, rate, drift, region[2]
-    assert C.sizeof(_abi.gbmd_system) == 4 + 4 + 24 + 8 + 32 + 16 * 24 + 24 + 8 + 4 + 4 + 16 + 24 + 16
+    # ... + the heat bath: four u32 (bath, species, axis, pad), t, rate, drift, region[2];
+    # + the walls: wall_kind[3][2] (u32), wall_t[3][2] (f64)
+    assert C.sizeof(_abi.gbmd_system) == 4 + 4 + 24 + 8 + 32 + 16 * 24 + 24 + 8 + 4 + 4 + 16 + 24 + 16 + 24 + 48
     assert C.sizeof(_abi.gbmd_options) == 48
     assert C.sizeof(_abi.gbmd_frame) == 64
 
@@ -138,3 +139,25 @@ def test_heat_bath_builders_and_validation(engine_lib):
         rc = engine_lib.gbmd_create(C.byref(bad), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
         assert rc == _abi.E_INVALID, field
         assert b"bath" in engine_lib.gbmd_last_error(), field
+
+
+def test_walls_builders_and_the_engine_refusal(engine_lib):
+    """with_walls clears the axis's periodic bit and records each side's kind (and a thermal
+    wall's kT); periodic / deterministic / has_soft_walls follow md-core. The GPU engine runs
+    periodic systems only and refuses walls before any device work."""
+    from micrographia_gb300 import Pair, System, System3, Wall, box_for, cube_for
+
+    s = System(box_for(200, 0.5, 1.0), 0.005, Pair.wca(), [1.0]).with_walls(1, Wall.soft(), Wall.thermal(1.5))
+    c = s.to_c()
+    assert c.periodic == 0b01 and list(c.wall_kind[1]) == [_abi.WALL_SOFT, _abi.WALL_THERMAL] and list(c.wall_t[1]) == [0.0, 1.5]
+    assert s.periodic(0) and not s.periodic(1) and s.has_soft_walls() and not s.deterministic()
+    s3 = System3(cube_for(300, 0.8), 0.005, Pair.wca(), [1.0]).with_walls(2, Wall.hard(), Wall.hard())
+    assert s3.to_c().periodic == 0b011 and s3.deterministic() and not s3.has_soft_walls()
+    n = 4
+    pos = np.full((n, 2), 1 << 33, np.int64)
+    vel = np.zeros((n, 2), np.int32)
+    sp = np.zeros(n, np.uint32)
+    P = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+    h = C.c_void_p()
+    rc = engine_lib.gbmd_create(C.byref(c), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
+    assert rc == _abi.E_UNSUPPORTED and b"wall" in engine_lib.gbmd_last_error()

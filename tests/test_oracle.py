@@ -390,3 +390,140 @@ def test_oracle_bath_draws_match_a_python_restatement(O, dim):
                 hits += 1
     assert hits > 40 * n // 4  # rate dt = 0.6; in 2D the fan's x range holds 5 of the 6
     assert c.ledger()[2] == hits and c.ledger()[3] == 40
+
+
+# ---------------------------------------------------------------- walls (md-ref/tests/boundaries.rs)
+def _gas_in_walls(O, n, density, aspect, seed):
+    """boundaries.rs:6-10: a WCA gas between hard walls on y (the lattice clear of them)."""
+    from micrographia_gb300 import Wall
+
+    sys_ = System(box_for(n, density, aspect), 0.005, Pair.wca(), [1.0]).with_walls(1, Wall.hard(), Wall.hard())
+    return sys_, O.fluid(sys_, n, 1.0, seed)
+
+
+@pytest.mark.parametrize("kind", ["hard", "soft"])
+def test_oracle_walls_and_gravity_reverse_exactly(O, kind):
+    """boundaries.rs:12-35: hard (soft) walls on both axes with gravity; 2000 steps, reverse,
+    2000 steps, reverse: the initial state exactly; the walls were hit (pushed)."""
+    from micrographia_gb300 import Wall
+
+    sys_, s0 = _gas_in_walls(O, 400, 0.3, 1.0, 1)
+    w = Wall.hard() if kind == "hard" else Wall.soft()
+    sys_.with_walls(0, w, w).with_gravity([0.0, -0.5])
+    if kind == "soft":
+        sys_.with_walls(1, w, w)
+    e = O.IntEngine(sys_, s0)
+    e.step(2000)
+    energy, impulse, hits = e.wall_ledger()
+    if kind == "hard":
+        assert sum(hits) > 100
+    else:
+        assert sum(impulse) > 1.0
+    e.reverse()
+    e.step(2000)
+    e.reverse()
+    assert e.state == s0
+
+
+def test_oracle_energy_with_gravity_and_soft_walls_is_conserved(O):
+    """boundaries.rs:37-54: a stratified gas (m g H / T = 2) between soft walls, f64 engine:
+    total energy per particle within 2e-3 over 2000 steps."""
+    from micrographia_gb300 import Wall
+
+    sys_, s0 = _gas_in_walls(O, 400, 0.3, 1.0, 2)
+    g = 2.0 / sys_.box_f64()[1]
+    sys_.with_walls(1, Wall.soft(), Wall.soft()).with_gravity([0.0, -g])
+    e = O.IntEngine(sys_, s0, f64=True)
+    e.step(200)
+    e0 = sum(e.energy())
+    worst = 0.0
+    for _ in range(20):
+        e.step(100)
+        worst = max(worst, abs(sum(e.energy()) - e0) / 400)
+    assert worst < 2e-3
+
+
+def _thermal_velocity_py(sys_, i, clock, t, m, inward, dim):
+    """walls::thermal_velocity (walls.rs:89-101) / three::thermal_velocity (three.rs:222-243)."""
+    from micrographia_gb300.workloads import threefry2x32
+
+    k0, k1 = sys_.seed & 0xFFFFFFFF, ((sys_.seed >> 32) ^ 0x57414C4C) & 0xFFFFFFFF
+    full = lambda r: (((r[0] << 21) ^ (r[1] >> 11)) & ((1 << 53) - 1)) * (1.0 / (1 << 53))
+    unit = lambda w: ((w << 21) & ((1 << 53) - 1)) * (1.0 / (1 << 53))
+    r = threefry2x32(i, clock, k0, k1)
+    r2 = threefry2x32(i, clock, k0, k1 ^ 1)
+    u1, u2, u3 = 1.0 - full(r), 1.0 - unit(r2[0]), unit(r2[1])
+    sd = math.sqrt(t / m)
+    normal = inward * sd * math.sqrt(-2.0 * math.log(u1))
+    if dim == 2:
+        return normal, [sd * math.sqrt(-2.0 * math.log(u2)) * math.cos(2.0 * math.pi * u3)]
+    rad = sd * math.sqrt(-2.0 * math.log(u2))
+    a = 2.0 * math.pi * u3
+    return normal, [rad * math.cos(a), rad * math.sin(a)]
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_wall_collisions_match_a_python_restatement(O, dim):
+    """Particles that never interact (a 0.1-sigma pair), moving at 0.25 sigma per step between a
+    hot thermal wall, a cold thermal wall and (3D) hard walls: every step the oracle's mirror and
+    collide (int_engine.rs:316-330, 363-390; int_engine3.rs:186-205) equal a Python restatement,
+    and the ledger's energy, impulse and hits equal the same sums in the same order."""
+    from micrographia_gb300 import State, State3, System3 as S3, Wall
+
+    L, n = 12.0, 6
+    tiny = Pair(1.0, 0.1, 0.1 * 2 ** (1 / 6))
+    box = [int(L * ONE)] * dim
+    wall_axis = 0
+    hot, cold = Wall.thermal(2.0), Wall.thermal(0.5)
+    if dim == 2:
+        sys_ = System(box, 0.005, tiny, [1.0, 3.0]).with_walls(0, hot, cold)
+    else:
+        sys_ = S3(box, 0.005, tiny, [1.0, 3.0]).with_walls(0, hot, cold).with_walls(2, Wall.hard(), Wall.hard())
+    sys_.seed = 0x2468_ACE0_1357
+    rng = np.random.default_rng(5)
+    pos = (rng.random((n, dim)) * (L - 2) + 1) * ONE
+    pos = pos.astype(np.int64)
+    vel = (rng.choice([-1, 1], (n, dim)) * rng.uniform(0.05, 0.25, (n, dim)) * ONE).astype(np.int32)
+    sp = np.array([k % 2 for k in range(n)], np.uint32)
+    st = (State if dim == 2 else State3)(pos, vel, sp)
+    c = O.IntEngine(sys_, st)
+    led_e, led_p, led_h = [0.0] * 7, [0.0] * 7, [0] * 7
+    lbox = box[0]
+    vfl = lambda v: float(v) / 2**32 / sys_.dt
+    for clock in range(300):
+        before = c.state
+        c.step(1)
+        after = c.state
+        for i in range(n):
+            x = [int(v) for v in before.pos[i]]
+            v = [int(u) for u in before.vel[i]]
+            x = [x[a] + v[a] for a in range(dim)]
+            for a in range(dim):
+                if sys_.periodic(a):
+                    x[a] %= lbox
+                    continue
+                side = 0 if x[a] < 0 else (1 if x[a] >= lbox else None)
+                if side is None:
+                    continue
+                x[a] = -1 - x[a] if side == 0 else 2 * lbox - 1 - x[a]
+                m = sys_.masses[int(sp[i])]
+                b = [vfl(u) for u in v]
+                w = sys_.walls[a][side]
+                if w.kind == 3:
+                    vn, vt = _thermal_velocity_py(sys_, i, clock, w.t, m, 1.0 if side == 0 else -1.0, dim)
+                    v[a] = sys_.to_step_displacement(vn)
+                    others = [1 - a] if dim == 2 else [(a + 1) % 3, (a + 2) % 3]
+                    for o, t in zip(others, vt):
+                        v[o] = sys_.to_step_displacement(t)
+                else:
+                    v[a] = -v[a]
+                af = [vfl(u) for u in v]
+                ke = lambda u: 0.5 * m * sum(q * q for q in u) if dim == 3 else 0.5 * m * (u[0] * u[0] + u[1] * u[1])
+                slot = 2 * a + side
+                led_e[slot] += ke(af) - ke(b)
+                led_p[slot] += abs(m * (b[a] - af[a]))
+                led_h[slot] += 1
+            assert list(after.pos[i]) == x and list(after.vel[i]) == v, (clock, i)
+    e_, p_, h_ = c.wall_ledger()
+    assert h_ == led_h and h_[0] > 0 and h_[1] > 0
+    assert e_ == led_e and p_ == led_p
