@@ -4,8 +4,9 @@
 // A C++17 restatement of micrographia's CPU semantics for the integer fixed-point LJ path:
 //   gpu-prims: threefry.rs (Threefry-2x32, uniforms, Box–Muller), fixed64.rs
 //   md-core:   fixed.rs, pair.rs, system.rs (System/State subset), init.rs, three.rs, table.rs
-//   md-ref:    real.rs (f32/f64 Real semantics), cells.rs, int_engine.rs (periodic NVE subset),
-//              int_engine3.rs, fast.rs (the SIMD fast path: the timed CPU baseline),
+//   md-ref:    real.rs (f32/f64 Real semantics), cells.rs, int_engine.rs and int_engine3.rs
+//              (periodic or walled boxes, the Andersen bath, the ledger), fast.rs (the SIMD fast
+//              path: the timed CPU baseline),
 //              float_engine.rs
 //   md:        the Verlet-list definition of shaders/neighbors.wgsl:27-64 / md3.wgsl:443-483
 // plus f64 instruments the reference lacks (virial pressure after mc/src/gibbs.rs:58-66,
@@ -969,8 +970,9 @@ inline void thermal_velocity(const System& sys, uint32_t id, uint32_t clock, dou
 }
 inline int64_t ledger_fixed(double de) { return (int64_t)std::round(de * 16777216.0); }
 
-// md-ref int_engine.rs:23-447 and int_engine3.rs:12-240, for periodic systems with an optional
-// Andersen bath (walls, bonds, pistons, membranes and compartments are outside this path). One template serves 2D and
+// md-ref int_engine.rs:23-447 and int_engine3.rs:12-240: periodic or walled (hard, soft,
+// thermal) boxes, an optional Andersen bath and the ledger (bonds, pistons, membranes and
+// compartments are outside this path). One template serves 2D and
 // 3D; in 2D `fast` selects fast.rs's half-shell path when it applies, as IntEngine::forces does.
 template <typename F> struct IntEngine {
     System sys;
