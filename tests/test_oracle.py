@@ -527,3 +527,53 @@ def test_oracle_wall_collisions_match_a_python_restatement(O, dim):
     e_, p_, h_ = c.wall_ledger()
     assert h_ == led_h and h_[0] > 0 and h_[1] > 0
     assert e_ == led_e and p_ == led_p
+
+
+def _on_step_temperatures(sys_, e):
+    """IntEngine::velocities (int_engine.rs:417-430), for systems without gravity: per particle
+    0.5 m |(v + v_next) / 2|^2 with v_next = v + kick."""
+    k, _ = e.kicks()
+    st = e.state
+    v0 = st.vel.astype(np.float64) / 2**32 / sys_.dt
+    v1 = (st.vel.astype(np.int64) + k).astype(np.float64) / 2**32 / sys_.dt
+    v = 0.5 * (v0 + v1)
+    m = np.array(sys_.masses)[st.species]
+    return 0.5 * m * (v * v).sum(axis=1), st.species
+
+
+def test_oracle_thermal_walls_set_the_temperature(O):
+    """boundaries.rs:91-110: a dilute WCA gas at T = 0.5 between thermal walls at 1.5 reaches
+    T = 1.5 within 0.06, taking more than 0.5 epsilon per particle from the walls."""
+    from micrographia_gb300 import Wall
+
+    n = 150
+    w = Wall.thermal(1.5)
+    sys_ = System(box_for(n, 0.1, 1.0), 0.005, Pair.wca(), [1.0]).with_walls(0, w, w).with_walls(1, w, w)
+    e = O.IntEngine(sys_, O.fluid(sys_, n, 0.5, 4))
+    e.step(40000)
+    t = 0.0
+    for _ in range(200):
+        e.step(100)
+        ke, _ = _on_step_temperatures(sys_, e)
+        t += ke.sum() / n / 200
+    heat = sum(e.wall_ledger()[0])
+    assert abs(t - 1.5) < 0.06, t
+    assert heat > 0.5 * n
+
+
+def test_oracle_andersen_sets_the_temperature_of_each_species(O):
+    """boundaries.rs:217-239: an LJ liquid of masses 1 and 4 from T = 2 under a bath at 0.8
+    (rate 1): each species' on-step temperature within 0.04 of 0.8."""
+    n = 800
+    sys_ = System(box_for(n, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 4.0]).with_thermostat(0.8, 1.0)
+    s0 = O.fluid(sys_, n, 2.0, 11)
+    s0.species[0::2] = 1
+    e = O.IntEngine(sys_, s0)
+    e.step(3000)
+    t = np.zeros(2)
+    for _ in range(40):
+        e.step(50)
+        ke, sp = _on_step_temperatures(sys_, e)
+        for s in (0, 1):
+            t[s] += ke[sp == s].sum() / (n / 2) / 40
+    assert abs(t[0] - 0.8) < 0.04 and abs(t[1] - 0.8) < 0.04, t
