@@ -104,6 +104,17 @@ typedef struct gbmd_system {
      * (GBMD_E_UNSUPPORTED otherwise); the fields carry the reference's System whole. */
     uint32_t wall_kind[3][2];
     double wall_t[3][2];
+    /* A semi-permeable membrane across a walled axis (md_core::Membrane, system.rs:119-141;
+     * with_membrane / with_pores, system.rs:259-274), 2D: it reflects the species in
+     * membrane_blocks about membrane_position - 1/2, except through pores membrane_pore_width wide
+     * every 2^membrane_pore_shift position units along it (shift 0: no pores). Carried for the
+     * oracle; the GPU engine refuses it (GBMD_E_UNSUPPORTED). */
+    uint32_t membrane;      /* 1: present */
+    uint32_t membrane_axis;
+    uint32_t membrane_blocks;
+    uint32_t membrane_pore_shift;
+    int64_t membrane_position;
+    int64_t membrane_pore_width;
 } gbmd_system;
 
 /* gbmd_system.wall_kind: md_core::Wall (walls.rs). */

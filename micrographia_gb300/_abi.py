@@ -60,6 +60,12 @@ class gbmd_system(C.Structure):
         ("bath_region", C.c_int64 * 2),
         ("wall_kind", (C.c_uint32 * 2) * 3),
         ("wall_t", (C.c_double * 2) * 3),
+        ("membrane", C.c_uint32),
+        ("membrane_axis", C.c_uint32),
+        ("membrane_blocks", C.c_uint32),
+        ("membrane_pore_shift", C.c_uint32),
+        ("membrane_position", C.c_int64),
+        ("membrane_pore_width", C.c_int64),
     ]
 
 

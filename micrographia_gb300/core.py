@@ -112,6 +112,7 @@ class _SystemBase:
         self.pinned = 0
         self.thermostat = None
         self.walls = [None] * self.DIM
+        self.membrane = None  # (axis, position, blocks mask, pore_shift, pore_width), 2D
 
     def species(self):
         return len(self.masses)
@@ -219,6 +220,9 @@ class _SystemBase:
             for side, w in enumerate(ws or ()):
                 s.wall_kind[a][side] = w.kind
                 s.wall_t[a][side] = w.t
+        if self.membrane is not None:
+            s.membrane = 1
+            s.membrane_axis, s.membrane_position, s.membrane_blocks, s.membrane_pore_shift, s.membrane_pore_width = self.membrane
         s.pinned = self.pinned
         th = self.thermostat
         if th is not None:
@@ -271,6 +275,26 @@ class System(_SystemBase):
     """md_core::System (system.rs:26-64), periodic LJ subset."""
 
     DIM = 2
+
+    def with_membrane(self, axis, position_sigma, blocked):
+        """System::with_membrane (system.rs:259-265): a membrane across walled `axis` at
+        `position_sigma` that reflects the species in `blocked`."""
+        if self.walls[axis] is None:
+            raise ValueError("a membrane needs walls on its axis")
+        mask = 0
+        for b in blocked:
+            mask |= 1 << b
+        self.membrane = (axis, to_fixed(position_sigma), mask, 0, 0)
+        return self
+
+    def with_pores(self, log2_period, width):
+        """System::with_pores (system.rs:267-274): openings `width` sigma wide every
+        2^log2_period sigma along the membrane."""
+        if self.membrane is None:
+            raise ValueError("add a membrane first")
+        a, pos, mask, _, _ = self.membrane
+        self.membrane = (a, pos, mask, 32 + log2_period, to_fixed(width))
+        return self
 
     def with_fan(self, species, x0, x1, drift):
         """System::with_fan (system.rs:335-344): the bath acts on `species` (a bitmask) with

@@ -51,6 +51,7 @@ int validate_system(const gbmd_system& sys, uint32_t n) {
     uint32_t all = (1u << sys.dim) - 1u;
     if ((sys.periodic & all) != all)
         return fail(GBMD_E_UNSUPPORTED, "walls are not part of this engine: every axis must be periodic");
+    if (sys.membrane) return fail(GBMD_E_UNSUPPORTED, "membranes are not part of this engine");
     for (uint32_t a = 0; a < sys.dim; a++)
         if (sys.box_len[a] <= 0) return fail(GBMD_E_INVALID, "box lengths must be positive");
     for (uint32_t k = 0; k < sys.nspecies * sys.nspecies; k++) {

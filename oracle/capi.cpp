@@ -134,8 +134,15 @@ int oracle_init(const gbmd_system* csys, const gbmd_init* spec, int64_t* pos, in
         State st;
         switch (spec->recipe) {
             case GBMD_INIT_FLUID: {
+                // init::fluid (init.rs:105-121): on an axis with walls the lattice keeps 1 sigma
+                // clear of them (the GPU initialiser runs periodic systems only)
                 st.dim = 2;
-                st.pos = lattice(n, {sys.box[0], sys.box[1]}, spec->jitter, spec->seed);
+                int64_t inner[2];
+                for (int a = 0; a < 2; a++) inner[a] = sys.periodic(a) ? sys.box[a] : sys.box[a] - to_fixed(2.0);
+                st.pos = lattice(n, {inner[0], inner[1]}, spec->jitter, spec->seed);
+                for (size_t i = 0; i < n; i++)
+                    for (int a = 0; a < 2; a++)
+                        if (!sys.periodic(a)) st.pos[2 * i + a] += to_fixed(1.0);
                 st.species.assign(n, 0);
                 st.vel = maxwell(sys, st.species, spec->t, spec->seed);
                 break;

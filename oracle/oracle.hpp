@@ -205,6 +205,15 @@ struct System {
     std::array<std::array<uint32_t, 2>, 3> wall_kind{};
     std::array<std::array<double, 2>, 3> wall_t{};
     bool periodic(int a) const { return (periodic_bits >> a) & 1u; } // system.rs:384-386
+    // md_core::Membrane (system.rs:119-141), 2D
+    bool membrane = false;
+    int membrane_axis = 0;
+    uint32_t membrane_blocks = 0, membrane_pore_shift = 0;
+    int64_t membrane_position = 0, membrane_pore_width = 0;
+    bool membrane_blocks_species(uint32_t s) const { return (membrane_blocks >> s) & 1u; }
+    bool in_pore(int64_t along) const {
+        return membrane_pore_shift != 0 && (along & (((int64_t)1 << membrane_pore_shift) - 1)) < membrane_pore_width;
+    }
     bool all_periodic() const { return (periodic_bits & ((1u << dim) - 1u)) == ((1u << dim) - 1u); }
 
     static System from_c(const gbmd_system& s) {
@@ -219,6 +228,12 @@ struct System {
         o.seed = s.seed;
         o.pinned = s.pinned;
         o.periodic_bits = s.periodic | (s.dim == 2 ? 4u : 0u);
+        o.membrane = s.membrane != 0;
+        o.membrane_axis = (int)s.membrane_axis;
+        o.membrane_blocks = s.membrane_blocks;
+        o.membrane_pore_shift = s.membrane_pore_shift;
+        o.membrane_position = s.membrane_position;
+        o.membrane_pore_width = s.membrane_pore_width;
         for (int a = 0; a < 3; a++)
             for (int side = 0; side < 2; side++) {
                 o.wall_kind[a][side] = s.wall_kind[a][side];
@@ -923,7 +938,7 @@ inline bool andersen(const System& sys, uint32_t id, uint32_t clock, uint32_t s,
 // to the system and the normal momentum it gave the wall, summed in f64 in particle order as
 // IntEngine does, and the hits; for the bath also the events rounded to 2^-24 and summed as
 // integers (the order-free total the GPU engine keeps).
-constexpr int LEDGER_SLOTS = 7, LEDGER_BATH = 6;
+constexpr int LEDGER_SLOTS = 7, LEDGER_BATH = 6, MEMBRANE_LOW = 4, MEMBRANE_HIGH = 5; // walls.rs:7-14
 struct Ledger {
     double energy[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
     double impulse[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
@@ -1163,7 +1178,22 @@ template <typename F> struct IntEngine {
                     ledger.bath_energy_fixed += ledger_fixed(de);
                     ledger.hits[LEDGER_BATH] += 1;
                 }
+                int64_t old[3] = {x[0], x[1], d == 3 ? x[2] : 0};
                 for (int a = 0; a < d; a++) x[a] += (int64_t)v[a];
+                // the membrane (int_engine.rs:296-313): a blocked species outside a pore that
+                // crossed it is mirrored about position - 1/2 (walls::cross_membrane, walls.rs:18-25)
+                if (sys.membrane && d == 2 && sys.membrane_blocks_species(sp)) {
+                    const int a = sys.membrane_axis;
+                    const int64_t w = sys.membrane_position;
+                    if (!sys.in_pore(old[1 - a]) && (old[a] < w) != (x[a] < w)) {
+                        const int face = old[a] < w ? MEMBRANE_LOW : MEMBRANE_HIGH;
+                        x[a] = 2 * w - 1 - x[a];
+                        const double dp = 2.0 * sys.masses[sp] * std::fabs(sys.velocity(v[a]));
+                        v[a] = wneg(v[a]);
+                        ledger.impulse[face] += dp;
+                        ledger.hits[face] += 1;
+                    }
+                }
                 for (int a = 0; a < d; a++) {
                     if (sys.periodic(a)) {
                         x[a] = wrap(x[a], sys.box[a]);

@@ -577,3 +577,31 @@ def test_oracle_andersen_sets_the_temperature_of_each_species(O):
         for s in (0, 1):
             t[s] += ke[sp == s].sum() / (n / 2) / 40
     assert abs(t[0] - 0.8) < 0.04 and abs(t[1] - 0.8) < 0.04, t
+
+
+def test_oracle_membrane_confines_solute_and_is_reversible(O):
+    """md-ref/tests/boundaries.rs:241-268: soft walls on x, a membrane at the middle blocking
+    species 1 (the solute, 20% of the right half): after 3000 steps no solute has crossed, the
+    solute has hit the membrane, the solvent has crossed it, and the run reverses exactly."""
+    from micrographia_gb300 import Wall
+    from micrographia_gb300.workloads import uniform
+
+    n = 1200
+    sys_ = System(box_for(n, 0.4, 2.0), 0.005, Pair.wca(), [1.0, 1.0]).with_walls(0, Wall.soft(), Wall.soft())
+    half = sys_.box_f64()[0] / 2.0
+    sys_.with_membrane(0, half, [1])
+    s0 = O.fluid(sys_, n, 1.0, 13)
+    for i in range(n):
+        if to_f64(int(s0.pos[i, 0])) > half + 1.0 and uniform(13, 3, i) < 0.2:
+            s0.species[i] = 1
+    left0 = int((s0.pos[:, 0] < int(half * ONE)).sum())
+    e = O.IntEngine(sys_, s0)
+    e.step(3000)
+    st = e.state
+    assert all(to_f64(int(p)) > half - 0.5 for p in st.pos[st.species == 1, 0])
+    assert e.wall_ledger()[2][5] > 20
+    assert int((st.pos[:, 0] < int(half * ONE)).sum()) != left0
+    e.reverse()
+    e.step(3000)
+    e.reverse()
+    assert e.state == s0
