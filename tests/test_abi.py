@@ -161,3 +161,13 @@ def test_walls_builders_and_the_engine_refusal(engine_lib):
     h = C.c_void_p()
     rc = engine_lib.gbmd_create(C.byref(c), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
     assert rc == _abi.E_UNSUPPORTED and b"wall" in engine_lib.gbmd_last_error()
+    # a membrane needs walls on its axis (system.rs:259-265); the engine refuses membranes
+    with pytest.raises(ValueError):
+        System(box_for(200, 0.5, 1.0), 0.005, Pair.wca(), [1.0]).with_membrane(0, 5.0, [0])
+    m = System(box_for(200, 0.5, 2.0), 0.005, Pair.wca(), [1.0, 1.0]).with_walls(0, Wall.soft(), Wall.soft())
+    m.with_membrane(0, 8.0, [1]).with_pores(2, 0.5)
+    cm = m.to_c()
+    assert (cm.membrane, cm.membrane_axis, cm.membrane_blocks, cm.membrane_pore_shift) == (1, 0, 0b10, 34)
+    cm.periodic = 0b11  # even on a periodic box the membrane alone is refused
+    rc = engine_lib.gbmd_create(C.byref(cm), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
+    assert rc == _abi.E_UNSUPPORTED and b"membrane" in engine_lib.gbmd_last_error()
