@@ -115,6 +115,13 @@ typedef struct gbmd_system {
     uint32_t membrane_pore_shift;
     int64_t membrane_position;
     int64_t membrane_pore_width;
+    /* Compartments (System::with_compartments, system.rs:233-241), 2D: a walled axis split into
+     * boxes of 2^(compartments[axis] - 32) sigma by hard walls (0: none); particles in different
+     * boxes interact only when compartments_diathermal is 1 (CompartmentWalls, system.rs:143-153).
+     * Carried for the oracle; the GPU engine refuses them (GBMD_E_UNSUPPORTED). */
+    uint32_t compartments[2];
+    uint32_t compartments_diathermal;
+    uint32_t _compartments_pad;
 } gbmd_system;
 
 /* gbmd_system.wall_kind: md_core::Wall (walls.rs). */

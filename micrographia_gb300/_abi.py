@@ -66,6 +66,9 @@ class gbmd_system(C.Structure):
         ("membrane_pore_shift", C.c_uint32),
         ("membrane_position", C.c_int64),
         ("membrane_pore_width", C.c_int64),
+        ("compartments", C.c_uint32 * 2),
+        ("compartments_diathermal", C.c_uint32),
+        ("_compartments_pad", C.c_uint32),
     ]
 
 

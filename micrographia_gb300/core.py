@@ -113,6 +113,8 @@ class _SystemBase:
         self.thermostat = None
         self.walls = [None] * self.DIM
         self.membrane = None  # (axis, position, blocks mask, pore_shift, pore_width), 2D
+        self.compartments = [0, 0]  # shift per axis (32 + log2 side), 2D
+        self.compartments_diathermal = False
 
     def species(self):
         return len(self.masses)
@@ -220,6 +222,9 @@ class _SystemBase:
             for side, w in enumerate(ws or ()):
                 s.wall_kind[a][side] = w.kind
                 s.wall_t[a][side] = w.t
+        if self.DIM == 2:
+            s.compartments[0], s.compartments[1] = self.compartments
+            s.compartments_diathermal = 1 if self.compartments_diathermal else 0
         if self.membrane is not None:
             s.membrane = 1
             s.membrane_axis, s.membrane_position, s.membrane_blocks, s.membrane_pore_shift, s.membrane_pore_width = self.membrane
@@ -275,6 +280,30 @@ class System(_SystemBase):
     """md_core::System (system.rs:26-64), periodic LJ subset."""
 
     DIM = 2
+
+    def with_compartments(self, axis, log2_sigma):
+        """System::with_compartments (system.rs:233-241): `axis` (with walls) split into boxes of
+        2^log2_sigma sigma."""
+        shift = 32 + log2_sigma
+        if self.walls[axis] is None:
+            raise ValueError("compartments need walls on their axis")
+        if self.box_len[axis] % (1 << shift):
+            raise ValueError("box must be a whole number of compartments")
+        self.compartments[axis] = shift
+        return self
+
+    def with_diathermal_compartments(self):
+        """System::with_diathermal_compartments (system.rs:222-226)."""
+        self.compartments_diathermal = True
+        return self
+
+    def compartment_counts(self):
+        """System::compartment_counts (system.rs:247-251)."""
+        return [1 if self.compartments[a] == 0 else self.box_len[a] >> self.compartments[a] for a in range(2)]
+
+    def compartment_of(self, p):
+        """System::compartment_of (system.rs:253-257)."""
+        return [0 if self.compartments[a] == 0 else int(p[a]) >> self.compartments[a] for a in range(2)]
 
     def with_membrane(self, axis, position_sigma, blocked):
         """System::with_membrane (system.rs:259-265): a membrane across walled `axis` at

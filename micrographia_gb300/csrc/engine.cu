@@ -52,6 +52,7 @@ int validate_system(const gbmd_system& sys, uint32_t n) {
     if ((sys.periodic & all) != all)
         return fail(GBMD_E_UNSUPPORTED, "walls are not part of this engine: every axis must be periodic");
     if (sys.membrane) return fail(GBMD_E_UNSUPPORTED, "membranes are not part of this engine");
+    if (sys.compartments[0] || sys.compartments[1]) return fail(GBMD_E_UNSUPPORTED, "compartments are not part of this engine");
     for (uint32_t a = 0; a < sys.dim; a++)
         if (sys.box_len[a] <= 0) return fail(GBMD_E_INVALID, "box lengths must be positive");
     for (uint32_t k = 0; k < sys.nspecies * sys.nspecies; k++) {

@@ -211,6 +211,13 @@ struct System {
     uint32_t membrane_blocks = 0, membrane_pore_shift = 0;
     int64_t membrane_position = 0, membrane_pore_width = 0;
     bool membrane_blocks_species(uint32_t s) const { return (membrane_blocks >> s) & 1u; }
+    // compartments (system.rs:222-257), 2D: shift per axis (0: none), insulating or diathermal
+    uint32_t compartments[2] = {0, 0};
+    bool diathermal = false;
+    int64_t compartment_of(const int64_t* p, int a) const { return compartments[a] == 0 ? 0 : p[a] >> compartments[a]; }
+    bool interact_across(const int64_t* a, const int64_t* b) const { // system.rs:229-231
+        return dim != 2 || diathermal || (compartment_of(a, 0) == compartment_of(b, 0) && compartment_of(a, 1) == compartment_of(b, 1));
+    }
     bool in_pore(int64_t along) const {
         return membrane_pore_shift != 0 && (along & (((int64_t)1 << membrane_pore_shift) - 1)) < membrane_pore_width;
     }
@@ -228,6 +235,9 @@ struct System {
         o.seed = s.seed;
         o.pinned = s.pinned;
         o.periodic_bits = s.periodic | (s.dim == 2 ? 4u : 0u);
+        o.compartments[0] = s.dim == 2 ? s.compartments[0] : 0;
+        o.compartments[1] = s.dim == 2 ? s.compartments[1] : 0;
+        o.diathermal = s.compartments_diathermal != 0;
         o.membrane = s.membrane != 0;
         o.membrane_axis = (int)s.membrane_axis;
         o.membrane_blocks = s.membrane_blocks;
@@ -1078,6 +1088,7 @@ template <typename F> struct IntEngine {
                             size_t j = cl.items[q];
                             if (j == i) continue;
                             const int64_t* pj = &state.pos[d * j];
+                            if (!sys.interact_across(pi, pj)) continue; // int_engine.rs:161-163
                             int64_t dd[3];
                             for (int a = 0; a < d; a++) dd[a] = sys.periodic(a) ? min_image(pi[a], pj[a], sys.box[a]) : pj[a] - pi[a]; // int_engine.rs:118-120
                             if (tables) {
@@ -1200,7 +1211,19 @@ template <typename F> struct IntEngine {
                         continue;
                     }
                     const int side = mirror(x[a], sys.box[a]);
-                    if (side >= 0) collide(i, a, side, v);
+                    if (side >= 0) {
+                        collide(i, a, side, v);
+                    } else if (d == 2 && sys.compartments[a] != 0) {
+                        // int_engine.rs:324-330: a particle that crossed into another compartment
+                        // is mirrored back into its home one (walls::mirror_compartment, walls.rs:72-78)
+                        const uint32_t sh = sys.compartments[a];
+                        const int64_t home = old[a] >> sh;
+                        if ((x[a] >> sh) != home) {
+                            const int64_t lo = home << sh, hi = (home + 1) << sh;
+                            x[a] = x[a] < lo ? 2 * lo - 1 - x[a] : (x[a] >= hi ? 2 * hi - 1 - x[a] : x[a]);
+                            v[a] = wneg(v[a]);
+                        }
+                    }
                 }
             }
             steps += 1;

@@ -38,8 +38,9 @@ def test_struct_layouts_match_the_header():
     # sizes follow from the header's field order on LP64 (no packing pragmas)
     assert C.sizeof(_abi.gbmd_pair) == 24
     # ... + the heat bath: four u32 (bath, species, axis, pad), t, rate, drift, region[2];
-    # + the walls: wall_kind[3][2] (u32), wall_t[3][2] (f64); + the membrane: four u32, two i64
-    assert C.sizeof(_abi.gbmd_system) == 4 + 4 + 24 + 8 + 32 + 16 * 24 + 24 + 8 + 4 + 4 + 16 + 24 + 16 + 24 + 48 + 16 + 16
+    # + the walls: wall_kind[3][2] (u32), wall_t[3][2] (f64); + the membrane: four u32, two i64;
+    # + the compartments: four u32
+    assert C.sizeof(_abi.gbmd_system) == 4 + 4 + 24 + 8 + 32 + 16 * 24 + 24 + 8 + 4 + 4 + 16 + 24 + 16 + 24 + 48 + 16 + 16 + 16
     assert C.sizeof(_abi.gbmd_options) == 48
     assert C.sizeof(_abi.gbmd_frame) == 64
 

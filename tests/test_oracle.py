@@ -605,3 +605,51 @@ def test_oracle_membrane_confines_solute_and_is_reversible(O):
     e.step(3000)
     e.reverse()
     assert e.state == s0
+
+
+def _compartment_fluid(O, sys_, per_box, t, seed):
+    """init::compartment_fluid (init.rs:126-149): per_box particles on a small jittered lattice
+    in every compartment, 0.6 sigma clear of its walls, numbered box by box; Maxwell velocities."""
+    from micrographia_gb300 import State, to_fixed
+    from micrographia_gb300.workloads import uniform
+
+    cx, cy = sys_.compartment_counts()
+    side = [to_f64(sys_.box_len[0]) / cx, to_f64(sys_.box_len[1]) / cy]
+    nx = max(int(math.ceil(math.sqrt(per_box * side[0] / side[1]))), 1)
+    ny = -(-per_box // nx)
+    margin = 0.6
+    a = [(side[0] - 2.0 * margin) / nx, (side[1] - 2.0 * margin) / ny]
+    pos = []
+    for by in range(cy):
+        for bx in range(cx):
+            for k in range(per_box):
+                i = len(pos)
+                jx = 0.2 * a[0] * (uniform(seed, 2, 2 * i) - 0.5)
+                jy = 0.2 * a[1] * (uniform(seed, 2, 2 * i + 1) - 0.5)
+                x = bx * side[0] + margin + ((k % nx) + 0.5) * a[0] + jx
+                y = by * side[1] + margin + ((k // nx) + 0.5) * a[1] + jy
+                pos.append([to_fixed(x), to_fixed(y)])
+    n = len(pos)
+    sp = np.zeros(n, np.uint32)
+    return State(np.array(pos, np.int64), O.maxwell(sys_, sp, t, seed), sp)
+
+
+def test_oracle_compartments_are_independent_and_reversible(O):
+    """md-ref/tests/boundaries.rs:154-181: 16 x 16 compartments of 8 sigma between hard walls,
+    6 particles each: after 3000 steps every particle is still in its own compartment, and the run
+    reverses exactly."""
+    from micrographia_gb300 import Wall
+
+    side = 8 * ONE
+    sys_ = System([16 * side, 16 * side], 0.005, Pair.wca(), [1.0])
+    sys_.with_walls(0, Wall.hard(), Wall.hard()).with_walls(1, Wall.hard(), Wall.hard())
+    sys_.with_compartments(0, 3).with_compartments(1, 3)
+    s0 = _compartment_fluid(O, sys_, 6, 1.0, 7)
+    home = [sys_.compartment_of(p) for p in s0.pos]
+    e = O.IntEngine(sys_, s0)
+    e.step(3000)
+    assert [sys_.compartment_of(p) for p in e.state.pos] == home
+    e.reverse()
+    e.step(3000)
+    e.reverse()
+    assert e.state == s0
