@@ -172,3 +172,19 @@ def test_walls_builders_and_the_engine_refusal(engine_lib):
     cm.periodic = 0b11  # even on a periodic box the membrane alone is refused
     rc = engine_lib.gbmd_create(C.byref(cm), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
     assert rc == _abi.E_UNSUPPORTED and b"membrane" in engine_lib.gbmd_last_error()
+    # compartments need walls and whole boxes (system.rs:233-241); the engine refuses them
+    from micrographia_gb300 import ONE
+
+    box = System([32 * ONE, 32 * ONE], 0.005, Pair.wca(), [1.0])
+    with pytest.raises(ValueError):
+        box.with_compartments(0, 3)
+    box.with_walls(0, Wall.hard(), Wall.hard())
+    with pytest.raises(ValueError):
+        box.with_compartments(0, 6)  # 64 sigma boxes do not divide 32 sigma
+    box.with_compartments(0, 3).with_diathermal_compartments()
+    cc = box.to_c()
+    assert list(cc.compartments) == [35, 0] and cc.compartments_diathermal == 1
+    assert box.compartment_counts() == [4, 1] and box.compartment_of([17 * ONE, 3 * ONE]) == [2, 0]
+    cc.periodic = 0b11
+    rc = engine_lib.gbmd_create(C.byref(cc), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
+    assert rc == _abi.E_UNSUPPORTED and b"compartment" in engine_lib.gbmd_last_error()
