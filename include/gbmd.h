@@ -332,7 +332,9 @@ int gbmd_create_seeded(const gbmd_system* sys, const gbmd_init* spec, const gbmd
  * stream); the work is enqueued on it and the call returns without waiting.
  * The scratch is one static device array of about 4.3 MB (4 * GBMD_BIN_STATIC_MAX_N words plus
  * the sort's histograms), which every GPU that loads the library holds until the process
- * exits; n above GBMD_BIN_STATIC_MAX_N is rejected with GBMD_E_INVALID. The first call on each
+ * exits; n above GBMD_BIN_STATIC_MAX_N is rejected with GBMD_E_INVALID, as are a box length
+ * that is not positive and a cell count (product of `cells`) of 2^32 - 1 or more, all before any
+ * device work. With n = 0 only start[] is written (zeros). The first call on each
  * device looks up that array's device address (cudaGetSymbolAddress, with that device current),
  * so make the first call on a device before any stream capture. Every call shares the one
  * array: calls that overlap on the GPU (other streams, other threads) race and must be

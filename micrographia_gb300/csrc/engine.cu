@@ -685,7 +685,6 @@ int setup_step_loop(gbmd_engine* e) {
     if (!e->verlet || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath ||
         (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP))
         return GBMD_OK;
-    if (e->block_steps > (1u << 20)) return GBMD_OK; // (the barrier counts k x blocks arrivals in 32 bits)
     // Larger systems' steps are long enough that the graph's per-step nodes cost less than the
     // loop's barrier (3D N = 131,072: 71 us per step in graphs, 76 in the loop; 65,536: 53 vs 49).
     if (e->n >= STEP_LOOP_BELOW) return GBMD_OK;
@@ -699,6 +698,9 @@ int setup_step_loop(gbmd_engine* e) {
         int per = 0;
         GBMD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, e->D == 2 ? loop_kernel<2>(S) : loop_kernel<3>(S), 128, 0));
         const uint64_t blocks = ((uint64_t)e->n * S + 127) / 128;
+        // (one launch takes at most block_steps steps, and its grid barrier counts up to
+        // steps x blocks arrivals in the low 32 bits of a 64-bit word, cleared per launch)
+        if ((uint64_t)e->block_steps * blocks >= (1ull << 32)) continue;
         if (blocks >= 1 && blocks <= (uint64_t)per * (uint64_t)sms) {
             e->loop_lanes = S;
             e->loop_blocks = (uint32_t)blocks;
@@ -1584,8 +1586,12 @@ int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* r
 int gbmd_debug_bin(gbmd_engine* e, const uint32_t* cells, uint32_t* keys, uint32_t* start, uint32_t* items, uint32_t* order) {
     if (!e || !cells) return fail(GBMD_E_INVALID, "null argument");
     Params P = e->P;
-    for (int a = 0; a < e->D; a++)
+    uint64_t ncell = 1;
+    for (int a = 0; a < e->D; a++) {
         if (cells[a] < 1) return fail(GBMD_E_INVALID, "cells must be positive");
+        ncell *= cells[a];
+        if (ncell >= UINT32_MAX) return fail(GBMD_E_INVALID, "too many cells");
+    }
     set_cells(P, cells, (uint32_t)e->D);
     uint32_t* st2 = nullptr;
     GBMD_CUDA_TRY(cudaMalloc(&st2, ((size_t)P.ncell + 1) * 4));

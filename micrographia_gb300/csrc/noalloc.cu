@@ -29,7 +29,9 @@ constexpr size_t SCRATCH_WORDS = 4 * (size_t)MAX_N + HIST_WORDS + TMP_WORDS;
 
 __device__ __align__(256) uint32_t g_bin_scratch[SCRATCH_WORDS];
 
-// Device address of g_bin_scratch per device ordinal, looked up once per device.
+// Device address of g_bin_scratch per device ordinal, looked up once per device. (A
+// cudaDeviceReset of that device in this process would leave the cached address stale: callers
+// that reset a device do not use this entry point afterwards.)
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
 uint32_t* g_addr[MAX_DEVICES] = {};
@@ -85,10 +87,12 @@ extern "C" int gbmd_bin_cells_static(const gbmd_system* sys, const int64_t* pos,
     for (uint32_t a = 0; a < 3; a++) {
         B.nc[a] = a < sys->dim ? cells[a] : 1;
         if (B.nc[a] == 0) return fail(GBMD_E_INVALID, "cells must be positive");
+        if (a < sys->dim && sys->box_len[a] <= 0) return fail(GBMD_E_INVALID, "box lengths must be positive");
+        // (checked after every factor, so that the product cannot wrap past the bound)
         ncell *= B.nc[a];
+        if (ncell >= UINT32_MAX) return fail(GBMD_E_INVALID, "too many cells");
         B.box_f[a] = a < sys->dim ? (double)sys->box_len[a] * (1.0 / 4294967296.0) : 1.0;
     }
-    if (ncell >= UINT32_MAX) return fail(GBMD_E_INVALID, "too many cells");
     uint32_t* scratch = nullptr;
     GBMD_TRY(scratch_address(&scratch));
     cudaStream_t s = (cudaStream_t)stream;

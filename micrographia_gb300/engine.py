@@ -255,12 +255,18 @@ class _Engine:
         """Raw status of gbmd_debug_barrier_timeout (the step loop's barrier running out)."""
         return self._lib.gbmd_debug_barrier_timeout(self._h, int(blocks))
 
-    def debug_list(self, max_total=None):
+    def debug_list_flat(self, max_total=None):
+        """The Verlet lists in id order, packed: (counts, offsets, neighbour ids); particle i's
+        neighbours are ids[offsets[i]:offsets[i + 1]], unsorted."""
         counts = np.empty(self.n, np.uint32)
         cap = max_total or self.n * 256
         nbr = np.empty(cap, np.uint32)
         _abi.check(self._lib.gbmd_debug_list(self._h, _ptr(counts, C.c_uint32), _ptr(nbr, C.c_uint32), cap))
         offs = np.concatenate([[0], np.cumsum(counts.astype(np.int64))])
+        return counts, offs, nbr
+
+    def debug_list(self, max_total=None):
+        _, offs, nbr = self.debug_list_flat(max_total)
         return [np.sort(nbr[offs[i] : offs[i + 1]]) for i in range(self.n)]
 
 

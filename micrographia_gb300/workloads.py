@@ -87,3 +87,46 @@ def config5(count, rate, base_seed=1, n_min=1024, n_max=1 << 20):
             init = make_init(_abi.INIT_FCC, n, temp, seed, 0.05)
         out.append((t, sys_, init))
     return out
+
+
+def _profile_run(name):
+    """Runs one small workload on cuda:0 so that a profiler can capture the kernels it exercises
+    (each run ends by itself within seconds):
+    - frames3d: the 3D liquid (FCC N = 2^20, rho 0.8442, T 0.72, skin 0.3), 20 steps, then three
+      frames (the energy/virial pass k_kicks<3> and a 200-bin RDF to r = 5, k_rdf<3>);
+    - loop3d: one 3D liquid of N = 32,000 stepped 512 times by the persistent step loop
+      (k_force_loop);
+    - batch: the first 256 of the 1024 batched 2D replicas, 300 steps in 100-step graphs
+      (k_bforce_list, k_bbuild_list)."""
+    from .engine import BatchEngine, ForceMode, GpuEngine3, init_state
+
+    if name == "frames3d":
+        sys3, spec = config2()
+        with GpuEngine3(sys3, None, ForceMode.verlet_with_skin(sys3, spec.n, 0.3), init=spec) as e:
+            e.step(20)
+            for _ in range(3):
+                f, _, _ = e.observe(rdf_bins=200, rdf_rmax=5.0)
+            print(f"frames3d: T {f.temperature:.4f} P {f.pressure:.4f}")
+    elif name == "loop3d":
+        n = 32_000
+        sys3 = System3(cube_for(n, 0.8442), 0.005, Pair.lj(2.5), [1.0])
+        spec = make_init(_abi.INIT_FCC, n, 0.72, 1, 0.05)
+        with GpuEngine3(sys3, None, ForceMode.verlet_with_skin(sys3, n, 0.3), init=spec) as e:
+            e.step(512)
+            print(f"loop3d: {e.launch_count()} launches, rebuilds {e.read_list_stats()[0]}")
+    elif name == "batch":
+        cfg = config4()[:256]
+        systems = [s for s, _ in cfg]
+        states = [init_state(s, sp.recipe, sp.n, sp.t, sp.seed, sp.jitter) for s, sp in cfg]
+        with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.6), block_steps=100) as b:
+            b.step(300)
+            b.wait()
+            print(f"batch: {sum(st.n() for st in states)} particles, stats {b.stats()}")
+    else:
+        raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d or batch")
+
+
+if __name__ == "__main__":
+    import sys
+
+    _profile_run(sys.argv[1] if len(sys.argv) > 1 else "")

@@ -205,6 +205,22 @@ int64_t oracle_verlet_list(const gbmd_system* csys, const int64_t* pos, const ui
     return (int64_t)off;
 }
 
+// The lists of the particles idx[0..m) only, packed like oracle_verlet_list.
+int64_t oracle_verlet_list_of(const gbmd_system* csys, const int64_t* pos, const uint32_t* species, uint64_t n, double skin,
+                              const uint32_t* idx, uint64_t m, int threads, uint32_t* counts, uint32_t* nbr, uint64_t cap) {
+    System sys = System::from_c(*csys);
+    State s = make_state_pos(sys.dim, pos, species, n);
+    auto lists = verlet_lists_of(sys, s, skin, idx, m, threads > 0 ? threads : 1);
+    uint64_t off = 0;
+    for (size_t q = 0; q < m; q++) {
+        counts[q] = (uint32_t)lists[q].size();
+        if (off + lists[q].size() > cap) return -1;
+        std::memcpy(nbr + off, lists[q].data(), lists[q].size() * 4);
+        off += lists[q].size();
+    }
+    return (int64_t)off;
+}
+
 // ---- engines
 void* oracle_engine_create(const gbmd_system* csys, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint64_t n, int use_f64,
                            int fast, int int_tables, int threads) {
@@ -245,6 +261,13 @@ double oracle_engine_kicks(void* h, int32_t* kicks) {
     double pe = e->f32 ? e->f32->forces(k) : e->f64->forces(k);
     std::memcpy(kicks, k.data(), k.size() * 4);
     return pe;
+}
+// The kicks IntEngine's forces() gives the particles idx[0..m) of the engine's state (the
+// reference loop on those particles only).
+void oracle_engine_kicks_of(void* h, const uint32_t* idx, uint64_t m, int32_t* kicks) {
+    Engine* e = (Engine*)h;
+    if (e->f32) e->f32->forces_of(idx, m, kicks);
+    else e->f64->forces_of(idx, m, kicks);
 }
 void oracle_engine_state(void* h, int64_t* pos, int32_t* vel, uint32_t* species) {
     State& s = ((Engine*)h)->state();

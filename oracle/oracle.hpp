@@ -1048,12 +1048,90 @@ template <typename F> struct IntEngine {
         return {std::max(c[0], cells[0]), std::max(c[1], cells[1]), 1};
     }
 
+    // The kick on particle i and its share of the potential energy: the body of the reference
+    // loop over the 3^d neighbouring cells (int_engine.rs:144-243 / int_engine3.rs:56-128), with
+    // the soft walls' forces on i added into wf.
+    void force_on(size_t i, const CellList& cl, const uint32_t* nc, const double* b, int32_t* kout, double* pe_out, double* wf) const {
+        int d = sys.dim;
+        int ns = sys.species();
+        const int64_t* pi = &state.pos[d * i];
+        uint32_t si = state.species[i];
+        F c = kick_c[si];
+        uint32_t cc[3] = {0, 0, 0};
+        for (int a = 0; a < d; a++) cc[a] = cell_of(to_f64(pi[a]), b[a], nc[a]);
+        int32_t k[3] = {0, 0, 0};
+        F pe_i = (F)0;
+        double pe_i64 = 0.0;
+        int oz_n = d == 3 ? 3 : 1;
+        for (int oz = 0; oz < oz_n; oz++) {
+            uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
+            for (int oy = 0; oy < 3; oy++) {
+                uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
+                for (int ox = 0; ox < 3; ox++) {
+                    uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
+                    uint32_t cell = (z * nc[1] + y) * nc[0] + x;
+                    for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
+                        size_t j = cl.items[q];
+                        if (j == i) continue;
+                        const int64_t* pj = &state.pos[d * j];
+                        if (!sys.interact_across(pi, pj)) continue; // int_engine.rs:161-163
+                        int64_t dd[3];
+                        for (int a = 0; a < d; a++) dd[a] = sys.periodic(a) ? min_image(pi[a], pj[a], sys.box[a]) : pj[a] - pi[a]; // int_engine.rs:118-120
+                        if (tables) {
+                            int32_t kk[3];
+                            if (tables->kick(si, state.species[j], dd, d, kk)) {
+                                for (int a = 0; a < d; a++) k[a] = wadd(k[a], kk[a]);
+                                double r2 = 0.0;
+                                for (int a = 0; a < d; a++) r2 += to_f64(dd[a]) * to_f64(dd[a]);
+                                pe_i64 += sys.pair(si, state.species[j]).energy(r2);
+                            }
+                            continue;
+                        }
+                        F f[3];
+                        bool ok = true;
+                        for (int a = 0; a < d; a++) ok = ok && Real<F>::sep(dd[a], &f[a]);
+                        if (!ok) continue;
+                        F fr, u;
+                        if (consts[si * ns + state.species[j]].eval(f, d, &fr, &u)) {
+                            F aa = -fr * c;
+                            for (int a = 0; a < d; a++) k[a] = wadd(k[a], Real<F>::round_to_i32(aa * f[a]));
+                            pe_i += u;
+                        }
+                    }
+                }
+            }
+        }
+        // soft walls (int_engine.rs:203-227, int_engine3.rs:107-126): WCA in the distance to
+        // the wall, in F, its kick rounded like a pair's
+        double wall_pe = 0.0;
+        for (int a = 0; a < d; a++) {
+            if (sys.periodic(a)) continue;
+            for (int side = 0; side < 2; side++) {
+                if (sys.wall_kind[a][side] != GBMD_WALL_SOFT) continue;
+                const int64_t dw = side == 0 ? pi[a] : sys.box[a] - pi[a];
+                F df;
+                if (!Real<F>::sep(dw, &df)) continue;
+                if (df < Real<F>::from_f64(SOFT_RC)) {
+                    const F one = Real<F>::from_f64(1.0);
+                    const F s2 = one / (df * df);
+                    const F s6 = s2 * s2 * s2;
+                    const F f = Real<F>::from_f64(24.0) * s6 * (Real<F>::from_f64(2.0) * s6 - one) / df;
+                    const int32_t kw = Real<F>::round_to_i32(f * c);
+                    k[a] = wadd(k[a], side == 0 ? kw : wneg(kw));
+                    wf[2 * a + side] += (double)f;
+                    wall_pe += (double)(Real<F>::from_f64(4.0) * s6 * (s6 - one) + one);
+                }
+            }
+        }
+        for (int a = 0; a < d; a++) kout[a] = k[a];
+        *pe_out = (tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i) + wall_pe;
+    }
+
     // IntEngine::forces (int_engine.rs:130-251) / IntEngine3::forces (int_engine3.rs:48-131):
     // the reference loop over the 3^d neighbouring cells of each particle, or the fast path.
     double forces(std::vector<int32_t>& kicks) {
         int d = sys.dim;
         size_t n = state.n();
-        int ns = sys.species();
         kicks.assign(d * n, 0);
         auto cl_dims = present_cells();
         double pe = 0.0;
@@ -1068,80 +1146,26 @@ template <typename F> struct IntEngine {
 #pragma omp parallel for schedule(dynamic, 256) num_threads(threads) if (threads > 1)
         for (long long ii = 0; ii < (long long)n; ii++) {
             size_t i = (size_t)ii;
-            const int64_t* pi = &state.pos[d * i];
-            uint32_t si = state.species[i];
-            F c = kick_c[si];
-            uint32_t cc[3] = {0, 0, 0};
-            for (int a = 0; a < d; a++) cc[a] = cell_of(to_f64(pi[a]), b[a], nc[a]);
-            int32_t k[3] = {0, 0, 0};
-            F pe_i = (F)0;
-            double pe_i64 = 0.0;
-            int oz_n = d == 3 ? 3 : 1;
-            for (int oz = 0; oz < oz_n; oz++) {
-                uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
-                for (int oy = 0; oy < 3; oy++) {
-                    uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
-                    for (int ox = 0; ox < 3; ox++) {
-                        uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
-                        uint32_t cell = (z * nc[1] + y) * nc[0] + x;
-                        for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
-                            size_t j = cl.items[q];
-                            if (j == i) continue;
-                            const int64_t* pj = &state.pos[d * j];
-                            if (!sys.interact_across(pi, pj)) continue; // int_engine.rs:161-163
-                            int64_t dd[3];
-                            for (int a = 0; a < d; a++) dd[a] = sys.periodic(a) ? min_image(pi[a], pj[a], sys.box[a]) : pj[a] - pi[a]; // int_engine.rs:118-120
-                            if (tables) {
-                                int32_t kk[3];
-                                if (tables->kick(si, state.species[j], dd, d, kk)) {
-                                    for (int a = 0; a < d; a++) k[a] = wadd(k[a], kk[a]);
-                                    double r2 = 0.0;
-                                    for (int a = 0; a < d; a++) r2 += to_f64(dd[a]) * to_f64(dd[a]);
-                                    pe_i64 += sys.pair(si, state.species[j]).energy(r2);
-                                }
-                                continue;
-                            }
-                            F f[3];
-                            bool ok = true;
-                            for (int a = 0; a < d; a++) ok = ok && Real<F>::sep(dd[a], &f[a]);
-                            if (!ok) continue;
-                            F fr, u;
-                            if (consts[si * ns + state.species[j]].eval(f, d, &fr, &u)) {
-                                F aa = -fr * c;
-                                for (int a = 0; a < d; a++) k[a] = wadd(k[a], Real<F>::round_to_i32(aa * f[a]));
-                                pe_i += u;
-                            }
-                        }
-                    }
-                }
-            }
-            // soft walls (int_engine.rs:203-227, int_engine3.rs:107-126): WCA in the distance to
-            // the wall, in F, its kick rounded like a pair's
-            double wall_pe = 0.0;
-            for (int a = 0; a < d; a++) {
-                if (sys.periodic(a)) continue;
-                for (int side = 0; side < 2; side++) {
-                    if (sys.wall_kind[a][side] != GBMD_WALL_SOFT) continue;
-                    const int64_t dw = side == 0 ? pi[a] : sys.box[a] - pi[a];
-                    F df;
-                    if (!Real<F>::sep(dw, &df)) continue;
-                    if (df < Real<F>::from_f64(SOFT_RC)) {
-                        const F one = Real<F>::from_f64(1.0);
-                        const F s2 = one / (df * df);
-                        const F s6 = s2 * s2 * s2;
-                        const F f = Real<F>::from_f64(24.0) * s6 * (Real<F>::from_f64(2.0) * s6 - one) / df;
-                        const int32_t kw = Real<F>::round_to_i32(f * c);
-                        k[a] = wadd(k[a], side == 0 ? kw : wneg(kw));
-                        wall_force[i][2 * a + side] += (double)f;
-                        wall_pe += (double)(Real<F>::from_f64(4.0) * s6 * (s6 - one) + one);
-                    }
-                }
-            }
-            for (int a = 0; a < d; a++) kicks[d * i + a] = k[a];
-            pe_part[i] = (tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i) + wall_pe;
+            force_on(i, cl, nc, b, &kicks[d * i], &pe_part[i], wall_force[i].data());
         }
         for (size_t i = 0; i < n; i++) pe += pe_part[i];
         return pe;
+    }
+
+    // The reference loop's kicks on the particles idx[0..m) only (what forces() gives them, the
+    // fast path included, which equals the loop: fast_path.rs:20-54): a sample of a system too
+    // large to evaluate whole within a test.
+    void forces_of(const uint32_t* idx, size_t m, int32_t* out) const {
+        int d = sys.dim;
+        auto cl_dims = present_cells();
+        CellList cl = build_cells(sys, state, cl_dims);
+        uint32_t nc[3] = {cl_dims[0], cl_dims[1], d == 3 ? cl_dims[2] : 1u};
+        double b[3] = {sys.box_f64(0), sys.box_f64(1), d == 3 ? sys.box_f64(2) : 1.0};
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads) if (threads > 1)
+        for (long long q = 0; q < (long long)m; q++) {
+            double pe_i, wf[6] = {0, 0, 0, 0, 0, 0};
+            force_on(idx[q], cl, nc, b, out + d * q, &pe_i, wf);
+        }
     }
 
     // int_engine.rs:253-344 / int_engine3.rs:138-184 (periodic): v += kick + g; the Andersen
@@ -1419,45 +1443,60 @@ inline float sep_or_far(int64_t d) {
     float f;
     return sep_f32(d, &f) ? f : 1e30f;
 }
-// Returns, for each particle (storage index), the sorted indices of its listed neighbours.
-inline std::vector<std::vector<uint32_t>> verlet_lists(const System& sys, const State& s, double skin) {
+// The sorted indices of particle i's listed neighbours, from a cell list of the list radius.
+inline std::vector<uint32_t> verlet_list_of(const System& sys, const State& s, const CellList& cl, const uint32_t* nc, size_t i, double skin) {
     int d = sys.dim;
-    size_t n = s.n();
-    auto dims = sys.cells_for(sys.rc_max() + skin);
-    CellList cl = build_cells(sys, s, dims);
-    uint32_t nc[3] = {dims[0], dims[1], d == 3 ? dims[2] : 1u};
-    std::vector<std::vector<uint32_t>> out(n);
-    for (size_t i = 0; i < n; i++) {
-        uint32_t key = cl.keys[i];
-        uint32_t cc[3] = {key % nc[0], (key / nc[0]) % nc[1], key / (nc[0] * nc[1])};
-        const int64_t* pi = &s.pos[d * i];
-        std::vector<uint32_t> seen;
-        int oz_n = d == 3 ? 3 : 1;
-        for (int oz = 0; oz < oz_n; oz++) {
-            uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
-            for (int oy = 0; oy < 3; oy++) {
-                uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
-                for (int ox = 0; ox < 3; ox++) {
-                    uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
-                    uint32_t cell = (z * nc[1] + y) * nc[0] + x;
-                    // a 3-cell-wide axis visits a cell once per offset; count each cell once
-                    if (std::find(seen.begin(), seen.end(), cell) != seen.end()) continue;
-                    seen.push_back(cell);
-                    for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
-                        uint32_t j = cl.items[q];
-                        if (j == i) continue;
-                        const int64_t* pj = &s.pos[d * j];
-                        float f[3] = {0.0f, 0.0f, 0.0f};
-                        for (int a = 0; a < d; a++) f[a] = sep_or_far(min_image(pi[a], pj[a], sys.box[a]));
-                        float r2 = f[0] * f[0] + f[1] * f[1];
-                        if (d == 3) r2 = r2 + f[2] * f[2];
-                        if (r2 < pair_list_r2(sys, s.species[i], s.species[j], skin)) out[i].push_back(j);
-                    }
+    uint32_t key = cl.keys[i];
+    uint32_t cc[3] = {key % nc[0], (key / nc[0]) % nc[1], key / (nc[0] * nc[1])};
+    const int64_t* pi = &s.pos[d * i];
+    std::vector<uint32_t> out;
+    std::vector<uint32_t> seen;
+    int oz_n = d == 3 ? 3 : 1;
+    for (int oz = 0; oz < oz_n; oz++) {
+        uint32_t z = d == 3 ? (cc[2] + nc[2] + (uint32_t)oz - 1) % nc[2] : 0;
+        for (int oy = 0; oy < 3; oy++) {
+            uint32_t y = (cc[1] + nc[1] + (uint32_t)oy - 1) % nc[1];
+            for (int ox = 0; ox < 3; ox++) {
+                uint32_t x = (cc[0] + nc[0] + (uint32_t)ox - 1) % nc[0];
+                uint32_t cell = (z * nc[1] + y) * nc[0] + x;
+                // a 3-cell-wide axis visits a cell once per offset; count each cell once
+                if (std::find(seen.begin(), seen.end(), cell) != seen.end()) continue;
+                seen.push_back(cell);
+                for (uint32_t q = cl.start[cell]; q < cl.start[cell + 1]; q++) {
+                    uint32_t j = cl.items[q];
+                    if (j == i) continue;
+                    const int64_t* pj = &s.pos[d * j];
+                    float f[3] = {0.0f, 0.0f, 0.0f};
+                    for (int a = 0; a < d; a++) f[a] = sep_or_far(min_image(pi[a], pj[a], sys.box[a]));
+                    float r2 = f[0] * f[0] + f[1] * f[1];
+                    if (d == 3) r2 = r2 + f[2] * f[2];
+                    if (r2 < pair_list_r2(sys, s.species[i], s.species[j], skin)) out.push_back(j);
                 }
             }
         }
-        std::sort(out[i].begin(), out[i].end());
     }
+    std::sort(out.begin(), out.end());
+    return out;
+}
+// Returns, for each particle (storage index), the sorted indices of its listed neighbours.
+inline std::vector<std::vector<uint32_t>> verlet_lists(const System& sys, const State& s, double skin) {
+    auto dims = sys.cells_for(sys.rc_max() + skin);
+    CellList cl = build_cells(sys, s, dims);
+    uint32_t nc[3] = {dims[0], dims[1], sys.dim == 3 ? dims[2] : 1u};
+    std::vector<std::vector<uint32_t>> out(s.n());
+    for (size_t i = 0; i < s.n(); i++) out[i] = verlet_list_of(sys, s, cl, nc, i, skin);
+    return out;
+}
+// The lists of the particles idx[0..m) only (a sample of a system too large to list whole
+// within a test), in parallel.
+inline std::vector<std::vector<uint32_t>> verlet_lists_of(const System& sys, const State& s, double skin, const uint32_t* idx, size_t m,
+                                                          int threads) {
+    auto dims = sys.cells_for(sys.rc_max() + skin);
+    CellList cl = build_cells(sys, s, dims);
+    uint32_t nc[3] = {dims[0], dims[1], sys.dim == 3 ? dims[2] : 1u};
+    std::vector<std::vector<uint32_t>> out(m);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads) if (threads > 1)
+    for (long long q = 0; q < (long long)m; q++) out[q] = verlet_list_of(sys, s, cl, nc, idx[q], skin);
     return out;
 }
 // ForceMode::verlet_with_skin (engine.rs:130-141) / verlet3_with_skin (engine3.rs:61-68),

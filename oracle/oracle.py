@@ -50,11 +50,13 @@ _SIGS = [
     ("oracle_cell_list", C.c_int, [SYS, I64P, C.c_uint64, U32P, U32P, U32P, U32P]),
     ("oracle_verlet_cap", C.c_uint32, [SYS, C.c_uint64, C.c_double]),
     ("oracle_verlet_list", C.c_int64, [SYS, I64P, U32P, C.c_uint64, C.c_double, U32P, U32P, C.c_uint64]),
+    ("oracle_verlet_list_of", C.c_int64, [SYS, I64P, U32P, C.c_uint64, C.c_double, U32P, C.c_uint64, C.c_int, U32P, U32P, C.c_uint64]),
     ("oracle_engine_create", VP, [SYS, I64P, I32P, U32P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("oracle_engine_destroy", None, [VP]),
     ("oracle_engine_step", None, [VP, C.c_uint64]),
     ("oracle_engine_reverse", None, [VP]),
     ("oracle_engine_kicks", C.c_double, [VP, I32P]),
+    ("oracle_engine_kicks_of", None, [VP, U32P, C.c_uint64, I32P]),
     ("oracle_engine_state", None, [VP, I64P, I32P, U32P]),
     ("oracle_engine_set_state", None, [VP, I64P, I32P, U32P]),
     ("oracle_engine_hash", C.c_uint64, [VP]),
@@ -191,6 +193,23 @@ def verlet_lists(sys, state, skin):
     return [nbr[offs[i] : offs[i + 1]].copy() for i in range(n)]
 
 
+def verlet_lists_of(sys, state, skin, idx, threads=1):
+    """The lists of the particles idx only (sorted neighbour indices each): a sample of a system
+    too large to list whole within a test."""
+    idx = np.ascontiguousarray(idx, np.uint32)
+    m = len(idx)
+    counts = np.empty(m, np.uint32)
+    cap = m * 512
+    nbr = np.empty(cap, np.uint32)
+    c = sys.to_c()
+    tot = lib().oracle_verlet_list_of(C.byref(c), _p(state.pos, C.c_int64), _p(state.species, C.c_uint32), state.n(), skin,
+                                      _p(idx, C.c_uint32), m, threads, _p(counts, C.c_uint32), _p(nbr, C.c_uint32), cap)
+    if tot < 0:
+        raise ValueError("list buffer too small")
+    offs = np.concatenate([[0], np.cumsum(counts.astype(np.int64))])
+    return [nbr[offs[q] : offs[q + 1]].copy() for q in range(m)]
+
+
 def pair_sums(sys, state):
     pe, w = C.c_double(), C.c_double()
     c = sys.to_c()
@@ -316,6 +335,13 @@ class IntEngine:
         k = np.empty((self.n, self.D), np.int32)
         pe = lib().oracle_engine_kicks(self._h, _p(k, C.c_int32))
         return k, pe
+
+    def kicks_of(self, idx):
+        """The kicks forces() gives the particles idx only (the reference loop on them)."""
+        idx = np.ascontiguousarray(idx, np.uint32)
+        k = np.empty((len(idx), self.D), np.int32)
+        lib().oracle_engine_kicks_of(self._h, _p(idx, C.c_uint32), len(idx), _p(k, C.c_int32))
+        return k
 
     @property
     def state(self):

@@ -188,3 +188,25 @@ def test_walls_builders_and_the_engine_refusal(engine_lib):
     cc.periodic = 0b11
     rc = engine_lib.gbmd_create(C.byref(cc), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
     assert rc == _abi.E_UNSUPPORTED and b"compartment" in engine_lib.gbmd_last_error()
+
+
+def test_static_binning_rejects_bad_grids_before_any_device_work(engine_lib):
+    """gbmd_bin_cells_static validates its arguments on the host: a cell grid whose product
+    wraps modulo 2^64 (2^22 x 2^22 x 2^20), a product of 2^32 - 1 or more, and a box length that
+    is not positive are each rejected with GBMD_E_INVALID before any CUDA call (so this runs
+    without a GPU; the device pointers are never touched)."""
+    from micrographia_gb300 import Pair, System, System3, box_for, cube_for
+
+    fake = C.c_void_p(16)
+    s3 = System3(cube_for(1000, 0.8), 0.005, Pair.lj(2.5), [1.0]).to_c()
+    for cells in [(1 << 22, 1 << 22, 1 << 20), (1 << 16, 1 << 16, 1), (70000, 70000, 1)]:
+        grid = (C.c_uint32 * 3)(*cells)
+        rc = engine_lib.gbmd_bin_cells_static(C.byref(s3), fake, 1000, grid, fake, fake, fake, None)
+        assert rc == _abi.E_INVALID, cells
+        assert b"too many cells" in engine_lib.gbmd_last_error()
+    s2 = System(box_for(1000, 0.7, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    c2 = s2.to_c()
+    c2.box_len[1] = 0
+    grid = (C.c_uint32 * 3)(10, 10, 1)
+    assert engine_lib.gbmd_bin_cells_static(C.byref(c2), fake, 1000, grid, fake, fake, fake, None) == _abi.E_INVALID
+    assert b"box" in engine_lib.gbmd_last_error()

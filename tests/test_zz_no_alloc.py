@@ -17,7 +17,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _bin_static(lib, abi, sys_, st, dims):
+def _bin_static(lib, abi, sys_, st, dims, default_stream=False):
     import torch
 
     n = st.n()
@@ -30,9 +30,11 @@ def _bin_static(lib, abi, sys_, st, dims):
     cells = (C.c_uint32 * 3)(*(list(dims) + [1] * (3 - len(dims))))
     csys = sys_.to_c()
     stream = torch.cuda.current_stream(dev)
-    abi.check(lib.gbmd_bin_cells_static(C.byref(csys), pos.data_ptr(), n, cells, keys.data_ptr(), start.data_ptr(), items.data_ptr(),
-                                        C.c_void_p(stream.cuda_stream)))
-    stream.synchronize()
+    torch.cuda.synchronize(dev)
+    handle = None if default_stream else C.c_void_p(stream.cuda_stream)
+    abi.check(lib.gbmd_bin_cells_static(C.byref(csys), pos.data_ptr() if n else None, n, cells, keys.data_ptr(), start.data_ptr(),
+                                        items.data_ptr(), handle))
+    torch.cuda.synchronize(dev)
     as_u32 = lambda t: t.cpu().numpy().view(np.uint32)
     return as_u32(keys)[:n], as_u32(start), as_u32(items)[:n]
 
@@ -69,12 +71,44 @@ def test_static_binning_matches_the_engine_on_two_calls_in_a_row():
     from micrographia_gb300 import State3
 
     st3 = State3(p3, np.zeros((n3, 3), np.int32), np.zeros(n3, np.uint32))
+    from oracle import oracle as O
+
     for sys_, st in [(s2, st2), (s3, st3)]:
         dims = sys_.cells_for(2.8)
         got = _bin_static(lib, _abi, sys_, st, dims)
         want = _bin_engine(sys_, st, dims)
         for g, w in zip(got, want):
             assert np.array_equal(g, w)
+        # and directly against md-ref's CellList::build restated (cells.rs:1-55)
+        for g, w in zip(got, O.cell_list(sys_, st, dims)):
+            assert np.array_equal(g, w)
+
+
+def test_static_binning_on_the_default_stream_and_with_no_particles():
+    """A call on the legacy default stream (stream NULL) gives the engine's binning; a call with
+    n = 0 writes only the cell starts, all zero."""
+    pytest.importorskip("torch")
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from micrographia_gb300 import Pair, State, System, _abi, box_for, build
+
+    build.build()
+    lib = _abi.lib()
+    rng = np.random.default_rng(11)
+    n = 30_000
+    sys_ = System(box_for(n, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    st = State(np.stack([rng.integers(0, sys_.box_len[a], n) for a in range(2)], 1).astype(np.int64), np.zeros((n, 2), np.int32),
+               np.zeros(n, np.uint32))
+    dims = sys_.cells_for(2.5)
+    got = _bin_static(lib, _abi, sys_, st, dims, default_stream=True)
+    want = _bin_engine(sys_, st, dims)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+    empty = State(np.zeros((0, 2), np.int64), np.zeros((0, 2), np.int32), np.zeros(0, np.uint32))
+    _, start, _ = _bin_static(lib, _abi, sys_, empty, dims)
+    assert start.shape == (int(np.prod(dims)) + 1,) and not start.any()
 
 
 def test_static_binning_rejects_sizes_beyond_its_maximum():
