@@ -141,6 +141,10 @@ typedef struct gbmd_system {
 #define GBMD_FLAG_BUILD_LANES(s) ((uint32_t)(s) << 4)
 /* bits 8-12 of flags: lanes per particle of the force step (1, 2, 4, 8 or 16; 0 chooses by size) */
 #define GBMD_FLAG_FORCE_LANES(s) ((uint32_t)(s) << 8)
+/* Half-shell lists (3D, one species): each pair listed once and its pair chain evaluated once,
+ * its kick mirrored onto the other particle through shared-memory row windows. The trajectory is
+ * the same as with full lists, bit for bit; on GB300 the full-list step is faster (the default). */
+#define GBMD_FLAG_HALF_LISTS 16384u /* bit 14 */
 
 typedef struct gbmd_options {
     int32_t mode;          /* GBMD_MODE_* */

@@ -23,6 +23,7 @@
 #include "common.cuh"
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "half.cuh"
 #include "sort.cuh"
 
 namespace gbmd {
@@ -357,6 +358,8 @@ struct gbmd_engine {
     uint64_t launches = 0;
     uint32_t last_rebuilds = 0;
     bool failed = false;
+    bool half = false;       // half-shell lists (k_build_half / k_force_half / k_leap_half)
+    int32_t* acc = nullptr;  // half-shell kick accumulators, 3 x int32 per slot, zero between steps
     int32_t* itab = nullptr; // all-integer kick tables (GBMD_ARITH_INT)
     double* ipair = nullptr;
     // observation scratch, kept between frames (freeing it would synchronise the whole device)
@@ -440,7 +443,7 @@ void free_all(gbmd_engine* e) {
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
                     e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1],
-                    e->obs_bins, e->obs_start, e->itab, e->ipair, e->ledger};
+                    e->obs_bins, e->obs_start, e->itab, e->ipair, e->ledger, e->acc};
     for (void* p : ptrs)
         if (p) cudaFreeAsync(p, e->st);
     if (e->st) cudaStreamDestroy(e->st);
@@ -473,8 +476,18 @@ static uint32_t list_build_lanes(const gbmd_engine* e) {
     return o ? o : build_lanes(e->n);
 }
 
-template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t s) {
+template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t s, bool full) {
     enqueue_bin<D>(e, s, e->P);
+    if constexpr (D == 3 && !MULTI) {
+        if (e->half && !full) {
+            k_build_half<<<blocks_for(e->n, 128), 128, 0, s>>>(e->P, (const Rec<3>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr,
+                                                               e->keys[e->sorted], e->start, e->relf, (Rec<3>*)e->pos[e->cur], e->vel,
+                                                               e->species, e->ids, (Rec<3>*)e->ref_pos, e->nbr, e->nbr_count, e->ctl,
+                                                               e->qpos[e->cur]);
+            note_launch();
+            return;
+        }
+    }
 #define GBMD_BUILD(SS)                                                                                                              \
     k_build_list<D, MULTI, SS><<<blocks_for((uint64_t)e->n * SS, 128), 128, 0, s>>>(                                               \
         e->P, (const Rec<D>*)e->pos_scr, e->vel_scr, e->species_scr, e->ids_scr, e->keys[e->sorted], e->start, e->relf,            \
@@ -491,15 +504,18 @@ template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t
 
 __global__ void k_set_cond(cudaGraphConditionalHandle h, const uint32_t* ctl) { cudaGraphSetConditional(h, ctl[0] ? 1u : 0u); }
 
-void enqueue_rebuild(gbmd_engine* e, cudaStream_t s) {
+// The list the engine steps with (half-shell lists on a half engine), or with `full` a full list
+// whatever the engine (the instruments and reversal walk full lists).
+void enqueue_rebuild(gbmd_engine* e, cudaStream_t s, bool full = false) {
     if (e->D == 2) {
-        if (e->multi) enqueue_rebuild_t<2, true>(e, s);
-        else enqueue_rebuild_t<2, false>(e, s);
+        if (e->multi) enqueue_rebuild_t<2, true>(e, s, full);
+        else enqueue_rebuild_t<2, false>(e, s, full);
     } else {
-        if (e->multi) enqueue_rebuild_t<3, true>(e, s);
-        else enqueue_rebuild_t<3, false>(e, s);
+        if (e->multi) enqueue_rebuild_t<3, true>(e, s, full);
+        else enqueue_rebuild_t<3, false>(e, s, full);
     }
 }
+__global__ void k_set_trigger(uint32_t* ctl) { ctl[0] = 1; }
 
 // Below these particle counts the force kernel runs 8 (4, 2) lanes per particle.
 constexpr uint32_t FORCE_SPLIT8_BELOW = 20000, FORCE_SPLIT4_BELOW = 65536, FORCE_SPLIT2_BELOW = 262144;
@@ -511,6 +527,21 @@ static uint32_t force_lanes(const gbmd_engine* e) {
     return e->n < FORCE_SPLIT8_BELOW ? 8u : (e->n < FORCE_SPLIT4_BELOW ? 4u : (e->n < FORCE_SPLIT2_BELOW ? 2u : 1u));
 }
 template <int D, bool MULTI, bool INT> void enqueue_force_a(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
+    if constexpr (D == 3 && !MULTI && !INT) {
+        if (e->half) {
+            const size_t smem = (size_t)e->P.win_cap * 12;
+            const uint32_t rows = e->P.nc[1] * e->P.nc[2];
+            if (e->P.pc[0].sigma2s == 0x1p56f)
+                k_force_half<true><<<rows, HALF_THREADS, smem, s>>>(e->P, e->qpos[e->cur], e->nbr, e->nbr_count, e->start, e->acc);
+            else
+                k_force_half<false><<<rows, HALF_THREADS, smem, s>>>(e->P, e->qpos[e->cur], e->nbr, e->nbr_count, e->start, e->acc);
+            k_leap_half<<<blocks_for(e->n, 256), 256, 0, s>>>(e->P, (const Rec<3>*)e->pos[e->cur], (Rec<3>*)e->pos[e->cur ^ 1],
+                                                             e->qpos[e->cur ^ 1], e->vel, (int4*)e->acc, (const Rec<3>*)e->ref_pos, e->ctl);
+            note_launch(2);
+            e->cur ^= 1;
+            return;
+        }
+    }
     if (e->verlet) {
         // sigma = 1 for every pair type (the common LJ case): compiled into the f32 chain
         bool sig1 = !INT;
@@ -682,7 +713,7 @@ cudaError_t enqueue_loop(gbmd_engine* e, cudaStream_t s) {
 // kernel's; fewer if the grid would not be resident.
 int setup_step_loop(gbmd_engine* e) {
     e->loop_lanes = 0;
-    if (!e->verlet || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath ||
+    if (!e->verlet || e->half || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath ||
         (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP))
         return GBMD_OK;
     // Larger systems' steps are long enough that the graph's per-step nodes cost less than the
@@ -847,6 +878,15 @@ int run_graph(gbmd_engine* e, int which) {
 // rebuilt only if the displacement trigger has fired since the last build (the same device flag
 // and conditional graph node the steps use), a cell list binned into the scratch state.
 int prepare_pairs_cond(gbmd_engine* e) {
+    if (e->half) {
+        // the instruments walk full lists: build one now, and have the next step rebuild the
+        // half-shell list it steps with (the trajectory does not depend on the storage order)
+        enqueue_rebuild(e, e->st, true);
+        k_set_trigger<<<1, 1, 0, e->st>>>(e->ctl);
+        note_launch();
+        GBMD_CUDA_TRY(cudaGetLastError());
+        return GBMD_OK;
+    }
     if (!e->verlet) {
         if (e->D == 2) enqueue_bin<2>(e, e->st, e->P);
         else enqueue_bin<3>(e, e->st, e->P);
@@ -1076,7 +1116,20 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         cap = e->opt.cap ? e->opt.cap : (uint32_t)std::ceil(sphere * std::max(2.0 * density, 1.2)) + 8;
     }
     fill_params(e->P, *sys, n, e->skin, cap, nc);
-    if (e->verlet && !(e->opt.flags & GBMD_FLAG_WHOLE_CELLS) && list_build_lanes(e) > 1)
+    if (e->verlet && e->D == 3 && !e->multi && e->opt.arith == GBMD_ARITH_F32 && (e->opt.flags & GBMD_FLAG_HALF_LISTS)) {
+        // Half-shell lists address a neighbour by its offset in its row of cells (16 bits): rows
+        // must stay far below 65,536 particles (the build reports an overflow otherwise). The
+        // force step's shared-memory windows hold six mean rows with a tenth to spare; rows
+        // beyond that accumulate in global memory.
+        const double mean_row = (double)n / ((double)nc[1] * nc[2]);
+        if (mean_row * 4.0 < 65536.0) {
+            e->half = true;
+            const uint32_t max_slots = (uint32_t)((55u * 1024u) / 12u); // four blocks per SM
+            e->P.half_lists = 1;
+            e->P.win_cap = std::min<uint32_t>(max_slots, (uint32_t)std::ceil(mean_row * HALF_WINDOWS * 1.1) + 64u);
+        }
+    }
+    if (e->verlet && !e->half && !(e->opt.flags & GBMD_FLAG_WHOLE_CELLS) && list_build_lanes(e) > 1)
         set_sub_buckets(e->P, sys->dim, (rc_max(*sys) + e->skin) * (1.0 + 1e-4));
     e->block_steps = e->opt.block_steps ? e->opt.block_steps : 64;
     if (e->opt.rescale_every) {
@@ -1113,6 +1166,13 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     if (e->verlet) {
         GBMD_TRY(allocT(e, &e->nbr, ((size_t)n + 31) / 32 * 32 * (((size_t)cap + 3) & ~(size_t)3)));
         GBMD_TRY(allocT(e, &e->nbr_count, n));
+    }
+    if (e->half) {
+        GBMD_TRY(allocT(e, &e->acc, 4 * (size_t)n));
+        GBMD_CUDA_TRY(cudaMemsetAsync(e->acc, 0, 16 * (size_t)n, e->st));
+        const int smem = (int)(e->P.win_cap * 12);
+        GBMD_CUDA_TRY(cudaFuncSetAttribute(k_force_half<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        GBMD_CUDA_TRY(cudaFuncSetAttribute(k_force_half<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     }
     GBMD_TRY(allocT(e, &e->ctl, 16));
     GBMD_TRY(allocT(e, &e->ledger, 2));
@@ -1651,6 +1711,33 @@ int gbmd_debug_list(gbmd_engine* e, uint32_t* counts, uint32_t* nbr, uint64_t nb
     auto slot = [&](size_t i, size_t k) { return ((i >> 5) * cap4 + (k & ~(size_t)3)) * 32 + ((i & 31) << 2) + (k & 3); };
     std::vector<uint32_t> slot_of(n);
     for (size_t s = 0; s < n; s++) slot_of[ids[s]] = (uint32_t)s;
+    if (e->half) {
+        // Half-shell lists hold each pair once, by window and offset in the neighbour's row:
+        // decode them to slots and return both ends' sets, as a full list would hold them.
+        const uint32_t nx = e->P.nc[0], ny = e->P.nc[1], nz = e->P.nc[2];
+        std::vector<uint32_t> keys((size_t)n), start((size_t)e->P.ncell + 1);
+        GBMD_CUDA_TRY(cudaMemcpy(keys.data(), e->keys[e->sorted], n * 4, cudaMemcpyDeviceToHost));
+        GBMD_CUDA_TRY(cudaMemcpy(start.data(), e->start, start.size() * 4, cudaMemcpyDeviceToHost));
+        std::vector<std::vector<uint32_t>> sets(n);
+        for (size_t s = 0; s < n; s++) {
+            const uint32_t row = keys[s] / nx, y = row % ny, z = row / ny;
+            for (size_t q = 0; q < cnt[s]; q++) {
+                const uint32_t ent = lst[slot(s, q)], w = (ent >> HALF_WIN_SHIFT) & 15u;
+                if (w >= HALF_WINDOWS) return fail(GBMD_E_INVALID, "corrupt half-shell list entry");
+                const uint32_t j = start[(size_t)half_window_row(ny, nz, y, z, w) * nx] + (ent & HALF_OFF_MASK);
+                if (j >= n) return fail(GBMD_E_INVALID, "corrupt half-shell list entry");
+                sets[ids[s]].push_back(ids[j]);
+                sets[ids[j]].push_back(ids[s]);
+            }
+        }
+        uint64_t off = 0;
+        for (size_t id = 0; id < n; id++) {
+            counts[id] = (uint32_t)sets[id].size();
+            if (off + sets[id].size() > nbr_cap) return fail(GBMD_E_INVALID, "nbr_cap too small");
+            for (uint32_t j : sets[id]) nbr[off++] = j;
+        }
+        return GBMD_OK;
+    }
     uint64_t off = 0;
     for (size_t id = 0; id < n; id++) {
         size_t s = slot_of[id];
