@@ -179,7 +179,7 @@ def cpu_baseline(seconds_budget=20.0, threads=None):
     sys3 = system3()
     s0 = O.fcc_maxwell(sys3, N_ATOMS, T0, SEED, jitter=0.05)
     e = O.IntEngine(sys3, s0, threads=threads)
-    e.step(1)  # warm-up
+    e.step(5)  # warm-up: 5 steps, as the reference's own bench (crates/bench/src/main.rs:288)
     t0 = time.perf_counter()
     done = 0
     while done < 1 or (time.perf_counter() - t0 < seconds_budget and done < 20):
@@ -196,7 +196,7 @@ def cpu_baseline(seconds_budget=20.0, threads=None):
         "unit": UNIT,
         "cores": threads,
         "kind": "port",
-        "sample": f"{done} full steps of the {N_ATOMS}-atom system after 1 warm-up step ({dt:.1f} s), IntEngine3<f32> reference loop",
+        "sample": f"{done} full steps of the {N_ATOMS}-atom system after 5 warm-up steps ({dt:.1f} s), IntEngine3<f32> reference loop",
         "single_thread": {"value": N_ATOMS / dt1, "unit": UNIT, "sample": f"1 full step on one thread ({dt1:.1f} s)"},
     }
 
@@ -241,10 +241,8 @@ def run_ours(args, world, rank, local, pg):
     stream = torch.cuda.ExternalStream(eng.stream())
 
     # warm-up: captures the graphs and settles the lists
-    ke0, pe0 = eng.energy()
     eng.step(args.warmup)
     eng.wait()
-    e_warm = sum(eng.energy())
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -264,7 +262,6 @@ def run_ours(args, world, rank, local, pg):
     launches = eng.launch_count() - l0
     ms = barrier_max(pg, ms)
     value = world * N_ATOMS * args.steps / (ms * 1e-3)
-    e_end = sum(eng.energy())
     rebuilds, overflow = eng.read_list_stats()
 
     # per-phase device times (CUDA events on the engine's stream) for the roofline
@@ -316,6 +313,10 @@ def run_ours(args, world, rank, local, pg):
     fp64_err = float(np.sqrt((d * d).sum() / (k64.astype(np.float64) ** 2).sum()))
     fp64_max = int(np.abs(d).max())
 
+    # energy drift (outside the timed regions): total energy per atom every 100 steps over 4000
+    # steps after 1000 more steps of equilibration, its least-squares slope per step and its range
+    energy = energy_drift(eng, equilibrate=1000, steps=4000, every=100) if not args.no_drift else None
+
     line = {
         "metric": METRIC,
         "value": value,
@@ -352,42 +353,80 @@ def run_ours(args, world, rank, local, pg):
             "force_ms": f_ms.value,
         },
         "phases": {"force_ms": f_ms.value, "rebuild_ms": r_ms.value, "rebuilds_in_200": nreb.value, "rebuilds_timed_run": rebuilds},
-        "energy": {"e0_per_atom": (ke0 + pe0) / N_ATOMS, "drift_per_atom_per_step": (e_end - e_warm) / N_ATOMS / args.steps},
+        "energy": energy,
         "fp64_force_error": {"rel_rms": fp64_err, "max_abs_kick_diff": fp64_max, "bar": 1e-5, "n_atoms": N_ATOMS,
                              "reference": "kicks of the f64 pair chain (IntEngine<f64>) on the device, gbmd_kicks_f64"},
         "overflow": overflow,
     }
     if clk:
         line["clocks"] = clk
+    eng.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
+    if not args.no_sub:
+        # the batched and served forms against the plain form, on this GPU (whole job: every
+        # rank runs them, units summed and times maxed over ranks)
+        line["batched"] = run_c4(args, world, rank, local, pg, steps=100, warmup=5, emit=False)
+        line["served"] = run_c5(args, world, rank, local, pg, requests=32, rate=64.0, emit=False)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
     return 0
 
 
-def run_c4(args, world, rank, local, pg):
+def energy_drift(eng, equilibrate, steps, every):
+    """Total energy per atom (IntEngine's on-step kinetic energy + the pair potential, FP64) sampled
+    every `every` steps over `steps` steps after `equilibrate` more: the least-squares slope per
+    atom per step, the range, and the reference's bar for its 3D liquid (energy per particle within
+    2e-3 over 5000 steps, crates/md/tests/three.rs:95-111)."""
+    import numpy as np
+
+    eng.step(equilibrate)
+    ts, es = [], []
+    for k in range(steps // every + 1):
+        if k:
+            eng.step(every)
+        ke, pe = eng.energy()
+        ts.append(k * every)
+        es.append((ke + pe) / eng.n)
+    t = np.array(ts, np.float64)
+    e = np.array(es, np.float64)
+    slope = float(np.polyfit(t, e, 1)[0])
+    return {
+        "e_per_atom_start": float(e[0]),
+        "slope_per_atom_per_step": slope,
+        "range_per_atom": float(e.max() - e.min()),
+        "steps": steps,
+        "after_equilibration_steps": equilibrate,
+        "samples": len(es),
+        "bar": "range per atom < 2e-3 over 5000 steps (crates/md/tests/three.rs:95-111)",
+        "within_bar": bool(e.max() - e.min() < 2e-3),
+    }
+
+
+def run_c4(args, world, rank, local, pg, steps=None, warmup=None, emit=True):
     """1024 uneven 2D systems; batched (one persistent launch per step, 100-step
-    graphs) against the plain form (one engine per system, each on its own stream)."""
+    graphs) against the plain form: one engine per system, run (a) one after another, each to the
+    end of its steps before the next starts, and (b) all at once, each on its own stream. Every
+    arm is warmed up with the same steps first, so that no graph is captured while timed."""
     import torch
 
     from micrographia_gb300 import BatchEngine, ForceMode, GpuEngine, init_state, workloads
 
     torch.cuda.set_device(local)
+    K = steps or args.steps
+    W = warmup or args.warmup
     cfg = workloads.config4(args.systems)
     systems = [s for s, _ in cfg]
     states = [init_state(s, sp.recipe, sp.n, sp.t, sp.seed, sp.jitter) for s, sp in cfg]
     total = sum(st.n() for st in states)
     mode = ForceMode.verlet_with_skin(None, 0, SKIN)
-    K = args.steps
 
     # the skin autotuner times 0.3..0.7 sigma on these states (outside the timed region)
     batch = BatchEngine(systems, states, mode, block_steps=100, device=local, tune_skin=True)
     skin = batch.skin
     mode = ForceMode.verlet_with_skin(None, 0, skin)
     bstream = torch.cuda.ExternalStream(batch.stream())
-    batch.step(args.warmup)
+    batch.step(W)
     batch.wait()
     clocks = ClockSampler(local)
     clocks.start()
@@ -402,35 +441,43 @@ def run_c4(args, world, rank, local, pg):
     batch.wait()
     clk = clocks.stop()
     l1, r1 = batch.stats()
+    batch.step(2 * K)  # (untimed: to the plain arms' step count, for the identity check)
+    batch.wait()
     from micrographia_gb300 import replicas
 
     # replicas: every rank runs the whole batch; units summed, time maxed over ranks
     units, secs = replicas.aggregate(pg, total * K, ms_b * 1e-3)
     value = units / secs
-    # bit-exactness spot check: the first and last replicas against their plain runs
-    checks = {}
     plain = [GpuEngine(s, st, mode, device=local) for s, st in zip(systems, states)]
     for e in plain:
-        e.step(args.warmup)
+        e.step(W)
+        e.step(K)  # warm-up: every graph the timed steps replay is captured here
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for e in plain:
         e.step(K)
     torch.cuda.synchronize()
-    t_plain = time.perf_counter() - t0
-    value_plain = total * K / t_plain
+    t_conc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for e in plain:
+        e.step(K)
+        e.wait()
+    t_serial = time.perf_counter() - t0
+    value_conc = total * K / t_conc
+    value_serial = total * K / t_serial
+    checks = {}
     for k in (0, len(systems) - 1):
         checks[k] = plain[k].read_state() == batch.read_system(k)
     for e in plain:
         e.close()
     batch.close()
-    line = {
+    rec = {
         "metric": METRIC,
         "value": value,
         "unit": UNIT,
         "n_gpus": world,
         "steps": K,
-        "warmup": args.warmup,
+        "warmup": W,
         "ms_per_step": ms_b / K,
         "higher_is_better": True,
         "scaling": "weak",
@@ -440,21 +487,24 @@ def run_c4(args, world, rank, local, pg):
         "config": {
             "workload": f"{len(systems)} independent 2D LJ systems, N log-uniform [256, 65536] (sum {total}), rho U[0.3, 0.8], T U[0.5, 1.5], rc 2.5, dt 0.005",
             "skin": skin,
-            "skin_choice": "autotuned: fastest of 0.3..0.7 on two timed 100-step blocks per candidate; the plain form uses the same skin",
+            "skin_choice": "autotuned: fastest of 0.3..0.7 on two timed 100-step blocks per candidate; the plain forms use the same skin",
             "form": "batched: one persistent force launch per step over all systems, 100-step CUDA graphs",
-            "plain_value": value_plain,
-            "plain_form": "one engine per system, each stepped on its own stream, all issued back to back",
-            "batched_over_plain": value / value_plain,
+            "plain_value": value_serial,
+            "plain_form": "one engine per system, the systems run one after another (each synchronised before the next starts)",
+            "batched_over_plain": value / value_serial,
+            "plain_concurrent_value": value_conc,
+            "plain_concurrent_form": "one engine per system, each stepped on its own stream, all issued back to back",
+            "batched_over_plain_concurrent": value / value_conc,
             "replicas_bit_identical_to_plain": checks,
             "rebuilds": r1 - r0,
         },
         "gpu_launches": l1 - l0,
     }
     if clk:
-        line["clocks"] = clk
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    return 0
+        rec["clocks"] = clk
+    if rank == 0 and emit:
+        print(json.dumps(rec), flush=True)
+    return rec
 
 
 def run_c3(args, world, rank, local, pg):
@@ -529,7 +579,7 @@ def _pct(xs, q):
     return xs[k]
 
 
-def run_c5(args, world, rank, local, pg):
+def run_c5(args, world, rank, local, pg, requests=None, rate=None, emit=True):
     """A Poisson stream of 2D/3D requests (N log-uniform in [1024, 2^20], 2000 steps,
     a frame of T, P and a 200-bin RDF every 100 steps) served under a 64 GB HBM budget, against
     the same requests run one after another in plain form. Per-frame latency: the wall time a
@@ -543,8 +593,10 @@ def run_c5(args, world, rank, local, pg):
 
     torch.cuda.set_device(local)
     # replicas: the request stream is dealt out by rank (request k to rank k mod N)
-    reqs = replicas.shard(workloads.config5(args.requests, args.rate), rank, world)
-    steps = args.steps
+    n_req = requests or args.requests
+    lam = rate or args.rate
+    reqs = replicas.shard(workloads.config5(n_req, lam), rank, world)
+    steps = 2000
 
     # frame times per request (by its place in the stream): served deliveries, and the solo
     # schedule S_k = time from the start of service to frame k when the request runs alone
@@ -634,7 +686,7 @@ def run_c5(args, world, rank, local, pg):
         "dtype": "f32+int64",
         "data": "synthetic",
         "config": {
-            "workload": f"{args.requests} requests (dealt out over {world} GPU(s)), Poisson arrivals at {args.rate}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget",
+            "workload": f"{n_req} requests (dealt out over {world} GPU(s)), Poisson arrivals at {lam}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget",
             "form": "served: continuous batching (each admitted request on its own stream, intervals overlapped)",
             "makespan_s": mk_serve,
             "frame_latency_p50_ms": 1e3 * _pct(lat_serve, 50),
@@ -652,9 +704,9 @@ def run_c5(args, world, rank, local, pg):
             "frames": len(lat_serve),
         },
     }
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def main():
@@ -665,6 +717,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="default line without the batched and served sub-records")
+    ap.add_argument("--no-drift", action="store_true", help="default line without the energy-drift run")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="atoms (default 1,048,576; smaller only for profiling)")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2", help="c2 (default): 3D N=1M; c3: 2D slab 16.7M; c4: 1024 replicas; c5: served stream")
     ap.add_argument("--requests", type=int, default=48, help="requests for --config c5")
@@ -682,9 +736,11 @@ def main():
 
         build.build()
         if args.config == "c4":
-            rc = run_c4(args, world, rank, local, pg)
+            run_c4(args, world, rank, local, pg)
+            rc = 0
         elif args.config == "c5":
-            rc = run_c5(args, world, rank, local, pg)
+            run_c5(args, world, rank, local, pg)
+            rc = 0
         elif args.config == "c3":
             rc = run_c3(args, world, rank, local, pg)
         else:

@@ -276,6 +276,13 @@ int gbmd_launch_count(gbmd_engine* e, uint64_t* launches);
  * stream; returns the mean milliseconds of one force launch and of one list rebuild (all its
  * kernels), and how many rebuilds ran. The state advances by `steps` steps. */
 int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* rebuild_ms, uint32_t* rebuilds);
+/* The same for the persistent step loop of small systems (no counterpart in the reference: its
+ * engine has no such loop): at least `steps` steps taken by direct cooperative launches of the
+ * loop (each stops at the rebuild trigger or after the engine's block of steps), the list
+ * rebuilt between them where the trigger fired. Returns the steps taken, the mean milliseconds
+ * per step inside the loop launches and their count; GBMD_E_UNSUPPORTED when the engine does
+ * not use the loop. */
+int gbmd_time_loop(gbmd_engine* e, uint32_t steps, uint32_t* taken, double* ms_per_step, uint32_t* launches);
 
 /* ---- Introspection of the cell binning and the Verlet list (parity tests) ---- */
 
@@ -367,6 +374,9 @@ int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds);
 int gbmd_batch_read_ledger(gbmd_batch* b, uint32_t k, double* energy, double* impulse, uint64_t* hits);
 /* The batch's Verlet skin in sigma (the one GBMD_FLAG_TUNE_SKIN chose, or the one asked for). */
 int gbmd_batch_skin(gbmd_batch* b, double* skin);
+/* Per-phase device timing of a batch, as gbmd_time_phases: `steps` steps as individual launches
+ * with CUDA events around the force launch and the (all-system) list rebuild. */
+int gbmd_batch_time_phases(gbmd_batch* b, uint32_t steps, double* force_ms, double* rebuild_ms, uint32_t* rebuilds);
 int gbmd_batch_destroy(gbmd_batch* b);
 
 /* FNV-1a hash of an id-ordered state held on the host: State::hash (system.rs:460-477) for

@@ -220,6 +220,7 @@ SIGNATURES = [
     ("gbmd_stream", C.c_int, [VP, P(VP)]),
     ("gbmd_launch_count", C.c_int, [VP, _U64P]),
     ("gbmd_time_phases", C.c_int, [VP, C.c_uint32, _DP, _DP, _U32P]),
+    ("gbmd_time_loop", C.c_int, [VP, C.c_uint32, _U32P, _DP, _U32P]),
     ("gbmd_debug_bin", C.c_int, [VP, _U32P, _U32P, _U32P, _U32P, _U32P]),
     ("gbmd_debug_list", C.c_int, [VP, _U32P, _U32P, C.c_uint64]),
     ("gbmd_debug_barrier_timeout", C.c_int, [VP, C.c_uint32]),
@@ -233,6 +234,7 @@ SIGNATURES = [
     ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
     ("gbmd_batch_stats", C.c_int, [VP, _U64P, _U32P]),
     ("gbmd_batch_skin", C.c_int, [VP, C.POINTER(C.c_double)]),
+    ("gbmd_batch_time_phases", C.c_int, [VP, C.c_uint32, _DP, _DP, _U32P]),
     ("gbmd_batch_read_ledger", C.c_int, [VP, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double), _U64P]),
     ("gbmd_read_ledger", C.c_int, [VP, C.POINTER(C.c_double), C.POINTER(C.c_double), _U64P]),
     ("gbmd_batch_destroy", C.c_int, [VP]),

@@ -756,6 +756,48 @@ int gbmd_batch_step(gbmd_batch* b, uint64_t steps) {
     return GBMD_OK;
 }
 
+int gbmd_batch_time_phases(gbmd_batch* b, uint32_t steps, double* force_ms, double* rebuild_ms, uint32_t* rebuilds) {
+    if (!b) return fail(GBMD_E_INVALID, "null batch");
+    if (b->failed) return fail(GBMD_E_OVERFLOW, "the batch is in a failed state (a list overflowed)");
+    GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
+    cudaEvent_t e0, e1, e2;
+    GBMD_CUDA_TRY(cudaEventCreate(&e0));
+    GBMD_CUDA_TRY(cudaEventCreate(&e1));
+    GBMD_CUDA_TRY(cudaEventCreate(&e2));
+    double tf = 0.0, tr = 0.0;
+    uint32_t nr = 0;
+    const uint64_t l0 = launch_total();
+    for (uint32_t k = 0; k < steps; k++) {
+        uint32_t flag = 0;
+        GBMD_CUDA_TRY(cudaMemcpyAsync(&flag, b->ctl, 4, cudaMemcpyDeviceToHost, b->st));
+        GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
+        GBMD_CUDA_TRY(cudaEventRecord(e0, b->st));
+        if (flag) {
+            benqueue_rebuild(b, b->st);
+            nr++;
+        }
+        GBMD_CUDA_TRY(cudaEventRecord(e1, b->st));
+        benqueue_force(b, b->st);
+        GBMD_CUDA_TRY(cudaEventRecord(e2, b->st));
+        GBMD_CUDA_TRY(cudaEventSynchronize(e2));
+        float m1 = 0.f, m2 = 0.f;
+        cudaEventElapsedTime(&m1, e0, e1);
+        cudaEventElapsedTime(&m2, e1, e2);
+        if (flag) tr += m1;
+        tf += m2;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    // (gbmd_batch_stats counts each rebuild's kernels from the device's rebuild count)
+    b->launches += launch_total() - l0 - (uint64_t)nr * b->body_launches;
+    if (force_ms) *force_ms = steps ? tf / steps : 0.0;
+    if (rebuild_ms) *rebuild_ms = nr ? tr / nr : 0.0;
+    if (rebuilds) *rebuilds = nr;
+    GBMD_CUDA_TRY(cudaGetLastError());
+    return bcheck(b);
+}
+
 int gbmd_batch_sync(gbmd_batch* b) {
     if (!b) return fail(GBMD_E_INVALID, "null batch");
     GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));

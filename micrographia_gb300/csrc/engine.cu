@@ -1643,6 +1643,52 @@ int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* r
     return check_ctl(e);
 }
 
+int gbmd_time_loop(gbmd_engine* e, uint32_t steps, uint32_t* taken, double* ms_per_step, uint32_t* launches) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (!e->loop_lanes) return fail(GBMD_E_UNSUPPORTED, "this engine does not step through the persistent loop");
+    GBMD_TRY(gbmd_sync(e));
+    cudaEvent_t a, b;
+    GBMD_CUDA_TRY(cudaEventCreate(&a));
+    GBMD_CUDA_TRY(cudaEventCreate(&b));
+    uint32_t total = 0, nl = 0;
+    double t = 0.0;
+    int rc = GBMD_OK;
+    while (total < steps) {
+        uint32_t c[16];
+        GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, sizeof(c), cudaMemcpyDeviceToHost, e->st));
+        GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+        if (c[0]) enqueue_rebuild(e, e->st);
+        k_loop_begin<<<1, 1, 0, e->st>>>(e->ctl);
+        note_launch();
+        GBMD_CUDA_TRY(cudaEventRecord(a, e->st));
+        GBMD_CUDA_TRY(enqueue_loop(e, e->st));
+        GBMD_CUDA_TRY(cudaEventRecord(b, e->st));
+        GBMD_CUDA_TRY(cudaEventSynchronize(b));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        GBMD_CUDA_TRY(cudaMemcpyAsync(c, e->ctl, sizeof(c), cudaMemcpyDeviceToHost, e->st));
+        GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+        t += ms;
+        nl++;
+        total += c[CTL_LOOP_DONE];
+        if (c[CTL_LOOP_ERR] || c[CTL_LOOP_DONE] == 0) {
+            rc = check_ctl(e);
+            if (rc == GBMD_OK) rc = fail(GBMD_E_TIMEOUT, "the persistent loop took no step");
+            break;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    e->steps += total;
+    e->clock += total;
+    e->tcount += total;
+    if (taken) *taken = total;
+    if (ms_per_step) *ms_per_step = total ? t / total : 0.0;
+    if (launches) *launches = nl;
+    if (rc != GBMD_OK) return rc;
+    return check_ctl(e);
+}
+
 int gbmd_debug_bin(gbmd_engine* e, const uint32_t* cells, uint32_t* keys, uint32_t* start, uint32_t* items, uint32_t* order) {
     if (!e || !cells) return fail(GBMD_E_INVALID, "null argument");
     Params P = e->P;

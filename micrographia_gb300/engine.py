@@ -231,6 +231,20 @@ class _Engine:
         _abi.check(self._lib.gbmd_stream(self._h, C.byref(s)))
         return s.value
 
+    def time_phases(self, steps):
+        """`steps` steps as individual launches with CUDA events around each phase:
+        (mean ms of one force step, mean ms of one list rebuild, rebuilds)."""
+        f, r, n = C.c_double(), C.c_double(), C.c_uint32()
+        _abi.check(self._lib.gbmd_time_phases(self._h, steps, C.byref(f), C.byref(r), C.byref(n)))
+        return f.value, r.value, n.value
+
+    def time_loop(self, steps):
+        """At least `steps` steps by direct launches of the persistent step loop (small systems):
+        (steps taken, mean ms per step inside the loop launches, loop launches)."""
+        t, ms, n = C.c_uint32(), C.c_double(), C.c_uint32()
+        _abi.check(self._lib.gbmd_time_loop(self._h, steps, C.byref(t), C.byref(ms), C.byref(n)))
+        return t.value, ms.value, n.value
+
     def launch_count(self):
         c = C.c_uint64()
         _abi.check(self._lib.gbmd_launch_count(self._h, C.byref(c)))
@@ -398,6 +412,13 @@ class BatchEngine:
         l, r = C.c_uint64(), C.c_uint32()
         _abi.check(self._lib.gbmd_batch_stats(self._h, C.byref(l), C.byref(r)))
         return l.value, r.value
+
+    def time_phases(self, steps):
+        """`steps` steps as individual launches with CUDA events around the force launch and the
+        list rebuild: (mean ms of one force step, mean ms of one rebuild, rebuilds)."""
+        f, r, n = C.c_double(), C.c_double(), C.c_uint32()
+        _abi.check(self._lib.gbmd_batch_time_phases(self._h, steps, C.byref(f), C.byref(r), C.byref(n)))
+        return f.value, r.value, n.value
 
     def __enter__(self):
         return self

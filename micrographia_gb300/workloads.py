@@ -94,10 +94,11 @@ def _profile_run(name):
     (each run ends by itself within seconds):
     - frames3d: the 3D liquid (FCC N = 2^20, rho 0.8442, T 0.72, skin 0.3), 20 steps, then three
       frames (the energy/virial pass k_kicks<3> and a 200-bin RDF to r = 5, k_rdf<3>);
-    - loop3d: one 3D liquid of N = 32,000 stepped 512 times by the persistent step loop
-      (k_force_loop);
-    - batch: the first 256 of the 1024 batched 2D replicas, 300 steps in 100-step graphs
-      (k_bforce_list, k_bbuild_list)."""
+    - loop3d: one 3D liquid of N = 32,000 stepped 512 times by the persistent step loop, then 512
+      more by direct launches of the loop (k_force_loop; a profiler cannot see kernels inside the
+      graphs' conditional nodes);
+    - batch: the first 256 of the 1024 batched 2D replicas, 300 steps in 100-step graphs, then 50
+      steps by direct launches (k_bforce_list, k_bbuild_list)."""
     from .engine import BatchEngine, ForceMode, GpuEngine3, init_state
 
     if name == "frames3d":
@@ -113,7 +114,8 @@ def _profile_run(name):
         spec = make_init(_abi.INIT_FCC, n, 0.72, 1, 0.05)
         with GpuEngine3(sys3, None, ForceMode.verlet_with_skin(sys3, n, 0.3), init=spec) as e:
             e.step(512)
-            print(f"loop3d: {e.launch_count()} launches, rebuilds {e.read_list_stats()[0]}")
+            taken, ms, launches = e.time_loop(512)
+            print(f"loop3d: {taken} steps in {launches} loop launches, {ms * 1e3:.1f} us per step; rebuilds {e.read_list_stats()[0]}")
     elif name == "batch":
         cfg = config4()[:256]
         systems = [s for s, _ in cfg]
@@ -121,7 +123,8 @@ def _profile_run(name):
         with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.6), block_steps=100) as b:
             b.step(300)
             b.wait()
-            print(f"batch: {sum(st.n() for st in states)} particles, stats {b.stats()}")
+            f, r, nr = b.time_phases(50)
+            print(f"batch: {sum(st.n() for st in states)} particles, force {f:.3f} ms, rebuild {r:.3f} ms ({nr} in 50 steps)")
     else:
         raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d or batch")
 

@@ -1135,3 +1135,30 @@ def test_update_system_matches_oracle(O, dim):
         g.step(10)
         c.step(10)
         assert g.read_state() == c.state
+
+
+# ---------------------------------------------------------------- direct-launch timing paths
+def test_time_loop_and_batch_time_phases_keep_the_trajectory(O):
+    """The timing entry points step with direct launches (the persistent loop; the batch's force
+    and rebuild kernels) instead of graphs: the trajectories still equal the oracle's."""
+    from micrographia_gb300 import BatchEngine, workloads
+
+    sys3, st = liquid3(O, 8000, 0.8442, 1.0)
+    with GpuEngine3(sys3, st, ForceMode.verlet_with_skin(sys3, 8000, 0.3)) as g:
+        taken, ms, launches = g.time_loop(100)
+        assert taken >= 100 and launches >= 1 and ms > 0
+        got = g.read_state()
+    cpu = O.IntEngine(sys3, st)
+    cpu.step(taken)
+    assert got == cpu.state
+    cfg = workloads.config4(count=6, base_seed=3, n_min=256, n_max=4096)
+    systems = [s for s, _ in cfg]
+    states = [O.init(s, spec) for s, spec in cfg]
+    with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3)) as b:
+        b.step(30)
+        f, r, nr = b.time_phases(70)
+        assert f > 0 and nr >= 1
+        for k, (sys_, s0) in enumerate(zip(systems, states)):
+            c = O.IntEngine(sys_, s0)
+            c.step(100)
+            assert b.read_system(k) == c.state, k
