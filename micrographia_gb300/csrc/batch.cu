@@ -203,84 +203,24 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
     sysidx_o[i] = sys;
 }
 
-// Persistent fused force + leapfrog over every particle of every system, on the layout of the
-// single-system engine: warp-tiled lists with periodic-image codes, 16-byte quotient records and
-// positions left unwrapped between list builds. Warps step through the particles 32 at a time
-// (a warp is a list tile); each lane reads its own system's parameters.
+// Persistent fused force + leapfrog over every particle of every system: the single-system
+// engine's step (force_list_one: warp-tiled lists with periodic-image codes, 16-byte quotient
+// records, positions left unwrapped between list builds), each lane with the parameter block of
+// its own system. Warps step through the particles 32 at a time (a warp is a list tile).
 template <int D, bool MULTI, bool SIG1>
-__global__ void __launch_bounds__(128) k_bforce_list(uint32_t N, uint32_t cap, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx,
-                                                     const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
-                                                     const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
-                                                     int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
-                                                     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-                                                     const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
-    const uint32_t lane = threadIdx.x & 31u, nwarps = (gridDim.x * blockDim.x) >> 5, cap4 = (cap + 3u) & ~3u;
+__global__ void __launch_bounds__(128, 10) k_bforce_list(uint32_t N, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx,
+                                                         const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
+                                                         const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
+                                                         int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
+                                                         const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+                                                         const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
+    const uint32_t lane = threadIdx.x & 31u, nwarps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32u < N; w += nwarps) {
         const uint32_t i = w * 32u + lane;
         if (i >= N) continue;
-        const Params& P = tab[sysidx[i]];
-        const Geom G = geom_of(P);
-        int64_t xi[3];
-        const uint32_t si = load_particle<D, MULTI>(pos_in, species, i, xi);
-        const float cs = P.kick_cs[si];
-        const PairC pc0 = P.pc[0];
-        const uint32_t ns = P.ns;
-        int32_t k[3] = {0, 0, 0};
-        const uint32_t m = __ldg(nbr_count + i);
-        const uint4* groups = reinterpret_cast<const uint4*>(nbr + list_slot(i, 0, cap4));
-        const uint4 qi = __ldg(qpos_in + i);
-        const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
-        const uint32_t ngroups = (m + 3u) >> 2;
-        for (uint32_t g = 0; g < ngroups; g++) {
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * min(g + 2, ngroups - 1u)));
-            const uint4 jv = __ldg(groups + 32 * g);
-            const uint32_t jj[4] = {jv.x, jv.y, jv.z, jv.w};
-            const uint32_t left = m - 4 * g;
-            uint4 r[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) r[u] = __ldg(qpos_in + ((uint32_t)u < left ? (jj[u] & LIST_MASK) : i));
-            float f[4][3];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                uint32_t Xj[3] = {r[u].x, r[u].y, r[u].z};
-                uint32_t Rj[3] = {__byte_perm(r[u].w, 0u, 0x4440u), __byte_perm(r[u].w, 0u, 0x4441u), __byte_perm(r[u].w, 0u, 0x4442u)};
-                const uint32_t code = jj[u] >> LIST_BITS;
-                if (code) { // (a stale word past the list's end only shifts this particle's own record)
-#pragma unroll
-                    for (int a = 0; a < D; a++) quot_shift((code >> (2 * a)) & 3u, P.box[a], Xj[a], Rj[a]);
-                }
-#pragma unroll
-                for (int a = 0; a < D; a++) f[u][a] = quot_sep_mad(Xj[a], Rj[a], 0u - Xi[a], (qi.w >> (8 * a)) & 15u, P.one);
-                if (D == 2) f[u][2] = 0.0f;
-            }
-            if constexpr (!MULTI && SIG1) {
-#pragma unroll
-                for (int h = 0; h < 2; h++) pair_kicks2_sig1<D>(pc0, cs, f[2 * h], f[2 * h + 1], (uint32_t)(2 * h) < left, (uint32_t)(2 * h + 1) < left, k);
-            } else {
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if ((uint32_t)u >= left) break;
-                    const PairC& pc = MULTI ? P.pc[si * ns + (r[u].w >> 24)] : pc0;
-                    float fr, s6, r2;
-                    if (pair_fr<D>(pc, f[u], fr, s6, r2)) {
-                        const float am = __fmul_rn(-fr, cs);
-#pragma unroll
-                        for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(am, f[u][a])));
-                    }
-                }
-            }
-        }
-        int32_t v[3];
-#pragma unroll
-        for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
-        leapfrog<D, Geom, false>(G, si, k, v, xi);
-#pragma unroll
-        for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
-        store_pos<D>(pos_out, i, xi, si);
-        qpos_out[i] = quot_record<D>(xi, si);
-        int64_t xr[3];
-        load_particle<D, false>(ref_pos, nullptr, i, xr);
-        if (moved_half_skin<D>(G, xr, xi)) ctl[0] = 1;
+        if (force_list_one<D, MULTI, false, SIG1 && !MULTI, 1, false>(tab[sysidx[i]], N, i, pos_in, pos_out, qpos_in, qpos_out, vel, species,
+                                                                        nbr, nbr_count, ref_pos))
+            ctl[0] = 1;
     }
 }
 
@@ -443,11 +383,11 @@ void benqueue_rebuild(gbmd_batch* b, cudaStream_t s) {
 }
 template <int D, bool MULTI> void benqueue_force_t(gbmd_batch* b, cudaStream_t s) {
     if (b->sig1)
-        k_bforce_list<D, MULTI, true><<<b->grid, 128, 0, s>>>(b->N, b->cap, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
+        k_bforce_list<D, MULTI, true><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
                                                               (PosRec<D>*)b->pos[b->cur ^ 1], b->qpos[b->cur], b->qpos[b->cur ^ 1], b->vel,
                                                               b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
     else
-        k_bforce_list<D, MULTI, false><<<b->grid, 128, 0, s>>>(b->N, b->cap, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
+        k_bforce_list<D, MULTI, false><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
                                                                (PosRec<D>*)b->pos[b->cur ^ 1], b->qpos[b->cur], b->qpos[b->cur ^ 1], b->vel,
                                                                b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
     note_launch();

@@ -684,15 +684,17 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // particle takes its groups s, s + S, ... and the integer kicks are summed across the S lanes
 // (wrapping integer sums: the result does not depend on the split). CG: positions and records
 // are read through L2 only (the persistent step loop, where other blocks rewrite them).
+// `n`: the particles of the arrays (a batch passes all of its systems' particles, with P the
+// parameter block of the system that lane t's particle belongs to).
 template <int D, bool MULTI, bool INT, bool SIG1, int S, bool CG>
-__device__ __forceinline__ bool force_list_one(const Params& P, uint32_t t, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
-                                               const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out, int32_t* __restrict__ vel,
-                                               const uint32_t* __restrict__ species, const uint32_t* __restrict__ nbr,
+__device__ __forceinline__ bool force_list_one(const Params& P, uint32_t n, uint32_t t, const PosRec<D>* __restrict__ pos_in,
+                                               PosRec<D>* __restrict__ pos_out, const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
+                                               int32_t* __restrict__ vel, const uint32_t* __restrict__ species, const uint32_t* __restrict__ nbr,
                                                const uint32_t* __restrict__ nbr_count, const PosRec<D>* __restrict__ ref_pos) {
     const uint32_t i = S == 1 ? t : (t >> 5) * (32u / S) + (t & 31u) / S, seg = S == 1 ? 0u : (t & 31u) % S;
-    if (S == 1 && i >= P.n) return false;
-    const bool valid = i < P.n; // (S > 1: every lane takes part in the kick sum)
-    const uint32_t iv = valid ? i : P.n - 1;
+    if (S == 1 && i >= n) return false;
+    const bool valid = i < n; // (S > 1: every lane takes part in the kick sum)
+    const uint32_t iv = valid ? i : n - 1;
     int64_t xi[3];
     uint32_t si = load_particle<D, MULTI, CG>(pos_in, species, iv, xi);
     const float cs = P.kick_cs[si];
@@ -805,7 +807,7 @@ __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D
                                                     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                     const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (force_list_one<D, MULTI, INT, SIG1, S, false>(P, t, pos_in, pos_out, qpos_in, qpos_out, vel, species, nbr, nbr_count, ref_pos))
+    if (force_list_one<D, MULTI, INT, SIG1, S, false>(P, P.n, t, pos_in, pos_out, qpos_in, qpos_out, vel, species, nbr, nbr_count, ref_pos))
         ctl[0] = 1;
 }
 
@@ -913,7 +915,7 @@ __global__ void __launch_bounds__(128, 10) k_force_loop(Params P, PosRec<D>* __r
     uint32_t k = 0;
     while (!stop) {
         const bool odd = k & 1u;
-        const bool moved = force_list_one<D, false, false, true, S, true>(P, t, odd ? pos1 : pos0, odd ? pos0 : pos1, odd ? q1 : q0,
+        const bool moved = force_list_one<D, false, false, true, S, true>(P, P.n, t, odd ? pos1 : pos0, odd ? pos0 : pos1, odd ? q1 : q0,
                                                                           odd ? q0 : q1, vel, nullptr, nbr, nbr_count, ref_pos);
         if (moved) ctl[0] = 1;
         k++;
