@@ -67,8 +67,9 @@ typedef struct gbmd_pair {
 /*
  * The System fields the LJ path needs: md_core::System (crates/md-core/src/system.rs:26-64) and
  * md_core::three::System3 (crates/md-core/src/three.rs:13-31). `pairs` is row-major
- * [a * nspecies + b] like `System::pairs`. Walls, compartments, membranes, pistons and bonds are
- * outside this engine: `periodic` must have every axis set.
+ * [a * nspecies + b] like `System::pairs`. Walls (hard, soft, thermal) run on plain engines;
+ * compartments, membranes, pistons and bonds are outside this engine, and batches and served
+ * requests take periodic systems only.
  *
  * The Andersen heat bath (`bath` = 1): md_core::Thermostat (system.rs:156-175, built by
  * with_thermostat / with_fan / with_bath_layer, system.rs:326-353) in 2D and three::Bath
@@ -100,8 +101,10 @@ typedef struct gbmd_system {
     int64_t bath_region[2]; /* 2D: [lo, hi) along bath_axis in position units (all: INT64_MIN, INT64_MAX) */
     /* Walls on the axes whose `periodic` bit is clear (md_core::Wall, walls.rs; with_walls,
      * system.rs:209-212): wall_kind[axis][side] (side 0 at 0, 1 at L) is a GBMD_WALL_* kind,
-     * wall_t[axis][side] a thermal wall's kT. The GPU engine runs periodic systems only
-     * (GBMD_E_UNSUPPORTED otherwise); the fields carry the reference's System whole. */
+     * wall_t[axis][side] a thermal wall's kT. A walled axis needs a kind on each side. After each
+     * force step a pass adds the soft walls' kicks, applies the bath, and mirrors a particle that
+     * left the box back in (walls::mirror), colliding it with the wall (IntEngine::collide,
+     * int_engine.rs:363-390; int_engine3.rs:186-205). */
     uint32_t wall_kind[3][2];
     double wall_t[3][2];
     /* A semi-permeable membrane across a walled axis (md_core::Membrane, system.rs:119-141;
@@ -260,9 +263,9 @@ int gbmd_state_hash(gbmd_engine* e, uint64_t* hash);
 int gbmd_counters(gbmd_engine* e, int64_t* steps, uint32_t* clock);
 /* The energy/impulse ledger (md_core::walls::Ledger, walls.rs:40-50; GpuEngine::read_ledger):
  * GBMD_LEDGER_SLOTS entries each, slot 2 axis + side for walls, GBMD_LEDGER_BATH for the heat
- * bath. This engine has no walls or membranes, so only the bath slot fills: the energy it gave
- * (each event's f64 energy change rounded half away from zero to 2^-24 epsilon and summed as an
- * integer, so the total does not depend on the order of events) and its redraw count. */
+ * bath: the energy given to the system, the normal momentum given to the wall and the hits (the
+ * bath's redraws). Each event's f64 energy change and impulse is rounded half away from zero to
+ * 2^-24 and summed as an integer, so the totals do not depend on the order of events. */
 #define GBMD_LEDGER_SLOTS 7
 #define GBMD_LEDGER_BATH 6
 int gbmd_read_ledger(gbmd_engine* e, double* energy, double* impulse, uint64_t* hits);

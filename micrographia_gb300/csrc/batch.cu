@@ -32,7 +32,7 @@ namespace {
 struct Geom {
     int64_t box[3], half[3];
     int32_t gravity[3];
-    uint32_t pinned;
+    uint32_t pinned, periodic;
     float half_skin2s;
 };
 __device__ __forceinline__ Geom geom_of(const Params& P) {
@@ -43,6 +43,7 @@ __device__ __forceinline__ Geom geom_of(const Params& P) {
         g.gravity[a] = P.gravity[a];
     }
     g.pinned = P.pinned;
+    g.periodic = P.periodic;
     g.half_skin2s = P.half_skin2s;
     return g;
 }
@@ -538,6 +539,8 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     uint32_t D = systems[0].dim;
     for (uint32_t k = 0; k < count; k++) {
         GBMD_TRY(validate_system(systems[k], offsets[k + 1] - offsets[k]));
+        if ((systems[k].periodic & ((1u << systems[k].dim) - 1u)) != ((1u << systems[k].dim) - 1u))
+            return fail(GBMD_E_UNSUPPORTED, "batches hold periodic systems only (walls run on a plain engine)");
         if (systems[k].dim != D) return fail(GBMD_E_INVALID, "a batch holds systems of one dimension");
         if (offsets[k + 1] <= offsets[k]) return fail(GBMD_E_INVALID, "every system needs at least one particle");
     }

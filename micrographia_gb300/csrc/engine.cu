@@ -49,9 +49,16 @@ static double to_f64h(int64_t x) { return (double)x * (1.0 / 4294967296.0); }
 int validate_system(const gbmd_system& sys, uint32_t n) {
     if (sys.dim != 2 && sys.dim != 3) return fail(GBMD_E_INVALID, "dim must be 2 or 3");
     if (sys.nspecies < 1 || sys.nspecies > GBMD_MAX_SPECIES) return fail(GBMD_E_INVALID, "species must number 1 to 4");
-    uint32_t all = (1u << sys.dim) - 1u;
-    if ((sys.periodic & all) != all)
-        return fail(GBMD_E_UNSUPPORTED, "walls are not part of this engine: every axis must be periodic");
+    for (uint32_t a = 0; a < sys.dim; a++) {
+        if ((sys.periodic >> a) & 1u) continue;
+        for (int side = 0; side < 2; side++) {
+            const uint32_t k = sys.wall_kind[a][side];
+            if (k != GBMD_WALL_HARD && k != GBMD_WALL_SOFT && k != GBMD_WALL_THERMAL)
+                return fail(GBMD_E_INVALID, "a non-periodic axis needs a wall (hard, soft or thermal) on each side");
+            if (k == GBMD_WALL_THERMAL && !(sys.wall_t[a][side] >= 0.0 && sys.wall_t[a][side] < INFINITY))
+                return fail(GBMD_E_INVALID, "a thermal wall needs a finite temperature >= 0");
+        }
+    }
     if (sys.membrane) return fail(GBMD_E_UNSUPPORTED, "membranes are not part of this engine");
     if (sys.compartments[0] || sys.compartments[1]) return fail(GBMD_E_UNSUPPORTED, "compartments are not part of this engine");
     for (uint32_t a = 0; a < sys.dim; a++)
@@ -184,12 +191,23 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
     P.dim = s.dim;
     P.ns = s.nspecies;
     P.cap = cap;
+    P.periodic = (s.periodic | (s.dim == 2 ? 4u : 0u)) & 7u;
     for (uint32_t a = 0; a < 3; a++) {
         P.box[a] = a < s.dim ? s.box_len[a] : 1;
-        P.half[a] = P.box[a] / 2;
+        // (a walled axis: no separation reaches half, so min_image is the plain difference)
+        P.half[a] = ((P.periodic >> a) & 1u) ? P.box[a] / 2 : INT64_MAX / 4;
         P.box_f[a] = to_f64h(P.box[a]);
         P.nc[a] = a < s.dim ? nc[a] : 1;
+        if (a < s.dim && !((P.periodic >> a) & 1u)) {
+            P.walls = 1;
+            for (int side = 0; side < 2; side++) {
+                P.wall_kind[a][side] = s.wall_kind[a][side];
+                P.wall_t[a][side] = s.wall_t[a][side];
+            }
+        }
     }
+    P.wall_key[0] = (uint32_t)s.seed;
+    P.wall_key[1] = (uint32_t)(s.seed >> 32) ^ 0x57414c4cu; // STREAM_WALL (walls.rs:86)
     P.ncell = P.nc[0] * P.nc[1] * P.nc[2];
     for (uint32_t sp = 0; sp < GBMD_MAX_SPECIES; sp++) {
         double kc = 0.0;
@@ -326,7 +344,7 @@ struct gbmd_engine {
     float4* relf = nullptr;  // cell-relative f32 coordinates of the sorted scratch state
     uint4* qpos[2] = {nullptr, nullptr}; // quotient records of the positions (ping-pong)
     uint32_t* ctl = nullptr; // [0] rebuild, [1] overflow, [2] rebuilds; [CTL_CLOCK] the bath's step clock
-    unsigned long long* ledger = nullptr; // the bath's ledger slot: energy (2^-24 epsilon), redraws
+    unsigned long long* ledger = nullptr; // per ledger slot: energy given (2^-24 epsilon), hits, impulse (2^-24)
     double* partial = nullptr;
     void* staging = nullptr;  // id-ordered I/O staging (n * D int64)
     int32_t* staging_v = nullptr;
@@ -602,14 +620,26 @@ void enqueue_force(gbmd_engine* e, cudaStream_t s) {
         if (e->multi) enqueue_force_t<3, true>(e, s, threads);
         else enqueue_force_t<3, false>(e, s, threads);
     }
-    if (e->P.bath) { // the Andersen bath on the moved state, then the step clock advances
+    if (e->P.walls) { // the soft walls' kicks, the bath, the mirror and collisions; then the clock
+        const uint32_t nb = blocks_for(e->n, 256);
+        unsigned long long* l = e->ledger;
+        if (e->D == 2) {
+            if (e->verlet) k_walls<2, true><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<2>*)e->ref_pos, e->ctl, l);
+            else k_walls<2, false><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, l);
+        } else {
+            if (e->verlet) k_walls<3, true><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<3>*)e->ref_pos, e->ctl, l);
+            else k_walls<3, false><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, l);
+        }
+        k_clock_tick<<<1, 1, 0, s>>>(e->ctl);
+        note_launch(2);
+    } else if (e->P.bath) { // the Andersen bath on the moved state, then the step clock advances
         const uint32_t nb = blocks_for(e->n, 256);
         if (e->D == 2) {
-            if (e->verlet) k_bath<2, true><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<2>*)e->ref_pos, e->ctl, e->ledger);
-            else k_bath<2, false><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger);
+            if (e->verlet) k_bath<2, true><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<2>*)e->ref_pos, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
+            else k_bath<2, false><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
         } else {
-            if (e->verlet) k_bath<3, true><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<3>*)e->ref_pos, e->ctl, e->ledger);
-            else k_bath<3, false><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger);
+            if (e->verlet) k_bath<3, true><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<3>*)e->ref_pos, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
+            else k_bath<3, false><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
         }
         k_clock_tick<<<1, 1, 0, s>>>(e->ctl);
         note_launch(2);
@@ -713,7 +743,7 @@ cudaError_t enqueue_loop(gbmd_engine* e, cudaStream_t s) {
 // kernel's; fewer if the grid would not be resident.
 int setup_step_loop(gbmd_engine* e) {
     e->loop_lanes = 0;
-    if (!e->verlet || e->half || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath ||
+    if (!e->verlet || e->half || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath || e->P.walls ||
         (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP))
         return GBMD_OK;
     // Larger systems' steps are long enough that the graph's per-step nodes cost less than the
@@ -1116,7 +1146,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         cap = e->opt.cap ? e->opt.cap : (uint32_t)std::ceil(sphere * std::max(2.0 * density, 1.2)) + 8;
     }
     fill_params(e->P, *sys, n, e->skin, cap, nc);
-    if (e->verlet && e->D == 3 && !e->multi && e->opt.arith == GBMD_ARITH_F32 && (e->opt.flags & GBMD_FLAG_HALF_LISTS)) {
+    if (e->verlet && e->D == 3 && !e->multi && e->opt.arith == GBMD_ARITH_F32 && !e->P.walls && (e->opt.flags & GBMD_FLAG_HALF_LISTS)) {
         // Half-shell lists address a neighbour by its offset in its row of cells (16 bits): rows
         // must stay far below 65,536 particles (the build reports an overflow otherwise). The
         // force step's shared-memory windows hold six mean rows with a tenth to spare; rows
@@ -1175,8 +1205,8 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         GBMD_CUDA_TRY(cudaFuncSetAttribute(k_force_half<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     }
     GBMD_TRY(allocT(e, &e->ctl, 16));
-    GBMD_TRY(allocT(e, &e->ledger, 2));
-    GBMD_CUDA_TRY(cudaMemsetAsync(e->ledger, 0, 16, e->st));
+    GBMD_TRY(allocT(e, &e->ledger, 3 * GBMD_LEDGER_SLOTS));
+    GBMD_CUDA_TRY(cudaMemsetAsync(e->ledger, 0, 24 * GBMD_LEDGER_SLOTS, e->st));
     if (e->opt.arith == GBMD_ARITH_INT) {
         std::vector<int32_t> tab;
         std::vector<double> pair4;
@@ -1355,6 +1385,7 @@ int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential) {
 // path, on the device so that it runs at full size.
 int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (e->P.walls) return fail(GBMD_E_UNSUPPORTED, "the f64 reference kicks are for periodic systems");
     GBMD_TRY(prepare_pairs_cond(e));
     PairsF64 Q;
     std::memset(&Q, 0, sizeof(Q));
@@ -1568,13 +1599,13 @@ int gbmd_state_hash(gbmd_engine* e, uint64_t* hash) {
 
 int gbmd_read_ledger(gbmd_engine* e, double* energy, double* impulse, uint64_t* hits) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    unsigned long long l[2];
-    GBMD_CUDA_TRY(cudaMemcpyAsync(l, e->ledger, 16, cudaMemcpyDeviceToHost, e->st));
+    unsigned long long l[3 * GBMD_LEDGER_SLOTS];
+    GBMD_CUDA_TRY(cudaMemcpyAsync(l, e->ledger, sizeof(l), cudaMemcpyDeviceToHost, e->st));
     GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
     for (int w = 0; w < GBMD_LEDGER_SLOTS; w++) {
-        if (energy) energy[w] = w == GBMD_LEDGER_BATH ? (double)(long long)l[0] * (1.0 / 16777216.0) : 0.0;
-        if (impulse) impulse[w] = 0.0;
-        if (hits) hits[w] = w == GBMD_LEDGER_BATH ? (uint64_t)l[1] : 0;
+        if (energy) energy[w] = (double)(long long)l[3 * w] * (1.0 / 16777216.0);
+        if (hits) hits[w] = (uint64_t)l[3 * w + 1];
+        if (impulse) impulse[w] = (double)(long long)l[3 * w + 2] * (1.0 / 16777216.0);
     }
     return GBMD_OK;
 }
@@ -1862,16 +1893,16 @@ __global__ void __launch_bounds__(128) k_rdf(Params P, const Rec<D>* pos, const 
         const float top = (float)bins - margin, hi = 1.0f - margin;
         for (int oz = 0; oz < (D == 3 ? 3 : 1); oz++) {
             int64_t z = D == 3 ? (int64_t)c[2] + oz - 1 : 0, sz = 0;
-            if (D == 3 && z < 0) z += P.nc[2], sz = -P.box[2];
-            if (D == 3 && z >= (int64_t)P.nc[2]) z -= P.nc[2], sz = P.box[2];
+            if (D == 3 && z < 0) z += P.nc[2], sz = image_shift(P, 2, -P.box[2]);
+            if (D == 3 && z >= (int64_t)P.nc[2]) z -= P.nc[2], sz = image_shift(P, 2, P.box[2]);
             for (int oy = 0; oy < 3; oy++) {
                 int64_t y = (int64_t)c[1] + oy - 1, sy = 0;
-                if (y < 0) y += P.nc[1], sy = -P.box[1];
-                if (y >= (int64_t)P.nc[1]) y -= P.nc[1], sy = P.box[1];
+                if (y < 0) y += P.nc[1], sy = image_shift(P, 1, -P.box[1]);
+                if (y >= (int64_t)P.nc[1]) y -= P.nc[1], sy = image_shift(P, 1, P.box[1]);
                 for (int ox = 0; ox < 3; ox++) {
                     int64_t x = (int64_t)c[0] + ox - 1, sx = 0;
-                    if (x < 0) x += P.nc[0], sx = -P.box[0];
-                    if (x >= (int64_t)P.nc[0]) x -= P.nc[0], sx = P.box[0];
+                    if (x < 0) x += P.nc[0], sx = image_shift(P, 0, -P.box[0]);
+                    if (x >= (int64_t)P.nc[0]) x -= P.nc[0], sx = image_shift(P, 0, P.box[0]);
                     const uint32_t cell = (uint32_t)((z * P.nc[1] + y) * P.nc[0] + x);
                     const uint32_t j0 = max(start[cell], i + 1), j1 = start[cell + 1];
                     if (j0 >= j1) continue;

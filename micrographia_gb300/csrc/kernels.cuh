@@ -292,7 +292,8 @@ __device__ __forceinline__ void leapfrog(const G& P, uint32_t si, const int32_t*
 #pragma unroll
     for (int a = 0; a < D; a++) {
         v[a] = wadd(wadd(v[a], k[a]), pinned ? 0 : P.gravity[a]);
-        x[a] = WRAP ? wrap(x[a] + (int64_t)v[a], P.box[a]) : x[a] + (int64_t)v[a];
+        // (a walled axis is not wrapped: a particle that left the box is mirrored after the step)
+        x[a] = (WRAP && ((P.periodic >> a) & 1u)) ? wrap(x[a] + (int64_t)v[a], P.box[a]) : x[a] + (int64_t)v[a];
     }
 }
 
@@ -531,11 +532,11 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     for (int oz = 0; oz < (D == 3 ? 3 : 1); oz++) {
         int tz = (int)c[2] + oz - 1;
         uint32_t z = D == 3 ? (tz < 0 ? nz - 1 : (tz >= (int)nz ? 0 : (uint32_t)tz)) : 0;
-        int64_t sz = D == 3 ? (tz < 0 ? -P.box[2] : (tz >= (int)nz ? P.box[2] : 0)) : 0;
+        int64_t sz = D == 3 ? image_shift(P, 2, tz < 0 ? -P.box[2] : (tz >= (int)nz ? P.box[2] : 0)) : 0;
         for (int oy = 0; oy < 3; oy++) {
             int ty = (int)c[1] + oy - 1;
             uint32_t y = ty < 0 ? ny - 1 : (ty >= (int)ny ? 0 : (uint32_t)ty);
-            int64_t sy = ty < 0 ? -P.box[1] : (ty >= (int)ny ? P.box[1] : 0);
+            int64_t sy = image_shift(P, 1, ty < 0 ? -P.box[1] : (ty >= (int)ny ? P.box[1] : 0));
             const int layer = D == 3 ? oz : oy; // along the last axis: 0 down, 1 same, 2 up
             const uint32_t slab0 = layer == 0 ? dn : 0u, slab1 = layer == 2 ? up + 1u : (1u << sh);
             if constexpr (D == 2 && S == 1) {
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
             for (int ox = 0; ox < 3; ox++) {
                 int tx = (int)c[0] + ox - 1;
                 uint32_t x = tx < 0 ? nx - 1 : (tx >= (int)nx ? 0 : (uint32_t)tx);
-                int64_t sx = tx < 0 ? -P.box[0] : (tx >= (int)nx ? P.box[0] : 0);
+                int64_t sx = image_shift(P, 0, tx < 0 ? -P.box[0] : (tx >= (int)nx ? P.box[0] : 0));
                 uint32_t cell = (z * ny + y) * nx + x;
                 const int64_t xs[3] = {xi[0] - sx, xi[1] - sy, D == 3 ? xi[2] - sz : 0};
                 const uint32_t code = image_code(sx, sy, sz);
@@ -945,6 +946,27 @@ __global__ void __launch_bounds__(128, 10) k_force_loop(Params P, PosRec<D>* __r
 // lists the quotient record is rewritten and the displacement trigger re-tested at the new
 // position (a trigger the force step already set stays set: an extra rebuild changes nothing).
 // The draw is keyed on the clock word, which the next launch in the stream advances.
+// The bath on one particle's moved state (x, v as the step left them): returns whether it drew.
+template <int D>
+__device__ __forceinline__ bool bath_one(const Params& P, uint32_t si, uint32_t id, uint32_t clock, int64_t* x, int32_t* v,
+                                         unsigned long long* ledger) {
+    if (((P.pinned >> si) & 1u) || !((P.bath_species >> si) & 1u)) return false;
+    if (D == 2) {
+        const uint32_t ax = P.bath_axis;
+        const int64_t p = wrap(x[ax] - (int64_t)v[ax], P.box[ax]);
+        if (!(p >= P.bath_region[0] && p < P.bath_region[1])) return false;
+    }
+    const BathDraw o = bath_draw<D>(id, clock, P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si], P.masses[si], P.dt, P.bath_drift,
+                                    v[0], v[1], v[2], ledger);
+    if (!o.hit) return false;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        x[a] += (int64_t)o.v[a] - (int64_t)v[a];
+        v[a] = o.v[a];
+    }
+    return true;
+}
+
 template <int D, bool LIST>
 __global__ void k_bath(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict__ qpos, int32_t* __restrict__ vel,
                        const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids, const PosRec<D>* __restrict__ ref_pos,
@@ -958,20 +980,159 @@ __global__ void k_bath(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict_
     int32_t v[3] = {0, 0, 0};
 #pragma unroll
     for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
-    if (D == 2) {
-        const uint32_t ax = P.bath_axis;
-        const int64_t p = wrap(x[ax] - (int64_t)v[ax], P.box[ax]);
-        if (!(p >= P.bath_region[0] && p < P.bath_region[1])) return;
-    }
-    const BathDraw o = bath_draw<D>(ids[i], ctl[CTL_CLOCK], P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si], P.masses[si], P.dt,
-                                    P.bath_drift, v[0], v[1], v[2], ledger);
-    if (!o.hit) return;
+    if (!bath_one<D>(P, si, ids[i], ctl[CTL_CLOCK], x, v, ledger)) return;
 #pragma unroll
     for (int a = 0; a < D; a++) {
-        const int64_t y = x[a] + ((int64_t)o.v[a] - (int64_t)v[a]);
-        x[a] = LIST ? y : wrap(y, P.box[a]);
-        vel[D * i + a] = o.v[a];
+        if (!LIST) x[a] = wrap(x[a], P.box[a]);
+        vel[D * i + a] = v[a];
     }
+    store_pos<D>(pos, i, x, si);
+    if (LIST) {
+        qpos[i] = quot_record<D>(x, si);
+        int64_t xr[3];
+        load_particle<D, false>(ref_pos, nullptr, i, xr);
+        if (moved_half_skin<D>(P, xr, x)) ctl[0] = 1;
+    }
+}
+
+// ---------------------------------------------------------------- walls
+// md_core::walls (walls.rs) as IntEngine runs them (int_engine.rs:203-227 and 256-263, the soft
+// walls' kicks and impulses; 316-330, the mirror; 363-390, collide; int_engine3.rs:107-126,
+// 140-145 and 186-205 in 3D). Ledger slots 2 axis + side, three words each: the energy given
+// (2^-24 epsilon), the hits, the normal momentum given to the wall (2^-24); each event's f64
+// value is rounded half away from zero before it is added, so the totals do not depend on the
+// order in which the GPU books events.
+constexpr float SOFT_WALL_RC = 1.12246204830937298f; // walls.rs:104, 2^(1/6) (f32 of the f64 constant)
+__device__ __forceinline__ unsigned long long ledger_fixed(double x) {
+    return (unsigned long long)sat_i64_f64(round_away(__dmul_rn(x, 16777216.0)));
+}
+// The soft wall's WCA force at distance dw from the wall, in f32 (Real<f32>, no contraction):
+// s2 = 1 / (d d), s6 = s2 s2 s2, f = 24 s6 (2 s6 - 1) / d; false beyond its range.
+__device__ __forceinline__ bool soft_wall_force(int64_t dw, float& f, float& s6_out) {
+    bool ok = true;
+    const float d = __fmul_rn(sep_s(dw, ok), 1.0f / 268435456.0f); // sep_f32: 2^-28 sigma units
+    if (!ok || !(d < SOFT_WALL_RC)) return false;
+    const float s2 = __fdiv_rn(1.0f, __fmul_rn(d, d));
+    const float s6 = __fmul_rn(__fmul_rn(s2, s2), s2);
+    f = __fdiv_rn(__fmul_rn(__fmul_rn(24.0f, s6), __fsub_rn(__fmul_rn(2.0f, s6), 1.0f)), d);
+    s6_out = s6;
+    return true;
+}
+// walls::thermal_velocity (walls.rs:89-101) / three::thermal_velocity (three.rs:222-243): the
+// normal component (into the box) and the tangential ones of a Maxwell-flux draw at kT = t.
+template <int D>
+__device__ __forceinline__ void thermal_velocity(const Params& P, uint32_t id, uint32_t clock, double t, double m, double inward,
+                                                 double& vn, double* vt) {
+    uint32_t r0, r1, q0, q1;
+    threefry2x32(id, clock, P.wall_key[0], P.wall_key[1], r0, r1);
+    threefry2x32(id, clock, P.wall_key[0], P.wall_key[1] ^ 1u, q0, q1);
+    const double u1 = __dsub_rn(1.0, to_unit_f64(r0, r1));
+    const double u2 = __dsub_rn(1.0, to_unit_f64(q0, 0u)), u3 = to_unit_f64(q1, 0u);
+    const double tau = 6.28318530717958647692;
+    const double sd = __dsqrt_rn(__ddiv_rn(t, m));
+    vn = __dmul_rn(__dmul_rn(inward, sd), __dsqrt_rn(__dmul_rn(-2.0, dev_log(u1))));
+    if (D == 2) {
+        vt[0] = __dmul_rn(__dmul_rn(sd, __dsqrt_rn(__dmul_rn(-2.0, dev_log(u2)))), dev_cos(__dmul_rn(tau, u3)));
+    } else {
+        const double rad = __dmul_rn(sd, __dsqrt_rn(__dmul_rn(-2.0, dev_log(u2))));
+        const double a = __dmul_rn(tau, u3);
+        vt[0] = __dmul_rn(rad, dev_cos(a));
+        vt[1] = __dmul_rn(rad, dev_sin(a));
+    }
+}
+// After the force step on a system with walls: the step left v' = v + k + g and x' = x + v' with
+// k the pair kicks only. This pass adds each soft wall's kick (from the position at the step's
+// start, x' - v', exact in integers) to v' and x', applies the heat bath if there is one (in the
+// reference's order: after the kick, before the move), then mirrors a particle that left the box
+// on a walled axis back in and collides it with that wall: hard and soft walls reverse the normal
+// component, a thermal wall draws a new velocity on (id, step clock).
+template <int D, bool LIST>
+__global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict__ qpos, int32_t* __restrict__ vel,
+                        const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids, const PosRec<D>* __restrict__ ref_pos,
+                        uint32_t* __restrict__ ctl, unsigned long long* __restrict__ ledger) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const uint32_t si = species[i], id = ids[i], clock = ctl[CTL_CLOCK];
+    int64_t x[3] = {0, 0, 0};
+    load_particle<D, false>(pos, nullptr, i, x);
+    int32_t v[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
+    bool changed = false;
+    const float c = __fmul_rn(P.kick_cs[si], 1.0f / 268435456.0f); // kick_coeff in f32
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        if ((P.periodic >> a) & 1u) continue;
+        const int64_t xo = x[a] - (int64_t)v[a];
+        int32_t kw_sum = 0;
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            if (P.wall_kind[a][side] != GBMD_WALL_SOFT) continue;
+            float f, s6;
+            if (!soft_wall_force(side == 0 ? xo : P.box[a] - xo, f, s6)) continue;
+            const int32_t kw = rni_f32(__fmul_rn(f, c));
+            kw_sum = wadd(kw_sum, side == 0 ? kw : (int32_t)(0u - (uint32_t)kw));
+            atomicAdd(ledger + 3 * (2 * a + side) + 2, ledger_fixed(__dmul_rn((double)f, P.dt)));
+        }
+        if (kw_sum) {
+            v[a] = wadd(v[a], kw_sum);
+            x[a] += (int64_t)kw_sum;
+            changed = true;
+        }
+    }
+    if (P.bath && bath_one<D>(P, si, id, clock, x, v, ledger + 3 * GBMD_LEDGER_BATH)) changed = true;
+    const double m = P.masses[si];
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        if ((P.periodic >> a) & 1u) {
+            if (!LIST) x[a] = wrap(x[a], P.box[a]);
+            continue;
+        }
+        int side = -1;
+        if (x[a] < 0) {
+            x[a] = -1 - x[a];
+            side = 0;
+        } else if (x[a] >= P.box[a]) {
+            x[a] = 2 * P.box[a] - 1 - x[a];
+            side = 1;
+        }
+        if (side < 0) continue;
+        changed = true;
+        double before[3], after[3];
+        auto vel_of = [&](int32_t q) { return __ddiv_rn(__dmul_rn((double)q, 1.0 / 4294967296.0), P.dt); };
+        auto step_of = [&](double q) { return sat_i32_f64(round_away(__dmul_rn(__dmul_rn(q, P.dt), 4294967296.0))); };
+#pragma unroll
+        for (int b = 0; b < D; b++) before[b] = vel_of(v[b]);
+        if (P.wall_kind[a][side] == GBMD_WALL_THERMAL) {
+            double vn, vt[2];
+            thermal_velocity<D>(P, id, clock, P.wall_t[a][side], m, side == 0 ? 1.0 : -1.0, vn, vt);
+            v[a] = step_of(vn);
+            if (D == 2) {
+                v[1 - a] = step_of(vt[0]);
+            } else {
+                v[(a + 1) % 3] = step_of(vt[0]);
+                v[(a + 2) % 3] = step_of(vt[1]);
+            }
+        } else {
+            v[a] = (int32_t)(0u - (uint32_t)v[a]);
+        }
+#pragma unroll
+        for (int b = 0; b < D; b++) after[b] = vel_of(v[b]);
+        auto ke = [&](const double* u) {
+            double q = __dadd_rn(__dmul_rn(u[0], u[0]), __dmul_rn(u[1], u[1]));
+            if (D == 3) q = __dadd_rn(q, __dmul_rn(u[2], u[2]));
+            return __dmul_rn(__dmul_rn(0.5, m), q);
+        };
+        const double de = __dsub_rn(ke(after), ke(before));
+        const double imp = fabs(__dmul_rn(m, __dsub_rn(before[a], after[a])));
+        unsigned long long* l = ledger + 3 * (2 * a + side);
+        atomicAdd(l, ledger_fixed(de));
+        atomicAdd(l + 1, 1ull);
+        atomicAdd(l + 2, ledger_fixed(imp));
+    }
+    if (!changed) return;
+#pragma unroll
+    for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
     store_pos<D>(pos, i, x, si);
     if (LIST) {
         qpos[i] = quot_record<D>(x, si);
@@ -1091,6 +1252,22 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
         }
         pe *= 0.5;
         w *= 0.5;
+        if (P.walls) {
+            // the soft walls' kicks and potential (int_engine.rs:203-227, int_engine3.rs:107-126)
+            const float c = __fmul_rn(cs, 1.0f / 268435456.0f);
+#pragma unroll
+            for (int a = 0; a < D; a++) {
+                if ((P.periodic >> a) & 1u) continue;
+#pragma unroll
+                for (int side = 0; side < 2; side++) {
+                    float f, s6;
+                    if (P.wall_kind[a][side] != GBMD_WALL_SOFT || !soft_wall_force(side == 0 ? xi[a] : P.box[a] - xi[a], f, s6)) continue;
+                    const int32_t kw = rni_f32(__fmul_rn(f, c));
+                    k[a] = wadd(k[a], side == 0 ? kw : (int32_t)(0u - (uint32_t)kw));
+                    pe += (double)__fadd_rn(__fmul_rn(__fmul_rn(4.0f, s6), __fsub_rn(s6, 1.0f)), 1.0f);
+                }
+            }
+        }
         double m = P.masses[si];
         for (int a = 0; a < D; a++) {
             int32_t v0 = vel[D * i + a];

@@ -164,6 +164,8 @@ int gbmd_serve_submit(gbmd_server* sv, const gbmd_serve_request* req, uint64_t* 
     if (!sv || !req) return fail(GBMD_E_INVALID, "null argument");
     GBMD_TRY(validate_system(req->sys, req->init.n));
     if (req->init.n == 0 || req->steps == 0) return fail(GBMD_E_INVALID, "a request needs particles and steps");
+    if ((req->sys.periodic & ((1u << req->sys.dim) - 1u)) != ((1u << req->sys.dim) - 1u))
+        return fail(GBMD_E_UNSUPPORTED, "served requests are periodic systems");
     Request r;
     r.id = sv->next_id++;
     r.spec = *req;

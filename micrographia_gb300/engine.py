@@ -202,8 +202,8 @@ class _Engine:
         return f, rdf, prof
 
     def read_ledger(self):
-        """GpuEngine::read_ledger: (energy, impulse, hits), one entry per ledger slot; this engine
-        fills the heat bath's slot (_abi.LEDGER_BATH): the energy it gave and its redraws."""
+        """GpuEngine::read_ledger: (energy, impulse, hits), one entry per ledger slot: the walls'
+        (2 axis + side) and the heat bath's (_abi.LEDGER_BATH), each event rounded to 2^-24."""
         e = (C.c_double * _abi.LEDGER_SLOTS)()
         p = (C.c_double * _abi.LEDGER_SLOTS)()
         h = (C.c_uint64 * _abi.LEDGER_SLOTS)()

@@ -295,6 +295,13 @@ void oracle_engine_wall_ledger(void* h, double* energy, double* impulse, uint64_
     const Ledger& l = e->f32 ? e->f32->ledger : e->f64->ledger;
     for (int w = 0; w < LEDGER_SLOTS; w++) energy[w] = l.energy[w], impulse[w] = l.impulse[w], hits[w] = l.hits[w];
 }
+void oracle_engine_wall_ledger_fixed(void* h, int64_t* energy, int64_t* impulse) {
+    const Ledger& l = ((Engine*)h)->f32 ? ((Engine*)h)->f32->ledger : ((Engine*)h)->f64->ledger;
+    for (int w = 0; w < LEDGER_SLOTS; w++) {
+        energy[w] = w == LEDGER_BATH ? l.bath_energy_fixed : l.energy_fixed[w];
+        impulse[w] = l.impulse_fixed[w];
+    }
+}
 void oracle_engine_set_system(void* h, const gbmd_system* csys) {
     Engine* e = (Engine*)h;
     System sys = System::from_c(*csys);

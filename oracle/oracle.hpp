@@ -954,6 +954,10 @@ struct Ledger {
     double impulse[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
     uint64_t hits[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
     int64_t bath_energy_fixed = 0;
+    // every event's energy change and impulse also rounded to 2^-24 and summed as integers (the
+    // order-free totals a parallel engine can reproduce exactly)
+    int64_t energy_fixed[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
+    int64_t impulse_fixed[LEDGER_SLOTS] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 constexpr uint32_t STREAM_WALL = 0x57414c4cu; // walls.rs:86
@@ -1179,7 +1183,10 @@ template <typename F> struct IntEngine {
             // the soft walls' impulses (int_engine.rs:256-263, int_engine3.rs:140-145)
             for (size_t i = 0; i < state.n(); i++)
                 for (int w = 0; w < 6; w++)
-                    if (wall_force[i][w] != 0.0) ledger.impulse[w] += wall_force[i][w] * sys.dt;
+                    if (wall_force[i][w] != 0.0) {
+                        ledger.impulse[w] += wall_force[i][w] * sys.dt;
+                        ledger.impulse_fixed[w] += ledger_fixed(wall_force[i][w] * sys.dt);
+                    }
             for (size_t i = 0; i < state.n(); i++) {
                 const uint32_t sp = state.species[i];
                 bool pinned = sys.is_pinned(sp);
@@ -1278,8 +1285,11 @@ template <typename F> struct IntEngine {
         }
         for (int a = 0; a < d; a++) after[a] = sys.velocity(v[a]);
         auto ke = [&](const double* u) { return d == 2 ? 0.5 * m * (u[0] * u[0] + u[1] * u[1]) : 0.5 * m * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]); };
-        ledger.energy[w] += ke(after) - ke(before);
-        ledger.impulse[w] += std::fabs(m * (before[axis] - after[axis]));
+        const double de = ke(after) - ke(before), imp = std::fabs(m * (before[axis] - after[axis]));
+        ledger.energy[w] += de;
+        ledger.impulse[w] += imp;
+        ledger.energy_fixed[w] += ledger_fixed(de);
+        ledger.impulse_fixed[w] += ledger_fixed(imp);
         ledger.hits[w] += 1;
     }
     // int_engine.rs:396-413
@@ -1467,7 +1477,7 @@ inline std::vector<uint32_t> verlet_list_of(const System& sys, const State& s, c
                     if (j == i) continue;
                     const int64_t* pj = &s.pos[d * j];
                     float f[3] = {0.0f, 0.0f, 0.0f};
-                    for (int a = 0; a < d; a++) f[a] = sep_or_far(min_image(pi[a], pj[a], sys.box[a]));
+                    for (int a = 0; a < d; a++) f[a] = sep_or_far(sys.periodic(a) ? min_image(pi[a], pj[a], sys.box[a]) : pj[a] - pi[a]);
                     float r2 = f[0] * f[0] + f[1] * f[1];
                     if (d == 3) r2 = r2 + f[2] * f[2];
                     if (r2 < pair_list_r2(sys, s.species[i], s.species[j], skin)) out.push_back(j);
@@ -1540,7 +1550,8 @@ inline PairSums pair_sums_f32(const System& sys, const State& s) {
                         const int64_t* pj = &s.pos[d * j];
                         float f[3];
                         bool ok = true;
-                        for (int a = 0; a < d; a++) ok = ok && sep_f32(min_image(pi[a], pj[a], sys.box[a]), &f[a]);
+                        for (int a = 0; a < d; a++)
+                            ok = ok && sep_f32(sys.periodic(a) ? min_image(pi[a], pj[a], sys.box[a]) : pj[a] - pi[a], &f[a]);
                         if (!ok) continue;
                         float fr, u;
                         if (consts[s.species[i] * ns + s.species[j]].eval(f, d, &fr, &u)) {
@@ -1576,7 +1587,7 @@ inline std::vector<uint64_t> rdf_counts(const System& sys, const State& s, uint3
             for (size_t j = i + 1; j < s.n(); j++) {
                 double r2 = 0.0;
                 for (int a = 0; a < d; a++) {
-                    double dd = to_f64(min_image(s.pos[d * i + a], s.pos[d * j + a], sys.box[a]));
+                    double dd = to_f64(sys.periodic(a) ? min_image(s.pos[d * i + a], s.pos[d * j + a], sys.box[a]) : s.pos[d * j + a] - s.pos[d * i + a]);
                     r2 = r2 + dd * dd;
                 }
                 double r = std::sqrt(r2) * scale;
@@ -1607,7 +1618,7 @@ inline std::vector<uint64_t> rdf_counts(const System& sys, const State& s, uint3
                         if (j <= i) continue;
                         double r2 = 0.0;
                         for (int a = 0; a < d; a++) {
-                            double dd = to_f64(min_image(pi[a], s.pos[d * j + a], sys.box[a]));
+                            double dd = to_f64(sys.periodic(a) ? min_image(pi[a], s.pos[d * j + a], sys.box[a]) : s.pos[d * j + a] - pi[a]);
                             r2 = r2 + dd * dd;
                         }
                         double r = std::sqrt(r2) * scale;

@@ -63,6 +63,7 @@ _SIGS = [
     ("oracle_engine_ledger", None, [VP, DP, I64P, U64P, U32P]),
     ("oracle_engine_set_system", None, [VP, SYS]),
     ("oracle_engine_wall_ledger", None, [VP, DP, DP, U64P]),
+    ("oracle_engine_wall_ledger_fixed", None, [VP, I64P, I64P]),
     ("oracle_engine_steps", C.c_int64, [VP]),
     ("oracle_engine_energy", None, [VP, DP, DP]),
     ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
@@ -369,6 +370,13 @@ class IntEngine:
         e, p, h = (C.c_double * 7)(), (C.c_double * 7)(), (C.c_uint64 * 7)()
         lib().oracle_engine_wall_ledger(self._h, e, p, h)
         return list(e), list(p), list(h)
+
+    def wall_ledger_fixed(self):
+        """Every ledger event's energy change and impulse rounded to 2^-24 and summed as integers
+        (in 2^-24 units), 7 slots each: the totals that do not depend on the order of events."""
+        e, p = (C.c_int64 * 7)(), (C.c_int64 * 7)()
+        lib().oracle_engine_wall_ledger_fixed(self._h, e, p)
+        return list(e), list(p)
 
     def ledger(self):
         """The bath's ledger slot and the clock: (energy summed in f64 in particle order, the

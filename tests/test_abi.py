@@ -142,10 +142,11 @@ def test_heat_bath_builders_and_validation(engine_lib):
         assert b"bath" in engine_lib.gbmd_last_error(), field
 
 
-def test_walls_builders_and_the_engine_refusal(engine_lib):
+def test_walls_builders_and_the_engine_checks(engine_lib):
     """with_walls clears the axis's periodic bit and records each side's kind (and a thermal
-    wall's kT); periodic / deterministic / has_soft_walls follow md-core. The GPU engine runs
-    periodic systems only and refuses walls before any device work."""
+    wall's kT); periodic / deterministic / has_soft_walls follow md-core. The GPU engine checks
+    the walls before any device work: a walled axis needs a wall kind on each side and a thermal
+    wall a finite kT >= 0. It refuses membranes and compartments."""
     from micrographia_gb300 import Pair, System, System3, Wall, box_for, cube_for
 
     s = System(box_for(200, 0.5, 1.0), 0.005, Pair.wca(), [1.0]).with_walls(1, Wall.soft(), Wall.thermal(1.5))
@@ -160,8 +161,14 @@ def test_walls_builders_and_the_engine_refusal(engine_lib):
     sp = np.zeros(n, np.uint32)
     P = lambda a, t: a.ctypes.data_as(C.POINTER(t))
     h = C.c_void_p()
-    rc = engine_lib.gbmd_create(C.byref(c), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
-    assert rc == _abi.E_UNSUPPORTED and b"wall" in engine_lib.gbmd_last_error()
+    bad = s.to_c()
+    bad.wall_t[1][1] = -1.0
+    rc = engine_lib.gbmd_create(C.byref(bad), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
+    assert rc == _abi.E_INVALID and b"thermal wall" in engine_lib.gbmd_last_error()
+    bad = s.to_c()
+    bad.wall_kind[1][0] = 0
+    rc = engine_lib.gbmd_create(C.byref(bad), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
+    assert rc == _abi.E_INVALID and b"wall" in engine_lib.gbmd_last_error()
     # a membrane needs walls on its axis (system.rs:259-265); the engine refuses membranes
     with pytest.raises(ValueError):
         System(box_for(200, 0.5, 1.0), 0.005, Pair.wca(), [1.0]).with_membrane(0, 5.0, [0])

@@ -1,0 +1,155 @@
+"""Walls on the GPU engine (md_core::walls, walls.rs): hard, soft and thermal walls, against the
+oracle's IntEngine (md-ref int_engine.rs:203-227, 256-263, 316-330, 363-390; int_engine3.rs:107-126,
+140-145, 186-205), bit for bit, with the ledger.
+
+The ledger is compared exactly in the order-free form the engine keeps (each event's energy change
+and impulse rounded to 2^-24 and summed as integers; the hit counts), and the oracle's f64 sums in
+particle order within half a unit of 2^-24 per event. The scenarios follow the reference's own wall
+tests (crates/md-ref/tests/boundaries.rs:6-110)."""
+
+import numpy as np
+import pytest
+
+from micrographia_gb300 import ONE, ForceMode, GpuEngine, GpuEngine3, Pair, State, State3, System, System3, Wall, box_for, cube_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _same_ledger(g, c):
+    """GPU ledger (each event rounded to 2^-24, integer sums) against the oracle's."""
+    ge, gp, gh = g.read_ledger()
+    oe, op = c.wall_ledger_fixed()
+    fe, fp, oh = c.wall_ledger()
+    assert list(gh) == list(oh)
+    assert [round(x * 2**24) for x in ge] == list(oe)
+    assert [round(x * 2**24) for x in gp] == list(op)
+    for w in range(7):  # the f64 sums in particle order, within 2^-25 per event
+        events = max(int(oh[w]), 1)
+        assert abs(ge[w] - fe[w]) <= events * 2.0**-25 + 1e-12
+    return sum(gh)
+
+
+def _gas_in_walls(O, n, density, seed, kind, gravity):
+    """boundaries.rs:6-35: a WCA gas in a box walled on both axes (hard or soft), with gravity."""
+    w = Wall.hard() if kind == "hard" else Wall.soft()
+    sys_ = System(box_for(n, density, 1.0), 0.005, Pair.wca(), [1.0]).with_walls(1, w, w).with_walls(0, w, w)
+    sys_.with_gravity([0.0, -gravity])
+    return sys_, O.fluid(sys_, n, 1.0, seed)
+
+
+@pytest.mark.parametrize("kind", ["hard", "soft"])
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_walls_with_gravity_follow_the_oracle_and_reverse(O, kind, mode):
+    """boundaries.rs:12-35 on the GPU: 400 WCA discs between hard (soft) walls on both axes under
+    gravity, 2000 steps equal IntEngine's bit for bit with the same ledger; then reversed, 2000
+    steps and reversed again, the initial state exactly."""
+    n = 400
+    sys_, s0 = _gas_in_walls(O, n, 0.3, 1, kind, 0.5)
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_with_skin(sys_, n, 0.3)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, m) as g:
+        g.step(2000)
+        c.step(2000)
+        assert g.read_state() == c.state
+        hits = _same_ledger(g, c)
+        if kind == "hard":
+            assert hits > 100
+        else:
+            assert sum(g.read_ledger()[1]) > 1.0  # the soft walls were pushed
+        kg, _ = g.kicks()
+        kc, _ = c.kicks()
+        assert np.array_equal(kg, kc)
+        g.reverse()
+        g.step(2000)
+        g.reverse()
+        assert g.read_state() == s0
+
+
+def test_soft_walls_energy_matches_the_oracle(O):
+    """The instruments with soft walls (the walls' WCA potential in forces(), int_engine.rs:
+    203-227): the GPU's kicks equal the oracle's, the potential within 1e-9 relative."""
+    n = 600
+    w = Wall.soft()
+    sys_ = System(box_for(n, 0.5, 1.5), 0.005, Pair.lj(2.5), [1.0]).with_walls(0, w, w)
+    s0 = O.fluid(sys_, n, 1.0, 3)
+    c = O.IntEngine(sys_, s0)
+    c.step(300)
+    st = c.state
+    with GpuEngine(sys_, st, ForceMode.verlet_with_skin(sys_, n, 0.3)) as g:
+        kg, _ = g.kicks()
+        ke, pe = g.energy()
+    kc, _ = c.kicks()
+    assert np.array_equal(kg, kc)
+    oke, ope = c.energy()
+    assert abs(pe - ope) <= 1e-9 * abs(ope) + 1e-9
+    assert abs(ke - oke) <= 1e-9 * abs(oke)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_thermal_walls_follow_the_oracle(O, dim):
+    """Non-interacting particles (a 0.1-sigma pair) at up to 0.25 sigma per step between a hot and
+    a cold thermal wall (and, in 3D, hard walls on z): every collision draws on (id, step clock)
+    as walls::thermal_velocity / three::thermal_velocity do; 600 steps equal the oracle's bit for
+    bit, with the same ledger."""
+    L, n = 12.0, 64
+    tiny = Pair(1.0, 0.1, 0.1 * 2 ** (1 / 6))
+    box = [int(L * ONE)] * dim
+    hot, cold = Wall.thermal(2.0), Wall.thermal(0.5)
+    if dim == 2:
+        sys_ = System(box, 0.005, tiny, [1.0, 3.0]).with_walls(0, hot, cold)
+    else:
+        sys_ = System3(box, 0.005, tiny, [1.0, 3.0]).with_walls(0, hot, cold).with_walls(2, Wall.hard(), Wall.hard())
+    sys_.seed = 0x2468_ACE0_1357
+    rng = np.random.default_rng(5)
+    pos = ((rng.random((n, dim)) * (L - 2) + 1) * ONE).astype(np.int64)
+    vel = (rng.choice([-1, 1], (n, dim)) * rng.uniform(0.05, 0.25, (n, dim)) * ONE).astype(np.int32)
+    sp = np.array([k % 2 for k in range(n)], np.uint32)
+    st = (State if dim == 2 else State3)(pos, vel, sp)
+    cls = GpuEngine if dim == 2 else GpuEngine3
+    c = O.IntEngine(sys_, st)
+    with cls(sys_, st, ForceMode.cell_list()) as g:
+        for _ in range(6):
+            g.step(100)
+            c.step(100)
+            assert g.read_state() == c.state
+        hits = _same_ledger(g, c)
+    assert hits > 50
+
+
+def test_thermal_walls_set_the_temperature(O):
+    """boundaries.rs:91-110 on the GPU: a dilute WCA gas at T = 0.5 between thermal walls at 1.5
+    reaches T = 1.5 within 0.06, taking more than 0.5 epsilon per particle from the walls."""
+    n = 150
+    w = Wall.thermal(1.5)
+    sys_ = System(box_for(n, 0.1, 1.0), 0.005, Pair.wca(), [1.0]).with_walls(0, w, w).with_walls(1, w, w)
+    s0 = O.fluid(sys_, n, 0.5, 4)
+    with GpuEngine(sys_, s0, ForceMode.cell_list()) as g:
+        g.step(40000)
+        t = 0.0
+        for _ in range(200):
+            g.step(100)
+            ke, _ = g.energy()
+            t += ke / n / 200  # 2D: T = KE / N (kT per particle of 2 degrees of freedom)
+        heat = sum(g.read_ledger()[0])
+    assert abs(t - 1.5) < 0.06, t
+    assert heat > 0.5 * n
+
+
+def test_walled_liquid_3d_follows_the_oracle(O):
+    """A 3D LJ liquid (N = 20,000, rho 0.8) between soft walls on z, Verlet lists: 300 steps equal
+    IntEngine3's bit for bit, with the same ledger, and a frame's RDF equals the oracle's counts
+    (plain differences across the walled axis)."""
+    n = 20_000
+    sys3 = System3(cube_for(n, 0.8), 0.005, Pair.lj(2.5), [1.0]).with_walls(2, Wall.soft(), Wall.soft())
+    s0 = O.fcc_maxwell(sys3, n, 1.0, 7, jitter=0.05)
+    # keep the lattice a sigma clear of the walls: squeeze z into [1, L - 1)
+    L = sys3.box_len[2]
+    s0.pos[:, 2] = (ONE + s0.pos[:, 2].astype(np.float64) / L * (L - 2 * ONE)).astype(np.int64)
+    c = O.IntEngine(sys3, s0, threads=8)
+    with GpuEngine3(sys3, s0, ForceMode.verlet_with_skin(sys3, n, 0.3)) as g:
+        g.step(300)
+        c.step(300)
+        assert g.read_state() == c.state
+        _same_ledger(g, c)
+        f, rdf, _ = g.observe(rdf_bins=100, rdf_rmax=3.0)
+    assert np.array_equal(rdf, O.rdf(sys3, c.state, 100, 3.0))
