@@ -67,7 +67,9 @@ def test_walls_with_gravity_follow_the_oracle_and_reverse(O, kind, mode):
 
 def test_soft_walls_energy_matches_the_oracle(O):
     """The instruments with soft walls (the walls' WCA potential in forces(), int_engine.rs:
-    203-227): the GPU's kicks equal the oracle's, the potential within 1e-9 relative."""
+    203-227): the GPU's kicks equal the oracle's; the potential within 1e-5 relative (the oracle
+    sums each particle's f32 pair energies in f32, as IntEngine<f32> does; the GPU sums them more
+    exactly), the kinetic energy within 1e-9."""
     n = 600
     w = Wall.soft()
     sys_ = System(box_for(n, 0.5, 1.5), 0.005, Pair.lj(2.5), [1.0]).with_walls(0, w, w)
@@ -81,7 +83,7 @@ def test_soft_walls_energy_matches_the_oracle(O):
     kc, _ = c.kicks()
     assert np.array_equal(kg, kc)
     oke, ope = c.energy()
-    assert abs(pe - ope) <= 1e-9 * abs(ope) + 1e-9
+    assert abs(pe - ope) <= 1e-5 * abs(ope)
     assert abs(ke - oke) <= 1e-9 * abs(oke)
 
 
