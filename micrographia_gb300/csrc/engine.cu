@@ -59,8 +59,18 @@ int validate_system(const gbmd_system& sys, uint32_t n) {
                 return fail(GBMD_E_INVALID, "a thermal wall needs a finite temperature >= 0");
         }
     }
-    if (sys.membrane) return fail(GBMD_E_UNSUPPORTED, "membranes are not part of this engine");
-    if (sys.compartments[0] || sys.compartments[1]) return fail(GBMD_E_UNSUPPORTED, "compartments are not part of this engine");
+    if (sys.membrane) {
+        if (sys.dim != 2) return fail(GBMD_E_UNSUPPORTED, "membranes are two-dimensional (md_core::Membrane)");
+        if (sys.membrane_axis >= 2 || ((sys.periodic >> sys.membrane_axis) & 1u))
+            return fail(GBMD_E_INVALID, "a membrane lies across a walled axis (system.rs:259-265)");
+        if (sys.membrane_pore_shift > 62) return fail(GBMD_E_INVALID, "bad membrane pore spacing");
+    }
+    if (sys.compartments[0] || sys.compartments[1]) {
+        if (sys.dim != 2) return fail(GBMD_E_UNSUPPORTED, "compartments are two-dimensional (System::with_compartments)");
+        for (uint32_t a = 0; a < 2; a++)
+            if (sys.compartments[a] && (((sys.periodic >> a) & 1u) || sys.compartments[a] > 62))
+                return fail(GBMD_E_INVALID, "compartments split a walled axis (system.rs:233-241)");
+    }
     for (uint32_t a = 0; a < sys.dim; a++)
         if (sys.box_len[a] <= 0) return fail(GBMD_E_INVALID, "box lengths must be positive");
     for (uint32_t k = 0; k < sys.nspecies * sys.nspecies; k++) {
@@ -205,6 +215,16 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
                 P.wall_t[a][side] = s.wall_t[a][side];
             }
         }
+    }
+    if (s.dim == 2) {
+        P.membrane = s.membrane ? 1u : 0u;
+        P.membrane_axis = s.membrane_axis;
+        P.membrane_blocks = s.membrane_blocks;
+        P.membrane_pore_shift = s.membrane_pore_shift;
+        P.membrane_position = s.membrane_position;
+        P.membrane_pore_width = s.membrane_pore_width;
+        for (int a = 0; a < 2; a++) P.comp_shift[a] = s.compartments[a];
+        P.comp_filter = (s.compartments[0] || s.compartments[1]) && !s.compartments_diathermal ? 1u : 0u;
     }
     P.wall_key[0] = (uint32_t)s.seed;
     P.wall_key[1] = (uint32_t)(s.seed >> 32) ^ 0x57414c4cu; // STREAM_WALL (walls.rs:86)
@@ -518,6 +538,12 @@ template <int D, bool MULTI> void enqueue_rebuild_t(gbmd_engine* e, cudaStream_t
     }
 #undef GBMD_BUILD
     note_launch();
+    if constexpr (D == 2) {
+        if (e->P.comp_filter) {
+            k_filter_compartments<<<blocks_for(e->n, 128), 128, 0, s>>>(e->P, (const Rec<2>*)e->pos[e->cur], e->nbr, e->nbr_count);
+            note_launch();
+        }
+    }
 }
 
 __global__ void k_set_cond(cudaGraphConditionalHandle h, const uint32_t* ctl) { cudaGraphSetConditional(h, ctl[0] ? 1u : 0u); }

@@ -995,6 +995,29 @@ __global__ void k_bath(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict_
     }
 }
 
+// Insulating compartments with Verlet lists: the build lists every pair within the list radius;
+// this pass drops, in place, the pairs whose particles are in different boxes (they never interact,
+// int_engine.rs:161-163, and a particle never leaves its box, so the list stays right until the
+// next build). The compartment axes are walled: no periodic image enters.
+static __global__ void k_filter_compartments(Params P, const PosRec<2>* __restrict__ pos, uint32_t* __restrict__ nbr,
+                                      uint32_t* __restrict__ nbr_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    int64_t xi[3];
+    load_particle<2, false>(pos, nullptr, i, xi);
+    const uint32_t m = nbr_count[i], cap4 = (P.cap + 3u) & ~3u;
+    uint32_t kept = 0;
+    for (uint32_t q = 0; q < m; q++) {
+        const uint32_t e = nbr[list_slot(i, q, cap4)];
+        int64_t xj[3];
+        load_particle<2, false>(pos, nullptr, e & LIST_MASK, xj);
+        if (!same_compartment(P.comp_shift, xi, xj)) continue;
+        nbr[list_slot(i, kept, cap4)] = e;
+        kept++;
+    }
+    nbr_count[i] = kept;
+}
+
 // ---------------------------------------------------------------- walls
 // md_core::walls (walls.rs) as IntEngine runs them (int_engine.rs:203-227 and 256-263, the soft
 // walls' kicks and impulses; 316-330, the mirror; 363-390, collide; int_engine3.rs:107-126,
@@ -1082,6 +1105,27 @@ __global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict
     }
     if (P.bath && bath_one<D>(P, si, id, clock, x, v, ledger + 3 * GBMD_LEDGER_BATH)) changed = true;
     const double m = P.masses[si];
+    int64_t old[3];
+#pragma unroll
+    for (int a = 0; a < D; a++) old[a] = x[a] - (int64_t)v[a]; // the position before the move
+    if (D == 2 && P.membrane && ((P.membrane_blocks >> si) & 1u)) {
+        // the membrane (int_engine.rs:296-313, walls::cross_membrane walls.rs:18-25): a blocked
+        // species that crossed it outside a pore is mirrored about position - 1/2
+        const uint32_t a = P.membrane_axis;
+        // (the other axis may be periodic and, with Verlet lists, left unwrapped between builds)
+        const int64_t w = P.membrane_position, along = ((P.periodic >> (1 - a)) & 1u) ? wrap(old[1 - a], P.box[1 - a]) : old[1 - a];
+        const bool pore = P.membrane_pore_shift != 0 && (along & (((int64_t)1 << P.membrane_pore_shift) - 1)) < P.membrane_pore_width;
+        if (!pore && (old[a] < w) != (x[a] < w)) {
+            const int face = old[a] < w ? 4 : 5; // walls::MEMBRANE faces (walls.rs:7-14)
+            x[a] = 2 * w - 1 - x[a];
+            const double vel_a = __ddiv_rn(__dmul_rn((double)v[a], 1.0 / 4294967296.0), P.dt);
+            const double dp = __dmul_rn(__dmul_rn(2.0, m), fabs(vel_a));
+            v[a] = (int32_t)(0u - (uint32_t)v[a]);
+            atomicAdd(ledger + 3 * face + 1, 1ull);
+            atomicAdd(ledger + 3 * face + 2, ledger_fixed(dp));
+            changed = true;
+        }
+    }
 #pragma unroll
     for (int a = 0; a < D; a++) {
         if ((P.periodic >> a) & 1u) {
@@ -1096,7 +1140,21 @@ __global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict
             x[a] = 2 * P.box[a] - 1 - x[a];
             side = 1;
         }
-        if (side < 0) continue;
+        if (side < 0) {
+            if (D == 2 && a < 2 && P.comp_shift[a]) {
+                // a particle that crossed into another compartment is mirrored back into its home
+                // one (int_engine.rs:324-330, walls::mirror_compartment walls.rs:72-78)
+                const uint32_t sh = P.comp_shift[a];
+                const int64_t home = old[a] >> sh;
+                if ((x[a] >> sh) != home) {
+                    const int64_t lo = home << sh, hi = (home + 1) << sh;
+                    x[a] = x[a] < lo ? 2 * lo - 1 - x[a] : (x[a] >= hi ? 2 * hi - 1 - x[a] : x[a]);
+                    v[a] = (int32_t)(0u - (uint32_t)v[a]);
+                    changed = true;
+                }
+            }
+            continue;
+        }
         changed = true;
         double before[3], after[3];
         auto vel_of = [&](int32_t q) { return __ddiv_rn(__dmul_rn((double)q, 1.0 / 4294967296.0), P.dt); };
@@ -1164,6 +1222,7 @@ __global__ void __launch_bounds__(128) k_force_cells(Params P, const PosRec<D>* 
             if (j == i) continue;
             int64_t xj[3];
             uint32_t sj = load_particle<D, MULTI>(pos_s, species_s, j, xj);
+            if (D == 2 && P.comp_filter && !same_compartment(P.comp_shift, xi, xj)) continue; // int_engine.rs:161-163
             if constexpr (INT) {
                 int64_t d[3] = {0, 0, 0};
 #pragma unroll
@@ -1209,6 +1268,7 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
         auto visit = [&](uint32_t j) {
             int64_t xj[3];
             uint32_t sj = load_particle<D, MULTI>(pos, species, j, xj);
+            if (D == 2 && P.comp_filter && !same_compartment(P.comp_shift, xi, xj)) return; // int_engine.rs:161-163
             if constexpr (INT) {
                 int64_t d[3] = {0, 0, 0};
 #pragma unroll

@@ -1233,6 +1233,7 @@ template <typename F> struct IntEngine {
                         const double dp = 2.0 * sys.masses[sp] * std::fabs(sys.velocity(v[a]));
                         v[a] = wneg(v[a]);
                         ledger.impulse[face] += dp;
+                        ledger.impulse_fixed[face] += ledger_fixed(dp);
                         ledger.hits[face] += 1;
                     }
                 }

@@ -146,7 +146,7 @@ def test_walls_builders_and_the_engine_checks(engine_lib):
     """with_walls clears the axis's periodic bit and records each side's kind (and a thermal
     wall's kT); periodic / deterministic / has_soft_walls follow md-core. The GPU engine checks
     the walls before any device work: a walled axis needs a wall kind on each side and a thermal
-    wall a finite kT >= 0. It refuses membranes and compartments."""
+    wall a finite kT >= 0; a membrane and compartments need a walled axis."""
     from micrographia_gb300 import Pair, System, System3, Wall, box_for, cube_for
 
     s = System(box_for(200, 0.5, 1.0), 0.005, Pair.wca(), [1.0]).with_walls(1, Wall.soft(), Wall.thermal(1.5))
@@ -176,9 +176,9 @@ def test_walls_builders_and_the_engine_checks(engine_lib):
     m.with_membrane(0, 8.0, [1]).with_pores(2, 0.5)
     cm = m.to_c()
     assert (cm.membrane, cm.membrane_axis, cm.membrane_blocks, cm.membrane_pore_shift) == (1, 0, 0b10, 34)
-    cm.periodic = 0b11  # even on a periodic box the membrane alone is refused
+    cm.periodic = 0b11  # a membrane lies across a walled axis
     rc = engine_lib.gbmd_create(C.byref(cm), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
-    assert rc == _abi.E_UNSUPPORTED and b"membrane" in engine_lib.gbmd_last_error()
+    assert rc == _abi.E_INVALID and b"membrane" in engine_lib.gbmd_last_error()
     # compartments need walls and whole boxes (system.rs:233-241); the engine refuses them
     from micrographia_gb300 import ONE
 
@@ -192,9 +192,9 @@ def test_walls_builders_and_the_engine_checks(engine_lib):
     cc = box.to_c()
     assert list(cc.compartments) == [35, 0] and cc.compartments_diathermal == 1
     assert box.compartment_counts() == [4, 1] and box.compartment_of([17 * ONE, 3 * ONE]) == [2, 0]
-    cc.periodic = 0b11
+    cc.periodic = 0b11  # compartments split a walled axis
     rc = engine_lib.gbmd_create(C.byref(cc), P(pos, C.c_int64), P(vel, C.c_int32), P(sp, C.c_uint32), n, None, C.byref(h))
-    assert rc == _abi.E_UNSUPPORTED and b"compartment" in engine_lib.gbmd_last_error()
+    assert rc == _abi.E_INVALID and b"compartment" in engine_lib.gbmd_last_error()
 
 
 def test_static_binning_rejects_bad_grids_before_any_device_work(engine_lib):

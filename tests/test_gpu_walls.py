@@ -155,3 +155,70 @@ def test_walled_liquid_3d_follows_the_oracle(O):
         _same_ledger(g, c)
         f, rdf, _ = g.observe(rdf_bins=100, rdf_rmax=3.0)
     assert np.array_equal(rdf, O.rdf(sys3, c.state, 100, 3.0))
+
+
+# ---------------------------------------------------------------- membranes and compartments (2D)
+@pytest.mark.parametrize("diathermal", [False, True])
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_compartments_follow_the_oracle_and_reverse(O, diathermal, mode):
+    """md-ref/tests/boundaries.rs:154-181 on the GPU: 16 x 16 compartments of 8 sigma between hard
+    walls, 6 particles each; insulating (pairs in different boxes do not interact) or diathermal.
+    1500 steps equal IntEngine's bit for bit; every particle is still in its own box; the run
+    reverses exactly."""
+    from test_oracle import _compartment_fluid
+
+    side = 8 * ONE
+    sys_ = System([16 * side, 16 * side], 0.005, Pair.wca(), [1.0])
+    sys_.with_walls(0, Wall.hard(), Wall.hard()).with_walls(1, Wall.hard(), Wall.hard())
+    sys_.with_compartments(0, 3).with_compartments(1, 3)
+    if diathermal:
+        sys_.with_diathermal_compartments()
+    s0 = _compartment_fluid(O, sys_, 6, 1.0, 7)
+    home = [sys_.compartment_of(p) for p in s0.pos]
+    n = s0.n()
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_with_skin(sys_, n, 0.3)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, m) as g:
+        g.step(1500)
+        c.step(1500)
+        got = g.read_state()
+        assert got == c.state
+        assert [sys_.compartment_of(p) for p in got.pos] == home
+        _same_ledger(g, c)
+        g.reverse()
+        g.step(1500)
+        g.reverse()
+        assert g.read_state() == s0
+
+
+@pytest.mark.parametrize("mode,pores", [("cells", False), ("verlet", False), ("verlet", True)])
+def test_membrane_follows_the_oracle(O, mode, pores):
+    """md-ref/tests/boundaries.rs:241-268 on the GPU: soft walls on x, a membrane at the middle
+    blocking species 1 (the solute, 20% of the right half), optionally with pores 0.5 sigma wide
+    every 2 sigma: 3000 steps equal IntEngine's bit for bit with the same ledger (membrane faces 4
+    and 5); without pores no solute crossed."""
+    from micrographia_gb300.workloads import uniform
+
+    from micrographia_gb300 import to_f64
+
+    n = 1200
+    sys_ = System(box_for(n, 0.4, 2.0), 0.005, Pair.wca(), [1.0, 1.0]).with_walls(0, Wall.soft(), Wall.soft())
+    half = sys_.box_f64()[0] / 2.0
+    sys_.with_membrane(0, half, [1])
+    if pores:
+        sys_.with_pores(1, 0.5)
+    s0 = O.fluid(sys_, n, 1.0, 13)
+    for i in range(n):
+        if to_f64(int(s0.pos[i, 0])) > half + 1.0 and uniform(13, 3, i) < 0.2:
+            s0.species[i] = 1
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_with_skin(sys_, n, 0.3)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, m) as g:
+        g.step(3000)
+        c.step(3000)
+        st = g.read_state()
+        assert st == c.state
+        _same_ledger(g, c)
+        assert g.read_ledger()[2][5] > 20  # the solute hit the membrane from the right
+    if not pores:
+        assert all(to_f64(int(p)) > half - 0.5 for p in st.pos[st.species == 1, 0])
