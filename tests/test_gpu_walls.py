@@ -219,6 +219,7 @@ def test_membrane_follows_the_oracle(O, mode, pores):
         st = g.read_state()
         assert st == c.state
         _same_ledger(g, c)
-        assert g.read_ledger()[2][5] > 20  # the solute hit the membrane from the right
+        hits_right = g.read_ledger()[2][5]
     if not pores:
+        assert hits_right > 20  # the solute hit the membrane from the right
         assert all(to_f64(int(p)) > half - 0.5 for p in st.pos[st.species == 1, 0])
