@@ -15,6 +15,7 @@ works without a GPU, and every engine call fails loudly when the library or the 
 from .core import (
     DT,
     ONE,
+    Bond,
     ForceMode,
     Pair,
     State,
@@ -24,6 +25,7 @@ from .core import (
     Thermostat,
     Wall,
     box_for,
+    chains,
     cube_for,
     fcc_cells,
     to_f64,
@@ -35,6 +37,7 @@ from . import init, workloads
 __all__ = [
     "DT",
     "ONE",
+    "Bond",
     "ForceMode",
     "Pair",
     "State",
@@ -48,6 +51,7 @@ __all__ = [
     "BatchEngine",
     "Server",
     "box_for",
+    "chains",
     "cube_for",
     "fcc_cells",
     "to_f64",

@@ -115,9 +115,28 @@ class _SystemBase:
         self.membrane = None  # (axis, position, blocks mask, pore_shift, pore_width), 2D
         self.compartments = [0, 0]  # shift per axis (32 + log2 side), 2D
         self.compartments_diathermal = False
+        self.bond_types = []  # Bond values
+        self.bonds = []  # (id a, id b, type index)
 
     def species(self):
         return len(self.masses)
+
+    def with_bonds(self, types, bonds):
+        """System::with_bonds (system.rs:284-299): bond types (Bond values, at most 4) and bonds
+        (id a, id b, type index), at most 4 per particle."""
+        if len(types) > 4:
+            raise ValueError("at most 4 bond types")
+        count = {}
+        for a, b, t in bonds:
+            if a == b or t >= len(types):
+                raise ValueError("a bond joins two particles with a known type")
+            for p in (a, b):
+                count[p] = count.get(p, 0) + 1
+                if count[p] > 4:
+                    raise ValueError(f"particle {p} has more than 4 bonds")
+        self.bond_types = list(types)
+        self.bonds = [tuple(int(x) for x in b) for b in bonds]
+        return self
 
     def with_pair(self, a, b, pair):
         """System::with_pair (system.rs:201-207): both orders."""
@@ -237,6 +256,55 @@ class _SystemBase:
             s.bath_t, s.bath_rate, s.bath_drift = th.t, th.rate, th.drift
             s.bath_region[0], s.bath_region[1] = th.region
         return s
+
+
+class Bond:
+    """md_core::BondType (system.rs:70-96): Bond.harmonic(k, r0), U = k (r - r0)^2 / 2;
+    Bond.fene(k, r0), U = -k r0^2 ln(1 - (r / r0)^2) / 2; Bond.kremer_grest() = fene(30, 1.5)."""
+
+    def __init__(self, fene, k, r0):
+        self.fene, self.k, self.r0 = bool(fene), float(k), float(r0)
+
+    @staticmethod
+    def harmonic(k, r0):
+        return Bond(False, k, r0)
+
+    @staticmethod
+    def fene_bond(k, r0):
+        return Bond(True, k, r0)
+
+    @staticmethod
+    def kremer_grest():
+        return Bond(True, 30.0, 1.5)
+
+    def __eq__(self, o):
+        return isinstance(o, Bond) and (self.fene, self.k, self.r0) == (o.fene, o.k, o.r0)
+
+    def __repr__(self):
+        return f"Bond.{'fene_bond' if self.fene else 'harmonic'}({self.k}, {self.r0})"
+
+
+def chains(sys, chains, length, bond):
+    """init::chains (md-core/src/init.rs:196-217): `chains` straight chains of `length` beads,
+    `bond` sigma apart, laid out in rows 1 sigma clear of the box edges; returns the positions
+    (id order) and the bonds (id a, id b, type 0)."""
+    b = [to_f64(sys.box_len[0]), to_f64(sys.box_len[1])]
+    per_row = max(int(math.floor((b[0] - 2.0) / (length * bond + 1.0))), 1)
+    rows = -(-chains // per_row)
+    dy = (b[1] - 2.0) / rows
+    if dy < 1.0:
+        raise ValueError(f"box too small for {chains} chains of {length}")
+    pos, bonds = [], []
+    for c in range(chains):
+        row, col = c // per_row, c % per_row
+        x0 = 1.0 + col * (length * bond + 1.0)
+        y = 1.0 + (row + 0.5) * dy
+        for k in range(length):
+            i = len(pos)
+            pos.append([to_fixed(x0 + k * bond), to_fixed(y)])
+            if k > 0:
+                bonds.append((i - 1, i, 0))
+    return np.array(pos, np.int64), bonds
 
 
 class Wall:

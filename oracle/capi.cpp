@@ -295,6 +295,18 @@ void oracle_engine_wall_ledger(void* h, double* energy, double* impulse, uint64_
     const Ledger& l = e->f32 ? e->f32->ledger : e->f64->ledger;
     for (int w = 0; w < LEDGER_SLOTS; w++) energy[w] = l.energy[w], impulse[w] = l.impulse[w], hits[w] = l.hits[w];
 }
+// System::with_bonds: ntypes bond types (fene 1 or harmonic 0, k, r0) and nbonds bonds
+// (id a, id b, type), three words each.
+void oracle_engine_set_bonds(void* h, const uint32_t* fene, const double* k, const double* r0, uint32_t ntypes, const uint32_t* bonds,
+                             uint64_t nbonds) {
+    std::vector<BondType> t(ntypes);
+    for (uint32_t q = 0; q < ntypes; q++) t[q] = {fene[q] != 0, k[q], r0[q]};
+    std::vector<std::array<uint32_t, 3>> b(nbonds);
+    for (uint64_t q = 0; q < nbonds; q++) b[q] = {bonds[3 * q], bonds[3 * q + 1], bonds[3 * q + 2]};
+    Engine* e = (Engine*)h;
+    if (e->f32) e->f32->set_bonds(t, b);
+    else e->f64->set_bonds(t, b);
+}
 void oracle_engine_wall_ledger_fixed(void* h, int64_t* energy, int64_t* impulse) {
     const Ledger& l = ((Engine*)h)->f32 ? ((Engine*)h)->f32->ledger : ((Engine*)h)->f64->ledger;
     for (int w = 0; w < LEDGER_SLOTS; w++) {

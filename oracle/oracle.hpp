@@ -145,6 +145,15 @@ inline bool sep_f32(int64_t d, float* out) {
     *out = d < 0 ? -mag : mag;
     return true;
 }
+// fixed.rs:63-72: sep_f32 within 8 sigma; beyond, the magnitude's whole sigma plus its fraction
+// in f32, then the sign (bonds can be longer than the pair separation handles).
+inline float sep_long_f32(int64_t d) {
+    float s;
+    if (sep_f32(d, &s)) return s;
+    const uint64_t m = d < 0 ? (uint64_t)0 - (uint64_t)d : (uint64_t)d;
+    const float mag = (float)(uint32_t)(m >> 32) + (float)(uint32_t)m * (1.0f / 4294967296.0f);
+    return d < 0 ? -mag : mag;
+}
 // md-ref real.rs:59-64: branch-free sep for |d| < 8 sigma, bit-identical to sep_f32.
 inline float sep_near_f32(int64_t d) {
     int64_t q = (d + ((d >> 63) & 15)) >> 4;
@@ -610,6 +619,7 @@ template <typename F> struct Real;
 template <> struct Real<float> {
     static bool sep(int64_t d, float* o) { return sep_f32(d, o); }
     static float sep_near(int64_t d) { return sep_near_f32(d); }
+    static float sep_long(int64_t d) { return sep_long_f32(d); } // real.rs:52-54
     static float from_f64(double x) { return (float)x; }
     static int32_t round_to_i32(float x) { return sat_i32f(std::rint(x)); }
     static constexpr bool is_f32 = true;
@@ -621,10 +631,42 @@ template <> struct Real<double> {
         return true;
     }
     static double sep_near(int64_t d) { return to_f64(d); }
+    static double sep_long(int64_t d) { return to_f64(d); } // real.rs:91-93
     static double from_f64(double x) { return x; }
     static int32_t round_to_i32(double x) { return sat_i32(std::rint(x)); }
     static constexpr bool is_f32 = false;
 };
+// md_core::BondType (system.rs:70-96) and md-ref's BondConsts (real.rs:161-197): the bond's
+// -U'(r)/r and U at squared separation r2, in F, the reference's operation order.
+struct BondType {
+    bool fene = false; // else harmonic
+    double k = 0.0, r0 = 0.0;
+};
+template <typename F> struct BondConsts {
+    bool fene;
+    F k, r0;
+    static BondConsts make(const BondType& b) { return {b.fene, Real<F>::from_f64(b.k), Real<F>::from_f64(b.r0)}; }
+    void eval(F r2, F* fr, F* u) const {
+        const F one = Real<F>::from_f64(1.0), half = Real<F>::from_f64(0.5);
+        if (fene) {
+            F x = r2 / (r0 * r0);
+            const F cap = Real<F>::from_f64(0.999999);
+            if (x > cap) x = cap;
+            *u = -half * k * r0 * r0 * Real<F>::from_f64(std::log((double)(one - x)));
+            *fr = -k / (one - x);
+        } else if (r0 == Real<F>::from_f64(0.0)) { // a zero-length spring (tethers): -k exactly
+            *fr = -k;
+            *u = half * k * r2;
+        } else {
+            const F r = std::sqrt(r2);
+            const F dr = r - r0;
+            *fr = -k * dr / r;
+            *u = half * k * dr * dr;
+        }
+    }
+};
+constexpr uint32_t MAX_BONDS = 4; // system.rs:66
+
 // real.rs:105-157
 template <typename F> struct PairConsts {
     F rc2, eps4, sigma2, shift;
@@ -1018,8 +1060,27 @@ template <typename F> struct IntEngine {
     IntTables* tables = nullptr;
     FastScratch<F> scratch;
     int threads = 1; // OpenMP threads for the 3D/2D reference loop (the CPU baseline)
+    // Bonds (2D; md-ref int_engine.rs:27-29, 55-56): per particle id its partners' ids and bond
+    // types (System::partner_table, system.rs:311-324), padded with UINT32_MAX.
+    std::vector<BondConsts<F>> bond_consts;
+    std::vector<std::array<uint32_t, 2 * MAX_BONDS>> partners;
 
     IntEngine(const System& s, const State& st) : state(st) { set_system(s); }
+    // System::with_bonds (system.rs:284-299) and the engine's partner table.
+    void set_bonds(const std::vector<BondType>& types, const std::vector<std::array<uint32_t, 3>>& bonds) {
+        bond_consts.clear();
+        for (auto& t : types) bond_consts.push_back(BondConsts<F>::make(t));
+        partners.assign(bonds.empty() ? 0 : state.n(), {});
+        for (auto& p : partners) p.fill(UINT32_MAX);
+        std::vector<uint32_t> used(state.n(), 0);
+        for (auto& b : bonds)
+            for (int e = 0; e < 2; e++) {
+                const uint32_t me = e ? b[1] : b[0], other = e ? b[0] : b[1];
+                const uint32_t k = used[me]++;
+                partners[me][2 * k] = other;
+                partners[me][2 * k + 1] = b[2];
+            }
+    }
     // The constructor's derived constants; alone, a run-time change of system (GpuEngine::
     // update_system, engine.rs:895-934) that keeps the state, counters, clock and ledger.
     void set_system(const System& s) {
@@ -1105,6 +1166,27 @@ template <typename F> struct IntEngine {
                 }
             }
         }
+        // bonds (int_engine.rs:185-202): rounded per bond like pairs, separations by sep_long
+        double bond_part = 0.0;
+        if (!partners.empty()) {
+            F bond_pe = (F)0;
+            for (uint32_t q = 0; q < MAX_BONDS; q++) {
+                const uint32_t j = partners[i][2 * q];
+                if (j == UINT32_MAX) break;
+                const BondConsts<F>& bc = bond_consts[partners[i][2 * q + 1]];
+                const int64_t* pj = &state.pos[d * j];
+                F f[3] = {(F)0, (F)0, (F)0};
+                for (int a = 0; a < d; a++) f[a] = Real<F>::sep_long(sys.periodic(a) ? min_image(pi[a], pj[a], sys.box[a]) : pj[a] - pi[a]);
+                F r2 = f[0] * f[0] + f[1] * f[1];
+                if (d == 3) r2 = r2 + f[2] * f[2];
+                F fr, u;
+                bc.eval(r2, &fr, &u);
+                const F aa = -fr * c;
+                for (int a = 0; a < d; a++) k[a] = wadd(k[a], Real<F>::round_to_i32(aa * f[a]));
+                bond_pe += u;
+            }
+            bond_part = 0.5 * (double)bond_pe;
+        }
         // soft walls (int_engine.rs:203-227, int_engine3.rs:107-126): WCA in the distance to
         // the wall, in F, its kick rounded like a pair's
         double wall_pe = 0.0;
@@ -1128,7 +1210,7 @@ template <typename F> struct IntEngine {
             }
         }
         for (int a = 0; a < d; a++) kout[a] = k[a];
-        *pe_out = (tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i) + wall_pe;
+        *pe_out = bond_part + (tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i) + wall_pe;
     }
 
     // IntEngine::forces (int_engine.rs:130-251) / IntEngine3::forces (int_engine3.rs:48-131):
@@ -1141,7 +1223,7 @@ template <typename F> struct IntEngine {
         double pe = 0.0;
         wall_force.assign(n, {0, 0, 0, 0, 0, 0});
         // (with walls the reference loop: fast.rs gives the same kicks, fast_path.rs:20-54)
-        bool use_fast = d == 2 && fast && !tables && sys.all_periodic() && fast_eligible(sys, cl_dims);
+        bool use_fast = d == 2 && fast && !tables && partners.empty() && sys.all_periodic() && fast_eligible(sys, cl_dims);
         if (use_fast) return pair_kicks_fast<F>(sys, state, consts, kick_c, cl_dims, scratch, kicks.data());
         CellList cl = build_cells(sys, state, cl_dims);
         uint32_t nc[3] = {cl_dims[0], cl_dims[1], d == 3 ? cl_dims[2] : 1u};

@@ -64,6 +64,7 @@ _SIGS = [
     ("oracle_engine_set_system", None, [VP, SYS]),
     ("oracle_engine_wall_ledger", None, [VP, DP, DP, U64P]),
     ("oracle_engine_wall_ledger_fixed", None, [VP, I64P, I64P]),
+    ("oracle_engine_set_bonds", None, [VP, U32P, DP, DP, C.c_uint32, U32P, C.c_uint64]),
     ("oracle_engine_steps", C.c_int64, [VP]),
     ("oracle_engine_energy", None, [VP, DP, DP]),
     ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
@@ -320,6 +321,8 @@ class IntEngine:
         )
         if not self._h:
             raise ValueError("oracle engine creation failed")
+        if getattr(sys, "bonds", None):
+            self.set_bonds([("fene" if t.fene else "harmonic", t.k, t.r0) for t in sys.bond_types], sys.bonds)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -370,6 +373,17 @@ class IntEngine:
         e, p, h = (C.c_double * 7)(), (C.c_double * 7)(), (C.c_uint64 * 7)()
         lib().oracle_engine_wall_ledger(self._h, e, p, h)
         return list(e), list(p), list(h)
+
+    def set_bonds(self, types, bonds):
+        """System::with_bonds (system.rs:284-299): `types` a list of ("fene" | "harmonic", k, r0),
+        `bonds` a list of (id a, id b, type index)."""
+        nt = len(types)
+        fene = np.array([1 if t[0] == "fene" else 0 for t in types], np.uint32)
+        k = np.array([t[1] for t in types], np.float64)
+        r0 = np.array([t[2] for t in types], np.float64)
+        b = np.ascontiguousarray(np.array(bonds, np.uint32).reshape(-1, 3))
+        lib().oracle_engine_set_bonds(self._h, _p(fene, C.c_uint32), _p(k, C.c_double), _p(r0, C.c_double), nt, _p(b, C.c_uint32), len(b))
+        return self
 
     def wall_ledger_fixed(self):
         """Every ledger event's energy change and impulse rounded to 2^-24 and summed as integers

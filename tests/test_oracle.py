@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from micrographia_gb300 import ONE, Pair, System, System3, box_for, cube_for, fcc_cells, to_f64
+from micrographia_gb300 import ONE, Pair, State, System, System3, box_for, cube_for, fcc_cells, to_f64
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 VEC = json.load(open(os.path.join(HERE, "golden", "reference_vectors.json")))
@@ -653,3 +653,95 @@ def test_oracle_compartments_are_independent_and_reversible(O):
     e.step(3000)
     e.reverse()
     assert e.state == s0
+
+
+# ---------------------------------------------------------------- bonds (md-ref/tests/polymers.rs)
+def _melt(O, n_chains, length, density, seed):
+    """polymers.rs:6-14: Kremer-Grest chains (FENE k = 30, R0 = 1.5, WCA beads) laid out
+    straight (init::chains, bond 0.97 sigma), Maxwell velocities at T = 1."""
+    from micrographia_gb300 import Bond, chains
+
+    n = n_chains * length
+    sys_ = System(box_for(n, density, 1.0), 0.005, Pair.wca(), [1.0])
+    pos, bonds = chains(sys_, n_chains, length, 0.97)
+    sys_.with_bonds([Bond.kremer_grest()], bonds)
+    sp = np.zeros(n, np.uint32)
+    return sys_, State(pos, O.maxwell(sys_, sp, 1.0, seed), sp)
+
+
+def test_oracle_chains_are_exactly_reversible(O):
+    """polymers.rs:17-25: 20 chains of 20 beads at density 0.3, IntEngine<f32>: 2000 steps,
+    reverse, 2000 steps, reverse: the initial state exactly."""
+    sys_, s0 = _melt(O, 20, 20, 0.3, 1)
+    e = O.IntEngine(sys_, s0)
+    e.step(2000)
+    assert e.state != s0
+    e.reverse()
+    e.step(2000)
+    e.reverse()
+    assert e.state == s0
+
+
+def test_oracle_chains_hold_together_and_conserve_energy(O):
+    """polymers.rs:28-50: the f64 engine's energy per bead within 2e-3 over 2000 steps after 500,
+    and the mean bond length within 0.03 of the Kremer-Grest 0.97 sigma."""
+    sys_, s0 = _melt(O, 20, 20, 0.3, 2)
+    e = O.IntEngine(sys_, s0, f64=True)
+    e.step(500)
+    e0 = sum(e.energy())
+    worst = 0.0
+    for _ in range(10):
+        e.step(200)
+        worst = max(worst, abs(sum(e.energy()) - e0) / 400.0)
+    st = e.state
+    box = np.array(sys_.box_len, np.int64)
+    lengths = []
+    for a, b, _ in sys_.bonds:
+        d = st.pos[b] - st.pos[a]
+        d = np.where(d >= box // 2, d - box, np.where(d < -(box // 2), d + box, d))
+        lengths.append(math.hypot(*(d / 2**32)))
+    assert worst < 2e-3, worst
+    assert abs(np.mean(lengths) - 0.97) < 0.03, np.mean(lengths)
+
+
+def test_oracle_bond_kicks_match_a_python_restatement(O):
+    """A harmonic bond (k = 50, r0 = 1), a zero-length tether and a FENE bond stretched past its
+    0.999999 cap, between non-interacting particles: the oracle's kicks equal BondConsts::eval
+    (real.rs:175-196) and the rounding of IntEngine::forces (int_engine.rs:185-202) restated in
+    numpy f32, and Newton's third law holds exactly."""
+    from micrographia_gb300 import Bond
+
+    tiny = Pair(1.0, 0.1, 0.1 * 2 ** (1 / 6))
+    sys_ = System([int(40 * ONE), int(40 * ONE)], 0.005, tiny, [1.0, 2.0])
+    types = [Bond.harmonic(50.0, 1.0), Bond.harmonic(3.0, 0.0), Bond.fene_bond(30.0, 1.5)]
+    pos = np.array([[5, 5], [6.3, 5.4], [20, 20], [20.7, 21.1], [30, 30], [31.6, 30.05], [2, 2], [38.5, 39.2]], np.float64)
+    pos = (pos * ONE).astype(np.int64)
+    bonds = [(0, 1, 0), (2, 3, 1), (4, 5, 2), (6, 7, 0)]  # the last across the periodic boundary
+    sys_.with_bonds(types, bonds)
+    sp = np.array([0, 1, 0, 1, 0, 1, 1, 0], np.uint32)
+    st = State(pos, np.zeros((8, 2), np.int32), sp)
+    k, _ = O.IntEngine(sys_, st).kicks()
+    f32 = np.float32
+    box = np.array(sys_.box_len, np.int64)
+    for a, b, t in bonds:
+        assert (k[a].astype(np.int64) + k[b] == 0).all() or sys_.masses[sp[a]] != sys_.masses[sp[b]]
+        for i, j in ((a, b), (b, a)):
+            d = pos[j] - pos[i]
+            d = np.where(d >= box // 2, d - box, np.where(d < -(box // 2), d + box, d))
+            f = [f32(O.sep_f32(int(x))) for x in d]
+            r2 = f32(f[0] * f[0]) + f32(f[1] * f[1])
+            bt = types[t]
+            kk, r0 = f32(bt.k), f32(bt.r0)
+            if bt.fene:
+                x = min(f32(r2 / f32(r0 * r0)), f32(0.999999))
+                fr = f32(-kk / f32(f32(1) - x))
+            elif r0 == 0:
+                fr = -kk
+            else:
+                r = f32(np.sqrt(r2))
+                fr = f32(f32(-kk * f32(r - r0)) / r)
+            c = f32(sys_.dt * sys_.dt / sys_.masses[sp[i]] * 2**32)
+            aa = f32(-fr * c)
+            # round half to even, saturating like Rust's `as i32` (the stretched FENE bond saturates)
+            want = [int(min(max(np.rint(f32(aa * fa)), -(2**31)), 2**31 - 1)) for fa in f]
+            assert list(k[i]) == want, (i, j, t)
