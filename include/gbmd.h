@@ -237,6 +237,23 @@ int gbmd_sort_now(gbmd_engine* e);
  * tables (pairs, masses, dt, pinned). Velocities are kept as they are (position units per step).
  * The lists are rebuilt before the next step. GBMD_E_INVALID otherwise, the engine unchanged. */
 int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys);
+/* Bonds (md_core::BondType, system.rs:70-96; System::with_bonds, system.rs:284-299), 2D: `ntypes`
+ * bond types and `nbonds` bonds, three words each (particle id a, id b, type index), at most
+ * GBMD_MAX_BONDS per particle; each bond's kick is rounded on its own like a pair's
+ * (IntEngine::forces, int_engine.rs:185-202), with the separation's long form beyond 8 sigma
+ * (fixed.rs:63-72). Replaces the engine's bonds (nbonds 0: none), before stepping or between
+ * steps. GBMD_E_UNSUPPORTED in 3D (IntEngine3 has no bonds) and with integer table forces. */
+#define GBMD_MAX_BONDS 4      /* system.rs:66 */
+#define GBMD_MAX_BOND_TYPES 4 /* system.rs:67 */
+#define GBMD_BOND_HARMONIC 0  /* U = k (r - r0)^2 / 2 (a zero-length spring when r0 = 0) */
+#define GBMD_BOND_FENE 1      /* U = -k r0^2 ln(1 - (r / r0)^2) / 2, its argument capped at 1 - 1e-6 */
+typedef struct gbmd_bond_type {
+    uint32_t kind; /* GBMD_BOND_* */
+    uint32_t _pad;
+    double k;
+    double r0;
+} gbmd_bond_type;
+int gbmd_set_bonds(gbmd_engine* e, const gbmd_bond_type* types, uint32_t ntypes, const uint32_t* bonds, uint32_t nbonds);
 
 /* ---- Observables: IntEngine::energy (int_engine.rs:433-446) and the new instruments ---- */
 

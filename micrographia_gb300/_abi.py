@@ -72,6 +72,16 @@ class gbmd_system(C.Structure):
     ]
 
 
+MAX_BONDS = 4  # system.rs:66, bonds per particle
+MAX_BOND_TYPES = 4  # system.rs:67
+BOND_HARMONIC = 0  # md_core::BondType::Harmonic
+BOND_FENE = 1  # md_core::BondType::Fene
+
+
+class gbmd_bond_type(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("_pad", C.c_uint32), ("k", C.c_double), ("r0", C.c_double)]
+
+
 WALL_HARD = 1  # md_core::Wall::Hard: exact mirror
 WALL_SOFT = 2  # Wall::Soft: WCA repulsion from the wall
 WALL_THERMAL = 3  # Wall::Thermal(t): a hit draws a Maxwell-flux velocity at kT = t
@@ -210,6 +220,7 @@ SIGNATURES = [
     ("gbmd_set_species_velocity", C.c_int, [VP, C.c_uint32, _DP]),
     ("gbmd_sort_now", C.c_int, [VP]),
     ("gbmd_update_system", C.c_int, [VP, P(gbmd_system)]),
+    ("gbmd_set_bonds", C.c_int, [VP, P(gbmd_bond_type), C.c_uint32, P(C.c_uint32), C.c_uint32]),
     ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
     ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),
     ("gbmd_observe_begin", C.c_int, [VP, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32]),

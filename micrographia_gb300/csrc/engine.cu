@@ -397,6 +397,8 @@ struct gbmd_engine {
     uint32_t last_rebuilds = 0;
     bool failed = false;
     bool half = false;       // half-shell lists (k_build_half / k_force_half / k_leap_half)
+    uint32_t* bond_tab = nullptr; // bonds: per id 4 x (partner id, type), padded with UINT32_MAX
+    uint32_t* slot_of = nullptr;  // bonds: the storage slot of each id
     int32_t* acc = nullptr;  // half-shell kick accumulators, 3 x int32 per slot, zero between steps
     int32_t* itab = nullptr; // all-integer kick tables (GBMD_ARITH_INT)
     double* ipair = nullptr;
@@ -481,7 +483,7 @@ void free_all(gbmd_engine* e) {
     void* ptrs[] = {e->pos[0], e->pos[1], e->pos_scr, e->ref_pos, e->vel, e->vel_scr, e->kicks, e->species, e->species_scr, e->ids,
                     e->ids_scr, e->keys[0], e->keys[1], e->vals[0], e->vals[1], e->hist, e->scan_tmp, e->start, e->nbr,
                     e->nbr_count, e->ctl, e->partial, e->staging, e->staging_v, e->staging_s, e->mrank, e->tpart, e->vpart, e->tfac, e->relf, e->qpos[0], e->qpos[1],
-                    e->obs_bins, e->obs_start, e->itab, e->ipair, e->ledger, e->acc};
+                    e->obs_bins, e->obs_start, e->itab, e->ipair, e->ledger, e->acc, e->bond_tab, e->slot_of};
     for (void* p : ptrs)
         if (p) cudaFreeAsync(p, e->st);
     if (e->st) cudaStreamDestroy(e->st);
@@ -646,6 +648,17 @@ void enqueue_force(gbmd_engine* e, cudaStream_t s) {
         if (e->multi) enqueue_force_t<3, true>(e, s, threads);
         else enqueue_force_t<3, false>(e, s, threads);
     }
+    if (e->P.bonds && e->D == 2) { // the bonds' kicks from the step's start positions
+        const uint32_t nb = blocks_for(e->n, 256);
+        k_slot_of<<<nb, 256, 0, s>>>(e->n, e->ids, e->slot_of);
+        if (e->verlet)
+            k_bonds<2, true><<<nb, 256, 0, s>>>(e->P, (const Rec<2>*)e->pos[e->cur ^ 1], (Rec<2>*)e->pos[e->cur], e->qpos[e->cur], e->vel,
+                                                e->species, e->ids, (const Rec<2>*)e->ref_pos, e->ctl);
+        else
+            k_bonds<2, false><<<nb, 256, 0, s>>>(e->P, (const Rec<2>*)e->pos_scr, (Rec<2>*)e->pos[e->cur], nullptr, e->vel, e->species,
+                                                 e->ids, nullptr, e->ctl);
+        note_launch(2);
+    }
     if (e->P.walls) { // the soft walls' kicks, the bath, the mirror and collisions; then the clock
         const uint32_t nb = blocks_for(e->n, 256);
         unsigned long long* l = e->ledger;
@@ -769,7 +782,7 @@ cudaError_t enqueue_loop(gbmd_engine* e, cudaStream_t s) {
 // kernel's; fewer if the grid would not be resident.
 int setup_step_loop(gbmd_engine* e) {
     e->loop_lanes = 0;
-    if (!e->verlet || e->half || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath || e->P.walls ||
+    if (!e->verlet || e->half || e->multi || e->opt.arith != GBMD_ARITH_F32 || e->P.int_mode || e->opt.rescale_every || e->P.bath || e->P.walls || e->P.bonds ||
         (e->opt.flags & GBMD_FLAG_NO_STEP_LOOP))
         return GBMD_OK;
     // Larger systems' steps are long enough that the graph's per-step nodes cost less than the
@@ -969,11 +982,15 @@ int prepare_pairs(gbmd_engine* e) {
 template <int D, bool MULTI, bool INT> void kicks_launch(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
     uint32_t threads = 128;
     uint32_t nb = blocks_for(e->n, threads);
+    if (e->P.bonds) {
+        k_slot_of<<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->verlet ? e->ids : e->ids_scr, e->slot_of);
+        note_launch();
+    }
     if (e->verlet)
-        k_kicks<D, MULTI, INT><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos[e->cur], e->species, e->nbr, e->nbr_count, nullptr,
-                                                          nullptr, e->vel, kicks, partial, reverse);
+        k_kicks<D, MULTI, INT><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos[e->cur], e->species, e->ids, e->nbr, e->nbr_count,
+                                                          nullptr, nullptr, e->vel, kicks, partial, reverse);
     else
-        k_kicks<D, MULTI, INT><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos_scr, e->species_scr, nullptr, nullptr,
+        k_kicks<D, MULTI, INT><<<nb, threads, 0, e->st>>>(e->P, (const Rec<D>*)e->pos_scr, e->species_scr, e->ids_scr, nullptr, nullptr,
                                                           e->keys[e->sorted], e->start, e->vel_scr, kicks, partial, reverse);
 }
 template <int D, bool MULTI> int kicks_t(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
@@ -1411,7 +1428,7 @@ int gbmd_kicks(gbmd_engine* e, int32_t* kicks, double* potential) {
 // path, on the device so that it runs at full size.
 int gbmd_kicks_f64(gbmd_engine* e, int32_t* kicks, double* potential) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    if (e->P.walls) return fail(GBMD_E_UNSUPPORTED, "the f64 reference kicks are for periodic systems");
+    if (e->P.walls || e->P.bonds) return fail(GBMD_E_UNSUPPORTED, "the f64 reference kicks are for periodic pair systems");
     GBMD_TRY(prepare_pairs_cond(e));
     PairsF64 Q;
     std::memset(&Q, 0, sizeof(Q));
@@ -1546,6 +1563,58 @@ int gbmd_sort_now(gbmd_engine* e) {
     return gbmd_sync(e);
 }
 
+int gbmd_set_bonds(gbmd_engine* e, const gbmd_bond_type* types, uint32_t ntypes, const uint32_t* bonds, uint32_t nbonds) {
+    if (!e || (ntypes && !types) || (nbonds && !bonds)) return fail(GBMD_E_INVALID, "null argument");
+    if (e->D != 2 && nbonds) return fail(GBMD_E_UNSUPPORTED, "bonds are two-dimensional (IntEngine; IntEngine3 has none)");
+    if (e->opt.arith != GBMD_ARITH_F32 && nbonds) return fail(GBMD_E_UNSUPPORTED, "integer table forces take plain pair systems only");
+    if (ntypes > GBMD_MAX_BOND_TYPES) return fail(GBMD_E_INVALID, "at most GBMD_MAX_BOND_TYPES bond types");
+    for (uint32_t t = 0; t < ntypes; t++) {
+        const gbmd_bond_type& b = types[t];
+        if ((b.kind != GBMD_BOND_HARMONIC && b.kind != GBMD_BOND_FENE) || !(std::fabs(b.k) < INFINITY) || !(b.r0 >= 0.0 && b.r0 < INFINITY) ||
+            (b.kind == GBMD_BOND_FENE && !(b.r0 > 0.0)))
+            return fail(GBMD_E_INVALID, "a bond type is harmonic or FENE with finite k and r0 >= 0 (FENE: r0 > 0)");
+    }
+    std::vector<uint32_t> tab;
+    if (nbonds) {
+        tab.assign((size_t)e->n * 8, 0xffffffffu);
+        std::vector<uint32_t> used(e->n, 0);
+        for (uint32_t q = 0; q < nbonds; q++) {
+            const uint32_t a = bonds[3 * q], b = bonds[3 * q + 1], t = bonds[3 * q + 2];
+            if (a >= e->n || b >= e->n || a == b || t >= ntypes) return fail(GBMD_E_INVALID, "a bond joins two particles (ids < n) with a known type");
+            for (int end = 0; end < 2; end++) { // System::partner_table (system.rs:311-324)
+                const uint32_t me = end ? b : a, other = end ? a : b;
+                if (used[me] >= GBMD_MAX_BONDS) return fail(GBMD_E_INVALID, "at most GBMD_MAX_BONDS bonds per particle");
+                tab[(size_t)me * 8 + 2 * used[me]] = other;
+                tab[(size_t)me * 8 + 2 * used[me] + 1] = t;
+                used[me]++;
+            }
+        }
+    }
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    if (nbonds && !e->bond_tab) {
+        GBMD_TRY(allocT(e, &e->bond_tab, (size_t)e->n * 8));
+        GBMD_TRY(allocT(e, &e->slot_of, (size_t)e->n));
+    }
+    if (nbonds) GBMD_CUDA_TRY(cudaMemcpyAsync(e->bond_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, e->st));
+    e->P.bonds = nbonds ? 1u : 0u;
+    e->P.bond_tab = e->bond_tab;
+    e->P.slot_of = e->slot_of;
+    for (uint32_t t = 0; t < 4; t++) {
+        e->P.bond_fene[t] = t < ntypes && types[t].kind == GBMD_BOND_FENE;
+        e->P.bond_k[t] = t < ntypes ? (float)types[t].k : 0.0f;
+        e->P.bond_r0[t] = t < ntypes ? (float)types[t].r0 : 0.0f;
+    }
+    // graphs hold the old parameter block by value: capture again on the next step
+    for (int p = 0; p < 2; p++)
+        for (int b = 0; b < 5; b++)
+            if (e->exec[p][b]) {
+                GBMD_CUDA_TRY(cudaGraphExecDestroy(e->exec[p][b]));
+                e->exec[p][b] = nullptr;
+            }
+    GBMD_TRY(setup_step_loop(e));
+    return gbmd_sync(e);
+}
+
 int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
     if (!e || !sys) return fail(GBMD_E_INVALID, "null argument");
     GBMD_TRY(validate_system(*sys, e->n));
@@ -1575,6 +1644,15 @@ int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
     e->P.itab = old.itab;
     e->P.ipair = old.ipair;
     std::memcpy(e->P.irc2, old.irc2, sizeof(old.irc2));
+    // the half-shell windows and the bonds (set apart from the System)
+    e->P.half_lists = old.half_lists;
+    e->P.win_cap = old.win_cap;
+    e->P.bonds = old.bonds;
+    std::memcpy(e->P.bond_fene, old.bond_fene, sizeof(old.bond_fene));
+    std::memcpy(e->P.bond_k, old.bond_k, sizeof(old.bond_k));
+    std::memcpy(e->P.bond_r0, old.bond_r0, sizeof(old.bond_r0));
+    e->P.bond_tab = old.bond_tab;
+    e->P.slot_of = old.slot_of;
     // graphs hold the old parameter block by value: capture again on the next step
     for (int p = 0; p < 2; p++)
         for (int b = 0; b < 5; b++)

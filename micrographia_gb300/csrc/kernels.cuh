@@ -1018,6 +1018,99 @@ static __global__ void k_filter_compartments(Params P, const PosRec<2>* __restri
     nbr_count[i] = kept;
 }
 
+// ---------------------------------------------------------------- bonds (2D)
+// fixed.rs:63-72 sep_long_f32: sep_f32 within 8 sigma (in sigma units); beyond, the magnitude's
+// whole sigma plus its fraction in f32, then the sign.
+__device__ __forceinline__ float sep_long_f32(int64_t d) {
+    bool ok = true;
+    const float s = __fmul_rn(sep_s(d, ok), 1.0f / 268435456.0f);
+    if (ok) return s;
+    const uint64_t m = d < 0 ? (uint64_t)0 - (uint64_t)d : (uint64_t)d;
+    const float mag = __fadd_rn(__uint2float_rn((uint32_t)(m >> 32)), __fmul_rn(__uint2float_rn((uint32_t)m), 1.0f / 4294967296.0f));
+    return d < 0 ? -mag : mag;
+}
+// BondConsts::eval (real.rs:175-196) in f32: -U'(r)/r and U at r2 (sigma^2), the reference's
+// operation order, the FENE logarithm in IEEE double (fdlibm).
+__device__ __forceinline__ void bond_eval(const Params& P, uint32_t t, float r2, float& fr, float& u) {
+    const float k = P.bond_k[t], r0 = P.bond_r0[t];
+    if (P.bond_fene[t]) {
+        float x = __fdiv_rn(r2, __fmul_rn(r0, r0));
+        if (x > 0.999999f) x = 0.999999f;
+        const float om = __fsub_rn(1.0f, x);
+        u = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(-0.5f, k), r0), r0), (float)dev_log((double)om));
+        fr = __fdiv_rn(-k, om);
+    } else if (r0 == 0.0f) { // a zero-length spring (tethers): -k exactly
+        fr = -k;
+        u = __fmul_rn(__fmul_rn(0.5f, k), r2);
+    } else {
+        const float r = __fsqrt_rn(r2), dr = __fsub_rn(r, r0);
+        fr = __fdiv_rn(__fmul_rn(-k, dr), r);
+        u = __fmul_rn(__fmul_rn(__fmul_rn(0.5f, k), dr), dr);
+    }
+}
+// IntEngine::forces' bond kicks on a particle (int_engine.rs:185-202): each bond rounded on its
+// own like a pair, from the positions `pos` (partners found through P.slot_of), c the particle's
+// kick coefficient in f32; adds to k and returns the bonds' f32 energy sum.
+template <int D>
+__device__ __forceinline__ float bond_kicks(const Params& P, uint32_t id, const int64_t* xi, const PosRec<D>* pos, float c, int32_t* k) {
+    float pe = 0.0f;
+    for (uint32_t q = 0; q < 4; q++) {
+        const uint32_t jid = P.bond_tab[8 * (size_t)id + 2 * q];
+        if (jid == 0xffffffffu) break;
+        const uint32_t t = P.bond_tab[8 * (size_t)id + 2 * q + 1] & 3u;
+        int64_t xj[3];
+        load_particle<D, false>(pos, nullptr, P.slot_of[jid], xj);
+        float f[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int a = 0; a < D; a++) f[a] = sep_long_f32(min_image(xj[a] - xi[a], P.box[a], P.half[a]));
+        float r2 = __fadd_rn(__fmul_rn(f[0], f[0]), __fmul_rn(f[1], f[1]));
+        if (D == 3) r2 = __fadd_rn(r2, __fmul_rn(f[2], f[2]));
+        float fr, u;
+        bond_eval(P, t, r2, fr, u);
+        const float aa = __fmul_rn(-fr, c);
+#pragma unroll
+        for (int a = 0; a < D; a++) k[a] = wadd(k[a], rni_f32(__fmul_rn(aa, f[a])));
+        pe = __fadd_rn(pe, u);
+    }
+    return pe;
+}
+// The storage slot of each particle id, for the bond pass.
+static __global__ void k_slot_of(uint32_t n, const uint32_t* __restrict__ ids, uint32_t* __restrict__ slot_of) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) slot_of[ids[s]] = s;
+}
+// After the force step of a bonded system: each particle's bond kicks from the step's start
+// positions `x0` (read only here, so no particle sees another's update) are added to its velocity
+// and to its moved position, exactly as if the force step had summed them with the pair kicks.
+template <int D, bool LIST>
+__global__ void k_bonds(Params P, const PosRec<D>* __restrict__ x0, PosRec<D>* __restrict__ pos, uint4* __restrict__ qpos,
+                        int32_t* __restrict__ vel, const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids,
+                        const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const uint32_t si = species[i];
+    int64_t xs[3];
+    load_particle<D, false>(x0, nullptr, i, xs);
+    int32_t kb[3] = {0, 0, 0};
+    bond_kicks<D>(P, ids[i], xs, x0, __fmul_rn(P.kick_cs[si], 1.0f / 268435456.0f), kb);
+    if (!(kb[0] | kb[1] | (D == 3 ? kb[2] : 0))) return;
+    int64_t x[3];
+    load_particle<D, false>(pos, nullptr, i, x);
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        vel[D * i + a] = wadd(vel[D * i + a], kb[a]);
+        x[a] += (int64_t)kb[a];
+        if (!LIST && ((P.periodic >> a) & 1u)) x[a] = wrap(x[a], P.box[a]);
+    }
+    store_pos<D>(pos, i, x, si);
+    if (LIST) {
+        qpos[i] = quot_record<D>(x, si);
+        int64_t xr[3];
+        load_particle<D, false>(ref_pos, nullptr, i, xr);
+        if (moved_half_skin<D>(P, xr, x)) ctl[0] = 1;
+    }
+}
+
 // ---------------------------------------------------------------- walls
 // md_core::walls (walls.rs) as IntEngine runs them (int_engine.rs:203-227 and 256-263, the soft
 // walls' kicks and impulses; 316-330, the mirror; 363-390, collide; int_engine3.rs:107-126,
@@ -1252,6 +1345,7 @@ __global__ void __launch_bounds__(128) k_force_cells(Params P, const PosRec<D>* 
 // velocities become -(v + kick + g) (int_engine.rs:396-413).
 template <int D, bool MULTI, bool INT = false>
 __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __restrict__ pos, const uint32_t* __restrict__ species,
+                                               const uint32_t* __restrict__ ids,
                                                const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
                                                int32_t* __restrict__ vel, int32_t* __restrict__ kicks, double* __restrict__ partial,
@@ -1312,6 +1406,8 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
         }
         pe *= 0.5;
         w *= 0.5;
+        if (P.bonds) // (slot_of holds this array's slots)
+            pe += 0.5 * (double)bond_kicks<D>(P, ids[i], xi, pos, __fmul_rn(cs, 1.0f / 268435456.0f), k);
         if (P.walls) {
             // the soft walls' kicks and potential (int_engine.rs:203-227, int_engine3.rs:107-126)
             const float c = __fmul_rn(cs, 1.0f / 268435456.0f);

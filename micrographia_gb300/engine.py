@@ -76,6 +76,8 @@ class _Engine:
                 )
             )
         self._h = h
+        if getattr(sys, "bonds", None):
+            self.set_bonds(sys.bond_types, sys.bonds)
 
     # -- lifecycle
     def close(self):
@@ -166,6 +168,17 @@ class _Engine:
 
     def sort_now(self):
         _abi.check(self._lib.gbmd_sort_now(self._h))
+
+    def set_bonds(self, types, bonds):
+        """System::with_bonds (system.rs:284-299), 2D: `types` Bond values, `bonds` (id a, id b,
+        type index) triples; replaces the engine's bonds (none: an empty list)."""
+        nt = len(types)
+        tarr = (_abi.gbmd_bond_type * max(nt, 1))()
+        for q, t in enumerate(types):
+            tarr[q].kind = _abi.BOND_FENE if t.fene else _abi.BOND_HARMONIC
+            tarr[q].k, tarr[q].r0 = t.k, t.r0
+        b = np.ascontiguousarray(np.array(bonds, np.uint32).reshape(-1, 3))
+        _abi.check(self._lib.gbmd_set_bonds(self._h, tarr, nt, _ptr(b, C.c_uint32), len(b)))
 
     def update_system(self, sys):
         """Replace interactions, masses, gravity, pinned species or dt (same box and species
@@ -350,6 +363,8 @@ class BatchEngine:
         D = systems[0].DIM
         if any(s.DIM != D for s in systems):
             raise ValueError("a batch holds systems of one dimension")
+        if any(getattr(s, "bonds", None) for s in systems):
+            raise ValueError("a batch holds pair systems: bonded systems run on GpuEngine")
         self.D = D
         self.count = len(systems)
         self.sizes = [st.n() for st in states]
@@ -449,6 +464,8 @@ class Server:
         self._buf = (_abi.gbmd_serve_frame * 64)()
 
     def submit(self, sys, init, steps, frame_every=100, rdf_bins=200, rdf_rmax=5.0, skin=0.3):
+        if getattr(sys, "bonds", None):
+            raise ValueError("the server runs pair systems: bonded systems run on GpuEngine")
         r = _abi.gbmd_serve_request()
         r.sys = sys.to_c()
         r.init = init

@@ -65,6 +65,35 @@ def test_walls_with_gravity_follow_the_oracle_and_reverse(O, kind, mode):
         assert g.read_state() == s0
 
 
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_wca_mixture_with_walls_and_gravity_follows_the_oracle(O, mode):
+    """md-ref/tests/fast_path.rs:27-46 on the GPU: a WCA mixture of three masses (1, 4, 30) and two
+    sizes (the heavy species 2 sigma from the others, 3 among themselves), hard walls on x, soft
+    on y, gravity 0.01; the small particles within 2 sigma of a big one removed. 300 steps equal
+    IntEngine<f32>'s bit for bit with the same ledger."""
+
+    def wca(s):
+        return Pair(1.0, s, s * 2 ** (1 / 6))
+
+    sys_ = System(box_for(1500, 0.3, 1.5), 0.005, wca(1.0), [1.0, 4.0, 30.0])
+    sys_.with_pair(0, 2, wca(2.0)).with_pair(1, 2, wca(2.0)).with_pair(2, 2, wca(3.0))
+    sys_.with_walls(0, Wall.hard(), Wall.hard()).with_walls(1, Wall.soft(), Wall.soft()).with_gravity([0.0, -0.01])
+    st = O.fluid(sys_, 1500, 1.0, 2)
+    st.species[:] = [2 if i % 50 == 0 else i % 2 for i in range(1500)]
+    big = st.pos[st.species == 2]
+    d2 = (((big[None, :, :] - st.pos[:, None, :]).astype(np.float64) / ONE) ** 2).sum(-1)
+    keep = (st.species == 2) | (d2 > 4.0).all(1)
+    s0 = State(st.pos[keep].copy(), st.vel[keep].copy(), st.species[keep].copy())
+    n = s0.n()
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_with_skin(sys_, n, 0.3)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, m) as g:
+        g.step(300)
+        c.step(300)
+        assert g.read_state() == c.state
+        _same_ledger(g, c)
+
+
 def test_soft_walls_energy_matches_the_oracle(O):
     """The instruments with soft walls (the walls' WCA potential in forces(), int_engine.rs:
     203-227): the GPU's kicks equal the oracle's; the potential within 1e-5 relative (the oracle
