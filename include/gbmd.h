@@ -254,6 +254,32 @@ typedef struct gbmd_bond_type {
     double r0;
 } gbmd_bond_type;
 int gbmd_set_bonds(gbmd_engine* e, const gbmd_bond_type* types, uint32_t ntypes, const uint32_t* bonds, uint32_t nbonds);
+/* The piston (md_core::Piston, system.rs:100-116; System::with_piston, system.rs:274-282), 2D: a
+ * soft wall that replaces the top of y (the axis must have walls), starting at height `start`
+ * sigma and stopping at `min` and at the box height. GBMD_PISTON_SPEED moves it at `speed`
+ * sigma/tau (positive opens the box; a heat bath then draws relative to its affine flow,
+ * int_engine.rs:282-286); GBMD_PISTON_FREE lets the gas move it against `force` eps/sigma pushing
+ * down, with mass `mass` (walls::piston_kick, walls.rs:143-146). Each step the gas's force on it
+ * is summed in 2^-16 eps/sigma units (walls.rs:140-141) and the piston moves after the particles
+ * (IntEngine::move_piston, int_engine.rs:346-361); particles that pass it are mirrored below it.
+ * GBMD_PISTON_NONE removes it. Set before stepping or between steps; GBMD_E_UNSUPPORTED in 3D,
+ * GBMD_E_INVALID for a periodic y or bad values. */
+#define GBMD_PISTON_NONE 0
+#define GBMD_PISTON_SPEED 1
+#define GBMD_PISTON_FREE 2
+typedef struct gbmd_piston {
+    uint32_t drive; /* GBMD_PISTON_* */
+    uint32_t _pad;
+    double speed;   /* sigma/tau (GBMD_PISTON_SPEED) */
+    double mass;    /* GBMD_PISTON_FREE */
+    double force;   /* eps/sigma pushing down (GBMD_PISTON_FREE) */
+    double start;   /* sigma */
+    double min;     /* sigma */
+} gbmd_piston;
+int gbmd_set_piston(gbmd_engine* e, const gbmd_piston* piston);
+/* IntEngine's piston_w (height, position units), piston_v (position units per step) and
+ * piston_work (the gas's work on the piston, eps). Any pointer may be NULL. */
+int gbmd_read_piston(gbmd_engine* e, int64_t* height, int32_t* velocity, double* work);
 
 /* ---- Observables: IntEngine::energy (int_engine.rs:433-446) and the new instruments ---- */
 

@@ -18,6 +18,7 @@ from .core import (
     Bond,
     ForceMode,
     Pair,
+    Piston,
     State,
     State3,
     System,
@@ -40,6 +41,7 @@ __all__ = [
     "Bond",
     "ForceMode",
     "Pair",
+    "Piston",
     "State",
     "State3",
     "System",

@@ -82,6 +82,23 @@ class gbmd_bond_type(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("_pad", C.c_uint32), ("k", C.c_double), ("r0", C.c_double)]
 
 
+PISTON_NONE = 0
+PISTON_SPEED = 1  # md_core::PistonDrive::Speed
+PISTON_FREE = 2  # PistonDrive::Free
+
+
+class gbmd_piston(C.Structure):
+    _fields_ = [
+        ("drive", C.c_uint32),
+        ("_pad", C.c_uint32),
+        ("speed", C.c_double),
+        ("mass", C.c_double),
+        ("force", C.c_double),
+        ("start", C.c_double),
+        ("min", C.c_double),
+    ]
+
+
 WALL_HARD = 1  # md_core::Wall::Hard: exact mirror
 WALL_SOFT = 2  # Wall::Soft: WCA repulsion from the wall
 WALL_THERMAL = 3  # Wall::Thermal(t): a hit draws a Maxwell-flux velocity at kT = t
@@ -221,6 +238,8 @@ SIGNATURES = [
     ("gbmd_sort_now", C.c_int, [VP]),
     ("gbmd_update_system", C.c_int, [VP, P(gbmd_system)]),
     ("gbmd_set_bonds", C.c_int, [VP, P(gbmd_bond_type), C.c_uint32, P(C.c_uint32), C.c_uint32]),
+    ("gbmd_set_piston", C.c_int, [VP, P(gbmd_piston)]),
+    ("gbmd_read_piston", C.c_int, [VP, P(C.c_int64), P(C.c_int32), P(C.c_double)]),
     ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
     ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),
     ("gbmd_observe_begin", C.c_int, [VP, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32]),

@@ -117,6 +117,7 @@ class _SystemBase:
         self.compartments_diathermal = False
         self.bond_types = []  # Bond values
         self.bonds = []  # (id a, id b, type index)
+        self.piston = None  # (Piston drive, start, min), 2D
 
     def species(self):
         return len(self.masses)
@@ -136,6 +137,19 @@ class _SystemBase:
                     raise ValueError(f"particle {p} has more than 4 bonds")
         self.bond_types = list(types)
         self.bonds = [tuple(int(x) for x in b) for b in bonds]
+        return self
+
+    def with_piston(self, drive, start, min):
+        """System::with_piston (system.rs:274-282), 2D: the top wall of y becomes a soft piston
+        starting at height `start` sigma, stopping at `min` and at the box height; y must have
+        walls."""
+        if self.DIM != 2:
+            raise ValueError("pistons are two-dimensional")
+        if self.walls[1] is None:
+            raise ValueError("a piston needs walls on y")
+        if not (min < start <= to_f64(self.box_len[1])):
+            raise ValueError("min < start <= the box height")
+        self.piston = (drive, float(start), float(min))
         return self
 
     def with_pair(self, a, b, pair):
@@ -305,6 +319,28 @@ def chains(sys, chains, length, bond):
             if k > 0:
                 bonds.append((i - 1, i, 0))
     return np.array(pos, np.int64), bonds
+
+
+class Piston:
+    """md_core::PistonDrive (system.rs:100-107): Piston.speed(u), moved at u sigma/tau (positive
+    opens the box); Piston.free(mass, force), moved by the gas and a constant force pushing down
+    (eps/sigma)."""
+
+    SPEED, FREE = 1, 2
+
+    def __init__(self, kind, speed=0.0, mass=0.0, force=0.0):
+        self.kind, self.speed, self.mass, self.force = int(kind), float(speed), float(mass), float(force)
+
+    @classmethod
+    def speed_drive(cls, u):
+        return cls(cls.SPEED, speed=u)
+
+    @classmethod
+    def free(cls, mass, force):
+        return cls(cls.FREE, mass=mass, force=force)
+
+    def __repr__(self):
+        return f"Piston.speed_drive({self.speed})" if self.kind == self.SPEED else f"Piston.free({self.mass}, {self.force})"
 
 
 class Wall:

@@ -252,7 +252,7 @@ __global__ void k_bbath(uint32_t N, const Params* __restrict__ tab, const uint32
         if (!(p >= P.bath_region[0] && p < P.bath_region[1])) return;
     }
     const BathDraw o = bath_draw<D>(ids[i] - P.id_base, ctl[CTL_CLOCK], P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si],
-                                    P.masses[si], P.dt, P.bath_drift, v[0], v[1], v[2], ledger + 2 * k);
+                                    P.masses[si], P.dt, P.bath_drift, 0, v[0], v[1], v[2], ledger + 2 * k);
     if (!o.hit) return;
 #pragma unroll
     for (int a = 0; a < D; a++) {

@@ -132,6 +132,12 @@ static double powi_rs(double x, int n) {
     }
     return have ? res : 1.0;
 }
+static int64_t sat_i64_host(double x) {
+    if (x != x) return 0;
+    if (x >= 9223372036854775807.0) return INT64_MAX;
+    if (x <= -9223372036854775808.0) return INT64_MIN;
+    return (int64_t)x;
+}
 static int32_t sat_i32_host(double x) {
     if (x != x) return 0;
     if (x >= 2147483647.0) return INT32_MAX;
@@ -399,6 +405,7 @@ struct gbmd_engine {
     bool half = false;       // half-shell lists (k_build_half / k_force_half / k_leap_half)
     uint32_t* bond_tab = nullptr; // bonds: per id 4 x (partner id, type), padded with UINT32_MAX
     uint32_t* slot_of = nullptr;  // bonds: the storage slot of each id
+    PistonState* piston = nullptr; // the piston's moving state (2D)
     int32_t* acc = nullptr;  // half-shell kick accumulators, 3 x int32 per slot, zero between steps
     int32_t* itab = nullptr; // all-integer kick tables (GBMD_ARITH_INT)
     double* ipair = nullptr;
@@ -669,7 +676,8 @@ void enqueue_force(gbmd_engine* e, cudaStream_t s) {
             if (e->verlet) k_walls<3, true><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<3>*)e->ref_pos, e->ctl, l);
             else k_walls<3, false><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, l);
         }
-        k_clock_tick<<<1, 1, 0, s>>>(e->ctl);
+        if (e->P.piston_drive) k_piston_tick<<<1, 1, 0, s>>>(e->P, e->ctl); // the piston moves, then the clock
+        else k_clock_tick<<<1, 1, 0, s>>>(e->ctl);
         note_launch(2);
     } else if (e->P.bath) { // the Andersen bath on the moved state, then the step clock advances
         const uint32_t nb = blocks_for(e->n, 256);
@@ -996,6 +1004,10 @@ template <int D, bool MULTI, bool INT> void kicks_launch(gbmd_engine* e, int32_t
 template <int D, bool MULTI> int kicks_t(gbmd_engine* e, int32_t* kicks, double* partial, int reverse) {
     if (e->P.int_mode) kicks_launch<D, MULTI, true>(e, kicks, partial, reverse);
     else kicks_launch<D, MULTI, false>(e, kicks, partial, reverse);
+    if (reverse && e->P.piston_drive) {
+        k_piston_reverse<<<1, 1, 0, e->st>>>(e->P);
+        note_launch();
+    }
     if (!e->verlet) {
         // positions, velocities and ids live in scratch (sorted) until copied back
         GBMD_CUDA_TRY(cudaMemcpyAsync(e->pos[e->cur], e->pos_scr, (size_t)e->n * e->rec, cudaMemcpyDeviceToDevice, e->st));
@@ -1615,9 +1627,61 @@ int gbmd_set_bonds(gbmd_engine* e, const gbmd_bond_type* types, uint32_t ntypes,
     return gbmd_sync(e);
 }
 
+int gbmd_set_piston(gbmd_engine* e, const gbmd_piston* p) {
+    if (!e || !p) return fail(GBMD_E_INVALID, "null argument");
+    if (p->drive == GBMD_PISTON_NONE) {
+        GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+        e->P.piston_drive = 0;
+    } else {
+        if (e->D != 2) return fail(GBMD_E_UNSUPPORTED, "pistons are two-dimensional (IntEngine; IntEngine3 has none)");
+        if ((e->P.periodic >> 1) & 1u) return fail(GBMD_E_INVALID, "a piston needs walls on y");
+        const double top = (double)e->sys.box_len[1] * (1.0 / 4294967296.0);
+        const bool finite = std::isfinite(p->speed) && std::isfinite(p->mass) && std::isfinite(p->force) && std::isfinite(p->start) &&
+                            std::isfinite(p->min);
+        if (p->drive > GBMD_PISTON_FREE || !finite || !(p->min < p->start && p->start <= top) || (p->drive == GBMD_PISTON_FREE && !(p->mass > 0.0)))
+            return fail(GBMD_E_INVALID, "a piston is driven at a speed or free (mass > 0), with min < start <= the box height");
+        GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+        if (!e->piston) GBMD_TRY(allocT(e, &e->piston, 1));
+        PistonState ps{};
+        ps.w = sat_i64_host(std::round(p->start * 4294967296.0)); // fixed::to_fixed (fixed.rs:21-23)
+        ps.v = p->drive == GBMD_PISTON_SPEED ? to_step_displacement(e->sys, p->speed) : 0;
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->piston, &ps, sizeof(ps), cudaMemcpyHostToDevice, e->st));
+        e->P.piston_drive = p->drive;
+        e->P.piston_mass = p->mass;
+        e->P.piston_ext = p->force;
+        e->P.piston_lo = sat_i64_host(std::round(p->min * 4294967296.0));
+        e->P.piston_hi = sat_i64_host(std::round(top * 4294967296.0));
+        e->P.piston = e->piston;
+    }
+    // graphs hold the old parameter block by value: capture again on the next step
+    for (int q = 0; q < 2; q++)
+        for (int b = 0; b < 5; b++)
+            if (e->exec[q][b]) {
+                GBMD_CUDA_TRY(cudaGraphExecDestroy(e->exec[q][b]));
+                e->exec[q][b] = nullptr;
+            }
+    GBMD_TRY(setup_step_loop(e));
+    return gbmd_sync(e);
+}
+
+int gbmd_read_piston(gbmd_engine* e, int64_t* height, int32_t* velocity, double* work) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    PistonState ps{};
+    if (e->P.piston_drive) {
+        GBMD_CUDA_TRY(cudaMemcpyAsync(&ps, e->piston, sizeof(ps), cudaMemcpyDeviceToHost, e->st));
+        GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    }
+    if (height) *height = ps.w;
+    if (velocity) *velocity = ps.v;
+    if (work) *work = ps.work;
+    return GBMD_OK;
+}
+
 int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
     if (!e || !sys) return fail(GBMD_E_INVALID, "null argument");
     GBMD_TRY(validate_system(*sys, e->n));
+    if (e->P.piston_drive && ((sys->periodic >> 1) & 1u))
+        return fail(GBMD_E_INVALID, "the engine has a piston: y keeps its walls");
     const gbmd_system& o = e->sys;
     if (sys->dim != o.dim || sys->nspecies != o.nspecies) return fail(GBMD_E_INVALID, "update_system keeps the dimension and the species count");
     for (uint32_t a = 0; a < o.dim; a++)
@@ -1653,6 +1717,12 @@ int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
     std::memcpy(e->P.bond_r0, old.bond_r0, sizeof(old.bond_r0));
     e->P.bond_tab = old.bond_tab;
     e->P.slot_of = old.slot_of;
+    e->P.piston_drive = old.piston_drive; // and the piston
+    e->P.piston_mass = old.piston_mass;
+    e->P.piston_ext = old.piston_ext;
+    e->P.piston_lo = old.piston_lo;
+    e->P.piston_hi = old.piston_hi;
+    e->P.piston = old.piston;
     // graphs hold the old parameter block by value: capture again on the next step
     for (int p = 0; p < 2; p++)
         for (int b = 0; b < 5; b++)

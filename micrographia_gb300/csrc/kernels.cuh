@@ -303,7 +303,7 @@ __device__ __forceinline__ void leapfrog(const G& P, uint32_t si, const int32_t*
 // under the thermostat key decides, with probability rate dt, to replace the kicked velocity by a
 // Maxwell draw at the bath's temperature (fdlibm ln, cos, sin in IEEE double, the reference's
 // operation order), each component rounded by to_step_displacement; 2D adds the fan's drift to
-// x. The energy change 0.5 m (|v'|^2 - |v|^2), in the reference's f64 order, is booked on the
+// x and flow1 to y (the affine flow under a driven piston, int_engine.rs:282-286). The energy change 0.5 m (|v'|^2 - |v|^2), in the reference's f64 order, is booked on the
 // ledger rounded half away from zero to 2^-24 epsilon, so the total does not depend on the order
 // in which the GPU books events.
 struct BathDraw {
@@ -312,7 +312,8 @@ struct BathDraw {
 };
 template <int D>
 __device__ __forceinline__ BathDraw bath_draw(uint32_t id, uint32_t clock, uint32_t k0, uint32_t k1, double rate_dt, double sd, double m,
-                                           double dt, int32_t drift, int32_t v0, int32_t v1, int32_t v2, unsigned long long* ledger) {
+                                           double dt, int32_t drift, int32_t flow1, int32_t v0, int32_t v1, int32_t v2,
+                                           unsigned long long* ledger) {
     BathDraw o{{v0, v1, v2}, 0};
     uint32_t r0, r1;
     threefry2x32(id, clock, k0, k1, r0, r1);
@@ -343,7 +344,7 @@ __device__ __forceinline__ BathDraw bath_draw(uint32_t id, uint32_t clock, uint3
     if (D == 2) {
         const double b0 = vel(v0), b1 = vel(v1);
         o.v[0] = wadd(step(u[0]), drift);
-        o.v[1] = step(u[1]);
+        o.v[1] = wadd(step(u[1]), flow1);
         const double a0 = vel(o.v[0]), a1 = vel(o.v[1]);
         // 0.5 m (a0 a0 + a1 a1 - b0 b0 - b1 b1), left to right
         const double s = __dsub_rn(__dsub_rn(__dadd_rn(__dmul_rn(a0, a0), __dmul_rn(a1, a1)), __dmul_rn(b0, b0)), __dmul_rn(b1, b1));
@@ -946,6 +947,13 @@ __global__ void __launch_bounds__(128, 10) k_force_loop(Params P, PosRec<D>* __r
 // lists the quotient record is rewritten and the displacement trigger re-tested at the new
 // position (a trigger the force step already set stays set: an extra rebuild changes nothing).
 // The draw is keyed on the clock word, which the next launch in the stream advances.
+// The velocity a drawn particle at height y (position units, before the move) takes from a
+// driven piston's affine flow: round(piston_v clamp(y / piston_w, 0, 1)) (int_engine.rs:282-286).
+__device__ __forceinline__ int32_t piston_flow(const Params& P, int64_t y) {
+    double f = __ddiv_rn(to_f64(y), to_f64(P.piston->w));
+    f = f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f); // (NaN stays NaN and converts to 0)
+    return sat_i32_f64(round_away(__dmul_rn((double)P.piston->v, f)));
+}
 // The bath on one particle's moved state (x, v as the step left them): returns whether it drew.
 template <int D>
 __device__ __forceinline__ bool bath_one(const Params& P, uint32_t si, uint32_t id, uint32_t clock, int64_t* x, int32_t* v,
@@ -956,8 +964,9 @@ __device__ __forceinline__ bool bath_one(const Params& P, uint32_t si, uint32_t 
         const int64_t p = wrap(x[ax] - (int64_t)v[ax], P.box[ax]);
         if (!(p >= P.bath_region[0] && p < P.bath_region[1])) return false;
     }
+    const int32_t flow1 = (D == 2 && P.piston_drive == 1) ? piston_flow(P, x[1] - (int64_t)v[1]) : 0;
     const BathDraw o = bath_draw<D>(id, clock, P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si], P.masses[si], P.dt, P.bath_drift,
-                                    v[0], v[1], v[2], ledger);
+                                    flow1, v[0], v[1], v[2], ledger);
     if (!o.hit) return false;
 #pragma unroll
     for (int a = 0; a < D; a++) {
@@ -1095,11 +1104,11 @@ __global__ void k_bonds(Params P, const PosRec<D>* __restrict__ x0, PosRec<D>* _
     bond_kicks<D>(P, ids[i], xs, x0, __fmul_rn(P.kick_cs[si], 1.0f / 268435456.0f), kb);
     if (!(kb[0] | kb[1] | (D == 3 ? kb[2] : 0))) return;
     int64_t x[3];
-    load_particle<D, false>(pos, nullptr, i, x);
 #pragma unroll
-    for (int a = 0; a < D; a++) {
-        vel[D * i + a] = wadd(vel[D * i + a], kb[a]);
-        x[a] += (int64_t)kb[a];
+    for (int a = 0; a < D; a++) { // the move from the start with the wrapped velocity sum (x += v)
+        const int32_t v = wadd(vel[D * i + a], kb[a]);
+        vel[D * i + a] = v;
+        x[a] = xs[a] + (int64_t)v;
         if (!LIST && ((P.periodic >> a) & 1u)) x[a] = wrap(x[a], P.box[a]);
     }
     store_pos<D>(pos, i, x, si);
@@ -1190,10 +1199,27 @@ __global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict
             kw_sum = wadd(kw_sum, side == 0 ? kw : (int32_t)(0u - (uint32_t)kw));
             atomicAdd(ledger + 3 * (2 * a + side) + 2, ledger_fixed(__dmul_rn((double)f, P.dt)));
         }
-        if (kw_sum) {
+        if (kw_sum) { // (the move uses the wrapped velocity sum, as the reference's x += v does)
             v[a] = wadd(v[a], kw_sum);
-            x[a] += (int64_t)kw_sum;
+            x[a] = xo + (int64_t)v[a];
             changed = true;
+        }
+    }
+    int64_t pw = 0;
+    if (D == 2 && P.piston_drive) {
+        // the piston (int_engine.rs:230-246): a soft wall at the step's piston height pushing
+        // down; the gas's force on it summed in 2^-16 eps/sigma units (walls.rs:140-141)
+        pw = P.piston->w;
+        const int64_t yo = x[1] - (int64_t)v[1];
+        float f, s6;
+        if (soft_wall_force(pw - yo, f, s6)) {
+            const int32_t kw = rni_f32(__fmul_rn(f, c));
+            atomicAdd(&P.piston->force_fixed, (unsigned long long)sat_i64_f64(round_away(__dmul_rn((double)f, 65536.0))));
+            if (kw) {
+                v[1] = wadd(v[1], (int32_t)(0u - (uint32_t)kw));
+                x[1] = yo + (int64_t)v[1];
+                changed = true;
+            }
         }
     }
     if (P.bath && bath_one<D>(P, si, id, clock, x, v, ledger + 3 * GBMD_LEDGER_BATH)) changed = true;
@@ -1281,6 +1307,11 @@ __global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict
         atomicAdd(l + 1, 1ull);
         atomicAdd(l + 2, ledger_fixed(imp));
     }
+    if (D == 2 && P.piston_drive && x[1] >= pw) { // mirrored below the piston (int_engine.rs:333-336)
+        x[1] = 2 * pw - 1 - x[1];
+        v[1] = (int32_t)(0u - (uint32_t)v[1]);
+        changed = true;
+    }
     if (!changed) return;
 #pragma unroll
     for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
@@ -1291,6 +1322,38 @@ __global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict
         load_particle<D, false>(ref_pos, nullptr, i, xr);
         if (moved_half_skin<D>(P, xr, x)) ctl[0] = 1;
     }
+}
+
+// walls::piston_kick (walls.rs:143-146): F dt^2 / M in position units, rounded half away from
+// zero, in the reference's f64 order.
+__device__ __forceinline__ int32_t piston_kick(const Params& P, double net) {
+    return sat_i32_f64(round_away(__dmul_rn(__ddiv_rn(__dmul_rn(__dmul_rn(net, P.dt), P.dt), P.piston_mass), 4294967296.0)));
+}
+// After the walls pass: IntEngine::move_piston (int_engine.rs:346-361) on the step's force sum
+// (a free piston's kick, the drift, the stops, the work), then the step clock advances.
+static __global__ void k_piston_tick(Params P, uint32_t* ctl) {
+    PistonState& ps = *P.piston;
+    const double gas = __dmul_rn(__ll2double_rn((long long)ps.force_fixed), 1.0 / 65536.0);
+    ps.force_fixed = 0ull;
+    if (P.piston_drive == 2) ps.v = wadd(ps.v, piston_kick(P, __dsub_rn(gas, P.piston_ext)));
+    const int64_t old = ps.w;
+    int64_t w = old + (int64_t)ps.v;
+    if (w < P.piston_lo || w > P.piston_hi) {
+        w = w < P.piston_lo ? P.piston_lo : P.piston_hi;
+        ps.v = 0;
+    }
+    ps.w = w;
+    ps.work = __dadd_rn(ps.work, __dmul_rn(gas, to_f64(w - old)));
+    ctl[CTL_CLOCK] += 1u;
+}
+// Reversal's piston step (int_engine.rs:404-410): v <- -(v + kick), a free piston's kick from the
+// force the reversing kicks pass summed.
+static __global__ void k_piston_reverse(Params P) {
+    PistonState& ps = *P.piston;
+    const double gas = __dmul_rn(__ll2double_rn((long long)ps.force_fixed), 1.0 / 65536.0);
+    ps.force_fixed = 0ull;
+    const int32_t kick = P.piston_drive == 2 ? piston_kick(P, __dsub_rn(gas, P.piston_ext)) : 0;
+    ps.v = (int32_t)(0u - (uint32_t)wadd(ps.v, kick));
 }
 
 // Cell-list force + leapfrog (ForceMode::CellList; md.wgsl:39-76): scans the 3^D cells of the
@@ -1422,6 +1485,12 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
                     k[a] = wadd(k[a], side == 0 ? kw : (int32_t)(0u - (uint32_t)kw));
                     pe += (double)__fadd_rn(__fmul_rn(__fmul_rn(4.0f, s6), __fsub_rn(s6, 1.0f)), 1.0f);
                 }
+            }
+            float f, s6; // the piston (int_engine.rs:230-246); reversing sums its force for its own kick
+            if (D == 2 && P.piston_drive && soft_wall_force(P.piston->w - xi[1], f, s6)) {
+                k[1] = wadd(k[1], (int32_t)(0u - (uint32_t)rni_f32(__fmul_rn(f, c))));
+                pe += (double)__fadd_rn(__fmul_rn(__fmul_rn(4.0f, s6), __fsub_rn(s6, 1.0f)), 1.0f);
+                if (reverse) atomicAdd(&P.piston->force_fixed, (unsigned long long)sat_i64_f64(round_away(__dmul_rn((double)f, 65536.0))));
             }
         }
         double m = P.masses[si];

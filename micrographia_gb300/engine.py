@@ -78,6 +78,8 @@ class _Engine:
         self._h = h
         if getattr(sys, "bonds", None):
             self.set_bonds(sys.bond_types, sys.bonds)
+        if getattr(sys, "piston", None):
+            self.set_piston(*sys.piston)
 
     # -- lifecycle
     def close(self):
@@ -179,6 +181,22 @@ class _Engine:
             tarr[q].k, tarr[q].r0 = t.k, t.r0
         b = np.ascontiguousarray(np.array(bonds, np.uint32).reshape(-1, 3))
         _abi.check(self._lib.gbmd_set_bonds(self._h, tarr, nt, _ptr(b, C.c_uint32), len(b)))
+
+    def set_piston(self, drive, start, min):
+        """System::with_piston (system.rs:274-282), 2D: a Piston drive (None removes the piston),
+        the starting height and the lower stop in sigma; the upper stop is the box height."""
+        p = _abi.gbmd_piston()
+        if drive is not None:
+            p.drive, p.speed, p.mass, p.force = drive.kind, drive.speed, drive.mass, drive.force
+            p.start, p.min = float(start), float(min)
+        _abi.check(self._lib.gbmd_set_piston(self._h, C.byref(p)))
+
+    def piston(self):
+        """The piston's height (position units), velocity (position units per step) and the gas's
+        work on it (eps): IntEngine's piston_w, piston_v, piston_work."""
+        w, v, work = C.c_int64(), C.c_int32(), C.c_double()
+        _abi.check(self._lib.gbmd_read_piston(self._h, C.byref(w), C.byref(v), C.byref(work)))
+        return w.value, v.value, work.value
 
     def update_system(self, sys):
         """Replace interactions, masses, gravity, pinned species or dt (same box and species

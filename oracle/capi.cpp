@@ -307,6 +307,23 @@ void oracle_engine_set_bonds(void* h, const uint32_t* fene, const double* k, con
     if (e->f32) e->f32->set_bonds(t, b);
     else e->f64->set_bonds(t, b);
 }
+// System::with_piston (system.rs:274-282): drive 0 none, 1 a set speed (sigma/tau), 2 free
+// (mass, external force in eps/sigma); 0 on success, -1 for a system or piston it refuses.
+int oracle_engine_set_piston(void* h, int drive, double speed, double mass, double force, double start, double min) {
+    Engine* e = (Engine*)h;
+    const bool ok = e->f32 ? e->f32->set_piston(drive, speed, mass, force, start, min) : e->f64->set_piston(drive, speed, mass, force, start, min);
+    return ok ? 0 : -1;
+}
+// The piston's height (position units), velocity (per step), the gas's work on it (eps) and
+// the gas's force on it in the last force evaluation (eps/sigma).
+void oracle_engine_piston(void* h, int64_t* w, int32_t* v, double* work, double* force) {
+    Engine* e = (Engine*)h;
+    if (e->f32) {
+        *w = e->f32->piston_w, *v = e->f32->piston_v, *work = e->f32->piston_work, *force = e->f32->piston_force;
+    } else {
+        *w = e->f64->piston_w, *v = e->f64->piston_v, *work = e->f64->piston_work, *force = e->f64->piston_force;
+    }
+}
 void oracle_engine_wall_ledger_fixed(void* h, int64_t* energy, int64_t* impulse) {
     const Ledger& l = ((Engine*)h)->f32 ? ((Engine*)h)->f32->ledger : ((Engine*)h)->f64->ledger;
     for (int w = 0; w < LEDGER_SLOTS; w++) {

@@ -1042,9 +1042,8 @@ inline void thermal_velocity(const System& sys, uint32_t id, uint32_t clock, dou
 inline int64_t ledger_fixed(double de) { return (int64_t)std::round(de * 16777216.0); }
 
 // md-ref int_engine.rs:23-447 and int_engine3.rs:12-240: periodic or walled (hard, soft,
-// thermal) boxes, an optional Andersen bath and the ledger (bonds, pistons, membranes and
-// compartments are outside this path). One template serves 2D and
-// 3D; in 2D `fast` selects fast.rs's half-shell path when it applies, as IntEngine::forces does.
+// thermal) boxes, an optional Andersen bath, the ledger, and in 2D bonds, membranes,
+// compartments and the piston. One template serves 2D and 3D; in 2D `fast` selects fast.rs's half-shell path when it applies, as IntEngine::forces does.
 template <typename F> struct IntEngine {
     System sys;
     State state;
@@ -1064,6 +1063,16 @@ template <typename F> struct IntEngine {
     // types (System::partner_table, system.rs:311-324), padded with UINT32_MAX.
     std::vector<BondConsts<F>> bond_consts;
     std::vector<std::array<uint32_t, 2 * MAX_BONDS>> partners;
+    // The piston (2D; int_engine.rs:40-44, 61-69; system.rs:100-116, 274-282): a soft wall that
+    // replaces the top of y at height piston_w (position units) and moves piston_v per step,
+    // driven at a set speed (drive 1) or free (drive 2) under the gas and an external force
+    // pushing down; it stops at [piston_lo, piston_hi]. piston_work is the gas's work on it
+    // and piston_force the gas's force in the last forces() (eps/sigma, summed in 2^-16 units).
+    int piston_drive = 0;
+    double piston_mass = 0.0, piston_ext = 0.0;
+    int64_t piston_w = 0, piston_lo = 0, piston_hi = 0;
+    int32_t piston_v = 0;
+    double piston_work = 0.0, piston_force = 0.0;
 
     IntEngine(const System& s, const State& st) : state(st) { set_system(s); }
     // System::with_bonds (system.rs:284-299) and the engine's partner table.
@@ -1080,6 +1089,40 @@ template <typename F> struct IntEngine {
                 partners[me][2 * k] = other;
                 partners[me][2 * k + 1] = b[2];
             }
+    }
+    // System::with_piston (system.rs:274-282) and the engine's piston state (int_engine.rs:61-69).
+    bool set_piston(int drive, double speed, double mass, double force, double start, double min) {
+        if (drive == 0) {
+            piston_drive = 0;
+            return true;
+        }
+        const double max = sys.box_f64(1);
+        if (sys.dim != 2 || sys.periodic(1) || drive < 1 || drive > 2 || !(start <= max && min < start) || (drive == 2 && !(mass > 0.0)))
+            return false;
+        piston_drive = drive;
+        piston_mass = mass;
+        piston_ext = force;
+        piston_w = to_fixed(start);
+        piston_v = drive == 1 ? sys.to_step_displacement(speed) : 0;
+        piston_lo = to_fixed(min);
+        piston_hi = to_fixed(max);
+        piston_work = 0.0;
+        return true;
+    }
+    // walls::piston_kick (walls.rs:143-146): the integer kick on a free piston for a net upward
+    // force, F dt^2 / M in position units, rounded half away from zero.
+    int32_t piston_kick(double net) const { return sat_i32(std::round(net * sys.dt * sys.dt / piston_mass * 4294967296.0)); }
+    // IntEngine::move_piston (int_engine.rs:346-361): a free piston's kick, the drift, the stops.
+    void move_piston(double gas_force) {
+        if (!piston_drive) return;
+        if (piston_drive == 2) piston_v = wadd(piston_v, piston_kick(gas_force - piston_ext));
+        const int64_t old = piston_w;
+        piston_w += (int64_t)piston_v;
+        if (piston_w < piston_lo || piston_w > piston_hi) {
+            piston_w = std::clamp(piston_w, piston_lo, piston_hi);
+            piston_v = 0;
+        }
+        piston_work += gas_force * to_f64(piston_w - old);
     }
     // The constructor's derived constants; alone, a run-time change of system (GpuEngine::
     // update_system, engine.rs:895-934) that keeps the state, counters, clock and ledger.
@@ -1116,7 +1159,8 @@ template <typename F> struct IntEngine {
     // The kick on particle i and its share of the potential energy: the body of the reference
     // loop over the 3^d neighbouring cells (int_engine.rs:144-243 / int_engine3.rs:56-128), with
     // the soft walls' forces on i added into wf.
-    void force_on(size_t i, const CellList& cl, const uint32_t* nc, const double* b, int32_t* kout, double* pe_out, double* wf) const {
+    void force_on(size_t i, const CellList& cl, const uint32_t* nc, const double* b, int32_t* kout, double* pe_out, double* wf,
+                  int64_t* piston_out) const {
         int d = sys.dim;
         int ns = sys.species();
         const int64_t* pi = &state.pos[d * i];
@@ -1209,6 +1253,18 @@ template <typename F> struct IntEngine {
                 }
             }
         }
+        // the piston (int_engine.rs:230-246): a soft wall at piston_w pushing down; its force
+        // summed in 2^-16 eps/sigma units (walls::PISTON_FORCE_SCALE, walls.rs:140-141)
+        F df;
+        if (piston_drive && Real<F>::sep(piston_w - pi[1], &df) && df < Real<F>::from_f64(SOFT_RC)) {
+            const F one = Real<F>::from_f64(1.0);
+            const F s2 = one / (df * df);
+            const F s6 = s2 * s2 * s2;
+            const F f = Real<F>::from_f64(24.0) * s6 * (Real<F>::from_f64(2.0) * s6 - one) / df;
+            k[1] = wadd(k[1], wneg(Real<F>::round_to_i32(f * c)));
+            *piston_out = sat_i64(std::round((double)f * 65536.0));
+            wall_pe += (double)(Real<F>::from_f64(4.0) * s6 * (s6 - one) + one);
+        }
         for (int a = 0; a < d; a++) kout[a] = k[a];
         *pe_out = bond_part + (tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i) + wall_pe;
     }
@@ -1229,12 +1285,18 @@ template <typename F> struct IntEngine {
         uint32_t nc[3] = {cl_dims[0], cl_dims[1], d == 3 ? cl_dims[2] : 1u};
         double b[3] = {sys.box_f64(0), sys.box_f64(1), d == 3 ? sys.box_f64(2) : 1.0};
         std::vector<double> pe_part(n, 0.0);
+        std::vector<int64_t> piston_part(n, 0);
 #pragma omp parallel for schedule(dynamic, 256) num_threads(threads) if (threads > 1)
         for (long long ii = 0; ii < (long long)n; ii++) {
             size_t i = (size_t)ii;
-            force_on(i, cl, nc, b, &kicks[d * i], &pe_part[i], wall_force[i].data());
+            force_on(i, cl, nc, b, &kicks[d * i], &pe_part[i], wall_force[i].data(), &piston_part[i]);
         }
-        for (size_t i = 0; i < n; i++) pe += pe_part[i];
+        uint64_t piston_fixed = 0; // an integer sum (wrapping): the same in any order
+        for (size_t i = 0; i < n; i++) {
+            pe += pe_part[i];
+            piston_fixed += (uint64_t)piston_part[i];
+        }
+        piston_force = (double)(int64_t)piston_fixed / 65536.0;
         return pe;
     }
 
@@ -1250,7 +1312,8 @@ template <typename F> struct IntEngine {
 #pragma omp parallel for schedule(dynamic, 64) num_threads(threads) if (threads > 1)
         for (long long q = 0; q < (long long)m; q++) {
             double pe_i, wf[6] = {0, 0, 0, 0, 0, 0};
-            force_on(idx[q], cl, nc, b, out + d * q, &pe_i, wf);
+            int64_t pf = 0;
+            force_on(idx[q], cl, nc, b, out + d * q, &pe_i, wf, &pf);
         }
     }
 
@@ -1283,6 +1346,10 @@ template <typename F> struct IntEngine {
                         const double b0 = sys.velocity(v[0]), b1 = sys.velocity(v[1]);
                         v[0] = wadd(sys.to_step_displacement(u[0]), drift);
                         v[1] = sys.to_step_displacement(u[1]);
+                        if (piston_drive == 1) { // relative to the affine flow under a driven piston (int_engine.rs:282-286)
+                            const double f = std::clamp(to_f64(x[1]) / to_f64(piston_w), 0.0, 1.0);
+                            v[1] = wadd(v[1], sat_i32(std::round((double)piston_v * f)));
+                        }
                         const double a0 = sys.velocity(v[0]), a1 = sys.velocity(v[1]);
                         de = 0.5 * m * (a0 * a0 + a1 * a1 - b0 * b0 - b1 * b1);
                     } else {
@@ -1339,7 +1406,12 @@ template <typename F> struct IntEngine {
                         }
                     }
                 }
+                if (piston_drive && x[1] >= piston_w) { // int_engine.rs:333-336: mirrored below the piston
+                    x[1] = 2 * piston_w - 1 - x[1];
+                    v[1] = wneg(v[1]);
+                }
             }
+            move_piston(piston_force);
             steps += 1;
             clock += 1;
         }
@@ -1386,6 +1458,10 @@ template <typename F> struct IntEngine {
                 int32_t g = pinned ? 0 : gravity[a];
                 state.vel[d * i + a] = wneg(wadd(wadd(state.vel[d * i + a], kicks[d * i + a]), g));
             }
+        }
+        if (piston_drive) { // int_engine.rs:404-410
+            const int32_t kick = piston_drive == 2 ? piston_kick(piston_force - piston_ext) : 0;
+            piston_v = wneg(wadd(piston_v, kick));
         }
         steps = -steps;
     }

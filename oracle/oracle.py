@@ -65,6 +65,8 @@ _SIGS = [
     ("oracle_engine_wall_ledger", None, [VP, DP, DP, U64P]),
     ("oracle_engine_wall_ledger_fixed", None, [VP, I64P, I64P]),
     ("oracle_engine_set_bonds", None, [VP, U32P, DP, DP, C.c_uint32, U32P, C.c_uint64]),
+    ("oracle_engine_set_piston", C.c_int, [VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
+    ("oracle_engine_piston", None, [VP, I64P, I32P, DP, DP]),
     ("oracle_engine_steps", C.c_int64, [VP]),
     ("oracle_engine_energy", None, [VP, DP, DP]),
     ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
@@ -323,6 +325,10 @@ class IntEngine:
             raise ValueError("oracle engine creation failed")
         if getattr(sys, "bonds", None):
             self.set_bonds([("fene" if t.fene else "harmonic", t.k, t.r0) for t in sys.bond_types], sys.bonds)
+        if getattr(sys, "piston", None):
+            drive, start, lo = sys.piston
+            if lib().oracle_engine_set_piston(self._h, drive.kind, drive.speed, drive.mass, drive.force, start, lo) != 0:
+                raise ValueError("the oracle refused the piston")
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -384,6 +390,13 @@ class IntEngine:
         b = np.ascontiguousarray(np.array(bonds, np.uint32).reshape(-1, 3))
         lib().oracle_engine_set_bonds(self._h, _p(fene, C.c_uint32), _p(k, C.c_double), _p(r0, C.c_double), nt, _p(b, C.c_uint32), len(b))
         return self
+
+    def piston(self):
+        """IntEngine's piston_w (position units), piston_v (per step), piston_work (eps) and the
+        gas's force on it in the last force evaluation (eps/sigma)."""
+        w, v, work, f = C.c_int64(), C.c_int32(), C.c_double(), C.c_double()
+        lib().oracle_engine_piston(self._h, C.byref(w), C.byref(v), C.byref(work), C.byref(f))
+        return w.value, v.value, work.value, f.value
 
     def wall_ledger_fixed(self):
         """Every ledger event's energy change and impulse rounded to 2^-24 and summed as integers

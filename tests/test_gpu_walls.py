@@ -252,3 +252,84 @@ def test_membrane_follows_the_oracle(O, mode, pores):
     if not pores:
         assert hits_right > 20  # the solute hit the membrane from the right
         assert all(to_f64(int(p)) > half - 0.5 for p in st.pos[st.species == 1, 0])
+
+
+# ---------------------------------------------------------------- pistons (2D)
+def _piston_gas(O, n, density, drive, seed):
+    """md-ref/tests/boundaries.rs:270-285: a WCA gas under a piston (soft floor, hard roof at twice
+    box_for's height, the piston starting at half of it and stopping at 2 sigma)."""
+    from test_oracle import _gas_under_piston
+
+    return _gas_under_piston(O, n, density, drive, seed)
+
+
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_driven_piston_follows_the_oracle_and_reverses(O, mode):
+    """boundaries.rs:287-298 on the GPU: 500 particles under a piston driven down at 0.5 sigma/tau:
+    2000 steps equal IntEngine<f32>'s bit for bit (state, piston height, velocity and work, and
+    the ledger); reversed, 2000 steps and reversed again, the initial state and height exactly."""
+    from micrographia_gb300 import Piston
+
+    sys_, s0 = _piston_gas(O, 500, 0.3, Piston.speed_drive(-0.5), 16)
+    n = s0.n()
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_with_skin(sys_, n, 0.3)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, m) as g:
+        w0 = g.piston()[0]
+        assert w0 == c.piston()[0]
+        g.step(2000)
+        c.step(2000)
+        assert g.read_state() == c.state
+        assert g.piston() == c.piston()[:3]
+        assert g.piston()[0] < w0
+        _same_ledger(g, c)
+        kg, peg = g.kicks()
+        kc, pec = c.kicks()
+        assert np.array_equal(kg, kc)
+        g.reverse()
+        g.step(2000)
+        g.reverse()
+        assert g.read_state() == s0
+        assert g.piston()[0] == w0
+
+
+def test_free_piston_follows_the_oracle_and_balances_the_pressure(O):
+    """boundaries.rs:300-319 on the GPU: a free piston (mass 50, 15 eps/sigma down) over 600
+    particles; 3000 steps equal IntEngine<f32>'s bit for bit (the piston's kicks come from the
+    gas's force summed in 2^-16 units, so in any order the same); then, after 10,000 steps, the
+    floor's time-averaged pressure over 60,000 steps equals the external pressure within 5%."""
+    from micrographia_gb300 import Piston
+
+    force = 15.0
+    sys_, s0 = _piston_gas(O, 600, 0.2, Piston.free(50.0, force), 17)
+    width = sys_.box_f64()[0]
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, ForceMode.verlet_with_skin(sys_, s0.n(), 0.3)) as g:
+        g.step(3000)
+        c.step(3000)
+        assert g.read_state() == c.state
+        assert g.piston() == c.piston()[:3]
+        g.step(7000)
+        before = g.read_ledger()[1][2]
+        steps = 60000
+        g.step(steps)
+        p_bottom = (g.read_ledger()[1][2] - before) / (steps * sys_.dt * width)
+    assert abs(p_bottom / (force / width) - 1.0) < 0.05, p_bottom
+
+
+def test_driven_piston_with_a_bath_follows_the_oracle(O):
+    """A piston driven up at 0.3 sigma/tau over a gas in an Andersen bath (T 1.2, rate 2 per tau):
+    redrawn particles take the piston's affine flow (int_engine.rs:282-286); 1500 steps equal
+    IntEngine<f32>'s bit for bit, with the same ledger (the bath's energy included)."""
+    from micrographia_gb300 import Piston
+
+    sys_, s0 = _piston_gas(O, 400, 0.3, Piston.speed_drive(0.3), 19)
+    sys_.with_thermostat(1.2, 2.0)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, ForceMode.cell_list()) as g:
+        for _ in range(3):
+            g.step(500)
+            c.step(500)
+            assert g.read_state() == c.state
+            assert g.piston() == c.piston()[:3]
+        _same_ledger(g, c)

@@ -745,3 +745,75 @@ def test_oracle_bond_kicks_match_a_python_restatement(O):
             # round half to even, saturating like Rust's `as i32` (the stretched FENE bond saturates)
             want = [int(min(max(np.rint(f32(aa * fa)), -(2**31)), 2**31 - 1)) for fa in f]
             assert list(k[i]) == want, (i, j, t)
+
+
+# ---------------------------------------------------------------- pistons (md-ref/tests/boundaries.rs:270-338)
+def _gas_under_piston(O, n, density, drive, seed):
+    """boundaries.rs:270-285: a WCA gas in a box twice the height of box_for's, soft floor, hard
+    roof, the piston starting at half the height (stopping at 2 sigma); the fluid lattice
+    squeezed into the lower half."""
+    from micrographia_gb300 import Wall
+
+    bl = box_for(n, density, 1.0)
+    bl[1] *= 2
+    h = to_f64(bl[1]) / 2.0
+    sys_ = System(bl, 0.005, Pair.wca(), [1.0]).with_walls(1, Wall.soft(), Wall.hard()).with_piston(drive, h, 2.0)
+    s = O.fluid(sys_, n, 1.0, seed)
+    s.pos[:, 1] //= 2
+    return sys_, s
+
+
+def test_oracle_moving_piston_is_exactly_reversible(O):
+    """boundaries.rs:287-298: 500 particles under a piston driven down at 0.5 sigma/tau: 2000 steps
+    lower it; reversed, 2000 steps and reversed again, the state and the piston's height exactly."""
+    from micrographia_gb300 import Piston
+
+    sys_, s0 = _gas_under_piston(O, 500, 0.3, Piston.speed_drive(-0.5), 16)
+    e = O.IntEngine(sys_, s0)
+    w0 = e.piston()[0]
+    e.step(2000)
+    assert e.piston()[0] < w0
+    e.reverse()
+    e.step(2000)
+    e.reverse()
+    assert e.state == s0
+    assert e.piston()[0] == w0
+
+
+def test_oracle_free_piston_balances_the_pressure(O):
+    """boundaries.rs:300-319: a free piston (mass 50, 15 eps/sigma pushing down) over 600 particles
+    settles where the time-averaged pressure on the floor (its ledger impulse over 60,000 steps
+    after 10,000) equals the piston's external pressure within 5%."""
+    from micrographia_gb300 import Piston
+
+    force = 15.0
+    sys_, s0 = _gas_under_piston(O, 600, 0.2, Piston.free(50.0, force), 17)
+    width = sys_.box_f64()[0]
+    e = O.IntEngine(sys_, s0)
+    e.step(10000)
+    before = e.wall_ledger()[1][2]
+    steps = 60000
+    e.step(steps)
+    p_bottom = (e.wall_ledger()[1][2] - before) / (steps * sys_.dt * width)
+    assert abs(p_bottom / (force / width) - 1.0) < 0.05, p_bottom
+
+
+def test_oracle_fast_compression_heats_more_than_adiabatic(O):
+    """boundaries.rs:321-338: 400 particles (density 0.05) compressed to a third of the height at
+    0.4 sigma/tau by IntEngine<f64>: T A grows by more than 5% (slow compression keeps T A, the 2D
+    adiabat), and the work the piston did is the energy the gas gained, within 1%."""
+    from micrographia_gb300 import Piston
+
+    n = 400
+    sys_, s0 = _gas_under_piston(O, n, 0.05, Piston.speed_drive(-0.4), 18)
+    width = sys_.box_f64()[0]
+    e = O.IntEngine(sys_, s0, f64=True)
+    t0, h0 = e.energy()[0] / n, to_f64(e.piston()[0])
+    k0 = sum(e.energy())
+    steps = int((h0 * 2.0 / 3.0) / (0.4 * sys_.dt))
+    e.step(steps)
+    t1, h1 = e.energy()[0] / n, to_f64(e.piston()[0])
+    a0, a1 = width * (h0 - 1.0), width * (h1 - 1.0)
+    assert t1 * a1 > 1.05 * t0 * a0, (t0 * a0, t1 * a1)
+    gained = sum(e.energy()) - k0
+    assert abs(gained + e.piston()[2]) < 0.01 * gained, (gained, e.piston()[2])
