@@ -98,7 +98,11 @@ def _profile_run(name):
       more by direct launches of the loop (k_force_loop; a profiler cannot see kernels inside the
       graphs' conditional nodes);
     - batch: the first 256 of the 1024 batched 2D replicas, 300 steps in 100-step graphs, then 50
-      steps by direct launches (k_bforce_list, k_bbuild_list)."""
+      steps by direct launches (k_bforce_list, k_bbuild_list);
+    - scenario2d: a 2D Kremer-Grest melt of 32,768 chains of 32 beads (N = 2^20, rho 0.3, WCA
+      beads, FENE bonds) between a soft floor and a hard roof, under a piston driven down at
+      0.1 sigma/tau from the roof; 50 steps in graphs, then 30 by direct launches (k_force_list,
+      k_slot_of, k_bonds, k_walls, k_piston_tick)."""
     from .engine import BatchEngine, ForceMode, GpuEngine3, init_state
 
     if name == "frames3d":
@@ -125,8 +129,27 @@ def _profile_run(name):
             b.wait()
             f, r, nr = b.time_phases(50)
             print(f"batch: {sum(st.n() for st in states)} particles, force {f:.3f} ms, rebuild {r:.3f} ms ({nr} in 50 steps)")
+    elif name == "scenario2d":
+        import numpy as np
+
+        from .core import Bond, Piston, State, Wall, chains, to_f64
+        from .engine import GpuEngine
+
+        n_chains, length = 32768, 32
+        n = n_chains * length
+        sys2 = System(box_for(n, 0.3, 1.0), 0.005, Pair.wca(), [1.0]).with_walls(1, Wall.soft(), Wall.hard())
+        pos, bonds = chains(sys2, n_chains, length, 0.97)
+        sys2.with_bonds([Bond.kremer_grest()], bonds)
+        sys2.with_piston(Piston.speed_drive(-0.1), to_f64(sys2.box_len[1]), 2.0)
+        vel = init_state(sys2, _abi.INIT_FLUID, n, 1.0, 5).vel  # Maxwell velocities with zero sum
+        st = State(pos, vel, np.zeros(n, np.uint32))
+        with GpuEngine(sys2, st, ForceMode.verlet_with_skin(sys2, n, 0.3)) as e:
+            e.step(50)
+            f, r, nr = e.time_phases(30)
+            w, v, work = e.piston()
+            print(f"scenario2d: N {n}, force pass {f:.3f} ms, rebuild {r:.3f} ms ({nr} in 30 steps), piston at {to_f64(w):.2f}")
     else:
-        raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d or batch")
+        raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d, batch or scenario2d")
 
 
 if __name__ == "__main__":
