@@ -413,6 +413,20 @@ int gbmd_batch_step(gbmd_batch* b, uint64_t steps);
 int gbmd_batch_sync(gbmd_batch* b);
 /* The id-ordered state of system k. */
 int gbmd_batch_read_system(gbmd_batch* b, uint32_t k, int64_t* pos, int32_t* vel, uint32_t* species);
+/* Set each system's step clock (IntEngine::clock, on which its heat bath draws) to clocks[k]: a
+ * system that continues a run elsewhere keeps its clock. Systems start at 0 otherwise. */
+int gbmd_batch_set_clocks(gbmd_batch* b, const uint32_t* clocks);
+/* The id-ordered states of every system, concatenated at the batch's offsets (one conversion). */
+int gbmd_batch_read_all(gbmd_batch* b, int64_t* pos, int32_t* vel, uint32_t* species);
+/* A frame of every system at once: gbmd_observe's energies, virial, temperature and pressure per
+ * system into frames[count] (`step` is the batch's steps), and, with rdf_bins > 0, each system's
+ * RDF counts (unordered pairs, floor(r rdf_bins / rdf_rmax)) into rdf[count * rdf_bins], system by
+ * system; the counts equal a plain engine's exactly, the sums agree to rounding (they are added in
+ * another order). _begin enqueues the work and copies on the batch's stream and returns at once;
+ * _end waits for them. Stepping is refused while a frame is in flight. */
+int gbmd_batch_observe_begin(gbmd_batch* b, uint32_t rdf_bins, double rdf_rmax);
+int gbmd_batch_observe_end(gbmd_batch* b, gbmd_frame* frames, uint64_t* rdf);
+int gbmd_batch_observe(gbmd_batch* b, gbmd_frame* frames, uint64_t* rdf, uint32_t rdf_bins, double rdf_rmax);
 int gbmd_batch_stream(gbmd_batch* b, void** stream);
 /* Kernel launches of the batch so far (graph nodes included) and its list rebuilds. */
 int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds);
@@ -477,12 +491,16 @@ typedef struct gbmd_serve_stats_t {
     uint64_t bytes_in_use;
     uint64_t budget;
     uint64_t atom_steps;
+    uint64_t lane_requests; /* requests served in a lane (stepped together in a batch) */
+    uint64_t lane_repacks;  /* lane batches built: one per interval boundary where members joined or left */
 } gbmd_serve_stats_t;
 
 typedef struct gbmd_server gbmd_server;
 
 /* A server on `device` holding at most `max_active` requests (0: 64) within `hbm_budget_bytes`
- * of device memory. Requests are admitted first come, first served as memory and slots free up. */
+ * of device memory. Requests are admitted first come, first served as memory and slots free up.
+ * Small requests of one dimension are stepped together in a batch (gbmd_serve_set_lanes), the
+ * others each on an engine of their own; all of them overlap on the device. */
 int gbmd_serve_create(uint64_t hbm_budget_bytes, uint32_t max_active, int32_t device, gbmd_server** out);
 int gbmd_serve_submit(gbmd_server* sv, const gbmd_serve_request* req, uint64_t* request_id);
 /* Drive the loop once without blocking on the GPU: collect finished frame intervals, enqueue the
@@ -491,6 +509,11 @@ int gbmd_serve_poll(gbmd_server* sv, gbmd_serve_frame* frames, uint32_t cap, uin
 int gbmd_serve_cancel(gbmd_server* sv, uint64_t request_id);
 int gbmd_serve_stats(gbmd_server* sv, gbmd_serve_stats_t* stats);
 int gbmd_serve_destroy(gbmd_server* sv);
+/* Requests of at most `lane_max_n` particles (default 65,536; 0: none) whose frame cadence divides
+ * their steps are served in their dimension's lane: stepped together in one batch with the lane's
+ * other members, which share its cadence and RDF shape (those of the lane's first member), joining
+ * and leaving it at frame boundaries. Set before the first request. */
+int gbmd_serve_set_lanes(gbmd_server* sv, uint32_t lane_max_n);
 /* Device bytes a request of this size is charged against the budget. */
 uint64_t gbmd_serve_estimate_bytes(const gbmd_system* sys, uint32_t n, double skin);
 

@@ -206,6 +206,8 @@ class gbmd_serve_stats_t(C.Structure):
         ("bytes_in_use", C.c_uint64),
         ("budget", C.c_uint64),
         ("atom_steps", C.c_uint64),
+        ("lane_requests", C.c_uint64),
+        ("lane_repacks", C.c_uint64),
     ]
 
 
@@ -261,6 +263,11 @@ SIGNATURES = [
     ("gbmd_batch_step", C.c_int, [VP, C.c_uint64]),
     ("gbmd_batch_sync", C.c_int, [VP]),
     ("gbmd_batch_read_system", C.c_int, [VP, C.c_uint32, _I64P, _I32P, _U32P]),
+    ("gbmd_batch_read_all", C.c_int, [VP, _I64P, _I32P, _U32P]),
+    ("gbmd_batch_set_clocks", C.c_int, [VP, _U32P]),
+    ("gbmd_batch_observe_begin", C.c_int, [VP, C.c_uint32, C.c_double]),
+    ("gbmd_batch_observe_end", C.c_int, [VP, P(gbmd_frame), P(C.c_uint64)]),
+    ("gbmd_batch_observe", C.c_int, [VP, P(gbmd_frame), P(C.c_uint64), C.c_uint32, C.c_double]),
     ("gbmd_batch_stream", C.c_int, [VP, P(VP)]),
     ("gbmd_batch_stats", C.c_int, [VP, _U64P, _U32P]),
     ("gbmd_batch_skin", C.c_int, [VP, C.POINTER(C.c_double)]),
@@ -275,6 +282,7 @@ SIGNATURES = [
     ("gbmd_serve_stats", C.c_int, [VP, P(gbmd_serve_stats_t)]),
     ("gbmd_serve_destroy", C.c_int, [VP]),
     ("gbmd_serve_estimate_bytes", C.c_uint64, [P(gbmd_system), C.c_uint32, C.c_double]),
+    ("gbmd_serve_set_lanes", C.c_int, [VP, C.c_uint32]),
     ("gbmd_hash_state", C.c_uint64, [C.c_uint32, _I64P, _I32P, _U32P, C.c_uint32]),
     ("gbmd_check_pair_math", C.c_int, [P(gbmd_system), C.c_uint64, C.c_int32, P(C.c_uint64), P(C.c_uint64)]),
     ("gbmd_last_error", C.c_char_p, []),

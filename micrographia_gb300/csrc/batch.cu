@@ -251,7 +251,7 @@ __global__ void k_bbath(uint32_t N, const Params* __restrict__ tab, const uint32
         const int64_t p = wrap(x[ax] - (int64_t)v[ax], P.box[ax]);
         if (!(p >= P.bath_region[0] && p < P.bath_region[1])) return;
     }
-    const BathDraw o = bath_draw<D>(ids[i] - P.id_base, ctl[CTL_CLOCK], P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si],
+    const BathDraw o = bath_draw<D>(ids[i] - P.id_base, ctl[CTL_CLOCK] + P.clock_base, P.bath_key[0], P.bath_key[1], P.bath_rate_dt, P.bath_sd[si],
                                     P.masses[si], P.dt, P.bath_drift, 0, v[0], v[1], v[2], ledger + 2 * k);
     if (!o.hit) return;
 #pragma unroll
@@ -340,25 +340,49 @@ struct gbmd_batch {
     uint64_t exec_launches[2][2] = {{0, 0}, {0, 0}};
     uint64_t body_launches = 0, launches = 0;
     bool failed = false;
+    uint64_t steps = 0;
+    // frames (gbmd_batch_observe_*): a rebuild when the trigger is set, then per-tile partial sums
+    // (a tile: up to 128 slots of one system, whose slots are contiguous) and per-system RDF bins
+    cudaGraphExec_t exec_prep[2] = {nullptr, nullptr};
+    uint64_t exec_prep_launches[2] = {0, 0};
+    std::vector<uint4> tiles_h; // (system, first slot, slots, 0)
+    uint4* tiles = nullptr;
+    double* part = nullptr;
+    unsigned long long* obs_bins = nullptr;
+    size_t obs_bins_cap = 0;
+    double* part_h = nullptr;
+    size_t part_h_cap = 0;
+    unsigned long long* bins_h = nullptr;
+    size_t bins_h_cap = 0;
+    bool obs_pending = false;
+    uint32_t obs_nbins = 0;
 };
 
 namespace {
 
-template <typename T> int balloc(T** p, size_t count) {
-    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
-    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GBMD_E_NOMEM : GBMD_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+// Stream-ordered device memory (cudaFree would synchronise the whole device, stalling every other
+// engine and batch of a server each time one is retired).
+template <typename T> int balloc(T** p, size_t count, cudaStream_t s) {
+    cudaError_t e = cudaMallocAsync((void**)p, std::max<size_t>(count, 1) * sizeof(T), s);
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? GBMD_E_NOMEM : GBMD_E_CUDA, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
     return GBMD_OK;
 }
 
 void bfree(gbmd_batch* b) {
-    for (int p = 0; p < 2; p++)
+    for (int p = 0; p < 2; p++) {
         for (int k = 0; k < 2; k++)
             if (b->exec[p][k]) cudaGraphExecDestroy(b->exec[p][k]);
+        if (b->exec_prep[p]) cudaGraphExecDestroy(b->exec_prep[p]);
+    }
     void* ptrs[] = {b->tab, b->pos[0], b->pos[1], b->pos_scr, b->ref_pos, b->vel, b->vel_scr, b->species, b->species_scr, b->ids, b->ids_scr,
                     b->sysidx, b->sysidx_scr, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->scan_tmp, b->start, b->nbr,
-                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1], b->relf, b->ledger};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
+                    b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1], b->relf, b->ledger,
+                    b->tiles, b->part, b->obs_bins};
+    if (b->st)
+        for (void* p : ptrs)
+            if (p) cudaFreeAsync(p, b->st);
+    pinned_release(b->part_h, b->part_h_cap);
+    pinned_release(b->bins_h, b->bins_h_cap);
     if (b->st) cudaStreamDestroy(b->st);
     if (b->st_body) cudaStreamDestroy(b->st_body);
 }
@@ -405,7 +429,9 @@ void benqueue_force(gbmd_batch* b, cudaStream_t s) {
     else b->multi ? benqueue_force_t<3, true>(b, s) : benqueue_force_t<3, false>(b, s);
 }
 
-int bcapture(gbmd_batch* b, int parity, uint32_t count, cudaGraphExec_t* out, uint64_t* launches) {
+// `count` steps (a conditional rebuild, then the force step, each); with `force` false a single
+// conditional rebuild (before a frame).
+int bcapture(gbmd_batch* b, int parity, uint32_t count, cudaGraphExec_t* out, uint64_t* launches, bool force = true) {
     int saved = b->cur;
     b->cur = parity;
     uint64_t l0 = launch_total();
@@ -439,7 +465,7 @@ int bcapture(gbmd_batch* b, int parity, uint32_t count, cudaGraphExec_t* out, ui
         cudaGraph_t tmp;
         GBMD_CUDA_TRY(cudaStreamEndCapture(b->st_body, &tmp));
         GBMD_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-        benqueue_force(b, s);
+        if (force) benqueue_force(b, s);
     }
     cudaGraph_t graph;
     cudaError_t err = cudaStreamEndCapture(s, &graph);
@@ -461,6 +487,125 @@ int brun(gbmd_batch* b, int which) {
     b->launches += b->exec_launches[parity][which];
     if (count & 1) b->cur ^= 1;
     return GBMD_OK;
+}
+
+// The per-system observables of gbmd_observe over the batch's Verlet lists (IntEngine::energy's
+// on-step kinetic energy, the pair potential and virial): the list path of k_kicks with the
+// system's own parameter block. Each block takes one tile of one system's slots and writes its
+// partial sums (potential, virial, kinetic), which the host adds per system in tile order.
+template <int D, bool MULTI>
+__global__ void __launch_bounds__(128) k_bframe(const Params* __restrict__ tab, const uint4* __restrict__ tiles, const PosRec<D>* __restrict__ pos,
+                                                const uint32_t* __restrict__ species, const uint32_t* __restrict__ nbr,
+                                                const uint32_t* __restrict__ nbr_count, const int32_t* __restrict__ vel,
+                                                double* __restrict__ partial) {
+    __shared__ double sh[3][4];
+    const uint4 t = tiles[blockIdx.x];
+    const Params& P = tab[t.x];
+    double pe = 0.0, w = 0.0, ke = 0.0;
+    if (threadIdx.x < t.z) {
+        const uint32_t i = t.y + threadIdx.x;
+        int64_t xi[3];
+        const uint32_t si = load_particle<D, MULTI>(pos, species, i, xi);
+        const float cs = P.kick_cs[si];
+        int32_t k[3] = {0, 0, 0};
+        F32Sum pe32, w32;
+        const uint32_t m = nbr_count[i], cap4 = (P.cap + 3u) & ~3u;
+        for (uint32_t q = 0; q < m; q++) {
+            const uint32_t j = nbr[list_slot(i, q, cap4)] & LIST_MASK;
+            int64_t xj[3];
+            const uint32_t sj = load_particle<D, MULTI>(pos, species, j, xj);
+            const PairC& pc = P.pc[si * P.ns + sj];
+            float fr, s6, r2;
+            if (pair_kick<D>(P, pc, cs, xi, xj, k, fr, s6, r2)) {
+                pe32.add(pair_u(pc, s6));
+                w32.add(__fmul_rn(fr, r2));
+            }
+        }
+        pe = 0.5 * pe32.value();
+        w = 0.5 * w32.value();
+        const double m_i = P.masses[si];
+        for (int a = 0; a < D; a++) {
+            const int32_t v0 = vel[D * i + a];
+            const int32_t next = wadd(wadd(v0, k[a]), P.gravity[a]);
+            const double vh = __dmul_rn(0.5, __dadd_rn(__ddiv_rn(__dmul_rn((double)v0, 1.0 / 4294967296.0), P.dt),
+                                                       __ddiv_rn(__dmul_rn((double)next, 1.0 / 4294967296.0), P.dt)));
+            ke += 0.5 * m_i * vh * vh;
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double vals[3] = {pe, w, ke};
+    for (int q = 0; q < 3; q++) {
+        double x = vals[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[q][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int wq = 0; wq < (int)(blockDim.x >> 5); wq++) s += sh[threadIdx.x][wq];
+        partial[4 * blockIdx.x + threadIdx.x] = s;
+    }
+}
+
+// Per-system RDF counts (unordered pairs, each once: slot j > slot i; floor(r bins / rmax) of
+// the exact minimum-image separation, rdf_bin) over the cells of the last list build. Every
+// particle is within half the skin of the position it was binned at, so a pair within rmax has
+// binned positions within rmax + skin: its cells differ by at most R = ceil((rmax + skin) nc / L)
+// per axis (every cell of an axis with 2R + 1 >= nc, each once). Each block counts one tile of
+// one system into shared memory and adds its counts to that system's bins.
+template <int D>
+__global__ void __launch_bounds__(128) k_brdf(const Params* __restrict__ tab, const uint4* __restrict__ tiles, const PosRec<D>* __restrict__ pos,
+                                              const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start, uint32_t bins, double rmax,
+                                              double skin, double scale, float scalef, float lim2f, float margin,
+                                              unsigned long long* __restrict__ out) {
+    extern __shared__ uint32_t h[];
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const uint4 t = tiles[blockIdx.x];
+    const Params& P = tab[t.x];
+    if (threadIdx.x < t.z) {
+        const uint32_t i = t.y + threadIdx.x;
+        int64_t xi[3] = {0, 0, 0};
+        load_particle<D, false>(pos, nullptr, i, xi);
+#pragma unroll
+        for (int a = 0; a < D; a++) xi[a] = wrap(xi[a], P.box[a]);
+        uint32_t c[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, span[3] = {1, 1, 1};
+        cell_coords(P, keys[i] - P.cell_base, c);
+#pragma unroll
+        for (int a = 0; a < D; a++) {
+            const uint32_t nc = P.nc[a];
+            const uint32_t R = (uint32_t)ceil(__dmul_rn(rmax + skin, (double)nc) / P.box_f[a] + 1e-9);
+            if (2 * R + 1 >= nc) {
+                lo[a] = 0;
+                span[a] = nc;
+            } else {
+                lo[a] = c[a] + nc - R;
+                span[a] = 2 * R + 1;
+            }
+        }
+        for (uint32_t oz = 0; oz < span[2]; oz++) {
+            const uint32_t z = D == 3 ? (lo[2] + oz) % P.nc[2] : 0u;
+            for (uint32_t oy = 0; oy < span[1]; oy++) {
+                const uint32_t y = (lo[1] + oy) % P.nc[1];
+                for (uint32_t ox = 0; ox < span[0]; ox++) {
+                    const uint32_t x = (lo[0] + ox) % P.nc[0];
+                    const uint32_t cell = P.cell_base + (z * P.nc[1] + y) * P.nc[0] + x;
+                    const uint32_t j1 = start[cell + 1];
+                    for (uint32_t j = max(start[cell], i + 1); j < j1; j++) {
+                        int64_t xj[3] = {0, 0, 0}, d[3] = {0, 0, 0};
+                        load_particle<D, false>(pos, nullptr, j, xj);
+#pragma unroll
+                        for (int a = 0; a < D; a++) d[a] = min_image(wrap(xj[a], P.box[a]) - xi[a], P.box[a], P.half[a]);
+                        const int k = rdf_bin<D>(d, bins, scale, scalef, lim2f, margin);
+                        if (k >= 0) atomicAdd(&h[k], 1u);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x)
+        if (h[b]) atomicAdd(out + (size_t)t.x * bins + b, (unsigned long long)h[b]);
 }
 
 int bcheck(gbmd_batch* b) {
@@ -611,38 +756,45 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
     if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st_body, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
     size_t N = b->N;
-    step(balloc(&b->tab, count));
-    step(balloc((char**)&b->pos[0], N * b->rec));
-    step(balloc((char**)&b->pos[1], N * b->rec));
-    step(balloc((char**)&b->pos_scr, N * b->rec));
-    step(balloc((char**)&b->ref_pos, N * b->rec));
-    step(balloc(&b->vel, N * D));
-    step(balloc(&b->vel_scr, N * D));
-    step(balloc(&b->species, N));
-    step(balloc(&b->species_scr, N));
-    step(balloc(&b->ids, N));
-    step(balloc(&b->ids_scr, N));
-    step(balloc(&b->sysidx, N));
-    step(balloc(&b->sysidx_scr, N));
+    step(balloc(&b->tab, count, b->st));
+    step(balloc((char**)&b->pos[0], N * b->rec, b->st));
+    step(balloc((char**)&b->pos[1], N * b->rec, b->st));
+    step(balloc((char**)&b->pos_scr, N * b->rec, b->st));
+    step(balloc((char**)&b->ref_pos, N * b->rec, b->st));
+    step(balloc(&b->vel, N * D, b->st));
+    step(balloc(&b->vel_scr, N * D, b->st));
+    step(balloc(&b->species, N, b->st));
+    step(balloc(&b->species_scr, N, b->st));
+    step(balloc(&b->ids, N, b->st));
+    step(balloc(&b->ids_scr, N, b->st));
+    step(balloc(&b->sysidx, N, b->st));
+    step(balloc(&b->sysidx_scr, N, b->st));
     for (int k = 0; k < 2; k++) {
-        step(balloc(&b->keys[k], N));
-        step(balloc(&b->vals[k], N));
+        step(balloc(&b->keys[k], N, b->st));
+        step(balloc(&b->vals[k], N, b->st));
     }
     size_t hist_n = radix_hist_elems(N);
-    step(balloc(&b->hist, hist_n));
-    step(balloc(&b->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(N))));
-    step(balloc(&b->start, (size_t)b->ncell + 1));
-    step(balloc(&b->nbr, (N + 31) / 32 * 32 * (((size_t)b->cap + 3) & ~(size_t)3))); // warp-tiled (list_slot)
-    step(balloc(&b->qpos[0], N));
-    step(balloc(&b->relf, N));
-    step(balloc(&b->qpos[1], N));
-    step(balloc(&b->nbr_count, N));
-    step(balloc(&b->ctl, 16));
-    step(balloc(&b->ledger, 2 * (size_t)count));
+    step(balloc(&b->hist, hist_n, b->st));
+    step(balloc(&b->scan_tmp, std::max(scan_tmp_elems(hist_n), scan_tmp_elems(N)), b->st));
+    step(balloc(&b->start, (size_t)b->ncell + 1, b->st));
+    step(balloc(&b->nbr, (N + 31) / 32 * 32 * (((size_t)b->cap + 3) & ~(size_t)3), b->st)); // warp-tiled (list_slot)
+    step(balloc(&b->qpos[0], N, b->st));
+    step(balloc(&b->relf, N, b->st));
+    step(balloc(&b->qpos[1], N, b->st));
+    step(balloc(&b->nbr_count, N, b->st));
+    step(balloc(&b->ctl, 16, b->st));
+    step(balloc(&b->ledger, 2 * (size_t)count, b->st));
+    for (uint32_t k = 0; k < count; k++) // frame tiles: up to 128 slots of one system each
+        for (uint32_t s0 = offsets[k]; s0 < offsets[k + 1]; s0 += 128)
+            b->tiles_h.push_back(make_uint4(k, s0, std::min<uint32_t>(128u, offsets[k + 1] - s0), 0u));
+    step(balloc(&b->tiles, b->tiles_h.size(), b->st));
+    step(balloc(&b->part, 4 * b->tiles_h.size(), b->st));
+    if (r == GBMD_OK)
+        cudaMemcpyAsync(b->tiles, b->tiles_h.data(), b->tiles_h.size() * sizeof(uint4), cudaMemcpyHostToDevice, b->st);
     if (r == GBMD_OK) cudaMemsetAsync(b->ledger, 0, 16 * (size_t)count, b->st);
-    step(balloc((char**)&b->staging, N * D * 8));
-    step(balloc(&b->staging_v, N * D));
-    step(balloc(&b->staging_s, N));
+    step(balloc((char**)&b->staging, N * D * 8, b->st));
+    step(balloc(&b->staging_v, N * D, b->st));
+    step(balloc(&b->staging_s, N, b->st));
     if (r == GBMD_OK) {
         std::vector<uint32_t> sysi(N);
         for (uint32_t k = 0; k < count; k++)
@@ -654,7 +806,7 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
                 if (pos[D * i + a] < 0 || pos[D * i + a] >= systems[k].box_len[a]) r = fail(GBMD_E_INVALID, "positions must lie in [0, L)");
         }
         uint32_t* dsys = nullptr;
-        if (r == GBMD_OK) step(balloc(&dsys, N));
+        if (r == GBMD_OK) step(balloc(&dsys, N, b->st));
         if (r == GBMD_OK) {
             cudaMemcpyAsync(b->tab, b->P.data(), count * sizeof(Params), cudaMemcpyHostToDevice, b->st);
             cudaMemcpyAsync(b->staging, pos, N * D * 8, cudaMemcpyHostToDevice, b->st);
@@ -674,7 +826,7 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
             cudaError_t e = cudaStreamSynchronize(b->st);
             if (e != cudaSuccess) r = fail(GBMD_E_CUDA, cudaGetErrorString(e));
         }
-        if (dsys) cudaFree(dsys);
+        if (dsys) cudaFreeAsync(dsys, b->st);
     }
     if (r != GBMD_OK) {
         std::string msg = gbmd_last_error();
@@ -689,6 +841,8 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
 int gbmd_batch_step(gbmd_batch* b, uint64_t steps) {
     if (!b) return fail(GBMD_E_INVALID, "null batch");
     if (b->failed) return fail(GBMD_E_OVERFLOW, "the batch is in a failed state (a list overflowed)");
+    if (b->obs_pending) return fail(GBMD_E_INVALID, "a frame is in flight (gbmd_batch_observe_end first)");
+    b->steps += steps;
     uint64_t left = steps;
     while (left >= b->block_steps) {
         GBMD_TRY(brun(b, 1));
@@ -739,6 +893,135 @@ int gbmd_batch_time_phases(gbmd_batch* b, uint32_t steps, double* force_ms, doub
     if (rebuilds) *rebuilds = nr;
     GBMD_CUDA_TRY(cudaGetLastError());
     return bcheck(b);
+}
+
+int gbmd_batch_observe_begin(gbmd_batch* b, uint32_t rdf_bins, double rdf_rmax) {
+    if (!b) return fail(GBMD_E_INVALID, "null batch");
+    if (b->obs_pending) return fail(GBMD_E_INVALID, "a frame is already in flight (gbmd_batch_observe_end first)");
+    if (rdf_bins && (rdf_bins > 8192 || !(rdf_rmax > 0.0))) return fail(GBMD_E_INVALID, "bad RDF arguments");
+    const int parity = b->cur;
+    if (!b->exec_prep[parity]) GBMD_TRY(bcapture(b, parity, 1, &b->exec_prep[parity], &b->exec_prep_launches[parity], false));
+    GBMD_CUDA_TRY(cudaGraphLaunch(b->exec_prep[parity], b->st)); // the lists and cells, rebuilt if the trigger is set
+    b->launches += b->exec_prep_launches[parity];
+    const uint32_t nt = (uint32_t)b->tiles_h.size();
+    if (b->D == 2) {
+        if (b->multi)
+            k_bframe<2, true><<<nt, 128, 0, b->st>>>(b->tab, b->tiles, (const PosRec<2>*)b->pos[b->cur], b->species, b->nbr, b->nbr_count, b->vel, b->part);
+        else
+            k_bframe<2, false><<<nt, 128, 0, b->st>>>(b->tab, b->tiles, (const PosRec<2>*)b->pos[b->cur], b->species, b->nbr, b->nbr_count, b->vel, b->part);
+    } else {
+        if (b->multi)
+            k_bframe<3, true><<<nt, 128, 0, b->st>>>(b->tab, b->tiles, (const PosRec<3>*)b->pos[b->cur], b->species, b->nbr, b->nbr_count, b->vel, b->part);
+        else
+            k_bframe<3, false><<<nt, 128, 0, b->st>>>(b->tab, b->tiles, (const PosRec<3>*)b->pos[b->cur], b->species, b->nbr, b->nbr_count, b->vel, b->part);
+    }
+    note_launch();
+    if (!b->part_h) {
+        b->part_h = (double*)pinned_alloc(4 * (size_t)nt * 8, &b->part_h_cap);
+        if (!b->part_h) return fail(GBMD_E_NOMEM, "pinned frame buffer");
+    }
+    GBMD_CUDA_TRY(cudaMemcpyAsync(b->part_h, b->part, 4 * (size_t)nt * 8, cudaMemcpyDeviceToHost, b->st));
+    if (rdf_bins) {
+        const size_t nbins = (size_t)rdf_bins * b->K;
+        if (nbins > b->obs_bins_cap) {
+            if (b->obs_bins) GBMD_CUDA_TRY(cudaFreeAsync(b->obs_bins, b->st));
+            b->obs_bins = nullptr;
+            b->obs_bins_cap = 0;
+            GBMD_TRY(balloc(&b->obs_bins, nbins, b->st));
+            b->obs_bins_cap = nbins;
+        }
+        if (nbins * 8 > b->bins_h_cap) {
+            pinned_release(b->bins_h, b->bins_h_cap);
+            b->bins_h = (unsigned long long*)pinned_alloc(nbins * 8, &b->bins_h_cap);
+            if (!b->bins_h) return fail(GBMD_E_NOMEM, "pinned RDF buffer");
+        }
+        GBMD_CUDA_TRY(cudaMemsetAsync(b->obs_bins, 0, nbins * 8, b->st));
+        const double scale = (double)rdf_bins / rdf_rmax;
+        const float scalef = (float)scale, lim2f = (float)(rdf_rmax * rdf_rmax * (1.0 + 1e-4));
+        const float margin = (float)(1e-6 * rdf_bins + 1e-5);
+        const size_t shm = (size_t)rdf_bins * 4;
+        if (b->D == 2)
+            k_brdf<2><<<nt, 128, shm, b->st>>>(b->tab, b->tiles, (const PosRec<2>*)b->pos[b->cur], b->keys[b->sorted], b->start, rdf_bins,
+                                               rdf_rmax, b->skin, scale, scalef, lim2f, margin, b->obs_bins);
+        else
+            k_brdf<3><<<nt, 128, shm, b->st>>>(b->tab, b->tiles, (const PosRec<3>*)b->pos[b->cur], b->keys[b->sorted], b->start, rdf_bins,
+                                               rdf_rmax, b->skin, scale, scalef, lim2f, margin, b->obs_bins);
+        note_launch();
+        GBMD_CUDA_TRY(cudaMemcpyAsync(b->bins_h, b->obs_bins, nbins * 8, cudaMemcpyDeviceToHost, b->st));
+    }
+    GBMD_CUDA_TRY(cudaGetLastError());
+    b->obs_pending = true;
+    b->obs_nbins = rdf_bins;
+    return GBMD_OK;
+}
+
+int gbmd_batch_observe_end(gbmd_batch* b, gbmd_frame* frames, uint64_t* rdf) {
+    if (!b) return fail(GBMD_E_INVALID, "null batch");
+    if (!b->obs_pending) return fail(GBMD_E_INVALID, "no frame in flight (gbmd_batch_observe_begin first)");
+    b->obs_pending = false;
+    GBMD_TRY(gbmd_batch_sync(b)); // returns at once when the frame's work is done
+    if (rdf && b->obs_nbins) std::memcpy(rdf, b->bins_h, (size_t)b->obs_nbins * b->K * 8);
+    if (!frames) return GBMD_OK;
+    std::vector<double> pe(b->K, 0.0), w(b->K, 0.0), ke(b->K, 0.0);
+    for (size_t t = 0; t < b->tiles_h.size(); t++) { // per system, in tile order
+        const uint32_t k = b->tiles_h[t].x;
+        pe[k] += b->part_h[4 * t];
+        w[k] += b->part_h[4 * t + 1];
+        ke[k] += b->part_h[4 * t + 2];
+    }
+    bool finite = true;
+    for (uint32_t k = 0; k < b->K; k++) { // as gbmd_observe_end
+        const gbmd_system& s = b->sys[k];
+        const uint32_t n = b->offsets[k + 1] - b->offsets[k];
+        double vol = 1.0;
+        for (int a = 0; a < b->D; a++) vol *= (double)s.box_len[a] * (1.0 / 4294967296.0);
+        const double dof = 0.5 * b->D * std::max((double)n - 1.0, 1.0);
+        gbmd_frame& f = frames[k];
+        f.step = b->steps;
+        f.kinetic = ke[k];
+        f.potential = pe[k];
+        f.virial = w[k];
+        f.temperature = ke[k] / dof;
+        f.pressure = (double)n / vol * f.temperature + w[k] / (b->D * vol);
+        f.volume = vol;
+        f.n = n;
+        f.dim = (uint32_t)b->D;
+        finite = finite && std::isfinite(ke[k]) && std::isfinite(pe[k]) && std::isfinite(w[k]);
+    }
+    if (!finite) return fail(GBMD_E_NONFINITE, "a non-finite energy or virial (the frames are filled in)");
+    return GBMD_OK;
+}
+
+int gbmd_batch_observe(gbmd_batch* b, gbmd_frame* frames, uint64_t* rdf, uint32_t rdf_bins, double rdf_rmax) {
+    GBMD_TRY(gbmd_batch_observe_begin(b, rdf_bins, rdf_rmax));
+    return gbmd_batch_observe_end(b, frames, rdf);
+}
+
+int gbmd_batch_set_clocks(gbmd_batch* b, const uint32_t* clocks) {
+    if (!b || !clocks) return fail(GBMD_E_INVALID, "null argument");
+    if (b->obs_pending) return fail(GBMD_E_INVALID, "a frame is in flight (gbmd_batch_observe_end first)");
+    uint32_t c = 0;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(&c, b->ctl + CTL_CLOCK, 4, cudaMemcpyDeviceToHost, b->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(b->st));
+    for (uint32_t k = 0; k < b->K; k++) b->P[k].clock_base = clocks[k] - c; // (wrapping, as the clock)
+    GBMD_CUDA_TRY(cudaMemcpyAsync(b->tab, b->P.data(), b->K * sizeof(Params), cudaMemcpyHostToDevice, b->st));
+    return gbmd_batch_sync(b);
+}
+
+int gbmd_batch_read_all(gbmd_batch* b, int64_t* pos, int32_t* vel, uint32_t* species) {
+    if (!b) return fail(GBMD_E_INVALID, "null batch");
+    size_t N = b->N, D = b->D;
+    if (D == 2)
+        k_bto_ids<2><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, b->tab, b->sysidx, (const PosRec<2>*)b->pos[b->cur], b->vel,
+                                                        b->species, b->ids, (int64_t*)b->staging, b->staging_v, b->staging_s);
+    else
+        k_bto_ids<3><<<nblocks(N, 256), 256, 0, b->st>>>((uint32_t)N, b->tab, b->sysidx, (const PosRec<3>*)b->pos[b->cur], b->vel,
+                                                        b->species, b->ids, (int64_t*)b->staging, b->staging_v, b->staging_s);
+    note_launch();
+    if (pos) GBMD_CUDA_TRY(cudaMemcpyAsync(pos, b->staging, N * D * 8, cudaMemcpyDeviceToHost, b->st));
+    if (vel) GBMD_CUDA_TRY(cudaMemcpyAsync(vel, b->staging_v, N * D * 4, cudaMemcpyDeviceToHost, b->st));
+    if (species) GBMD_CUDA_TRY(cudaMemcpyAsync(species, b->staging_s, N * 4, cudaMemcpyDeviceToHost, b->st));
+    return gbmd_batch_sync(b);
 }
 
 int gbmd_batch_sync(gbmd_batch* b) {

@@ -1294,6 +1294,17 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
 
 } // namespace
 
+// The pinned pool for the batches' frames.
+namespace gbmd {
+void* pinned_alloc(size_t bytes, size_t* cap) {
+    *cap = pin_class(bytes);
+    void* p = pinned_take(*cap);
+    if (!p) *cap = 0;
+    return p;
+}
+void pinned_release(void* p, size_t cap) { pinned_give(p, cap); }
+} // namespace gbmd
+
 // ================================================================== C ABI
 extern "C" {
 
@@ -2007,41 +2018,6 @@ const char* gbmd_version(void) { return "gbmd 0.1 (sm_103a)"; }
 // ------------------------------------------------------------------ observables
 namespace {
 
-// The exact bin of a pair whose f32 estimate was too close to a bin edge or to rmax.
-template <int D> __device__ __forceinline__ int rdf_bin_exact(const int64_t* d, uint32_t bins, double scale) {
-    double r2 = 0.0;
-#pragma unroll
-    for (int a = 0; a < D; a++) {
-        const double x = to_f64(d[a]);
-        r2 = __dadd_rn(r2, __dmul_rn(x, x));
-    }
-    const double r = __dmul_rn(__dsqrt_rn(r2), scale);
-    return r < (double)bins ? (int)(uint32_t)r : -1;
-}
-
-// RDF pair counts over unordered pairs of the cell-sorted scratch state: bin
-// floor(sqrt(r2) * scale) with r2 the f64 square of the exact minimum-image separation.
-// The RDF bin of a pair at minimum-image separation d: k = floor(sqrt(r2) bins / rmax) with r2
-// the f64 square of the exact separation, or -1 beyond rmax. Decided in f32 when that is safe:
-// the f32 estimate of r bins / rmax is within 3.3e-7 of it relatively (separations rounded to
-// f32, a fused sum of squares, a square root, one product), so a pair farther than `margin` bins
-// from a bin edge, or clearly beyond rmax (r2 above lim2f), is binned without f64 arithmetic,
-// which runs at a small fraction of the f32 rate on this GPU; the rest takes the f64 definition.
-template <int D>
-__device__ __forceinline__ int rdf_bin(const int64_t* d, uint32_t bins, double scale, float scalef, float lim2f, float margin) {
-    float r2f = 0.0f;
-#pragma unroll
-    for (int a = 0; a < D; a++) {
-        const float x = __fmul_rn(__ll2float_rn(d[a]), 1.0f / 4294967296.0f);
-        r2f = __fmaf_rn(x, x, r2f);
-    }
-    if (r2f > lim2f) return -1;
-    const float rf = __fmul_rn(__fsqrt_rn(r2f), scalef);
-    const float fl = floorf(rf), fr = rf - fl;
-    if (fr > margin && fr < 1.0f - margin && rf < (float)bins - margin) return (int)fl;
-    return rdf_bin_exact<D>(d, bins, scale);
-}
-
 // RDF pair counts over unordered pairs of the cell-sorted scratch state (cells of side >= rmax,
 // at least three per axis). A candidate j of neighbour cell cj sits at d = relf[j] + base with
 // base = (cj - c) cell_w + image - (xi - c cell_w), an exact integer converted once per cell, so
@@ -2468,8 +2444,9 @@ extern "C" int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, in
     int32_t* dvel = nullptr;
     uint32_t* dsp = nullptr;
     int rc = GBMD_OK;
-    if (cudaMalloc(&dpos, n * (D == 2 ? 16 : 32)) != cudaSuccess || cudaMalloc(&dvel, n * D * 4) != cudaSuccess ||
-        cudaMalloc(&dsp, n * 4) != cudaSuccess)
+    // (stream-ordered: a server creates states while other requests run)
+    if (cudaMallocAsync(&dpos, n * (D == 2 ? 16 : 32), s) != cudaSuccess || cudaMallocAsync((void**)&dvel, n * D * 4, s) != cudaSuccess ||
+        cudaMallocAsync((void**)&dsp, n * 4, s) != cudaSuccess)
         rc = fail(GBMD_E_NOMEM, "init buffers");
     if (rc == GBMD_OK) rc = init_state_device(*sys, *spec, dpos, dvel, dsp, s);
     std::vector<int64_t> rec;
@@ -2486,9 +2463,10 @@ extern "C" int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, in
         for (size_t i = 0; i < n; i++)
             for (size_t a = 0; a < D; a++) pos[D * i + a] = rec[w * i + a];
     }
-    cudaFree(dpos);
-    cudaFree(dvel);
-    cudaFree(dsp);
+    if (dpos) cudaFreeAsync(dpos, s);
+    if (dvel) cudaFreeAsync(dvel, s);
+    if (dsp) cudaFreeAsync(dsp, s);
+    cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     return rc;
 }

@@ -28,6 +28,10 @@ double rc_max(const gbmd_system& s);
 int cells_for(const gbmd_system& s, double r, uint32_t* c);                 // System::cells_for
 void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint32_t cap, const uint32_t* nc);
 int key_bits(uint32_t ncell);
+// Pinned host memory from a process-wide pool that is never freed (freeing pinned memory
+// synchronises the device): at least `bytes`, its block size in *cap (0 on failure).
+void* pinned_alloc(size_t bytes, size_t* cap);
+void pinned_release(void* p, size_t cap);
 void set_cells(Params& P, const uint32_t* nc, uint32_t dim);
 
 } // namespace gbmd

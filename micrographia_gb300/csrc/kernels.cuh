@@ -1702,4 +1702,38 @@ __global__ void k_zero_apply(uint32_t n, int32_t* __restrict__ vel, const uint32
     }
 }
 
+// ---------------------------------------------------------------- RDF bins
+// The exact bin of a pair whose f32 estimate was too close to a bin edge or to rmax.
+template <int D> __device__ __forceinline__ int rdf_bin_exact(const int64_t* d, uint32_t bins, double scale) {
+    double r2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const double x = to_f64(d[a]);
+        r2 = __dadd_rn(r2, __dmul_rn(x, x));
+    }
+    const double r = __dmul_rn(__dsqrt_rn(r2), scale);
+    return r < (double)bins ? (int)(uint32_t)r : -1;
+}
+
+// The RDF bin of a pair at minimum-image separation d: k = floor(sqrt(r2) bins / rmax) with r2
+// the f64 square of the exact separation, or -1 beyond rmax. Decided in f32 when that is safe:
+// the f32 estimate of r bins / rmax is within 3.3e-7 of it relatively (separations rounded to
+// f32, a fused sum of squares, a square root, one product), so a pair farther than `margin` bins
+// from a bin edge, or clearly beyond rmax (r2 above lim2f), is binned without f64 arithmetic,
+// which runs at a small fraction of the f32 rate on this GPU; the rest takes the f64 definition.
+template <int D>
+__device__ __forceinline__ int rdf_bin(const int64_t* d, uint32_t bins, double scale, float scalef, float lim2f, float margin) {
+    float r2f = 0.0f;
+#pragma unroll
+    for (int a = 0; a < D; a++) {
+        const float x = __fmul_rn(__ll2float_rn(d[a]), 1.0f / 4294967296.0f);
+        r2f = __fmaf_rn(x, x, r2f);
+    }
+    if (r2f > lim2f) return -1;
+    const float rf = __fmul_rn(__fsqrt_rn(r2f), scalef);
+    const float fl = floorf(rf), fr = rf - fl;
+    if (fr > margin && fr < 1.0f - margin && rf < (float)bins - margin) return (int)fl;
+    return rdf_bin_exact<D>(d, bins, scale);
+}
+
 } // namespace gbmd

@@ -436,6 +436,25 @@ class BatchEngine:
         _abi.check(self._lib.gbmd_batch_read_system(self._h, k, _ptr(pos, C.c_int64), _ptr(vel, C.c_int32), _ptr(sp, C.c_uint32)))
         return (State if self.D == 2 else State3)(pos, vel, sp)
 
+    def read_all(self):
+        """Every system's id-ordered state (one conversion for the whole batch), as a list."""
+        N = int(self.offsets[-1])
+        pos = np.empty((N, self.D), np.int64)
+        vel = np.empty((N, self.D), np.int32)
+        sp = np.empty(N, np.uint32)
+        _abi.check(self._lib.gbmd_batch_read_all(self._h, _ptr(pos, C.c_int64), _ptr(vel, C.c_int32), _ptr(sp, C.c_uint32)))
+        cls = State if self.D == 2 else State3
+        o = self.offsets
+        return [cls(pos[o[k] : o[k + 1]].copy(), vel[o[k] : o[k + 1]].copy(), sp[o[k] : o[k + 1]].copy()) for k in range(self.count)]
+
+    def observe(self, rdf_bins=0, rdf_rmax=5.0):
+        """A frame of every system (gbmd_batch_observe): a list of gbmd_frame, and the RDF counts
+        as an array of shape (systems, rdf_bins) or None."""
+        frames = (_abi.gbmd_frame * self.count)()
+        rdf = np.zeros((self.count, rdf_bins), np.uint64) if rdf_bins else None
+        _abi.check(self._lib.gbmd_batch_observe(self._h, frames, _ptr(rdf, C.c_uint64) if rdf is not None else None, rdf_bins, rdf_rmax))
+        return list(frames), rdf
+
     def stream(self):
         s = C.c_void_p()
         _abi.check(self._lib.gbmd_batch_stream(self._h, C.byref(s)))
@@ -474,12 +493,17 @@ class BatchEngine:
 class Server:
     """The serving loop (gbmd_serve_*): submit requests, poll frames."""
 
-    def __init__(self, hbm_budget_bytes, max_active=64, device=0):
+    def __init__(self, hbm_budget_bytes, max_active=64, device=0, lane_max_n=None):
+        """`lane_max_n`: requests of at most this many particles are stepped together in their
+        dimension's lane batch (None: the library's default, 65,536; 0: every request on an
+        engine of its own)."""
         self._lib = _abi.lib()
         h = C.c_void_p()
         _abi.check(self._lib.gbmd_serve_create(int(hbm_budget_bytes), max_active, device, C.byref(h)))
         self._h = h
         self._buf = (_abi.gbmd_serve_frame * 64)()
+        if lane_max_n is not None:
+            _abi.check(self._lib.gbmd_serve_set_lanes(self._h, int(lane_max_n)))
 
     def submit(self, sys, init, steps, frame_every=100, rdf_bins=200, rdf_rmax=5.0, skin=0.3):
         if getattr(sys, "bonds", None):

@@ -924,6 +924,44 @@ def test_batch_3d(O):
             assert b.read_system(k) == c.state
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_batch_frames_equal_plain_frames(O, dim):
+    """gbmd_batch_observe: every system's frame of a batch (uneven sizes, small boxes where the RDF
+    range covers the whole box included) equals a plain engine's frame of that system at the same
+    step: RDF counts exactly, kinetic and potential energy, virial, temperature and pressure to
+    1e-12 relative (the same terms summed in another order); the states stay bit-identical."""
+    from micrographia_gb300 import BatchEngine
+
+    if dim == 2:
+        sizes = [(300, 0.5), (1500, 0.8), (4000, 0.35), (700, 0.7)]
+        systems = [System(box_for(n, rho, 1.0), 0.005, Pair.lj(2.5), [1.0]).with_seed(40 + k) for k, (n, rho) in enumerate(sizes)]
+        states = [O.fluid(s, n, 1.1, 40 + k) for k, (s, (n, _)) in enumerate(zip(systems, sizes))]
+    else:
+        sizes = [(500, 0.8), (2048, 0.6), (864, 0.85)]
+        systems = [System3(cube_for(n, rho), 0.005, Pair.lj(2.5), [1.0]) for n, rho in sizes]
+        states = [O.fcc_maxwell(s, n, 0.9, 50 + k) for k, (s, (n, _)) in enumerate(zip(systems, sizes))]
+    bins, rmax = 64, 4.0
+    with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3), block_steps=50) as b:
+        for steps in (0, 137, 100):
+            b.step(steps)
+            frames, rdf = b.observe(rdf_bins=bins, rdf_rmax=rmax)
+            got = b.read_all()
+            for k, (sys_, st) in enumerate(zip(systems, states)):
+                cls = GpuEngine if dim == 2 else GpuEngine3
+                with cls(sys_, got[k], ForceMode.verlet_with_skin(sys_, st.n(), 0.3)) as g:
+                    f, r, _ = g.observe(rdf_bins=bins, rdf_rmax=rmax)
+                assert np.array_equal(rdf[k], r), (steps, k)
+                for name in ("kinetic", "potential", "virial", "temperature", "pressure"):
+                    x, y = getattr(frames[k], name), getattr(f, name)
+                    assert abs(x - y) <= 1e-12 * max(abs(y), 1.0), (steps, k, name, x, y)
+                assert frames[k].n == f.n and frames[k].volume == f.volume
+        # the batch's states still follow the oracle
+        for k, (sys_, st) in enumerate(zip(systems, states)):
+            c = O.IntEngine(sys_, st)
+            c.step(237)
+            assert got[k] == c.state, k
+
+
 # ---------------------------------------------------------------- serving
 def _drain(sv, want_last, limit_s=120.0):
     import time
@@ -941,15 +979,25 @@ def _drain(sv, want_last, limit_s=120.0):
     return frames, last
 
 
-def test_served_results_equal_solo_runs():
-    """Mixed 2D/3D requests, more than the server holds at once: each request's frames and final
-    state are bit-identical to the same request run alone."""
+@pytest.mark.parametrize("lanes", [True, False])
+def test_served_results_equal_solo_runs(O, lanes):
+    """Mixed 2D/3D requests, more than the server holds at once, served in lanes (stepped together
+    in batches that members join and leave at frame boundaries) or each on its own engine: each
+    request's final state is bit-identical to the same request run alone and to the oracle's
+    IntEngine run; its RDF counts equal the solo run's exactly and its energies and virial agree
+    to 1e-12 relative (a lane sums the same terms in another order; an engine bit for bit)."""
     from micrographia_gb300 import Server, workloads
 
-    cfg = workloads.config5(count=6, rate=1e9, base_seed=3, n_min=800, n_max=6000)
-    with Server(hbm_budget_bytes=4 << 30, max_active=3) as sv:
+    cfg = workloads.config5(count=8, rate=1e9, base_seed=3, n_min=800, n_max=6000)
+    with Server(hbm_budget_bytes=4 << 30, max_active=3, lane_max_n=None if lanes else 0) as sv:
         ids = [sv.submit(s, spec, steps=300, frame_every=100, rdf_bins=64, rdf_rmax=4.0) for _, s, spec in cfg]
         frames, last = _drain(sv, len(ids))
+        st = sv.stats()
+    if lanes:
+        assert st.lane_requests == len(ids)
+        assert st.lane_repacks >= 3  # members joined and left at frame boundaries
+    else:
+        assert st.lane_requests == 0
     by_req = {}
     for f in frames:
         by_req.setdefault(f.request, []).append(f)
@@ -963,8 +1011,54 @@ def test_served_results_equal_solo_runs():
                 solo.append((f.kinetic, f.potential, f.virial, list(rdf)))
             h = g.state_hash()
         served = [(f.frame.kinetic, f.frame.potential, f.frame.virial, list(f.rdf[:64])) for f in sorted(by_req[rid], key=lambda f: f.index)]
-        assert served == solo
+        assert len(served) == 3
+        for (k1, p1, w1, r1), (k2, p2, w2, r2) in zip(served, solo):
+            assert r1 == r2
+            if lanes:
+                for x, y in ((k1, k2), (p1, p2), (w1, w2)):
+                    assert abs(x - y) <= 1e-12 * max(abs(y), 1.0)
+            else:
+                assert (k1, p1, w1) == (k2, p2, w2)
+        assert [f.frame.step for f in sorted(by_req[rid], key=lambda f: f.index)] == [100, 200, 300]
         assert last[rid].state_hash == h
+        c = O.IntEngine(s, O.init(s, spec))
+        c.step(300)
+        assert h == c.hash()
+
+
+def test_served_lanes_and_engines_mix():
+    """Requests routed both ways at once: small ones with the lane's cadence into lanes, a large one
+    and one with another frame cadence onto engines; a request cancelled while in a lane leaves it
+    at the next frame boundary with its last frame; every other request finishes with the final
+    state of its solo run."""
+    from micrographia_gb300 import Server, workloads
+
+    cfg = workloads.config5(count=6, rate=1e9, base_seed=21, n_min=600, n_max=5000)
+    with Server(hbm_budget_bytes=4 << 30, max_active=8, lane_max_n=3000) as sv:
+        ids = []
+        for k, (_, s, spec) in enumerate(cfg):
+            every = 50 if k == 5 else 100  # (the 3D lane has taken a cadence of 100 by then)
+            ids.append(sv.submit(s, spec, steps=400, frame_every=every, rdf_bins=32, rdf_rmax=3.0))
+        sv.poll()
+        small = [rid for rid, (_, s, spec) in zip(ids, cfg) if spec.n <= 3000 and rid != ids[5]]
+        victim = small[-1]
+        sv.cancel(victim)
+        frames, last = _drain(sv, len(ids))
+        st = sv.stats()
+    assert st.lane_requests == len(small)
+    assert st.completed == len(ids)
+    by_req = {}
+    for f in frames:
+        by_req.setdefault(f.request, []).append(f)
+    assert len(by_req[ids[5]]) == 8  # its own cadence, on an engine
+    assert len(by_req[victim]) < 4
+    for rid, (_, s, spec) in zip(ids, cfg):
+        if rid == victim:
+            continue
+        cls = GpuEngine if s.DIM == 2 else GpuEngine3
+        with cls(s, None, ForceMode.verlet_with_skin(s, spec.n, 0.3), init=spec) as g:
+            g.step(400)
+            assert last[rid].state_hash == g.state_hash()
 
 
 def test_served_bath_requests_equal_the_oracle(O):
