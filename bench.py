@@ -605,9 +605,11 @@ def run_c5(args, world, rank, local, pg, requests=None, rate=None, emit=True):
     solo = [[] for _ in reqs]
     start_plain = [0.0] * len(reqs)
 
+    lane_stats = {}
+
     def serve():
         frames_lat, done, t_arr, t_prev, order = [], 0, {}, {}, {}
-        sv = Server(64 << 30, max_active=64, device=local)
+        sv = Server(64 << 30, max_active=64, device=local, lane_max_n=0 if getattr(args, "no_lanes", False) else None)
         t0 = time.perf_counter()
         pending = list(enumerate(reqs))
         total = 0
@@ -631,6 +633,8 @@ def run_c5(args, world, rank, local, pg, requests=None, rate=None, emit=True):
             if not got:
                 time.sleep(0.0002)
         makespan = time.perf_counter() - t0
+        st = sv.stats()
+        lane_stats.update(lane_requests=st.lane_requests, lane_repacks=st.lane_repacks)
         sv.close()
         return total / makespan, makespan, frames_lat
 
@@ -687,7 +691,11 @@ def run_c5(args, world, rank, local, pg, requests=None, rate=None, emit=True):
         "data": "synthetic",
         "config": {
             "workload": f"{n_req} requests (dealt out over {world} GPU(s)), Poisson arrivals at {lam}/s, 50% 2D / 50% 3D LJ, N log-uniform [1024, 2^20], rho U[0.3, 0.85], T U[0.5, 1.5], {steps} steps, T/P/RDF frame every 100 steps, 64 GB HBM budget",
-            "form": "served: continuous batching (each admitted request on its own stream, intervals overlapped)",
+            "form": "served: continuous batching (requests of N <= 65,536 stepped together per dimension in a lane batch that they join and leave at frame boundaries, larger ones each on an engine of its own; all overlapped on the device)"
+            if not getattr(args, "no_lanes", False)
+            else "served: every request on an engine of its own, intervals overlapped",
+            "lane_requests": lane_stats.get("lane_requests"),
+            "lane_repacks": lane_stats.get("lane_repacks"),
             "makespan_s": mk_serve,
             "frame_latency_p50_ms": 1e3 * _pct(lat_serve, 50),
             "frame_latency_p99_ms": 1e3 * _pct(lat_serve, 99),
@@ -718,6 +726,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sub", action="store_true", help="default line without the batched and served sub-records")
+    ap.add_argument("--no-lanes", action="store_true", help="--config c5: serve every request on an engine of its own")
     ap.add_argument("--no-drift", action="store_true", help="default line without the energy-drift run")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="atoms (default 1,048,576; smaller only for profiling)")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2", help="c2 (default): 3D N=1M; c3: 2D slab 16.7M; c4: 1024 replicas; c5: served stream")
