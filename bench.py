@@ -421,9 +421,11 @@ def run_c4(args, world, rank, local, pg, steps=None, warmup=None, emit=True):
     total = sum(st.n() for st in states)
     mode = ForceMode.verlet_with_skin(None, 0, SKIN)
 
-    # the skin autotuner times 0.3..0.7 sigma on these states (outside the timed region)
+    # the autotuner times skins 0.3..0.7 sigma, then 2 and 4 force lanes per particle, on these
+    # states (outside the timed region)
     batch = BatchEngine(systems, states, mode, block_steps=100, device=local, tune_skin=True)
     skin = batch.skin
+    force_lanes = batch.force_lanes
     mode = ForceMode.verlet_with_skin(None, 0, skin)
     bstream = torch.cuda.ExternalStream(batch.stream())
     batch.step(W)
@@ -487,7 +489,8 @@ def run_c4(args, world, rank, local, pg, steps=None, warmup=None, emit=True):
         "config": {
             "workload": f"{len(systems)} independent 2D LJ systems, N log-uniform [256, 65536] (sum {total}), rho U[0.3, 0.8], T U[0.5, 1.5], rc 2.5, dt 0.005",
             "skin": skin,
-            "skin_choice": "autotuned: fastest of 0.3..0.7 on two timed 100-step blocks per candidate; the plain forms use the same skin",
+            "force_lanes": force_lanes,
+            "skin_choice": "autotuned: fastest of 0.3..0.7 on two timed 100-step blocks per candidate, then of 1, 2 and 4 force lanes per particle at that skin; the plain forms use the same skin",
             "form": "batched: one persistent force launch per step over all systems, 100-step CUDA graphs",
             "plain_value": value_serial,
             "plain_form": "one engine per system, the systems run one after another (each synchronised before the next starts)",

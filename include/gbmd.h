@@ -136,9 +136,12 @@ typedef struct gbmd_system {
 /* gbmd_options.flags */
 #define GBMD_FLAG_WHOLE_CELLS 1u /* list builds scan whole neighbour cells (no slab sub-buckets): timing comparisons */
 #define GBMD_FLAG_NO_STEP_LOOP 2u /* small systems step through per-step graph nodes, not the persistent step loop: comparisons */
-/* batches only: gbmd_batch_create times two blocks of (at most 100) steps from the given state at
- * each skin of 0.3, 0.4, 0.5, 0.6 and 0.7 sigma and keeps the fastest; `skin` is ignored. The
- * trajectory does not depend on the skin (the lists hold exactly the pairs within the cutoff). */
+/* batches only: gbmd_batch_create's autotuner. It times two blocks of (at most 100) steps from the
+ * given state at each skin of 0.3, 0.4, 0.5, 0.6 and 0.7 sigma (the rebuild cadence) with one force
+ * lane per particle, then 2 and 4 lanes per particle (neighbours per warp) at the fastest skin, and
+ * keeps the fastest; `skin` and the force lanes asked for are ignored. The trajectory depends on
+ * neither (the lists hold exactly the pairs within the cutoff; integer kicks sum in any order).
+ * Batches take 1, 2 or 4 force lanes (GBMD_FLAG_FORCE_LANES; others: 1). */
 #define GBMD_FLAG_TUNE_SKIN 4u
 /* bits 4-7 of flags: lanes per particle of the list build (1, 2, 4 or 8; 0 chooses by size) */
 #define GBMD_FLAG_BUILD_LANES(s) ((uint32_t)(s) << 4)
@@ -434,6 +437,8 @@ int gbmd_batch_stats(gbmd_batch* b, uint64_t* launches, uint32_t* rebuilds);
 int gbmd_batch_read_ledger(gbmd_batch* b, uint32_t k, double* energy, double* impulse, uint64_t* hits);
 /* The batch's Verlet skin in sigma (the one GBMD_FLAG_TUNE_SKIN chose, or the one asked for). */
 int gbmd_batch_skin(gbmd_batch* b, double* skin);
+/* The batch's force lanes per particle (the autotuner's choice, or the one asked for). */
+int gbmd_batch_force_lanes(gbmd_batch* b, uint32_t* lanes);
 /* Per-phase device timing of a batch, as gbmd_time_phases: `steps` steps as individual launches
  * with CUDA events around the force launch and the (all-system) list rebuild. */
 int gbmd_batch_time_phases(gbmd_batch* b, uint32_t steps, double* force_ms, double* rebuild_ms, uint32_t* rebuilds);

@@ -264,6 +264,7 @@ SIGNATURES = [
     ("gbmd_batch_sync", C.c_int, [VP]),
     ("gbmd_batch_read_system", C.c_int, [VP, C.c_uint32, _I64P, _I32P, _U32P]),
     ("gbmd_batch_read_all", C.c_int, [VP, _I64P, _I32P, _U32P]),
+    ("gbmd_batch_force_lanes", C.c_int, [VP, _U32P]),
     ("gbmd_batch_set_clocks", C.c_int, [VP, _U32P]),
     ("gbmd_batch_observe_begin", C.c_int, [VP, C.c_uint32, C.c_double]),
     ("gbmd_batch_observe_end", C.c_int, [VP, P(gbmd_frame), P(C.c_uint64)]),

@@ -207,20 +207,23 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
 // Persistent fused force + leapfrog over every particle of every system: the single-system
 // engine's step (force_list_one: warp-tiled lists with periodic-image codes, 16-byte quotient
 // records, positions left unwrapped between list builds), each lane with the parameter block of
-// its own system. Warps step through the particles 32 at a time (a warp is a list tile).
-template <int D, bool MULTI, bool SIG1>
+// its own system. Warps step through the particles 32 / S at a time, S lanes per particle (each
+// takes every S-th group of the particle's list; the kicks are summed across its lanes).
+template <int D, bool MULTI, bool SIG1, int S>
 __global__ void __launch_bounds__(128, 10) k_bforce_list(uint32_t N, const Params* __restrict__ tab, const uint32_t* __restrict__ sysidx,
                                                          const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
                                                          const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                          int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
                                                          const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                          const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
+    constexpr uint32_t PER = 32u / S; // particles per warp
     const uint32_t lane = threadIdx.x & 31u, nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32u < N; w += nwarps) {
-        const uint32_t i = w * 32u + lane;
-        if (i >= N) continue;
-        if (force_list_one<D, MULTI, false, SIG1 && !MULTI, 1, false>(tab[sysidx[i]], N, i, pos_in, pos_out, qpos_in, qpos_out, vel, species,
-                                                                        nbr, nbr_count, ref_pos))
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * PER < N; w += nwarps) { // (warp-uniform)
+        const uint32_t i = w * PER + lane / S;
+        if (S == 1 && i >= N) continue;
+        const uint32_t iv = i < N ? i : N - 1; // (S > 1: every lane of the warp takes part in the sums)
+        if (force_list_one<D, MULTI, false, SIG1 && !MULTI, S, false>(tab[sysidx[iv]], N, w * 32u + lane, pos_in, pos_out, qpos_in, qpos_out,
+                                                                        vel, species, nbr, nbr_count, ref_pos))
             ctl[0] = 1;
     }
 }
@@ -341,6 +344,7 @@ struct gbmd_batch {
     uint64_t body_launches = 0, launches = 0;
     bool failed = false;
     uint64_t steps = 0;
+    uint32_t S = 1; // force lanes per particle
     // frames (gbmd_batch_observe_*): a rebuild when the trigger is set, then per-tile partial sums
     // (a tile: up to 128 slots of one system, whose slots are contiguous) and per-system RDF bins
     cudaGraphExec_t exec_prep[2] = {nullptr, nullptr};
@@ -406,15 +410,27 @@ void benqueue_rebuild(gbmd_batch* b, cudaStream_t s) {
     if (b->D == 2) b->multi ? benqueue_rebuild_t<2, true>(b, s) : benqueue_rebuild_t<2, false>(b, s);
     else b->multi ? benqueue_rebuild_t<3, true>(b, s) : benqueue_rebuild_t<3, false>(b, s);
 }
+// The force kernel variant of a batch: its dimension, species, sigma = 1 and lanes per particle.
+template <int D, bool MULTI> const void* bforce_kernel(bool sig1, uint32_t S) {
+    if (sig1 && !MULTI)
+        return S == 4 ? (const void*)k_bforce_list<D, MULTI, true, 4> : S == 2 ? (const void*)k_bforce_list<D, MULTI, true, 2>
+                                                                        : (const void*)k_bforce_list<D, MULTI, true, 1>;
+    return S == 4 ? (const void*)k_bforce_list<D, MULTI, false, 4> : S == 2 ? (const void*)k_bforce_list<D, MULTI, false, 2>
+                                                                     : (const void*)k_bforce_list<D, MULTI, false, 1>;
+}
+const void* bforce_kernel_of(int D, bool multi, bool sig1, uint32_t S) {
+    if (D == 2) return multi ? bforce_kernel<2, true>(sig1, S) : bforce_kernel<2, false>(sig1, S);
+    return multi ? bforce_kernel<3, true>(sig1, S) : bforce_kernel<3, false>(sig1, S);
+}
 template <int D, bool MULTI> void benqueue_force_t(gbmd_batch* b, cudaStream_t s) {
-    if (b->sig1)
-        k_bforce_list<D, MULTI, true><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
-                                                              (PosRec<D>*)b->pos[b->cur ^ 1], b->qpos[b->cur], b->qpos[b->cur ^ 1], b->vel,
-                                                              b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
-    else
-        k_bforce_list<D, MULTI, false><<<b->grid, 128, 0, s>>>(b->N, b->tab, b->sysidx, (const PosRec<D>*)b->pos[b->cur],
-                                                               (PosRec<D>*)b->pos[b->cur ^ 1], b->qpos[b->cur], b->qpos[b->cur ^ 1], b->vel,
-                                                               b->species, b->nbr, b->nbr_count, (const PosRec<D>*)b->ref_pos, b->ctl);
+    const PosRec<D>* pin = (const PosRec<D>*)b->pos[b->cur];
+    PosRec<D>* pout = (PosRec<D>*)b->pos[b->cur ^ 1];
+    const uint4* qin = b->qpos[b->cur];
+    uint4* qout = b->qpos[b->cur ^ 1];
+    const PosRec<D>* ref = (const PosRec<D>*)b->ref_pos;
+    void* args[] = {(void*)&b->N, (void*)&b->tab, (void*)&b->sysidx, (void*)&pin, (void*)&pout, (void*)&qin, (void*)&qout, (void*)&b->vel,
+                    (void*)&b->species, (void*)&b->nbr, (void*)&b->nbr_count, (void*)&ref, (void*)&b->ctl};
+    cudaLaunchKernel(bforce_kernel<D, MULTI>(b->sig1, b->S), dim3(b->grid), dim3(128), args, 0, s);
     note_launch();
     b->cur ^= 1;
     if (b->bath) {
@@ -626,10 +642,31 @@ extern "C" int gbmd_batch_create(const gbmd_system* systems, uint32_t count, con
 
 namespace {
 
-// The skin autotuner: a trial batch per candidate skin, from the caller's state, timed with
-// CUDA events over its second block of steps (the first captures the graphs and warms up).
-// A candidate whose lists overflow a fixed capacity, or that does not fit in memory, drops out.
-// Sets o.skin to the fastest and clears the flag.
+// One autotuner trial: a batch with options t from the caller's state, timed with CUDA events
+// over its second block of steps (the first captures the graphs and warms up).
+int time_trial(const gbmd_system* systems, uint32_t count, const uint32_t* offsets, const int64_t* pos, const int32_t* vel,
+               const uint32_t* species, const gbmd_options& t, float* ms) {
+    gbmd_batch* tb = nullptr;
+    int r = gbmd_batch_create(systems, count, offsets, pos, vel, species, &t, &tb);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (r == GBMD_OK) r = gbmd_batch_step(tb, t.block_steps);
+    if (r == GBMD_OK) r = gbmd_batch_sync(tb);
+    if (r == GBMD_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) r = fail(GBMD_E_CUDA, "cudaEventCreate");
+    if (r == GBMD_OK && cudaEventRecord(e0, tb->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventRecord");
+    if (r == GBMD_OK) r = gbmd_batch_step(tb, t.block_steps);
+    if (r == GBMD_OK && cudaEventRecord(e1, tb->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventRecord");
+    if (r == GBMD_OK) r = gbmd_batch_sync(tb);
+    if (r == GBMD_OK && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventElapsedTime");
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (tb) gbmd_batch_destroy(tb);
+    return r;
+}
+
+// The autotuner: the rebuild cadence (the skin, one trial per candidate with one force lane per
+// particle), then the neighbours per warp (1, 2 or 4 lanes per particle at that skin). A
+// candidate whose lists overflow a fixed capacity, or that does not fit in memory, drops out.
+// Sets o.skin and o's force lanes to the fastest and clears the flag.
 int tune_skin(const gbmd_system* systems, uint32_t count, const uint32_t* offsets, const int64_t* pos, const int32_t* vel,
               const uint32_t* species, gbmd_options& o) {
     static const double cand[] = {0.3, 0.4, 0.5, 0.6, 0.7};
@@ -640,23 +677,11 @@ int tune_skin(const gbmd_system* systems, uint32_t count, const uint32_t* offset
     float best_ms = 0.0f;
     int last = GBMD_OK;
     std::string last_msg;
+    t.flags = (o.flags & ~(31u << 8)) | GBMD_FLAG_FORCE_LANES(1);
     for (double sk : cand) {
         t.skin = sk;
-        gbmd_batch* tb = nullptr;
-        int r = gbmd_batch_create(systems, count, offsets, pos, vel, species, &t, &tb);
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
         float ms = 0.0f;
-        if (r == GBMD_OK) r = gbmd_batch_step(tb, t.block_steps);
-        if (r == GBMD_OK) r = gbmd_batch_sync(tb);
-        if (r == GBMD_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) r = fail(GBMD_E_CUDA, "cudaEventCreate");
-        if (r == GBMD_OK && cudaEventRecord(e0, tb->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventRecord");
-        if (r == GBMD_OK) r = gbmd_batch_step(tb, t.block_steps);
-        if (r == GBMD_OK && cudaEventRecord(e1, tb->st) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventRecord");
-        if (r == GBMD_OK) r = gbmd_batch_sync(tb);
-        if (r == GBMD_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(GBMD_E_CUDA, "cudaEventElapsedTime");
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
-        if (tb) gbmd_batch_destroy(tb);
+        int r = time_trial(systems, count, offsets, pos, vel, species, t, &ms);
         if (r == GBMD_OK && (best == 0.0 || ms < best_ms)) best = sk, best_ms = ms;
         if (r != GBMD_OK) {
             if (r != GBMD_E_OVERFLOW && r != GBMD_E_NOMEM) return r;
@@ -665,7 +690,18 @@ int tune_skin(const gbmd_system* systems, uint32_t count, const uint32_t* offset
         }
     }
     if (best == 0.0) return fail(last, "skin tuning: no candidate ran (" + last_msg + ")");
+    // then the force lanes per particle (neighbours per warp) at that skin
+    uint32_t best_s = 1;
+    for (uint32_t S : {2u, 4u}) {
+        t.skin = best;
+        t.flags = (o.flags & ~(31u << 8)) | GBMD_FLAG_FORCE_LANES(S);
+        float ms = 0.0f;
+        int r = time_trial(systems, count, offsets, pos, vel, species, t, &ms);
+        if (r == GBMD_OK && ms < best_ms) best_s = S, best_ms = ms;
+        if (r != GBMD_OK && r != GBMD_E_OVERFLOW && r != GBMD_E_NOMEM) return r;
+    }
     o.skin = best;
+    o.flags = (o.flags & ~(31u << 8)) | GBMD_FLAG_FORCE_LANES(best_s);
     return GBMD_OK;
 }
 
@@ -743,15 +779,13 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
     b->sig1 = !b->multi;
     for (uint32_t k = 0; k < count; k++)
         for (uint32_t q = 0; q < b->P[k].ns * b->P[k].ns; q++) b->sig1 = b->sig1 && b->P[k].pc[q].sigma2s == 0x1p56f;
+    // lanes per particle of the force step (1, 2 or 4; the autotuner's or the caller's choice)
+    {
+        const uint32_t fl = (o.flags >> 8) & 31u;
+        b->S = fl == 2u || fl == 4u ? fl : 1u;
+    }
     // the persistent grid: as many blocks as stay resident for the variant that will run
-    if (D == 2)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<2, true, false>
-                                                                     : (b->sig1 ? k_bforce_list<2, false, true> : k_bforce_list<2, false, false>),
-                                                      128, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->multi ? k_bforce_list<3, true, false>
-                                                                     : (b->sig1 ? k_bforce_list<3, false, true> : k_bforce_list<3, false, false>),
-                                                      128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bforce_kernel_of((int)D, b->multi, b->sig1, b->S), 128, 0);
     b->grid = std::max<uint32_t>(1, std::min<uint32_t>(nblocks(b->N, 128), (uint32_t)std::max(dev_sms, 1) * (uint32_t)std::max(occ, 1)));
     if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
     if (r == GBMD_OK && cudaStreamCreateWithFlags(&b->st_body, cudaStreamNonBlocking) != cudaSuccess) r = fail(GBMD_E_CUDA, "stream");
@@ -1079,6 +1113,12 @@ int gbmd_batch_read_ledger(gbmd_batch* b, uint32_t k, double* energy, double* im
 int gbmd_batch_skin(gbmd_batch* b, double* skin) {
     if (!b || !skin) return fail(GBMD_E_INVALID, "null argument");
     *skin = b->skin;
+    return GBMD_OK;
+}
+
+int gbmd_batch_force_lanes(gbmd_batch* b, uint32_t* lanes) {
+    if (!b || !lanes) return fail(GBMD_E_INVALID, "null argument");
+    *lanes = b->S;
     return GBMD_OK;
 }
 

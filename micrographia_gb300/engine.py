@@ -372,9 +372,10 @@ def make_init(recipe, n, t, seed, jitter=0.1, rho_liquid=0.7, rho_vapour=0.05, s
 class BatchEngine:
     """Many independent periodic systems stepped together (gbmd_batch_*)."""
 
-    def __init__(self, systems, states, mode=None, threads=0, block_steps=0, device=0, tune_skin=False):
-        """With `tune_skin`, the Verlet skin is the fastest of 0.3..0.7 sigma on a short timed
-        run from these states (mode's skin ignored); the trajectory is the same for any skin."""
+    def __init__(self, systems, states, mode=None, threads=0, block_steps=0, device=0, tune_skin=False, force_lanes=0):
+        """With `tune_skin`, the autotuner picks the Verlet skin (the fastest of 0.3..0.7 sigma)
+        and then the force lanes per particle (1, 2 or 4) on short timed runs from these states
+        (mode's skin and `force_lanes` ignored); the trajectory is the same for any choice."""
         self._lib = _abi.lib()
         if len(systems) != len(states) or not systems:
             raise ValueError("one state per system")
@@ -392,7 +393,7 @@ class BatchEngine:
         vel = np.ascontiguousarray(np.concatenate([st.vel for st in states]))
         sp = np.ascontiguousarray(np.concatenate([st.species for st in states]))
         opts = _options(mode or ForceMode.verlet_for(systems[0], 0), threads, block_steps, device=device,
-                        flags=_abi.FLAG_TUNE_SKIN if tune_skin else 0)
+                        flags=(_abi.FLAG_TUNE_SKIN if tune_skin else 0) | (int(force_lanes) << 8))
         h = C.c_void_p()
         _abi.check(
             self._lib.gbmd_batch_create(
@@ -415,6 +416,12 @@ class BatchEngine:
     def skin(self):
         v = C.c_double()
         _abi.check(self._lib.gbmd_batch_skin(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def force_lanes(self):
+        v = C.c_uint32()
+        _abi.check(self._lib.gbmd_batch_force_lanes(self._h, C.byref(v)))
         return v.value
 
     def read_ledger(self, k):

@@ -890,8 +890,9 @@ def test_batch_replicas_match_their_plain_runs(O):
 
 
 def test_batch_skin_tuner_keeps_the_trajectory(O):
-    """The skin autotuner picks one of its candidates from timed trial runs on the given states;
-    the replicas still equal their plain oracle runs bit for bit at that skin."""
+    """The autotuner picks a skin and a force-lane split from timed trial runs on the given states;
+    the replicas still equal their plain oracle runs bit for bit at that choice, and at every
+    force-lane split asked for."""
     from micrographia_gb300 import BatchEngine, workloads
 
     cfg = workloads.config4(count=6, base_seed=9, n_min=512, n_max=4096)
@@ -899,6 +900,7 @@ def test_batch_skin_tuner_keeps_the_trajectory(O):
     states = [O.init(s, spec) for s, spec in cfg]
     with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3), tune_skin=True) as b:
         assert b.skin in (0.3, 0.4, 0.5, 0.6, 0.7)
+        assert b.force_lanes in (1, 2, 4)
         b.step(120)
         for k, (sys_, st) in enumerate(zip(systems, states)):
             c = O.IntEngine(sys_, st)
@@ -906,6 +908,15 @@ def test_batch_skin_tuner_keeps_the_trajectory(O):
             assert b.read_system(k) == c.state, k
     with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.45)) as b:
         assert b.skin == 0.45
+        assert b.force_lanes == 1
+    for lanes in (2, 4):  # every force-lane split gives the same trajectory
+        with BatchEngine(systems, states, ForceMode.verlet_with_skin(None, 0, 0.3), force_lanes=lanes) as b:
+            assert b.force_lanes == lanes
+            b.step(120)
+            for k, (sys_, st) in enumerate(zip(systems, states)):
+                c = O.IntEngine(sys_, st)
+                c.step(120)
+                assert b.read_system(k) == c.state, (lanes, k)
 
 
 def test_batch_3d(O):
