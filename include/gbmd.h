@@ -172,7 +172,7 @@ typedef struct gbmd_engine gbmd_engine;
 typedef struct gbmd_frame {
     uint64_t step;        /* net steps taken */
     double kinetic;       /* on-step kinetic energy (IntEngine::energy, int_engine.rs:433-446) */
-    double potential;     /* pair potential energy */
+    double potential;     /* potential energy: pairs, bonds, soft walls, the piston, and gravity's -m g . x */
     double virial;        /* sum over pairs of r . F = sum fr r^2 (mc/src/gibbs.rs:58-66) */
     double temperature;   /* 2 KE / (dim (N - 1)) */
     double pressure;      /* rho T + virial / (dim V) */

@@ -514,10 +514,10 @@ __global__ void __launch_bounds__(128) k_bframe(const Params* __restrict__ tab, 
                                                 const uint32_t* __restrict__ species, const uint32_t* __restrict__ nbr,
                                                 const uint32_t* __restrict__ nbr_count, const int32_t* __restrict__ vel,
                                                 double* __restrict__ partial) {
-    __shared__ double sh[3][4];
+    __shared__ double sh[4][4];
     const uint4 t = tiles[blockIdx.x];
     const Params& P = tab[t.x];
-    double pe = 0.0, w = 0.0, ke = 0.0;
+    double pe = 0.0, w = 0.0, ke = 0.0, gpe = 0.0;
     if (threadIdx.x < t.z) {
         const uint32_t i = t.y + threadIdx.x;
         int64_t xi[3];
@@ -539,24 +539,29 @@ __global__ void __launch_bounds__(128) k_bframe(const Params* __restrict__ tab, 
         }
         pe = 0.5 * pe32.value();
         w = 0.5 * w32.value();
+        // the kinetic energy as k_kicks sums it (m (v + next)^2, scaled on the host), and gravity's
+        // potential in its own partial
         const double m_i = P.masses[si];
+        const bool counted = !(D == 3 && ((P.pinned >> si) & 1u));
         for (int a = 0; a < D; a++) {
             const int32_t v0 = vel[D * i + a];
             const int32_t next = wadd(wadd(v0, k[a]), P.gravity[a]);
-            const double vh = __dmul_rn(0.5, __dadd_rn(__ddiv_rn(__dmul_rn((double)v0, 1.0 / 4294967296.0), P.dt),
-                                                       __ddiv_rn(__dmul_rn((double)next, 1.0 / 4294967296.0), P.dt)));
-            ke += 0.5 * m_i * vh * vh;
+            const double sv = (double)((int64_t)v0 + (int64_t)next);
+            if (counted) {
+                ke = __fma_rn(__dmul_rn(m_i, sv), sv, ke);
+                if (P.grav_f[a] != 0.0) gpe = __fma_rn(-__dmul_rn(m_i, P.grav_f[a]), to_f64(wrap(xi[a], P.box[a])), gpe);
+            }
         }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double vals[3] = {pe, w, ke};
-    for (int q = 0; q < 3; q++) {
+    double vals[4] = {pe, w, ke, gpe};
+    for (int q = 0; q < 4; q++) {
         double x = vals[q];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if (lane == 0) sh[q][warp] = x;
     }
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < 4) {
         double s = 0.0;
         for (int wq = 0; wq < (int)(blockDim.x >> 5); wq++) s += sh[threadIdx.x][wq];
         partial[4 * blockIdx.x + threadIdx.x] = s;
@@ -996,12 +1001,17 @@ int gbmd_batch_observe_end(gbmd_batch* b, gbmd_frame* frames, uint64_t* rdf) {
     GBMD_TRY(gbmd_batch_sync(b)); // returns at once when the frame's work is done
     if (rdf && b->obs_nbins) std::memcpy(rdf, b->bins_h, (size_t)b->obs_nbins * b->K * 8);
     if (!frames) return GBMD_OK;
-    std::vector<double> pe(b->K, 0.0), w(b->K, 0.0), ke(b->K, 0.0);
+    std::vector<double> pe(b->K, 0.0), w(b->K, 0.0), ke(b->K, 0.0), gpe(b->K, 0.0);
     for (size_t t = 0; t < b->tiles_h.size(); t++) { // per system, in tile order
         const uint32_t k = b->tiles_h[t].x;
         pe[k] += b->part_h[4 * t];
         w[k] += b->part_h[4 * t + 1];
         ke[k] += b->part_h[4 * t + 2];
+        gpe[k] += b->part_h[4 * t + 3];
+    }
+    for (uint32_t k = 0; k < b->K; k++) { // as gbmd_observe_end
+        ke[k] *= 0x1p-64 / (8.0 * b->sys[k].dt * b->sys[k].dt);
+        pe[k] += gpe[k];
     }
     bool finite = true;
     for (uint32_t k = 0; k < b->K; k++) { // as gbmd_observe_end

@@ -243,6 +243,7 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
     }
     for (uint32_t a = 0; a < 3; a++) {
         double g = a < s.dim ? s.gravity[a] : 0.0;
+        P.grav_f[a] = g;
         double v = std::round(g * s.dt * s.dt * 4294967296.0); // System::gravity_kick
         P.gravity[a] = v != v ? 0 : (v >= 2147483647.0 ? INT32_MAX : (v <= -2147483648.0 ? INT32_MIN : (int32_t)v));
     }
@@ -2338,12 +2339,15 @@ extern "C" int gbmd_observe_end(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf
     if (frame) {
         const uint32_t n = e->n, nb = e->obs_nb;
         const double* part = e->obs_part_h;
-        double pe = 0.0, w = 0.0, ke = 0.0;
+        double pe = 0.0, w = 0.0, ke = 0.0, gpe = 0.0;
         for (uint32_t b = 0; b < nb; b++) {
             pe += part[4 * b];
             w += part[4 * b + 1];
             ke += part[4 * b + 2];
+            gpe += part[4 * b + 3];
         }
+        ke *= 0x1p-64 / (8.0 * e->sys.dt * e->sys.dt); // sum of m (v + next)^2 -> 0.5 m vh^2 (k_kicks)
+        pe += gpe;
         double vol = 1.0;
         for (int a = 0; a < e->D; a++) vol *= to_f64h(e->sys.box_len[a]);
         double dof = 0.5 * e->D * std::max((double)n - 1.0, 1.0);

@@ -1413,9 +1413,9 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
                                                const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
                                                int32_t* __restrict__ vel, int32_t* __restrict__ kicks, double* __restrict__ partial,
                                                int reverse) {
-    __shared__ double sh[3][4];
+    __shared__ double sh[4][4];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    double pe = 0.0, w = 0.0, ke = 0.0;
+    double pe = 0.0, w = 0.0, ke = 0.0, gpe = 0.0;
     F32Sum pe32, w32; // the f32 chain's pair terms, summed without f64 arithmetic
     if (i < P.n) {
         int64_t xi[3];
@@ -1493,14 +1493,25 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
                 if (reverse) atomicAdd(&P.piston->force_fixed, (unsigned long long)sat_i64_f64(round_away(__dmul_rn((double)f, 65536.0))));
             }
         }
-        double m = P.masses[si];
+        // IntEngine::energy / IntEngine3::energy (int_engine.rs:433-446, int_engine3.rs:222-239):
+        // the on-step velocity 0.5 (velocity(v) + velocity(next)), velocity(v) = v UNIT / dt, so
+        // 0.5 m vh^2 = m (v + next)^2 UNIT^2 / (8 dt^2); the sum of m (v + next)^2 (exact integers
+        // squared in f64) is scaled by UNIT^2 / (8 dt^2) on the host (no f64 division per particle:
+        // f64 runs at a small fraction of the f32 rate on this GPU). 3D leaves pinned species out.
+        // The gravity potential -m g . x goes to its own partial (the kicks' potential has none).
+        const double m = P.masses[si];
+        const bool counted = !(D == 3 && ((P.pinned >> si) & 1u));
         for (int a = 0; a < D; a++) {
             int32_t v0 = vel[D * i + a];
             int32_t next = wadd(wadd(v0, k[a]), P.gravity[a]);
-            // 0.5 (velocity(v) + velocity(next)), velocity(v) = v UNIT / dt (system.rs:423-425)
-            double vh = __dmul_rn(0.5, __dadd_rn(__ddiv_rn(__dmul_rn((double)v0, 1.0 / 4294967296.0), P.dt),
-                                                 __ddiv_rn(__dmul_rn((double)next, 1.0 / 4294967296.0), P.dt)));
-            ke += 0.5 * m * vh * vh;
+            const double sv = (double)((int64_t)v0 + (int64_t)next);
+            if (counted) {
+                ke = __fma_rn(__dmul_rn(m, sv), sv, ke);
+                if (P.grav_f[a] != 0.0) {
+                    const int64_t xa = ((P.periodic >> a) & 1u) ? wrap(xi[a], P.box[a]) : xi[a];
+                    gpe = __fma_rn(-__dmul_rn(m, P.grav_f[a]), to_f64(xa), gpe);
+                }
+            }
             if (kicks) kicks[D * i + a] = k[a];
             if (reverse) {
                 bool pinned = (P.pinned >> si) & 1u;
@@ -1510,14 +1521,14 @@ __global__ void __launch_bounds__(128) k_kicks(Params P, const PosRec<D>* __rest
     }
     if (!partial) return;
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double vals[3] = {pe, w, ke};
-    for (int q = 0; q < 3; q++) {
+    double vals[4] = {pe, w, ke, gpe};
+    for (int q = 0; q < 4; q++) {
         double x = vals[q];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if (lane == 0) sh[q][warp] = x;
     }
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < 4) {
         double s = 0.0;
         for (int wq = 0; wq < (int)(blockDim.x >> 5); wq++) s += sh[threadIdx.x][wq];
         partial[4 * blockIdx.x + threadIdx.x] = s;
@@ -1717,16 +1728,19 @@ template <int D> __device__ __forceinline__ int rdf_bin_exact(const int64_t* d, 
 
 // The RDF bin of a pair at minimum-image separation d: k = floor(sqrt(r2) bins / rmax) with r2
 // the f64 square of the exact separation, or -1 beyond rmax. Decided in f32 when that is safe:
-// the f32 estimate of r bins / rmax is within 3.3e-7 of it relatively (separations rounded to
-// f32, a fused sum of squares, a square root, one product), so a pair farther than `margin` bins
-// from a bin edge, or clearly beyond rmax (r2 above lim2f), is binned without f64 arithmetic,
-// which runs at a small fraction of the f32 rate on this GPU; the rest takes the f64 definition.
+// the f32 estimate of r bins / rmax is within 3.3e-7 of it relatively plus 2^-24 sqrt(D) sigma
+// (separations truncated to 2^-24 sigma and rounded to f32 through a 32-bit conversion, a fused
+// sum of squares, a square root, one product), so a pair farther than `margin` bins from a bin
+// edge, or clearly beyond rmax (r2 above lim2f), is binned without f64 arithmetic, which runs at
+// a small fraction of the f32 rate on this GPU (so does a 64-bit integer conversion); the rest
+// takes the f64 definition, as does any pair 64 sigma or more apart on an axis.
 template <int D>
 __device__ __forceinline__ int rdf_bin(const int64_t* d, uint32_t bins, double scale, float scalef, float lim2f, float margin) {
     float r2f = 0.0f;
 #pragma unroll
     for (int a = 0; a < D; a++) {
-        const float x = __fmul_rn(__ll2float_rn(d[a]), 1.0f / 4294967296.0f);
+        if (d[a] >= ((int64_t)1 << 38) || d[a] <= -((int64_t)1 << 38)) return rdf_bin_exact<D>(d, bins, scale);
+        const float x = __fmul_rn(__int2float_rn((int32_t)(d[a] >> 8)), 0x1p-24f);
         r2f = __fmaf_rn(x, x, r2f);
     }
     if (r2f > lim2f) return -1;

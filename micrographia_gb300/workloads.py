@@ -98,7 +98,8 @@ def _profile_run(name):
       more by direct launches of the loop (k_force_loop; a profiler cannot see kernels inside the
       graphs' conditional nodes);
     - batch: the first 256 of the 1024 batched 2D replicas, 300 steps in 100-step graphs, then 50
-      steps by direct launches (k_bforce_list, k_bbuild_list);
+      steps by direct launches (k_bforce_list, k_bbuild_list), then two frames of every system
+      (k_bframe, and a 200-bin RDF to r = 5, k_brdf);
     - scenario2d: a 2D Kremer-Grest melt of 32,768 chains of 32 beads (N = 2^20, rho 0.3, WCA
       beads, FENE bonds) between a soft floor and a hard roof, under a piston driven down at
       0.1 sigma/tau from the roof; 50 steps in graphs, then 30 by direct launches (k_force_list,
@@ -129,6 +130,9 @@ def _profile_run(name):
             b.wait()
             f, r, nr = b.time_phases(50)
             print(f"batch: {sum(st.n() for st in states)} particles, force {f:.3f} ms, rebuild {r:.3f} ms ({nr} in 50 steps)")
+            for _ in range(2):
+                frames, rdf = b.observe(rdf_bins=200, rdf_rmax=5.0)
+            print(f"batch frames: T[0] {frames[0].temperature:.4f}, RDF counts {int(rdf.sum())}")
     elif name == "scenario2d":
         import numpy as np
 
