@@ -351,6 +351,8 @@ struct gbmd_batch {
     uint64_t exec_prep_launches[2] = {0, 0};
     std::vector<uint4> tiles_h; // (system, first slot, slots, 0)
     uint4* tiles = nullptr;
+    uint32_t* reach = nullptr; // per system: the RDF walk's cell reach per axis (8 bits each)
+    double reach_for = -1.0;   // the rmax `reach` was computed for
     double* part = nullptr;
     unsigned long long* obs_bins = nullptr;
     size_t obs_bins_cap = 0;
@@ -381,7 +383,7 @@ void bfree(gbmd_batch* b) {
     void* ptrs[] = {b->tab, b->pos[0], b->pos[1], b->pos_scr, b->ref_pos, b->vel, b->vel_scr, b->species, b->species_scr, b->ids, b->ids_scr,
                     b->sysidx, b->sysidx_scr, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->scan_tmp, b->start, b->nbr,
                     b->nbr_count, b->ctl, b->staging, b->staging_v, b->staging_s, b->qpos[0], b->qpos[1], b->relf, b->ledger,
-                    b->tiles, b->part, b->obs_bins};
+                    b->tiles, b->part, b->obs_bins, b->reach};
     if (b->st)
         for (void* p : ptrs)
             if (p) cudaFreeAsync(p, b->st);
@@ -572,16 +574,19 @@ __global__ void __launch_bounds__(128) k_bframe(const Params* __restrict__ tab, 
 // the exact minimum-image separation, rdf_bin) over the cells of the last list build. Every
 // particle is within half the skin of the position it was binned at, so a pair within rmax has
 // binned positions within rmax + skin: its cells differ by at most R = ceil((rmax + skin) nc / L)
-// per axis (every cell of an axis with 2R + 1 >= nc, each once). Each block counts one tile of
-// one system into shared memory and adds its counts to that system's bins.
+// per axis (every cell of an axis with 2R + 1 >= nc, each once); `reach` holds R per system (8
+// bits per axis). Each block counts one tile of one system; each warp into its own shared
+// histogram when `bins` allows (`per_warp`), then the block adds its counts to that system's bins.
 template <int D>
 __global__ void __launch_bounds__(128) k_brdf(const Params* __restrict__ tab, const uint4* __restrict__ tiles, const PosRec<D>* __restrict__ pos,
-                                              const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start, uint32_t bins, double rmax,
-                                              double skin, double scale, float scalef, float lim2f, float margin,
-                                              unsigned long long* __restrict__ out) {
+                                              const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
+                                              const uint32_t* __restrict__ reach, uint32_t bins, bool per_warp, double scale, float scalef,
+                                              float lim2f, float margin, unsigned long long* __restrict__ out) {
     extern __shared__ uint32_t h[];
-    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0;
+    const uint32_t nh = per_warp ? (blockDim.x >> 5) : 1u;
+    for (uint32_t b = threadIdx.x; b < bins * nh; b += blockDim.x) h[b] = 0;
     __syncthreads();
+    uint32_t* hw = per_warp ? h + (threadIdx.x >> 5) * bins : h;
     const uint4 t = tiles[blockIdx.x];
     const Params& P = tab[t.x];
     if (threadIdx.x < t.z) {
@@ -592,10 +597,10 @@ __global__ void __launch_bounds__(128) k_brdf(const Params* __restrict__ tab, co
         for (int a = 0; a < D; a++) xi[a] = wrap(xi[a], P.box[a]);
         uint32_t c[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, span[3] = {1, 1, 1};
         cell_coords(P, keys[i] - P.cell_base, c);
+        const uint32_t rr = reach[t.x];
 #pragma unroll
         for (int a = 0; a < D; a++) {
-            const uint32_t nc = P.nc[a];
-            const uint32_t R = (uint32_t)ceil(__dmul_rn(rmax + skin, (double)nc) / P.box_f[a] + 1e-9);
+            const uint32_t nc = P.nc[a], R = (rr >> (8 * a)) & 255u;
             if (2 * R + 1 >= nc) {
                 lo[a] = 0;
                 span[a] = nc;
@@ -618,15 +623,18 @@ __global__ void __launch_bounds__(128) k_brdf(const Params* __restrict__ tab, co
 #pragma unroll
                         for (int a = 0; a < D; a++) d[a] = min_image(wrap(xj[a], P.box[a]) - xi[a], P.box[a], P.half[a]);
                         const int k = rdf_bin<D>(d, bins, scale, scalef, lim2f, margin);
-                        if (k >= 0) atomicAdd(&h[k], 1u);
+                        if (k >= 0) atomicAdd(&hw[k], 1u);
                     }
                 }
             }
         }
     }
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x)
-        if (h[b]) atomicAdd(out + (size_t)t.x * bins + b, (unsigned long long)h[b]);
+    for (uint32_t b = threadIdx.x; b < bins; b += blockDim.x) {
+        uint32_t v = 0;
+        for (uint32_t q = 0; q < nh; q++) v += h[q * bins + b];
+        if (v) atomicAdd(out + (size_t)t.x * bins + b, (unsigned long long)v);
+    }
 }
 
 int bcheck(gbmd_batch* b) {
@@ -828,6 +836,7 @@ int gbmd_batch_create(const gbmd_system* systems, uint32_t count, const uint32_t
             b->tiles_h.push_back(make_uint4(k, s0, std::min<uint32_t>(128u, offsets[k + 1] - s0), 0u));
     step(balloc(&b->tiles, b->tiles_h.size(), b->st));
     step(balloc(&b->part, 4 * b->tiles_h.size(), b->st));
+    step(balloc(&b->reach, count, b->st));
     if (r == GBMD_OK)
         cudaMemcpyAsync(b->tiles, b->tiles_h.data(), b->tiles_h.size() * sizeof(uint4), cudaMemcpyHostToDevice, b->st);
     if (r == GBMD_OK) cudaMemsetAsync(b->ledger, 0, 16 * (size_t)count, b->st);
@@ -975,16 +984,29 @@ int gbmd_batch_observe_begin(gbmd_batch* b, uint32_t rdf_bins, double rdf_rmax) 
             if (!b->bins_h) return fail(GBMD_E_NOMEM, "pinned RDF buffer");
         }
         GBMD_CUDA_TRY(cudaMemsetAsync(b->obs_bins, 0, nbins * 8, b->st));
+        if (b->reach_for != rdf_rmax) { // R = ceil((rmax + skin) nc / L) per system and axis
+            std::vector<uint32_t> rr(b->K, 0);
+            for (uint32_t k = 0; k < b->K; k++)
+                for (int a = 0; a < b->D; a++) {
+                    const double L = (double)b->sys[k].box_len[a] * (1.0 / 4294967296.0);
+                    const double R = std::ceil((rdf_rmax + b->skin) * b->P[k].nc[a] / L + 1e-9);
+                    rr[k] |= (uint32_t)std::min(R, 255.0) << (8 * a);
+                }
+            GBMD_CUDA_TRY(cudaMemcpyAsync(b->reach, rr.data(), b->K * 4, cudaMemcpyHostToDevice, b->st));
+            GBMD_CUDA_TRY(cudaStreamSynchronize(b->st)); // (rr leaves scope)
+            b->reach_for = rdf_rmax;
+        }
         const double scale = (double)rdf_bins / rdf_rmax;
         const float scalef = (float)scale, lim2f = (float)(rdf_rmax * rdf_rmax * (1.0 + 1e-4));
         const float margin = (float)(1e-6 * rdf_bins + 1e-5);
-        const size_t shm = (size_t)rdf_bins * 4;
+        const bool per_warp = rdf_bins <= 2048; // four histograms of 8 KB at most
+        const size_t shm = (size_t)rdf_bins * 4 * (per_warp ? 4 : 1);
         if (b->D == 2)
-            k_brdf<2><<<nt, 128, shm, b->st>>>(b->tab, b->tiles, (const PosRec<2>*)b->pos[b->cur], b->keys[b->sorted], b->start, rdf_bins,
-                                               rdf_rmax, b->skin, scale, scalef, lim2f, margin, b->obs_bins);
+            k_brdf<2><<<nt, 128, shm, b->st>>>(b->tab, b->tiles, (const PosRec<2>*)b->pos[b->cur], b->keys[b->sorted], b->start, b->reach,
+                                               rdf_bins, per_warp, scale, scalef, lim2f, margin, b->obs_bins);
         else
-            k_brdf<3><<<nt, 128, shm, b->st>>>(b->tab, b->tiles, (const PosRec<3>*)b->pos[b->cur], b->keys[b->sorted], b->start, rdf_bins,
-                                               rdf_rmax, b->skin, scale, scalef, lim2f, margin, b->obs_bins);
+            k_brdf<3><<<nt, 128, shm, b->st>>>(b->tab, b->tiles, (const PosRec<3>*)b->pos[b->cur], b->keys[b->sorted], b->start, b->reach,
+                                               rdf_bins, per_warp, scale, scalef, lim2f, margin, b->obs_bins);
         note_launch();
         GBMD_CUDA_TRY(cudaMemcpyAsync(b->bins_h, b->obs_bins, nbins * 8, cudaMemcpyDeviceToHost, b->st));
     }
