@@ -568,6 +568,10 @@ void enqueue_rebuild(gbmd_engine* e, cudaStream_t s, bool full = false) {
         if (e->multi) enqueue_rebuild_t<3, true>(e, s, full);
         else enqueue_rebuild_t<3, false>(e, s, full);
     }
+    if (e->verlet && e->P.bonds && e->D == 2) { // the slots of the ids, which only a list build moves
+        k_slot_of<<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->ids, e->slot_of);
+        note_launch();
+    }
 }
 __global__ void k_set_trigger(uint32_t* ctl) { ctl[0] = 1; }
 
@@ -579,6 +583,13 @@ static uint32_t force_lanes(const gbmd_engine* e) {
     const uint32_t o = (e->opt.flags >> 8) & 31u;
     if (o == 1 || o == 2 || o == 4 || o == 8 || o == 16) return o;
     return e->n < FORCE_SPLIT8_BELOW ? 8u : (e->n < FORCE_SPLIT4_BELOW ? 4u : (e->n < FORCE_SPLIT2_BELOW ? 2u : 1u));
+}
+// Whether the force kernel takes the scenario's bonds, walls, piston and bath in its own epilogue
+// (Verlet lists, f32 pairs, one lane per particle): one pass over the state instead of up to three.
+static bool scenario_epilogue(const gbmd_engine* e) {
+    if (!e->verlet || e->half || e->P.int_mode) return false;
+    if (!(e->P.walls || (e->P.bonds && e->D == 2) || e->P.bath)) return false;
+    return e->multi || force_lanes(e) == 1;
 }
 template <int D, bool MULTI, bool INT> void enqueue_force_a(gbmd_engine* e, cudaStream_t s, uint32_t threads) {
     if constexpr (D == 3 && !MULTI && !INT) {
@@ -622,6 +633,15 @@ template <int D, bool MULTI, bool INT> void enqueue_force_a(gbmd_engine* e, cuda
                 else GBMD_SPLIT(2, false);
             }
 #undef GBMD_SPLIT
+        } else if (!INT && scenario_epilogue(e)) {
+            if (sig1 && !MULTI)
+                k_force_list<D, MULTI, false, true, 1, true><<<blocks_for(e->n, threads), threads, 0, s>>>(
+                    e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur], e->qpos[e->cur ^ 1], e->vel,
+                    e->species, e->nbr, e->nbr_count, (const Rec<D>*)e->ref_pos, e->ctl);
+            else
+                k_force_list<D, MULTI, false, false, 1, true><<<blocks_for(e->n, threads), threads, 0, s>>>(
+                    e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur], e->qpos[e->cur ^ 1], e->vel,
+                    e->species, e->nbr, e->nbr_count, (const Rec<D>*)e->ref_pos, e->ctl);
         } else if (sig1)
             k_force_list<D, MULTI, INT, true><<<blocks_for(e->n, threads), threads, 0, s>>>(
                 e->P, (const Rec<D>*)e->pos[e->cur], (Rec<D>*)e->pos[e->cur ^ 1], e->qpos[e->cur], e->qpos[e->cur ^ 1], e->vel,
@@ -655,6 +675,15 @@ void enqueue_force(gbmd_engine* e, cudaStream_t s) {
     } else {
         if (e->multi) enqueue_force_t<3, true>(e, s, threads);
         else enqueue_force_t<3, false>(e, s, threads);
+    }
+    const bool epi = scenario_epilogue(e);
+    if (epi) { // the force kernel took the bonds, walls, piston and bath: the piston moves, the clock
+        if (e->P.walls || e->P.bath) {
+            if (e->P.piston_drive) k_piston_tick<<<1, 1, 0, s>>>(e->P, e->ctl);
+            else k_clock_tick<<<1, 1, 0, s>>>(e->ctl);
+            note_launch();
+        }
+        return;
     }
     if (e->P.bonds && e->D == 2) { // the bonds' kicks from the step's start positions
         const uint32_t nb = blocks_for(e->n, 256);
@@ -1262,6 +1291,9 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     }
     GBMD_TRY(allocT(e, &e->ctl, 16));
     GBMD_TRY(allocT(e, &e->ledger, 3 * GBMD_LEDGER_SLOTS));
+    e->P.ids_list = e->ids; // (the force kernel's scenario epilogue)
+    e->P.ledger = e->ledger;
+    e->P.clock_word = e->ctl + CTL_CLOCK;
     GBMD_CUDA_TRY(cudaMemsetAsync(e->ledger, 0, 24 * GBMD_LEDGER_SLOTS, e->st));
     if (e->opt.arith == GBMD_ARITH_INT) {
         std::vector<int32_t> tab;
@@ -1619,7 +1651,11 @@ int gbmd_set_bonds(gbmd_engine* e, const gbmd_bond_type* types, uint32_t ntypes,
         GBMD_TRY(allocT(e, &e->bond_tab, (size_t)e->n * 8));
         GBMD_TRY(allocT(e, &e->slot_of, (size_t)e->n));
     }
-    if (nbonds) GBMD_CUDA_TRY(cudaMemcpyAsync(e->bond_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, e->st));
+    if (nbonds) {
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->bond_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, e->st));
+        k_slot_of<<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->ids, e->slot_of); // (list builds keep it after)
+        note_launch();
+    }
     e->P.bonds = nbonds ? 1u : 0u;
     e->P.bond_tab = e->bond_tab;
     e->P.slot_of = e->slot_of;
@@ -1729,6 +1765,9 @@ int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
     std::memcpy(e->P.bond_r0, old.bond_r0, sizeof(old.bond_r0));
     e->P.bond_tab = old.bond_tab;
     e->P.slot_of = old.slot_of;
+    e->P.ids_list = old.ids_list;
+    e->P.ledger = old.ledger;
+    e->P.clock_word = old.clock_word;
     e->P.piston_drive = old.piston_drive; // and the piston
     e->P.piston_mass = old.piston_mass;
     e->P.piston_ext = old.piston_ext;

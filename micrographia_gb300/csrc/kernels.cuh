@@ -676,6 +676,15 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     ids_o[i] = ids_s[i];
 }
 
+// The scenario epilogue's pieces (defined with the bonds and walls below).
+template <int D>
+__device__ __forceinline__ float bond_kicks(const Params& P, uint32_t id, const int64_t* xi, const PosRec<D>* pos, float c, int32_t* k);
+template <int D>
+__device__ __forceinline__ void wall_kicks(const Params& P, const int64_t* xo, float c, int32_t* k, unsigned long long* ledger);
+template <int D>
+__device__ __forceinline__ bool wall_post(const Params& P, uint32_t si, uint32_t id, uint32_t clock, int64_t* x, int32_t* v,
+                                          unsigned long long* ledger, bool wrap_periodic);
+
 // The hot kernel: LJ pair kicks over the Verlet list fused with the integer leapfrog and the
 // rebuild trigger. Reads positions from pos_in and writes the moved ones to pos_out (the engine
 // ping-pongs the two), so every kick sees positions of the same time step.
@@ -688,7 +697,7 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
 // are read through L2 only (the persistent step loop, where other blocks rewrite them).
 // `n`: the particles of the arrays (a batch passes all of its systems' particles, with P the
 // parameter block of the system that lane t's particle belongs to).
-template <int D, bool MULTI, bool INT, bool SIG1, int S, bool CG>
+template <int D, bool MULTI, bool INT, bool SIG1, int S, bool CG, bool EXT = false>
 __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t n, uint32_t t, const PosRec<D>* __restrict__ pos_in,
                                                PosRec<D>* __restrict__ pos_out, const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                int32_t* __restrict__ vel, const uint32_t* __restrict__ species, const uint32_t* __restrict__ nbr,
@@ -789,10 +798,22 @@ __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t n, uint
             for (int a = 0; a < D; a++) k[a] = wadd(k[a], __shfl_xor_sync(0xffffffffu, k[a], o));
         if (!valid || seg != 0) return false;
     }
+    if constexpr (EXT) {
+        // the scenario's other kicks, from the step's start positions, as IntEngine::forces sums
+        // them with the pair kicks (int_engine.rs:185-246): bonds (partners read from pos_in
+        // through the id -> slot map of the last list build), soft walls and the piston
+        const float c = __fmul_rn(cs, 1.0f / 268435456.0f);
+        if (D == 2 && P.bonds) bond_kicks<D>(P, P.ids_list[i], xi, pos_in, c, k);
+        if (P.walls) wall_kicks<D>(P, xi, c, k, P.ledger);
+    }
     int32_t v[3];
 #pragma unroll
     for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
     leapfrog<D, Params, false>(P, si, k, v, xi);
+    if constexpr (EXT) {
+        // then the bath, the membrane, the walls' mirrors and collisions, the piston's mirror
+        if (P.walls || P.bath) wall_post<D>(P, si, P.ids_list[i], *P.clock_word, xi, v, P.ledger, false);
+    }
 #pragma unroll
     for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
     store_pos<D>(pos_out, i, xi, si);
@@ -802,14 +823,17 @@ __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t n, uint
     return moved_half_skin<D>(P, xr, xi);
 }
 
-template <int D, bool MULTI, bool INT = false, bool SIG1 = false, int S = 1>
+// EXT: the scenario variant (bonds, walls, the piston, the bath), which takes those in its own
+// epilogue instead of separate passes over the state.
+template <int D, bool MULTI, bool INT = false, bool SIG1 = false, int S = 1, bool EXT = false>
 __global__ void __launch_bounds__(128, 10) k_force_list(Params P, const PosRec<D>* __restrict__ pos_in, PosRec<D>* __restrict__ pos_out,
                                                     const uint4* __restrict__ qpos_in, uint4* __restrict__ qpos_out,
                                                     int32_t* __restrict__ vel, const uint32_t* __restrict__ species,
                                                     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
                                                     const PosRec<D>* __restrict__ ref_pos, uint32_t* __restrict__ ctl) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (force_list_one<D, MULTI, INT, SIG1, S, false>(P, P.n, t, pos_in, pos_out, qpos_in, qpos_out, vel, species, nbr, nbr_count, ref_pos))
+    if (force_list_one<D, MULTI, INT, SIG1, S, false, EXT>(P, P.n, t, pos_in, pos_out, qpos_in, qpos_out, vel, species, nbr, nbr_count,
+                                                           ref_pos))
         ctl[0] = 1;
 }
 
@@ -1165,63 +1189,44 @@ __device__ __forceinline__ void thermal_velocity(const Params& P, uint32_t id, u
         vt[1] = __dmul_rn(rad, dev_sin(a));
     }
 }
-// After the force step on a system with walls: the step left v' = v + k + g and x' = x + v' with
-// k the pair kicks only. This pass adds each soft wall's kick (from the position at the step's
-// start, x' - v', exact in integers) to v' and x', applies the heat bath if there is one (in the
-// reference's order: after the kick, before the move), then mirrors a particle that left the box
-// on a walled axis back in and collides it with that wall: hard and soft walls reverse the normal
-// component, a thermal wall draws a new velocity on (id, step clock).
-template <int D, bool LIST>
-__global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict__ qpos, int32_t* __restrict__ vel,
-                        const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids, const PosRec<D>* __restrict__ ref_pos,
-                        uint32_t* __restrict__ ctl, unsigned long long* __restrict__ ledger) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const uint32_t si = species[i], id = ids[i], clock = ctl[CTL_CLOCK];
-    int64_t x[3] = {0, 0, 0};
-    load_particle<D, false>(pos, nullptr, i, x);
-    int32_t v[3] = {0, 0, 0};
-#pragma unroll
-    for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
-    bool changed = false;
-    const float c = __fmul_rn(P.kick_cs[si], 1.0f / 268435456.0f); // kick_coeff in f32
+// The walls' kicks on one particle at its step-start position xo (int_engine.rs:203-246): each
+// soft wall's WCA kick (its impulse booked on the ledger) and the piston's (its force summed in
+// 2^-16 eps/sigma units), added to k like the pair kicks; c is the particle's kick coefficient.
+template <int D>
+__device__ __forceinline__ void wall_kicks(const Params& P, const int64_t* xo, float c, int32_t* k, unsigned long long* ledger) {
 #pragma unroll
     for (int a = 0; a < D; a++) {
         if ((P.periodic >> a) & 1u) continue;
-        const int64_t xo = x[a] - (int64_t)v[a];
-        int32_t kw_sum = 0;
 #pragma unroll
         for (int side = 0; side < 2; side++) {
             if (P.wall_kind[a][side] != GBMD_WALL_SOFT) continue;
             float f, s6;
-            if (!soft_wall_force(side == 0 ? xo : P.box[a] - xo, f, s6)) continue;
+            if (!soft_wall_force(side == 0 ? xo[a] : P.box[a] - xo[a], f, s6)) continue;
             const int32_t kw = rni_f32(__fmul_rn(f, c));
-            kw_sum = wadd(kw_sum, side == 0 ? kw : (int32_t)(0u - (uint32_t)kw));
+            k[a] = wadd(k[a], side == 0 ? kw : (int32_t)(0u - (uint32_t)kw));
             atomicAdd(ledger + 3 * (2 * a + side) + 2, ledger_fixed(__dmul_rn((double)f, P.dt)));
         }
-        if (kw_sum) { // (the move uses the wrapped velocity sum, as the reference's x += v does)
-            v[a] = wadd(v[a], kw_sum);
-            x[a] = xo + (int64_t)v[a];
-            changed = true;
-        }
     }
-    int64_t pw = 0;
     if (D == 2 && P.piston_drive) {
-        // the piston (int_engine.rs:230-246): a soft wall at the step's piston height pushing
-        // down; the gas's force on it summed in 2^-16 eps/sigma units (walls.rs:140-141)
-        pw = P.piston->w;
-        const int64_t yo = x[1] - (int64_t)v[1];
+        // the piston (int_engine.rs:230-246): a soft wall at the step's piston height pushing down
         float f, s6;
-        if (soft_wall_force(pw - yo, f, s6)) {
-            const int32_t kw = rni_f32(__fmul_rn(f, c));
+        if (soft_wall_force(P.piston->w - xo[1], f, s6)) {
+            k[1] = wadd(k[1], (int32_t)(0u - (uint32_t)rni_f32(__fmul_rn(f, c))));
             atomicAdd(&P.piston->force_fixed, (unsigned long long)sat_i64_f64(round_away(__dmul_rn((double)f, 65536.0))));
-            if (kw) {
-                v[1] = wadd(v[1], (int32_t)(0u - (uint32_t)kw));
-                x[1] = yo + (int64_t)v[1];
-                changed = true;
-            }
         }
     }
+}
+
+// One particle's step after its move (x = x_start + v, v = v_start + k + g with every kick): the
+// heat bath if there is one, a blocked species' membrane crossing, a wall on a walled axis that
+// it passed (mirrored back in and collided: hard and soft walls reverse the normal component, a
+// thermal wall draws a new velocity on (id, step clock)), a crossing into another compartment,
+// and the piston (int_engine.rs:265-336, int_engine3.rs:147-179, in that order). Returns whether
+// it changed x or v. Periodic axes are wrapped only with `wrap_periodic` (cell lists).
+template <int D>
+__device__ __forceinline__ bool wall_post(const Params& P, uint32_t si, uint32_t id, uint32_t clock, int64_t* x, int32_t* v,
+                                          unsigned long long* ledger, bool wrap_periodic) {
+    bool changed = false;
     if (P.bath && bath_one<D>(P, si, id, clock, x, v, ledger + 3 * GBMD_LEDGER_BATH)) changed = true;
     const double m = P.masses[si];
     int64_t old[3];
@@ -1248,7 +1253,7 @@ __global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict
 #pragma unroll
     for (int a = 0; a < D; a++) {
         if ((P.periodic >> a) & 1u) {
-            if (!LIST) x[a] = wrap(x[a], P.box[a]);
+            if (wrap_periodic) x[a] = wrap(x[a], P.box[a]);
             continue;
         }
         int side = -1;
@@ -1307,11 +1312,48 @@ __global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict
         atomicAdd(l + 1, 1ull);
         atomicAdd(l + 2, ledger_fixed(imp));
     }
-    if (D == 2 && P.piston_drive && x[1] >= pw) { // mirrored below the piston (int_engine.rs:333-336)
-        x[1] = 2 * pw - 1 - x[1];
-        v[1] = (int32_t)(0u - (uint32_t)v[1]);
-        changed = true;
+    if (D == 2 && P.piston_drive) {
+        const int64_t pw = P.piston->w; // mirrored below the piston (int_engine.rs:333-336)
+        if (x[1] >= pw) {
+            x[1] = 2 * pw - 1 - x[1];
+            v[1] = (int32_t)(0u - (uint32_t)v[1]);
+            changed = true;
+        }
     }
+    return changed;
+}
+
+// After the force step on a system with walls (when the force kernel did not take them itself):
+// the step left v' = v + k + g and x' = x + v' with k the pair (and bond) kicks. This pass adds
+// the walls' kicks, from the position at the step's start x' - v' (exact in integers), to v' and
+// moves the particle from there again (the reference's x += v with the wrapped velocity sum), then
+// runs wall_post.
+template <int D, bool LIST>
+__global__ void k_walls(Params P, PosRec<D>* __restrict__ pos, uint4* __restrict__ qpos, int32_t* __restrict__ vel,
+                        const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids, const PosRec<D>* __restrict__ ref_pos,
+                        uint32_t* __restrict__ ctl, unsigned long long* __restrict__ ledger) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const uint32_t si = species[i], id = ids[i], clock = ctl[CTL_CLOCK];
+    int64_t x[3] = {0, 0, 0};
+    load_particle<D, false>(pos, nullptr, i, x);
+    int32_t v[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; a++) v[a] = vel[D * i + a];
+    int64_t xo[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; a++) xo[a] = x[a] - (int64_t)v[a];
+    int32_t kw[3] = {0, 0, 0};
+    wall_kicks<D>(P, xo, __fmul_rn(P.kick_cs[si], 1.0f / 268435456.0f), kw, ledger); // kick_coeff in f32
+    bool changed = false;
+#pragma unroll
+    for (int a = 0; a < D; a++)
+        if (kw[a]) {
+            v[a] = wadd(v[a], kw[a]);
+            x[a] = xo[a] + (int64_t)v[a];
+            changed = true;
+        }
+    if (wall_post<D>(P, si, id, clock, x, v, ledger, !LIST)) changed = true;
     if (!changed) return;
 #pragma unroll
     for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
