@@ -49,6 +49,32 @@ double oracle_uniform(uint64_t seed, uint32_t stream, uint32_t i) { return unifo
 double oracle_normal(uint64_t seed, uint32_t stream, uint32_t i) { return normal(seed, stream, i); }
 double oracle_log(double x) { return fdlibm::log(x); }
 double oracle_cos(double x) { return fdlibm::cos(x); }
+double oracle_sin(double x) { return fdlibm::sin(x); }
+// How often the device's fdlibm ln, cos and sin and the platform libm (what the reference's f64
+// methods call on a native build) round differently on the heat bath's own arguments, and how
+// often that changes a redrawn velocity: n 2D draws as walls::andersen makes them (u1 = 1 - U,
+// a = 2 pi U', Threefry on (k, 0) under the key of `seed`), each component rounded by
+// to_step_displacement at kT/m = t_over_m and step dt. out: ln, cos, sin disagreements, then the
+// draws whose x or y step displacement differs.
+void oracle_libm_compare(uint64_t n, uint64_t seed, double t_over_m, double dt, uint64_t* out) {
+    const std::array<uint32_t, 2> key{(uint32_t)seed, (uint32_t)(seed >> 32) ^ STREAM_THERMO};
+    uint64_t c[4] = {0, 0, 0, 0};
+    const double sd = std::sqrt(t_over_m);
+    auto step = [&](double u) { return sat_i32(std::round(u * dt * 4294967296.0)); };
+    for (uint64_t k = 0; k < n; k++) {
+        const auto r = threefry2x32({(uint32_t)k, (uint32_t)(k >> 32)}, key);
+        const auto r2 = threefry2x32({(uint32_t)k, (uint32_t)(k >> 32)}, {key[0], key[1] ^ 1u});
+        const double u1 = 1.0 - to_unit_f64({r[1], 0}), a = TAU * to_unit_f64({r2[0], 0});
+        const double lf = fdlibm::log(u1), lg = std::log(u1);
+        const double cf = fdlibm::cos(a), cg = std::cos(a), sf = fdlibm::sin(a), sg = std::sin(a);
+        c[0] += lf != lg;
+        c[1] += cf != cg;
+        c[2] += sf != sg;
+        const double rf = std::sqrt(-2.0 * lf), rg = std::sqrt(-2.0 * lg);
+        c[3] += step(sd * rf * cf) != step(sd * rg * cg) || step(sd * rf * sf) != step(sd * rg * sg);
+    }
+    for (int q = 0; q < 4; q++) out[q] = c[q];
+}
 int64_t oracle_to_fixed(double x) { return to_fixed(x); }
 
 // ---- System helpers

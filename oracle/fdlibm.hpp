@@ -242,5 +242,25 @@ inline double cos(double x) {
     }
 }
 
+// s_sin.c: the same reduction, the kernels rotated by a quarter turn.
+inline double sin(double x) {
+    uint32_t ix = (uint32_t)(bits(x) >> 32) & 0x7fffffffu;
+    if (ix <= 0x3fe921fbu) {    /* |x| ~< pi/4 */
+        if (ix < 0x3e500000u) { /* |x| < 2^-26 */
+            if ((int)x == 0) return x;
+        }
+        return k_sin(x, 0.0, 0);
+    }
+    if (ix >= 0x7ff00000u) return x - x;
+    double y0, y1;
+    int n = rem_pio2(x, &y0, &y1);
+    switch (n & 3) {
+        case 0: return k_sin(y0, y1, 1);
+        case 1: return k_cos(y0, y1);
+        case 2: return -k_sin(y0, y1, 1);
+        default: return -k_cos(y0, y1);
+    }
+}
+
 } // namespace fdlibm
 } // namespace oracle

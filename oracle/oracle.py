@@ -32,6 +32,8 @@ _SIGS = [
     ("oracle_normal", C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32]),
     ("oracle_log", C.c_double, [C.c_double]),
     ("oracle_cos", C.c_double, [C.c_double]),
+    ("oracle_sin", C.c_double, [C.c_double]),
+    ("oracle_libm_compare", None, [C.c_uint64, C.c_uint64, C.c_double, C.c_double, U64P]),
     ("oracle_to_fixed", C.c_int64, [C.c_double]),
     ("oracle_box_for", None, [C.c_uint64, C.c_double, C.c_double, I64P]),
     ("oracle_cube_for", None, [C.c_uint64, C.c_double, I64P]),
@@ -141,6 +143,14 @@ def init(sys, spec):
     if lib().oracle_init(C.byref(c), C.byref(spec), _p(pos, C.c_int64), _p(vel, C.c_int32), _p(sp, C.c_uint32)) != 0:
         raise ValueError("oracle init failed")
     return (State if D == 2 else State3)(pos, vel, sp)
+
+
+def libm_compare(n, seed, t_over_m, dt):
+    """oracle_libm_compare: over n of the heat bath's 2D draws, how often fdlibm's ln, cos and sin
+    and the platform libm's round differently, and how many draws' step displacements differ."""
+    out = (C.c_uint64 * 4)()
+    lib().oracle_libm_compare(n, seed, t_over_m, dt, out)
+    return list(out)
 
 
 def fluid(sys, n, t, seed):
