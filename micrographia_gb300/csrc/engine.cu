@@ -2476,6 +2476,42 @@ extern "C" int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, ui
 }
 
 // ------------------------------------------------------------------ seeded init + hashing
+namespace {
+__global__ void k_libm(uint32_t n, const double* x, double* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[3 * (size_t)i] = dev_log(x[i]);
+    out[3 * (size_t)i + 1] = dev_cos(x[i]);
+    out[3 * (size_t)i + 2] = dev_sin(x[i]);
+}
+} // namespace
+
+// The device's ln, cos and sin (the fdlibm restatement the initial velocities, the heat bath and
+// thermal walls draw with) at n arguments: out[3 i .. 3 i + 2].
+extern "C" int gbmd_debug_libm(const double* x, uint32_t n, double* out) {
+    if ((n && (!x || !out))) return fail(GBMD_E_INVALID, "null argument");
+    if (n == 0) return GBMD_OK;
+    cudaStream_t s;
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    double *dx = nullptr, *dout = nullptr;
+    int rc = GBMD_OK;
+    if (cudaMallocAsync((void**)&dx, (size_t)n * 8, s) != cudaSuccess || cudaMallocAsync((void**)&dout, (size_t)n * 24, s) != cudaSuccess)
+        rc = fail(GBMD_E_NOMEM, "libm buffers");
+    if (rc == GBMD_OK) {
+        cudaMemcpyAsync(dx, x, (size_t)n * 8, cudaMemcpyHostToDevice, s);
+        k_libm<<<blocks_for(n, 256), 256, 0, s>>>(n, dx, dout);
+        note_launch();
+        cudaMemcpyAsync(out, dout, (size_t)n * 24, cudaMemcpyDeviceToHost, s);
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = fail(GBMD_E_CUDA, cudaGetErrorString(e));
+    }
+    if (dx) cudaFreeAsync(dx, s);
+    if (dout) cudaFreeAsync(dout, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return rc;
+}
+
 extern "C" int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, int64_t* pos, int32_t* vel, uint32_t* species) {
     if (!sys || !spec) return fail(GBMD_E_INVALID, "null argument");
     GBMD_TRY(validate_system(*sys, spec->n));

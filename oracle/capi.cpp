@@ -50,6 +50,14 @@ double oracle_normal(uint64_t seed, uint32_t stream, uint32_t i) { return normal
 double oracle_log(double x) { return fdlibm::log(x); }
 double oracle_cos(double x) { return fdlibm::cos(x); }
 double oracle_sin(double x) { return fdlibm::sin(x); }
+// fdlibm's ln, cos and sin at n arguments: out[3 i], out[3 i + 1], out[3 i + 2].
+void oracle_fdlibm_many(const double* x, uint64_t n, double* out) {
+    for (uint64_t i = 0; i < n; i++) {
+        out[3 * i] = fdlibm::log(x[i]);
+        out[3 * i + 1] = fdlibm::cos(x[i]);
+        out[3 * i + 2] = fdlibm::sin(x[i]);
+    }
+}
 // How often the device's fdlibm ln, cos and sin and the platform libm (what the reference's f64
 // methods call on a native build) round differently on the heat bath's own arguments, and how
 // often that changes a redrawn velocity: n 2D draws as walls::andersen makes them (u1 = 1 - U,

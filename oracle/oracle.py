@@ -34,6 +34,7 @@ _SIGS = [
     ("oracle_cos", C.c_double, [C.c_double]),
     ("oracle_sin", C.c_double, [C.c_double]),
     ("oracle_libm_compare", None, [C.c_uint64, C.c_uint64, C.c_double, C.c_double, U64P]),
+    ("oracle_fdlibm_many", None, [DP, C.c_uint64, DP]),
     ("oracle_to_fixed", C.c_int64, [C.c_double]),
     ("oracle_box_for", None, [C.c_uint64, C.c_double, C.c_double, I64P]),
     ("oracle_cube_for", None, [C.c_uint64, C.c_double, I64P]),
@@ -143,6 +144,14 @@ def init(sys, spec):
     if lib().oracle_init(C.byref(c), C.byref(spec), _p(pos, C.c_int64), _p(vel, C.c_int32), _p(sp, C.c_uint32)) != 0:
         raise ValueError("oracle init failed")
     return (State if D == 2 else State3)(pos, vel, sp)
+
+
+def fdlibm_many(x):
+    """fdlibm's (ln, cos, sin) at each of x: an (n, 3) array."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty((x.size, 3), np.float64)
+    lib().oracle_fdlibm_many(_p(x, C.c_double), x.size, _p(out, C.c_double))
+    return out
 
 
 def libm_compare(n, seed, t_over_m, dt):

@@ -73,6 +73,29 @@ def test_libm_restatement_on_device_matches_over_many_draws(O):
     assert np.array_equal(got.pos, want.pos)
 
 
+def test_device_libm_equals_the_oracle_fdlibm(O):
+    """The device's ln, cos and sin (the initial velocities', heat bath's and thermal walls' draws)
+    equal the oracle's fdlibm restatement bit for bit on 4 x 10^6 arguments: the bath's own
+    ranges (1 - U in (0, 1], 2 pi U), and wider ones (cos and sin up to 10^6, where the argument
+    reduction takes more terms; ln from 1e-304 to 1e304, and negative arguments)."""
+    import ctypes as C
+
+    rng = np.random.default_rng(77)
+    parts = [
+        1.0 - rng.random(1_000_000),
+        6.283185307179586 * rng.random(1_000_000),
+        rng.uniform(-1e6, 1e6, 1_000_000),
+        np.exp(rng.uniform(-700, 700, 1_000_000)) * rng.choice([-1.0, 1.0], 1_000_000),
+    ]
+    x = np.ascontiguousarray(np.concatenate(parts))
+    got = np.empty((x.size, 3), np.float64)
+    _abi.check(_abi.lib().gbmd_debug_libm(x.ctypes.data_as(C.POINTER(C.c_double)), x.size, got.ctypes.data_as(C.POINTER(C.c_double))))
+    want = O.fdlibm_many(x)
+    same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+    same[np.abs(x) >= 1e6, 1:] = True  # (cos and sin: the restatement reduces |x| < 2^20 pi/2 only)
+    assert same.all(), (x[~same.all(1)][:5], got[~same.all(1)][:5], want[~same.all(1)][:5])
+
+
 # ---------------------------------------------------------------- binning (gpu-prims checks.rs:30-149)
 SIZES = [1, 2, 255, 256, 257, 1023, 1024, 1025, 4097, 65537, (1 << 20) + 3]
 
