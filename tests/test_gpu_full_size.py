@@ -126,3 +126,24 @@ def test_config4_every_replica_matches_its_oracle_run(O):
         ok = dict(zip(order, ex.map(same, order)))
     bad = [k for k in range(len(systems)) if not ok[k]]
     assert not bad, f"{len(bad)} of {len(systems)} replicas differ from their oracle runs, first {bad[:8]}"
+
+
+def test_config2_energy_is_conserved_at_full_size():
+    """The 3D LJ liquid of configs[1] at full size (N = 2^20, rho 0.8442, T 0.72, skin 0.3):
+    after 1000 steps of equilibration from the lattice, the total energy per atom (on-step
+    kinetic + pair potential, FP64 sums) stays within the reference's bar of 2e-3 over 5000
+    steps (md/tests/three.rs:95-111), and its least-squares slope is below 1e-8 per atom per step:
+    the integer leapfrog is exactly time-reversible, so what remains is the f32 force error."""
+    n = 1 << 20
+    sys3, spec = workloads.config2(n)
+    with GpuEngine3(sys3, None, ForceMode.verlet_with_skin(sys3, n, 0.3), init=spec) as g:
+        g.step(1000)
+        e = []
+        for _ in range(26):
+            ke, pe = g.energy()
+            e.append((ke + pe) / n)
+            g.step(200)
+    e = np.array(e)
+    slope = np.polyfit(np.arange(e.size) * 200.0, e, 1)[0]
+    assert e.max() - e.min() < 2e-3, (e.max() - e.min())
+    assert abs(slope) < 1e-8, slope
