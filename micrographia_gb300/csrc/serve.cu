@@ -194,8 +194,20 @@ int lane_collect(gbmd_server* sv, Lane& L) {
 }
 
 // Start a lane's next interval, re-packing its batch first when members left or are joining.
+// The new batch is built before the old one is freed: if building fails, the lane keeps its
+// batch, members and joiners, and the next poll tries again.
 int lane_start(gbmd_server* sv, Lane& L) {
     if (L.running) return GBMD_OK;
+    for (size_t q = 0; q < L.joining.size();) { // cancelled before it started: it leaves with no frame
+        if (L.joining[q].cancelled) {
+            sv->completed++;
+            sv->in_use -= L.joining[q].bytes;
+            L.joining.erase(L.joining.begin() + (long)q);
+            L.changed = true;
+        } else {
+            q++;
+        }
+    }
     if (!L.joining.empty() || L.changed) {
         // the states to carry over: the survivors, picked out of the old batch by their index in
         // it; then the joiners. Each keeps its own step clock (its steps so far).
@@ -204,6 +216,7 @@ int lane_start(gbmd_server* sv, Lane& L) {
         std::vector<int64_t> pos;
         std::vector<int32_t> vel;
         std::vector<uint32_t> sp;
+        std::vector<Request> next;
         if (L.b && !L.members.empty()) {
             std::vector<size_t> first(L.old_n.size() + 1, 0);
             for (size_t k = 0; k < L.old_n.size(); k++) first[k + 1] = first[k] + L.old_n[k];
@@ -219,14 +232,10 @@ int lane_start(gbmd_server* sv, Lane& L) {
                 vel.insert(vel.end(), av.begin() + o * L.dim, av.begin() + (o + n) * L.dim);
                 sp.insert(sp.end(), as.begin() + o, as.begin() + o + n);
                 offsets.push_back(offsets.back() + (uint32_t)n);
+                next.push_back(L.members[q]);
             }
         }
         for (auto& r : L.joining) { // the joiners' seeded initial states
-            if (r.cancelled) { // cancelled before it started: it leaves with no frame
-                sv->completed++;
-                sv->in_use -= r.bytes;
-                continue;
-            }
             const size_t n = r.spec.init.n, o = pos.size() / L.dim;
             pos.resize((o + n) * L.dim);
             vel.resize((o + n) * L.dim);
@@ -234,23 +243,37 @@ int lane_start(gbmd_server* sv, Lane& L) {
             GBMD_TRY(gbmd_init_state(&r.spec.sys, &r.spec.init, pos.data() + o * L.dim, vel.data() + o * L.dim, sp.data() + o));
             systems.push_back(r.spec.sys);
             offsets.push_back(offsets.back() + (uint32_t)n);
-            L.members.push_back(r);
+            next.push_back(r);
         }
+        gbmd_batch* nb = nullptr;
+        if (!next.empty()) {
+            gbmd_options o{};
+            o.mode = GBMD_MODE_VERLET;
+            o.skin = L.skin;
+            o.device = sv->device;
+            o.block_steps = L.frame_every;
+            GBMD_TRY(gbmd_batch_create(systems.data(), (uint32_t)systems.size(), offsets.data(), pos.data(), vel.data(), sp.data(), &o, &nb));
+            std::vector<uint32_t> clocks;
+            for (auto& m : next) clocks.push_back((uint32_t)m.steps_done);
+            const int rc = gbmd_batch_set_clocks(nb, clocks.data());
+            if (rc != GBMD_OK) {
+                gbmd_batch_destroy(nb);
+                return rc;
+            }
+            sv->lane_repacks++;
+        }
+        if (L.b) gbmd_batch_destroy(L.b);
+        L.b = nb;
+        L.members.swap(next);
         L.joining.clear();
         L.changed = false;
-        if (L.b) gbmd_batch_destroy(L.b);
-        L.b = nullptr;
-        if (L.members.empty()) return GBMD_OK;
-        gbmd_options o{};
-        o.mode = GBMD_MODE_VERLET;
-        o.skin = L.skin;
-        o.device = sv->device;
-        o.block_steps = L.frame_every;
-        GBMD_TRY(gbmd_batch_create(systems.data(), (uint32_t)systems.size(), offsets.data(), pos.data(), vel.data(), sp.data(), &o, &L.b));
-        std::vector<uint32_t> clocks;
-        for (auto& m : L.members) clocks.push_back((uint32_t)m.steps_done);
-        GBMD_TRY(gbmd_batch_set_clocks(L.b, clocks.data()));
-        sv->lane_repacks++;
+        // the new batch's systems are the members, in order, all kept until the next interval ends
+        L.old_n.clear();
+        L.keep.clear();
+        for (size_t q = 0; q < L.members.size(); q++) {
+            L.old_n.push_back(L.members[q].spec.init.n);
+            L.keep.push_back((uint32_t)q);
+        }
     }
     if (L.members.empty()) return GBMD_OK;
     if (!L.done) GBMD_CUDA_TRY(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
