@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(128) k_bframe(const Params* __restrict__ tab, 
 // particle is within half the skin of the position it was binned at, so a pair within rmax has
 // binned positions within rmax + skin: its cells differ by at most R = ceil((rmax + skin) nc / L)
 // per axis (every cell of an axis with 2R + 1 >= nc, each once); `reach` holds R per system (8
-// bits per axis). Each block counts one tile of one system; each warp into its own shared
+// bits per axis; 255 stands for any reach of 255 or more, and walks every cell). Each block counts one tile of one system; each warp into its own shared
 // histogram when `bins` allows (`per_warp`), then the block adds its counts to that system's bins.
 template <int D>
 __global__ void __launch_bounds__(128) k_brdf(const Params* __restrict__ tab, const uint4* __restrict__ tiles, const PosRec<D>* __restrict__ pos,
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(128) k_brdf(const Params* __restrict__ tab, co
 #pragma unroll
         for (int a = 0; a < D; a++) {
             const uint32_t nc = P.nc[a], R = (rr >> (8 * a)) & 255u;
-            if (2 * R + 1 >= nc) {
+            if (R == 255u || 2 * R + 1 >= nc) { // (255: a reach beyond 8 bits, every cell)
                 lo[a] = 0;
                 span[a] = nc;
             } else {
