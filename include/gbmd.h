@@ -332,6 +332,11 @@ int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* r
  * per step inside the loop launches and their count; GBMD_E_UNSUPPORTED when the engine does
  * not use the loop. */
 int gbmd_time_loop(gbmd_engine* e, uint32_t steps, uint32_t* taken, double* ms_per_step, uint32_t* launches);
+/* The velocity-rescale thermostat's kernels (exact kinetic energy, factor, rescale, exact zero
+ * momentum) run `reps` times as direct launches with CUDA events around each (a profiler sees
+ * them; inside the step graphs it does not): the mean milliseconds. Each run rescales the
+ * velocities, as a rescale step does. GBMD_E_INVALID without a thermostat. */
+int gbmd_time_thermostat(gbmd_engine* e, uint32_t reps, double* ms);
 
 /* ---- Introspection of the cell binning and the Verlet list (parity tests) ---- */
 

@@ -1899,6 +1899,29 @@ int gbmd_time_phases(gbmd_engine* e, uint32_t steps, double* force_ms, double* r
     return check_ctl(e);
 }
 
+int gbmd_time_thermostat(gbmd_engine* e, uint32_t reps, double* ms) {
+    if (!e || !ms) return fail(GBMD_E_INVALID, "null argument");
+    if (!e->opt.rescale_every) return fail(GBMD_E_INVALID, "the engine has no velocity-rescale thermostat");
+    GBMD_TRY(gbmd_sync(e));
+    cudaEvent_t a, b;
+    GBMD_CUDA_TRY(cudaEventCreate(&a));
+    GBMD_CUDA_TRY(cudaEventCreate(&b));
+    double total = 0.0;
+    for (uint32_t k = 0; k < reps; k++) {
+        GBMD_CUDA_TRY(cudaEventRecord(a, e->st));
+        enqueue_thermo(e, e->st);
+        GBMD_CUDA_TRY(cudaEventRecord(b, e->st));
+        GBMD_CUDA_TRY(cudaEventSynchronize(b));
+        float m = 0.0f;
+        cudaEventElapsedTime(&m, a, b);
+        total += m;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = reps ? total / reps : 0.0;
+    return check_ctl(e);
+}
+
 int gbmd_time_loop(gbmd_engine* e, uint32_t steps, uint32_t* taken, double* ms_per_step, uint32_t* launches) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
     if (!e->loop_lanes) return fail(GBMD_E_UNSUPPORTED, "this engine does not step through the persistent loop");

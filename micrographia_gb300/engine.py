@@ -276,6 +276,13 @@ class _Engine:
         _abi.check(self._lib.gbmd_time_loop(self._h, steps, C.byref(t), C.byref(ms), C.byref(n)))
         return t.value, ms.value, n.value
 
+    def time_thermostat(self, reps):
+        """The velocity-rescale thermostat's kernels run `reps` times by direct launches (each
+        rescales the velocities, as a rescale step does): the mean milliseconds."""
+        ms = C.c_double()
+        _abi.check(self._lib.gbmd_time_thermostat(self._h, reps, C.byref(ms)))
+        return ms.value
+
     def launch_count(self):
         c = C.c_uint64()
         _abi.check(self._lib.gbmd_launch_count(self._h, C.byref(c)))

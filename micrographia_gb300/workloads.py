@@ -102,8 +102,11 @@ def _profile_run(name):
       (k_bframe, and a 200-bin RDF to r = 5, k_brdf);
     - scenario2d: a 2D Kremer-Grest melt of 32,768 chains of 32 beads (N = 2^20, rho 0.3, WCA
       beads, FENE bonds) between a soft floor and a hard roof, under a piston driven down at
-      0.1 sigma/tau from the roof; 50 steps in graphs, then 30 by direct launches (k_force_list,
-      k_slot_of, k_bonds, k_walls, k_piston_tick)."""
+      0.1 sigma/tau from the roof; 50 steps in graphs, then 30 by direct launches (the force
+      kernel with its scenario epilogue, k_piston_tick, and k_slot_of with each list build);
+    - thermo2d: the liquid-vapour slab of configs[2] at a quarter of its size (N = 2^22) with its
+      velocity rescale to T = 0.45 every 10 steps, 20 steps, then the thermostat's kernels four
+      times by direct launches (k_ke_exact, k_thermo_factor, k_rescale, k_zero_apply)."""
     from .engine import BatchEngine, ForceMode, GpuEngine3, init_state
 
     if name == "frames3d":
@@ -152,8 +155,16 @@ def _profile_run(name):
             f, r, nr = e.time_phases(30)
             w, v, work = e.piston()
             print(f"scenario2d: N {n}, force pass {f:.3f} ms, rebuild {r:.3f} ms ({nr} in 30 steps), piston at {to_f64(w):.2f}")
+    elif name == "thermo2d":
+        from .engine import GpuEngine
+
+        sys2, spec = config3(1 << 22)
+        with GpuEngine(sys2, None, ForceMode.verlet_with_skin(sys2, spec.n, 0.4), init=spec, rescale_every=10, rescale_t=0.45) as e:
+            e.step(20)
+            ms = e.time_thermostat(4)
+            print(f"thermo2d: N {spec.n}, thermostat {ms:.3f} ms")
     else:
-        raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d, batch or scenario2d")
+        raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d, batch, scenario2d or thermo2d")
 
 
 if __name__ == "__main__":
