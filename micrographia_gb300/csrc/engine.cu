@@ -735,12 +735,12 @@ void enqueue_thermo(gbmd_engine* e, cudaStream_t s) {
     uint32_t nb = e->thermo_nb;
     if (e->D == 2) {
         k_ke_exact<2><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tpart);
-        k_thermo_factor<<<1, 1, 0, s>>>(T, e->tpart, e->tfac);
+        k_thermo_factor<<<1, 256, 0, s>>>(T, e->tpart, e->tfac);
         k_rescale<2><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tfac, e->vpart);
         k_zero_apply<2><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving, e->vpart, nb, e->tfac);
     } else {
         k_ke_exact<3><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tpart);
-        k_thermo_factor<<<1, 1, 0, s>>>(T, e->tpart, e->tfac);
+        k_thermo_factor<<<1, 256, 0, s>>>(T, e->tpart, e->tfac);
         k_rescale<3><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tfac, e->vpart);
         k_zero_apply<3><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving, e->vpart, nb, e->tfac);
     }

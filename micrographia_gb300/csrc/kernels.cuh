@@ -1678,12 +1678,23 @@ struct ThermoP {
 };
 // fac[0] = sqrt(t / now) with now = KE / dof, KE = sum_s 1/2 m_s S_s (UNIT / dt)^2 in f64 in
 // species order; fac[1] = 1 when now <= 0 (set_temperature then leaves the state alone).
+// One block of 256 threads: the per-block integer sums added in 128 bits (exact, so in any
+// order), then one thread's f64 arithmetic.
 static __global__ void k_thermo_factor(ThermoP T, const unsigned long long* __restrict__ part, double* __restrict__ fac) {
+    __shared__ unsigned long long lo[GBMD_MAX_SPECIES][256], hi[GBMD_MAX_SPECIES][256];
+    for (uint32_t s = 0; s < T.ns; s++) {
+        unsigned __int128 S = 0;
+        for (uint32_t b = threadIdx.x; b < T.nblocks; b += blockDim.x) S += ((unsigned __int128)part[8 * b + 2 * s + 1] << 64) | part[8 * b + 2 * s];
+        lo[s][threadIdx.x] = (unsigned long long)S;
+        hi[s][threadIdx.x] = (unsigned long long)(S >> 64);
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     double ke = 0.0;
     double u = __ddiv_rn(1.0 / 4294967296.0, T.dt);
     for (uint32_t s = 0; s < T.ns; s++) {
         unsigned __int128 S = 0;
-        for (uint32_t b = 0; b < T.nblocks; b++) S += ((unsigned __int128)part[8 * b + 2 * s + 1] << 64) | part[8 * b + 2 * s];
+        for (uint32_t k = 0; k < blockDim.x; k++) S += ((unsigned __int128)hi[s][k] << 64) | lo[s][k];
         double sum = __dadd_rn(__dmul_rn(__ull2double_rn((unsigned long long)(S >> 64)), 18446744073709551616.0),
                                __ull2double_rn((unsigned long long)S));
         ke = __dadd_rn(ke, __dmul_rn(__dmul_rn(__dmul_rn(0.5, T.masses[s]), sum), __dmul_rn(u, u)));
