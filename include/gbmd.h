@@ -462,6 +462,10 @@ uint64_t gbmd_hash_state(uint32_t dim, const int64_t* pos, const int32_t* vel, c
  * kernel's packed (f32x2) two-pair kicks against two scalar kicks. `checked`
  * receives the number of cases, `mismatched` those that differ (0 when the arithmetic holds). */
 int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quotients, int32_t device, uint64_t* checked, uint64_t* mismatched);
+/* Self-check of the velocity rescale's integer arithmetic (round(v f) as i32 from the exact
+ * product, without f64 arithmetic) against the f64 product and rounding, on `count` seeded
+ * random (v, f) pairs on `device`: `mismatched` receives the cases that differ (0 when it holds). */
+int gbmd_check_rescale(uint64_t count, int32_t device, uint64_t* checked, uint64_t* mismatched);
 /* The device's ln, cos and sin (its fdlibm restatement, which the initial velocities, the heat
  * bath and the thermal walls draw with) at n arguments: out[3 i], out[3 i + 1], out[3 i + 2]. */
 int gbmd_debug_libm(const double* x, uint32_t n, double* out);

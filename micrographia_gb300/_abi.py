@@ -286,6 +286,7 @@ SIGNATURES = [
     ("gbmd_serve_set_lanes", C.c_int, [VP, C.c_uint32]),
     ("gbmd_debug_libm", C.c_int, [P(C.c_double), C.c_uint32, P(C.c_double)]),
     ("gbmd_time_thermostat", C.c_int, [VP, C.c_uint32, P(C.c_double)]),
+    ("gbmd_check_rescale", C.c_int, [C.c_uint64, C.c_int32, _U64P, _U64P]),
     ("gbmd_hash_state", C.c_uint64, [C.c_uint32, _I64P, _I32P, _U32P, C.c_uint32]),
     ("gbmd_check_pair_math", C.c_int, [P(gbmd_system), C.c_uint64, C.c_int32, P(C.c_uint64), P(C.c_uint64)]),
     ("gbmd_last_error", C.c_char_p, []),

@@ -1705,6 +1705,41 @@ static __global__ void k_thermo_factor(ThermoP T, const unsigned long long* __re
     fac[1] = skip ? 1.0 : 0.0;
 }
 
+// (v as f64 * f).round() as i32 (init.rs:99-101: the velocity rescale) in integer arithmetic,
+// for f = m 2^e with m the 53-bit significand of a normal positive f64: the exact product |v| m
+// (at most 85 bits, in two 64-bit words) rounded to nearest-even at 53 significant bits, which is
+// the f64 multiply's rounding, then half away from zero to an integer, saturating as Rust's `as`
+// conversion does. The same value as sat_i32_f64(round(__dmul_rn((double)v, f))), without the
+// FP64 pipe, which runs at a small fraction of the integer rate on this GPU.
+__device__ __forceinline__ int32_t rescale_i32(int32_t v, uint64_t m, int e) {
+    if (v == 0) return 0;
+    const uint64_t a = v < 0 ? (uint64_t)0 - (uint64_t)(int64_t)v : (uint64_t)v; // |v| <= 2^31
+    const uint64_t lo = a * m, hi = __umul64hi(a, m);
+    const int L = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo); // bits of |v| m
+    int s = L - 53;
+    uint64_t q = lo;
+    if (s > 0) { // (s <= 32: |v| m < 2^85)
+        q = (lo >> s) | (hi << (64 - s));
+        const uint64_t rem = lo & ((1ull << s) - 1), half = 1ull << (s - 1);
+        if (rem > half || (rem == half && (q & 1ull))) {
+            q += 1;
+            if (q == (1ull << 53)) {
+                q >>= 1;
+                s += 1;
+            }
+        }
+    } else {
+        s = 0;
+    }
+    const int t = e + s; // |v f| rounded to f64 is q 2^t, q < 2^53
+    uint64_t r;
+    if (t >= 0) r = ~0ull; // at least 2^52: saturates
+    else if (-t >= 54) r = 0; // below one half
+    else r = (q + (1ull << (-t - 1))) >> (-t); // half away from zero, on the magnitude
+    if (v > 0) return r > 2147483647ull ? INT32_MAX : (int32_t)r;
+    return r > 2147483648ull ? INT32_MIN : (int32_t)(0u - (uint32_t)r);
+}
+
 // v <- round(v f) as i32 for moving particles (init.rs:99-101), then per-block sums of the new
 // velocities of moving particles (vpart[3 b + a]).
 template <int D>
@@ -1713,13 +1748,19 @@ __global__ void k_rescale(uint32_t n, int32_t* __restrict__ vel, const uint32_t*
     __shared__ long long sh[3][32];
     const double f = fac[0];
     const bool skip = fac[1] != 0.0;
+    // f = m 2^e; a zero, subnormal or non-finite f takes the f64 path
+    const uint64_t fb = (uint64_t)__double_as_longlong(f);
+    const uint32_t fe = (uint32_t)(fb >> 52) & 0x7ffu;
+    const bool ints = !(fb >> 63) && fe != 0u && fe != 0x7ffu;
+    const uint64_t m = (fb & ((1ull << 52) - 1)) | (1ull << 52);
+    const int e = (int)fe - 1075;
     long long acc[3] = {0, 0, 0};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if ((pinned >> species[i]) & 1u) continue;
         for (int a = 0; a < D; a++) {
             int32_t v = vel[D * i + a];
             if (!skip) {
-                v = sat_i32_f64(round(__dmul_rn((double)v, f)));
+                v = ints ? rescale_i32(v, m, e) : sat_i32_f64(round(__dmul_rn((double)v, f)));
                 vel[D * i + a] = v;
             }
             acc[a] += v;

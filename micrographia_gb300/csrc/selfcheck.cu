@@ -98,6 +98,66 @@ __global__ void k_check_kicks2(PairC p, float cs, uint64_t count, uint32_t seed)
 
 } // namespace
 
+namespace {
+// Seeded random (v, f): v over the whole int32 range (with 0, +-1 and the extremes), f with a
+// random 53-bit significand and an exponent of 2^-40 .. 2^40, or within 2^-20 of 1 (a thermostat's
+// factors), or an integer plus one half over 2^k (ties after the product): rescale_i32 equals the
+// f64 path, sat_i32_f64(round(v f)), bit for bit.
+__global__ void k_check_rescale(uint64_t count, uint32_t seed) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k - (k & 31u) < count; k += (uint64_t)gridDim.x * blockDim.x) {
+        bool bad = false;
+        if (k < count) {
+            uint32_t r0, r1, r2, r3;
+            threefry2x32((uint32_t)k, (uint32_t)(k >> 32), seed, 0x7e5c41eu, r0, r1);
+            threefry2x32((uint32_t)k, (uint32_t)(k >> 32), seed, 0x5ca1eu, r2, r3);
+            int32_t v = (int32_t)r0;
+            const uint32_t pick = r3 & 7u;
+            if (pick == 0) v = (int32_t)(r0 % 5u) - 2;                       // 0, +-1, +-2
+            else if (pick == 1) v = (r0 & 1u) ? INT32_MAX : INT32_MIN;        // the extremes
+            else if (pick == 2) v = (int32_t)(r0 >> (r2 % 31u)) * ((r0 & 2u) ? 1 : -1);
+            uint64_t fb;
+            const uint32_t kind = (r3 >> 3) % 3u;
+            if (kind == 0) fb = ((uint64_t)(1023u - 40u + (r2 % 81u)) << 52) | ((((uint64_t)r1 << 32) | r2) & ((1ull << 52) - 1));
+            else if (kind == 1) fb = ((uint64_t)(1022u + (r2 & 1u)) << 52) | (((uint64_t)r1 << 32 | r2) & ((1ull << 52) - 1) & (r2 & 1u ? 0xfffffull : ~0ull));
+            else fb = (uint64_t)__double_as_longlong(__dmul_rn((double)((r1 & 0xfffffu) * 2u + 1u), ldexp(1.0, -(int)(1u + r2 % 40u))));
+            const double f = __longlong_as_double((long long)fb);
+            const uint32_t fe = (uint32_t)(fb >> 52) & 0x7ffu;
+            if (fe != 0u && fe != 0x7ffu && !(fb >> 63)) {
+                const int32_t want = sat_i32_f64(round(__dmul_rn((double)v, f)));
+                const int32_t got = rescale_i32(v, (fb & ((1ull << 52) - 1)) | (1ull << 52), (int)fe - 1075);
+                bad = got != want;
+            }
+        }
+        note_bad(bad);
+    }
+}
+} // namespace
+
+// The velocity rescale's integer arithmetic (rescale_i32) against the f64 product and rounding
+// it replaces, on `count` seeded random cases.
+extern "C" int gbmd_check_rescale(uint64_t count, int32_t device, uint64_t* checked, uint64_t* mismatched) {
+    if (!checked || !mismatched) return fail(GBMD_E_INVALID, "null argument");
+    GBMD_CUDA_TRY(cudaSetDevice(device));
+    cudaStream_t s;
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    unsigned long long zero = 0, bad = 0;
+    int rc = GBMD_OK;
+    if (cudaMemcpyToSymbolAsync(g_bad, &zero, 8, 0, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "self-check counter");
+    if (rc == GBMD_OK && count) {
+        k_check_rescale<<<152 * 8, 256, 0, s>>>(count, 0x2e5ca1eu);
+        note_launch();
+    }
+    if (rc == GBMD_OK && cudaMemcpyFromSymbolAsync(&bad, g_bad, 8, 0, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "self-check counter");
+    if (rc == GBMD_OK) {
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = fail(GBMD_E_CUDA, cudaGetErrorString(e));
+    }
+    cudaStreamDestroy(s);
+    *checked = count;
+    *mismatched = bad;
+    return rc;
+}
+
 extern "C" int gbmd_check_pair_math(const gbmd_system* sys, uint64_t random_quotients, int32_t device, uint64_t* checked,
                                     uint64_t* mismatched) {
     if (!sys || !checked || !mismatched) return fail(GBMD_E_INVALID, "null argument");

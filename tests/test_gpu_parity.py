@@ -73,6 +73,18 @@ def test_libm_restatement_on_device_matches_over_many_draws(O):
     assert np.array_equal(got.pos, want.pos)
 
 
+def test_velocity_rescale_integer_arithmetic():
+    """The thermostat's v <- round(v f) as i32 in integers (the exact product rounded as the f64
+    multiply rounds it, then half away from zero) equals the f64 product and rounding on 2^26
+    seeded random cases: extreme and tiny velocities, factors near 1, wide exponents, ties."""
+    import ctypes as C
+
+    checked, bad = C.c_uint64(), C.c_uint64()
+    _abi.check(_abi.lib().gbmd_check_rescale(1 << 26, 0, C.byref(checked), C.byref(bad)))
+    assert checked.value == 1 << 26
+    assert bad.value == 0, bad.value
+
+
 def test_device_libm_equals_the_oracle_fdlibm(O):
     """The device's ln, cos and sin (the initial velocities', heat bath's and thermal walls' draws)
     equal the oracle's fdlibm restatement bit for bit on 4 x 10^6 arguments: the bath's own
