@@ -737,14 +737,18 @@ void enqueue_thermo(gbmd_engine* e, cudaStream_t s) {
         k_ke_exact<2><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tpart);
         k_thermo_factor<<<1, 256, 0, s>>>(T, e->tpart, e->tfac);
         k_rescale<2><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tfac, e->vpart);
-        k_zero_apply<2><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving, e->vpart, nb, e->tfac);
+        k_vsum<<<1, 256, 0, s>>>(e->vpart, nb, e->vpart + 3 * (size_t)nb);
+        k_zero_apply<2><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving,
+                                                               e->vpart + 3 * (size_t)nb, e->tfac);
     } else {
         k_ke_exact<3><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tpart);
         k_thermo_factor<<<1, 256, 0, s>>>(T, e->tpart, e->tfac);
         k_rescale<3><<<nb, 256, 0, s>>>(e->n, e->vel, e->species, e->sys.pinned, e->tfac, e->vpart);
-        k_zero_apply<3><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving, e->vpart, nb, e->tfac);
+        k_vsum<<<1, 256, 0, s>>>(e->vpart, nb, e->vpart + 3 * (size_t)nb);
+        k_zero_apply<3><<<blocks_for(e->n, 256), 256, 0, s>>>(e->n, e->vel, e->species, e->ids, e->mrank, e->sys.pinned, e->moving,
+                                                               e->vpart + 3 * (size_t)nb, e->tfac);
     }
-    note_launch(4);
+    note_launch(5);
 }
 
 // Ranks of the moving particles in id order (zero_velocity_sum's order) from id-ordered species.
@@ -1315,7 +1319,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
     GBMD_TRY(allocT(e, &e->qpos[1], n));
     GBMD_TRY(allocT(e, &e->mrank, n));
     GBMD_TRY(allocT(e, &e->tpart, 8 * (size_t)e->thermo_nb));
-    GBMD_TRY(allocT(e, &e->vpart, 3 * (size_t)e->thermo_nb));
+    GBMD_TRY(allocT(e, &e->vpart, 3 * ((size_t)e->thermo_nb + 1))); // the block partials, then their total
     GBMD_TRY(allocT(e, &e->tfac, 2));
     GBMD_TRY(allocT(e, &e->partial, 4 * (size_t)blocks_for(n, 128) + 4));
     GBMD_TRY(alloc(e, &e->staging, n * D * 8));

@@ -1740,6 +1740,23 @@ __device__ __forceinline__ int32_t rescale_i32(int32_t v, uint64_t m, int e) {
     return r > 2147483648ull ? INT32_MIN : (int32_t)(0u - (uint32_t)r);
 }
 
+// The velocity sums of the moving particles: the per-block partials vpart[3 b + a] added by one
+// block of 256 threads (integers: exact in any order) into tot[a].
+static __global__ void k_vsum(const long long* __restrict__ vpart, uint32_t nblocks, long long* __restrict__ tot) {
+    __shared__ long long sh[3][256];
+    for (int a = 0; a < 3; a++) {
+        long long t = 0;
+        for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x) t += vpart[3 * b + a];
+        sh[a][threadIdx.x] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        long long t = 0;
+        for (uint32_t k = 0; k < blockDim.x; k++) t += sh[threadIdx.x][k];
+        tot[threadIdx.x] = t;
+    }
+}
+
 // v <- round(v f) as i32 for moving particles (init.rs:99-101), then per-block sums of the new
 // velocities of moving particles (vpart[3 b + a]).
 template <int D>
@@ -1785,15 +1802,8 @@ __global__ void k_rescale(uint32_t n, int32_t* __restrict__ vel, const uint32_t*
 // mrank[id] is k.
 template <int D>
 __global__ void k_zero_apply(uint32_t n, int32_t* __restrict__ vel, const uint32_t* __restrict__ species, const uint32_t* __restrict__ ids,
-                             const uint32_t* __restrict__ mrank, uint32_t pinned, uint32_t moving, const long long* __restrict__ vpart,
-                             uint32_t nblocks, const double* __restrict__ fac) {
-    __shared__ long long tot[3];
-    if (threadIdx.x < 3) {
-        long long t = 0;
-        for (uint32_t b = 0; b < nblocks; b++) t += vpart[3 * b + threadIdx.x];
-        tot[threadIdx.x] = t;
-    }
-    __syncthreads();
+                             const uint32_t* __restrict__ mrank, uint32_t pinned, uint32_t moving, const long long* __restrict__ tot,
+                             const double* __restrict__ fac) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fac[1] != 0.0 || moving == 0 || ((pinned >> species[i]) & 1u)) return;
     long long m = moving, k = mrank[ids[i]];
