@@ -217,6 +217,9 @@ int gbmd_snapshot(gbmd_engine* e, void* buf, size_t cap, size_t* written);
 int gbmd_restore(gbmd_engine* e, const void* buf, size_t size);
 /* Flip one bit of one coordinate of particle `id` (engine.rs:964, State::flip_bit). */
 int gbmd_flip_bit(gbmd_engine* e, uint32_t id, uint32_t axis, uint32_t bit);
+/* GpuEngine::flip_species_bit (engine.rs:1014-1024): XOR bit `bit` of coordinate `axis` of every
+ * particle whose species is in the mask `species_mask`. */
+int gbmd_flip_species_bit(gbmd_engine* e, uint32_t species_mask, uint32_t axis, uint32_t bit);
 
 /* ---- Page commands and run-time changes: md::GpuEngine (crates/md/src/engine.rs:895-1063) ---- */
 
@@ -257,6 +260,12 @@ typedef struct gbmd_bond_type {
     double r0;
 } gbmd_bond_type;
 int gbmd_set_bonds(gbmd_engine* e, const gbmd_bond_type* types, uint32_t ntypes, const uint32_t* bonds, uint32_t nbonds);
+/* GpuEngine::add_bond / remove_bond (engine.rs:976-1012): bond ids a and b with bond type `type`
+ * (one of the types gbmd_set_bonds gave), as in a reaction, or break their bond for good; *done
+ * is 1 if the bond list changed, 0 if they were already bonded (or one has GBMD_MAX_BONDS bonds,
+ * or a == b) / had no bond. Between steps. */
+int gbmd_add_bond(gbmd_engine* e, uint32_t a, uint32_t b, uint32_t type, int32_t* done);
+int gbmd_remove_bond(gbmd_engine* e, uint32_t a, uint32_t b, int32_t* done);
 /* The piston (md_core::Piston, system.rs:100-116; System::with_piston, system.rs:274-282), 2D: a
  * soft wall that replaces the top of y (the axis must have walls), starting at height `start`
  * sigma and stopping at `min` and at the box height. GBMD_PISTON_SPEED moves it at `speed`
@@ -280,9 +289,13 @@ typedef struct gbmd_piston {
     double min;     /* sigma */
 } gbmd_piston;
 int gbmd_set_piston(gbmd_engine* e, const gbmd_piston* piston);
-/* IntEngine's piston_w (height, position units), piston_v (position units per step) and
- * piston_work (the gas's work on the piston, eps). Any pointer may be NULL. */
-int gbmd_read_piston(gbmd_engine* e, int64_t* height, int32_t* velocity, double* work);
+/* IntEngine's piston_w (height, position units), piston_v (position units per step),
+ * piston_work (the gas's work on the piston, eps) and the gas's force on it in the last step
+ * (eps/sigma; GpuEngine::read_piston, engine.rs:958-961). Any pointer may be NULL. */
+int gbmd_read_piston(gbmd_engine* e, int64_t* height, int32_t* velocity, double* work, double* force);
+/* GpuEngine::set_piston_speed (engine.rs:936-939): the piston's velocity, sigma/tau (positive
+ * opens the box), as a step displacement. */
+int gbmd_set_piston_speed(gbmd_engine* e, double speed);
 
 /* ---- Observables: IntEngine::energy (int_engine.rs:433-446) and the new instruments ---- */
 

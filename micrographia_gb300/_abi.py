@@ -241,7 +241,11 @@ SIGNATURES = [
     ("gbmd_update_system", C.c_int, [VP, P(gbmd_system)]),
     ("gbmd_set_bonds", C.c_int, [VP, P(gbmd_bond_type), C.c_uint32, P(C.c_uint32), C.c_uint32]),
     ("gbmd_set_piston", C.c_int, [VP, P(gbmd_piston)]),
-    ("gbmd_read_piston", C.c_int, [VP, P(C.c_int64), P(C.c_int32), P(C.c_double)]),
+    ("gbmd_read_piston", C.c_int, [VP, P(C.c_int64), P(C.c_int32), P(C.c_double), P(C.c_double)]),
+    ("gbmd_set_piston_speed", C.c_int, [VP, C.c_double]),
+    ("gbmd_add_bond", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_int32)]),
+    ("gbmd_remove_bond", C.c_int, [VP, C.c_uint32, C.c_uint32, P(C.c_int32)]),
+    ("gbmd_flip_species_bit", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32]),
     ("gbmd_energy", C.c_int, [VP, _DP, _DP]),
     ("gbmd_observe", C.c_int, [VP, P(gbmd_frame), _U64P, C.c_uint32, C.c_double, _U64P, C.c_uint32, C.c_uint32]),
     ("gbmd_observe_begin", C.c_int, [VP, C.c_uint32, C.c_double, C.c_uint32, C.c_uint32]),

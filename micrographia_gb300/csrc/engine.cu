@@ -11,6 +11,9 @@
 // cooperative launches that step until the trigger fires, in a WHILE node with the rebuild in a
 // nested IF.
 #include <algorithm>
+#include <array>
+#include <cstddef>
+#include <initializer_list>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -405,6 +408,8 @@ struct gbmd_engine {
     bool failed = false;
     bool half = false;       // half-shell lists (k_build_half / k_force_half / k_leap_half)
     uint32_t* bond_tab = nullptr; // bonds: per id 4 x (partner id, type), padded with UINT32_MAX
+    std::vector<gbmd_bond_type> bond_types_h;        // the bond types and bonds as set (host copies:
+    std::vector<std::array<uint32_t, 3>> bonds_h;     // add_bond / remove_bond edit them)
     uint32_t* slot_of = nullptr;  // bonds: the storage slot of each id
     PistonState* piston = nullptr; // the piston's moving state (2D)
     int32_t* acc = nullptr;  // half-shell kick accumulators, 3 x int32 per slot, zero between steps
@@ -1102,6 +1107,15 @@ template <int D> __global__ void k_flip(uint32_t n, const uint32_t* ids, uint32_
     long long* p = reinterpret_cast<long long*>(pos + s);
     p[axis] ^= (long long)(1ull << bit);
 }
+// GpuEngine::flip_species_bit (engine.rs:1014-1024): the same bit of every particle whose species
+// is in the mask.
+template <int D>
+__global__ void k_flip_species(uint32_t n, const uint32_t* species, uint32_t mask, uint32_t axis, uint32_t bit, Rec<D>* pos) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || !((mask >> species[s]) & 1u)) return;
+    long long* p = reinterpret_cast<long long*>(pos + s);
+    p[axis] ^= (long long)(1ull << bit);
+}
 
 // ---- page commands (md::GpuEngine, crates/md/src/engine.rs:1026-1063)
 struct RegionCmd {
@@ -1662,6 +1676,9 @@ int gbmd_set_bonds(gbmd_engine* e, const gbmd_bond_type* types, uint32_t ntypes,
     }
     e->P.bonds = nbonds ? 1u : 0u;
     e->P.bond_tab = e->bond_tab;
+    e->bond_types_h.assign(types, types + ntypes);
+    e->bonds_h.clear();
+    for (uint32_t q = 0; q < nbonds; q++) e->bonds_h.push_back({bonds[3 * q], bonds[3 * q + 1], bonds[3 * q + 2]});
     e->P.slot_of = e->slot_of;
     for (uint32_t t = 0; t < 4; t++) {
         e->P.bond_fene[t] = t < ntypes && types[t].kind == GBMD_BOND_FENE;
@@ -1716,7 +1733,7 @@ int gbmd_set_piston(gbmd_engine* e, const gbmd_piston* p) {
     return gbmd_sync(e);
 }
 
-int gbmd_read_piston(gbmd_engine* e, int64_t* height, int32_t* velocity, double* work) {
+int gbmd_read_piston(gbmd_engine* e, int64_t* height, int32_t* velocity, double* work, double* force) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
     PistonState ps{};
     if (e->P.piston_drive) {
@@ -1726,7 +1743,86 @@ int gbmd_read_piston(gbmd_engine* e, int64_t* height, int32_t* velocity, double*
     if (height) *height = ps.w;
     if (velocity) *velocity = ps.v;
     if (work) *work = ps.work;
+    if (force) *force = ps.gas;
     return GBMD_OK;
+}
+
+int gbmd_set_piston_speed(gbmd_engine* e, double speed) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (!e->P.piston_drive) return fail(GBMD_E_INVALID, "the engine has no piston");
+    if (!std::isfinite(speed)) return fail(GBMD_E_INVALID, "a finite speed");
+    const int32_t v = to_step_displacement(e->sys, speed);
+    GBMD_CUDA_TRY(cudaMemcpyAsync((char*)e->piston + offsetof(PistonState, v), &v, 4, cudaMemcpyHostToDevice, e->st));
+    return gbmd_sync(e);
+}
+
+// The partner-table rows of these ids from the bond list (System::partner_table, system.rs:
+// 311-324: each bond appended to both ends' rows in list order), uploaded.
+static int upload_partner_rows(gbmd_engine* e, std::initializer_list<uint32_t> ids) {
+    for (uint32_t id : ids) {
+        uint32_t row[8];
+        std::fill(row, row + 8, 0xffffffffu);
+        uint32_t used = 0;
+        for (const auto& b : e->bonds_h)
+            for (int end = 0; end < 2; end++)
+                if (b[end] == id && used < GBMD_MAX_BONDS) {
+                    row[2 * used] = b[1 - end];
+                    row[2 * used + 1] = b[2];
+                    used++;
+                }
+        GBMD_CUDA_TRY(cudaMemcpyAsync(e->bond_tab + 8 * (size_t)id, row, sizeof(row), cudaMemcpyHostToDevice, e->st));
+    }
+    return gbmd_sync(e);
+}
+
+int gbmd_remove_bond(gbmd_engine* e, uint32_t a, uint32_t b, int32_t* removed) {
+    if (!e || !removed) return fail(GBMD_E_INVALID, "null argument");
+    *removed = 0;
+    const size_t before = e->bonds_h.size();
+    e->bonds_h.erase(std::remove_if(e->bonds_h.begin(), e->bonds_h.end(),
+                                    [&](const std::array<uint32_t, 3>& x) { return (x[0] == a && x[1] == b) || (x[0] == b && x[1] == a); }),
+                     e->bonds_h.end());
+    if (e->bonds_h.size() == before) return GBMD_OK;
+    *removed = 1;
+    return upload_partner_rows(e, {a, b});
+}
+
+int gbmd_add_bond(gbmd_engine* e, uint32_t a, uint32_t b, uint32_t type, int32_t* added) {
+    if (!e || !added) return fail(GBMD_E_INVALID, "null argument");
+    *added = 0;
+    if (e->D != 2) return fail(GBMD_E_UNSUPPORTED, "bonds are two-dimensional (IntEngine; IntEngine3 has none)");
+    if (type >= e->bond_types_h.size()) return fail(GBMD_E_INVALID, "add_bond needs a system built with that bond type (gbmd_set_bonds)");
+    if (a >= e->n || b >= e->n) return fail(GBMD_E_INVALID, "particle ids < n");
+    auto count = [&](uint32_t id) {
+        uint32_t c = 0;
+        for (const auto& x : e->bonds_h) c += (x[0] == id) + (x[1] == id);
+        return c;
+    };
+    for (const auto& x : e->bonds_h)
+        if ((x[0] == a && x[1] == b) || (x[0] == b && x[1] == a)) return GBMD_OK; // already bonded
+    if (a == b || count(a) >= GBMD_MAX_BONDS || count(b) >= GBMD_MAX_BONDS) return GBMD_OK;
+    e->bonds_h.push_back({a, b, type});
+    if (!e->P.bonds) { // the first bond: the table, and graphs that take the bond pass
+        std::vector<uint32_t> flat;
+        for (const auto& x : e->bonds_h) flat.insert(flat.end(), x.begin(), x.end());
+        std::vector<gbmd_bond_type> types = e->bond_types_h;
+        GBMD_TRY(gbmd_set_bonds(e, types.data(), (uint32_t)types.size(), flat.data(), (uint32_t)e->bonds_h.size()));
+    } else {
+        GBMD_TRY(upload_partner_rows(e, {a, b}));
+    }
+    *added = 1;
+    return GBMD_OK;
+}
+
+int gbmd_flip_species_bit(gbmd_engine* e, uint32_t species_mask, uint32_t axis, uint32_t bit) {
+    if (!e || axis >= (uint32_t)e->D || bit > 62) return fail(GBMD_E_INVALID, "bad flip_species_bit argument");
+    GBMD_TRY(prepare_pairs(e)); // wraps the positions into the box (they drift out between list builds)
+    if (e->D == 2) k_flip_species<2><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->species, species_mask, axis, bit, (Rec<2>*)e->pos[e->cur]);
+    else k_flip_species<3><<<blocks_for(e->n, 256), 256, 0, e->st>>>(e->n, e->species, species_mask, axis, bit, (Rec<3>*)e->pos[e->cur]);
+    note_launch();
+    uint32_t one = 1;
+    GBMD_CUDA_TRY(cudaMemcpyAsync(e->ctl, &one, 4, cudaMemcpyHostToDevice, e->st));
+    return gbmd_sync(e);
 }
 
 int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {

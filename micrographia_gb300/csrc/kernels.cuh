@@ -1377,6 +1377,7 @@ static __global__ void k_piston_tick(Params P, uint32_t* ctl) {
     PistonState& ps = *P.piston;
     const double gas = __dmul_rn(__ll2double_rn((long long)ps.force_fixed), 1.0 / 65536.0);
     ps.force_fixed = 0ull;
+    ps.gas = gas;
     if (P.piston_drive == 2) ps.v = wadd(ps.v, piston_kick(P, __dsub_rn(gas, P.piston_ext)));
     const int64_t old = ps.w;
     int64_t w = old + (int64_t)ps.v;

@@ -195,8 +195,35 @@ class _Engine:
         """The piston's height (position units), velocity (position units per step) and the gas's
         work on it (eps): IntEngine's piston_w, piston_v, piston_work."""
         w, v, work = C.c_int64(), C.c_int32(), C.c_double()
-        _abi.check(self._lib.gbmd_read_piston(self._h, C.byref(w), C.byref(v), C.byref(work)))
+        _abi.check(self._lib.gbmd_read_piston(self._h, C.byref(w), C.byref(v), C.byref(work), None))
         return w.value, v.value, work.value
+
+    def read_piston(self):
+        """GpuEngine::read_piston (engine.rs:958-961): (height sigma, velocity sigma/tau, the gas's
+        force on it in the last step eps/sigma, the gas's work on it eps)."""
+        w, v, work, f = C.c_int64(), C.c_int32(), C.c_double(), C.c_double()
+        _abi.check(self._lib.gbmd_read_piston(self._h, C.byref(w), C.byref(v), C.byref(work), C.byref(f)))
+        return w.value / 4294967296.0, v.value / 4294967296.0 / self.sys.dt, f.value, work.value
+
+    def set_piston_speed(self, u):
+        """GpuEngine::set_piston_speed (engine.rs:936-939): sigma/tau, positive opens the box."""
+        _abi.check(self._lib.gbmd_set_piston_speed(self._h, float(u)))
+
+    def add_bond(self, a, b, ty):
+        """GpuEngine::add_bond (engine.rs:999-1012): whether the bond was added."""
+        done = C.c_int32()
+        _abi.check(self._lib.gbmd_add_bond(self._h, int(a), int(b), int(ty), C.byref(done)))
+        return bool(done.value)
+
+    def remove_bond(self, a, b):
+        """GpuEngine::remove_bond (engine.rs:976-985): whether there was such a bond."""
+        done = C.c_int32()
+        _abi.check(self._lib.gbmd_remove_bond(self._h, int(a), int(b), C.byref(done)))
+        return bool(done.value)
+
+    def flip_species_bit(self, species_mask, axis, bit):
+        """GpuEngine::flip_species_bit (engine.rs:1014-1024)."""
+        _abi.check(self._lib.gbmd_flip_species_bit(self._h, int(species_mask), int(axis), int(bit)))
 
     def update_system(self, sys):
         """Replace interactions, masses, gravity, pinned species or dt (same box and species

@@ -348,6 +348,13 @@ int oracle_engine_set_piston(void* h, int drive, double speed, double mass, doub
     const bool ok = e->f32 ? e->f32->set_piston(drive, speed, mass, force, start, min) : e->f64->set_piston(drive, speed, mass, force, start, min);
     return ok ? 0 : -1;
 }
+// GpuEngine::set_piston_speed (md/src/engine.rs:936-939): the piston's velocity as a step
+// displacement.
+void oracle_engine_set_piston_speed(void* h, double speed) {
+    Engine* e = (Engine*)h;
+    if (e->f32) e->f32->piston_v = e->f32->sys.to_step_displacement(speed);
+    else e->f64->piston_v = e->f64->sys.to_step_displacement(speed);
+}
 // The piston's height (position units), velocity (per step), the gas's work on it (eps) and
 // the gas's force on it in the last force evaluation (eps/sigma).
 void oracle_engine_piston(void* h, int64_t* w, int32_t* v, double* work, double* force) {

@@ -70,6 +70,7 @@ _SIGS = [
     ("oracle_engine_set_bonds", None, [VP, U32P, DP, DP, C.c_uint32, U32P, C.c_uint64]),
     ("oracle_engine_set_piston", C.c_int, [VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
     ("oracle_engine_piston", None, [VP, I64P, I32P, DP, DP]),
+    ("oracle_engine_set_piston_speed", None, [VP, C.c_double]),
     ("oracle_engine_steps", C.c_int64, [VP]),
     ("oracle_engine_energy", None, [VP, DP, DP]),
     ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
@@ -409,6 +410,10 @@ class IntEngine:
         b = np.ascontiguousarray(np.array(bonds, np.uint32).reshape(-1, 3))
         lib().oracle_engine_set_bonds(self._h, _p(fene, C.c_uint32), _p(k, C.c_double), _p(r0, C.c_double), nt, _p(b, C.c_uint32), len(b))
         return self
+
+    def set_piston_speed(self, u):
+        """GpuEngine::set_piston_speed: the piston's velocity, u sigma/tau as a step displacement."""
+        lib().oracle_engine_set_piston_speed(self._h, float(u))
 
     def piston(self):
         """IntEngine's piston_w (position units), piston_v (per step), piston_work (eps) and the

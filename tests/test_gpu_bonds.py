@@ -120,3 +120,35 @@ def test_bonds_are_checked(O):
         for bad in ([(0, 0, 0)], [(0, 1, 1)], [(0, k, 0) for k in range(1, 6)], [(0, 40, 0)]):
             with pytest.raises(RuntimeError):
                 g.set_bonds([Bond.kremer_grest()], bad)
+
+
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_bonds_added_and_removed_between_steps(O, mode):
+    """GpuEngine::add_bond / remove_bond (engine.rs:976-1012): a chain cut in the middle, two chain
+    ends joined and two beads of a chain bonded, with a second (harmonic) bond type, between steps;
+    the oracle's partner table is rebuilt from the same bond list, and the runs stay bit-identical
+    (cells, and Verlet lists with the force kernel's epilogue)."""
+    from micrographia_gb300 import Bond, _abi
+
+    sys_, s0 = _melt(O, 20, 20, 0.3, 7)
+    types = [Bond.kremer_grest(), Bond.harmonic(20.0, 1.2)]
+    sys_.with_bonds(types, sys_.bonds)
+    bonds = list(sys_.bonds)
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_with_skin(sys_, s0.n(), 0.3)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, m, flags=_abi.force_lanes_flag(1)) as g:
+        g.step(300)
+        c.step(300)
+        assert g.remove_bond(9, 10)
+        assert not g.remove_bond(9, 10)
+        assert g.add_bond(19, 20, 1)  # the end of chain 0 to the start of chain 1 (harmonic)
+        assert g.add_bond(45, 47, 1)
+        assert not g.add_bond(45, 47, 1)  # already bonded
+        bonds = [b for b in bonds if {b[0], b[1]} != {9, 10}] + [(19, 20, 1), (45, 47, 1)]
+        c.set_bonds([("fene" if t.fene else "harmonic", t.k, t.r0) for t in types], bonds)
+        g.step(500)
+        c.step(500)
+        assert g.read_state() == c.state
+        kg, _ = g.kicks()
+        kc, _ = c.kicks()
+        assert np.array_equal(kg, kc)

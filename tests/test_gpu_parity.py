@@ -1302,3 +1302,23 @@ def test_time_loop_and_batch_time_phases_keep_the_trajectory(O):
             c = O.IntEngine(sys_, s0)
             c.step(100)
             assert b.read_system(k) == c.state, k
+
+
+def test_flip_species_bit_matches_the_oracle(O):
+    """GpuEngine::flip_species_bit (engine.rs:1014-1024): bit 30 of x of every particle of species 1
+    flipped between steps; the run then equals the oracle's from the same flipped state."""
+    n = 3000
+    sys_ = System(box_for(n, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 2.0])
+    s0 = O.fluid(sys_, n, 1.0, 61)
+    s0.species[:] = np.arange(n) % 2
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, ForceMode.verlet_with_skin(sys_, n, 0.3)) as g:
+        g.step(200)
+        c.step(200)
+        st = c.state.copy()
+        st.pos[st.species == 1, 0] ^= np.int64(1 << 30)
+        g.flip_species_bit(0b10, 0, 30)
+        c2 = O.IntEngine(sys_, st)
+        g.step(200)
+        c2.step(200)
+        assert g.read_state() == c2.state

@@ -333,3 +333,27 @@ def test_driven_piston_with_a_bath_follows_the_oracle(O):
             assert g.read_state() == c.state
             assert g.piston() == c.piston()[:3]
         _same_ledger(g, c)
+
+
+def test_piston_page_commands(O):
+    """GpuEngine::read_piston and set_piston_speed (engine.rs:936-961): the gas's force on the
+    piston in the last step equals the oracle's; a new speed set on both between steps keeps the
+    runs bit-identical."""
+    from micrographia_gb300 import Piston
+    from test_oracle import _gas_under_piston
+
+    sys_, s0 = _gas_under_piston(O, 500, 0.3, Piston.speed_drive(-0.5), 16)
+    c = O.IntEngine(sys_, s0)
+    with GpuEngine(sys_, s0, ForceMode.verlet_with_skin(sys_, s0.n(), 0.3)) as g:
+        g.step(600)
+        c.step(600)
+        h, v, f, work = g.read_piston()
+        w, vi, cwork, cf = c.piston()
+        assert (h, v) == (w / 2**32, vi / 2**32 / sys_.dt) and work == cwork
+        assert f == cf and f > 0.0
+        g.set_piston_speed(0.25)
+        c.set_piston_speed(0.25)
+        g.step(600)
+        c.step(600)
+        assert g.read_state() == c.state
+        assert g.piston() == c.piston()[:3]
