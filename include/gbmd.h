@@ -328,6 +328,12 @@ int gbmd_counters(gbmd_engine* e, int64_t* steps, uint32_t* clock);
 #define GBMD_LEDGER_SLOTS 7
 #define GBMD_LEDGER_BATH 6
 int gbmd_read_ledger(gbmd_engine* e, double* energy, double* impulse, uint64_t* hits);
+/* GpuEngine::read_compartment_ledger (engine.rs:455-470, walls::CompartmentLedger walls.rs:52-72):
+ * the same per slot and per compartment along its wall (compartment c along the other axis of the
+ * wall's axis; 0 for the bath and without compartments), slot w, compartment c at [w cap + c] for
+ * c < cap (entries past the engine's count are 0). *per_wall receives the engine's count (the
+ * most compartments along either axis, 1 without); with all three arrays NULL only that. */
+int gbmd_read_compartment_ledger(gbmd_engine* e, uint32_t cap, double* energy, double* impulse, uint64_t* hits, uint32_t* per_wall);
 /* The CUDA stream the engine launches on (a cudaStream_t), for event timing by the caller. */
 int gbmd_stream(gbmd_engine* e, void** stream);
 /* Kernels launched by this engine so far (every launch, graph nodes included). */

@@ -717,11 +717,11 @@ void enqueue_force(gbmd_engine* e, cudaStream_t s) {
     } else if (e->P.bath) { // the Andersen bath on the moved state, then the step clock advances
         const uint32_t nb = blocks_for(e->n, 256);
         if (e->D == 2) {
-            if (e->verlet) k_bath<2, true><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<2>*)e->ref_pos, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
-            else k_bath<2, false><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
+            if (e->verlet) k_bath<2, true><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<2>*)e->ref_pos, e->ctl, e->ledger + 3 * (size_t)GBMD_LEDGER_BATH * e->P.ledger_per_wall);
+            else k_bath<2, false><<<nb, 256, 0, s>>>(e->P, (Rec<2>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger + 3 * (size_t)GBMD_LEDGER_BATH * e->P.ledger_per_wall);
         } else {
-            if (e->verlet) k_bath<3, true><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<3>*)e->ref_pos, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
-            else k_bath<3, false><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger + 3 * GBMD_LEDGER_BATH);
+            if (e->verlet) k_bath<3, true><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], e->qpos[e->cur], e->vel, e->species, e->ids, (const Rec<3>*)e->ref_pos, e->ctl, e->ledger + 3 * (size_t)GBMD_LEDGER_BATH * e->P.ledger_per_wall);
+            else k_bath<3, false><<<nb, 256, 0, s>>>(e->P, (Rec<3>*)e->pos[e->cur], nullptr, e->vel, e->species, e->ids, nullptr, e->ctl, e->ledger + 3 * (size_t)GBMD_LEDGER_BATH * e->P.ledger_per_wall);
         }
         k_clock_tick<<<1, 1, 0, s>>>(e->ctl);
         note_launch(2);
@@ -1308,11 +1308,18 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         GBMD_CUDA_TRY(cudaFuncSetAttribute(k_force_half<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     }
     GBMD_TRY(allocT(e, &e->ctl, 16));
-    GBMD_TRY(allocT(e, &e->ledger, 3 * GBMD_LEDGER_SLOTS));
+    {
+        // per ledger slot, one entry per compartment along its wall (the most on either axis)
+        uint32_t pw = 1;
+        for (uint32_t a = 0; a < 2 && e->D == 2; a++)
+            if (e->P.comp_shift[a]) pw = std::max<uint32_t>(pw, (uint32_t)(e->sys.box_len[a] >> e->P.comp_shift[a]));
+        e->P.ledger_per_wall = pw;
+    }
+    GBMD_TRY(allocT(e, &e->ledger, 3 * (size_t)GBMD_LEDGER_SLOTS * e->P.ledger_per_wall));
     e->P.ids_list = e->ids; // (the force kernel's scenario epilogue)
     e->P.ledger = e->ledger;
     e->P.clock_word = e->ctl + CTL_CLOCK;
-    GBMD_CUDA_TRY(cudaMemsetAsync(e->ledger, 0, 24 * GBMD_LEDGER_SLOTS, e->st));
+    GBMD_CUDA_TRY(cudaMemsetAsync(e->ledger, 0, 24 * (size_t)GBMD_LEDGER_SLOTS * e->P.ledger_per_wall, e->st));
     if (e->opt.arith == GBMD_ARITH_INT) {
         std::vector<int32_t> tab;
         std::vector<double> pair4;
@@ -1867,6 +1874,7 @@ int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
     e->P.slot_of = old.slot_of;
     e->P.ids_list = old.ids_list;
     e->P.ledger = old.ledger;
+    e->P.ledger_per_wall = old.ledger_per_wall;
     e->P.clock_word = old.clock_word;
     e->P.piston_drive = old.piston_drive; // and the piston
     e->P.piston_mass = old.piston_mass;
@@ -1922,15 +1930,39 @@ int gbmd_state_hash(gbmd_engine* e, uint64_t* hash) {
     return GBMD_OK;
 }
 
+int gbmd_read_compartment_ledger(gbmd_engine* e, uint32_t cap, double* energy, double* impulse, uint64_t* hits, uint32_t* per_wall) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    const uint32_t pw = e->P.ledger_per_wall;
+    if (per_wall) *per_wall = pw;
+    if (!energy && !impulse && !hits) return GBMD_OK;
+    if (cap < pw) return fail(GBMD_E_INVALID, "room for fewer compartments per wall than the engine keeps");
+    std::vector<unsigned long long> l(3 * (size_t)GBMD_LEDGER_SLOTS * pw);
+    GBMD_CUDA_TRY(cudaMemcpyAsync(l.data(), e->ledger, l.size() * 8, cudaMemcpyDeviceToHost, e->st));
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    for (int w = 0; w < GBMD_LEDGER_SLOTS; w++)
+        for (uint32_t c = 0; c < cap; c++) {
+            const size_t q = (size_t)w * cap + c, at = 3 * ((size_t)w * pw + c);
+            const bool in = c < pw;
+            if (energy) energy[q] = in ? (double)(long long)l[at] * (1.0 / 16777216.0) : 0.0;
+            if (hits) hits[q] = in ? (uint64_t)l[at + 1] : 0;
+            if (impulse) impulse[q] = in ? (double)(long long)l[at + 2] * (1.0 / 16777216.0) : 0.0;
+        }
+    return GBMD_OK;
+}
+
 int gbmd_read_ledger(gbmd_engine* e, double* energy, double* impulse, uint64_t* hits) {
     if (!e) return fail(GBMD_E_INVALID, "null engine");
-    unsigned long long l[3 * GBMD_LEDGER_SLOTS];
-    GBMD_CUDA_TRY(cudaMemcpyAsync(l, e->ledger, sizeof(l), cudaMemcpyDeviceToHost, e->st));
+    const uint32_t pw = e->P.ledger_per_wall;
+    std::vector<unsigned long long> l(3 * (size_t)GBMD_LEDGER_SLOTS * pw);
+    GBMD_CUDA_TRY(cudaMemcpyAsync(l.data(), e->ledger, l.size() * 8, cudaMemcpyDeviceToHost, e->st));
     GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
-    for (int w = 0; w < GBMD_LEDGER_SLOTS; w++) {
-        if (energy) energy[w] = (double)(long long)l[3 * w] * (1.0 / 16777216.0);
-        if (hits) hits[w] = (uint64_t)l[3 * w + 1];
-        if (impulse) impulse[w] = (double)(long long)l[3 * w + 2] * (1.0 / 16777216.0);
+    for (int w = 0; w < GBMD_LEDGER_SLOTS; w++) { // CompartmentLedger::totals (walls.rs:63-71), in integers
+        unsigned long long t[3] = {0, 0, 0};
+        for (uint32_t c = 0; c < pw; c++)
+            for (int q = 0; q < 3; q++) t[q] += l[3 * ((size_t)w * pw + c) + q];
+        if (energy) energy[w] = (double)(long long)t[0] * (1.0 / 16777216.0);
+        if (hits) hits[w] = (uint64_t)t[1];
+        if (impulse) impulse[w] = (double)(long long)t[2] * (1.0 / 16777216.0);
     }
     return GBMD_OK;
 }

@@ -1189,6 +1189,18 @@ __device__ __forceinline__ void thermal_velocity(const Params& P, uint32_t id, u
         vt[1] = __dmul_rn(rad, dev_sin(a));
     }
 }
+// The ledger entry of slot w for a particle at x: its compartment along the wall, i.e. along the
+// other axis (IntEngine::ledger_compartment, int_engine.rs:392-394; 0 without compartments, in 3D
+// and for the bath).
+template <int D>
+__device__ __forceinline__ unsigned long long* ledger_at(const Params& P, unsigned long long* ledger, int w, int axis, const int64_t* x) {
+    uint32_t c = 0;
+    if (D == 2 && axis < 2) {
+        const uint32_t o = 1 - axis, sh = P.comp_shift[o];
+        if (sh) c = (uint32_t)(x[o] >> sh);
+    }
+    return ledger + 3 * ((size_t)w * P.ledger_per_wall + c);
+}
 // The walls' kicks on one particle at its step-start position xo (int_engine.rs:203-246): each
 // soft wall's WCA kick (its impulse booked on the ledger) and the piston's (its force summed in
 // 2^-16 eps/sigma units), added to k like the pair kicks; c is the particle's kick coefficient.
@@ -1204,7 +1216,7 @@ __device__ __forceinline__ void wall_kicks(const Params& P, const int64_t* xo, f
             if (!soft_wall_force(side == 0 ? xo[a] : P.box[a] - xo[a], f, s6)) continue;
             const int32_t kw = rni_f32(__fmul_rn(f, c));
             k[a] = wadd(k[a], side == 0 ? kw : (int32_t)(0u - (uint32_t)kw));
-            atomicAdd(ledger + 3 * (2 * a + side) + 2, ledger_fixed(__dmul_rn((double)f, P.dt)));
+            atomicAdd(ledger_at<D>(P, ledger, 2 * a + side, a, xo) + 2, ledger_fixed(__dmul_rn((double)f, P.dt)));
         }
     }
     if (D == 2 && P.piston_drive) {
@@ -1227,7 +1239,7 @@ template <int D>
 __device__ __forceinline__ bool wall_post(const Params& P, uint32_t si, uint32_t id, uint32_t clock, int64_t* x, int32_t* v,
                                           unsigned long long* ledger, bool wrap_periodic) {
     bool changed = false;
-    if (P.bath && bath_one<D>(P, si, id, clock, x, v, ledger + 3 * GBMD_LEDGER_BATH)) changed = true;
+    if (P.bath && bath_one<D>(P, si, id, clock, x, v, ledger + 3 * (size_t)GBMD_LEDGER_BATH * P.ledger_per_wall)) changed = true;
     const double m = P.masses[si];
     int64_t old[3];
 #pragma unroll
@@ -1245,8 +1257,9 @@ __device__ __forceinline__ bool wall_post(const Params& P, uint32_t si, uint32_t
             const double vel_a = __ddiv_rn(__dmul_rn((double)v[a], 1.0 / 4294967296.0), P.dt);
             const double dp = __dmul_rn(__dmul_rn(2.0, m), fabs(vel_a));
             v[a] = (int32_t)(0u - (uint32_t)v[a]);
-            atomicAdd(ledger + 3 * face + 1, 1ull);
-            atomicAdd(ledger + 3 * face + 2, ledger_fixed(dp));
+            unsigned long long* l = ledger_at<D>(P, ledger, face, (int)a, old);
+            atomicAdd(l + 1, 1ull);
+            atomicAdd(l + 2, ledger_fixed(dp));
             changed = true;
         }
     }
@@ -1307,7 +1320,7 @@ __device__ __forceinline__ bool wall_post(const Params& P, uint32_t si, uint32_t
         };
         const double de = __dsub_rn(ke(after), ke(before));
         const double imp = fabs(__dmul_rn(m, __dsub_rn(before[a], after[a])));
-        unsigned long long* l = ledger + 3 * (2 * a + side);
+        unsigned long long* l = ledger_at<D>(P, ledger, 2 * a + side, a, old);
         atomicAdd(l, ledger_fixed(de));
         atomicAdd(l + 1, 1ull);
         atomicAdd(l + 2, ledger_fixed(imp));

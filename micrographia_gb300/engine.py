@@ -259,6 +259,18 @@ class _Engine:
         )
         return f, rdf, prof
 
+    def read_compartment_ledger(self):
+        """GpuEngine::read_compartment_ledger (engine.rs:455-470): (energy, impulse, hits), arrays of
+        shape (ledger slots, compartments per wall), each event rounded to 2^-24."""
+        pw = C.c_uint32()
+        _abi.check(self._lib.gbmd_read_compartment_ledger(self._h, 0, None, None, None, C.byref(pw)))
+        k = pw.value
+        e = np.zeros((_abi.LEDGER_SLOTS, k), np.float64)
+        p = np.zeros((_abi.LEDGER_SLOTS, k), np.float64)
+        h = np.zeros((_abi.LEDGER_SLOTS, k), np.uint64)
+        _abi.check(self._lib.gbmd_read_compartment_ledger(self._h, k, _ptr(e, C.c_double), _ptr(p, C.c_double), _ptr(h, C.c_uint64), None))
+        return e, p, h
+
     def read_ledger(self):
         """GpuEngine::read_ledger: (energy, impulse, hits), one entry per ledger slot: the walls'
         (2 axis + side) and the heat bath's (_abi.LEDGER_BATH), each event rounded to 2^-24."""

@@ -365,6 +365,21 @@ void oracle_engine_piston(void* h, int64_t* w, int32_t* v, double* work, double*
         *w = e->f64->piston_w, *v = e->f64->piston_v, *work = e->f64->piston_work, *force = e->f64->piston_force;
     }
 }
+// The compartment ledger in integers: per_wall, then (energy, impulse, hits) per slot and
+// compartment at [w per_wall + c] (arrays of at least LEDGER_SLOTS x per_wall; NULL: the count only).
+uint32_t oracle_engine_compartment_ledger(void* h, int64_t* energy, int64_t* impulse, uint64_t* hits) {
+    Engine* e = (Engine*)h;
+    auto take = [&](auto* g) {
+        if (energy)
+            for (size_t q = 0; q < g->comp_hits.size(); q++) {
+                energy[q] = g->comp_energy_fixed[q];
+                impulse[q] = g->comp_impulse_fixed[q];
+                hits[q] = g->comp_hits[q];
+            }
+        return g->per_wall;
+    };
+    return e->f32 ? take(e->f32.get()) : take(e->f64.get());
+}
 void oracle_engine_wall_ledger_fixed(void* h, int64_t* energy, int64_t* impulse) {
     const Ledger& l = ((Engine*)h)->f32 ? ((Engine*)h)->f32->ledger : ((Engine*)h)->f64->ledger;
     for (int w = 0; w < LEDGER_SLOTS; w++) {

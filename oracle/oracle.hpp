@@ -1074,7 +1074,30 @@ template <typename F> struct IntEngine {
     int32_t piston_v = 0;
     double piston_work = 0.0, piston_force = 0.0;
 
-    IntEngine(const System& s, const State& st) : state(st) { set_system(s); }
+    // walls::CompartmentLedger (walls.rs:52-72; IntEngine::compartment_ledger, int_engine.rs:
+    // 30-32): per slot and per compartment along the wall (compartment_of along the other axis,
+    // 0 for the bath), each event rounded to 2^-24 and summed as integers, with the hits.
+    uint32_t per_wall = 1;
+    std::vector<int64_t> comp_energy_fixed, comp_impulse_fixed;
+    std::vector<uint64_t> comp_hits;
+    size_t comp_slot(int w, int axis, const int64_t* x) const {
+        int64_t c = 0;
+        if (sys.dim == 2 && axis < 2) {
+            const int o = 1 - axis;
+            if (sys.compartments[o]) c = x[o] >> sys.compartments[o];
+        }
+        return (size_t)w * per_wall + (size_t)c;
+    }
+
+    IntEngine(const System& s, const State& st) : state(st) {
+        set_system(s);
+        // System::compartment_counts (system.rs:247-250): the most along either axis
+        for (int a = 0; a < 2 && sys.dim == 2; a++)
+            if (sys.compartments[a]) per_wall = std::max<uint32_t>(per_wall, (uint32_t)(sys.box[a] >> sys.compartments[a]));
+        comp_energy_fixed.assign((size_t)LEDGER_SLOTS * per_wall, 0);
+        comp_impulse_fixed.assign((size_t)LEDGER_SLOTS * per_wall, 0);
+        comp_hits.assign((size_t)LEDGER_SLOTS * per_wall, 0);
+    }
     // System::with_bonds (system.rs:284-299) and the engine's partner table.
     void set_bonds(const std::vector<BondType>& types, const std::vector<std::array<uint32_t, 3>>& bonds) {
         bond_consts.clear();
@@ -1331,6 +1354,7 @@ template <typename F> struct IntEngine {
                     if (wall_force[i][w] != 0.0) {
                         ledger.impulse[w] += wall_force[i][w] * sys.dt;
                         ledger.impulse_fixed[w] += ledger_fixed(wall_force[i][w] * sys.dt);
+                        comp_impulse_fixed[comp_slot(w, w / 2, &state.pos[d * i])] += ledger_fixed(wall_force[i][w] * sys.dt);
                     }
             for (size_t i = 0; i < state.n(); i++) {
                 const uint32_t sp = state.species[i];
@@ -1367,6 +1391,8 @@ template <typename F> struct IntEngine {
                     }
                     ledger.energy[LEDGER_BATH] += de;
                     ledger.bath_energy_fixed += ledger_fixed(de);
+                    comp_energy_fixed[(size_t)LEDGER_BATH * per_wall] += ledger_fixed(de);
+                    comp_hits[(size_t)LEDGER_BATH * per_wall] += 1;
                     ledger.hits[LEDGER_BATH] += 1;
                 }
                 int64_t old[3] = {x[0], x[1], d == 3 ? x[2] : 0};
@@ -1383,6 +1409,8 @@ template <typename F> struct IntEngine {
                         v[a] = wneg(v[a]);
                         ledger.impulse[face] += dp;
                         ledger.impulse_fixed[face] += ledger_fixed(dp);
+                        comp_impulse_fixed[comp_slot(face, a, old)] += ledger_fixed(dp);
+                        comp_hits[comp_slot(face, a, old)] += 1;
                         ledger.hits[face] += 1;
                     }
                 }
@@ -1393,7 +1421,7 @@ template <typename F> struct IntEngine {
                     }
                     const int side = mirror(x[a], sys.box[a]);
                     if (side >= 0) {
-                        collide(i, a, side, v);
+                        collide(i, a, side, v, old);
                     } else if (d == 2 && sys.compartments[a] != 0) {
                         // int_engine.rs:324-330: a particle that crossed into another compartment
                         // is mirrored back into its home one (walls::mirror_compartment, walls.rs:72-78)
@@ -1419,7 +1447,7 @@ template <typename F> struct IntEngine {
     // IntEngine::collide (int_engine.rs:363-390) / IntEngine3::collide (int_engine3.rs:186-205):
     // hard and soft walls reflect the normal component; a thermal wall draws a new velocity; the
     // ledger books the energy change and the normal momentum given to the wall.
-    void collide(size_t i, int axis, int side, int32_t* v) {
+    void collide(size_t i, int axis, int side, int32_t* v, const int64_t* old) {
         const int d = sys.dim;
         const double m = sys.masses[state.species[i]];
         const int w = 2 * axis + side;
@@ -1446,6 +1474,10 @@ template <typename F> struct IntEngine {
         ledger.energy_fixed[w] += ledger_fixed(de);
         ledger.impulse_fixed[w] += ledger_fixed(imp);
         ledger.hits[w] += 1;
+        const size_t q = comp_slot(w, axis, old); // (the position before the move, as the reference's)
+        comp_energy_fixed[q] += ledger_fixed(de);
+        comp_impulse_fixed[q] += ledger_fixed(imp);
+        comp_hits[q] += 1;
     }
     // int_engine.rs:396-413
     void reverse() {

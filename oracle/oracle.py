@@ -71,6 +71,7 @@ _SIGS = [
     ("oracle_engine_set_piston", C.c_int, [VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
     ("oracle_engine_piston", None, [VP, I64P, I32P, DP, DP]),
     ("oracle_engine_set_piston_speed", None, [VP, C.c_double]),
+    ("oracle_engine_compartment_ledger", C.c_uint32, [VP, I64P, I64P, U64P]),
     ("oracle_engine_steps", C.c_int64, [VP]),
     ("oracle_engine_energy", None, [VP, DP, DP]),
     ("oracle_state_hash", C.c_uint64, [C.c_uint32, I64P, I32P, U32P, C.c_uint64]),
@@ -410,6 +411,16 @@ class IntEngine:
         b = np.ascontiguousarray(np.array(bonds, np.uint32).reshape(-1, 3))
         lib().oracle_engine_set_bonds(self._h, _p(fene, C.c_uint32), _p(k, C.c_double), _p(r0, C.c_double), nt, _p(b, C.c_uint32), len(b))
         return self
+
+    def compartment_ledger_fixed(self):
+        """walls::CompartmentLedger in integers: (energy, impulse) in 2^-24 units and hits, arrays
+        of shape (ledger slots, compartments per wall)."""
+        k = lib().oracle_engine_compartment_ledger(self._h, None, None, None)
+        e = np.zeros((7, k), np.int64)
+        p = np.zeros((7, k), np.int64)
+        h = np.zeros((7, k), np.uint64)
+        lib().oracle_engine_compartment_ledger(self._h, _p(e, C.c_int64), _p(p, C.c_int64), _p(h, C.c_uint64))
+        return e, p, h
 
     def set_piston_speed(self, u):
         """GpuEngine::set_piston_speed: the piston's velocity, u sigma/tau as a step displacement."""

@@ -29,6 +29,18 @@ def _same_ledger(g, c):
     return sum(gh)
 
 
+def _same_compartment_ledger(g, c):
+    """GpuEngine::read_compartment_ledger against the oracle's walls::CompartmentLedger (integer
+    sums per slot and compartment along the wall)."""
+    ge, gp, gh = g.read_compartment_ledger()
+    oe, op, oh = c.compartment_ledger_fixed()
+    assert ge.shape == oe.shape
+    assert np.array_equal(gh, oh)
+    assert np.array_equal(np.round(ge * 2**24).astype(np.int64), oe)
+    assert np.array_equal(np.round(gp * 2**24).astype(np.int64), op)
+    return oh
+
+
 def _gas_in_walls(O, n, density, seed, kind, gravity):
     """boundaries.rs:6-35: a WCA gas in a box walled on both axes (hard or soft), with gravity."""
     w = Wall.hard() if kind == "hard" else Wall.soft()
@@ -214,6 +226,8 @@ def test_compartments_follow_the_oracle_and_reverse(O, diathermal, mode):
         assert got == c.state
         assert [sys_.compartment_of(p) for p in got.pos] == home
         _same_ledger(g, c)
+        hits = _same_compartment_ledger(g, c)
+        assert hits.shape == (7, 16) and (hits[:4].sum(axis=1) > 0).all()  # every outer wall, per box along it
         g.reverse()
         g.step(1500)
         g.reverse()
@@ -248,6 +262,7 @@ def test_membrane_follows_the_oracle(O, mode, pores):
         st = g.read_state()
         assert st == c.state
         _same_ledger(g, c)
+        _same_compartment_ledger(g, c)
         hits_right = g.read_ledger()[2][5]
     if not pores:
         assert hits_right > 20  # the solute hit the membrane from the right
