@@ -300,6 +300,11 @@ int gbmd_set_piston_speed(gbmd_engine* e, double speed);
 /* ---- Observables: IntEngine::energy (int_engine.rs:433-446) and the new instruments ---- */
 
 int gbmd_energy(gbmd_engine* e, double* kinetic, double* potential);
+/* GpuEngine3::read_kinetic / read_kinetic_total (engine3.rs:618-637) and
+ * Observer::read_kinetic_energies (observe.rs:99-117): each particle's kinetic energy 1/2 m |v|^2
+ * from its half-step velocity (0 for a pinned species), and its species, in id order, and their
+ * total (f64, where the reference reads f32; any pointer may be NULL). */
+int gbmd_read_kinetic(gbmd_engine* e, double* kinetic, uint32_t* species, double* total);
 /* One frame of instruments. `rdf` (may be NULL) receives `rdf_bins` integer pair counts of
  * unordered pairs with floor(r * rdf_bins / rdf_rmax) = k; `profile` (may be NULL) receives
  * `profile_bins` particle counts along `profile_axis`. */
@@ -311,6 +316,15 @@ int gbmd_observe(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint32_t rdf_
  * and fills `frame`, `rdf` (rdf_bins counts) and `profile`. One frame in flight per engine. */
 int gbmd_observe_begin(gbmd_engine* e, uint32_t rdf_bins, double rdf_rmax, uint32_t profile_bins, uint32_t profile_axis);
 int gbmd_observe_end(gbmd_engine* e, gbmd_frame* frame, uint64_t* rdf, uint64_t* profile);
+/* Observer::read (crates/md/src/observe.rs:86-97; histogram and kinetic, observe.wgsl:31-56), 2D
+ * engines: a gx x gy density grid over the box, bin (min(u32(coord(x) gx/Lx), gx-1),
+ * min(u32(coord(y) gy/Ly), gy-1)) with coord the f32 value of the wrapped position and gx/Lx
+ * rounded to f32, stored row-major (by * gx + bx); counts of all particles into `all` and of
+ * species `marked` into `marked_counts` (gx * gy words each, either may be NULL), and the
+ * half-step kinetic energy of the moving particles into `kinetic` (summed exactly in integers,
+ * returned in f64; the reference sums f32). Synchronous. GBMD_E_UNSUPPORTED in 3D. */
+int gbmd_observe_grid(gbmd_engine* e, uint32_t gx, uint32_t gy, uint32_t marked, uint32_t* all, uint32_t* marked_counts,
+                      double* kinetic);
 
 /* ---- Diagnostics ---- */
 

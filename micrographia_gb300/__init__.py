@@ -6,6 +6,7 @@ the `with_thermostat` / `with_fan` / `with_bath_layer` builders) and `init` help
 (crates/md-core/src/{pair,system,init,three}.rs), and the engines `GpuEngine` / `GpuEngine3`
 (crates/md/src/engine.rs:598-1098, engine3.rs:334-648) with `step`, `reverse`, `kicks`,
 `read_state`, `upload`, `energy`, `flip_bit`, `read_list_stats`, `read_ledger` and `ForceMode`;
+the Observer's `Reading` with `mixing` and `segregation` (crates/md/src/observe.rs);
 `BatchEngine` and `Server` run many systems at once.
 
 All compute runs in the CUDA library libgbmd.so through its C ABI (include/gbmd.h); importing
@@ -33,6 +34,7 @@ from .core import (
     to_fixed,
 )
 from .engine import BatchEngine, GpuEngine, GpuEngine3, Server, init_state
+from .observe import Reading, mixing, segregation
 from . import init, workloads
 
 __all__ = [
@@ -52,6 +54,9 @@ __all__ = [
     "GpuEngine3",
     "BatchEngine",
     "Server",
+    "Reading",
+    "mixing",
+    "segregation",
     "box_for",
     "chains",
     "cube_for",

@@ -1472,6 +1472,31 @@ int gbmd_read_state(gbmd_engine* e, int64_t* pos, int32_t* vel, uint32_t* specie
     return gbmd_sync(e);
 }
 
+int gbmd_read_kinetic(gbmd_engine* e, double* kinetic, uint32_t* species, double* total) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    GBMD_TRY(read_state_dev(e));
+    const size_t n = e->n, D = e->D;
+    std::vector<int32_t> vel(n * D);
+    std::vector<uint32_t> sp(n);
+    GBMD_CUDA_TRY(cudaMemcpyAsync(vel.data(), e->staging_v, n * D * 4, cudaMemcpyDeviceToHost, e->st));
+    GBMD_CUDA_TRY(cudaMemcpyAsync(sp.data(), e->staging_s, n * 4, cudaMemcpyDeviceToHost, e->st));
+    GBMD_TRY(gbmd_sync(e));
+    double sum = 0.0;
+    for (size_t i = 0; i < n; i++) { // 1/2 m |v|^2, v = velocity(v) = v UNIT / dt (system.rs:423-425)
+        double k = 0.0;
+        for (size_t a = 0; a < D; a++) {
+            const double u = (double)vel[D * i + a] * (1.0 / 4294967296.0) / e->sys.dt;
+            k += u * u;
+        }
+        k *= ((e->sys.pinned >> sp[i]) & 1u) ? 0.0 : 0.5 * e->sys.masses[sp[i]]; // pinned: 0 (observe.wgsl:55)
+        if (kinetic) kinetic[i] = k;
+        if (species) species[i] = sp[i];
+        sum += k;
+    }
+    if (total) *total = sum;
+    return GBMD_OK;
+}
+
 int gbmd_upload(gbmd_engine* e, const int64_t* pos, const int32_t* vel, const uint32_t* species) {
     if (!e || !pos || !vel || !species) return fail(GBMD_E_INVALID, "null argument");
     GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
@@ -2385,6 +2410,39 @@ __global__ void k_profile_wide(uint32_t n, const Rec<D>* pos, uint32_t axis, int
     atomicAdd(out + cell_of(wrap(p[axis], lfix), l, bins), 1ull);
 }
 
+// Observer::histogram (observe.wgsl:31-45): per particle the bin
+// (min(u32(coord(x) sx), gx - 1), min(u32(coord(y) sy), gy - 1)), coord(x) = f32(x_hi) +
+// f32(x_lo) 2^-32 in f32, of the wrapped position; counts of all particles in h[0, gx gy) and of
+// the marked species in h[gx gy, 2 gx gy). Shared-memory counts when they fit (shm > 0), else one
+// global atomic per count.
+__device__ __forceinline__ uint32_t grid_bin(int64_t x, float scale, uint32_t g) {
+    const float c = __fadd_rn(__uint2float_rn((uint32_t)((uint64_t)x >> 32)), __fmul_rn(__uint2float_rn((uint32_t)x), 0x1p-32f));
+    const uint32_t b = __float2uint_rz(__fmul_rn(c, scale));
+    return b < g - 1 ? b : g - 1;
+}
+
+__global__ void k_grid_hist(uint32_t n, const Rec<2>* pos, const uint32_t* species, int64_t lx, int64_t ly, float sx, float sy,
+                            uint32_t gx, uint32_t gy, uint32_t marked, bool shm, uint32_t* out) {
+    extern __shared__ uint32_t h[];
+    const uint32_t bins = gx * gy;
+    uint32_t* dst = shm ? h : out;
+    if (shm) {
+        for (uint32_t b = threadIdx.x; b < 2 * bins; b += blockDim.x) h[b] = 0;
+        __syncthreads();
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long* p = reinterpret_cast<const long long*>(pos + i);
+        const uint32_t b = grid_bin(wrap(p[1], ly), sy, gy) * gx + grid_bin(wrap(p[0], lx), sx, gx);
+        atomicAdd(dst + b, 1u);
+        if (species[i] == marked) atomicAdd(dst + bins + b, 1u);
+    }
+    if (shm) {
+        __syncthreads();
+        for (uint32_t b = threadIdx.x; b < 2 * bins; b += blockDim.x)
+            if (h[b]) atomicAdd(out + b, h[b]);
+    }
+}
+
 } // namespace
 
 // Host memory that the device copies a frame into without the host waiting (pinned, grown on
@@ -2519,6 +2577,51 @@ extern "C" int gbmd_observe_begin(gbmd_engine* e, uint32_t rdf_bins, double rdf_
     e->obs_rdf_bins = rdf_bins;
     e->obs_profile_bins = profile_bins;
     e->obs_nb = nb;
+    return GBMD_OK;
+}
+
+extern "C" int gbmd_observe_grid(gbmd_engine* e, uint32_t gx, uint32_t gy, uint32_t marked, uint32_t* all, uint32_t* marked_counts,
+                                 double* kinetic) {
+    if (!e) return fail(GBMD_E_INVALID, "null engine");
+    if (e->D != 2) return fail(GBMD_E_UNSUPPORTED, "the density grid is two-dimensional (Observer takes a 2D engine)");
+    if (e->obs_pending) return fail(GBMD_E_INVALID, "a frame is in flight (gbmd_observe_end first)");
+    if (gx == 0 || gy == 0 || (uint64_t)gx * gy > (1u << 24)) return fail(GBMD_E_INVALID, "grid must have 1 to 2^24 bins");
+    const uint32_t n = e->n, bins = gx * gy;
+    uint32_t* d = nullptr;
+    if (cudaMallocAsync((void**)&d, 2 * (size_t)bins * 4, e->st) != cudaSuccess) return fail(GBMD_E_NOMEM, "grid counts");
+    std::vector<uint32_t> h(2 * (size_t)bins);
+    std::vector<unsigned long long> part(8 * (size_t)e->thermo_nb);
+    cudaError_t err = cudaMemsetAsync(d, 0, 2 * (size_t)bins * 4, e->st);
+    if (err == cudaSuccess) {
+        // scale = (g / L) as f32 (observe.rs:58): the f64 quotient rounded once
+        const float sx = (float)((double)gx / to_f64h(e->sys.box_len[0])), sy = (float)((double)gy / to_f64h(e->sys.box_len[1]));
+        const bool shm = 2 * (size_t)bins * 4 <= 48 * 1024;
+        const uint32_t grid = shm ? std::min(blocks_for(n, 256), 1024u) : blocks_for(n, 256);
+        k_grid_hist<<<std::max(grid, 1u), 256, shm ? 2 * (size_t)bins * 4 : 0, e->st>>>(n, (const Rec<2>*)e->pos[e->cur], e->species, e->P.box[0],
+                                                                                           e->P.box[1], sx, sy, gx, gy, marked, shm, d);
+        k_ke_exact<2><<<e->thermo_nb, 256, 0, e->st>>>(n, e->vel, e->species, e->sys.pinned, e->tpart);
+        note_launch(2);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(h.data(), d, 2 * (size_t)bins * 4, cudaMemcpyDeviceToHost, e->st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(part.data(), e->tpart, part.size() * 8, cudaMemcpyDeviceToHost, e->st);
+    cudaFreeAsync(d, e->st);
+    GBMD_CUDA_TRY(err);
+    GBMD_CUDA_TRY(cudaStreamSynchronize(e->st));
+    if (all) std::memcpy(all, h.data(), (size_t)bins * 4);
+    if (marked_counts) std::memcpy(marked_counts, h.data() + bins, (size_t)bins * 4);
+    if (kinetic) {
+        // sum_s 1/2 m_s S_s (UNIT / dt)^2, S_s the exact sum of v^2 over the moving particles of s
+        const double u = (1.0 / 4294967296.0) / e->sys.dt;
+        double ke = 0.0;
+        for (uint32_t s = 0; s < e->sys.nspecies; s++) {
+            unsigned __int128 S = 0;
+            for (uint32_t b = 0; b < e->thermo_nb; b++) S += ((unsigned __int128)part[8 * b + 2 * s + 1] << 64) | part[8 * b + 2 * s];
+            const double sum = (double)(uint64_t)(S >> 64) * 18446744073709551616.0 + (double)(uint64_t)S;
+            ke += 0.5 * e->sys.masses[s] * sum * (u * u);
+        }
+        *kinetic = ke;
+    }
     return GBMD_OK;
 }
 

@@ -5,7 +5,7 @@ Their methods mirror md::GpuEngine (crates/md/src/engine.rs:598-1098) and md::Gp
 `reverse`, `kicks`, `read_state` (id order), `upload`, `flip_bit`, `read_list_stats`,
 `read_ledger`, the page commands (`kick_region`, `set_species`, `set_species_velocity`,
 `sort_now`) and `update_system`, plus the CPU twins' `energy` (int_engine.rs:433-446) and the new
-FP64 instruments (`observe`).
+FP64 instruments (`observe`), and the Observer's density grid (`observe_grid`, observe.rs:26-130).
 """
 
 import ctypes as C
@@ -14,6 +14,7 @@ import numpy as np
 
 from . import _abi
 from .core import ForceMode, State, State3
+from .observe import Reading
 
 P = C.POINTER
 
@@ -118,6 +119,17 @@ class _Engine:
         sp = np.empty(self.n, np.uint32)
         _abi.check(self._lib.gbmd_read_state(self._h, _ptr(pos, C.c_int64), _ptr(vel, C.c_int32), _ptr(sp, C.c_uint32)))
         return self.STATE(pos, vel, sp)
+
+    def read_positions(self):
+        """GpuEngine::read_positions (engine.rs:1085-1088): positions in id order."""
+        pos = np.empty((self.n, self.DIM), np.int64)
+        _abi.check(self._lib.gbmd_read_state(self._h, _ptr(pos, C.c_int64), None, None))
+        return pos
+
+    def read_potential(self):
+        """GpuEngine3::read_potential (engine3.rs:639-643): the potential energy of the pair forces
+        and soft walls at the current positions (gbmd_kicks' sum)."""
+        return self.kicks()[1]
 
     def upload(self, state):
         if state.n() != self.n:
@@ -258,6 +270,30 @@ class _Engine:
             )
         )
         return f, rdf, prof
+
+    def observe_grid(self, grid, marked):
+        """Observer::read (observe.rs:86-97): a Reading of the gx x gy density grid, all particles
+        and the `marked` species, with the half-step kinetic energy."""
+        gx, gy = int(grid[0]), int(grid[1])
+        all_ = np.zeros(gx * gy, np.uint32)
+        mk = np.zeros(gx * gy, np.uint32)
+        ke = C.c_double()
+        _abi.check(self._lib.gbmd_observe_grid(self._h, gx, gy, int(marked), _ptr(all_, C.c_uint32), _ptr(mk, C.c_uint32), C.byref(ke)))
+        return Reading(all_, mk, ke.value)
+
+    def read_kinetic(self):
+        """GpuEngine3::read_kinetic (engine3.rs:626-630): per-particle kinetic energies from the
+        half-step velocities and the species, in id order."""
+        ke = np.empty(self.n, np.float64)
+        sp = np.empty(self.n, np.uint32)
+        _abi.check(self._lib.gbmd_read_kinetic(self._h, _ptr(ke, C.c_double), _ptr(sp, C.c_uint32), None))
+        return ke, sp
+
+    def read_kinetic_total(self):
+        """GpuEngine3::read_kinetic_total (engine3.rs:632-637)."""
+        t = C.c_double()
+        _abi.check(self._lib.gbmd_read_kinetic(self._h, None, None, C.byref(t)))
+        return t.value
 
     def read_compartment_ledger(self):
         """GpuEngine::read_compartment_ledger (engine.rs:455-470): (energy, impulse, hits), arrays of

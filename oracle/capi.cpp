@@ -440,6 +440,12 @@ void oracle_profile(const gbmd_system* csys, const int64_t* pos, uint64_t n, uin
     auto h = density_profile(sys, make_state_pos(sys.dim, pos, nullptr, n), bins, (int)axis);
     std::memcpy(out, h.data(), bins * 8);
 }
+void oracle_observer_grid(const gbmd_system* csys, const int64_t* pos, const uint32_t* species, uint64_t n, uint32_t gx, uint32_t gy,
+                          uint32_t marked, uint32_t* out) {
+    System sys = System::from_c(*csys);
+    auto h = observer_grid(sys, make_state_pos(sys.dim, pos, species, n), gx, gy, marked);
+    std::memcpy(out, h.data(), h.size() * 4);
+}
 
 // ---- all-integer tables (md-core table.rs)
 int oracle_int_kick(const gbmd_system* csys, uint32_t sa, uint32_t sb, const int64_t* d, int32_t* out) {

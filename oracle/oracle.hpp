@@ -1827,6 +1827,28 @@ inline std::vector<uint64_t> density_profile(const System& sys, const State& s, 
     for (size_t i = 0; i < s.n(); i++) h[cell_of(to_f64(s.pos[sys.dim * i + axis]), sys.box_f64(axis), bins)]++;
     return h;
 }
+// Observer's density grid (crates/md/src/observe.rs:47-67, observe.wgsl:25-45): per particle the
+// bin (min(u32(coord(x) sx), gx - 1), min(u32(coord(y) sy), gy - 1)) with coord(x) =
+// f32(x_hi) + ldexp(f32(x_lo), -32) in f32 and s = (g / L) as f32; counts of all particles in
+// out[0, gx gy), of species `marked` in out[gx gy, 2 gx gy).
+inline uint32_t observer_bin(int64_t x, float scale, uint32_t g) {
+    const uint64_t u = (uint64_t)x;
+    const float c = (float)(uint32_t)(u >> 32) + std::ldexp((float)(uint32_t)u, -32);
+    const float t = c * scale;
+    const uint32_t b = (uint32_t)t; // t >= 0 and below 2^32 for a position in [0, L)
+    return std::min(b, g - 1);
+}
+inline std::vector<uint32_t> observer_grid(const System& sys, const State& s, uint32_t gx, uint32_t gy, uint32_t marked) {
+    std::vector<uint32_t> h(2 * (size_t)gx * gy, 0);
+    const float sx = (float)((double)gx / sys.box_f64(0)), sy = (float)((double)gy / sys.box_f64(1));
+    for (size_t i = 0; i < s.n(); i++) {
+        const int64_t x = wrap(s.pos[2 * i], sys.box[0]), y = wrap(s.pos[2 * i + 1], sys.box[1]);
+        const size_t b = (size_t)observer_bin(y, sy, gy) * gx + observer_bin(x, sx, gx);
+        h[b]++;
+        if (s.species[i] == marked) h[(size_t)gx * gy + b]++;
+    }
+    return h;
+}
 // The velocity-rescale thermostat of this engine: the half-step kinetic energy summed exactly as
 // integers per species (sum of v^2 in 128 bits), then f = sqrt(t / now) as set_temperature
 // (init.rs:92-103) with v <- round(v f) and an exact zero velocity sum.

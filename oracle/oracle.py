@@ -83,6 +83,7 @@ _SIGS = [
     ("oracle_pair_sums", None, [SYS, I64P, U32P, C.c_uint64, DP, DP]),
     ("oracle_rdf", None, [SYS, I64P, C.c_uint64, C.c_uint32, C.c_double, U64P]),
     ("oracle_profile", None, [SYS, I64P, C.c_uint64, C.c_uint32, C.c_uint32, U64P]),
+    ("oracle_observer_grid", None, [SYS, I64P, U32P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, U32P]),
     ("oracle_int_kick", C.c_int, [SYS, C.c_uint32, C.c_uint32, I64P, I32P]),
 ]
 
@@ -254,6 +255,15 @@ def profile(sys, state, bins, axis):
     c = sys.to_c()
     lib().oracle_profile(C.byref(c), _p(state.pos, C.c_int64), state.n(), bins, axis, _p(out, C.c_uint64))
     return out
+
+
+def observer_grid(sys, state, grid, marked):
+    """Observer's counts (observe.wgsl:31-45): (all, marked), gx * gy each, row-major."""
+    gx, gy = grid
+    out = np.zeros(2 * gx * gy, np.uint32)
+    c = sys.to_c()
+    lib().oracle_observer_grid(C.byref(c), _p(state.pos, C.c_int64), _p(state.species, C.c_uint32), state.n(), gx, gy, marked, _p(out, C.c_uint32))
+    return out[: gx * gy], out[gx * gy :]
 
 
 def half_step_kinetic(sys, state):

@@ -486,6 +486,71 @@ def test_frame_3d(O):
     assert np.array_equal(rdf, O.rdf(sys3, s, 200, 5.0))
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_read_kinetic_in_id_order(O, dim):
+    """GpuEngine3::read_kinetic / read_kinetic_total (engine3.rs:626-637): per-particle kinetic
+    energies from the half-step velocities, with their species, in id order, after the storage
+    order has been shuffled by list builds; a two-species mixture (masses 1 and 2.5)."""
+    if dim == 2:
+        sys_ = System(box_for(2000, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 2.5])
+        s0 = O.fluid(sys_, 2000, 1.0, 5)
+        eng, mode = GpuEngine, ForceMode.verlet_with_skin(sys_, 2000, 0.3)
+    else:
+        sys_ = System3(cube_for(2048, 0.8442), 0.005, Pair.lj(2.5), [1.0, 2.5])
+        s0 = O.fcc_maxwell(sys_, 2048, 0.72, 3, jitter=0.05)
+        eng, mode = GpuEngine3, ForceMode.verlet_with_skin(sys_, 2048, 0.3)
+    sp = (np.arange(s0.n()) % 3 == 0).astype(np.uint32)
+    s0 = type(s0)(s0.pos, s0.vel, sp)
+    c = O.IntEngine(sys_, s0)
+    with eng(sys_, s0, mode) as g:
+        g.step(120)
+        c.step(120)
+        ke, spg = g.read_kinetic()
+        tot = g.read_kinetic_total()
+        assert np.array_equal(g.read_positions(), c.state.pos)
+        assert g.read_potential() == g.kicks()[1]
+    st = c.state
+    u = st.vel.astype(np.float64) * (1.0 / 4294967296.0) / sys_.dt
+    want = 0.5 * np.array([1.0, 2.5])[st.species] * (u * u).sum(axis=1)
+    assert np.array_equal(spg, st.species)
+    assert np.allclose(ke, want, rtol=1e-14, atol=0.0)
+    assert abs(tot - want.sum()) < 1e-12 * want.sum()
+
+
+@pytest.mark.parametrize("mode", ["cells", "verlet"])
+def test_observer_grid_matches_the_oracle(O, mode):
+    """Observer::read (observe.rs:86-97) on a two-species fluid with species 1 pinned: the density
+    grid of all particles and of species 0 equals the oracle's count for count, with grids that
+    fit in shared memory and one that does not (200 x 100), taken between list builds (positions
+    up to the skin outside the box); the kinetic energy equals the oracle's exact half-step sum.
+    Mixing and segregation of the reading match the oracle's counts'. 3D engines refuse."""
+    from micrographia_gb300 import Reading, mixing, segregation
+
+    n = 3000
+    sys_ = System(box_for(n, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 3.0])
+    s0 = O.fluid(sys_, n, 1.0, 8)
+    sp = (np.arange(n) % 4 == 0).astype(np.uint32)
+    s0 = State(s0.pos, np.where(sp[:, None] == 1, 0, s0.vel).astype(np.int32), sp)
+    sys_.with_pinned(1)
+    m = ForceMode.cell_list() if mode == "cells" else ForceMode.verlet_with_skin(sys_, n, 0.5)
+    with GpuEngine(sys_, s0, m) as g:
+        for k, grid in enumerate([(16, 12), (1, 1), (200, 100), (33, 7)]):
+            g.step(7)
+            r = g.observe_grid(grid, 0)
+            st = g.read_state()
+            wa, wm = O.observer_grid(sys_, st, grid, 0)
+            assert np.array_equal(r.all, wa)
+            assert np.array_equal(r.marked, wm)
+            assert r.kinetic == O.exact_kinetic(sys_, st)
+            assert r.all.sum() == n and r.marked.sum() == (sp == 0).sum()
+            want = Reading(wa, wm, 0.0)
+            assert mixing(r) == mixing(want) and segregation(r) == segregation(want)
+    sys3 = System3(cube_for(500, 0.5), 0.005, Pair.wca(), [1.0])
+    with GpuEngine3(sys3, O.fcc_maxwell(sys3, 500, 1.0, 1)) as g3:
+        with pytest.raises(RuntimeError):
+            _abi.check(g3._lib.gbmd_observe_grid(g3._h, 4, 4, 0, None, None, None))
+
+
 def test_frame_between_list_builds(O):
     """Frames taken mid-way between list builds, when positions may sit outside [0, L) by up to
     the skin, count the same RDF and profile as the oracle on the wrapped state."""
