@@ -411,6 +411,10 @@ typedef struct gbmd_init {
  * it to the host arrays (any of which may be NULL). */
 int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, int64_t* pos, int32_t* vel,
                     uint32_t* species);
+/* init::maxwell (crates/md-core/src/init.rs:42-57) and three::maxwell for the given id-ordered
+ * species (each drawn at kT = t with its own mass), with the exact zero velocity sum, into `vel`
+ * (n * dim words), on the device. */
+int gbmd_maxwell(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel);
 /* Create an engine whose state is generated on the device by `spec` (no host round trip). */
 int gbmd_create_seeded(const gbmd_system* sys, const gbmd_init* spec, const gbmd_options* opts,
                        gbmd_engine** out);

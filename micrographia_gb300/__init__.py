@@ -35,7 +35,7 @@ from .core import (
 )
 from .engine import BatchEngine, GpuEngine, GpuEngine3, Server, init_state
 from .observe import Reading, mixing, segregation
-from . import init, workloads
+from . import checks, init, workloads
 
 __all__ = [
     "DT",
@@ -63,6 +63,7 @@ __all__ = [
     "fcc_cells",
     "to_f64",
     "to_fixed",
+    "checks",
     "init",
     "init_state",
     "workloads",

@@ -2808,6 +2808,34 @@ extern "C" int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, in
     return rc;
 }
 
+extern "C" int gbmd_maxwell(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel) {
+    if (!sys || (n && (!species || !vel))) return fail(GBMD_E_INVALID, "null argument");
+    GBMD_TRY(validate_system(*sys, n));
+    for (uint32_t i = 0; i < n; i++)
+        if (species[i] >= sys->nspecies) return fail(GBMD_E_INVALID, "species out of range");
+    if (n == 0) return GBMD_OK;
+    const size_t D = sys->dim;
+    cudaStream_t s;
+    GBMD_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int32_t* dvel = nullptr;
+    uint32_t* dsp = nullptr;
+    int rc = GBMD_OK;
+    if (cudaMallocAsync((void**)&dvel, n * D * 4, s) != cudaSuccess || cudaMallocAsync((void**)&dsp, (size_t)n * 4, s) != cudaSuccess)
+        rc = fail(GBMD_E_NOMEM, "maxwell buffers");
+    if (rc == GBMD_OK && cudaMemcpyAsync(dsp, species, (size_t)n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "copy");
+    if (rc == GBMD_OK) rc = maxwell_state_device(*sys, n, t, seed, dsp, dvel, s);
+    if (rc == GBMD_OK && cudaMemcpyAsync(vel, dvel, n * D * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "copy");
+    if (rc == GBMD_OK) {
+        cudaError_t err = cudaStreamSynchronize(s);
+        if (err != cudaSuccess) rc = fail(GBMD_E_CUDA, cudaGetErrorString(err));
+    }
+    if (dvel) cudaFreeAsync(dvel, s);
+    if (dsp) cudaFreeAsync(dsp, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return rc;
+}
+
 // FNV-1a of an id-ordered state (State::hash, system.rs:460-477; State3::hash, three.rs:281-297).
 extern "C" uint64_t gbmd_hash_state(uint32_t dim, const int64_t* pos, const int32_t* vel, const uint32_t* species, uint32_t n) {
     uint64_t h = 0xcbf29ce484222325ull;

@@ -38,6 +38,7 @@ struct Lattice2 {
     double a0, a1;
     int64_t origin[2];
     int64_t wrap_len[2];
+    int64_t post[2]; // added after the wrap (init::fluid's 1 sigma clear of a wall)
     double jitter;
     uint64_t seed;
     uint32_t first_id; // id of site 0 (jitter counters and the output slot)
@@ -57,7 +58,7 @@ __global__ void k_lattice2(Lattice2 L, longlong2* pos) {
     double cy = __dadd_rn((double)j, 0.5);
     int64_t x = L.origin[0] + to_fixed(__dadd_rn(__dmul_rn(cx, L.a0), jx));
     int64_t y = L.origin[1] + to_fixed(__dadd_rn(__dmul_rn(cy, L.a1), jy));
-    pos[id] = make_longlong2(wrap(x, L.wrap_len[0]), wrap(y, L.wrap_len[1]));
+    pos[id] = make_longlong2(wrap(x, L.wrap_len[0]) + L.post[0], wrap(y, L.wrap_len[1]) + L.post[1]);
 }
 
 struct Vapour2 {
@@ -274,6 +275,11 @@ static int maxwell_device(const gbmd_system& sys, uint32_t n, double t, uint64_t
     return GBMD_OK;
 }
 
+int maxwell_state_device(const gbmd_system& sys, uint32_t n, double t, uint64_t seed, const uint32_t* species_dev, int32_t* vel_dev,
+                         cudaStream_t s) {
+    return maxwell_device(sys, n, t, seed, species_dev, vel_dev, s);
+}
+
 int init_state_device(const gbmd_system& sys, const gbmd_init& spec, void* pos_dev, int32_t* vel_dev, uint32_t* species_dev, cudaStream_t s) {
     uint32_t n = spec.n;
     if (n == 0) return GBMD_OK;
@@ -285,17 +291,29 @@ int init_state_device(const gbmd_system& sys, const gbmd_init& spec, void* pos_d
             if (sys.dim != 2) return fail(GBMD_E_INVALID, "2D recipe on a 3D system");
             Lattice2 L{};
             uint32_t nx, ny;
+            // init::fluid (init.rs:105-121): on an axis with walls the lattice fills the box less
+            // 2 sigma and is then moved 1 sigma in, clear of the walls
+            int64_t inner[2] = {sys.box_len[0], sys.box_len[1]};
             if (spec.recipe == GBMD_INIT_FLUID) {
+                for (int a = 0; a < 2; a++)
+                    if (!((sys.periodic >> a) & 1u)) {
+                        inner[a] = sys.box_len[a] - host_to_fixed(2.0);
+                        L.post[a] = host_to_fixed(1.0);
+                    }
+                if (inner[0] <= 0 || inner[1] <= 0) return fail(GBMD_E_INVALID, "a walled axis is too short for the fluid lattice");
+                b0 = host_to_f64(inner[0]);
+                b1 = host_to_f64(inner[1]);
                 nx = lattice_nx(n, b0, b1);
                 ny = (uint32_t)(((uint64_t)n + nx - 1) / nx);
             } else {
+                if ((sys.periodic & 3u) != 3u) return fail(GBMD_E_UNSUPPORTED, "the triangular recipe is for periodic boxes");
                 triangular_shape(n, b0, b1, &nx, &ny);
             }
             L.nx = nx;
             L.a0 = b0 / (double)nx;
             L.a1 = b1 / (double)ny;
-            L.wrap_len[0] = sys.box_len[0];
-            L.wrap_len[1] = sys.box_len[1];
+            L.wrap_len[0] = inner[0];
+            L.wrap_len[1] = inner[1];
             L.jitter = spec.jitter;
             L.seed = spec.seed;
             L.count = n;
@@ -305,6 +323,7 @@ int init_state_device(const gbmd_system& sys, const gbmd_init& spec, void* pos_d
         }
         case GBMD_INIT_SLAB: {
             if (sys.dim != 2) return fail(GBMD_E_INVALID, "the slab recipe is 2D");
+            if ((sys.periodic & 3u) != 3u) return fail(GBMD_E_UNSUPPORTED, "the slab recipe is for periodic boxes");
             double lx = b0, ly = b1, frac = spec.slab_frac;
             int64_t x0 = host_to_fixed(lx * (1.0 - frac) * 0.5), x1 = host_to_fixed(lx * (1.0 + frac) * 0.5);
             double wl = host_to_f64(x1 - x0);

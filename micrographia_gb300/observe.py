@@ -12,6 +12,20 @@ from dataclasses import dataclass
 import numpy as np
 
 
+def _div(a, b):
+    """a / b with IEEE semantics (as Rust's f64 division): +-inf for b = 0, NaN for 0 / 0."""
+    if b != 0.0:
+        return a / b
+    if a == 0.0 or math.isnan(a):
+        return math.nan
+    return math.copysign(math.inf, a) * math.copysign(1.0, b)
+
+
+def _clamp01(x):
+    """f64::clamp(0.0, 1.0): NaN stays NaN."""
+    return x if math.isnan(x) else min(max(x, 0.0), 1.0)
+
+
 @dataclass
 class Reading:
     """observe.rs:38-44: counts of all particles and of the marked species per bin, and the
@@ -25,7 +39,8 @@ class Reading:
 def mixing(r):
     """observe.rs:134-155: 1 - D / D_max, clamped to [0, 1], where D = sum p ln(p / q) is the
     relative entropy of the marked particles' distribution p over the bins with respect to all
-    particles' q, and D_max = ln(all / marked). 0 when there is nothing to measure."""
+    particles' q, and D_max = ln(all / marked). 0 when there is nothing to measure; NaN when every
+    particle is marked (0 / 0, as in the reference's f64 arithmetic)."""
     total = sum(float(c) for c in r.marked)
     alln = sum(float(c) for c in r.all)
     if total == 0.0 or alln == 0.0:
@@ -37,13 +52,13 @@ def mixing(r):
             q = float(a) / alln
             d += p * math.log(p / q)
     d_max = math.log(alln / total)
-    return min(max(1.0 - d / d_max, 0.0), 1.0)
+    return _clamp01(1.0 - _div(d, d_max))
 
 
 def segregation(r):
     """observe.rs:157-181: the particle-weighted variance of the bins' marked fraction in excess
     of binomial noise, over its maximum f (1 - f), clamped to [0, 1]; 0 when either kind is
-    absent."""
+    absent; NaN when no bin holds two particles (the noise then equals the maximum: 0 / 0)."""
     n = m = 0.0
     for a, k in zip(r.all, r.marked):
         n += float(a)
@@ -61,4 +76,4 @@ def segregation(r):
     var /= n
     noise /= n
     mx = f * (1.0 - f)
-    return min(max((var - noise) / (mx - noise), 0.0), 1.0)
+    return _clamp01(_div(var - noise, mx - noise))

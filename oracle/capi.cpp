@@ -169,7 +169,7 @@ int oracle_init(const gbmd_system* csys, const gbmd_init* spec, int64_t* pos, in
         switch (spec->recipe) {
             case GBMD_INIT_FLUID: {
                 // init::fluid (init.rs:105-121): on an axis with walls the lattice keeps 1 sigma
-                // clear of them (the GPU initialiser runs periodic systems only)
+                // clear of them
                 st.dim = 2;
                 int64_t inner[2];
                 for (int a = 0; a < 2; a++) inner[a] = sys.periodic(a) ? sys.box[a] : sys.box[a] - to_fixed(2.0);

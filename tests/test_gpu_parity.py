@@ -63,6 +63,48 @@ def test_seeded_init_is_bit_identical(O, recipe, dim, n, args):
     assert got.velocity_sum() == [0] * dim
 
 
+@pytest.mark.parametrize("walls", [(0,), (1,), (0, 1)])
+def test_seeded_fluid_with_walls_is_bit_identical(O, walls):
+    """init::fluid (init.rs:105-121) in a box with walls: on each walled axis the lattice fills
+    the box less 2 sigma and sits 1 sigma clear of the walls; the triangular and slab recipes
+    refuse walled boxes."""
+    from micrographia_gb300 import Wall
+
+    n = 2500
+    sys_ = System(box_for(n, 0.5, 1.3), 0.005, Pair.lj(2.5), [1.0])
+    for a in walls:
+        sys_.with_walls(a, Wall.soft(), Wall.hard())
+    spec = make_init(_abi.INIT_FLUID, n, 1.0, 11, 0.1, 0.7, 0.05, 0.25)
+    want = O.init(sys_, spec)
+    got = init_state(sys_, _abi.INIT_FLUID, n, 1.0, 11, 0.1)
+    assert np.array_equal(got.pos, want.pos)
+    assert np.array_equal(got.vel, want.vel)
+    for a in walls:
+        assert got.pos[:, a].min() >= ONE and got.pos[:, a].max() < sys_.box_len[a] - ONE
+    for recipe in (_abi.INIT_TRIANGULAR, _abi.INIT_SLAB):
+        with pytest.raises(RuntimeError):
+            init_state(sys_, recipe, n, 1.0, 11)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_maxwell_for_given_species_is_bit_identical(O, dim):
+    """init::maxwell (init.rs:42-57) / three::maxwell for a species pattern with three masses and
+    (3D) a pinned species: equal to the oracle's draw, velocity sums exactly zero."""
+    from micrographia_gb300 import init
+
+    n = 3001
+    if dim == 2:
+        sys_ = System(box_for(n, 0.6, 1.0), 0.005, Pair.lj(2.5), [1.0, 2.0, 0.5])
+    else:
+        sys_ = System3(cube_for(n, 0.8), 0.005, Pair.lj(2.5), [1.0, 2.0, 0.5])
+        sys_.with_pinned(2)
+    sp = (np.arange(n) % 3).astype(np.uint32)
+    got = init.maxwell(sys_, sp, 0.9, 2026)
+    assert np.array_equal(got, O.maxwell(sys_, sp, 0.9, 2026))
+    moving = ~((sys_.pinned >> sp) & 1).astype(bool) if dim == 3 else np.ones(n, bool)
+    assert (got[moving].astype(np.int64).sum(axis=0) == 0).all()
+
+
 def test_libm_restatement_on_device_matches_over_many_draws(O):
     """Millions of Box–Muller draws (log, cos): the device velocities equal the oracle's."""
     n = 1 << 20
@@ -544,7 +586,8 @@ def test_observer_grid_matches_the_oracle(O, mode):
             assert r.kinetic == O.exact_kinetic(sys_, st)
             assert r.all.sum() == n and r.marked.sum() == (sp == 0).sum()
             want = Reading(wa, wm, 0.0)
-            assert mixing(r) == mixing(want) and segregation(r) == segregation(want)
+            for f in (mixing, segregation):
+                assert f(r) == f(want) or (math.isnan(f(r)) and math.isnan(f(want)))
     sys3 = System3(cube_for(500, 0.5), 0.005, Pair.wca(), [1.0])
     with GpuEngine3(sys3, O.fcc_maxwell(sys3, 500, 1.0, 1)) as g3:
         with pytest.raises(RuntimeError):

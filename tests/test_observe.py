@@ -28,6 +28,13 @@ def test_mixing_and_segregation_at_their_ends():
     assert mixing(_r([3, 4], [0, 0])) == 0.0
 
 
+def test_mixing_and_segregation_zero_over_zero():
+    """Where the reference divides 0 by 0 the result is NaN, as Rust's f64 gives (clamp keeps
+    NaN): segregation when no bin holds two particles, mixing when every particle is marked."""
+    assert math.isnan(segregation(_r([1, 1, 0, 1], [1, 0, 0, 0])))
+    assert math.isnan(mixing(_r([4, 6], [4, 6])))
+
+
 def test_mixing_and_segregation_in_between():
     """A partial case against the formulas written out: D = sum p ln(p/q), 1 - D/ln(N/M); the
     excess variance over binomial noise, over f(1 - f) minus the noise."""
