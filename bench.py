@@ -170,15 +170,17 @@ def system3():
     return System3(cube_for(N_ATOMS, RHO), DT, Pair.lj(RC), [1.0])
 
 
-def cpu_baseline(seconds_budget=20.0, threads=None):
-    """md-ref's CPU engine (C++ restatement, IntEngine3<f32> reference loop, OpenMP over all host
-    threads) on the same workload; a bounded sample of steps."""
+def cpu_baseline(seconds_budget=20.0, threads=None, half3=True):
+    """md-ref's CPU engine (C++ restatement of IntEngine3<f32>, OpenMP over all host threads) on the
+    same workload; a bounded sample of steps. `half3`: its pair loop over half shells (each pair
+    once, each side's kick rounded as the reference loop rounds it; the same kicks bit for bit,
+    tests/test_oracle.py), else the reference loop itself."""
     from oracle import oracle as O
 
     threads = threads or os.cpu_count() or 1
     sys3 = system3()
     s0 = O.fcc_maxwell(sys3, N_ATOMS, T0, SEED, jitter=0.05)
-    e = O.IntEngine(sys3, s0, threads=threads)
+    e = O.IntEngine(sys3, s0, threads=threads, half3=half3)
     e.step(5)  # warm-up: 5 steps, as the reference's own bench (crates/bench/src/main.rs:288)
     t0 = time.perf_counter()
     done = 0
@@ -187,7 +189,7 @@ def cpu_baseline(seconds_budget=20.0, threads=None):
         done += 1
     dt = time.perf_counter() - t0
     # one thread, as the reference's own bench times its CPU engine (bench/src/main.rs:279-298)
-    e1 = O.IntEngine(sys3, e.state, threads=1)
+    e1 = O.IntEngine(sys3, e.state, threads=1, half3=half3)
     t1 = time.perf_counter()
     e1.step(1)
     dt1 = time.perf_counter() - t1
@@ -196,7 +198,8 @@ def cpu_baseline(seconds_budget=20.0, threads=None):
         "unit": UNIT,
         "cores": threads,
         "kind": "port",
-        "sample": f"{done} full steps of the {N_ATOMS}-atom system after 5 warm-up steps ({dt:.1f} s), IntEngine3<f32> reference loop",
+        "sample": f"{done} full steps of the {N_ATOMS}-atom system after 5 warm-up steps ({dt:.1f} s), IntEngine3<f32> "
+        + ("over half shells (the reference loop's kicks bit for bit)" if half3 else "reference loop"),
         "single_thread": {"value": N_ATOMS / dt1, "unit": UNIT, "sample": f"1 full step on one thread ({dt1:.1f} s)"},
     }
 
@@ -204,7 +207,8 @@ def cpu_baseline(seconds_budget=20.0, threads=None):
 def run_reference(args, world, rank, pg):
     if rank != 0:
         return 0
-    base = cpu_baseline(seconds_budget=min(60.0, 5.0 + 2.0 * args.steps))
+    # the reference's own algorithm: IntEngine3's loop over all 27 cells (it has no half-shell form)
+    base = cpu_baseline(seconds_budget=min(60.0, 5.0 + 2.0 * args.steps), half3=False)
     line = {
         "metric": METRIC,
         "value": base["value"],

@@ -279,6 +279,12 @@ void* oracle_engine_create(const gbmd_system* csys, const int64_t* pos, const in
     }
 }
 void oracle_engine_destroy(void* h) { delete (Engine*)h; }
+// The half-shell 3D pair loop (IntEngine::half3): same kicks, about half the work.
+void oracle_engine_set_half3(void* h, int on) {
+    Engine* e = (Engine*)h;
+    if (e->f32) e->f32->half3 = on != 0;
+    else e->f64->half3 = on != 0;
+}
 void oracle_engine_step(void* h, uint64_t steps) {
     Engine* e = (Engine*)h;
     if (e->f32) e->f32->step(steps);

@@ -1292,6 +1292,88 @@ template <typename F> struct IntEngine {
         *pe_out = bond_part + (tables ? 0.5 * pe_i64 : 0.5 * (double)pe_i) + wall_pe;
     }
 
+    // A half shell for the 3D pair loop (the CPU baseline's form, off unless `half3` is set): each
+    // pair in reach is evaluated once, from the particle earlier in cell order (the same cell after
+    // it, and 13 of the 26 neighbouring cells), and each side's kick is rounded as the reference
+    // loop rounds it: i gets round(-fr c_i f), j round(-fr c_j (-f)), with f = sep(min_image(x_i,
+    // x_j)). j's own separation in the loop is exactly -f (min_image and sep are antisymmetric away
+    // from half the box and from 8 sigma, both beyond every cutoff when the box holds three cells a
+    // side), and r2 and fr are the same for both, so the kicks equal the loop's bit for bit in any
+    // order of the wrapping integer sums. The potential is summed in f64 over pairs (its rounding
+    // differs from the loop's per-particle f32 sums). Periodic pair systems, symmetric pair table.
+    bool half3 = false;
+    bool half3_ok(const std::array<uint32_t, 3>& nc) const {
+        if (sys.dim != 3 || tables || !partners.empty() || !sys.all_periodic() || piston_drive) return false;
+        for (int a = 0; a < 3; a++)
+            if (nc[a] < 3) return false;
+        const int ns = sys.species();
+        for (int a = 0; a < ns; a++)
+            for (int b = 0; b < ns; b++) {
+                const Pair &p = sys.pairs[a * ns + b], &q = sys.pairs[b * ns + a];
+                if (p.eps != q.eps || p.sigma != q.sigma || p.rc != q.rc) return false;
+            }
+        return true;
+    }
+    double forces_half3(std::vector<int32_t>& kicks, const std::array<uint32_t, 3>& dims) {
+        const int ns = sys.species();
+        CellList cl = build_cells(sys, state, dims);
+        const uint32_t nc[3] = {dims[0], dims[1], dims[2]};
+        uint32_t* ku = reinterpret_cast<uint32_t*>(kicks.data()); // wrapping sums (unsigned)
+        static const int fwd[13][3] = {{1, 0, 0},  {-1, 1, 0}, {0, 1, 0},  {1, 1, 0},  {-1, -1, 1}, {0, -1, 1}, {1, -1, 1},
+                                       {-1, 0, 1}, {0, 0, 1},  {1, 0, 1},  {-1, 1, 1}, {0, 1, 1},   {1, 1, 1}};
+        const long long ncell = (long long)nc[0] * nc[1] * nc[2];
+        double pe = 0.0;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads) reduction(+ : pe) if (threads > 1)
+        for (long long cc = 0; cc < ncell; cc++) {
+            const uint32_t cell = (uint32_t)cc;
+            const uint32_t cx = cell % nc[0], cy = (cell / nc[0]) % nc[1], cz = cell / (nc[0] * nc[1]);
+            uint32_t nb[14];
+            nb[0] = cell;
+            for (int k = 0; k < 13; k++) {
+                const uint32_t x = (cx + nc[0] + (uint32_t)(fwd[k][0] + 1) - 1) % nc[0];
+                const uint32_t y = (cy + nc[1] + (uint32_t)(fwd[k][1] + 1) - 1) % nc[1];
+                const uint32_t z = (cz + nc[2] + (uint32_t)(fwd[k][2] + 1) - 1) % nc[2];
+                nb[k + 1] = (z * nc[1] + y) * nc[0] + x;
+            }
+            for (uint32_t p = cl.start[cell]; p < cl.start[cell + 1]; p++) {
+                const size_t i = cl.items[p];
+                const int64_t* pi = &state.pos[3 * i];
+                const uint32_t si = state.species[i];
+                const F ci = kick_c[si];
+                int32_t k[3] = {0, 0, 0};
+                for (int c = 0; c < 14; c++) {
+                    const uint32_t q0 = c == 0 ? p + 1 : cl.start[nb[c]];
+                    for (uint32_t q = q0; q < cl.start[nb[c] + 1]; q++) {
+                        const size_t j = cl.items[q];
+                        const int64_t* pj = &state.pos[3 * j];
+                        F f[3];
+                        bool ok = true;
+                        for (int a = 0; a < 3; a++) ok = ok && Real<F>::sep(min_image(pi[a], pj[a], sys.box[a]), &f[a]);
+                        if (!ok) continue;
+                        const uint32_t sj = state.species[j];
+                        F fr, u;
+                        if (!consts[si * ns + sj].eval(f, 3, &fr, &u)) continue;
+                        const F ai = -fr * ci, aj = -fr * kick_c[sj];
+                        for (int a = 0; a < 3; a++) {
+                            k[a] = wadd(k[a], Real<F>::round_to_i32(ai * f[a]));
+                            const uint32_t kj = (uint32_t)Real<F>::round_to_i32(aj * (-f[a]));
+#pragma omp atomic
+                            ku[3 * j + a] += kj;
+                        }
+                        pe += (double)u;
+                    }
+                }
+                for (int a = 0; a < 3; a++) {
+                    const uint32_t ki = (uint32_t)k[a];
+#pragma omp atomic
+                    ku[3 * i + a] += ki;
+                }
+            }
+        }
+        piston_force = 0.0;
+        return pe;
+    }
+
     // IntEngine::forces (int_engine.rs:130-251) / IntEngine3::forces (int_engine3.rs:48-131):
     // the reference loop over the 3^d neighbouring cells of each particle, or the fast path.
     double forces(std::vector<int32_t>& kicks) {
@@ -1304,6 +1386,7 @@ template <typename F> struct IntEngine {
         // (with walls the reference loop: fast.rs gives the same kicks, fast_path.rs:20-54)
         bool use_fast = d == 2 && fast && !tables && partners.empty() && sys.all_periodic() && fast_eligible(sys, cl_dims);
         if (use_fast) return pair_kicks_fast<F>(sys, state, consts, kick_c, cl_dims, scratch, kicks.data());
+        if (half3 && half3_ok(cl_dims)) return forces_half3(kicks, cl_dims);
         CellList cl = build_cells(sys, state, cl_dims);
         uint32_t nc[3] = {cl_dims[0], cl_dims[1], d == 3 ? cl_dims[2] : 1u};
         double b[3] = {sys.box_f64(0), sys.box_f64(1), d == 3 ? sys.box_f64(2) : 1.0};

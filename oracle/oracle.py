@@ -56,6 +56,7 @@ _SIGS = [
     ("oracle_verlet_list_of", C.c_int64, [SYS, I64P, U32P, C.c_uint64, C.c_double, U32P, C.c_uint64, C.c_int, U32P, U32P, C.c_uint64]),
     ("oracle_engine_create", VP, [SYS, I64P, I32P, U32P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("oracle_engine_destroy", None, [VP]),
+    ("oracle_engine_set_half3", None, [VP, C.c_int]),
     ("oracle_engine_step", None, [VP, C.c_uint64]),
     ("oracle_engine_reverse", None, [VP]),
     ("oracle_engine_kicks", C.c_double, [VP, I32P]),
@@ -334,9 +335,10 @@ def set_species_velocity(sys, state, species, v):
 
 class IntEngine:
     """md_ref::IntEngine<F> (2D) / IntEngine3<F> (3D) on the CPU: F = f32 unless f64=True;
-    `fast` selects fast.rs's path in 2D; `integer` the all-integer tables (IntEngine::integer)."""
+    `fast` selects fast.rs's path in 2D; `integer` the all-integer tables (IntEngine::integer);
+    `half3` the half-shell 3D pair loop (the same kicks; the CPU baseline's form)."""
 
-    def __init__(self, sys, state, f64=False, fast=True, integer=False, threads=1):
+    def __init__(self, sys, state, f64=False, fast=True, integer=False, threads=1, half3=False):
         self.sys = sys
         self.n = state.n()
         self.D = sys.DIM
@@ -354,6 +356,8 @@ class IntEngine:
         )
         if not self._h:
             raise ValueError("oracle engine creation failed")
+        if half3:
+            lib().oracle_engine_set_half3(self._h, 1)
         if getattr(sys, "bonds", None):
             self.set_bonds([("fene" if t.fene else "harmonic", t.k, t.r0) for t in sys.bond_types], sys.bonds)
         if getattr(sys, "piston", None):

@@ -831,3 +831,32 @@ def test_fdlibm_and_the_platform_libm_on_bath_draws(O):
     print(f"ln {d_log / n:.2e}, cos {d_cos / n:.2e}, sin {d_sin / n:.2e} of draws rounded differently; {flips} velocity changes")
     assert flips == 0
     assert max(d_log, d_cos, d_sin) < n // 10  # (measured: ln 7%, cos and sin 3% of draws, last bit)
+
+
+def test_half_shell_3d_equals_the_reference_loop(O):
+    """The CPU baseline's half-shell 3D loop (each pair once, each side rounded on its own) gives
+    IntEngine3's kicks bit for bit, and the same 40-step trajectory: one species, and a mixture
+    with two masses, an unlike pair and a pair 0.3 sigma apart whose kicks saturate."""
+    from micrographia_gb300 import ONE, Pair, System3, cube_for
+
+    for masses in ([1.0], [1.0, 2.5]):
+        n = 2048
+        sys3 = System3(cube_for(n, 0.8442), 0.005, Pair.lj(2.5), masses)
+        if len(masses) == 2:
+            sys3.with_pair(0, 1, Pair(0.7, 1.05, 2.5))
+        s0 = O.fcc_maxwell(sys3, n, 0.72, 3, jitter=0.05)
+        if len(masses) == 2:
+            s0.species[::3] = 1
+            s0.pos[1] = s0.pos[0] + np.array([int(0.3 * ONE), 0, 0])
+        a = O.IntEngine(sys3, s0, threads=2)
+        b = O.IntEngine(sys3, s0, threads=2, half3=True)
+        ka, pa = a.kicks()
+        kb, pb = b.kicks()
+        assert np.array_equal(ka, kb)
+        assert abs(pa - pb) < 1e-6 * abs(pa)
+        if len(masses) == 2:
+            assert np.abs(ka[:2, 0].astype(np.int64)).min() > 2**30  # the saturated pair dominates
+        if len(masses) == 1:
+            a.step(40)
+            b.step(40)
+            assert a.state == b.state
