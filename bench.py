@@ -184,7 +184,7 @@ def cpu_baseline(seconds_budget=20.0, threads=None, half3=True):
     e.step(5)  # warm-up: 5 steps, as the reference's own bench (crates/bench/src/main.rs:288)
     t0 = time.perf_counter()
     done = 0
-    while done < 1 or (time.perf_counter() - t0 < seconds_budget and done < 20):
+    while done < 1 or (time.perf_counter() - t0 < seconds_budget and done < 64):
         e.step(1)
         done += 1
     dt = time.perf_counter() - t0

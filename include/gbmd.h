@@ -415,6 +415,9 @@ int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, int64_t* pos,
  * species (each drawn at kT = t with its own mass), with the exact zero velocity sum, into `vel`
  * (n * dim words), on the device. */
 int gbmd_maxwell(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel);
+/* init::fixed_speed (init.rs:61-74), 2D: every particle at speed sqrt(2 t / m) in a direction
+ * drawn on (seed, stream 3, id), with the exact zero velocity sum, on the device. */
+int gbmd_fixed_speed(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel);
 /* Create an engine whose state is generated on the device by `spec` (no host round trip). */
 int gbmd_create_seeded(const gbmd_system* sys, const gbmd_init* spec, const gbmd_options* opts,
                        gbmd_engine** out);

@@ -245,6 +245,7 @@ SIGNATURES = [
     ("gbmd_set_piston_speed", C.c_int, [VP, C.c_double]),
     ("gbmd_read_kinetic", C.c_int, [VP, P(C.c_double), P(C.c_uint32), P(C.c_double)]),
     ("gbmd_maxwell", C.c_int, [P(gbmd_system), P(C.c_uint32), C.c_uint32, C.c_double, C.c_uint64, P(C.c_int32)]),
+    ("gbmd_fixed_speed", C.c_int, [P(gbmd_system), P(C.c_uint32), C.c_uint32, C.c_double, C.c_uint64, P(C.c_int32)]),
     ("gbmd_observe_grid", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_uint32), P(C.c_uint32), P(C.c_double)]),
     ("gbmd_read_compartment_ledger", C.c_int, [VP, C.c_uint32, P(C.c_double), P(C.c_double), P(C.c_uint64), P(C.c_uint32)]),
     ("gbmd_add_bond", C.c_int, [VP, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_int32)]),

@@ -2808,7 +2808,8 @@ extern "C" int gbmd_init_state(const gbmd_system* sys, const gbmd_init* spec, in
     return rc;
 }
 
-extern "C" int gbmd_maxwell(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel) {
+static int velocities_on_device(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel,
+                                bool fixed_speed) {
     if (!sys || (n && (!species || !vel))) return fail(GBMD_E_INVALID, "null argument");
     GBMD_TRY(validate_system(*sys, n));
     for (uint32_t i = 0; i < n; i++)
@@ -2823,7 +2824,7 @@ extern "C" int gbmd_maxwell(const gbmd_system* sys, const uint32_t* species, uin
     if (cudaMallocAsync((void**)&dvel, n * D * 4, s) != cudaSuccess || cudaMallocAsync((void**)&dsp, (size_t)n * 4, s) != cudaSuccess)
         rc = fail(GBMD_E_NOMEM, "maxwell buffers");
     if (rc == GBMD_OK && cudaMemcpyAsync(dsp, species, (size_t)n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "copy");
-    if (rc == GBMD_OK) rc = maxwell_state_device(*sys, n, t, seed, dsp, dvel, s);
+    if (rc == GBMD_OK) rc = maxwell_state_device(*sys, n, t, seed, dsp, dvel, s, fixed_speed);
     if (rc == GBMD_OK && cudaMemcpyAsync(vel, dvel, n * D * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = fail(GBMD_E_CUDA, "copy");
     if (rc == GBMD_OK) {
         cudaError_t err = cudaStreamSynchronize(s);
@@ -2834,6 +2835,14 @@ extern "C" int gbmd_maxwell(const gbmd_system* sys, const uint32_t* species, uin
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     return rc;
+}
+
+extern "C" int gbmd_maxwell(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel) {
+    return velocities_on_device(sys, species, n, t, seed, vel, false);
+}
+extern "C" int gbmd_fixed_speed(const gbmd_system* sys, const uint32_t* species, uint32_t n, double t, uint64_t seed, int32_t* vel) {
+    if (sys && sys->dim != 2) return fail(GBMD_E_UNSUPPORTED, "fixed_speed is two-dimensional (init::fixed_speed)");
+    return velocities_on_device(sys, species, n, t, seed, vel, true);
 }
 
 // FNV-1a of an id-ordered state (State::hash, system.rs:460-477; State3::hash, three.rs:281-297).

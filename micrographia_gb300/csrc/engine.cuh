@@ -20,9 +20,10 @@ int init_state_device(const gbmd_system& sys, const gbmd_init& spec, void* pos_d
                       cudaStream_t s);
 
 // init::maxwell (init.rs:42-57) / three::maxwell for the given device species: Maxwell draws at
-// kT = t, then the exact zero velocity sum over the moving particles.
+// kT = t, then the exact zero velocity sum over the moving particles; with `fixed_speed`,
+// init::fixed_speed's draws (init.rs:61-74, 2D) instead of Maxwell's.
 int maxwell_state_device(const gbmd_system& sys, uint32_t n, double t, uint64_t seed, const uint32_t* species_dev, int32_t* vel_dev,
-                         cudaStream_t s);
+                         cudaStream_t s, bool fixed_speed = false);
 
 // Validate a system for this engine (periodic LJ subset); GBMD_OK or an error (message set).
 int validate_system(const gbmd_system& sys, uint32_t n);

@@ -30,7 +30,7 @@ __device__ double dev_normal(uint64_t seed, uint32_t stream, uint32_t i) {
     return __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, dev_log(u1))), dev_cos(__dmul_rn(6.28318530717958647692, u2)));
 }
 
-constexpr uint32_t STREAM_VELOCITY = 1, STREAM_JITTER = 2, STREAM_VAPOUR = 4;
+constexpr uint32_t STREAM_VELOCITY = 1, STREAM_JITTER = 2, STREAM_DIRECTION = 3, STREAM_VAPOUR = 4;
 
 // ---------------------------------------------------------------- position kernels
 struct Lattice2 {
@@ -127,6 +127,17 @@ __global__ void k_maxwell(MaxwellP M, const uint32_t* species, int32_t* vel) {
         }
         vel[M.dim * i + a] = v;
     }
+}
+
+// init::fixed_speed (init.rs:61-74), 2D: every particle at speed sqrt(2 t / m) in the direction
+// TAU u, u = uniform(seed, STREAM_DIRECTION, i), cos and sin as fdlibm's.
+__global__ void k_fixed_speed(MaxwellP M, const uint32_t* species, int32_t* vel) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.n) return;
+    const double speed = __dsqrt_rn(__ddiv_rn(__dmul_rn(2.0, M.t), M.masses[species[i]]));
+    const double th = __dmul_rn(6.28318530717958647692, uniform01(M.seed, STREAM_DIRECTION, i));
+    vel[2 * i] = sat_i32_f64(round(__dmul_rn(__dmul_rn(__dmul_rn(speed, dev_cos(th)), M.dt), 4294967296.0)));
+    vel[2 * i + 1] = sat_i32_f64(round(__dmul_rn(__dmul_rn(__dmul_rn(speed, dev_sin(th)), M.dt), 4294967296.0)));
 }
 
 __global__ void k_moving_flags(const uint32_t* species, uint32_t n, uint32_t pinned, int skip_pinned, uint32_t* flags) {
@@ -235,7 +246,7 @@ static int launch_lattice(const Lattice2& L, longlong2* pos, cudaStream_t s) {
 
 // Velocities: Maxwell draws, then the exact zero sum over moving particles in id order.
 static int maxwell_device(const gbmd_system& sys, uint32_t n, double t, uint64_t seed, const uint32_t* species, int32_t* vel,
-                          cudaStream_t s) {
+                          cudaStream_t s, bool fixed_speed = false) {
     if (n == 0) return GBMD_OK;
     MaxwellP M;
     M.n = n;
@@ -245,7 +256,8 @@ static int maxwell_device(const gbmd_system& sys, uint32_t n, double t, uint64_t
     for (int k = 0; k < GBMD_MAX_SPECIES; k++) M.masses[k] = k < (int)sys.nspecies ? sys.masses[k] : 1.0;
     M.pinned = sys.pinned;
     M.seed = seed;
-    k_maxwell<<<blocks(n, 128), 128, 0, s>>>(M, species, vel);
+    if (fixed_speed) k_fixed_speed<<<blocks(n, 128), 128, 0, s>>>(M, species, vel);
+    else k_maxwell<<<blocks(n, 128), 128, 0, s>>>(M, species, vel);
     note_launch();
     const uint32_t nb = std::min<uint32_t>(blocks(n, 256), 1024);
     uint32_t *flags = nullptr, *rank = nullptr, *tmp = nullptr;
@@ -276,8 +288,9 @@ static int maxwell_device(const gbmd_system& sys, uint32_t n, double t, uint64_t
 }
 
 int maxwell_state_device(const gbmd_system& sys, uint32_t n, double t, uint64_t seed, const uint32_t* species_dev, int32_t* vel_dev,
-                         cudaStream_t s) {
-    return maxwell_device(sys, n, t, seed, species_dev, vel_dev, s);
+                         cudaStream_t s, bool fixed_speed) {
+    if (fixed_speed && sys.dim != 2) return fail(GBMD_E_UNSUPPORTED, "fixed_speed is two-dimensional (init::fixed_speed)");
+    return maxwell_device(sys, n, t, seed, species_dev, vel_dev, s, fixed_speed);
 }
 
 int init_state_device(const gbmd_system& sys, const gbmd_init& spec, void* pos_dev, int32_t* vel_dev, uint32_t* species_dev, cudaStream_t s) {

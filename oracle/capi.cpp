@@ -446,6 +446,25 @@ void oracle_profile(const gbmd_system* csys, const int64_t* pos, uint64_t n, uin
     auto h = density_profile(sys, make_state_pos(sys.dim, pos, nullptr, n), bins, (int)axis);
     std::memcpy(out, h.data(), bins * 8);
 }
+void oracle_fixed_speed(const gbmd_system* csys, const uint32_t* species, uint64_t n, double t, uint64_t seed, int32_t* vel) {
+    System sys = System::from_c(*csys);
+    auto v = fixed_speed(sys, std::vector<uint32_t>(species, species + n), t, seed);
+    std::memcpy(vel, v.data(), v.size() * 4);
+}
+void oracle_barometric(const gbmd_system* csys, const uint32_t* species, uint64_t n, double t, double min_sep, double margin, uint64_t seed,
+                       int64_t* pos) {
+    System sys = System::from_c(*csys);
+    auto p = barometric_positions(sys, std::vector<uint32_t>(species, species + n), t, min_sep, margin, seed);
+    std::memcpy(pos, p.data(), p.size() * 8);
+}
+void oracle_mark_disc(const gbmd_system* csys, const int64_t* pos, uint32_t* species, uint64_t n, double cx, double cy, double radius,
+                      uint32_t mark) {
+    System sys = System::from_c(*csys);
+    State s = make_state_pos(sys.dim, pos, species, n);
+    const double c[2] = {cx, cy};
+    mark_disc(sys, s, c, radius, mark);
+    std::memcpy(species, s.species.data(), n * 4);
+}
 void oracle_observer_grid(const gbmd_system* csys, const int64_t* pos, const uint32_t* species, uint64_t n, uint32_t gx, uint32_t gy,
                           uint32_t marked, uint32_t* out) {
     System sys = System::from_c(*csys);

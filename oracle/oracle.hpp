@@ -407,6 +407,79 @@ inline std::vector<int32_t> maxwell(const System& sys, const std::vector<uint32_
     zero_velocity_sum(sys, species, vel, d == 3);
     return vel;
 }
+// init.rs:61-74 (2D): speed sqrt(2 t / m), direction TAU uniform(seed, 3, i), libm (fdlibm) cos
+// and sin; then the zero velocity sum over every particle.
+inline std::vector<int32_t> fixed_speed(const System& sys, const std::vector<uint32_t>& species, double t, uint64_t seed) {
+    const size_t n = species.size();
+    std::vector<int32_t> vel(2 * n, 0);
+    for (size_t i = 0; i < n; i++) {
+        const double speed = std::sqrt(2.0 * t / sys.masses[species[i]]);
+        const double th = 6.28318530717958647692 * uniform(seed, 3, (uint32_t)i);
+        vel[2 * i] = sys.to_step_displacement(speed * fdlibm::cos(th));
+        vel[2 * i + 1] = sys.to_step_displacement(speed * fdlibm::sin(th));
+    }
+    zero_velocity_sum(sys, species, vel, false);
+    return vel;
+}
+// init.rs:223-260 (2D): heights from the barometric law between margin and L_y - margin, x
+// uniform, draws (stream 2 for x, 3 for y, one counter across attempts) rejected within min_sep
+// of a placed particle (x periodic); positions only (the caller draws Maxwell velocities).
+inline std::vector<int64_t> barometric_positions(const System& sys, const std::vector<uint32_t>& species, double t, double min_sep,
+                                                 double margin, uint64_t seed) {
+    const double b[2] = {sys.box_f64(0), sys.box_f64(1)};
+    const double g = -sys.gravity[1];
+    const double h = b[1] - 2.0 * margin;
+    const double cell = std::max(min_sep, 0.5);
+    const size_t gx = (size_t)std::ceil(b[0] / cell), gy = (size_t)std::ceil(b[1] / cell);
+    std::vector<std::vector<size_t>> grid(gx * gy);
+    std::vector<std::array<double, 2>> pos;
+    uint32_t draw = 0;
+    for (uint32_t s : species) {
+        const double lam = sys.masses[s] * g / t;
+        for (;;) {
+            const double ux = uniform(seed, 2, draw), uy = uniform(seed, 3, draw);
+            draw++;
+            const double x = ux * b[0];
+            const double y = margin + (lam > 1e-12 ? -std::log(1.0 - uy * (1.0 - std::exp(-lam * h))) / lam : uy * h);
+            const size_t cx = std::min((size_t)(x / cell), gx - 1), cy = std::min((size_t)(y / cell), gy - 1);
+            bool clash = false;
+            for (size_t yy = cy > 0 ? cy - 1 : 0; yy < std::min(cy + 2, gy) && !clash; yy++)
+                for (size_t ox = 0; ox < 3 && !clash; ox++) {
+                    const size_t xx = (cx + gx + ox - 1) % gx;
+                    for (size_t j : grid[yy * gx + xx]) {
+                        double dx = std::fabs(pos[j][0] - x);
+                        dx = std::min(dx, b[0] - dx);
+                        const double dy = pos[j][1] - y;
+                        if (dx * dx + dy * dy < min_sep * min_sep) {
+                            clash = true;
+                            break;
+                        }
+                    }
+                }
+            if (!clash) {
+                grid[cy * gx + cx].push_back(pos.size());
+                pos.push_back({x, y});
+                break;
+            }
+        }
+    }
+    std::vector<int64_t> out(2 * pos.size());
+    for (size_t i = 0; i < pos.size(); i++) {
+        out[2 * i] = to_fixed(pos[i][0]);
+        out[2 * i + 1] = to_fixed(pos[i][1]);
+    }
+    return out;
+}
+// init.rs:152-163: species of the particles within radius of center (min image, f64).
+inline void mark_disc(const System& sys, State& s, const double* center, double radius, uint32_t species) {
+    const int64_t c[2] = {to_fixed(center[0]), to_fixed(center[1])};
+    const double r2 = radius * radius;
+    for (size_t i = 0; i < s.n(); i++) {
+        const double dx = to_f64(min_image(c[0], s.pos[2 * i], sys.box[0]));
+        const double dy = to_f64(min_image(c[1], s.pos[2 * i + 1], sys.box[1]));
+        if (dx * dx + dy * dy < r2) s.species[i] = species;
+    }
+}
 // init.rs:105-121: on an axis with walls the lattice keeps 1 sigma clear of them.
 inline State fluid(const System& sys, size_t n, double t, uint64_t seed) {
     State s;

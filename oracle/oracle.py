@@ -84,6 +84,9 @@ _SIGS = [
     ("oracle_pair_sums", None, [SYS, I64P, U32P, C.c_uint64, DP, DP]),
     ("oracle_rdf", None, [SYS, I64P, C.c_uint64, C.c_uint32, C.c_double, U64P]),
     ("oracle_profile", None, [SYS, I64P, C.c_uint64, C.c_uint32, C.c_uint32, U64P]),
+    ("oracle_fixed_speed", None, [SYS, U32P, C.c_uint64, C.c_double, C.c_uint64, I32P]),
+    ("oracle_barometric", None, [SYS, U32P, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64, I64P]),
+    ("oracle_mark_disc", None, [SYS, I64P, U32P, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint32]),
     ("oracle_observer_grid", None, [SYS, I64P, U32P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, U32P]),
     ("oracle_int_kick", C.c_int, [SYS, C.c_uint32, C.c_uint32, I64P, I32P]),
 ]
@@ -256,6 +259,32 @@ def profile(sys, state, bins, axis):
     c = sys.to_c()
     lib().oracle_profile(C.byref(c), _p(state.pos, C.c_int64), state.n(), bins, axis, _p(out, C.c_uint64))
     return out
+
+
+def fixed_speed(sys, species, t, seed):
+    """init::fixed_speed (init.rs:61-74)."""
+    species = np.ascontiguousarray(species, np.uint32)
+    vel = np.empty((len(species), 2), np.int32)
+    c = sys.to_c()
+    lib().oracle_fixed_speed(C.byref(c), _p(species, C.c_uint32), len(species), t, seed, _p(vel, C.c_int32))
+    return vel
+
+
+def barometric_positions(sys, species, t, min_sep, margin, seed):
+    """init::barometric's positions (init.rs:223-260)."""
+    species = np.ascontiguousarray(species, np.uint32)
+    pos = np.empty((len(species), 2), np.int64)
+    c = sys.to_c()
+    lib().oracle_barometric(C.byref(c), _p(species, C.c_uint32), len(species), t, min_sep, margin, seed, _p(pos, C.c_int64))
+    return pos
+
+
+def mark_disc(sys, state, center, radius, species):
+    """init::mark_disc (init.rs:152-163): the marked species array."""
+    sp = state.species.copy()
+    c = sys.to_c()
+    lib().oracle_mark_disc(C.byref(c), _p(state.pos, C.c_int64), _p(sp, C.c_uint32), state.n(), center[0], center[1], radius, species)
+    return sp
 
 
 def observer_grid(sys, state, grid, marked):
