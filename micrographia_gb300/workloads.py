@@ -108,7 +108,10 @@ def _profile_run(name):
       velocity rescale to T = 0.45 every 10 steps, 20 steps, then the thermostat's kernels four
       times by direct launches (k_ke_exact, k_thermo_factor, k_rescale, k_zero_apply);
     - half3d: the 3D liquid of configs[1] on the opt-in half-shell lists, 20 steps in graphs,
-      then 20 by direct launches (k_build_half, k_force_half, k_leap_half)."""
+      then 20 by direct launches (k_build_half, k_force_half, k_leap_half);
+    - slab2d: the liquid-vapour slab of configs[2] at a quarter of its size (N = 2^22), skin 0.4,
+      100 steps in graphs, then 30 by direct launches (k_force_list<2>, k_build_list<2> and the
+      binning)."""
     from .engine import BatchEngine, ForceMode, GpuEngine3, init_state
 
     if name == "frames3d":
@@ -165,6 +168,14 @@ def _profile_run(name):
             e.step(20)
             ms = e.time_thermostat(4)
             print(f"thermo2d: N {spec.n}, thermostat {ms:.3f} ms")
+    elif name == "slab2d":
+        from .engine import GpuEngine
+
+        sys2, spec = config3(1 << 22)
+        with GpuEngine(sys2, None, ForceMode.verlet_with_skin(sys2, spec.n, 0.4), init=spec, rescale_every=10, rescale_t=0.45) as e:
+            e.step(100)
+            f, r, nr = e.time_phases(30)
+            print(f"slab2d: N {spec.n}, force {f:.3f} ms, rebuild {r:.3f} ms ({nr} in 30 steps)")
     elif name == "half3d":
         sys3, spec = config2()
         with GpuEngine3(sys3, None, ForceMode.verlet_with_skin(sys3, spec.n, 0.3), init=spec, flags=_abi.FLAG_HALF_LISTS) as e:
@@ -172,7 +183,7 @@ def _profile_run(name):
             f, r, nr = e.time_phases(20)
             print(f"half3d: force {f:.3f} ms, rebuild {r:.3f} ms ({nr} in 20 steps)")
     else:
-        raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d, batch, scenario2d, thermo2d or half3d")
+        raise SystemExit(f"unknown workload {name!r}: frames3d, loop3d, batch, scenario2d, thermo2d, half3d or slab2d")
 
 
 if __name__ == "__main__":
