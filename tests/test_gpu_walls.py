@@ -372,3 +372,38 @@ def test_piston_page_commands(O):
         c.step(600)
         assert g.read_state() == c.state
         assert g.piston() == c.piston()[:3]
+
+
+def _liquid3(n, density, t, walls):
+    """crates/md/tests/three.rs:15-31: an FCC liquid (jitter 0.05, seed 7) with Maxwell velocities
+    (seed 3); with hard walls on z, the sites kept half a sigma clear of them."""
+    from micrographia_gb300 import DT, ONE, State3, System3, init
+
+    sys3 = System3(cube_for(n, density), DT, Pair.lj(2.5), [1.0])
+    if walls:
+        sys3.with_walls(2, Wall.hard(), Wall.hard())
+    pos = init.fcc_maxwell(sys3, n, t, 7, jitter=0.05).pos
+    if walls:
+        pos[:, 2] = np.clip(pos[:, 2], ONE // 2, sys3.box_len[2] - ONE // 2)
+    sp = np.zeros(n, np.uint32)
+    return sys3, State3(pos, init.maxwell(sys3, sp, t, 3), sp)
+
+
+def test_bath_and_hot_walls_set_the_temperature_3d():
+    """three.rs:113-133: a 3D Andersen bath at 1.6 brings a liquid (4000 at density 0.5, T 0.8) to
+    kT 1.6 within 0.06 in 4000 steps; heat-bath walls at 2.0 on z bring a thin gas (2000 at 0.05)
+    to kT 2.0 within 0.1 in 60000 steps, the walls' ledger showing the energy they gave."""
+    sys3, s = _liquid3(4000, 0.5, 0.8, False)
+    sys3.with_thermostat(1.6, 2.0)
+    with GpuEngine3(sys3, s) as g:
+        g.step(4000)
+        t = g.read_kinetic_total() / (1.5 * 4000)
+    assert abs(t - 1.6) < 0.06, t
+    sys3, s = _liquid3(2000, 0.05, 0.5, True)
+    sys3.with_walls(2, Wall.thermal(2.0), Wall.thermal(2.0))
+    with GpuEngine3(sys3, s) as g:
+        g.step(60000)
+        t = g.read_kinetic_total() / (1.5 * 2000)
+        e, _, h = g.read_ledger()
+    assert abs(t - 2.0) < 0.1, t
+    assert h[4] + h[5] > 0 and e[4] + e[5] > 0
