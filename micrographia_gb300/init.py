@@ -95,9 +95,10 @@ def half_step_kinetic(sys, state):
 
 
 def _round_i32(x):
-    """f64::round (half away from zero) then `as i32` (saturating)."""
+    """f64::round (half away from zero) then `as i32` (saturating, NaN to 0)."""
     r = np.trunc(x)
     r = r + np.where(np.abs(x - r) >= 0.5, np.sign(x), 0.0)
+    r = np.where(np.isnan(r), 0.0, r)
     return np.clip(r, -2147483648.0, 2147483647.0).astype(np.int32)
 
 
@@ -110,7 +111,7 @@ def set_temperature(state, sys, t):
     else:
         dof = 1.5 * max(_moving(sys, state.species).size - 1.0, 1.0)
     now = half_step_kinetic(sys, state) / dof
-    if not now > 0.0:
+    if now <= 0.0:
         return state
     f = math.sqrt(t / now)
     state.vel = _round_i32(state.vel.astype(np.float64) * f)
