@@ -110,8 +110,8 @@ typedef struct gbmd_system {
     /* A semi-permeable membrane across a walled axis (md_core::Membrane, system.rs:119-141;
      * with_membrane / with_pores, system.rs:259-274), 2D: it reflects the species in
      * membrane_blocks about membrane_position - 1/2, except through pores membrane_pore_width wide
-     * every 2^membrane_pore_shift position units along it (shift 0: no pores). Carried for the
-     * oracle; the GPU engine refuses it (GBMD_E_UNSUPPORTED). */
+     * every 2^membrane_pore_shift position units along it (shift 0: no pores). A crossing is
+     * mirrored after the force step and booked in the ledger's faces 4 and 5. */
     uint32_t membrane;      /* 1: present */
     uint32_t membrane_axis;
     uint32_t membrane_blocks;
@@ -121,7 +121,8 @@ typedef struct gbmd_system {
     /* Compartments (System::with_compartments, system.rs:233-241), 2D: a walled axis split into
      * boxes of 2^(compartments[axis] - 32) sigma by hard walls (0: none); particles in different
      * boxes interact only when compartments_diathermal is 1 (CompartmentWalls, system.rs:143-153).
-     * Carried for the oracle; the GPU engine refuses them (GBMD_E_UNSUPPORTED). */
+     * A particle that crossed into another box is mirrored back home after the force step;
+     * insulating boxes are filtered from the lists and the cell-list pairs. */
     uint32_t compartments[2];
     uint32_t compartments_diathermal;
     uint32_t _compartments_pad;
