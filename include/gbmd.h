@@ -152,6 +152,11 @@ typedef struct gbmd_system {
  * its kick mirrored onto the other particle through shared-memory row windows. The trajectory is
  * the same as with full lists, bit for bit; on GB300 the full-list step is faster (the default). */
 #define GBMD_FLAG_HALF_LISTS 16384u /* bit 14 */
+/* 2D Verlet lists: each particle's path since the list build (the sum of |vx| + |vy| over its
+ * steps) rides in its quotient record, and while it stays below what could fire the displacement
+ * trigger the step skips the test (and the read of the reference position). The trigger fires at
+ * the same steps either way. This flag turns the bound off: comparisons. */
+#define GBMD_FLAG_NO_PATH_BOUND 32768u /* bit 15 */
 
 typedef struct gbmd_options {
     int32_t mode;          /* GBMD_MODE_* */

@@ -112,6 +112,7 @@ FLAG_WHOLE_CELLS = 1  # list builds scan whole neighbour cells (no slab sub-buck
 FLAG_NO_STEP_LOOP = 2  # small systems step through per-step graph nodes, not the persistent loop
 FLAG_TUNE_SKIN = 4  # batches: time each skin of 0.3..0.7 sigma on the given state, keep the fastest
 FLAG_HALF_LISTS = 1 << 14  # half-shell lists (3D, one species): each pair evaluated once; full lists by default
+FLAG_NO_PATH_BOUND = 1 << 15  # 2D: always run the displacement test (no path bound): comparisons
 
 
 def build_lanes_flag(lanes):

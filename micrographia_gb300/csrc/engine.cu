@@ -254,6 +254,13 @@ void fill_params(Params& P, const gbmd_system& s, uint32_t n, double skin, uint3
     P.one = 1;
     double hs = 0.5 * skin * (1.0 - 1e-3);
     P.half_skin2s = scale2((float)(hs * hs), 56);
+    // The trigger's f32 value for a displacement d is at most (|d| / 16)^2 (1 + 2^-21) (three
+    // roundings of 2^-24), and |d| is at most the path U: U below 16 sqrt(half_skin2s) (1 - 2^-20)
+    // cannot fire it.
+    {
+        const double u = 16.0 * std::sqrt((double)P.half_skin2s) * (1.0 - 0x1p-20);
+        P.ub_thr = (s.dim == 2 && skin > 0.0 && u >= 1.0) ? (uint32_t)std::min(std::floor(u), 4294967294.0) : 0u;
+    }
     P.dt = s.dt;
     for (uint32_t a = 0; a < s.nspecies; a++)
         for (uint32_t b = 0; b < s.nspecies; b++) {
@@ -1249,6 +1256,7 @@ int create_common(gbmd_engine* e, const gbmd_system* sys, uint32_t n, const gbmd
         cap = e->opt.cap ? e->opt.cap : (uint32_t)std::ceil(sphere * std::max(2.0 * density, 1.2)) + 8;
     }
     fill_params(e->P, *sys, n, e->skin, cap, nc);
+    if (e->opt.flags & GBMD_FLAG_NO_PATH_BOUND) e->P.ub_thr = 0;
     if (e->verlet && e->D == 3 && !e->multi && e->opt.arith == GBMD_ARITH_F32 && !e->P.walls && (e->opt.flags & GBMD_FLAG_HALF_LISTS)) {
         // Half-shell lists address a neighbour by its offset in its row of cells (16 bits): rows
         // must stay far below 65,536 particles (the build reports an overflow otherwise). The
@@ -1879,6 +1887,7 @@ int gbmd_update_system(gbmd_engine* e, const gbmd_system* sys) {
     Params old = e->P;
     e->sys = *sys;
     fill_params(e->P, e->sys, e->n, e->skin, old.cap, old.nc);
+    if (e->opt.flags & GBMD_FLAG_NO_PATH_BOUND) e->P.ub_thr = 0;
     // the geometry and list sizing of creation, the integer tables, the slabs
     e->P.key_shift = old.key_shift;
     e->P.sub_scale = old.sub_scale;

@@ -669,7 +669,11 @@ __global__ void __launch_bounds__(128) k_build_list(Params P, const PosRec<D>* _
     nbr_count[i] = count;
     pos_o[i] = pos_s[i];
     ref_pos[i] = pos_s[i];
-    if (qpos_o) qpos_o[i] = quot_record<D>(xi, si);
+    if (qpos_o) {
+        uint4 q = quot_record<D>(xi, si);
+        if (D == 2) q.z = 1u; // the path since this build: 0 (the unused z word, as U + 1)
+        qpos_o[i] = q;
+    }
 #pragma unroll
     for (int a = 0; a < D; a++) vel_o[D * i + a] = vel_s[D * i + a];
     species_o[i] = species_s[i];
@@ -712,6 +716,7 @@ __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t n, uint
     int32_t k[3] = {0, 0, 0};
     const uint32_t m = valid ? __ldg(nbr_count + i) : 0u, cap4 = (P.cap + 3u) & ~3u;
     const PairC pc0 = P.pc[0];
+    uint32_t path = 0; // 2D: the quotient record's z word, the path since the list build + 1 (0: unknown)
     const uint4* groups = reinterpret_cast<const uint4*>(nbr + list_slot(iv, 0, cap4)); // group g at groups[32 g]
     // Every listed neighbour is within 8 sigma of xi at its recorded image (list radius + skin),
     // so neither a minimum image nor a range check is needed.
@@ -730,6 +735,7 @@ __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t n, uint
         // its quotient record shifted by that image exactly (quot_shift). 2D and 3D alike.
         const uint4 qi = ld_in<CG>(qpos_in + iv);
         const uint32_t Xi[3] = {qi.x, qi.y, qi.z};
+        if (D == 2) path = qi.z;
         for (uint32_t g = seg; g < ngroups; g += S) {
             // (the prefetch index clamped to the last group rather than guarded: no branch)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(groups + 32 * min(g + 2 * S, ngroups - 1u)));
@@ -817,7 +823,22 @@ __device__ __forceinline__ bool force_list_one(const Params& P, uint32_t n, uint
 #pragma unroll
     for (int a = 0; a < D; a++) vel[D * i + a] = v[a];
     store_pos<D>(pos_out, i, xi, si);
-    qpos_out[i] = quot_record<D>(xi, si);
+    uint4 qo = quot_record<D>(xi, si);
+    if constexpr (D == 2 && !EXT) {
+        // Positions move by exactly v each step between list builds (no wrap), so |x - ref| is at
+        // most the path U = sum of |vx| + |vy|. While U stays below ub_thr the trigger cannot fire
+        // and the reference record need not be read. Any other writer of the record leaves z = 0,
+        // and the test then runs until the next build.
+        if (path != 0u && P.ub_thr != 0u) {
+            const uint64_t U = (uint64_t)(path - 1u) + (uint64_t)uabs32(v[0]) + (uint64_t)uabs32(v[1]);
+            if (U < P.ub_thr) {
+                qo.z = (uint32_t)U + 1u;
+                qpos_out[i] = qo;
+                return false;
+            }
+        }
+    }
+    qpos_out[i] = qo;
     int64_t xr[3];
     load_particle<D, false>(ref_pos, nullptr, i, xr);
     return moved_half_skin<D>(P, xr, xi);

@@ -431,6 +431,37 @@ def test_a_few_particles_follow_the_oracle(O, dim, n):
             assert g.read_state() == s0
 
 
+@pytest.mark.parametrize("loop", [False, True])
+def test_path_bound_fires_the_trigger_at_the_same_steps(O, loop):
+    """2D Verlet lists with the path bound (the displacement test skipped while a particle's path
+    since the list build cannot reach half the skin) against the same engine testing every
+    particle every step: the same rebuild count after every chunk of steps and the same states,
+    through a kick to a region, a flipped bit and a reversal. `loop`: the persistent step loop,
+    else per-step graph nodes."""
+    n = 20000
+    sys_ = System(box_for(n, 0.7, 1.0), 0.005, Pair.lj(2.5), [1.0])
+    s0 = O.fluid(sys_, n, 1.0, 12)
+    m = ForceMode.verlet_with_skin(sys_, n, 0.3)
+    L = sys_.box_f64()
+    f = 0 if loop else _abi.FLAG_NO_STEP_LOOP
+    with GpuEngine(sys_, s0, m, flags=f) as a, GpuEngine(sys_, s0, m, flags=f | _abi.FLAG_NO_PATH_BOUND) as b:
+        for k in range(60):
+            a.step(7)
+            b.step(7)
+            assert a.read_list_stats() == b.read_list_stats(), k
+            if k == 20:
+                for e in (a, b):
+                    e.kick_region([0.0, 0.0], [0.3 * L[0], L[1]], 0.0, [2.0, 0.0])
+            if k == 35:
+                for e in (a, b):
+                    e.flip_bit(5, 0, 30)
+            if k == 45:
+                for e in (a, b):
+                    e.reverse()
+        assert a.read_state() == b.read_state()
+        assert a.read_list_stats()[0] > 20
+
+
 def test_run_to_run_identical(O):
     sys_, s = fluid(O, 5000, 0.6, Pair.wca(), 2)
     hs = []
