@@ -197,7 +197,9 @@ __global__ void __launch_bounds__(128) k_bbuild_list(uint32_t N, uint32_t cap, c
     nbr_count[i] = count;
     pos_o[i] = pos_s[i];
     ref_pos[i] = pos_s[i];
-    qpos_o[i] = quot_record<D>(xi, si);
+    uint4 q = quot_record<D>(xi, si);
+    if (D == 2) q.z = 1u; // the path since this build: 0 (force_list_one's path bound)
+    qpos_o[i] = q;
     for (int a = 0; a < D; a++) vel_o[D * i + a] = vel_s[D * i + a];
     species_o[i] = species_s[i];
     ids_o[i] = ids_s[i];
