@@ -217,3 +217,20 @@ def test_static_binning_rejects_bad_grids_before_any_device_work(engine_lib):
     grid = (C.c_uint32 * 3)(10, 10, 1)
     assert engine_lib.gbmd_bin_cells_static(C.byref(c2), fake, 1000, grid, fake, fake, fake, None) == _abi.E_INVALID
     assert b"box" in engine_lib.gbmd_last_error()
+
+
+def test_new_entry_points_reject_bad_arguments_on_the_host(engine_lib):
+    """The Observer, kinetic-energy and velocity entry points check their arguments before any
+    device work: a null engine or system, and species out of range or fixed_speed in 3D."""
+    lib = _abi.lib()
+    assert lib.gbmd_observe_grid(None, 4, 4, 0, None, None, None) == _abi.E_INVALID
+    assert lib.gbmd_read_kinetic(None, None, None, None) == _abi.E_INVALID
+    assert lib.gbmd_maxwell(None, None, 0, 1.0, 1, None) == _abi.E_INVALID
+    from micrographia_gb300 import Pair, System, System3, box_for, cube_for
+
+    sys2 = System(box_for(100, 0.5, 1.0), 0.005, Pair.lj(2.5), [1.0]).to_c()
+    sp = (C.c_uint32 * 2)(0, 3)  # species 3 of a one-species system
+    vel = (C.c_int32 * 4)()
+    assert lib.gbmd_maxwell(C.byref(sys2), sp, 2, 1.0, 1, vel) == _abi.E_INVALID
+    sys3 = System3(cube_for(100, 0.5), 0.005, Pair.lj(2.5), [1.0]).to_c()
+    assert lib.gbmd_fixed_speed(C.byref(sys3), (C.c_uint32 * 1)(0), 1, 1.0, 1, (C.c_int32 * 3)()) == _abi.E_UNSUPPORTED
